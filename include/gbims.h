@@ -1,0 +1,217 @@
+/*
+ * gbims.h -- C ABI of the GB300-native Iterative Model Solution (IMS) hot path
+ * for MODFLOW 6.
+ *
+ * The library replaces, behind the same calling contract, the IMS linear
+ * accelerator of MODFLOW 6 (src/Solution/LinearMethods/ImsLinear.f90) and the
+ * NPF conductance fill (src/Model/GroundWaterFlow/gwf-npf.f90).  All entry
+ * points take plain pointers and sizes, never abort, and return an int status:
+ *   0  success
+ *  >0  warning (e.g. GBIMS_WARN_PIVOT: the ILU0 pivot guard added a diagonal
+ *      increment, ImsLinearBase.f90:812-863)
+ *  <0  error (see gbims_status_string)
+ *
+ * Index arrays (ia, ja, node lists) are 0-based unless index_base is 1 in the
+ * settings (Fortran callers pass 1).  The diagonal entry must be the first
+ * entry of each CSR row, as in MODFLOW 6 (src/Utilities/Matrix/SparseMatrix.f90:16).
+ */
+#ifndef GBIMS_H
+#define GBIMS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBIMS_OK 0
+#define GBIMS_WARN_PIVOT 1
+#define GBIMS_ERR_ARG (-1)
+#define GBIMS_ERR_CUDA (-2)
+#define GBIMS_ERR_UNSUPPORTED (-3)
+#define GBIMS_ERR_NONFINITE (-4)
+#define GBIMS_ERR_NOMEM (-5)
+#define GBIMS_ERR_STATE (-6)
+
+/* precision modes */
+#define GBIMS_FP64 0  /* FP64 everywhere: the plain drop-in */
+#define GBIMS_MIXED 1 /* FP32 matrix, factors and inner vectors; FP64 true
+                         residual, Krylov scalars, head update and closure */
+
+/* IMS LINEAR block options, with the meaning of
+ * src/Solution/LinearMethods/ImsLinearSettings.f90:10-253 and
+ * ImsLinear.f90:178-185 (IPC derived from relax/level/droptol). */
+typedef struct gbims_settings {
+  double dvclose;   /* INNER_DVCLOSE */
+  double rclose;    /* INNER_RCLOSE */
+  int icnvgopt;     /* RCLOSE option 0..4 (ImsLinearBase.f90:1101-1146) */
+  int iter1;        /* INNER_MAXIMUM */
+  int ilinmeth;     /* LINEAR_ACCELERATION: 1 CG, 2 BICGSTAB */
+  int iscl;         /* SCALING_METHOD: 0 none, 1 diagonal, 2 L2 norm */
+  int iord;         /* REORDERING_METHOD: 0 none (others: GBIMS_ERR_UNSUPPORTED) */
+  int north;        /* NUMBER_ORTHOGONALIZATIONS */
+  double relax;     /* RELAXATION_FACTOR (> 0 selects MILU0) */
+  int level;        /* PRECONDITIONER_LEVELS (> 0: ILUT, unsupported) */
+  double droptol;   /* PRECONDITIONER_DROP_TOLERANCE (> 0: ILUT, unsupported) */
+  int precision;    /* GBIMS_FP64 or GBIMS_MIXED */
+  int index_base;   /* 0 (C) or 1 (Fortran) for ia/ja */
+  int nlay, nrow, ncol; /* optional DIS shape; enables the structured
+                           (7-point) triangular-sweep kernels when the CSR
+                           pattern matches a full DIS grid.  0 = none. */
+} gbims_settings;
+
+/* Convergence summary of the last apply (ConvergenceSummary.f90 fields for a
+ * solution with one model). */
+typedef struct gbims_summary {
+  int iter_cnt;        /* inner iterations of the last apply */
+  int icnvg;           /* 1 converged, 0 not */
+  int pivot_retries;   /* ims_base_pcu retries (0 = none) */
+  int exit_reason;     /* 0 none, 1 closure, 2 stagnation, 3 itmax, 4 exact, 5 zero rho */
+  double dvmax;        /* signed max head change of the last inner iteration */
+  int locdv;           /* its 0-based row */
+  double rmax;         /* signed max residual of the last inner iteration */
+  int locr;            /* its 0-based row */
+  double l2norm0;      /* initial residual L2 norm */
+  double l2norm;       /* last residual L2 norm */
+  double solve_ms;     /* device time of the apply (CUDA events) */
+  int refinements;     /* mixed precision: FP64 refinement steps */
+  int structured;      /* 1 if the structured 7-point sweeps were used */
+} gbims_summary;
+
+typedef struct gbims_handle gbims_handle;
+
+/* Replaces ImsLinearDataType%imslinear_allocate (ImsLinear.f90:111-339):
+ * validates options, derives IPC, builds IAPC/JAPC (ims_base_pccrs,
+ * ImsLinearBase.f90:1207-1261), the ILU0 level schedule and the device
+ * layouts.  neq/nja are the solution's NEQ and NJA. */
+int gbims_create(const gbims_settings *settings, int neq, int nja, const int *ia,
+                 const int *ja, gbims_handle **out);
+
+/* Replaces ImsLinearDataType%imslinear_apply (ImsLinear.f90:617-750) with host
+ * arrays: amat (nja), rhs (neq) and x (neq) are read, x is overwritten with
+ * the solution (x on entry is the initial guess).  amat and rhs are left as
+ * passed (the reference restores them after scaling).  icnvg and in_iter have
+ * the meaning of ICNVG and IN_ITER.  summary may be NULL. */
+int gbims_apply(gbims_handle *h, double *amat, double *rhs, double *x, int kstp,
+                int kiter, int *icnvg, int *in_iter, gbims_summary *summary);
+
+/* Same as gbims_apply with device pointers (the device-resident assembly
+ * path); amat, rhs and x live in HBM and stay there. */
+int gbims_apply_device(gbims_handle *h, double *d_amat, double *d_rhs, double *d_x,
+                       int kstp, int kiter, int *icnvg, int *in_iter,
+                       gbims_summary *summary);
+
+/* Replaces ImsLinearDataType%imslinear_da. */
+int gbims_destroy(gbims_handle *h);
+
+/* Building blocks of apply, exposed for callers that drive their own loop
+ * and for kernel-level checks (host arrays):
+ *  gbims_factor       preconditioner update, ims_base_pcu + ims_base_pcilu0
+ *                     (ImsLinearBase.f90:761-864, 928-1042), from amat (nja);
+ *  gbims_get_apc      copies APC (nja, the reference's layout: APC(1:NEQ) the
+ *                     inverse pivots, then the L\U entries in JAPC order);
+ *  gbims_matvec       y = A*x, amux (sparsekit.f90:1-59), with the matrix of
+ *                     the last gbims_factor or apply;
+ *  gbims_precondition z = M^-1 r, ims_base_ilu0a (ImsLinearBase.f90:1049-1092),
+ *                     with the last factor (FP32 factors in GBIMS_MIXED). */
+int gbims_factor(gbims_handle *h, const double *amat, int *pivot_retries);
+int gbims_get_apc(gbims_handle *h, double *apc);
+int gbims_matvec(gbims_handle *h, const double *x, double *y);
+int gbims_precondition(gbims_handle *h, const double *r, double *z);
+
+/* Message of the last error on this handle (never NULL). */
+const char *gbims_last_error(const gbims_handle *h);
+const char *gbims_status_string(int status);
+
+/* ---- GWF NPF conductance fill (gwf-npf.f90:474-698) ---------------------- */
+
+/* NPF options with the meaning of the NPF OPTIONS block. */
+typedef struct gbnpf_options {
+  int inewton;      /* NEWTON formulation */
+  int ivarcv;       /* VARIABLECV */
+  int idewatcv;     /* DEWATERED */
+  int icellavg;     /* ALTERNATIVE_CELL_AVERAGING: 0 harmonic, 1 log, 2 AMT-LMK, 3 AMT-HMK */
+  double satomega;  /* Newton saturation smoothing (default 1e-6) */
+  int index_base;   /* 0 or 1 for the index arrays */
+} gbnpf_options;
+
+typedef struct gbnpf_handle gbnpf_handle;
+
+/* Uploads the grid connectivity (Connections.f90:26-35: ia, ja, jas, isym,
+ * ihc, cl1, cl2, hwva), cell geometry and K, and computes the saturated
+ * conductance (calc_condsat, gwf-npf.f90:1950-2044) on the device. */
+int gbnpf_create(const gbnpf_options *opt, int nodes, int nja, int njas, const int *ia,
+                 const int *ja, const int *jas, const int *isym, const int *ihc,
+                 const double *cl1, const double *cl2, const double *hwva,
+                 const double *top, const double *bot, const double *k11,
+                 const double *k33, const int *icelltype, gbnpf_handle **out);
+
+/* npf_cf + npf_fc (+ npf_fn when inewton) on device arrays: adds the
+ * conductance terms to d_amat (nja) and d_rhs (nodes) in the reference's
+ * per-row summation order.  d_ibound (nodes, int) and d_hnew are device
+ * pointers. */
+int gbnpf_fill(gbnpf_handle *h, const int *d_ibound, const double *d_hnew,
+               double *d_amat, double *d_rhs);
+
+/* Copies the saturated conductance (njas) to the host. */
+int gbnpf_get_condsat(gbnpf_handle *h, double *condsat);
+
+int gbnpf_destroy(gbnpf_handle *h);
+
+/* ---- Device-resident single-model solution ------------------------------ */
+
+/* A GWF DIS model whose whole outer Picard/Newton loop (NumericalSolution
+ * solve, NumericalSolution.f90:1482-1837) runs with x, amat and rhs in HBM:
+ * NPF/STO/CHD/WEL/RCH fill, sln_ls fixups, IMS apply, dxmax, under-relaxation. */
+typedef struct gbsln_model {
+  int nlay, nrow, ncol;
+  const double *delr, *delc;  /* ncol, nrow */
+  const double *top;          /* nrow*ncol (model top) */
+  const double *botm;         /* nlay*nrow*ncol */
+  const double *k11, *k33;    /* nodes */
+  const int *icelltype;       /* nodes */
+  const double *ss, *sy;      /* nodes, or NULL for steady state only */
+  int nchd;
+  const int *chd_node;        /* 0-based node numbers */
+  const double *chd_head;
+  int nwel;
+  const int *wel_node;
+  const double *wel_q;
+  int nrch;
+  const int *rch_node;
+  const double *rch_rate;
+} gbsln_model;
+
+/* NONLINEAR block (NumericalSolution.f90:567-866, sln_setouter :2623-2671). */
+typedef struct gbsln_nonlinear {
+  double dvclose;  /* OUTER_DVCLOSE */
+  int mxiter;      /* OUTER_MAXIMUM */
+  int nonmeth;     /* UNDER_RELAXATION: 0 none, 1 simple, 2 cooley, 3 dbd */
+  double theta, akappa, gamma, amomentum;
+  int iallowptc;   /* 1 = pseudo-transient continuation allowed (default) */
+} gbsln_nonlinear;
+
+typedef struct gbsln_handle gbsln_handle;
+
+typedef struct gbsln_stats {
+  int outer;          /* outer iterations of the last time step */
+  int inner_total;    /* inner iterations summed over them */
+  int converged;
+  int pivot_retries;
+  double dxmax;       /* last outer max head change */
+  double fill_ms, solve_ms, total_ms; /* device time of the step */
+} gbsln_stats;
+
+int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,
+                 const gbims_settings *ims, const gbsln_nonlinear *nl,
+                 const double *strt, gbsln_handle **out);
+/* One time step (prepareSolve + outer loop + finalize).  delt <= 0 means a
+ * steady-state step (no storage). */
+int gbsln_timestep(gbsln_handle *h, int kper, int kstp, double delt, gbsln_stats *st);
+int gbsln_get_heads(gbsln_handle *h, double *x);
+int gbsln_set_heads(gbsln_handle *h, const double *x);
+gbims_handle *gbsln_ims(gbsln_handle *h);
+int gbsln_destroy(gbsln_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,634 @@
+// gbims_api.cu -- C ABI of the IMS linear accelerator (include/gbims.h).
+//
+// gbims_create mirrors ImsLinearDataType%imslinear_allocate
+// (src/Solution/LinearMethods/ImsLinear.f90:111-339) and gbims_apply mirrors
+// %imslinear_apply (:617-750): preconditioner update with the pivot retry of
+// ims_base_pcu (ImsLinearBase.f90:761-864), zeroed work vectors, the initial
+// residual and L2NORM0, then PCG or BiCGSTAB.
+//
+// The inner Krylov loop is one CUDA graph: a WHILE conditional node whose body
+// is one iteration; the device control kernels clear the condition when the
+// reference would EXIT INNER.  One graph launch per linear solve, no host
+// round trip per iteration.
+#include "gbims_internal.cuh"
+#include "k_krylov.cuh"
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <new>
+
+using namespace gb;
+
+struct gbims_handle {
+  gbims_settings s{};
+  int n = 0, nja = 0, ipc = 1;
+  bool mixed = false, bcgs = false;
+  std::vector<int> ia, ja, iapc, japc;
+  int *d_ia = nullptr, *d_ja = nullptr, *d_iapc = nullptr, *d_japc = nullptr;
+  double *d_apc = nullptr;
+  float *d_apc32 = nullptr;
+  Sell S;
+  Levels F, B;
+  Dia7 D;
+  bool structured = false;
+  // owned FP64 buffers
+  double *d_amat = nullptr, *d_rhs = nullptr, *d_x = nullptr;
+  double *v_d = nullptr, *v_p = nullptr, *v_q = nullptr, *v_z = nullptr, *v_t = nullptr,
+         *v_v = nullptr, *v_dhat = nullptr, *v_phat = nullptr, *v_qhat = nullptr;
+  // FP32 inner vectors (mixed)
+  float *f_d = nullptr, *f_p = nullptr, *f_q = nullptr, *f_z = nullptr, *f_t = nullptr,
+        *f_v = nullptr, *f_dhat = nullptr, *f_phat = nullptr, *f_qhat = nullptr;
+  double *d_part = nullptr;
+  int G = 1;
+  Ctl *d_ctl = nullptr, *h_ctl = nullptr;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool graph_tried = false, graph_ok = false;
+  double refine_factor = 1.0e-5;
+  bool factored = false;
+  std::string err;
+};
+
+#define GB_CUDA(h, call)                                                            \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      if (h) (h)->err = std::string(#call) + ": " + cudaGetErrorString(e_);         \
+      return GBIMS_ERR_CUDA;                                                        \
+    }                                                                               \
+  } while (0)
+
+template <typename T>
+static cudaError_t dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void **)p, sizeof(T) * count);
+}
+
+static int fail(gbims_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+// ---------------------------------------------------------------------------
+// graph body: one inner iteration
+// ---------------------------------------------------------------------------
+static void precond64(gbims_handle *h, const double *r, double *z) {
+  if (h->structured) launch_dia7_apply64(h->D, r, z, h->d_ctl, h->st);
+  else launch_ilu_apply_levels(h->n, h->d_iapc, h->d_japc, h->d_apc, h->F, h->B, r, z, h->d_ctl, h->st);
+}
+
+static void precond32(gbims_handle *h, const float *r, float *z) {
+  if (h->structured) launch_dia7_apply32(h->D, r, z, h->d_ctl, h->st);
+  else launch_ilu_apply_levels32(h->n, h->d_iapc, h->d_japc, h->d_apc32, h->F, h->B, r, z, h->d_ctl, h->st);
+}
+
+static void enqueue_iteration(gbims_handle *h, unsigned long long cond, int use_cond) {
+  const int n = h->n, G = h->G;
+  Ctl *c = h->d_ctl;
+  cudaStream_t st = h->st;
+  double *part = h->d_part;
+  if (!h->mixed && !h->bcgs) {
+    // ims_base_cg, ImsLinearBase.f90:100-236
+    precond64(h, h->v_d, h->v_z);
+    kr_dot64(n, h->v_d, h->v_z, part, G, c, st);
+    kr_ctl_cg_rho(c, part, G, st);
+    kr_cg_pupdate64(n, h->v_z, h->v_p, c, st);
+    launch_spmv64(h->S, h->v_p, h->v_q, c, st);
+    kr_dot64(n, h->v_p, h->v_q, part, G, c, st);
+    kr_ctl_alpha(c, part, G, st);
+    kr_cg_update64(n, h->d_x, h->v_d, h->v_p, h->v_q, part, G, c, st);
+    kr_ctl_cg_cnvg(c, part, G, cond, use_cond, st);
+    launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, c, 1, st);
+  } else if (!h->mixed && h->bcgs) {
+    // ims_base_bcgs, ImsLinearBase.f90:338-545
+    kr_dot64(n, h->v_dhat, h->v_d, part, G, c, st);
+    kr_ctl_bcgs_rho(c, part, G, st);
+    kr_bcgs_p64(n, h->v_d, h->v_p, h->v_v, c, st);
+    precond64(h, h->v_p, h->v_phat);
+    launch_spmv64(h->S, h->v_phat, h->v_v, c, st);
+    kr_dot64(n, h->v_dhat, h->v_v, part, G, c, st);
+    kr_ctl_alpha(c, part, G, st);
+    kr_bcgs_q64(n, h->v_d, h->v_v, h->v_q, c, st);
+    precond64(h, h->v_q, h->v_qhat);
+    launch_spmv64(h->S, h->v_qhat, h->v_t, c, st);
+    kr_dot_tq_tt64(n, h->v_t, h->v_q, part, G, c, st);
+    kr_ctl_omega(c, part, G, st);
+    kr_bcgs_update64(n, h->d_x, h->v_d, h->v_phat, h->v_qhat, h->v_q, h->v_t, nullptr, part, G, c, st);
+    kr_ctl_bcgs_cnvg(c, part, G, cond, use_cond, st);
+    launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, c, 1, st);
+  } else if (h->mixed && !h->bcgs) {
+    precond32(h, h->f_d, h->f_z);
+    kr_dot32(n, h->f_d, h->f_z, part, G, c, st);
+    kr_ctl_cg_rho(c, part, G, st);
+    kr_cg_pupdate32(n, h->f_z, h->f_p, c, st);
+    launch_spmv32(h->S, h->f_p, h->f_q, c, st);
+    kr_dot32(n, h->f_p, h->f_q, part, G, c, st);
+    kr_ctl_alpha(c, part, G, st);
+    kr_cg_update_mixed(n, h->d_x, h->f_d, h->f_p, h->f_q, part, G, c, st);
+    kr_ctl_mixed_inner(c, part, G, 0, h->refine_factor, st);
+    launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, c, 1, st);
+    kr_true_resid_stats(n, h->v_d, h->f_d, nullptr, part, G, c, st);
+    kr_ctl_refine(c, part, G, cond, use_cond, st);
+  } else {
+    kr_dot32(n, h->f_dhat, h->f_d, part, G, c, st);
+    kr_ctl_bcgs_rho(c, part, G, st);
+    kr_bcgs_p32(n, h->f_d, h->f_p, h->f_v, c, st);
+    precond32(h, h->f_p, h->f_phat);
+    launch_spmv32(h->S, h->f_phat, h->f_v, c, st);
+    kr_dot32(n, h->f_dhat, h->f_v, part, G, c, st);
+    kr_ctl_alpha(c, part, G, st);
+    kr_bcgs_q32(n, h->f_d, h->f_v, h->f_q, c, st);
+    precond32(h, h->f_q, h->f_qhat);
+    launch_spmv32(h->S, h->f_qhat, h->f_t, c, st);
+    kr_dot_tq_tt32(n, h->f_t, h->f_q, part, G, c, st);
+    kr_ctl_omega(c, part, G, st);
+    kr_bcgs_update32(n, h->d_x, h->f_d, h->f_phat, h->f_qhat, h->f_q, h->f_t, nullptr, part, G, c, st);
+    kr_ctl_mixed_inner(c, part, G, 1, h->refine_factor, st);
+    launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, c, 1, st);
+    kr_true_resid_stats(n, h->v_d, h->f_d, h->f_dhat, part, G, c, st);
+    kr_ctl_refine(c, part, G, cond, use_cond, st);
+  }
+}
+
+static bool build_graph(gbims_handle *h) {
+  h->graph_tried = true;
+  cudaGraph_t g = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+  cudaGraphConditionalHandle cond;
+  if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return false;
+  }
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  cp.conditional.handle = cond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return false;
+  }
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  if (cudaStreamBeginCaptureToGraph(h->st, body, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return false;
+  }
+  enqueue_iteration(h, (unsigned long long)cond, 1);
+  cudaGraph_t captured = nullptr;
+  cudaError_t e = cudaStreamEndCapture(h->st, &captured);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return false;
+  }
+  cudaGraphExec_t exec = nullptr;
+  if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return false;
+  }
+  h->graph = g;
+  h->exec = exec;
+  h->graph_ok = true;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// create
+// ---------------------------------------------------------------------------
+extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int *ia,
+                            const int *ja, gbims_handle **out) {
+  if (!out) return GBIMS_ERR_ARG;
+  *out = nullptr;
+  if (!s || !ia || !ja || neq <= 0 || nja < neq) return GBIMS_ERR_ARG;
+  gbims_handle *h = new (std::nothrow) gbims_handle();
+  if (!h) return GBIMS_ERR_NOMEM;
+  h->s = *s;
+  h->n = neq;
+  h->nja = nja;
+  // ImsLinear.f90:178-185: IPC from level/droptol/relax
+  h->ipc = (s->level > 0 || s->droptol > 0.0) ? 3 : 1;
+  if (s->relax > 0.0) h->ipc += 1;
+  // option checks (ImsLinear.f90:187-215)
+  if (s->ilinmeth != 1 && s->ilinmeth != 2) { *out = h; return fail(h, GBIMS_ERR_ARG, "ilinmeth must be 1 (CG) or 2 (BICGSTAB)"); }
+  if (s->iscl < 0 || s->iscl > 2) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR ISCL MUST BE <= 2"); }
+  if (s->iord < 0 || s->iord > 2) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR IORD MUST BE <= 2"); }
+  if (s->north < 0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR NORTH MUST >= 0"); }
+  if (s->rclose == 0.0 && s->icnvgopt != 3) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RCLOSE MUST > 0.0"); }
+  if (s->relax < 0.0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RELAX MUST BE >= 0.0"); }
+  if (s->relax > 1.0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RELAX MUST BE <= 1.0"); }
+  if (h->ipc >= 3) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "ILUT/MILUT (PRECONDITIONER_LEVELS/DROP_TOLERANCE > 0) is not supported"); }
+  if (s->iord != 0) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "REORDERING_METHOD RCM/MD is not supported"); }
+  if (s->iscl != 0) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "SCALING_METHOD other than NONE is not supported"); }
+  if (s->precision != GBIMS_FP64 && s->precision != GBIMS_MIXED) { *out = h; return fail(h, GBIMS_ERR_ARG, "precision must be GBIMS_FP64 or GBIMS_MIXED"); }
+  h->mixed = (s->precision == GBIMS_MIXED);
+  h->bcgs = (s->ilinmeth == 2);
+  // 0-based copies and checks: diagonal first in every row
+  int base = s->index_base ? 1 : 0;
+  h->ia.resize(neq + 1);
+  h->ja.resize(nja);
+  for (int i = 0; i <= neq; ++i) h->ia[i] = ia[i] - base;
+  for (int k = 0; k < nja; ++k) h->ja[k] = ja[k] - base;
+  if (h->ia[0] != 0 || h->ia[neq] != nja) { *out = h; return fail(h, GBIMS_ERR_ARG, "ia must start at index_base and end at nja+index_base"); }
+  for (int r = 0; r < neq; ++r) {
+    if (h->ia[r + 1] <= h->ia[r]) { *out = h; return fail(h, GBIMS_ERR_ARG, "empty CSR row (the diagonal must be present)"); }
+    if (h->ja[h->ia[r]] != r) { *out = h; return fail(h, GBIMS_ERR_ARG, "the diagonal must be the first entry of each row"); }
+    if (h->ia[r + 1] - h->ia[r] > kMaxRowLen) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "CSR row longer than 64 entries"); }
+    for (int k = h->ia[r]; k < h->ia[r + 1]; ++k)
+      if (h->ja[k] < 0 || h->ja[k] >= neq) { *out = h; return fail(h, GBIMS_ERR_ARG, "column index out of range"); }
+  }
+  // ims_base_pccrs (ImsLinearBase.f90:1207-1261)
+  h->iapc.assign(neq + 1, 0);
+  h->japc.assign(nja, 0);
+  {
+    int ip = neq;
+    std::vector<int> iarr;
+    for (int r = 0; r < neq; ++r) {
+      iarr.clear();
+      for (int k = h->ia[r]; k < h->ia[r + 1]; ++k)
+        if (h->ja[k] != r) iarr.push_back(h->ja[k]);
+      std::stable_sort(iarr.begin(), iarr.end());
+      h->iapc[r] = ip;
+      for (int c : iarr) h->japc[ip++] = c;
+    }
+    h->iapc[neq] = nja;
+    if (ip != nja) { *out = h; return fail(h, GBIMS_ERR_ARG, "nja is inconsistent with ia (one diagonal per row expected)"); }
+    for (int r = 0; r < neq; ++r) {
+      h->japc[r] = h->iapc[r + 1];
+      for (int j = h->iapc[r]; j < h->iapc[r + 1]; ++j)
+        if (h->japc[j] > r) { h->japc[r] = j; break; }
+    }
+  }
+  // device state
+  *out = h;
+  GB_CUDA(h, cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  GB_CUDA(h, cudaEventCreate(&h->ev0));
+  GB_CUDA(h, cudaEventCreate(&h->ev1));
+  GB_CUDA(h, dalloc(&h->d_ia, neq + 1));
+  GB_CUDA(h, dalloc(&h->d_ja, nja));
+  GB_CUDA(h, dalloc(&h->d_iapc, neq + 1));
+  GB_CUDA(h, dalloc(&h->d_japc, nja));
+  GB_CUDA(h, dalloc(&h->d_apc, nja));
+  GB_CUDA(h, cudaMemcpy(h->d_ia, h->ia.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
+  GB_CUDA(h, cudaMemcpy(h->d_ja, h->ja.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
+  GB_CUDA(h, cudaMemcpy(h->d_iapc, h->iapc.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
+  GB_CUDA(h, cudaMemcpy(h->d_japc, h->japc.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
+  GB_CUDA(h, cudaMemset(h->d_apc, 0, sizeof(double) * nja));
+  // SELL-32 layout of A
+  {
+    std::vector<int> ptr, col, src;
+    sell_build_host(neq, h->ia, h->ja, ptr, col, src);
+    if ((long long)col.size() > INT_MAX) return fail(h, GBIMS_ERR_UNSUPPORTED, "matrix too large for 32-bit SELL offsets");
+    h->S.n = neq;
+    h->S.nslices = (int)ptr.size() - 1;
+    h->S.nstored = (long long)col.size();
+    GB_CUDA(h, dalloc(&h->S.d_ptr, ptr.size()));
+    GB_CUDA(h, dalloc(&h->S.d_col, col.size()));
+    GB_CUDA(h, dalloc(&h->S.d_src, src.size()));
+    GB_CUDA(h, dalloc(&h->S.d_val, col.size()));
+    GB_CUDA(h, cudaMemcpy(h->S.d_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice));
+    GB_CUDA(h, cudaMemcpy(h->S.d_col, col.data(), sizeof(int) * col.size(), cudaMemcpyHostToDevice));
+    GB_CUDA(h, cudaMemcpy(h->S.d_src, src.data(), sizeof(int) * src.size(), cudaMemcpyHostToDevice));
+    if (h->mixed) GB_CUDA(h, dalloc(&h->S.d_val32, col.size()));
+  }
+  // level schedules of the triangular sweeps and the factorisation
+  levels_build_host(neq, h->iapc, h->japc, true, h->F);
+  levels_build_host(neq, h->iapc, h->japc, false, h->B);
+  // optional structured 7-point sweeps
+  if (s->nlay > 0 && s->nrow > 0 && s->ncol > 0 &&
+      dia7_matches(s->nlay, s->nrow, s->ncol, neq, h->ia, h->ja)) {
+    h->D.nlay = s->nlay;
+    h->D.nrow = s->nrow;
+    h->D.ncol = s->ncol;
+    size_t nn = (size_t)neq;
+    if (!h->mixed) {
+      GB_CUDA(h, dalloc(&h->D.d_lz, nn)); GB_CUDA(h, dalloc(&h->D.d_ly, nn)); GB_CUDA(h, dalloc(&h->D.d_lx, nn));
+      GB_CUDA(h, dalloc(&h->D.d_ux, nn)); GB_CUDA(h, dalloc(&h->D.d_uy, nn)); GB_CUDA(h, dalloc(&h->D.d_uz, nn));
+      GB_CUDA(h, dalloc(&h->D.d_dinv, nn));
+    } else {
+      GB_CUDA(h, dalloc(&h->D.f_lz, nn)); GB_CUDA(h, dalloc(&h->D.f_ly, nn)); GB_CUDA(h, dalloc(&h->D.f_lx, nn));
+      GB_CUDA(h, dalloc(&h->D.f_ux, nn)); GB_CUDA(h, dalloc(&h->D.f_uy, nn)); GB_CUDA(h, dalloc(&h->D.f_uz, nn));
+      GB_CUDA(h, dalloc(&h->D.f_dinv, nn));
+    }
+    h->D.nflags = s->nlay * s->nrow + 64;
+    GB_CUDA(h, dalloc(&h->D.d_flags, h->D.nflags));
+    GB_CUDA(h, dalloc(&h->D.d_err, 4));
+    GB_CUDA(h, cudaMemset(h->D.d_err, 0, sizeof(int) * 4));
+    h->structured = true;
+  }
+  // vectors
+  size_t nn = (size_t)neq;
+  GB_CUDA(h, dalloc(&h->d_amat, nja));
+  GB_CUDA(h, dalloc(&h->d_rhs, nn));
+  GB_CUDA(h, dalloc(&h->d_x, nn));
+  GB_CUDA(h, dalloc(&h->v_d, nn));
+  if (!h->mixed) {
+    GB_CUDA(h, dalloc(&h->v_p, nn));
+    GB_CUDA(h, dalloc(&h->v_q, nn));
+    GB_CUDA(h, dalloc(&h->v_z, nn));
+    if (h->bcgs) {
+      GB_CUDA(h, dalloc(&h->v_t, nn)); GB_CUDA(h, dalloc(&h->v_v, nn));
+      GB_CUDA(h, dalloc(&h->v_dhat, nn)); GB_CUDA(h, dalloc(&h->v_phat, nn));
+      GB_CUDA(h, dalloc(&h->v_qhat, nn));
+    }
+  } else {
+    GB_CUDA(h, dalloc(&h->d_apc32, nja));
+    GB_CUDA(h, dalloc(&h->f_d, nn)); GB_CUDA(h, dalloc(&h->f_p, nn));
+    GB_CUDA(h, dalloc(&h->f_q, nn)); GB_CUDA(h, dalloc(&h->f_z, nn));
+    if (h->bcgs) {
+      GB_CUDA(h, dalloc(&h->f_t, nn)); GB_CUDA(h, dalloc(&h->f_v, nn));
+      GB_CUDA(h, dalloc(&h->f_dhat, nn)); GB_CUDA(h, dalloc(&h->f_phat, nn));
+      GB_CUDA(h, dalloc(&h->f_qhat, nn));
+    }
+  }
+  h->G = std::max(1, std::min(kMaxRedBlocks, (neq + kRedBlock - 1) / kRedBlock));
+  GB_CUDA(h, dalloc(&h->d_part, (size_t)h->G * 8));
+  GB_CUDA(h, dalloc(&h->d_ctl, 1));
+  GB_CUDA(h, cudaMallocHost((void **)&h->h_ctl, sizeof(Ctl)));
+  memset(h->h_ctl, 0, sizeof(Ctl));
+  return GBIMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// apply
+// ---------------------------------------------------------------------------
+static double epfact_of(int icnvgopt, int kstp) {
+  // ims_base_epfact (ImsLinearBase.f90:1316-1333); 0.01/0.10 are default
+  // (single-precision) real literals in the Fortran source
+  if (icnvgopt == 2) return (kstp == 1) ? (double)0.01f : (double)0.10f;
+  if (icnvgopt == 4) return 1.0e-4;
+  return 1.0;
+}
+
+__global__ void k_zero_vec(int n, double *a, double *b, double *c, double *d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (a) a[i] = 0.0;
+    if (b) b[i] = 0.0;
+    if (c) c[i] = 0.0;
+    if (d) d[i] = 0.0;
+  }
+}
+
+// Preconditioner update from h->d_amat: ims_base_pcu with its retry loop
+// (ImsLinearBase.f90:761-864).  Returns the retry count or a negative status.
+static int factor_core(gbims_handle *h) {
+  const int n = h->n;
+  cudaStream_t st = h->st;
+  launch_sell_fill(h->S, h->d_amat, st);
+  int ipcflag = 0, icount = 0;
+  double delta = 0.0;
+  for (;;) {
+    Ctl init;
+    memset(&init, 0, sizeof(init));
+    init.pivot_fail = INT_MAX;
+    *h->h_ctl = init;
+    GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+    launch_ilu_factor(n, h->d_ia, h->d_ja, h->d_amat, h->d_iapc, h->d_japc, h->d_apc, h->F,
+                      h->s.relax, delta, ipcflag, h->d_ctl, st);
+    GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(h, cudaStreamSynchronize(st));
+    GB_CUDA(h, cudaGetLastError());
+    ipcflag = (h->h_ctl->pivot_fail != INT_MAX) ? 1 : 0;
+    if (ipcflag < 1) break;
+    delta = 1.5 * delta + 1.0e-3;
+    ipcflag = 0;
+    if (delta > 0.5) {
+      delta = 0.5;
+      ipcflag = 2;
+    }
+    icount += 1;
+    if (icount > 10) break;
+  }
+  if (h->mixed) kr_f64_to_f32(h->nja, h->d_apc, h->d_apc32, st);
+  if (h->structured) launch_dia7_extract(h->D, n, h->d_iapc, h->d_japc, h->d_apc, h->mixed, st);
+  GB_CUDA(h, cudaGetLastError());
+  h->factored = true;
+  return icount;
+}
+
+static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_iter,
+                      gbims_summary *summary) {
+  const int n = h->n;
+  cudaStream_t st = h->st;
+  (void)kiter;
+  GB_CUDA(h, cudaEventRecord(h->ev0, st));
+  int icount = factor_core(h);
+  if (icount < 0) return icount;
+  // control block
+  Ctl c;
+  memset(&c, 0, sizeof(c));
+  c.itmax = h->s.iter1;
+  c.icnvgopt = h->s.icnvgopt;
+  c.north = h->mixed ? 0 : h->s.north;
+  c.iscl = h->s.iscl;
+  c.dvclose = h->s.dvclose;
+  c.rclose = h->s.rclose;
+  c.epfact = epfact_of(h->s.icnvgopt, kstp);
+  c.iter = 1;
+  c.first = 1;
+  c.pivot_fail = INT_MAX;
+  *h->h_ctl = c;
+  GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+  // D, P, Q, Z = 0 ; D = B - A X ; L2NORM0 (ImsLinear.f90:686-703)
+  int eg = std::min(4 * kNumSM, (n + 255) / 256);
+  k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
+  launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, nullptr, 0, st);
+  kr_sumsq64(n, h->v_d, h->d_part, h->G, st);
+  kr_ctl_set_l2norm0(h->d_ctl, h->d_part, h->G, st);
+  if (h->bcgs && !h->mixed) GB_CUDA(h, cudaMemcpyAsync(h->v_dhat, h->v_d, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if (h->mixed) {
+    kr_f64_to_f32(n, h->v_d, h->f_d, st);
+    GB_CUDA(h, cudaMemsetAsync(h->f_p, 0, sizeof(float) * n, st));
+    if (h->bcgs) {
+      GB_CUDA(h, cudaMemcpyAsync(h->f_dhat, h->f_d, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+      GB_CUDA(h, cudaMemsetAsync(h->f_v, 0, sizeof(float) * n, st));
+    }
+  }
+  GB_CUDA(h, cudaGetLastError());
+  // inner loop
+  if (!h->graph_tried) build_graph(h);
+  if (h->graph_ok) {
+    GB_CUDA(h, cudaGraphLaunch(h->exec, st));
+  } else {
+    // fallback: host-driven loop in growing batches of iterations
+    int batch = 1, total = 0;
+    for (;;) {
+      for (int b = 0; b < batch; ++b) enqueue_iteration(h, 0ULL, 0);
+      total += batch;
+      GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      GB_CUDA(h, cudaStreamSynchronize(st));
+      if (h->h_ctl->done || total > 4 * (h->s.iter1 + 2)) break;
+      batch = std::min(batch * 2, 32);
+    }
+  }
+  GB_CUDA(h, cudaEventRecord(h->ev1, st));
+  GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(h, cudaStreamSynchronize(st));
+  GB_CUDA(h, cudaGetLastError());
+  const Ctl &r = *h->h_ctl;
+  int iters = (r.l2norm0 == 0.0 || h->s.iter1 <= 0) ? 0 : r.iter;
+  *icnvg = r.icnvg;
+  *in_iter = iters;
+  if (summary) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    summary->iter_cnt = iters;
+    summary->icnvg = r.icnvg;
+    summary->pivot_retries = icount;
+    summary->exit_reason = r.exit_reason;
+    summary->dvmax = r.deltax;
+    summary->locdv = (int)r.xloc;
+    summary->rmax = r.rmax;
+    summary->locr = (int)r.rloc;
+    summary->l2norm0 = r.l2norm0;
+    summary->l2norm = r.l2norm;
+    summary->solve_ms = ms;
+    summary->refinements = (int)r.scratch[3];
+    summary->structured = h->structured ? 1 : 0;
+  }
+  if (r.nonfinite) return fail(h, GBIMS_ERR_NONFINITE, "non-finite values in the residual or head change");
+  if (r.guard_tripped) return fail(h, GBIMS_ERR_STATE, "inner loop cut by the body limit");
+  if (h->structured) {
+    int derr = 0;
+    GB_CUDA(h, cudaMemcpy(&derr, h->D.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (derr) return fail(h, GBIMS_ERR_CUDA, "structured sweep wait limit reached");
+  }
+  return icount > 0 ? GBIMS_WARN_PIVOT : GBIMS_OK;
+}
+
+extern "C" int gbims_apply(gbims_handle *h, double *amat, double *rhs, double *x, int kstp,
+                           int kiter, int *icnvg, int *in_iter, gbims_summary *summary) {
+  if (!h || !amat || !rhs || !x || !icnvg || !in_iter) return GBIMS_ERR_ARG;
+  if (!h->d_ctl) return fail(h, GBIMS_ERR_STATE, "handle was not created successfully");
+  GB_CUDA(h, cudaMemcpyAsync(h->d_amat, amat, sizeof(double) * h->nja, cudaMemcpyHostToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_rhs, rhs, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_x, x, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  int rc = apply_core(h, kstp, kiter, icnvg, in_iter, summary);
+  if (rc < 0 && rc != GBIMS_ERR_NONFINITE) return rc;
+  cudaError_t e = cudaMemcpy(x, h->d_x, sizeof(double) * h->n, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(h, GBIMS_ERR_CUDA, cudaGetErrorString(e));
+  return rc;
+}
+
+extern "C" int gbims_apply_device(gbims_handle *h, double *d_amat, double *d_rhs, double *d_x,
+                                  int kstp, int kiter, int *icnvg, int *in_iter,
+                                  gbims_summary *summary) {
+  if (!h || !d_amat || !d_rhs || !d_x || !icnvg || !in_iter) return GBIMS_ERR_ARG;
+  if (!h->d_ctl) return fail(h, GBIMS_ERR_STATE, "handle was not created successfully");
+  GB_CUDA(h, cudaMemcpyAsync(h->d_amat, d_amat, sizeof(double) * h->nja, cudaMemcpyDeviceToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_rhs, d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_x, d_x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
+  int rc = apply_core(h, kstp, kiter, icnvg, in_iter, summary);
+  if (rc < 0 && rc != GBIMS_ERR_NONFINITE) return rc;
+  cudaError_t e = cudaMemcpyAsync(d_x, h->d_x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) return fail(h, GBIMS_ERR_CUDA, cudaGetErrorString(e));
+  return rc;
+}
+
+extern "C" int gbims_factor(gbims_handle *h, const double *amat, int *pivot_retries) {
+  if (!h || !amat) return GBIMS_ERR_ARG;
+  if (!h->d_ctl) return fail(h, GBIMS_ERR_STATE, "handle was not created successfully");
+  GB_CUDA(h, cudaMemcpyAsync(h->d_amat, amat, sizeof(double) * h->nja, cudaMemcpyHostToDevice, h->st));
+  int icount = factor_core(h);
+  if (icount < 0) return icount;
+  GB_CUDA(h, cudaStreamSynchronize(h->st));
+  if (pivot_retries) *pivot_retries = icount;
+  return icount > 0 ? GBIMS_WARN_PIVOT : GBIMS_OK;
+}
+
+extern "C" int gbims_get_apc(gbims_handle *h, double *apc) {
+  if (!h || !apc) return GBIMS_ERR_ARG;
+  if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no factor: call gbims_factor or gbims_apply first");
+  GB_CUDA(h, cudaStreamSynchronize(h->st));
+  GB_CUDA(h, cudaMemcpy(apc, h->d_apc, sizeof(double) * h->nja, cudaMemcpyDeviceToHost));
+  return GBIMS_OK;
+}
+
+extern "C" int gbims_matvec(gbims_handle *h, const double *x, double *y) {
+  if (!h || !x || !y) return GBIMS_ERR_ARG;
+  if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no matrix: call gbims_factor or gbims_apply first");
+  GB_CUDA(h, cudaMemcpyAsync(h->v_d, x, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  launch_spmv64(h->S, h->v_d, h->d_rhs, nullptr, h->st);
+  GB_CUDA(h, cudaGetLastError());
+  GB_CUDA(h, cudaMemcpyAsync(y, h->d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
+  GB_CUDA(h, cudaStreamSynchronize(h->st));
+  return GBIMS_OK;
+}
+
+extern "C" int gbims_precondition(gbims_handle *h, const double *r, double *z) {
+  if (!h || !r || !z) return GBIMS_ERR_ARG;
+  if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no factor: call gbims_factor or gbims_apply first");
+  GB_CUDA(h, cudaMemcpyAsync(h->v_d, r, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  // a control block with done = 0 lets the gated sweep kernels run
+  Ctl c;
+  memset(&c, 0, sizeof(c));
+  c.pivot_fail = INT_MAX;
+  *h->h_ctl = c;
+  GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->st));
+  if (!h->mixed) {
+    precond64(h, h->v_d, h->d_rhs);
+  } else {
+    kr_f64_to_f32(h->n, h->v_d, h->f_d, h->st);
+    precond32(h, h->f_d, h->f_z);
+    kr_f32_to_f64(h->n, h->f_z, h->d_rhs, h->st);
+  }
+  GB_CUDA(h, cudaGetLastError());
+  GB_CUDA(h, cudaMemcpyAsync(z, h->d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
+  GB_CUDA(h, cudaStreamSynchronize(h->st));
+  return GBIMS_OK;
+}
+
+extern "C" int gbims_destroy(gbims_handle *h) {
+  if (!h) return GBIMS_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->exec) cudaGraphExecDestroy(h->exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  void *ptrs[] = {h->d_ia, h->d_ja, h->d_iapc, h->d_japc, h->d_apc, h->d_apc32, h->S.d_ptr,
+                  h->S.d_col, h->S.d_src, h->S.d_val, h->S.d_val32, h->F.d_rows, h->B.d_rows,
+                  h->D.d_lz, h->D.d_ly, h->D.d_lx, h->D.d_ux, h->D.d_uy, h->D.d_uz, h->D.d_dinv,
+                  h->D.f_lz, h->D.f_ly, h->D.f_lx, h->D.f_ux, h->D.f_uy, h->D.f_uz, h->D.f_dinv,
+                  h->D.d_flags, h->D.d_err, h->d_amat, h->d_rhs, h->d_x, h->v_d, h->v_p, h->v_q,
+                  h->v_z, h->v_t, h->v_v, h->v_dhat, h->v_phat, h->v_qhat, h->f_d, h->f_p,
+                  h->f_q, h->f_z, h->f_t, h->f_v, h->f_dhat, h->f_phat, h->f_qhat, h->d_part,
+                  h->d_ctl};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (h->h_ctl) cudaFreeHost(h->h_ctl);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return GBIMS_OK;
+}
+
+extern "C" const char *gbims_last_error(const gbims_handle *h) {
+  if (!h) return "null handle";
+  return h->err.c_str();
+}
+
+extern "C" const char *gbims_status_string(int status) {
+  switch (status) {
+  case GBIMS_OK: return "ok";
+  case GBIMS_WARN_PIVOT: return "warning: small value added to ILU0 pivots";
+  case GBIMS_ERR_ARG: return "invalid argument";
+  case GBIMS_ERR_CUDA: return "CUDA error";
+  case GBIMS_ERR_UNSUPPORTED: return "unsupported option";
+  case GBIMS_ERR_NONFINITE: return "non-finite values";
+  case GBIMS_ERR_NOMEM: return "out of memory";
+  case GBIMS_ERR_STATE: return "invalid handle state";
+  default: return "unknown status";
+  }
+}
+
+// Accessors used by the device-resident solution (gbsln_*).
+namespace gb {
+double *ims_device_x(gbims_handle *h) { return h->d_x; }
+}

@@ -1,0 +1,144 @@
+// gbims_internal.cuh -- shared declarations of the GB300 IMS library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/gbims.h"
+
+namespace gb {
+
+constexpr int kNumSM = 152;       // GB300: 2 dies x 76 SMs
+constexpr int kRedBlock = 256;    // threads per reduction block
+constexpr int kMaxRedBlocks = 2 * kNumSM * 2;  // grid of reduction kernels
+constexpr int kSell = 32;         // SELL slice height (one warp)
+constexpr int kMaxRowLen = 64;    // ILU0 factor: longest supported CSR row
+
+// Exit reasons reported in gbims_summary.exit_reason.
+enum ExitReason { kExitNone = 0, kExitClosure = 1, kExitStagnation = 2, kExitItmax = 3,
+                  kExitExact = 4, kExitZeroRho = 5 };
+
+// Device control block of one Krylov solve: inputs, scalars and the loop
+// state.  Written by the single-thread control kernels, read by all others.
+struct Ctl {
+  // inputs
+  int itmax, icnvgopt, north, iscl;
+  double dvclose, rclose, l2norm0, epfact;
+  // loop state
+  int iter;        // current inner iteration (1-based, INNERIT)
+  int done;        // 1 = stop: every kernel of the loop returns at once
+  int icnvg;
+  int exit_reason;
+  int north_due;   // recompute the residual after this iteration
+  int first;       // 1 in the first iteration (P = Z)
+  double rho, rho0, alpha, alpha0, beta, omega, omega0;
+  double deltax, rmax, l2norm;
+  long long xloc, rloc;
+  double scratch[4];
+  int pivot_fail;  // factorization: first row whose pivot failed (or INT_MAX)
+  int nonfinite;
+  int bodies;         // loop bodies executed in this solve
+  int guard_tripped;  // the body limit ended the loop
+};
+
+// Reduction partial layout: value slots per block.
+struct MaxLoc {
+  double val;      // signed value
+  long long idx;   // row (-1 = none)
+};
+
+__device__ __forceinline__ bool absgt(double a, double b) {
+  // |a| > |b| on the integer image of |a|, |b|: for finite doubles the order
+  // of the bit patterns of the magnitudes is the order of the magnitudes,
+  // and it keeps the comparison off the FP64 pipe.  NaN magnitudes compare
+  // greater than every finite value here; the reference's strict > never
+  // selects a NaN, so NaN input is detected separately (Ctl::nonfinite).
+  unsigned long long ua = __double_as_longlong(a) & 0x7fffffffffffffffULL;
+  unsigned long long ub = __double_as_longlong(b) & 0x7fffffffffffffffULL;
+  return ua > ub;
+}
+
+__device__ __forceinline__ void maxloc_merge(MaxLoc &a, const MaxLoc &b) {
+  unsigned long long ua = __double_as_longlong(a.val) & 0x7fffffffffffffffULL;
+  unsigned long long ub = __double_as_longlong(b.val) & 0x7fffffffffffffffULL;
+  if (ub > ua || (ub == ua && ub != 0 && b.idx >= 0 && (a.idx < 0 || b.idx < a.idx))) a = b;
+}
+
+// ---------------------------------------------------------------------------
+// Sparse formats
+// ---------------------------------------------------------------------------
+
+// SELL-32: slices of 32 consecutive rows, entries stored column-major inside
+// the slice (entry k of row r at slice_ptr[s] + k*32 + r%32), padded to the
+// longest row of the slice.  Entry k of a row is its k-th CSR entry, so the
+// per-row summation order is the CSR (JA) order of amux.
+struct Sell {
+  int n = 0, nslices = 0;
+  long long nstored = 0;
+  int *d_ptr = nullptr;   // nslices+1 element offsets
+  int *d_col = nullptr;   // nstored, padded entries point at the row itself
+  int *d_src = nullptr;   // nstored, CSR position or -1 for padding
+  double *d_val = nullptr;
+  float *d_val32 = nullptr;
+};
+
+// Level schedule of a triangular sweep: rows grouped by level.
+struct Levels {
+  int nlev = 0;
+  std::vector<int> ptr;   // nlev+1
+  int *d_rows = nullptr;  // n
+  int maxwidth = 0;
+};
+
+// Structured 7-point DIS layout of the ILU0 factors for the wavefront sweeps.
+struct Dia7 {
+  int nlay = 0, nrow = 0, ncol = 0;
+  // lower coefficients L (unit diagonal) per row: z (layer above), y (row
+  // behind), x (column left); upper U: x, y, z; inverse pivot.  Length n each,
+  // 0 where the neighbour does not exist.
+  double *d_lz = nullptr, *d_ly = nullptr, *d_lx = nullptr;
+  double *d_ux = nullptr, *d_uy = nullptr, *d_uz = nullptr, *d_dinv = nullptr;
+  float *f_lz = nullptr, *f_ly = nullptr, *f_lx = nullptr;
+  float *f_ux = nullptr, *f_uy = nullptr, *f_uz = nullptr, *f_dinv = nullptr;
+  int *d_flags = nullptr;  // wavefront progress counters
+  int nflags = 0;
+  int *d_err = nullptr;    // wait-limit error flag
+};
+
+// ---------------------------------------------------------------------------
+// kernel launchers (implemented in the .cu files)
+// ---------------------------------------------------------------------------
+void sell_build_host(int n, const std::vector<int> &ia, const std::vector<int> &ja,
+                     std::vector<int> &ptr, std::vector<int> &col, std::vector<int> &src);
+void launch_sell_fill(const Sell &S, const double *d_amat, cudaStream_t st);
+void launch_spmv64(const Sell &S, const double *x, double *y, const Ctl *ctl, cudaStream_t st);
+void launch_spmv32(const Sell &S, const float *x, float *y, const Ctl *ctl, cudaStream_t st);
+void launch_residual64(const Sell &S, const double *x, const double *b, double *d,
+                       const Ctl *ctl, int only_if_north_due, cudaStream_t st);
+
+void levels_build_host(int n, const std::vector<int> &iapc, const std::vector<int> &japc,
+                       bool forward, Levels &L);
+void launch_ilu_factor(int n, const int *d_ia, const int *d_ja, const double *d_amat,
+                       const int *d_iapc, const int *d_japc, double *d_apc,
+                       const Levels &L, double relax, double delta, int ipcflag,
+                       Ctl *ctl, cudaStream_t st);
+void launch_ilu_apply_levels(int n, const int *d_iapc, const int *d_japc,
+                             const double *d_apc, const Levels &F, const Levels &B,
+                             const double *r, double *d, const Ctl *ctl, cudaStream_t st);
+void launch_ilu_apply_levels32(int n, const int *d_iapc, const int *d_japc,
+                               const float *d_apc32, const Levels &F, const Levels &B,
+                               const float *r, float *d, const Ctl *ctl, cudaStream_t st);
+
+bool dia7_matches(int nlay, int nrow, int ncol, int n, const std::vector<int> &ia,
+                  const std::vector<int> &ja);
+void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_japc,
+                         const double *d_apc, bool mixed, cudaStream_t st);
+void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
+                         cudaStream_t st);
+void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
+                         cudaStream_t st);
+
+}  // namespace gb

@@ -1,0 +1,766 @@
+// k_krylov.cu -- fused vector updates, deterministic reductions and the
+// device-side control logic of the IMS Krylov accelerators.
+//
+// PCG: ims_base_cg (src/Solution/LinearMethods/ImsLinearBase.f90:30-240).
+// BiCGSTAB: ims_base_bcgs (:249-549).  Convergence: ims_base_testcnvg
+// (:1101-1146) and is_close (src/Utilities/MathUtil.f90:45-86).
+//
+// Each reduction kernel writes one partial per block; a single-block control
+// kernel sums the partials in a fixed order (so results are reproducible run
+// to run), then runs the scalar logic of the reference on the device: beta,
+// alpha, omega with the +SIGN(DPREC, denominator) guard, the closure test,
+// the stagnation exits and the NORTH residual schedule.  It sets Ctl::done,
+// which every kernel of the loop checks first, and the WHILE condition of the
+// CUDA graph, so the whole inner loop runs without a host round trip.
+#include "gbims_internal.cuh"
+#include "k_krylov.cuh"
+#include <cfloat>
+
+namespace gb {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ MaxLoc warp_maxloc(MaxLoc m) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    MaxLoc b;
+    b.val = __shfl_xor_sync(0xffffffffu, m.val, o);
+    b.idx = __shfl_xor_sync(0xffffffffu, m.idx, o);
+    maxloc_merge(m, b);
+  }
+  return m;
+}
+
+// Sum NV values over the block; thread 0 gets the results (fixed order).
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+  __shared__ double sh[NV][kRedBlock / 32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double s = warp_sum(v[k]);
+    if (lane == 0) sh[k][wid] = s;
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = (lane < (int)(blockDim.x >> 5)) ? sh[k][lane] : 0.0;
+      v[k] = warp_sum(s);
+    }
+  }
+  __syncthreads();
+}
+
+template <int NM>
+__device__ __forceinline__ void block_maxloc(MaxLoc (&m)[NM]) {
+  __shared__ double shv[NM][kRedBlock / 32];
+  __shared__ long long shi[NM][kRedBlock / 32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NM; ++k) {
+    MaxLoc r = warp_maxloc(m[k]);
+    if (lane == 0) {
+      shv[k][wid] = r.val;
+      shi[k][wid] = r.idx;
+    }
+  }
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+      MaxLoc r;
+      r.val = 0.0;
+      r.idx = -1;
+      if (lane < (int)(blockDim.x >> 5)) {
+        r.val = shv[k][lane];
+        r.idx = shi[k][lane];
+      }
+      m[k] = warp_maxloc(r);
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ double to_d(double v) { return v; }
+__device__ __forceinline__ double to_d(float v) { return (double)v; }
+
+// ---------------------------------------------------------------------------
+// dot products: partial[b] (and partial[G+b])
+// ---------------------------------------------------------------------------
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(kRedBlock) k_dot(int n, const TA *__restrict__ a,
+                                                    const TB *__restrict__ b,
+                                                    double *__restrict__ part,
+                                                    const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    v[0] = fma(to_d(a[i]), to_d(b[i]), v[0]);
+  block_sum<1>(v);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+// t.q and t.t in one pass (BiCGSTAB omega)
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_dot_tq_tt(int n, const T *__restrict__ t,
+                                                          const T *__restrict__ q,
+                                                          double *__restrict__ part,
+                                                          const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  double v[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double ti = to_d(t[i]);
+    v[0] = fma(ti, to_d(q[i]), v[0]);
+    v[1] = fma(ti, ti, v[1]);
+  }
+  block_sum<2>(v);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = v[0];
+    part[gridDim.x + blockIdx.x] = v[1];
+  }
+}
+
+// sum of squares (L2NORM0)
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_sumsq(int n, const T *__restrict__ a,
+                                                      double *__restrict__ part) {
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double ai = to_d(a[i]);
+    v[0] = fma(ai, ai, v[0]);
+  }
+  block_sum<1>(v);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+// ---------------------------------------------------------------------------
+// partial-sum finalisation inside the single-block control kernels
+// ---------------------------------------------------------------------------
+__device__ double ctl_reduce_sum(const double *part, int G) {
+  double v[1] = {0.0};
+  for (int i = threadIdx.x; i < G; i += blockDim.x) v[0] += part[i];
+  block_sum<1>(v);
+  return v[0];  // valid in thread 0
+}
+
+__device__ MaxLoc ctl_reduce_maxloc(const double *pv, const double *pi, int G) {
+  MaxLoc m[1];
+  m[0].val = 0.0;
+  m[0].idx = -1;
+  for (int i = threadIdx.x; i < G; i += blockDim.x) {
+    MaxLoc b;
+    b.val = pv[i];
+    b.idx = (long long)pi[i];
+    maxloc_merge(m[0], b);
+  }
+  block_maxloc<1>(m);
+  return m[0];
+}
+
+__device__ __forceinline__ bool d_is_close(double a, double b) {
+  if (a == b) return true;
+  double tol = 100.0 * DBL_EPSILON * fmax(fabs(a), fabs(b));
+  if (tol < 0.0) tol = 0.0;
+  return fabs(a - b) <= tol;
+}
+
+__device__ __forceinline__ void d_testcnvg(int icnvgopt, int &icnvg, int iiter, double dvmax,
+                                           double rmax, double rmax0, double epfact,
+                                           double dvclose, double rclose) {
+  if (icnvgopt == 0) {
+    if (fabs(dvmax) <= dvclose && fabs(rmax) <= rclose) icnvg = 1;
+  } else if (icnvgopt == 1) {
+    if (fabs(dvmax) <= dvclose && fabs(rmax) <= rclose) icnvg = (iiter == 1) ? 1 : -1;
+  } else if (icnvgopt == 2) {
+    if (fabs(dvmax) <= dvclose || rmax <= rclose) icnvg = 1;
+    else if (rmax <= rmax0 * epfact) icnvg = -1;
+  } else if (icnvgopt == 3) {
+    if (fabs(dvmax) <= dvclose) icnvg = 1;
+    else if (rmax <= rmax0 * rclose) icnvg = -1;
+  } else if (icnvgopt == 4) {
+    if (fabs(dvmax) <= dvclose && rmax <= rclose) icnvg = 1;
+    else if (rmax <= rmax0 * epfact) icnvg = -1;
+  }
+}
+
+__device__ __forceinline__ double sign_dprec(double den) { return copysign(DBL_EPSILON, den); }
+
+// Sets the WHILE condition of the graph.  Independently of the IMS exit logic,
+// the loop is cut after 2*itmax + 16 bodies, so no input can keep the device
+// looping.
+__device__ __forceinline__ void set_loop(Ctl *ctl, unsigned long long cond, int use_cond) {
+  ctl->bodies += 1;
+  if (ctl->bodies > 2 * ctl->itmax + 16 && !ctl->done) {
+    ctl->done = 1;
+    ctl->guard_tripped = 1;
+  }
+  if (use_cond) cudaGraphSetConditional((cudaGraphConditionalHandle)cond, ctl->done ? 0u : 1u);
+}
+
+// ---------------------------------------------------------------------------
+// PCG
+// ---------------------------------------------------------------------------
+__global__ void k_ctl_cg_rho(Ctl *ctl, const double *part, int G) {
+  if (ctl->done) return;
+  double s = ctl_reduce_sum(part, G);
+  if (threadIdx.x == 0) {
+    ctl->rho = s;
+    ctl->beta = ctl->first ? 0.0 : s / ctl->rho0;
+  }
+}
+
+__global__ void k_ctl_alpha(Ctl *ctl, const double *part, int G) {
+  if (ctl->done) return;
+  double s = ctl_reduce_sum(part, G);
+  if (threadIdx.x == 0) {
+    double den = s + sign_dprec(s);
+    ctl->alpha = ctl->rho / den;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_cg_pupdate(int n, const T *__restrict__ z, T *__restrict__ p,
+                                                    const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (ctl->first) p[i] = z[i];
+  else p[i] = (T)fma((double)(T)ctl->beta, (double)p[i], (double)z[i]);
+}
+
+__global__ void __launch_bounds__(256) k_cg_pupdate64(int n, const double *__restrict__ z,
+                                                      double *__restrict__ p,
+                                                      const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  p[i] = ctl->first ? z[i] : fma(ctl->beta, p[i], z[i]);
+}
+
+__global__ void __launch_bounds__(256) k_cg_pupdate32(int n, const float *__restrict__ z,
+                                                      float *__restrict__ p,
+                                                      const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  p[i] = ctl->first ? z[i] : fmaf((float)ctl->beta, p[i], z[i]);
+}
+
+// x += alpha*p ; d -= alpha*q ; max|alpha p|, max|d|, sum d^2 (FP64 path).
+// partial slots: [0]=l2, [1]=dx val, [2]=dx idx, [3]=r val, [4]=r idx, [5]=nonfinite
+__global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__restrict__ x,
+                                                            double *__restrict__ d,
+                                                            const double *__restrict__ p,
+                                                            const double *__restrict__ q,
+                                                            double *__restrict__ part,
+                                                            const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  const double alpha = ctl->alpha;
+  double v[2] = {0.0, 0.0};
+  MaxLoc m[2];
+  m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double tv = alpha * p[i];
+    x[i] = x[i] + tv;
+    if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i; }
+    double di = fma(-alpha, q[i], d[i]);
+    d[i] = di;
+    if (absgt(di, m[1].val)) { m[1].val = di; m[1].idx = i; }
+    v[0] = fma(di, di, v[0]);
+    if (!isfinite(di) || !isfinite(tv)) v[1] += 1.0;
+  }
+  block_sum<2>(v);
+  block_maxloc<2>(m);
+  if (threadIdx.x == 0) {
+    int G = gridDim.x, b = blockIdx.x;
+    part[b] = v[0];
+    part[G + b] = m[0].val; part[2 * G + b] = (double)m[0].idx;
+    part[3 * G + b] = m[1].val; part[4 * G + b] = (double)m[1].idx;
+    part[5 * G + b] = v[1];
+  }
+}
+
+// Mixed inner update: x (FP64) += alpha*p (FP32 promoted); d32 -= alpha*q32.
+__global__ void __launch_bounds__(kRedBlock) k_cg_update_mixed(int n, double *__restrict__ x,
+                                                                float *__restrict__ d,
+                                                                const float *__restrict__ p,
+                                                                const float *__restrict__ q,
+                                                                double *__restrict__ part,
+                                                                const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  const double alpha = ctl->alpha;
+  const float alphaf = (float)alpha;
+  double v[2] = {0.0, 0.0};
+  MaxLoc m[2];
+  m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double tv = alpha * (double)p[i];
+    x[i] = x[i] + tv;
+    if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i; }
+    float di = fmaf(-alphaf, q[i], d[i]);
+    d[i] = di;
+    double dd = (double)di;
+    if (absgt(dd, m[1].val)) { m[1].val = dd; m[1].idx = i; }
+    v[0] = fma(dd, dd, v[0]);
+    if (!isfinite(di) || !isfinite(tv)) v[1] += 1.0;
+  }
+  block_sum<2>(v);
+  block_maxloc<2>(m);
+  if (threadIdx.x == 0) {
+    int G = gridDim.x, b = blockIdx.x;
+    part[b] = v[0];
+    part[G + b] = m[0].val; part[2 * G + b] = (double)m[0].idx;
+    part[3 * G + b] = m[1].val; part[4 * G + b] = (double)m[1].idx;
+    part[5 * G + b] = v[1];
+  }
+}
+
+// Finalise an update reduction into ctl (deltax, rmax, l2norm, nonfinite).
+__device__ void ctl_finish_update(Ctl *ctl, const double *part, int G) {
+  double l2 = ctl_reduce_sum(part, G);
+  MaxLoc dx = ctl_reduce_maxloc(part + G, part + 2 * G, G);
+  MaxLoc rm = ctl_reduce_maxloc(part + 3 * G, part + 4 * G, G);
+  double nf = ctl_reduce_sum(part + 5 * G, G);
+  if (threadIdx.x == 0) {
+    ctl->l2norm = sqrt(l2);
+    ctl->deltax = dx.val;
+    ctl->xloc = dx.idx;
+    ctl->rmax = rm.val;
+    ctl->rloc = rm.idx;
+    if (nf != 0.0) ctl->nonfinite = 1;
+  }
+}
+
+// End of a PCG iteration: closure test and loop control (ImsLinearBase.f90:196-236).
+__global__ void k_ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond,
+                              int use_cond) {
+  if (ctl->done) {
+    if (threadIdx.x == 0) set_loop(ctl, cond, use_cond);
+    return;
+  }
+  ctl_finish_update(ctl, part, G);
+  if (threadIdx.x != 0) return;
+  double rcnvg = (ctl->icnvgopt == 2 || ctl->icnvgopt == 3 || ctl->icnvgopt == 4) ? ctl->l2norm
+                                                                                : ctl->rmax;
+  int icnvg = ctl->icnvg;
+  d_testcnvg(ctl->icnvgopt, icnvg, ctl->iter, ctl->deltax, rcnvg, ctl->l2norm0, ctl->epfact,
+             ctl->dvclose, ctl->rclose);
+  if (rcnvg == 0.0) icnvg = 1;
+  ctl->icnvg = icnvg;
+  ctl->north_due = 0;
+  if (ctl->nonfinite) {
+    ctl->done = 1;
+  } else if (icnvg != 0) {
+    ctl->done = 1;
+    ctl->exit_reason = (rcnvg == 0.0) ? kExitExact : kExitClosure;
+  } else if (d_is_close(ctl->rho, ctl->rho0)) {
+    ctl->done = 1;
+    ctl->exit_reason = kExitStagnation;
+  } else {
+    if (ctl->north > 0 && ((ctl->iter + 1) % ctl->north) == 0) ctl->north_due = 1;
+    if (ctl->rho == 0.0) {
+      ctl->done = 1;
+      ctl->exit_reason = kExitZeroRho;
+    } else {
+      ctl->rho0 = ctl->rho;
+      if (ctl->iter >= ctl->itmax) {
+        ctl->done = 1;
+        ctl->exit_reason = kExitItmax;
+      } else {
+        ctl->iter += 1;
+        ctl->first = 0;
+      }
+    }
+  }
+  if (ctl->done && ctl->icnvg < 0) ctl->icnvg = 0;
+  set_loop(ctl, cond, use_cond);
+}
+
+// ---------------------------------------------------------------------------
+// BiCGSTAB
+// ---------------------------------------------------------------------------
+__global__ void k_ctl_bcgs_rho(Ctl *ctl, const double *part, int G) {
+  if (ctl->done) return;
+  double s = ctl_reduce_sum(part, G);
+  if (threadIdx.x == 0) {
+    ctl->rho = s;
+    if (!ctl->first) ctl->beta = (s / ctl->rho0) * (ctl->alpha0 / ctl->omega0);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_bcgs_p(int n, const T *__restrict__ d, T *__restrict__ p,
+                                                const T *__restrict__ v,
+                                                const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (ctl->first) {
+    p[i] = d[i];
+  } else {
+    T beta = (T)ctl->beta, om = (T)ctl->omega0;
+    T inner = fma(-om, v[i], p[i]);
+    p[i] = fma(beta, inner, d[i]);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_bcgs_q(int n, const T *__restrict__ d, const T *__restrict__ v,
+                                                T *__restrict__ q, const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  q[i] = fma(-(T)ctl->alpha, v[i], d[i]);
+}
+
+__global__ void k_ctl_omega(Ctl *ctl, const double *part, int G) {
+  if (ctl->done) return;
+  double num = ctl_reduce_sum(part, G);
+  double den = ctl_reduce_sum(part + G, G);
+  if (threadIdx.x == 0) {
+    den = den + sign_dprec(den);
+    ctl->omega = num / den;
+  }
+}
+
+// x += alpha*phat + omega*qhat ; d = q - omega*t (ImsLinearBase.f90:428-480).
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_bcgs_update(int n, double *__restrict__ x,
+                                                            T *__restrict__ d,
+                                                            const T *__restrict__ phat,
+                                                            const T *__restrict__ qhat,
+                                                            const T *__restrict__ q,
+                                                            const T *__restrict__ t,
+                                                            const double *__restrict__ dscale,
+                                                            double *__restrict__ part,
+                                                            const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  const double alpha = ctl->alpha, omega = ctl->omega;
+  const T omegat = (T)omega;
+  double v[2] = {0.0, 0.0};
+  MaxLoc m[2];
+  m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double tv = fma(alpha, to_d(phat[i]), omega * to_d(qhat[i]));
+    x[i] = x[i] + tv;
+    if (dscale) tv = tv * dscale[i];
+    if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i; }
+    T di = fma(-omegat, t[i], q[i]);
+    d[i] = di;
+    double rv = to_d(di);
+    if (dscale) rv = rv / dscale[i];
+    if (absgt(rv, m[1].val)) { m[1].val = rv; m[1].idx = i; }
+    v[0] = fma(rv, rv, v[0]);
+    if (!isfinite(rv) || !isfinite(tv)) v[1] += 1.0;
+  }
+  block_sum<2>(v);
+  block_maxloc<2>(m);
+  if (threadIdx.x == 0) {
+    int G = gridDim.x, b = blockIdx.x;
+    part[b] = v[0];
+    part[G + b] = m[0].val; part[2 * G + b] = (double)m[0].idx;
+    part[3 * G + b] = m[1].val; part[4 * G + b] = (double)m[1].idx;
+    part[5 * G + b] = v[1];
+  }
+}
+
+// End of a BiCGSTAB iteration (ImsLinearBase.f90:498-545).
+__global__ void k_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond,
+                                int use_cond) {
+  if (ctl->done) {
+    if (threadIdx.x == 0) set_loop(ctl, cond, use_cond);
+    return;
+  }
+  ctl_finish_update(ctl, part, G);
+  if (threadIdx.x != 0) return;
+  double rcnvg = (ctl->icnvgopt == 2 || ctl->icnvgopt == 3 || ctl->icnvgopt == 4) ? ctl->l2norm
+                                                                                : ctl->rmax;
+  int icnvg = ctl->icnvg;
+  d_testcnvg(ctl->icnvgopt, icnvg, ctl->iter, ctl->deltax, rcnvg, ctl->l2norm0, ctl->epfact,
+             ctl->dvclose, ctl->rclose);
+  if (rcnvg == 0.0) icnvg = 1;
+  ctl->icnvg = icnvg;
+  ctl->north_due = 0;
+  if (ctl->nonfinite) {
+    ctl->done = 1;
+  } else if (icnvg != 0) {
+    ctl->done = 1;
+    ctl->exit_reason = (rcnvg == 0.0) ? kExitExact : kExitClosure;
+  } else if (d_is_close(ctl->rho, ctl->rho0) || d_is_close(ctl->alpha, ctl->alpha0) ||
+             d_is_close(ctl->omega, ctl->omega0)) {
+    ctl->done = 1;
+    ctl->exit_reason = kExitStagnation;
+  } else {
+    if (ctl->north > 0 && ((ctl->iter + 1) % ctl->north) == 0) ctl->north_due = 1;
+    if (ctl->rho * ctl->omega == 0.0) {
+      ctl->done = 1;
+      ctl->exit_reason = kExitZeroRho;
+    } else {
+      ctl->rho0 = ctl->rho;
+      ctl->alpha0 = ctl->alpha;
+      ctl->omega0 = ctl->omega;
+      if (ctl->iter >= ctl->itmax) {
+        ctl->done = 1;
+        ctl->exit_reason = kExitItmax;
+      } else {
+        ctl->iter += 1;
+        ctl->first = 0;
+      }
+    }
+  }
+  if (ctl->done && ctl->icnvg < 0) ctl->icnvg = 0;
+  set_loop(ctl, cond, use_cond);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: FP64 iterative refinement around the FP32 inner loop
+// ---------------------------------------------------------------------------
+
+// End of a mixed inner iteration.  The IMS test runs on the recursive FP32
+// residual; when it passes, or the recursive residual has dropped by
+// refine_factor since the last refinement, the next true-residual check is
+// requested (Ctl::north_due = 2) instead of stopping.
+__global__ void k_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
+                                  double refine_factor) {
+  if (ctl->done) return;
+  ctl_finish_update(ctl, part, G);
+  if (threadIdx.x != 0) return;
+  double rcnvg = (ctl->icnvgopt == 2 || ctl->icnvgopt == 3 || ctl->icnvgopt == 4) ? ctl->l2norm
+                                                                                : ctl->rmax;
+  int icnvg = 0;
+  d_testcnvg(ctl->icnvgopt, icnvg, ctl->iter, ctl->deltax, rcnvg, ctl->l2norm0, ctl->epfact,
+             ctl->dvclose, ctl->rclose);
+  if (rcnvg == 0.0) icnvg = 1;
+  ctl->north_due = 0;
+  // scratch[0]: L2 norm of the residual at the start of this refinement
+  bool stag = d_is_close(ctl->rho, ctl->rho0);
+  if (bcgs) stag = stag || d_is_close(ctl->alpha, ctl->alpha0) || d_is_close(ctl->omega, ctl->omega0);
+  bool zero = bcgs ? (ctl->rho * ctl->omega == 0.0) : (ctl->rho == 0.0);
+  if (ctl->nonfinite) {
+    ctl->done = 1;
+    return;
+  }
+  if (icnvg != 0 || ctl->l2norm <= refine_factor * ctl->scratch[0] || stag || zero) {
+    ctl->north_due = 2;  // request the FP64 true residual
+    ctl->scratch[1] = ctl->deltax;
+    ctl->scratch[2] = (double)ctl->xloc;
+  }
+  ctl->rho0 = ctl->rho;
+  ctl->alpha0 = ctl->alpha;
+  ctl->omega0 = ctl->omega;
+  if (ctl->north_due != 2) {
+    if (ctl->iter >= ctl->itmax) {
+      ctl->north_due = 2;  // final true-residual check at the iteration limit
+      ctl->scratch[1] = ctl->deltax;
+      ctl->scratch[2] = (double)ctl->xloc;
+    } else {
+      ctl->iter += 1;
+      ctl->first = 0;
+    }
+  }
+}
+
+// True residual r = b - A x in FP64 with its max|r| and L2, only when
+// requested; the FP32 residual is reset from it.
+__global__ void __launch_bounds__(kRedBlock) k_true_resid_stats(int n, const double *__restrict__ r,
+                                                                 float *__restrict__ d32,
+                                                                 float *__restrict__ dhat32,
+                                                                 double *__restrict__ part,
+                                                                 const Ctl *__restrict__ ctl) {
+  if (ctl->done || ctl->north_due != 2) return;
+  double v[2] = {0.0, 0.0};
+  MaxLoc m[2];
+  m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double ri = r[i];
+    d32[i] = (float)ri;
+    if (dhat32) dhat32[i] = (float)ri;  // BiCGSTAB shadow residual restarts too
+    if (absgt(ri, m[1].val)) { m[1].val = ri; m[1].idx = i; }
+    v[0] = fma(ri, ri, v[0]);
+    if (!isfinite(ri)) v[1] += 1.0;
+  }
+  block_sum<2>(v);
+  block_maxloc<2>(m);
+  if (threadIdx.x == 0) {
+    int G = gridDim.x, b = blockIdx.x;
+    part[b] = v[0];
+    part[G + b] = 0.0; part[2 * G + b] = -1.0;
+    part[3 * G + b] = m[1].val; part[4 * G + b] = (double)m[1].idx;
+    part[5 * G + b] = v[1];
+  }
+}
+
+// Closure test on the FP64 true residual; restart the inner loop if needed.
+__global__ void k_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond,
+                             int use_cond) {
+  if (ctl->done || ctl->north_due != 2) {
+    if (threadIdx.x == 0) set_loop(ctl, cond, use_cond);
+    return;
+  }
+  double dsave = ctl->scratch[1];
+  long long lsave = (long long)ctl->scratch[2];
+  ctl_finish_update(ctl, part, G);
+  if (threadIdx.x != 0) return;
+  ctl->deltax = dsave;
+  ctl->xloc = lsave;
+  double rcnvg = (ctl->icnvgopt == 2 || ctl->icnvgopt == 3 || ctl->icnvgopt == 4) ? ctl->l2norm
+                                                                                : ctl->rmax;
+  int icnvg = 0;
+  d_testcnvg(ctl->icnvgopt, icnvg, ctl->iter, ctl->deltax, rcnvg, ctl->l2norm0, ctl->epfact,
+             ctl->dvclose, ctl->rclose);
+  if (rcnvg == 0.0) icnvg = 1;
+  ctl->north_due = 0;
+  if (ctl->nonfinite) {
+    ctl->done = 1;
+  } else if (icnvg > 0) {
+    ctl->icnvg = 1;
+    ctl->done = 1;
+    ctl->exit_reason = (rcnvg == 0.0) ? kExitExact : kExitClosure;
+  } else if (ctl->iter >= ctl->itmax) {
+    ctl->icnvg = 0;
+    ctl->done = 1;
+    ctl->exit_reason = kExitItmax;
+  } else {
+    // restart the inner Krylov recurrence from the true residual
+    ctl->scratch[0] = ctl->l2norm;
+    ctl->scratch[3] += 1.0;  // refinement count
+    ctl->first = 1;
+    ctl->rho0 = 0.0;
+    ctl->alpha0 = 0.0;
+    ctl->omega0 = 0.0;
+    ctl->iter += 1;
+  }
+  set_loop(ctl, cond, use_cond);
+}
+
+// ---------------------------------------------------------------------------
+// misc elementwise kernels
+// ---------------------------------------------------------------------------
+template <typename TD, typename TS>
+__global__ void k_convert(int n, const TS *__restrict__ s, TD *__restrict__ d) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = (TD)s[i];
+}
+
+__global__ void k_ctl_set_l2norm0(Ctl *ctl, const double *part, int G) {
+  double s = ctl_reduce_sum(part, G);
+  if (threadIdx.x == 0) {
+    ctl->l2norm0 = sqrt(s);
+    ctl->scratch[0] = ctl->l2norm0;
+    if (ctl->l2norm0 == 0.0 || ctl->itmax <= 0) {
+      ctl->done = 1;
+      if (ctl->l2norm0 == 0.0) {
+        ctl->icnvg = 1;
+        ctl->exit_reason = kExitExact;
+      }
+    }
+    if (!isfinite(s)) {
+      ctl->nonfinite = 1;
+      ctl->done = 1;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host launch wrappers
+// ---------------------------------------------------------------------------
+static inline int egrid(int n) { return std::max(1, (n + 255) / 256); }
+
+void kr_dot64(int n, const double *a, const double *b, double *part, int G, const Ctl *ctl, cudaStream_t st) {
+  k_dot<double, double><<<G, kRedBlock, 0, st>>>(n, a, b, part, ctl);
+}
+void kr_dot32(int n, const float *a, const float *b, double *part, int G, const Ctl *ctl, cudaStream_t st) {
+  k_dot<float, float><<<G, kRedBlock, 0, st>>>(n, a, b, part, ctl);
+}
+void kr_dot_tq_tt64(int n, const double *t, const double *q, double *part, int G, const Ctl *ctl, cudaStream_t st) {
+  k_dot_tq_tt<double><<<G, kRedBlock, 0, st>>>(n, t, q, part, ctl);
+}
+void kr_dot_tq_tt32(int n, const float *t, const float *q, double *part, int G, const Ctl *ctl, cudaStream_t st) {
+  k_dot_tq_tt<float><<<G, kRedBlock, 0, st>>>(n, t, q, part, ctl);
+}
+void kr_sumsq64(int n, const double *a, double *part, int G, cudaStream_t st) {
+  k_sumsq<double><<<G, kRedBlock, 0, st>>>(n, a, part);
+}
+void kr_ctl_set_l2norm0(Ctl *ctl, const double *part, int G, cudaStream_t st) {
+  k_ctl_set_l2norm0<<<1, kRedBlock, 0, st>>>(ctl, part, G);
+}
+void kr_ctl_cg_rho(Ctl *ctl, const double *part, int G, cudaStream_t st) {
+  k_ctl_cg_rho<<<1, kRedBlock, 0, st>>>(ctl, part, G);
+}
+void kr_ctl_alpha(Ctl *ctl, const double *part, int G, cudaStream_t st) {
+  k_ctl_alpha<<<1, kRedBlock, 0, st>>>(ctl, part, G);
+}
+void kr_cg_pupdate64(int n, const double *z, double *p, const Ctl *ctl, cudaStream_t st) {
+  k_cg_pupdate64<<<egrid(n), 256, 0, st>>>(n, z, p, ctl);
+}
+void kr_cg_pupdate32(int n, const float *z, float *p, const Ctl *ctl, cudaStream_t st) {
+  k_cg_pupdate32<<<egrid(n), 256, 0, st>>>(n, z, p, ctl);
+}
+void kr_cg_update64(int n, double *x, double *d, const double *p, const double *q, double *part,
+                    int G, const Ctl *ctl, cudaStream_t st) {
+  k_cg_update64<<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
+}
+void kr_cg_update_mixed(int n, double *x, float *d, const float *p, const float *q, double *part,
+                        int G, const Ctl *ctl, cudaStream_t st) {
+  k_cg_update_mixed<<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
+}
+void kr_ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
+                    cudaStream_t st) {
+  k_ctl_cg_cnvg<<<1, kRedBlock, 0, st>>>(ctl, part, G, cond, use_cond);
+}
+void kr_ctl_bcgs_rho(Ctl *ctl, const double *part, int G, cudaStream_t st) {
+  k_ctl_bcgs_rho<<<1, kRedBlock, 0, st>>>(ctl, part, G);
+}
+void kr_bcgs_p64(int n, const double *d, double *p, const double *v, const Ctl *ctl, cudaStream_t st) {
+  k_bcgs_p<double><<<egrid(n), 256, 0, st>>>(n, d, p, v, ctl);
+}
+void kr_bcgs_p32(int n, const float *d, float *p, const float *v, const Ctl *ctl, cudaStream_t st) {
+  k_bcgs_p<float><<<egrid(n), 256, 0, st>>>(n, d, p, v, ctl);
+}
+void kr_bcgs_q64(int n, const double *d, const double *v, double *q, const Ctl *ctl, cudaStream_t st) {
+  k_bcgs_q<double><<<egrid(n), 256, 0, st>>>(n, d, v, q, ctl);
+}
+void kr_bcgs_q32(int n, const float *d, const float *v, float *q, const Ctl *ctl, cudaStream_t st) {
+  k_bcgs_q<float><<<egrid(n), 256, 0, st>>>(n, d, v, q, ctl);
+}
+void kr_ctl_omega(Ctl *ctl, const double *part, int G, cudaStream_t st) {
+  k_ctl_omega<<<1, kRedBlock, 0, st>>>(ctl, part, G);
+}
+void kr_bcgs_update64(int n, double *x, double *d, const double *phat, const double *qhat,
+                      const double *q, const double *t, const double *dscale, double *part, int G,
+                      const Ctl *ctl, cudaStream_t st) {
+  k_bcgs_update<double><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
+}
+void kr_bcgs_update32(int n, double *x, float *d, const float *phat, const float *qhat,
+                      const float *q, const float *t, const double *dscale, double *part, int G,
+                      const Ctl *ctl, cudaStream_t st) {
+  k_bcgs_update<float><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
+}
+void kr_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
+                      cudaStream_t st) {
+  k_ctl_bcgs_cnvg<<<1, kRedBlock, 0, st>>>(ctl, part, G, cond, use_cond);
+}
+void kr_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs, double refine_factor,
+                        cudaStream_t st) {
+  k_ctl_mixed_inner<<<1, kRedBlock, 0, st>>>(ctl, part, G, bcgs, refine_factor);
+}
+void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, double *part, int G,
+                         const Ctl *ctl, cudaStream_t st) {
+  k_true_resid_stats<<<G, kRedBlock, 0, st>>>(n, r, d32, dhat32, part, ctl);
+}
+void kr_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
+                   cudaStream_t st) {
+  k_ctl_refine<<<1, kRedBlock, 0, st>>>(ctl, part, G, cond, use_cond);
+}
+void kr_f64_to_f32(int n, const double *s, float *d, cudaStream_t st) {
+  k_convert<float, double><<<std::min(egrid(n), 4 * kNumSM), 256, 0, st>>>(n, s, d);
+}
+void kr_f32_to_f64(int n, const float *s, double *d, cudaStream_t st) {
+  k_convert<double, float><<<std::min(egrid(n), 4 * kNumSM), 256, 0, st>>>(n, s, d);
+}
+
+}  // namespace gb

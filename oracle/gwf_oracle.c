@@ -1,0 +1,768 @@
+/*
+ * gwf_oracle.c -- CPU restatement of the MODFLOW 6 GWF assembly and the
+ * NumericalSolution outer loop around IMS, for a single DIS model with the
+ * NPF, STO, CHD, WEL and RCH packages.
+ *
+ * TEST INFRASTRUCTURE ONLY (the oracle).  The product never links this file.
+ *
+ * Summation order follows the Fortran exactly (add_value_pos sequences), so
+ * with -ffp-contract=off the assembled matrix is bit-for-bit the reference's.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <float.h>
+
+#include "gwf_oracle.h"
+
+#define DEM6 1.0e-6
+#define DEM15 1.0e-15
+#define DEM20 1.0e-20
+#define DP9 0.9
+#define DPREC DBL_EPSILON
+
+/* ------------------------------------------------------------------------ */
+/* Grid connectivity                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* Connections.f90:463-698 (disconnections, full grid, no IDOMAIN) plus
+ * Sparse.f90:217-239 (diagonal first, remaining columns ascending) and
+ * fillisym/filljas (Connections.f90:1205-1268).  Node numbering follows
+ * GeomUtil.f90:82-95 (column fastest, then row, then layer), 0-based.
+ * Arrays must be sized by or_dis_sizes(). */
+void or_dis_sizes(int nlay, int nrow, int ncol, int *nodes, int *nja, int *njas) {
+  long long n = (long long)nlay * nrow * ncol;
+  long long nh = (long long)nlay * nrow * (ncol - 1) + (long long)nlay * (nrow - 1) * ncol;
+  long long nv = (long long)(nlay - 1) * nrow * ncol;
+  *nodes = (int)n;
+  *njas = (int)(nh + nv);
+  *nja = (int)(n + 2 * (nh + nv));
+}
+
+void or_dis_connect(int nlay, int nrow, int ncol, const double *delr, const double *delc,
+                    const double *top, const double *bot, int *ia, int *ja, int *isym,
+                    int *jas, int *ihc, double *cl1, double *cl2, double *hwva) {
+  int nrc = nrow * ncol;
+  int pos = 0;
+  for (int k = 0; k < nlay; ++k)
+    for (int i = 0; i < nrow; ++i)
+      for (int j = 0; j < ncol; ++j) {
+        int n = j + i * ncol + k * nrc;
+        ia[n] = pos;
+        ja[pos++] = n; /* diagonal first */
+        if (k > 0) ja[pos++] = n - nrc;
+        if (i > 0) ja[pos++] = n - ncol;
+        if (j > 0) ja[pos++] = n - 1;
+        if (j < ncol - 1) ja[pos++] = n + 1;
+        if (i < nrow - 1) ja[pos++] = n + ncol;
+        if (k < nlay - 1) ja[pos++] = n + nrc;
+      }
+  int nodes = nlay * nrc;
+  ia[nodes] = pos;
+  /* fillisym */
+  for (int n = 0; n < nodes; ++n)
+    for (int ii = ia[n]; ii < ia[n + 1]; ++ii) {
+      int m = ja[ii];
+      if (m != n) {
+        isym[ii] = -1;
+        for (int jj = ia[m]; jj < ia[m + 1]; ++jj)
+          if (ja[jj] == n) {
+            isym[ii] = jj;
+            break;
+          }
+      } else {
+        isym[ii] = ii;
+      }
+    }
+  /* filljas: 0-based symmetric index, -1 on the diagonal */
+  int ipos = 0;
+  for (int n = 0; n < nodes; ++n) {
+    jas[ia[n]] = -1;
+    for (int ii = ia[n] + 1; ii < ia[n + 1]; ++ii)
+      if (ja[ii] > n) jas[ii] = ipos++;
+  }
+  for (int n = 0; n < nodes; ++n)
+    for (int ii = ia[n]; ii < ia[n + 1]; ++ii)
+      if (ja[ii] < n) jas[ii] = jas[isym[ii]];
+  /* symmetric geometry arrays in (right, front, down) order per node */
+  int isympos = 0;
+  for (int k = 0; k < nlay; ++k)
+    for (int i = 0; i < nrow; ++i)
+      for (int j = 0; j < ncol; ++j) {
+        int nr = j + i * ncol + k * nrc;
+        if (j < ncol - 1) {
+          ihc[isympos] = 1;
+          cl1[isympos] = 0.5 * delr[j];
+          cl2[isympos] = 0.5 * delr[j + 1];
+          hwva[isympos] = delc[i];
+          isympos++;
+        }
+        if (i < nrow - 1) {
+          ihc[isympos] = 1;
+          cl1[isympos] = 0.5 * delc[i];
+          cl2[isympos] = 0.5 * delc[i + 1];
+          hwva[isympos] = delr[j];
+          isympos++;
+        }
+        if (k < nlay - 1) {
+          int mr = nr + nrc;
+          ihc[isympos] = 0;
+          cl1[isympos] = 0.5 * (top[nr] - bot[nr]);
+          cl2[isympos] = 0.5 * (top[mr] - bot[mr]);
+          hwva[isympos] = delr[j] * delc[i];
+          isympos++;
+        }
+      }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Conductance utilities                                                     */
+/* ------------------------------------------------------------------------ */
+
+/* GwfConductanceUtils.f90:226-284, condmean (harmonic, CCOND_HMEAN, and the
+ * logarithmic/arithmetic variants). */
+static double logmean(double d1, double d2) {
+  double drat = d2 / d1;
+  if (drat <= 0.995 || drat >= 1.005) return (d2 - d1) / log(drat);
+  return 0.5 * (d1 + d2);
+}
+
+static double condmean(double k1, double k2, double thick1, double thick2, double cl1,
+                       double cl2, double width, int iavgmeth) {
+  double t1 = k1 * thick1;
+  double t2 = k2 * thick2;
+  switch (iavgmeth) {
+  case 0:
+    if (t1 * t2 > 0.0) return width * t1 * t2 / (t1 * cl2 + t2 * cl1);
+    return 0.0;
+  case 1: {
+    double tmean = (t1 * t2 > 0.0) ? logmean(t1, t2) : 0.0;
+    return tmean * width / (cl1 + cl2);
+  }
+  case 2: {
+    double kmean = (k1 * k2 > 0.0) ? logmean(k1, k2) : 0.0;
+    return kmean * 0.5 * (thick1 + thick2) * width / (cl1 + cl2);
+  }
+  default: {
+    double denom = (k1 * cl2 + k2 * cl1);
+    double kmean = (denom > 0.0) ? k1 * k2 / denom : 0.0;
+    return kmean * 0.5 * (thick1 + thick2) * width;
+  }
+  }
+}
+
+/* GwfConductanceUtils.f90:43-145, hcond (ihc 1 only; no staggered). */
+static double hcond(int ibdn, int ibdm, int ictn, int ictm, int iupstream, int icellavg,
+                    double condsat, double hn, double hm, double satn, double satm,
+                    double hkn, double hkm, double topn, double topm, double botn,
+                    double botm, double cln, double clm, double fawidth) {
+  if (ibdn == 0 || ibdm == 0) return 0.0;
+  if (ictn == 0 && ictm == 0) return condsat;
+  if (iupstream == 1) {
+    double sat_up = (hn > hm) ? satn : satm;
+    return sat_up * condsat;
+  }
+  double thksatn = satn * (topn - botn);
+  double thksatm = satm * (topm - botm);
+  return condmean(hkn, hkm, thksatn, thksatm, cln, clm, fawidth, icellavg);
+}
+
+/* GwfConductanceUtils.f90:149-222, vcond. */
+static double vcond(int ibdn, int ibdm, int ictn, int ictm, int ivarcv, int idewatcv,
+                    double condsat, double hn, double hm, double vkn, double vkm,
+                    double satn, double satm, double topn, double topm, double botn,
+                    double botm, double flowarea) {
+  if (ibdn == 0 || ibdm == 0) return 0.0;
+  if (ivarcv == 0) return condsat;
+  if (ictn == 0 && ictm == 0) return condsat;
+  if (hn >= topn && hm >= topm) return condsat;
+  double satntmp = satn, satmtmp = satm;
+  if (idewatcv == 0) {
+    if (botn > botm) satmtmp = 1.0;
+    else satntmp = 1.0;
+  }
+  double bovk1 = satntmp * (topn - botn) * 0.5 / vkn;
+  double bovk2 = satmtmp * (topm - botm) * 0.5 / vkm;
+  double denom = (bovk1 + bovk2);
+  if (denom != 0.0) return flowarea / denom;
+  return 0.0;
+}
+
+/* SmoothingFunctions.f90:275-324, sQuadraticSaturation. */
+double or_squadratic_sat(double top, double bot, double x, double eps) {
+  double teps = eps;
+  double b = top - bot;
+  double y;
+  if (b > 0.0) {
+    double br;
+    if (x < bot) br = 0.0;
+    else if (x > top) br = 1.0;
+    else br = (x - bot) / b;
+    double av = 1.0 / (1.0 - teps);
+    double bri = 1.0 - br;
+    if (br < teps) y = av * 0.5 * (br * br) / teps;
+    else if (br < (1.0 - teps)) y = av * br + 0.5 * (1.0 - av);
+    else if (br < 1.0) y = 1.0 - ((av * 0.5 * (bri * bri)) / teps);
+    else y = 1.0;
+  } else {
+    y = (x < bot) ? 0.0 : 1.0;
+  }
+  return y;
+}
+
+/* SmoothingFunctions.f90:364-406, sQuadraticSaturationDerivative. */
+double or_squadratic_sat_derv(double top, double bot, double x, double eps) {
+  double teps = eps;
+  double b = top - bot;
+  double br;
+  if (x < bot) br = 0.0;
+  else if (x > top) br = 1.0;
+  else br = (x - bot) / b;
+  double av = 1.0 / (1.0 - teps);
+  double bri = 1.0 - br;
+  double y;
+  if (br < teps) y = av * br / teps;
+  else if (br < (1.0 - teps)) y = av;
+  else if (br < 1.0) y = av * bri / teps;
+  else y = 0.0;
+  return y / b;
+}
+
+/* ------------------------------------------------------------------------ */
+/* NPF                                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* gwf-npf.f90:1950-2044, calc_condsat(node, upperOnly=.true.) for every node,
+ * with the default initial saturation of one (no THICKSTRT). */
+void or_npf_condsat(const or_gwf_model *m, double *condsat) {
+  for (int n = 0; n < m->nodes; ++n) {
+    for (int ii = m->ia[n] + 1; ii < m->ia[n + 1]; ++ii) {
+      int mm = m->ja[ii];
+      if (mm < n) continue;
+      int jj = m->jas[ii];
+      int ihc = m->ihc[jj];
+      double csat;
+      if (ihc == 0) {
+        double hyn = m->k33[n], hym = m->k33[mm];
+        csat = vcond(1, 1, 1, 1, 1, 1, 1.0, m->bot[n], m->bot[mm], hyn, hym, 1.0, 1.0,
+                     m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->hwva[jj]);
+      } else {
+        double hyn = m->k11[n], hym = m->k11[mm];
+        csat = hcond(1, 1, 1, 1, 0, m->icellavg, 1.0, m->top[n], m->top[mm], 1.0, 1.0,
+                     hyn, hym, m->top[n], m->top[mm], m->bot[n], m->bot[mm],
+                     m->cl1[jj], m->cl2[jj], m->hwva[jj]);
+      }
+      condsat[jj] = csat;
+    }
+  }
+}
+
+/* gwf-npf.f90:444-470 (npf_cf) and 775-794 (thksat). */
+void or_npf_cf(const or_gwf_model *m, const int *ibound, const double *hnew, double *sat) {
+  for (int n = 0; n < m->nodes; ++n) {
+    if (m->icelltype[n] != 0) {
+      double satn;
+      if (ibound[n] == 0) {
+        satn = 0.0;
+      } else {
+        if (hnew[n] >= m->top[n]) satn = 1.0;
+        else satn = (hnew[n] - m->bot[n]) / (m->top[n] - m->bot[n]);
+        if (m->inewton != 0)
+          satn = or_squadratic_sat(m->top[n], m->bot[n], hnew[n], m->satomega);
+      }
+      sat[n] = satn;
+    }
+  }
+}
+
+/* gwf-npf.f90:474-574, npf_fc (no XT3D, no perched). */
+void or_npf_fc(const or_gwf_model *m, const int *ibound, const double *condsat,
+               const double *sat, const double *hnew, double *amat, double *rhs) {
+  (void)rhs;
+  for (int n = 0; n < m->nodes; ++n) {
+    for (int ii = m->ia[n] + 1; ii < m->ia[n + 1]; ++ii) {
+      int mm = m->ja[ii];
+      if (mm < n) continue;
+      int jj = m->jas[ii];
+      int ihc = m->ihc[jj];
+      double cond;
+      if (ihc == 0) {
+        cond = vcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm],
+                     m->ivarcv, m->idewatcv, condsat[jj], hnew[n], hnew[mm], m->k33[n],
+                     m->k33[mm], sat[n], sat[mm], m->top[n], m->top[mm], m->bot[n],
+                     m->bot[mm], m->hwva[jj]);
+      } else {
+        cond = hcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm],
+                     m->inewton, m->icellavg, condsat[jj], hnew[n], hnew[mm], sat[n],
+                     sat[mm], m->k11[n], m->k11[mm], m->top[n], m->top[mm], m->bot[n],
+                     m->bot[mm], m->cl1[jj], m->cl2[jj], m->hwva[jj]);
+      }
+      int idiag = m->ia[n];
+      amat[ii] = amat[ii] + cond;
+      amat[idiag] = amat[idiag] + (-cond);
+      int isymcon = m->isym[ii];
+      int idiagm = m->ia[mm];
+      amat[isymcon] = amat[isymcon] + cond;
+      amat[idiagm] = amat[idiagm] + (-cond);
+    }
+  }
+}
+
+/* gwf-npf.f90:578-698, npf_fn (no XT3D).  The get/set pairs of the Fortran
+ * that store a value back unchanged are no-ops and are omitted. */
+void or_npf_fn(const or_gwf_model *m, const int *ibound, const double *condsat,
+               const double *hnew, double *amat, double *rhs) {
+  for (int n = 0; n < m->nodes; ++n) {
+    int idiag = m->ia[n];
+    for (int ii = m->ia[n] + 1; ii < m->ia[n + 1]; ++ii) {
+      int mm = m->ja[ii];
+      int isymcon = m->isym[ii];
+      if (mm < n) continue;
+      int jj = m->jas[ii];
+      if (m->ihc[jj] == 0 && m->ivarcv == 0) continue;
+      int iups = (hnew[mm] < hnew[n]) ? n : mm;
+      int idn = (iups == n) ? mm : n;
+      if (m->icelltype[iups] == 0) continue;
+      double topup = m->top[iups];
+      double botup = m->bot[iups];
+      double cond = condsat[jj];
+      double consterm = -cond * (hnew[iups] - hnew[idn]);
+      double derv = or_squadratic_sat_derv(topup, botup, hnew[iups], m->satomega);
+      int idiagm = m->ia[mm];
+      if (iups == n) {
+        double term = consterm * derv;
+        rhs[n] = rhs[n] + term * hnew[n];
+        rhs[mm] = rhs[mm] - term * hnew[n];
+        amat[idiag] = amat[idiag] + term;
+        if (ibound[mm] > 0) amat[isymcon] = amat[isymcon] + (-term);
+      } else {
+        double term = -consterm * derv;
+        rhs[n] = rhs[n] + term * hnew[mm];
+        rhs[mm] = rhs[mm] - term * hnew[mm];
+        if (ibound[n] > 0) amat[ii] = amat[ii] + term;
+        amat[idiagm] = amat[idiagm] + (-term);
+      }
+    }
+  }
+}
+
+/* gwf-npf.f90:705-741, npf_nur. */
+void or_npf_nur(const or_gwf_model *m, const int *ibound, double *x, const double *xtemp,
+                double *dx, int *inewtonur, double *dxmax, int *locmax) {
+  int nrc = m->nrow * m->ncol;
+  for (int n = 0; n < m->nodes; ++n) {
+    if (ibound[n] < 1) continue;
+    if (m->icelltype[n] > 0) {
+      int ibot = (m->nlay - 1) * nrc + (n % nrc); /* ibotnode: bottom cell in column */
+      double botm = m->bot[ibot];
+      if (x[n] < botm) {
+        *inewtonur = 1;
+        double xx = xtemp[n] * (1.0 - DP9) + botm * DP9;
+        double dxx = x[n] - xx;
+        if (fabs(dxx) > fabs(*dxmax)) {
+          *locmax = n;
+          *dxmax = dxx;
+        }
+        x[n] = xx;
+        dx[n] = 0.0;
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* STO and boundary packages                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* gwf-sto.f90:226-345 (sto_fc) with GwfStorageUtils.f90 SsTerms/SyTerms/
+ * SsCapacity/SyCapacity; istor_coef=0, iorig_ss=0, iconf_ss=0, no TVS. */
+void or_sto_fc(const or_gwf_model *m, const int *ibound, double delt, const double *hold,
+               const double *hnew, double *amat, double *rhs) {
+  double tled = 1.0 / delt;
+  for (int n = 0; n < m->nodes; ++n) {
+    int idiag = m->ia[n];
+    if (ibound[n] < 1) continue;
+    double tp = m->top[n], bt = m->bot[n];
+    int iconvert = m->iconvert[n];
+    double snold, snnew;
+    if (iconvert == 0) {
+      snold = 1.0;
+      snnew = 1.0;
+    } else {
+      snold = or_squadratic_sat(tp, bt, hold[n], m->satomega);
+      snnew = or_squadratic_sat(tp, bt, hnew[n], m->satomega);
+    }
+    double sc1 = m->ss[n] * (tp - bt) * m->area[n];
+    double rho1 = sc1 * tled;
+    double rho1old = rho1;
+    /* SsTerms */
+    double aterm = -rho1 * snnew;
+    double rhsterm;
+    if (iconvert != 0) {
+      double tthk = tp - bt;
+      double zold = bt + 0.5 * tthk * snold;
+      double znew = bt + 0.5 * tthk * snnew;
+      rhsterm = -rho1old * snold * (hold[n] - zold) - rho1 * snnew * znew;
+    } else {
+      rhsterm = -rho1old * snold * hold[n];
+    }
+    amat[idiag] = amat[idiag] + aterm;
+    rhs[n] = rhs[n] + rhsterm;
+    if (iconvert != 0) {
+      double sc2 = m->sy[n] * m->area[n];
+      double rho2 = sc2 * tled;
+      double rho2old = rho2;
+      double tthk = tp - bt;
+      aterm = 0.0;
+      if (snnew < 1.0) {
+        if (snnew > 0.0) {
+          aterm = -rho2;
+          rhsterm = -rho2old * tthk * snold - rho2 * bt;
+        } else {
+          rhsterm = tthk * (0.0 - rho2old * snold);
+        }
+      } else {
+        rhsterm = tthk * (rho2 * snnew - rho2old * snold);
+      }
+      amat[idiag] = amat[idiag] + aterm;
+      rhs[n] = rhs[n] + rhsterm;
+    }
+  }
+}
+
+/* gwf-sto.f90:353-439, sto_fn (the saturation here uses the default omega
+ * of the smoothing function, as in the Fortran call without eps). */
+void or_sto_fn(const or_gwf_model *m, const int *ibound, double delt, const double *hnew,
+               double *amat, double *rhs) {
+  double tled = 1.0 / delt;
+  for (int n = 0; n < m->nodes; ++n) {
+    int idiag = m->ia[n];
+    if (ibound[n] <= 0) continue;
+    double tp = m->top[n], bt = m->bot[n];
+    double tthk = tp - bt;
+    double h = hnew[n];
+    double snnew = or_squadratic_sat(tp, bt, h, DEM6);
+    double sc1 = m->ss[n] * (tp - bt) * m->area[n];
+    double sc2 = m->sy[n] * m->area[n];
+    double rho1 = sc1 * tled;
+    double rho2 = sc2 * tled;
+    if (m->iconvert[n] != 0) {
+      double derv = or_squadratic_sat_derv(tp, bt, h, DEM6);
+      double drterm = -rho1 * derv * (h - bt) + rho1 * tthk * snnew * derv;
+      amat[idiag] = amat[idiag] + drterm;
+      rhs[n] = rhs[n] + drterm * h;
+      if (snnew < 1.0) {
+        if (snnew > 0.0) {
+          double rterm = -rho2 * tthk * snnew;
+          drterm = -rho2 * tthk * derv;
+          amat[idiag] = amat[idiag] + (drterm + rho2);
+          rhs[n] = rhs[n] - rterm + drterm * h + rho2 * bt;
+        }
+      }
+    }
+  }
+}
+
+/* gwf-wel.f90:296-332 (wel_cf without AUTO_FLOW_REDUCE) and
+ * gwf-rch.f90:303-353 (rch_cf, recharge on the listed cell), each followed by
+ * BoundaryPackage.f90:453-472 (bnd_fc: rhs += rhs_i, diag += hcof_i = 0). */
+void or_bnd_fc(const or_gwf_model *m, const int *ibound, double *amat, double *rhs) {
+  for (int i = 0; i < m->nwel; ++i) {
+    int node = m->wel_node[i];
+    double r = (ibound[node] <= 0) ? 0.0 : -m->wel_q[i];
+    rhs[node] = rhs[node] + r;
+    amat[m->ia[node]] = amat[m->ia[node]] + 0.0;
+  }
+  for (int i = 0; i < m->nrch; ++i) {
+    int node = m->rch_node[i];
+    double r = -m->rch_rate[i] * m->area[node];
+    if (ibound[node] <= 0) r = 0.0;
+    rhs[node] = rhs[node] + r;
+    amat[m->ia[node]] = amat[m->ia[node]] + 0.0;
+  }
+}
+
+/* gwf.f90:466-555, gwf_fc order for the packages restated here:
+ * NPF fc, STO fc, BND fc, then NPF fn, STO fn.  amat and rhs must be zero on
+ * entry (NumericalSolution sln_reset). */
+void or_gwf_fc(const or_gwf_model *m, const int *ibound, const double *condsat,
+               double *sat, double delt, int transient, const double *hold,
+               const double *hnew, double *amat, double *rhs) {
+  or_npf_cf(m, ibound, hnew, sat);
+  or_npf_fc(m, ibound, condsat, sat, hnew, amat, rhs);
+  if (transient) or_sto_fc(m, ibound, delt, hold, hnew, amat, rhs);
+  or_bnd_fc(m, ibound, amat, rhs);
+  if (m->inewton) {
+    or_npf_fn(m, ibound, condsat, hnew, amat, rhs);
+    if (transient) or_sto_fn(m, ibound, delt, hnew, amat, rhs);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* NumericalSolution pieces                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* NumericalSolution.f90:2434-2478, sln_ls loose ends: small-diagonal fix,
+ * identity rows for CHD / inactive cells, and (CG) the symmetric column
+ * elimination of CHD cells. */
+void or_sln_ls_fixups(int neq, const int *ia, const int *ja, const int *active,
+                      int isymmetric, double *amat, double *rhs, const double *x,
+                      double *xtemp) {
+  for (int ieq = 0; ieq < neq; ++ieq) {
+    xtemp[ieq] = x[ieq];
+    if (active[ieq] > 0) {
+      double diagval = -1.0;
+      double adiag = fabs(amat[ia[ieq]]);
+      if (adiag < DEM15) {
+        amat[ia[ieq]] = diagval;
+        rhs[ieq] = rhs[ieq] + diagval * x[ieq];
+      }
+    } else {
+      amat[ia[ieq]] = 1.0;
+      for (int ipos = ia[ieq] + 1; ipos < ia[ieq + 1]; ++ipos) amat[ipos] = 0.0;
+      rhs[ieq] = x[ieq];
+    }
+  }
+  if (isymmetric) {
+    for (int ieq = 0; ieq < neq; ++ieq) {
+      if (active[ieq] > 0) {
+        for (int ipos = ia[ieq]; ipos < ia[ieq + 1]; ++ipos) {
+          int jcol = ja[ipos];
+          if (jcol == ieq) continue;
+          if (active[jcol] < 0) {
+            rhs[ieq] = rhs[ieq] - (amat[ipos] * x[jcol]);
+            amat[ipos] = 0.0;
+          }
+        }
+      }
+    }
+  }
+}
+
+/* NumericalSolution.f90:3122-3153, sln_get_dxmax. */
+double or_sln_get_dxmax(int neq, const int *active, const double *x, const double *xtemp,
+                        int *lrch) {
+  int nb = -1;
+  double bigch = 0.0, abigch = 0.0;
+  for (int n = 0; n < neq; ++n) {
+    if (active[n] < 1) continue;
+    double hdif = x[n] - xtemp[n];
+    double ahdif = fabs(hdif);
+    if (ahdif > abigch) {
+      bigch = hdif;
+      abigch = ahdif;
+      nb = n;
+    }
+  }
+  if (lrch) *lrch = nb;
+  return bigch;
+}
+
+/* NumericalSolution.f90:2989-3114, sln_underrelax (nonmeth 1, 2, 3). */
+void or_sln_underrelax(or_nonlinear *nl, int kiter, double bigch, int neq,
+                       const int *active, double *x, const double *xtemp) {
+  if (nl->nonmeth == 1) {
+    for (int n = 0; n < neq; ++n) {
+      if (active[n] < 1) continue;
+      double delx = x[n] - xtemp[n];
+      nl->dxold[n] = delx;
+      x[n] = xtemp[n] + nl->gamma * delx;
+    }
+  } else if (nl->nonmeth == 2) {
+    double relax;
+    nl->bigch = bigch;
+    if (kiter == 1) {
+      relax = 1.0;
+      nl->relaxold = 1.0;
+      nl->bigchold = bigch;
+    } else {
+      double es = nl->bigch / (nl->bigchold * nl->relaxold);
+      double aes = fabs(es);
+      if (es < -1.0) relax = 0.5 / aes;
+      else relax = (3.0 + es) / (3.0 + aes);
+    }
+    nl->relaxold = relax;
+    nl->bigchold = (1.0 - nl->gamma) * nl->bigch + nl->gamma * nl->bigchold;
+    if (relax < 1.0) {
+      for (int n = 0; n < neq; ++n) {
+        if (active[n] < 1) continue;
+        double delx = x[n] - xtemp[n];
+        nl->dxold[n] = delx;
+        x[n] = xtemp[n] + relax * delx;
+      }
+    }
+  } else if (nl->nonmeth == 3) {
+    for (int n = 0; n < neq; ++n) {
+      if (active[n] < 1) continue;
+      double delx = x[n] - xtemp[n];
+      if (kiter == 1) {
+        nl->wsave[n] = 1.0;
+        nl->hchold[n] = DEM20;
+        nl->deold[n] = 0.0;
+      }
+      double ww = nl->wsave[n];
+      if (nl->deold[n] * delx < 0.0) ww = nl->theta * nl->wsave[n];
+      else ww = nl->wsave[n] + nl->akappa;
+      if (ww > 1.0) ww = 1.0;
+      nl->wsave[n] = ww;
+      if (kiter == 1) nl->hchold[n] = delx;
+      else nl->hchold[n] = (1.0 - nl->gamma) * delx + nl->gamma * nl->hchold[n];
+      nl->deold[n] = delx;
+      nl->dxold[n] = delx;
+      double amom = 0.0;
+      if (kiter > 4) amom = nl->amomentum;
+      delx = delx * ww + amom * nl->hchold[n];
+      x[n] = xtemp[n] + delx;
+    }
+  }
+}
+
+/* NumericalSolution.f90:2878-2905, sln_maxval. */
+static double sln_maxval(int nsize, const double *v) {
+  double vmax = v[0];
+  for (int n = 1; n < nsize; ++n) {
+    double d = v[n];
+    double denom = fabs(vmax);
+    if (denom == 0.0) denom = DPREC;
+    double dnorm = fabs(d) / denom;
+    if (dnorm > 1.0) vmax = d;
+  }
+  return vmax;
+}
+
+/* NumericalSolution.f90:2966-2982 + SeqVector.f90:152-164: L2 norm of the
+ * residual A*x - b with inactive rows zeroed. */
+static double sln_l2norm(int neq, const int *ia, const int *ja, const double *amat,
+                         const double *x, const double *rhs, const int *active,
+                         double *work) {
+  or_amux(neq, x, work, amat, ja, ia);
+  double n2 = 0.0;
+  for (int n = 0; n < neq; ++n) {
+    double r = work[n] - rhs[n];
+    if (active[n] < 1) r = 0.0;
+    work[n] = r;
+    n2 = n2 + r * r;
+  }
+  return sqrt(n2);
+}
+
+/* One time step of NumericalSolution for a single GWF model:
+ * prepareSolve (gwf_ad, chd_ad) then the Picard/Newton outer loop of
+ * sln_ca/solve (NumericalSolution.f90:1287-1322, 1482-1837) with sln_ls
+ * (:2404-2615) including pseudo-transient continuation for steady-state
+ * Newton models (gwf.f90:625-687).  Backtracking is not restated
+ * (numtrack must be 0).  Returns 0 on success. */
+int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
+                    const double *condsat, int *ibound, int kper, int kstp, double delt,
+                    int transient, double *x, double *xold, or_timestep_stats *st) {
+  int neq = m->nodes, nja = m->nja;
+  double *amat = (double *)calloc(nja, sizeof(double));
+  double *rhs = (double *)calloc(neq, sizeof(double));
+  double *sat = (double *)calloc(neq, sizeof(double));
+  double *xtemp = (double *)calloc(neq, sizeof(double));
+  double *work = (double *)calloc(neq, sizeof(double));
+  /* gwf_ad: xold = x ; chd_ad: x = xold = chd head */
+  for (int n = 0; n < neq; ++n) xold[n] = x[n];
+  for (int i = 0; i < m->nchd; ++i) {
+    x[m->chd_node[i]] = m->chd_head[i];
+    xold[m->chd_node[i]] = m->chd_head[i];
+  }
+  int isymmetric = (ims_ilinmeth(ims) == 1);
+  int steady = !transient;
+  memset(st, 0, sizeof(*st));
+  int converged = 0;
+  double l2norm0_ptc = 0.0, ptcdel = 0.0;
+  for (int kiter = 1; kiter <= nl->mxiter; ++kiter) {
+    memset(amat, 0, sizeof(double) * nja);
+    memset(rhs, 0, sizeof(double) * neq);
+    or_gwf_fc(m, ibound, condsat, sat, delt, transient, xold, x, amat, rhs);
+    /* sln_calc_ptc -> gwf_ptc */
+    int iptc = 0;
+    double ptcf = 0.0;
+    int iptct = (steady && m->inewton > 0) ? 1 : 0;
+    if (iptct > 0) {
+      or_amux(neq, x, work, amat, m->ja, m->ia);
+      for (int n = 0; n < neq; ++n) {
+        work[n] = work[n] - rhs[n];
+        if (ibound[n] < 1) work[n] = 0.0;
+      }
+      for (int n = 0; n < neq; ++n) {
+        if (ibound[n] < 1) continue;
+        double v = m->area[n] * (m->top[n] - m->bot[n]);
+        double ptcdelem1 = fabs(work[n]) / v;
+        if (ptcdelem1 > ptcf) ptcf = ptcdelem1;
+      }
+      if (ptcf == 0.0) ptcf = 1.0 / (delt * 10.0);
+      iptc = 1;
+    }
+    /* sln_ls */
+    or_sln_ls_fixups(neq, m->ia, m->ja, ibound, isymmetric, amat, rhs, x, xtemp);
+    int iallowptc = nl->iallowptc;
+    if (iallowptc < 0) iallowptc = (kper > 1) ? 1 : 0;
+    iptct = iptc * iallowptc;
+    if (iptct != 0) {
+      double l2norm = sln_l2norm(neq, m->ia, m->ja, amat, x, rhs, ibound, work);
+      if (kiter == 1) {
+        if (kper > 1 || kstp > 1) {
+          if (l2norm <= l2norm0_ptc) iptc = 0;
+        }
+      } else {
+        if (or_is_close(l2norm, l2norm0_ptc)) iptc = 0;
+      }
+      iptct = iptc * iallowptc;
+      if (iptct != 0) {
+        if (kiter == 1) {
+          ptcdel = 1.0 / ptcf; /* iptcopt = 0, ptcdel0 = 0 */
+        } else {
+          if (l2norm > 0.0) ptcdel = ptcdel * (l2norm0_ptc / l2norm); /* ptcexp = 1 */
+          else ptcdel = 0.0;
+        }
+        double ptcval = (ptcdel > 0.0) ? 1.0 / ptcdel : 1.0;
+        for (int ieq = 0; ieq < neq; ++ieq) {
+          if (ibound[ieq] > 0) {
+            amat[m->ia[ieq]] = amat[m->ia[ieq]] + (-ptcval);
+            rhs[ieq] = rhs[ieq] - ptcval * x[ieq];
+          }
+        }
+        l2norm0_ptc = l2norm;
+      }
+    }
+    int icnvg = 0, in_iter = 0;
+    int rc = or_ims_apply(ims, amat, rhs, x, kstp, kiter, &icnvg, &in_iter, NULL, 0);
+    if (rc != 0) {
+      free(amat); free(rhs); free(sat); free(xtemp); free(work);
+      return rc;
+    }
+    st->inner_total += in_iter;
+    st->outer = kiter;
+    st->pivot_retries += or_ims_pivot_retries(ims);
+    int lrch;
+    double hncg = or_sln_get_dxmax(neq, ibound, x, xtemp, &lrch);
+    st->last_dxmax = hncg;
+    int cnvg = fabs(hncg) <= nl->dvclose;
+    if (!cnvg) {
+      if (nl->nonmeth > 0) or_sln_underrelax(nl, kiter, hncg, neq, ibound, x, xtemp);
+      else
+        for (int n = 0; n < neq; ++n) nl->dxold[n] = (ibound[n] < 1) ? 0.0 : x[n] - xtemp[n];
+      if (m->inewton) {
+        int inewtonur = 0, locmax = -1;
+        double dxmax_nur = 0.0;
+        or_npf_nur(m, ibound, x, xtemp, nl->dxold, &inewtonur, &dxmax_nur, &locmax);
+        if (inewtonur != 0) {
+          double dxold_max = sln_maxval(neq, nl->dxold);
+          if (fabs(dxold_max) <= nl->dvclose && fabs(hncg) <= nl->dvclose) {
+            cnvg = 1;
+            hncg = or_sln_get_dxmax(neq, ibound, x, xtemp, &lrch);
+          }
+        }
+      }
+    }
+    if (cnvg) {
+      converged = 1;
+      break;
+    }
+  }
+  st->converged = converged;
+  free(amat); free(rhs); free(sat); free(xtemp); free(work);
+  return 0;
+}

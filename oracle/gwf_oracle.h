@@ -1,0 +1,92 @@
+/*
+ * gwf_oracle.h -- CPU restatement of GWF assembly and the outer loop.
+ * TEST INFRASTRUCTURE ONLY (the oracle); the product never includes this.
+ */
+#ifndef GWF_ORACLE_H
+#define GWF_ORACLE_H
+
+#include "ims_oracle.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A single DIS model with NPF/STO/CHD/WEL/RCH.  All indices 0-based.  The
+ * struct only borrows the arrays; the caller keeps them alive. */
+typedef struct {
+  int nlay, nrow, ncol, nodes, nja, njas;
+  const int *ia, *ja, *isym, *jas, *ihc;
+  const double *cl1, *cl2, *hwva;
+  const double *top, *bot, *area;
+  const double *k11, *k33;
+  const int *icelltype;
+  int inewton, ivarcv, idewatcv, icellavg;
+  double satomega;
+  /* storage */
+  const double *ss, *sy;
+  const int *iconvert;
+  /* boundaries */
+  int nwel;
+  const int *wel_node;
+  const double *wel_q;
+  int nrch;
+  const int *rch_node;
+  const double *rch_rate;
+  int nchd;
+  const int *chd_node;
+  const double *chd_head;
+} or_gwf_model;
+
+/* NONLINEAR block state (NumericalSolution.f90 members). */
+typedef struct {
+  double dvclose;
+  int mxiter, nonmeth, iallowptc;
+  double theta, akappa, gamma, amomentum;
+  double bigch, bigchold, relaxold;
+  double *wsave, *hchold, *deold, *dxold; /* length neq, caller-owned */
+} or_nonlinear;
+
+typedef struct {
+  int outer, inner_total, converged, pivot_retries;
+  double last_dxmax;
+} or_timestep_stats;
+
+void or_dis_sizes(int nlay, int nrow, int ncol, int *nodes, int *nja, int *njas);
+void or_dis_connect(int nlay, int nrow, int ncol, const double *delr, const double *delc,
+                    const double *top, const double *bot, int *ia, int *ja, int *isym,
+                    int *jas, int *ihc, double *cl1, double *cl2, double *hwva);
+double or_squadratic_sat(double top, double bot, double x, double eps);
+double or_squadratic_sat_derv(double top, double bot, double x, double eps);
+void or_npf_condsat(const or_gwf_model *m, double *condsat);
+void or_npf_cf(const or_gwf_model *m, const int *ibound, const double *hnew, double *sat);
+void or_npf_fc(const or_gwf_model *m, const int *ibound, const double *condsat,
+               const double *sat, const double *hnew, double *amat, double *rhs);
+void or_npf_fn(const or_gwf_model *m, const int *ibound, const double *condsat,
+               const double *hnew, double *amat, double *rhs);
+void or_npf_nur(const or_gwf_model *m, const int *ibound, double *x, const double *xtemp,
+                double *dx, int *inewtonur, double *dxmax, int *locmax);
+void or_sto_fc(const or_gwf_model *m, const int *ibound, double delt, const double *hold,
+               const double *hnew, double *amat, double *rhs);
+void or_sto_fn(const or_gwf_model *m, const int *ibound, double delt, const double *hnew,
+               double *amat, double *rhs);
+void or_bnd_fc(const or_gwf_model *m, const int *ibound, double *amat, double *rhs);
+void or_gwf_fc(const or_gwf_model *m, const int *ibound, const double *condsat,
+               double *sat, double delt, int transient, const double *hold,
+               const double *hnew, double *amat, double *rhs);
+void or_sln_ls_fixups(int neq, const int *ia, const int *ja, const int *active,
+                      int isymmetric, double *amat, double *rhs, const double *x,
+                      double *xtemp);
+double or_sln_get_dxmax(int neq, const int *active, const double *x, const double *xtemp,
+                        int *lrch);
+void or_sln_underrelax(or_nonlinear *nl, int kiter, double bigch, int neq,
+                       const int *active, double *x, const double *xtemp);
+int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
+                    const double *condsat, int *ibound, int kper, int kstp, double delt,
+                    int transient, double *x, double *xold, or_timestep_stats *st);
+
+int ims_ilinmeth(const or_ims *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

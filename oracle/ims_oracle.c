@@ -1,0 +1,608 @@
+/*
+ * ims_oracle.c -- CPU restatement of the MODFLOW 6 IMS linear path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle that the GPU library is
+ * checked against; nothing in the product links or calls it.  Only tests/,
+ * __graft_entry__.smoke() and bench.py (its cpu_baseline / reference arm)
+ * load the shared library built from it.
+ *
+ * Each routine follows the cited Fortran routine of MODFLOW 6 (6.7.0.dev1)
+ * loop for loop, with 0-based indices in place of the Fortran 1-based ones.
+ * Summation order is kept, so with the same floating-point contraction
+ * setting the results are bit-for-bit those of the Fortran code.  The oracle
+ * is compiled with -ffp-contract=off (no fused multiply-add), which is what
+ * gfortran does on x86-64 without -march flags.
+ *
+ * Parity pins: the known answers of autotest/test_gwf_chd01.py:118-127 and
+ * autotest/test_gwf_newton01.py:95-103 (see tests/test_oracle_known_answers.py).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <float.h>
+
+#include "ims_oracle.h"
+
+/* src/Utilities/Constants.f90:120-122 */
+#define DPREC DBL_EPSILON
+#define DSAME (100.0 * DBL_EPSILON)
+#define DEM3 1.0e-3
+#define DEM4 1.0e-4
+#define DEM6 1.0e-6
+
+/* Fortran SIGN(a, b): |a| with the sign of b (signed zeros honoured). */
+static inline double f_sign(double a, double b) { return copysign(fabs(a), b); }
+
+/* src/Utilities/MathUtil.f90:45-86, is_close with default rtol=DSAME, atol=0,
+ * symmetric test. */
+int or_is_close(double a, double b) {
+  if (a == b) return 1;
+  double m = fmax(fabs(a), fabs(b));
+  double tol = DSAME * m;
+  if (tol < 0.0) tol = 0.0;
+  return fabs(a - b) <= tol;
+}
+
+/* src/Utilities/Libraries/sparsekit/sparsekit.f90:1-59, amux: y = A*x, row
+ * dot product in CSR order. */
+void or_amux(int n, const double *x, double *y, const double *a, const int *ja,
+             const int *ia) {
+  for (int i = 0; i < n; ++i) {
+    double t = 0.0;
+    for (int k = ia[i]; k < ia[i + 1]; ++k) t = t + a[k] * x[ja[k]];
+    y[i] = t;
+  }
+}
+
+/* src/Utilities/Libraries/blas/blas1_d.f90:295-386, ddot = dot_product,
+ * summed sequentially from the first element. */
+double or_ddot(int n, const double *x, const double *y) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s = s + x[i] * y[i];
+  return s;
+}
+
+/* src/Utilities/Libraries/blas/blas1_d.f90:387-470, dnrm2 with the scaled sum
+ * of squares. */
+double or_dnrm2(int n, const double *x) {
+  if (n < 1) return 0.0;
+  if (n == 1) return fabs(x[0]);
+  double scale = 0.0, ssq = 1.0;
+  for (int i = 0; i < n; ++i) {
+    if (x[i] != 0.0) {
+      double absxi = fabs(x[i]);
+      if (scale < absxi) {
+        double r = scale / absxi;
+        ssq = 1.0 + ssq * (r * r);
+        scale = absxi;
+      } else {
+        double r = absxi / scale;
+        ssq = ssq + r * r;
+      }
+    }
+  }
+  return scale * sqrt(ssq);
+}
+
+/* ImsLinearBase.f90:1291-1312, ims_base_residual: d = b - A*x. */
+void or_residual(int neq, const double *x, const double *b, double *d,
+                 const double *a, const int *ia, const int *ja) {
+  or_amux(neq, x, d, a, ja, ia);
+  for (int n = 0; n < neq; ++n) d[n] = b[n] - d[n];
+}
+
+/* ImsLinearBase.f90:1316-1333, ims_base_epfact.  The 0.01 and 0.10 literals
+ * are default (single-precision) reals in the Fortran source, so they are
+ * converted from float here to give the same double values. */
+double or_epfact(int icnvgopt, int kstp) {
+  if (icnvgopt == 2) return (kstp == 1) ? (double)0.01f : (double)0.10f;
+  if (icnvgopt == 4) return DEM4;
+  return 1.0;
+}
+
+/* ImsLinearBase.f90:1101-1146, ims_base_testcnvg. */
+void or_testcnvg(int icnvgopt, int *icnvg, int iiter, double dvmax, double rmax,
+                 double rmax0, double epfact, double dvclose, double rclose) {
+  if (icnvgopt == 0) {
+    if (fabs(dvmax) <= dvclose && fabs(rmax) <= rclose) *icnvg = 1;
+  } else if (icnvgopt == 1) {
+    if (fabs(dvmax) <= dvclose && fabs(rmax) <= rclose) *icnvg = (iiter == 1) ? 1 : -1;
+  } else if (icnvgopt == 2) {
+    if (fabs(dvmax) <= dvclose || rmax <= rclose) *icnvg = 1;
+    else if (rmax <= rmax0 * epfact) *icnvg = -1;
+  } else if (icnvgopt == 3) {
+    if (fabs(dvmax) <= dvclose) *icnvg = 1;
+    else if (rmax <= rmax0 * rclose) *icnvg = -1;
+  } else if (icnvgopt == 4) {
+    if (fabs(dvmax) <= dvclose && rmax <= rclose) *icnvg = 1;
+    else if (rmax <= rmax0 * epfact) *icnvg = -1;
+  }
+}
+
+/* ImsLinearBase.f90:1207-1261, ims_base_pccrs: builds IAPC/JAPC.  japc[0:neq]
+ * holds, per row, the position of the first upper entry; japc[neq:nja] the
+ * sorted off-diagonal columns.  Positions and columns are 0-based. */
+void or_pccrs(int neq, int nja, const int *ia, const int *ja, int *iapc, int *japc) {
+  int ip = neq;
+  int *iarr = (int *)malloc(sizeof(int) * 64);
+  int cap = 64;
+  for (int n = 0; n < neq; ++n) {
+    int i0 = ia[n], i1 = ia[n + 1];
+    int nlen = i1 - i0 - 1;
+    if (nlen + 1 > cap) {
+      cap = nlen + 1;
+      iarr = (int *)realloc(iarr, sizeof(int) * cap);
+    }
+    int ic = 0;
+    for (int j = i0; j < i1; ++j) {
+      int jcol = ja[j];
+      if (jcol == n) continue;
+      iarr[ic++] = jcol;
+    }
+    /* ims_base_isort (ImsLinearBase.f90:1268-1284): exchange sort */
+    for (int a = 0; a < nlen - 1; ++a)
+      for (int b = a + 1; b < nlen; ++b)
+        if (iarr[a] > iarr[b]) {
+          int t = iarr[b];
+          iarr[b] = iarr[a];
+          iarr[a] = t;
+        }
+    iapc[n] = ip;
+    for (int j = 0; j < nlen; ++j) japc[ip++] = iarr[j];
+  }
+  iapc[neq] = nja;
+  free(iarr);
+  for (int n = 0; n < neq; ++n) {
+    int i0 = iapc[n], i1 = iapc[n + 1];
+    japc[n] = iapc[n + 1];
+    for (int j = i0; j < i1; ++j) {
+      if (japc[j] > n) {
+        japc[n] = j;
+        break;
+      }
+    }
+  }
+}
+
+/* ImsLinearBase.f90:928-1042, ims_base_pcilu0: ILU0 (relax = 0) or MILU0
+ * (relax > 0) into APC.  iw/w are work vectors of length neq that must be
+ * zero on entry (they are left zero on normal exit). */
+void or_pcilu0(int nja, int neq, const double *amat, const int *ia, const int *ja,
+               double *apc, const int *iapc, const int *japc, int *iw, double *w,
+               double relax, int *ipcflag, double delta) {
+  double drelax = relax;
+  for (int n = 0; n < neq; ++n) {
+    iw[n] = 0;
+    w[n] = 0.0;
+  }
+  for (int n = 0; n < neq; ++n) {
+    for (int j = ia[n]; j < ia[n + 1]; ++j) {
+      int jcol = ja[j];
+      iw[jcol] = 1;
+      w[jcol] = w[jcol] + amat[j];
+    }
+    int ic0 = iapc[n], ic1 = iapc[n + 1];
+    int iu = japc[n];
+    double rs = 0.0;
+    for (int j = ic0; j < iu; ++j) {
+      int jcol = japc[j];
+      int iic1 = iapc[jcol + 1];
+      int iiu = japc[jcol];
+      double tl = w[jcol] * apc[jcol];
+      w[jcol] = tl;
+      for (int jj = iiu; jj < iic1; ++jj) {
+        int jjcol = japc[jj];
+        if (iw[jjcol] != 0) w[jjcol] = w[jjcol] - tl * apc[jj];
+        else rs = rs + tl * apc[jj];
+      }
+    }
+    double d = w[n];
+    double tl = (1.0 + delta) * d - (drelax * rs);
+    double sd1 = f_sign(d, tl);
+    if (sd1 != d) {
+      if (*ipcflag > 1) {
+        tl = f_sign(DEM6, d);
+      } else {
+        *ipcflag = 1;
+        goto cleanup_exit; /* EXIT MAIN */
+      }
+    }
+    if (fabs(tl) == 0.0) {
+      if (*ipcflag > 1) {
+        tl = f_sign(DEM6, d);
+      } else {
+        *ipcflag = 1;
+        goto cleanup_exit;
+      }
+    }
+    apc[n] = 1.0 / tl;
+    iw[n] = 0;
+    w[n] = 0.0;
+    for (int j = ic0; j < ic1; ++j) {
+      int jcol = japc[j];
+      apc[j] = w[jcol];
+      iw[jcol] = 0;
+      w[jcol] = 0.0;
+    }
+  }
+  *ipcflag = 0;
+  return;
+cleanup_exit:
+  /* The Fortran leaves IW/W dirty after EXIT MAIN; the next call re-zeroes
+   * them at its start, exactly as done at the top of this routine. */
+  return;
+}
+
+/* ImsLinearBase.f90:761-864, ims_base_pcu for IPC 1/2: retry with a growing
+ * diagonal increment.  Returns the number of retries (icount). */
+int or_pcu(int nja, int neq, int ipc, double relax, const double *amat,
+           const int *ia, const int *ja, double *apc, const int *iapc,
+           const int *japc, int *iw, double *w) {
+  int ipcflag = 0, icount = 0;
+  double delta = 0.0;
+  for (;;) {
+    if (ipc == 1 || ipc == 2) {
+      or_pcilu0(nja, neq, amat, ia, ja, apc, iapc, japc, iw, w, relax, &ipcflag, delta);
+    } else {
+      ipcflag = 0;
+    }
+    if (ipcflag < 1) break;
+    delta = 1.5 * delta + DEM3;
+    ipcflag = 0;
+    if (delta > 0.5) {
+      delta = 0.5;
+      ipcflag = 2;
+    }
+    icount = icount + 1;
+    if (icount > 10) break;
+  }
+  return icount;
+}
+
+/* ImsLinearBase.f90:1049-1092, ims_base_ilu0a: forward then backward solve. */
+void or_ilu0a(int nja, int neq, const double *apc, const int *iapc, const int *japc,
+              const double *r, double *d) {
+  (void)nja;
+  for (int n = 0; n < neq; ++n) {
+    double tv = r[n];
+    int ic0 = iapc[n];
+    int iu = japc[n];
+    for (int j = ic0; j < iu; ++j) tv = tv - apc[j] * d[japc[j]];
+    d[n] = tv;
+  }
+  for (int n = neq - 1; n >= 0; --n) {
+    int ic1 = iapc[n + 1];
+    int iu = japc[n];
+    double tv = d[n];
+    for (int j = iu; j < ic1; ++j) tv = tv - apc[j] * d[japc[j]];
+    d[n] = tv * apc[n];
+  }
+}
+
+/* ImsLinearBase.f90:619-754, ims_base_scale: iopt 0 scales, 1 unscales. */
+void or_scale(int iopt, int iscl, int neq, int nja, const int *ia, const int *ja,
+              double *amat, double *x, double *b, double *dscale, double *dscale2) {
+  (void)nja;
+  if (iopt == 0) {
+    if (iscl == 1) {
+      for (int n = 0; n < neq; ++n) {
+        double v = amat[ia[n]];
+        double c1 = 1.0 / sqrt(fabs(v));
+        dscale[n] = c1;
+        dscale2[n] = c1;
+      }
+      for (int n = 0; n < neq; ++n) {
+        double c1 = dscale[n];
+        for (int i = ia[n]; i < ia[n + 1]; ++i) {
+          double c2 = dscale2[ja[i]];
+          amat[i] = c1 * amat[i] * c2;
+        }
+      }
+    } else if (iscl == 2) {
+      for (int n = 0; n < neq; ++n) {
+        double c1 = 0.0;
+        for (int i = ia[n]; i < ia[n + 1]; ++i) c1 = c1 + amat[i] * amat[i];
+        c1 = sqrt(c1);
+        c1 = (c1 == 0.0) ? 1.0 : 1.0 / c1;
+        dscale[n] = c1;
+        for (int i = ia[n]; i < ia[n + 1]; ++i) amat[i] = c1 * amat[i];
+      }
+      for (int n = 0; n < neq; ++n) dscale2[n] = 0.0;
+      for (int n = 0; n < neq; ++n)
+        for (int i = ia[n]; i < ia[n + 1]; ++i) {
+          double c2 = amat[i];
+          dscale2[ja[i]] = dscale2[ja[i]] + c2 * c2;
+        }
+      for (int n = 0; n < neq; ++n) {
+        double c2 = dscale2[n];
+        c2 = (c2 == 0.0) ? 1.0 : 1.0 / sqrt(c2);
+        dscale2[n] = c2;
+      }
+      for (int n = 0; n < neq; ++n)
+        for (int i = ia[n]; i < ia[n + 1]; ++i) amat[i] = dscale2[ja[i]] * amat[i];
+    }
+    for (int n = 0; n < neq; ++n) {
+      x[n] = x[n] / dscale2[n];
+      b[n] = b[n] * dscale[n];
+    }
+  } else {
+    for (int n = 0; n < neq; ++n) {
+      double c1 = dscale[n];
+      for (int i = ia[n]; i < ia[n + 1]; ++i) {
+        double c2 = dscale2[ja[i]];
+        amat[i] = (1.0 / c1) * amat[i] * (1.0 / c2);
+      }
+      double c2 = dscale2[n];
+      x[n] = x[n] * c2;
+      b[n] = b[n] / c1;
+    }
+  }
+}
+
+/* ImsLinearBase.f90:30-240, ims_base_cg (single model, IPC 1/2). */
+static void or_cg(int *icnvg, int itmax, int *innerit, int neq, int nja, int icnvgopt,
+                  int north, double dvclose, double rclose, double l2norm0,
+                  double epfact, const int *ia0, const int *ja0, const double *a0,
+                  const int *iapc, const int *japc, const double *apc, double *x,
+                  double *b, double *d, double *p, double *q, double *z,
+                  or_cnvg_record *rec, int nrec) {
+  double rho0 = 0.0, rho = 0.0;
+  *innerit = 0;
+  for (int iiter = 1; iiter <= itmax; ++iiter) {
+    *innerit = *innerit + 1;
+    or_ilu0a(nja, neq, apc, iapc, japc, d, z);
+    rho = or_ddot(neq, d, z);
+    if (iiter == 1) {
+      for (int n = 0; n < neq; ++n) p[n] = z[n];
+    } else {
+      double beta = rho / rho0;
+      for (int n = 0; n < neq; ++n) p[n] = z[n] + beta * p[n];
+    }
+    or_amux(neq, p, q, a0, ja0, ia0);
+    double denominator = or_ddot(neq, p, q);
+    denominator = denominator + f_sign(DPREC, denominator);
+    double alpha = rho / denominator;
+    double deltax = 0.0, rmax = 0.0, l2norm = 0.0;
+    int xloc = -1, rloc = -1;
+    for (int n = 0; n < neq; ++n) {
+      double tv = alpha * p[n];
+      x[n] = x[n] + tv;
+      if (fabs(tv) > fabs(deltax)) {
+        deltax = tv;
+        xloc = n;
+      }
+      tv = d[n];
+      tv = tv - alpha * q[n];
+      d[n] = tv;
+      if (fabs(tv) > fabs(rmax)) {
+        rmax = tv;
+        rloc = n;
+      }
+      l2norm = l2norm + tv * tv;
+    }
+    l2norm = sqrt(l2norm);
+    if (rec && iiter <= nrec) {
+      or_cnvg_record *r = &rec[iiter - 1];
+      r->dvmax = deltax; r->rmax = rmax; r->locdv = xloc; r->locr = rloc;
+      r->l2norm = l2norm; r->alpha = alpha; r->beta = (iiter == 1) ? 0.0 : rho / rho0;
+      r->rho = rho; r->omega = 0.0;
+    }
+    double rcnvg = (icnvgopt == 2 || icnvgopt == 3 || icnvgopt == 4) ? l2norm : rmax;
+    or_testcnvg(icnvgopt, icnvg, *innerit, deltax, rcnvg, l2norm0, epfact, dvclose, rclose);
+    if (rcnvg == 0.0) *icnvg = 1;
+    if (*icnvg != 0) break;
+    if (or_is_close(rho, rho0)) break;
+    if (north > 0) {
+      if ((iiter + 1) % north == 0) or_residual(neq, x, b, d, a0, ia0, ja0);
+    }
+    if (rho == 0.0) break;
+    rho0 = rho;
+  }
+  if (*icnvg < 0) *icnvg = 0;
+}
+
+/* ImsLinearBase.f90:249-549, ims_base_bcgs (single model, IPC 1/2). */
+static void or_bcgs(int *icnvg, int itmax, int *innerit, int neq, int nja, int icnvgopt,
+                    int north, int iscl, const double *dscale, double dvclose,
+                    double rclose, double l2norm0, double epfact, const int *ia0,
+                    const int *ja0, const double *a0, const int *iapc, const int *japc,
+                    const double *apc, double *x, double *b, double *d, double *p,
+                    double *q, double *t, double *v, double *dhat, double *phat,
+                    double *qhat, or_cnvg_record *rec, int nrec) {
+  *innerit = 0;
+  double alpha = 0.0, alpha0 = 0.0, beta = 0.0, rho = 0.0, rho0 = 0.0;
+  double omega = 0.0, omega0 = 0.0;
+  for (int n = 0; n < neq; ++n) dhat[n] = d[n];
+  for (int iiter = 1; iiter <= itmax; ++iiter) {
+    *innerit = *innerit + 1;
+    rho = or_ddot(neq, dhat, d);
+    if (iiter == 1) {
+      for (int n = 0; n < neq; ++n) p[n] = d[n];
+    } else {
+      beta = (rho / rho0) * (alpha0 / omega0);
+      for (int n = 0; n < neq; ++n) p[n] = d[n] + beta * (p[n] - omega0 * v[n]);
+    }
+    or_ilu0a(nja, neq, apc, iapc, japc, p, phat);
+    or_amux(neq, phat, v, a0, ja0, ia0);
+    double denominator = or_ddot(neq, dhat, v);
+    denominator = denominator + f_sign(DPREC, denominator);
+    alpha = rho / denominator;
+    for (int n = 0; n < neq; ++n) q[n] = d[n] - alpha * v[n];
+    or_ilu0a(nja, neq, apc, iapc, japc, q, qhat);
+    or_amux(neq, qhat, t, a0, ja0, ia0);
+    double numerator = or_ddot(neq, t, q);
+    denominator = or_ddot(neq, t, t);
+    denominator = denominator + f_sign(DPREC, denominator);
+    omega = numerator / denominator;
+    double deltax = 0.0, rmax = 0.0, l2norm = 0.0;
+    int xloc = -1, rloc = -1;
+    for (int n = 0; n < neq; ++n) {
+      double tv = alpha * phat[n] + omega * qhat[n];
+      x[n] = x[n] + tv;
+      if (iscl != 0) tv = tv * dscale[n];
+      if (fabs(tv) > fabs(deltax)) {
+        deltax = tv;
+        xloc = n;
+      }
+      tv = q[n] - omega * t[n];
+      d[n] = tv;
+      if (iscl != 0) tv = tv / dscale[n];
+      if (fabs(tv) > fabs(rmax)) {
+        rmax = tv;
+        rloc = n;
+      }
+      l2norm = l2norm + tv * tv;
+    }
+    l2norm = sqrt(l2norm);
+    if (rec && iiter <= nrec) {
+      or_cnvg_record *r = &rec[iiter - 1];
+      r->dvmax = deltax; r->rmax = rmax; r->locdv = xloc; r->locr = rloc;
+      r->l2norm = l2norm; r->alpha = alpha; r->beta = beta; r->rho = rho; r->omega = omega;
+    }
+    double rcnvg = (icnvgopt == 2 || icnvgopt == 3 || icnvgopt == 4) ? l2norm : rmax;
+    or_testcnvg(icnvgopt, icnvg, *innerit, deltax, rcnvg, l2norm0, epfact, dvclose, rclose);
+    if (rcnvg == 0.0) *icnvg = 1;
+    if (*icnvg != 0) break;
+    if (or_is_close(rho, rho0)) break;
+    if (or_is_close(alpha, alpha0)) break;
+    if (or_is_close(omega, omega0)) break;
+    if (north > 0) {
+      if ((iiter + 1) % north == 0) or_residual(neq, x, b, d, a0, ia0, ja0);
+    }
+    if (rho * omega == 0.0) break;
+    rho0 = rho;
+    alpha0 = alpha;
+    omega0 = omega;
+  }
+  if (*icnvg < 0) *icnvg = 0;
+}
+
+/* ImsLinear.f90:111-339 (imslinear_ar, the parts that do not read files):
+ * choose IPC (:178-185) and build IAPC/JAPC (:267-270). */
+struct or_ims {
+  or_ims_settings s;
+  int neq, nja, ipc;
+  int *ia, *ja; /* 0-based copies */
+  int *iapc, *japc;
+  double *apc, *w;
+  int *iw;
+  double *d, *p, *q, *z, *t, *v, *dhat, *phat, *qhat;
+  double *dscale, *dscale2;
+  double l2norm0, epfact;
+  int npivot_retries;
+};
+
+or_ims *or_ims_create(const or_ims_settings *s, int neq, int nja, const int *ia,
+                      const int *ja) {
+  or_ims *h = (or_ims *)calloc(1, sizeof(or_ims));
+  h->s = *s;
+  h->neq = neq;
+  h->nja = nja;
+  if (s->level > 0 || s->droptol > 0.0) h->ipc = 3;
+  else h->ipc = 1;
+  if (s->relax > 0.0) h->ipc += 1;
+  h->ia = (int *)malloc(sizeof(int) * (neq + 1));
+  h->ja = (int *)malloc(sizeof(int) * nja);
+  memcpy(h->ia, ia, sizeof(int) * (neq + 1));
+  memcpy(h->ja, ja, sizeof(int) * nja);
+  h->iapc = (int *)calloc(neq + 1, sizeof(int));
+  h->japc = (int *)calloc(nja, sizeof(int));
+  h->apc = (double *)calloc(nja, sizeof(double));
+  h->iw = (int *)calloc(neq, sizeof(int));
+  h->w = (double *)calloc(neq, sizeof(double));
+  double **vecs[] = {&h->d, &h->p, &h->q, &h->z, &h->t, &h->v, &h->dhat, &h->phat,
+                     &h->qhat, &h->dscale, &h->dscale2};
+  for (size_t i = 0; i < sizeof(vecs) / sizeof(vecs[0]); ++i)
+    *vecs[i] = (double *)calloc(neq, sizeof(double));
+  for (int n = 0; n < neq; ++n) {
+    h->dscale[n] = 1.0;
+    h->dscale2[n] = 1.0;
+  }
+  if (h->ipc == 1 || h->ipc == 2) or_pccrs(neq, nja, h->ia, h->ja, h->iapc, h->japc);
+  return h;
+}
+
+void or_ims_destroy(or_ims *h) {
+  if (!h) return;
+  free(h->ia); free(h->ja); free(h->iapc); free(h->japc); free(h->apc);
+  free(h->iw); free(h->w); free(h->d); free(h->p); free(h->q); free(h->z);
+  free(h->t); free(h->v); free(h->dhat); free(h->phat); free(h->qhat);
+  free(h->dscale); free(h->dscale2);
+  free(h);
+}
+
+int or_ims_ipc(const or_ims *h) { return h->ipc; }
+const int *or_ims_iapc(const or_ims *h) { return h->iapc; }
+const int *or_ims_japc(const or_ims *h) { return h->japc; }
+const double *or_ims_apc(const or_ims *h) { return h->apc; }
+double or_ims_l2norm0(const or_ims *h) { return h->l2norm0; }
+int or_ims_pivot_retries(const or_ims *h) { return h->npivot_retries; }
+
+/* ImsLinear.f90:617-750, imslinear_ap (no reordering: IORD = 0). */
+int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int kiter,
+                 int *icnvg, int *in_iter, or_cnvg_record *rec, int nrec) {
+  const or_ims_settings *s = &h->s;
+  int neq = h->neq, nja = h->nja;
+  if (s->iord != 0) return -2; /* reordering is not restated here */
+  if (h->ipc != 1 && h->ipc != 2) return -3; /* ILUT is not restated here */
+  h->epfact = or_epfact(s->icnvgopt, kstp);
+  if (s->iscl != 0)
+    or_scale(0, s->iscl, neq, nja, h->ia, h->ja, amat, x, rhs, h->dscale, h->dscale2);
+  h->npivot_retries = or_pcu(nja, neq, h->ipc, s->relax, amat, h->ia, h->ja, h->apc,
+                             h->iapc, h->japc, h->iw, h->w);
+  (void)kiter;
+  *icnvg = 0;
+  for (int n = 0; n < neq; ++n) {
+    h->d[n] = 0.0; h->p[n] = 0.0; h->q[n] = 0.0; h->z[n] = 0.0;
+  }
+  or_residual(neq, x, rhs, h->d, amat, h->ia, h->ja);
+  h->l2norm0 = or_dnrm2(neq, h->d);
+  int itmax = s->iter1;
+  if (h->l2norm0 == 0.0) {
+    itmax = 0;
+    *icnvg = 1;
+  }
+  int innerit = 0;
+  if (s->ilinmeth == 1) {
+    or_cg(icnvg, itmax, &innerit, neq, nja, s->icnvgopt, s->north, s->dvclose,
+          s->rclose, h->l2norm0, h->epfact, h->ia, h->ja, amat, h->iapc, h->japc,
+          h->apc, x, rhs, h->d, h->p, h->q, h->z, rec, nrec);
+  } else {
+    or_bcgs(icnvg, itmax, &innerit, neq, nja, s->icnvgopt, s->north, s->iscl,
+            h->dscale, s->dvclose, s->rclose, h->l2norm0, h->epfact, h->ia, h->ja,
+            amat, h->iapc, h->japc, h->apc, x, rhs, h->d, h->p, h->q, h->t, h->v,
+            h->dhat, h->phat, h->qhat, rec, nrec);
+  }
+  if (s->iscl != 0)
+    or_scale(1, s->iscl, neq, nja, h->ia, h->ja, amat, x, rhs, h->dscale, h->dscale2);
+  *in_iter = innerit;
+  return 0;
+}
+
+int ims_ilinmeth(const or_ims *h) { return h->s.ilinmeth; }
+
+/* FMA-contracted variants of amux and ilu0a: the same loops with a*b+c
+ * evaluated as one fused operation, which is what gfortran emits on aarch64
+ * (GNU -ffp-contract=fast default) and what the GPU kernels compute. */
+void or_amux_fma(int n, const double *x, double *y, const double *a, const int *ja,
+                 const int *ia) {
+  for (int i = 0; i < n; ++i) {
+    double t = 0.0;
+    for (int k = ia[i]; k < ia[i + 1]; ++k) t = fma(a[k], x[ja[k]], t);
+    y[i] = t;
+  }
+}
+
+void or_ilu0a_fma(int neq, const double *apc, const int *iapc, const int *japc,
+                  const double *r, double *d) {
+  for (int n = 0; n < neq; ++n) {
+    double tv = r[n];
+    for (int j = iapc[n]; j < japc[n]; ++j) tv = fma(-apc[j], d[japc[j]], tv);
+    d[n] = tv;
+  }
+  for (int n = neq - 1; n >= 0; --n) {
+    double tv = d[n];
+    for (int j = japc[n]; j < iapc[n + 1]; ++j) tv = fma(-apc[j], d[japc[j]], tv);
+    d[n] = tv * apc[n];
+  }
+}

@@ -1,0 +1,289 @@
+"""ctypes wrapper of the CPU oracle (oracle/ims_oracle.c, oracle/gwf_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: this module is the checker.  It is imported by
+tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline and
+reference legs, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+_lib = None
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def build() -> Path:
+    srcs = [HERE / f for f in ("ims_oracle.c", "gwf_oracle.c", "ims_oracle.h", "gwf_oracle.h", "Makefile")]
+    if not LIB.exists() or LIB.stat().st_mtime < max(s.stat().st_mtime for s in srcs):
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+class Settings(C.Structure):
+    _fields_ = [("dvclose", C.c_double), ("rclose", C.c_double), ("icnvgopt", C.c_int),
+                ("iter1", C.c_int), ("ilinmeth", C.c_int), ("iscl", C.c_int), ("iord", C.c_int),
+                ("north", C.c_int), ("relax", C.c_double), ("level", C.c_int),
+                ("droptol", C.c_double)]
+
+
+class CnvgRecord(C.Structure):
+    _fields_ = [("dvmax", C.c_double), ("rmax", C.c_double), ("l2norm", C.c_double),
+                ("alpha", C.c_double), ("beta", C.c_double), ("rho", C.c_double),
+                ("omega", C.c_double), ("locdv", C.c_int), ("locr", C.c_int)]
+
+
+class GwfModel(C.Structure):
+    _fields_ = [("nlay", C.c_int), ("nrow", C.c_int), ("ncol", C.c_int), ("nodes", C.c_int),
+                ("nja", C.c_int), ("njas", C.c_int),
+                ("ia", _ip), ("ja", _ip), ("isym", _ip), ("jas", _ip), ("ihc", _ip),
+                ("cl1", _dp), ("cl2", _dp), ("hwva", _dp),
+                ("top", _dp), ("bot", _dp), ("area", _dp), ("k11", _dp), ("k33", _dp),
+                ("icelltype", _ip), ("inewton", C.c_int), ("ivarcv", C.c_int),
+                ("idewatcv", C.c_int), ("icellavg", C.c_int), ("satomega", C.c_double),
+                ("ss", _dp), ("sy", _dp), ("iconvert", _ip),
+                ("nwel", C.c_int), ("wel_node", _ip), ("wel_q", _dp),
+                ("nrch", C.c_int), ("rch_node", _ip), ("rch_rate", _dp),
+                ("nchd", C.c_int), ("chd_node", _ip), ("chd_head", _dp)]
+
+
+class Nonlinear(C.Structure):
+    _fields_ = [("dvclose", C.c_double), ("mxiter", C.c_int), ("nonmeth", C.c_int),
+                ("iallowptc", C.c_int), ("theta", C.c_double), ("akappa", C.c_double),
+                ("gamma", C.c_double), ("amomentum", C.c_double), ("bigch", C.c_double),
+                ("bigchold", C.c_double), ("relaxold", C.c_double),
+                ("wsave", _dp), ("hchold", _dp), ("deold", _dp), ("dxold", _dp)]
+
+
+class TimestepStats(C.Structure):
+    _fields_ = [("outer", C.c_int), ("inner_total", C.c_int), ("converged", C.c_int),
+                ("pivot_retries", C.c_int), ("last_dxmax", C.c_double)]
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB))
+        lib.or_ims_create.restype = C.c_void_p
+        lib.or_ims_create.argtypes = [C.POINTER(Settings), C.c_int, C.c_int, _ip, _ip]
+        lib.or_ims_destroy.argtypes = [C.c_void_p]
+        lib.or_ims_apply.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int, _ip, _ip,
+                                     C.POINTER(CnvgRecord), C.c_int]
+        lib.or_ims_apc.restype = _dp
+        lib.or_ims_apc.argtypes = [C.c_void_p]
+        lib.or_ims_iapc.restype = _ip
+        lib.or_ims_iapc.argtypes = [C.c_void_p]
+        lib.or_ims_japc.restype = _ip
+        lib.or_ims_japc.argtypes = [C.c_void_p]
+        lib.or_ims_l2norm0.restype = C.c_double
+        lib.or_ims_l2norm0.argtypes = [C.c_void_p]
+        lib.or_ims_pivot_retries.argtypes = [C.c_void_p]
+        lib.or_amux.argtypes = [C.c_int, _dp, _dp, _dp, _ip, _ip]
+        lib.or_ilu0a.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, _dp, _dp]
+        lib.or_amux_fma.argtypes = [C.c_int, _dp, _dp, _dp, _ip, _ip]
+        lib.or_ilu0a_fma.argtypes = [C.c_int, _dp, _ip, _ip, _dp, _dp]
+        lib.or_pccrs.argtypes = [C.c_int, C.c_int, _ip, _ip, _ip, _ip]
+        lib.or_pcu.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _dp]
+        lib.or_dnrm2.restype = C.c_double
+        lib.or_dnrm2.argtypes = [C.c_int, _dp]
+        lib.or_ddot.restype = C.c_double
+        lib.or_ddot.argtypes = [C.c_int, _dp, _dp]
+        lib.or_epfact.restype = C.c_double
+        lib.or_epfact.argtypes = [C.c_int, C.c_int]
+        lib.or_is_close.argtypes = [C.c_double, C.c_double]
+        lib.or_squadratic_sat.restype = C.c_double
+        lib.or_squadratic_sat.argtypes = [C.c_double] * 4
+        lib.or_squadratic_sat_derv.restype = C.c_double
+        lib.or_squadratic_sat_derv.argtypes = [C.c_double] * 4
+        lib.or_dis_sizes.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip]
+        lib.or_dis_connect.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, _ip, _ip,
+                                       _ip, _ip, _dp, _dp, _dp]
+        lib.or_npf_condsat.argtypes = [C.POINTER(GwfModel), _dp]
+        lib.or_gwf_fc.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, C.c_double, C.c_int, _dp, _dp, _dp, _dp]
+        lib.or_sln_ls_fixups.argtypes = [C.c_int, _ip, _ip, _ip, C.c_int, _dp, _dp, _dp, _dp]
+        lib.or_gwf_timestep.argtypes = [C.POINTER(GwfModel), C.c_void_p, C.POINTER(Nonlinear), _dp, _ip,
+                                        C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp,
+                                        C.POINTER(TimestepStats)]
+        _lib = lib
+    return _lib
+
+
+def dp(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous, (a.dtype, a.flags)
+    return a.ctypes.data_as(_dp)
+
+
+def ip(a):
+    assert a.dtype == np.int32 and a.flags.c_contiguous, (a.dtype, a.flags)
+    return a.ctypes.data_as(_ip)
+
+
+def settings(dvclose=1e-3, rclose=1e-1, icnvgopt=0, iter1=50, ilinmeth=1, iscl=0, iord=0,
+             north=0, relax=0.0, level=0, droptol=0.0) -> Settings:
+    return Settings(dvclose, rclose, icnvgopt, iter1, ilinmeth, iscl, iord, north, relax, level, droptol)
+
+
+class Ims:
+    """Oracle ImsLinearDataType (allocate / apply) for one matrix structure."""
+
+    def __init__(self, s: Settings, ia: np.ndarray, ja: np.ndarray):
+        self.lib = load()
+        self.ia = np.ascontiguousarray(ia, np.int32)
+        self.ja = np.ascontiguousarray(ja, np.int32)
+        self.neq = self.ia.size - 1
+        self.nja = self.ja.size
+        self.s = s
+        self.h = self.lib.or_ims_create(C.byref(s), self.neq, self.nja, ip(self.ia), ip(self.ja))
+
+    def apply(self, amat, rhs, x, kstp=1, kiter=1, nrec=0):
+        icnvg, in_iter = C.c_int(0), C.c_int(0)
+        rec = (CnvgRecord * max(nrec, 1))()
+        rc = self.lib.or_ims_apply(self.h, dp(amat), dp(rhs), dp(x), kstp, kiter, C.byref(icnvg),
+                                   C.byref(in_iter), rec if nrec else None, nrec)
+        if rc != 0:
+            raise RuntimeError(f"oracle apply failed: {rc}")
+        recs = [{f: getattr(rec[i], f) for f, _ in CnvgRecord._fields_} for i in range(min(nrec, in_iter.value))]
+        return icnvg.value, in_iter.value, recs
+
+    def apc(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.lib.or_ims_apc(self.h), shape=(self.nja,)).copy()
+
+    def iapc(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.lib.or_ims_iapc(self.h), shape=(self.neq + 1,)).copy()
+
+    def japc(self) -> np.ndarray:
+        return np.ctypeslib.as_array(self.lib.or_ims_japc(self.h), shape=(self.nja,)).copy()
+
+    def l2norm0(self) -> float:
+        return self.lib.or_ims_l2norm0(self.h)
+
+    def pivot_retries(self) -> int:
+        return self.lib.or_ims_pivot_retries(self.h)
+
+    def __del__(self):
+        try:
+            self.lib.or_ims_destroy(self.h)
+        except Exception:
+            pass
+
+
+def amux(ia, ja, a, x):
+    lib = load()
+    y = np.zeros(ia.size - 1)
+    lib.or_amux(ia.size - 1, dp(x), dp(y), dp(a), ip(ja), ip(ia))
+    return y
+
+
+def amux_fma(ia, ja, a, x):
+    lib = load()
+    y = np.zeros(ia.size - 1)
+    lib.or_amux_fma(ia.size - 1, dp(x), dp(y), dp(a), ip(ja), ip(ia))
+    return y
+
+
+def ilu0a(apc, iapc, japc, r, fma=False):
+    lib = load()
+    d = np.zeros(iapc.size - 1)
+    if fma:
+        lib.or_ilu0a_fma(iapc.size - 1, dp(apc), ip(iapc), ip(japc), dp(r), dp(d))
+    else:
+        lib.or_ilu0a(apc.size, iapc.size - 1, dp(apc), ip(iapc), ip(japc), dp(r), dp(d))
+    return d
+
+
+def dis_connect(nlay, nrow, ncol, delr, delc, top, bot) -> dict:
+    lib = load()
+    nodes, nja, njas = C.c_int(), C.c_int(), C.c_int()
+    lib.or_dis_sizes(nlay, nrow, ncol, C.byref(nodes), C.byref(nja), C.byref(njas))
+    n, nz, ns = nodes.value, nja.value, njas.value
+    out = dict(ia=np.zeros(n + 1, np.int32), ja=np.zeros(nz, np.int32), isym=np.zeros(nz, np.int32),
+               jas=np.zeros(nz, np.int32), ihc=np.zeros(ns, np.int32), cl1=np.zeros(ns),
+               cl2=np.zeros(ns), hwva=np.zeros(ns))
+    lib.or_dis_connect(nlay, nrow, ncol, dp(np.ascontiguousarray(delr, float)),
+                       dp(np.ascontiguousarray(delc, float)), dp(np.ascontiguousarray(top, float)),
+                       dp(np.ascontiguousarray(bot, float)), ip(out["ia"]), ip(out["ja"]),
+                       ip(out["isym"]), ip(out["jas"]), ip(out["ihc"]), dp(out["cl1"]),
+                       dp(out["cl2"]), dp(out["hwva"]))
+    out.update(nodes=n, nja=nz, njas=ns)
+    return out
+
+
+class Gwf:
+    """Oracle GWF model + NumericalSolution for one DIS model (a GwfDisModel)."""
+
+    def __init__(self, m, ims_settings: Settings, satomega=1.0e-6):
+        self.lib = load()
+        self.m = m
+        con = dis_connect(m.nlay, m.nrow, m.ncol, m.delr, m.delc, m.cell_top, m.cell_bot)
+        self.con = con
+        keep = {}
+
+        def d(a):
+            a = np.ascontiguousarray(a, np.float64)
+            keep[id(a)] = a
+            return dp(a)
+
+        def i(a):
+            a = np.ascontiguousarray(a, np.int32)
+            keep[id(a)] = a
+            return ip(a)
+
+        n = m.nodes
+        ss = m.ss if m.ss is not None else np.zeros(n)
+        sy = m.sy if m.sy is not None else np.zeros(n)
+        self.model = GwfModel(
+            m.nlay, m.nrow, m.ncol, n, con["nja"], con["njas"],
+            i(con["ia"]), i(con["ja"]), i(con["isym"]), i(con["jas"]), i(con["ihc"]),
+            d(con["cl1"]), d(con["cl2"]), d(con["hwva"]),
+            d(m.cell_top), d(m.cell_bot), d(m.area), d(m.k11), d(m.k33), i(m.icelltype),
+            int(m.inewton), 0, 0, 0, satomega, d(ss), d(sy), i(m.icelltype),
+            int(m.wel_node.size), i(m.wel_node), d(m.wel_q),
+            int(m.rch_node.size), i(m.rch_node), d(m.rch_rate),
+            int(m.chd_node.size), i(m.chd_node), d(m.chd_head))
+        self._keep = keep
+        self.condsat = np.zeros(con["njas"])
+        self.lib.or_npf_condsat(C.byref(self.model), dp(self.condsat))
+        self.ibound = np.ascontiguousarray(m.ibound, np.int32)
+        self.ims = Ims(ims_settings, con["ia"], con["ja"])
+        self.x = np.ascontiguousarray(m.strt, np.float64).copy()
+        self.xold = self.x.copy()
+        self._nlv = [np.zeros(n) for _ in range(4)]
+
+    def assemble(self, hnew, hold=None, delt=0.0, transient=False):
+        """gwf_fc into a zeroed amat/rhs (before the sln_ls fix-ups)."""
+        n, nja = self.m.nodes, self.con["nja"]
+        amat = np.zeros(nja)
+        rhs = np.zeros(n)
+        sat = np.zeros(n)
+        hnew = np.ascontiguousarray(hnew, np.float64)
+        hold = np.ascontiguousarray(hnew if hold is None else hold, np.float64)
+        self.lib.or_gwf_fc(C.byref(self.model), ip(self.ibound), dp(self.condsat), dp(sat), delt,
+                           int(transient), dp(hold), dp(hnew), dp(amat), dp(rhs))
+        return amat, rhs
+
+    def fixups(self, amat, rhs, x, isymmetric=True):
+        xtemp = np.zeros_like(x)
+        self.lib.or_sln_ls_fixups(x.size, ip(self.con["ia"]), ip(self.con["ja"]), ip(self.ibound),
+                                  int(isymmetric), dp(amat), dp(rhs), dp(x), dp(xtemp))
+        return amat, rhs
+
+    def timestep(self, kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-3, mxiter=25,
+                 nonmeth=0, theta=1.0, akappa=0.0, gamma=1.0, amomentum=0.0, iallowptc=1):
+        w = self._nlv
+        nl = Nonlinear(dvclose, mxiter, nonmeth, iallowptc, theta, akappa, gamma, amomentum,
+                       0.0, 0.0, 0.0, dp(w[0]), dp(w[1]), dp(w[2]), dp(w[3]))
+        st = TimestepStats()
+        rc = self.lib.or_gwf_timestep(C.byref(self.model), self.ims.h, C.byref(nl), dp(self.condsat),
+                                      ip(self.ibound), kper, kstp, delt, int(transient), dp(self.x),
+                                      dp(self.xold), C.byref(st))
+        if rc != 0:
+            raise RuntimeError(f"oracle timestep failed: {rc}")
+        return {f: getattr(st, f) for f, _ in TimestepStats._fields_}

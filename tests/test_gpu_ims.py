@@ -1,0 +1,195 @@
+"""GPU parity of the IMS linear path against the CPU oracle, through the C ABI.
+
+Bit-exact: the ILU0/MILU0 factor (ims_base_pcilu0 order, no FMA), the SpMV
+(amux order, FMA) and the preconditioner sweeps (ims_base_ilu0a order, FMA).
+Closure parity: heads within 0.1 x INNER_DVCLOSE of the oracle's IMS solve,
+inner-iteration counts within 2 (Krylov scalars are reduced in a different
+order on the GPU, so iterates differ in the last bits).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from modflow6_gb300 import _lib
+from modflow6_gb300.dis import make_config
+from modflow6_gb300.ims import ImsLinear, ImsLinearSettings
+
+pytestmark = pytest.mark.gpu
+
+
+def c1_system(isym=True, seed=0):
+    m = make_config("c1", seed=seed)
+    g = oracle.Gwf(m, oracle.settings())
+    x0 = g.x.copy()
+    for i, node in enumerate(m.chd_node):
+        x0[node] = m.chd_head[i]
+    amat, rhs = g.assemble(x0)
+    amat, rhs = g.fixups(amat, rhs, x0, isymmetric=isym)
+    return g.con, amat, rhs, x0
+
+
+def c2_small_system(scale=0.05, seed=3, isym=True):
+    m = make_config("c2", seed=seed, scale=scale)
+    g = oracle.Gwf(m, oracle.settings())
+    x0 = g.x.copy()
+    x0[m.chd_node] = m.chd_head
+    amat, rhs = g.assemble(x0)
+    amat, rhs = g.fixups(amat, rhs, x0, isymmetric=isym)
+    return m, g.con, amat, rhs, x0
+
+
+def gpu_ims(con, **kw):
+    s = ImsLinearSettings(**kw)
+    return ImsLinear(s).imslinear_allocate(con["nodes"], con["ia"], con["ja"])
+
+
+def oracle_solve(con, amat, rhs, x0, **kw):
+    s = oracle.settings(**{k: v for k, v in kw.items() if k != "precision"})
+    ims = oracle.Ims(s, con["ia"], con["ja"])
+    x = x0.copy()
+    icnvg, it, _ = ims.apply(amat.copy(), rhs.copy(), x)
+    return x, icnvg, it, ims
+
+
+@pytest.mark.parametrize("relax", [0.0, 0.97])
+def test_factor_bitexact(gblib, relax):
+    con, amat, rhs, x0 = c1_system()
+    ims = gpu_ims(con, relax=relax)
+    retries = C.c_int(-1)
+    rc = gblib.gbims_factor(ims._h, _lib.dptr(amat), C.byref(retries))
+    assert rc == 0 and retries.value == 0
+    apc = np.zeros(con["nja"])
+    assert gblib.gbims_get_apc(ims._h, _lib.dptr(apc)) == 0
+    s = oracle.settings(relax=relax)
+    o = oracle.Ims(s, con["ia"], con["ja"])
+    o.apply(amat.copy(), rhs.copy(), x0.copy())
+    np.testing.assert_array_equal(apc, o.apc())
+
+
+def test_matvec_and_precondition_bitexact(gblib):
+    m, con, amat, rhs, x0 = c2_small_system()
+    ims = gpu_ims(con)
+    assert gblib.gbims_factor(ims._h, _lib.dptr(amat), None) == 0
+    rng = np.random.default_rng(7)
+    v = rng.standard_normal(con["nodes"])
+    y = np.zeros_like(v)
+    assert gblib.gbims_matvec(ims._h, _lib.dptr(v), _lib.dptr(y)) == 0
+    np.testing.assert_array_equal(y, oracle.amux_fma(con["ia"], con["ja"], amat, v))
+    z = np.zeros_like(v)
+    assert gblib.gbims_precondition(ims._h, _lib.dptr(v), _lib.dptr(z)) == 0
+    o = oracle.Ims(oracle.settings(), con["ia"], con["ja"])
+    o.apply(amat.copy(), rhs.copy(), x0.copy())
+    np.testing.assert_array_equal(z, oracle.ilu0a(o.apc(), o.iapc(), o.japc(), v, fma=True))
+
+
+CASES = [
+    dict(ilinmeth=1),
+    dict(ilinmeth=2),
+    dict(ilinmeth=1, relax=0.97),
+    dict(ilinmeth=2, relax=0.97),
+    dict(ilinmeth=1, north=3),
+    dict(ilinmeth=2, north=2),
+    dict(ilinmeth=1, icnvgopt=2),
+    dict(ilinmeth=2, icnvgopt=4),
+]
+
+
+@pytest.mark.parametrize("kw", CASES, ids=lambda k: "-".join(f"{a}{b}" for a, b in k.items()))
+def test_solve_parity_c1(gblib, kw):
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=500)
+    con, amat, rhs, x0 = c1_system(isym=(kw["ilinmeth"] == 1))
+    xo, icnvg_o, it_o, _ = oracle_solve(con, amat, rhs, x0, **tol, **kw)
+    ims = gpu_ims(con, **tol, **kw)
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.icnvg == icnvg_o == 1
+    assert abs(r.in_iter - it_o) <= 2, (r.in_iter, it_o)
+    assert np.max(np.abs(x - xo)) <= 0.1 * tol["dvclose"]
+
+
+@pytest.mark.parametrize("ilinmeth", [1, 2])
+def test_solve_parity_c2_small(gblib, ilinmeth):
+    tol = dict(dvclose=1e-8, rclose=1e-4, iter1=1000)
+    m, con, amat, rhs, x0 = c2_small_system(isym=(ilinmeth == 1))
+    xo, icnvg_o, it_o, _ = oracle_solve(con, amat, rhs, x0, ilinmeth=ilinmeth, **tol)
+    ims = gpu_ims(con, ilinmeth=ilinmeth, **tol)
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.icnvg == icnvg_o == 1
+    assert abs(r.in_iter - it_o) <= 2, (r.in_iter, it_o)
+    assert np.max(np.abs(x - xo)) <= 0.1 * tol["dvclose"]
+
+
+@pytest.mark.parametrize("ilinmeth", [1, 2])
+def test_mixed_precision_closure(gblib, ilinmeth):
+    """FP32 matrix/factors inside FP64 refinement reach the FP64 closure."""
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=1000)
+    con, amat, rhs, x0 = c1_system(isym=(ilinmeth == 1))
+    xo, icnvg_o, it_o, _ = oracle_solve(con, amat, rhs, x0, ilinmeth=ilinmeth, **tol)
+    ims = gpu_ims(con, ilinmeth=ilinmeth, precision=_lib.GBIMS_MIXED, **tol)
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.icnvg == 1
+    # the FP64 true residual meets RCLOSE
+    resid = rhs - oracle.amux(con["ia"], con["ja"], amat, x)
+    assert np.max(np.abs(resid)) <= tol["rclose"] * 1.0001
+    assert np.max(np.abs(x - xo)) <= 0.1 * tol["dvclose"], np.max(np.abs(x - xo))
+
+
+def test_itmax_matches_oracle(gblib):
+    con, amat, rhs, x0 = c1_system()
+    xo, icnvg_o, it_o, _ = oracle_solve(con, amat, rhs, x0, dvclose=1e-12, rclose=1e-12, iter1=3)
+    ims = gpu_ims(con, dvclose=1e-12, rclose=1e-12, iter1=3)
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.in_iter == it_o == 3 and r.icnvg == icnvg_o == 0
+    assert r.summary["exit"] == "itmax"
+    np.testing.assert_allclose(x, xo, rtol=1e-10, atol=1e-10)
+
+
+def test_exact_initial_guess(gblib):
+    con, amat, rhs, x0 = c1_system()
+    ims = gpu_ims(con, dvclose=1e-8, rclose=1e-6)
+    z = np.zeros_like(x0)
+    r = ims.imslinear_apply(amat.copy(), np.zeros_like(rhs), z)
+    assert r.icnvg == 1 and r.in_iter == 0 and np.all(z == 0)
+
+
+def test_pivot_retry_matches_oracle(gblib):
+    # 3x3 with a pivot whose sign flips: ILU0 of [[1,2,0],[2,1,1],[0,1,3]]
+    ia = np.array([0, 2, 5, 7], np.int32)
+    ja = np.array([0, 1, 1, 0, 2, 2, 1], np.int32)
+    amat = np.array([1.0, 2.0, 1.0, 2.0, 1.0, 3.0, 1.0])
+    con = dict(nodes=3, nja=7, ia=ia, ja=ja)
+    ims = gpu_ims(con, ilinmeth=2)
+    retries = C.c_int(-1)
+    rc = _lib.load().gbims_factor(ims._h, _lib.dptr(amat), C.byref(retries))
+    o = oracle.Ims(oracle.settings(ilinmeth=2), ia, ja)
+    o.apply(amat.copy(), np.ones(3), np.zeros(3))
+    assert retries.value == o.pivot_retries() > 0
+    assert rc == _lib.GBIMS_WARN_PIVOT
+    apc = np.zeros(7)
+    _lib.load().gbims_get_apc(ims._h, _lib.dptr(apc))
+    np.testing.assert_array_equal(apc, o.apc())
+
+
+def test_nonfinite_rhs_is_an_error(gblib):
+    con, amat, rhs, x0 = c1_system()
+    ims = gpu_ims(con, dvclose=1e-8, rclose=1e-6)
+    bad = rhs.copy()
+    bad[17] = np.nan
+    with pytest.raises(_lib.GbimsError) as e:
+        ims.imslinear_apply(amat.copy(), bad, x0.copy())
+    assert e.value.status == _lib.GBIMS_ERR_NONFINITE
+
+
+def test_repeated_apply_is_reproducible(gblib):
+    con, amat, rhs, x0 = c1_system()
+    ims = gpu_ims(con, dvclose=1e-8, rclose=1e-6, iter1=500)
+    xa, xb = x0.copy(), x0.copy()
+    ra = ims.imslinear_apply(amat.copy(), rhs.copy(), xa)
+    rb = ims.imslinear_apply(amat.copy(), rhs.copy(), xb)
+    assert ra.in_iter == rb.in_iter
+    np.testing.assert_array_equal(xa, xb)

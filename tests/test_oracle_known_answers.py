@@ -1,0 +1,74 @@
+"""Pins the CPU oracle to the known answers held by the reference's own tests.
+
+* autotest/test_gwf_chd01.py:13-127: 1x1x100 confined column, CHD 1.0 and 0.0
+  at the ends, CG, inner/outer dvclose 1e-6, rclose 1e-6; answer
+  np.linspace(1, 0, 100) (:126-127).
+* autotest/test_gwf_newton01.py:8-103: 2x3x3 convertible Newton model, CHD 7
+  in layer 2, recharge 1 on layer 1; answers H1 = 8.0 at (0,1,1) and
+  H2 = 7.0 at (1,1,1) (:95-103).  The reference runs COMPLEXITY COMPLEX
+  (BiCGSTAB + ILUT); the IMS path built here is ILU0, so the case is run with
+  PRECONDITIONER_LEVELS 0 / DROP_TOLERANCE 0 (BiCGSTAB + ILU0), which must
+  reach the same heads.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from modflow6_gb300.dis import GwfDisModel
+
+
+def chd01_model():
+    nlay, nrow, ncol = 1, 1, 100
+    m = GwfDisModel(nlay, nrow, ncol, np.ones(ncol), np.ones(nrow), np.ones(ncol), np.zeros(ncol),
+                    np.ones(ncol), np.ones(ncol), np.zeros(ncol, np.int32), np.ones(ncol))
+    m.chd_node = np.array([0, 99], np.int32)
+    m.chd_head = np.array([1.0, 0.0])
+    return m
+
+
+def newton01_model():
+    nlay, nrow, ncol = 2, 3, 3
+    nrc = nrow * ncol
+    m = GwfDisModel(nlay, nrow, ncol, np.ones(ncol), np.ones(nrow), np.full(nrc, 20.0),
+                    np.concatenate([np.full(nrc, 10.0), np.zeros(nrc)]), np.full(2 * nrc, 10.0),
+                    np.full(2 * nrc, 10.0), np.ones(2 * nrc, np.int32), np.full(2 * nrc, 7.0),
+                    inewton=1)
+    m.chd_node = np.arange(nrc, 2 * nrc, dtype=np.int32)
+    m.chd_head = np.full(nrc, 7.0)
+    m.rch_node = np.arange(nrc, dtype=np.int32)
+    m.rch_rate = np.ones(nrc)
+    return m
+
+
+def test_chd01_linspace():
+    m = chd01_model()
+    s = oracle.settings(dvclose=1e-6, rclose=1e-6, iter1=300, ilinmeth=1)
+    g = oracle.Gwf(m, s)
+    st = g.timestep(kper=1, kstp=1, delt=5.0, transient=False, dvclose=1e-6, mxiter=100)
+    assert st["converged"] == 1
+    np.testing.assert_allclose(g.x, np.linspace(1, 0, 100), rtol=1e-5, atol=1e-8)
+
+
+@pytest.mark.parametrize("ilinmeth", [1, 2])
+def test_chd01_both_accelerators(ilinmeth):
+    m = chd01_model()
+    s = oracle.settings(dvclose=1e-9, rclose=1e-9, iter1=300, ilinmeth=ilinmeth)
+    g = oracle.Gwf(m, s)
+    st = g.timestep(kper=1, kstp=1, delt=5.0, dvclose=1e-9, mxiter=100)
+    assert st["converged"] == 1
+    np.testing.assert_allclose(g.x, np.linspace(1, 0, 100), atol=1e-7)
+
+
+def test_newton01_h1_h2():
+    m = newton01_model()
+    # COMPLEX preset (ImsLinearSettings.f90:100-111, sln_setouter :2657-2669)
+    # with ILU0 in place of ILUT and the test's dvclose 1e-9.
+    s = oracle.settings(dvclose=1e-9, rclose=0.1, iter1=500, ilinmeth=2, north=2)
+    g = oracle.Gwf(m, s)
+    st = g.timestep(kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-9, mxiter=100,
+                    nonmeth=3, theta=0.8, akappa=1e-4, gamma=0.0, amomentum=0.0)
+    assert st["converged"] == 1
+    h1 = g.x[0 * 9 + 1 * 3 + 1]
+    h2 = g.x[1 * 9 + 1 * 3 + 1]
+    assert np.isclose(h1, 8.0), h1
+    assert np.isclose(h2, 7.0), h2
