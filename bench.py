@@ -1,0 +1,396 @@
+#!/usr/bin/env python
+"""Benchmark: 10M-cell steady-state solve time to IMS closure on one GB300.
+
+Workload (1000x1000x10 DIS, 7-point, 10,000,000 cells, 67,960,000 nonzeros):
+per-layer lognormal Kh (ln K ~ N(0, 1.5^2), 20-cell correlation), Kv = 0.1 Kh,
+CHD 20 m / 0 m on the west / east faces, 5,000 wells U(-500, -50) m3/d,
+seeded synthetic data.  PCG + ILU0, INNER_DVCLOSE 1e-6 m, INNER_RCLOSE 1e-2,
+OUTER_DVCLOSE 1e-6 m.
+
+A step is one steady-state time step from the initial heads to closure: the
+NumericalSolution outer loop (fill, sln_ls fix-ups, IMS solve, dxmax) until
+OUTER_DVCLOSE holds.  `value` is the device-resident plain FP64 drop-in
+(inputs in HBM); `mixed_s` the FP32-matrix/FP64-refinement form; `e2e` the
+same FP64 step driven through the C ABI with host buffers (gbims_apply:
+amat, rhs and x copied host->device, x copied back, every outer iteration).
+
+--impl reference times the CPU restatement of the reference's IMS (the
+oracle; MODFLOW 6 itself is Fortran and no Fortran compiler exists on either
+machine) on a bounded sample of the same workload, on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "10M-cell solve time to IMS closure: FP64 vs mixed vs warm-start; SpMV HBM GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb", choices=["gb", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="grid scale (1.0 = 1000x1000x10)")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    lrank = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, lrank
+
+
+def workload_config(a, m):
+    from modflow6_gb300.workloads import C2_IMS, C2_OUTER
+    return {"workload": f"DIS {m.nlay}x{m.nrow}x{m.ncol} confined steady state (10M-cell case)"
+            if a.scale == 1.0 else f"DIS {m.nlay}x{m.nrow}x{m.ncol} (scaled {a.scale})",
+            "cells": m.nodes, "nonzeros": int(m.nodes + 2 * (m.nlay * m.nrow * (m.ncol - 1)
+                                                            + m.nlay * (m.nrow - 1) * m.ncol
+                                                            + (m.nlay - 1) * m.nrow * m.ncol)),
+            "accelerator": "PCG", "preconditioner": "ILU0", "inner_dvclose": C2_IMS["dvclose"],
+            "inner_rclose": C2_IMS["rclose"], "outer_dvclose": C2_OUTER["dvclose"],
+            "wells": int(m.wel_node.size), "seed": a.seed,
+            "l2_flush": "inputs larger than L2 (amat alone 544 MB vs 129 MB L2)"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.p = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+        return self
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return {}
+    return {}
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement (oracle): bounded sample, scaled to a solve to closure
+# ---------------------------------------------------------------------------
+def cpu_sample(m, inner_total: int, outer: int, budget_s: float = 25.0) -> dict:
+    """Times the oracle's IMS (PCG + ILU0, 1 core) on the same system: setup
+    (ILU0 factor + initial residual) and a few inner iterations, then scales
+    to outer * setup + inner_total * per-iteration."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    from modflow6_gb300.workloads import C2_IMS
+
+    t0 = time.perf_counter()
+    g = oracle.Gwf(m, oracle.settings(**C2_IMS))
+    x0 = g.x.copy()
+    x0[m.chd_node] = m.chd_head
+    amat, rhs = g.assemble(x0)
+    t_fill = time.perf_counter() - t0
+    amat, rhs = g.fixups(amat, rhs, x0, isymmetric=True)
+
+    def run(iters):
+        s = dict(C2_IMS)
+        s["iter1"] = iters
+        s["dvclose"] = 0.0
+        s["rclose"] = 1e-300
+        ims = oracle.Ims(oracle.settings(**s), g.con["ia"], g.con["ja"])
+        x = x0.copy()
+        t = time.perf_counter()
+        ims.apply(amat.copy(), rhs.copy(), x)
+        return time.perf_counter() - t
+
+    k1 = 2
+    t1 = run(k1)
+    per_guess = max(t1 / (k1 + 2), 1e-6)
+    k2 = k1 + max(3, min(40, int((budget_s - t1) / per_guess / 2)))
+    t2 = run(k2)
+    t_iter = max((t2 - t1) / (k2 - k1), 1e-9)
+    t_setup = max(t1 - k1 * t_iter, 0.0)
+    est = outer * (t_fill + t_setup) + inner_total * t_iter
+    return {"value": est, "unit": "s", "cores": 1, "kind": "port",
+            "sample": (f"oracle C restatement of IMS (gcc -O2, 1 thread) on the same system: "
+                       f"fill {t_fill:.2f}s, ILU0 factor + residual {t_setup:.2f}s, "
+                       f"{t_iter:.3f}s per PCG iteration from {k1}- and {k2}-iteration runs; "
+                       f"scaled to {outer} outer x (fill + setup) + {inner_total} inner iterations"),
+            "t_iter_s": t_iter, "t_setup_s": t_setup, "t_fill_s": t_fill}
+
+
+def reference_arm(a):
+    from modflow6_gb300.dis import make_config
+    ws, rank, _ = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    m = make_config("c2", seed=a.seed, scale=a.scale)
+    fx = ROOT / "tests" / "golden" / "c2_oracle_reference.json"
+    inner, outer, src = None, None, ""
+    if fx.exists() and a.scale == 1.0:
+        d = json.loads(fx.read_text())
+        inner, outer = int(d["stats"]["inner_total"]), int(d["stats"]["outer"])
+        src = f"inner/outer iteration counts of the oracle's own full solve ({fx.name})"
+    if inner is None:
+        inner, outer, src = 1000, 2, "assumed 1000 inner / 2 outer iterations (no full-solve record)"
+    vals = []
+    cb = None
+    for _ in range(a.warmup + a.steps):
+        cb = cpu_sample(m, inner, outer, budget_s=max(5.0, 60.0 / max(1, a.warmup + a.steps)))
+        vals.append(cb["value"])
+    v = float(np.mean(vals[a.warmup:])) if a.steps else float(vals[-1])
+    cb["value"] = v
+    cb["sample"] += "; " + src
+    line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(a, m), "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GB300 arm
+# ---------------------------------------------------------------------------
+def gb_arm(a):
+    import torch
+
+    ws, rank, lrank = dist_env()
+    torch.cuda.set_device(lrank)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from modflow6_gb300 import _lib, build
+    build.build()
+    from modflow6_gb300.dis import make_config
+    from modflow6_gb300.ims import ImsLinear, ImsLinearSettings
+    from modflow6_gb300.solution import GwfSolution, Nonlinear, sln_ls_fixups
+    from modflow6_gb300.workloads import C2_IMS, C2_OUTER
+    import ctypes as C
+
+    lib = _lib.load()
+    m = make_config("c2", seed=a.seed, scale=a.scale)
+    shape = (m.nlay, m.nrow, m.ncol)
+    nl = Nonlinear(dvclose=C2_OUTER["dvclose"], mxiter=C2_OUTER["mxiter"])
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def maxr(v):
+        if ws > 1:
+            t = torch.tensor([v], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return v
+
+    def run_form(precision, clocks=False):
+        sol = GwfSolution(m, ImsLinearSettings(precision=precision, structure=shape, **C2_IMS), nl)
+        stats = []
+        for _ in range(a.warmup):
+            sol.restart()
+            st = sol.timestep(1, 1, 1.0)
+            assert st["converged"] == 1, st
+        ims_h = sol.ims_handle()
+        l0 = lib.gbims_kernel_launches(ims_h)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        sampler = ClockSampler(lrank) if clocks else None
+        if sampler:
+            sampler.__enter__()
+        e0.record()
+        for _ in range(a.steps):
+            sol.restart()
+            stats.append(sol.timestep(1, 1, 1.0))
+        e1.record()
+        barrier()
+        if sampler:
+            sampler.__exit__(None, None, None)
+        ms = e0.elapsed_time(e1) / max(1, a.steps)
+        launches = lib.gbims_kernel_launches(ims_h) - l0
+        # per-step kernels outside the IMS handle: memsets excluded; npf_cf, fill,
+        # fix-ups, dxmax per outer iteration, CHD reset per step
+        launches += sum(4 * s["outer"] + 1 for s in stats)
+        heads = sol.heads
+        return sol, ms, stats, launches, sampler.summary() if sampler else None, heads
+
+    sol64, ms64, st64, launches64, clocks, h64 = run_form(_lib.GBIMS_FP64, clocks=True)
+    ms64 = maxr(ms64)
+    # per-kernel device times (CUDA events on the library stream) for the roofline
+    kt = _lib.GbimsKernelTimes()
+    rc = lib.gbims_time_kernels(sol64.ims_handle(), 20, C.byref(kt))
+    assert rc == 0, rc
+    peak, peak_kind = measured_peaks()
+    spmv_gbs = kt.spmv_bytes / (kt.spmv_ms * 1e-3) / 1e9
+    pre_gbs = kt.precond_bytes / (kt.precond_ms * 1e-3) / 1e9
+    traffic = ncu_traffic()
+    mixed = None
+    if not a.no_mixed:
+        solm, msm, stm, lm, _, hm = run_form(_lib.GBIMS_MIXED)
+        msm = maxr(msm)
+        ktm = _lib.GbimsKernelTimes()
+        lib.gbims_time_kernels(solm.ims_handle(), 20, C.byref(ktm))
+        mixed = {"value": msm / 1e3, "unit": "s", "inner_iterations": stm[-1]["inner_total"],
+                 "outer_iterations": stm[-1]["outer"],
+                 "max_head_diff_vs_fp64": float(np.max(np.abs(hm - h64))),
+                 "spmv_fp32_gbs": ktm.spmv_bytes / (ktm.spmv_ms * 1e-3) / 1e9,
+                 "precond_fp32_ms": ktm.precond_ms, "spmv_fp32_ms": ktm.spmv_ms}
+        solm.close()
+    # e2e: the same FP64 step through the C ABI with host buffers
+    e2e = None
+    if not a.no_e2e:
+        con = m.connections()
+        ia, ja = con["ia"], con["ja"]
+        amat0, rhs0 = sol64.formulate(0.0)  # assembled on the GPU, outside the timed region
+        x0 = m.strt.copy()
+        x0[m.chd_node] = m.chd_head
+        amat_h, rhs_h = sln_ls_fixups(ia, ja, m.ibound, amat0, rhs0, x0, isymmetric=True)
+        pin = lambda arr: torch.from_numpy(arr).pin_memory()
+        t_amat, t_rhs = pin(amat_h), pin(rhs_h)
+        t_x = pin(x0.copy())
+        ims = ImsLinear(ImsLinearSettings(structure=shape, **C2_IMS)).imslinear_allocate(m.nodes, ia, ja)
+        active = m.ibound > 0
+        amat_p = C.cast(t_amat.data_ptr(), C.POINTER(C.c_double))
+        rhs_p = C.cast(t_rhs.data_ptr(), C.POINTER(C.c_double))
+        x_p = C.cast(t_x.data_ptr(), C.POINTER(C.c_double))
+        xv = t_x.numpy()
+
+        def e2e_step():
+            xv[:] = x0
+            outer = 0
+            for kiter in range(1, nl.mxiter + 1):
+                xtemp = xv.copy()
+                ic, it = C.c_int(), C.c_int()
+                rc = lib.gbims_apply(ims._h, amat_p, rhs_p, x_p, 1, kiter, C.byref(ic), C.byref(it), None)
+                assert rc >= 0, lib.gbims_last_error(ims._h)
+                outer = kiter
+                if np.max(np.abs((xv - xtemp)[active])) <= nl.dvclose:
+                    break
+            return outer
+
+        for _ in range(min(a.warmup, 1)):
+            e2e_step()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        outers = [e2e_step() for _ in range(a.steps)]
+        e1.record()
+        barrier()
+        ms_e2e = maxr(e0.elapsed_time(e1) / max(1, a.steps))
+        no = float(np.mean(outers))
+        e2e = {"value": ms_e2e / 1e3, "unit": "s",
+               "h2d_bytes_per_step": int(no * (amat_h.nbytes + rhs_h.nbytes + x0.nbytes)),
+               "d2h_bytes_per_step": int(no * x0.nbytes),
+               "path": "gbims_apply (C ABI, pinned host amat/rhs/x) per outer iteration"}
+        ims.imslinear_da()
+    last = st64[-1]
+    line = {
+        "metric": METRIC, "value": ms64 / 1e3, "unit": "s", "n_gpus": ws, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms64, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lognormal K, CHD, WEL)",
+        "config": workload_config(a, m),
+        "inner_iterations": last["inner_total"], "outer_iterations": last["outer"],
+        "device_ms_per_step": float(np.mean([s["total_ms"] for s in st64])),
+        "fill_ms_per_step": float(np.mean([s["fill_ms"] for s in st64])),
+        "mixed": mixed, "mixed_s": mixed["value"] if mixed else None, "warmstart_s": None,
+        "spmv_gbs": spmv_gbs,
+        "roofline": {"kernel": "k_sell_spmv<double> (FP64 SpMV, SELL-32)", "bound": "hbm",
+                     "achieved": spmv_gbs, "peak": peak, "unit": "GB/s", "frac": spmv_gbs / peak,
+                     "peak_kind": f"{peak_kind} copy bandwidth",
+                     "algorithmic_bytes_per_launch": kt.spmv_bytes, "launch_ms": kt.spmv_ms,
+                     "traffic": traffic.get("spmv_fp64_bytes_per_launch")},
+        "kernels": {"spmv_ms": kt.spmv_ms, "spmv_gbs": spmv_gbs, "precond_ms": kt.precond_ms,
+                    "precond_gbs": pre_gbs, "dot_ms": kt.dot_ms, "update_ms": kt.update_ms},
+        "e2e": e2e, "gpu_launches": int(launches64), "clocks": clocks,
+    }
+    if rank == 0 and not a.no_cpu:
+        line["cpu_baseline"] = cpu_sample(m, last["inner_total"], last["outer"])
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        reference_arm(a)
+    else:
+        gb_arm(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -112,10 +112,24 @@ int gbims_destroy(gbims_handle *h);
  *                     the last gbims_factor or apply;
  *  gbims_precondition z = M^-1 r, ims_base_ilu0a (ImsLinearBase.f90:1049-1092),
  *                     with the last factor (FP32 factors in GBIMS_MIXED). */
+/* Per-kernel device times (ms per launch, CUDA events on the library's
+ * stream, averaged over reps launches after one warm-up) of the last factor:
+ * the SpMV, the preconditioner (forward+backward sweeps), a dot product and
+ * the x/residual update, in the handle's precision. */
+typedef struct gbims_kernel_times {
+  double spmv_ms, precond_ms, dot_ms, update_ms;
+  double spmv_bytes, precond_bytes; /* algorithmic bytes per launch */
+} gbims_kernel_times;
+int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times *t);
+
 int gbims_factor(gbims_handle *h, const double *amat, int *pivot_retries);
 int gbims_get_apc(gbims_handle *h, double *apc);
 int gbims_matvec(gbims_handle *h, const double *x, double *y);
 int gbims_precondition(gbims_handle *h, const double *r, double *z);
+
+/* Kernels this handle has launched so far (loop bodies of the inner-loop
+ * graph counted once per executed body). */
+long long gbims_kernel_launches(const gbims_handle *h);
 
 /* Message of the last error on this handle (never NULL). */
 const char *gbims_last_error(const gbims_handle *h);
@@ -203,9 +217,20 @@ typedef struct gbsln_stats {
 int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,
                  const gbims_settings *ims, const gbsln_nonlinear *nl,
                  const double *strt, gbsln_handle **out);
-/* One time step (prepareSolve + outer loop + finalize).  delt <= 0 means a
- * steady-state step (no storage). */
+/* One time step (prepareSolve + outer loop).  The step is transient when the
+ * model has ss/sy and delt > 0, steady state otherwise; delt is also the
+ * step length used by the pseudo-transient continuation default
+ * (gwf.f90:625-687). */
 int gbsln_timestep(gbsln_handle *h, int kper, int kstp, double delt, gbsln_stats *st);
+/* sln_buildsystem at the current heads (hold: previous-step heads, needed for
+ * a transient step): the assembled amat (nja, CSR order of the DIS grid) and
+ * rhs before the sln_ls fix-ups, copied to the host.  The reference writes
+ * the same system with its itestmat switch (NumericalSolution.f90:2581-2599). */
+int gbsln_formulate(gbsln_handle *h, double delt, const double *hold, double *amat, double *rhs);
+const char *gbsln_last_error(const gbsln_handle *h);
+/* Restores the initial heads (IC STRT) on the device: the state at the start
+ * of the simulation, for repeated runs of the same model. */
+int gbsln_restart(gbsln_handle *h);
 int gbsln_get_heads(gbsln_handle *h, double *x);
 int gbsln_set_heads(gbsln_handle *h, const double *x);
 gbims_handle *gbsln_ims(gbsln_handle *h);

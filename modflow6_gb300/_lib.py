@@ -48,6 +48,11 @@ class GbimsSummary(C.Structure):
     ]
 
 
+class GbimsKernelTimes(C.Structure):
+    _fields_ = [("spmv_ms", C.c_double), ("precond_ms", C.c_double), ("dot_ms", C.c_double),
+                ("update_ms", C.c_double), ("spmv_bytes", C.c_double), ("precond_bytes", C.c_double)]
+
+
 class GbnpfOptions(C.Structure):
     _fields_ = [
         ("inewton", C.c_int), ("ivarcv", C.c_int), ("idewatcv", C.c_int),
@@ -88,10 +93,12 @@ _SIGS = {
     "gbims_apply": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int, _ip, _ip, C.POINTER(GbimsSummary)]),
     "gbims_apply_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, _ip, _ip, C.POINTER(GbimsSummary)]),
     "gbims_destroy": (C.c_int, [C.c_void_p]),
+    "gbims_time_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "gbims_factor": (C.c_int, [C.c_void_p, _dp, _ip]),
     "gbims_get_apc": (C.c_int, [C.c_void_p, _dp]),
     "gbims_matvec": (C.c_int, [C.c_void_p, _dp, _dp]),
     "gbims_precondition": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "gbims_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "gbims_last_error": (C.c_char_p, [C.c_void_p]),
     "gbims_status_string": (C.c_char_p, [C.c_int]),
     "gbnpf_create": (C.c_int, [C.POINTER(GbnpfOptions), C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _ip, _ip,
@@ -102,6 +109,9 @@ _SIGS = {
     "gbsln_create": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbnpfOptions), C.POINTER(GbimsSettings),
                                C.POINTER(GbslnNonlinear), _dp, C.POINTER(C.c_void_p)]),
     "gbsln_timestep": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.POINTER(GbslnStats)]),
+    "gbsln_formulate": (C.c_int, [C.c_void_p, C.c_double, _dp, _dp, _dp]),
+    "gbsln_last_error": (C.c_char_p, [C.c_void_p]),
+    "gbsln_restart": (C.c_int, [C.c_void_p]),
     "gbsln_get_heads": (C.c_int, [C.c_void_p, _dp]),
     "gbsln_set_heads": (C.c_int, [C.c_void_p, _dp]),
     "gbsln_ims": (C.c_void_p, [C.c_void_p]),

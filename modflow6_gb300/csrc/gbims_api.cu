@@ -48,6 +48,8 @@ struct gbims_handle {
   bool graph_tried = false, graph_ok = false;
   double refine_factor = 1.0e-5;
   bool factored = false;
+  long long launches = 0;  // kernels launched by this handle (graph bodies counted per body)
+  int body_kernels = 0;    // kernel nodes in one inner-loop body
   std::string err;
 };
 
@@ -187,6 +189,16 @@ static bool build_graph(gbims_handle *h) {
     cudaGraphDestroy(g);
     cudaGetLastError();
     return false;
+  }
+  // kernel nodes per loop body, for the launch count
+  size_t nn = 0;
+  cudaGraphGetNodes(body, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn) cudaGraphGetNodes(body, nodes.data(), &nn);
+  h->body_kernels = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType ty;
+    if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) h->body_kernels++;
   }
   cudaGraphExec_t exec = nullptr;
   if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) {
@@ -382,6 +394,7 @@ static int factor_core(gbims_handle *h) {
   const int n = h->n;
   cudaStream_t st = h->st;
   launch_sell_fill(h->S, h->d_amat, st);
+  h->launches += 1;
   int ipcflag = 0, icount = 0;
   double delta = 0.0;
   for (;;) {
@@ -392,6 +405,7 @@ static int factor_core(gbims_handle *h) {
     GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
     launch_ilu_factor(n, h->d_ia, h->d_ja, h->d_amat, h->d_iapc, h->d_japc, h->d_apc, h->F,
                       h->s.relax, delta, ipcflag, h->d_ctl, st);
+    h->launches += h->F.nlev;
     GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     GB_CUDA(h, cudaStreamSynchronize(st));
     GB_CUDA(h, cudaGetLastError());
@@ -408,6 +422,7 @@ static int factor_core(gbims_handle *h) {
   }
   if (h->mixed) kr_f64_to_f32(h->nja, h->d_apc, h->d_apc32, st);
   if (h->structured) launch_dia7_extract(h->D, n, h->d_iapc, h->d_japc, h->d_apc, h->mixed, st);
+  h->launches += (h->mixed ? 1 : 0) + (h->structured ? 1 : 0);
   GB_CUDA(h, cudaGetLastError());
   h->factored = true;
   return icount;
@@ -473,6 +488,8 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
   GB_CUDA(h, cudaStreamSynchronize(st));
   GB_CUDA(h, cudaGetLastError());
   const Ctl &r = *h->h_ctl;
+  // zero, residual, sum of squares, L2NORM0 control (+ FP32 copy), then the loop bodies
+  h->launches += 4 + (h->mixed ? 1 : 0) + (long long)h->body_kernels * r.bodies;
   int iters = (r.l2norm0 == 0.0 || h->s.iter1 <= 0) ? 0 : r.iter;
   *icnvg = r.icnvg;
   *in_iter = iters;
@@ -586,6 +603,58 @@ extern "C" int gbims_precondition(gbims_handle *h, const double *r, double *z) {
   return GBIMS_OK;
 }
 
+extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times *t) {
+  if (!h || !t || reps <= 0) return GBIMS_ERR_ARG;
+  if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no factor: call gbims_factor or gbims_apply first");
+  const int n = h->n;
+  cudaStream_t st = h->st;
+  Ctl c;
+  memset(&c, 0, sizeof(c));
+  c.pivot_fail = INT_MAX;
+  c.alpha = 1.0e-30;  // keeps x unchanged to rounding in the update timing
+  *h->h_ctl = c;
+  GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+  int eg = std::min(4 * kNumSM, (n + 255) / 256);
+  // deterministic, finite operands
+  if (!h->mixed) {
+    k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
+    GB_CUDA(h, cudaMemcpyAsync(h->v_p, h->d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  } else {
+    kr_f64_to_f32(n, h->d_x, h->f_p, st);
+    GB_CUDA(h, cudaMemsetAsync(h->f_q, 0, sizeof(float) * n, st));
+    GB_CUDA(h, cudaMemsetAsync(h->f_d, 0, sizeof(float) * n, st));
+  }
+  auto time_it = [&](auto &&fn) -> double {
+    fn();
+    cudaEventRecord(h->ev0, st);
+    for (int r = 0; r < reps; ++r) fn();
+    cudaEventRecord(h->ev1, st);
+    cudaEventSynchronize(h->ev1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    return ms / reps;
+  };
+  if (!h->mixed) {
+    t->spmv_ms = time_it([&] { launch_spmv64(h->S, h->v_p, h->v_q, h->d_ctl, st); });
+    t->precond_ms = time_it([&] { precond64(h, h->v_p, h->v_z); });
+    t->dot_ms = time_it([&] { kr_dot64(n, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
+    t->update_ms = time_it([&] { kr_cg_update64(n, h->v_z, h->v_d, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
+  } else {
+    t->spmv_ms = time_it([&] { launch_spmv32(h->S, h->f_p, h->f_q, h->d_ctl, st); });
+    t->precond_ms = time_it([&] { precond32(h, h->f_p, h->f_z); });
+    t->dot_ms = time_it([&] { kr_dot32(n, h->f_p, h->f_q, h->d_part, h->G, h->d_ctl, st); });
+    t->update_ms = time_it([&] { kr_cg_update_mixed(n, h->v_d, h->f_d, h->f_p, h->f_q, h->d_part, h->G, h->d_ctl, st); });
+  }
+  GB_CUDA(h, cudaGetLastError());
+  // algorithmic bytes: CSR values + column indices + row pointers, x read
+  // once, y written once; preconditioner: APC + JAPC + IAPC, r read, z
+  // written, plus one intermediate vector written and read back.
+  double vb = h->mixed ? 4.0 : 8.0;
+  t->spmv_bytes = (vb + 4.0) * h->nja + 4.0 * (n + 1) + 2.0 * vb * n;
+  t->precond_bytes = (vb + 4.0) * h->nja + 4.0 * (n + 1) + 4.0 * vb * n;
+  return GBIMS_OK;
+}
+
 extern "C" int gbims_destroy(gbims_handle *h) {
   if (!h) return GBIMS_OK;
   if (h->st) cudaStreamSynchronize(h->st);
@@ -609,6 +678,8 @@ extern "C" int gbims_destroy(gbims_handle *h) {
   return GBIMS_OK;
 }
 
+extern "C" long long gbims_kernel_launches(const gbims_handle *h) { return h ? h->launches : 0; }
+
 extern "C" const char *gbims_last_error(const gbims_handle *h) {
   if (!h) return "null handle";
   return h->err.c_str();
@@ -628,7 +699,18 @@ extern "C" const char *gbims_status_string(int status) {
   }
 }
 
-// Accessors used by the device-resident solution (gbsln_*).
+// Accessors used by the device-resident solution (gbsln_*): the solution
+// assembles straight into the IMS handle's amat/rhs and keeps x there.
 namespace gb {
-double *ims_device_x(gbims_handle *h) { return h->d_x; }
+void ims_buffers(gbims_handle *h, double **amat, double **rhs, double **x) {
+  *amat = h->d_amat;
+  *rhs = h->d_rhs;
+  *x = h->d_x;
 }
+cudaStream_t ims_stream(gbims_handle *h) { return h->st; }
+int ims_apply_inplace(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_iter,
+                      gbims_summary *summary) {
+  return apply_core(h, kstp, kiter, icnvg, in_iter, summary);
+}
+const char *ims_error(gbims_handle *h) { return h->err.c_str(); }
+}  // namespace gb

@@ -141,4 +141,11 @@ void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *c
 void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
                          cudaStream_t st);
 
+// IMS handle internals shared with the device-resident solution.
+void ims_buffers(gbims_handle *h, double **amat, double **rhs, double **x);
+cudaStream_t ims_stream(gbims_handle *h);
+int ims_apply_inplace(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_iter,
+                      gbims_summary *summary);
+const char *ims_error(gbims_handle *h);
+
 }  // namespace gb

@@ -1,25 +1,648 @@
-// gbsln_api.cu -- NPF fill and device-resident solution (C ABI).
+// gbsln_api.cu -- NPF fill and the device-resident solution (C ABI).
+//
+// gbnpf_*: the NPF package's fill (npf_cf/npf_fc/npf_fn, gwf-npf.f90:444-698)
+//          on caller-owned device arrays.
+// gbsln_*: one GWF DIS model and its NumericalSolution outer loop
+//          (NumericalSolution.f90:1482-1837) with x, amat and rhs resident in
+//          HBM: prepareSolve (gwf_ad, chd_ad), sln_buildsystem (the fill),
+//          sln_calc_ptc, sln_ls (fix-ups, pseudo-transient continuation, IMS
+//          apply), sln_get_dxmax, sln_underrelax and npf_nur.  The host only
+//          reads back a few scalars per outer iteration.
 #include "gbims_internal.cuh"
+#include "k_gwf.cuh"
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
 
-extern "C" int gbnpf_create(const gbnpf_options *, int, int, int, const int *, const int *,
-                            const int *, const int *, const int *, const double *,
-                            const double *, const double *, const double *, const double *,
-                            const double *, const double *, const int *, gbnpf_handle **out) {
-  if (out) *out = nullptr;
-  return GBIMS_ERR_UNSUPPORTED;
+using namespace gb;
+
+namespace {
+
+template <typename T>
+cudaError_t up(T **d, const T *h, size_t n) {
+  *d = nullptr;
+  cudaError_t e = cudaMalloc((void **)d, sizeof(T) * std::max<size_t>(n, 1));
+  if (e != cudaSuccess || n == 0 || !h) return e;
+  return cudaMemcpy(*d, h, sizeof(T) * n, cudaMemcpyHostToDevice);
 }
-extern "C" int gbnpf_fill(gbnpf_handle *, const int *, const double *, double *, double *) {
-  return GBIMS_ERR_UNSUPPORTED;
+
+// Full-grid DIS connectivity (Connections.f90:463-698 with the JA sort of
+// Sparse.f90:217-239 and fillisym/filljas :1205-1268), 0-based.
+struct Conn {
+  std::vector<int> ia, ja, isym, jas, ihc;
+  std::vector<double> cl1, cl2, hwva;
+  int njas = 0;
+};
+
+void build_connections(int nlay, int nrow, int ncol, const double *delr, const double *delc,
+                       const std::vector<double> &top, const std::vector<double> &bot, Conn &c) {
+  const long long nrc = (long long)nrow * ncol;
+  const int n = (int)(nlay * nrc);
+  c.ia.assign(n + 1, 0);
+  c.ja.clear();
+  c.ja.reserve((size_t)n * 7);
+  for (int k = 0; k < nlay; ++k)
+    for (int i = 0; i < nrow; ++i)
+      for (int j = 0; j < ncol; ++j) {
+        int p = (int)(j + (long long)i * ncol + k * nrc);
+        c.ia[p] = (int)c.ja.size();
+        c.ja.push_back(p);
+        if (k > 0) c.ja.push_back((int)(p - nrc));
+        if (i > 0) c.ja.push_back(p - ncol);
+        if (j > 0) c.ja.push_back(p - 1);
+        if (j < ncol - 1) c.ja.push_back(p + 1);
+        if (i < nrow - 1) c.ja.push_back(p + ncol);
+        if (k < nlay - 1) c.ja.push_back((int)(p + nrc));
+      }
+  c.ia[n] = (int)c.ja.size();
+  const size_t nja = c.ja.size();
+  c.isym.assign(nja, -1);
+  c.jas.assign(nja, -1);
+  for (int p = 0; p < n; ++p)
+    for (int q = c.ia[p]; q < c.ia[p + 1]; ++q) {
+      int m = c.ja[q];
+      if (m == p) { c.isym[q] = q; continue; }
+      for (int r = c.ia[m]; r < c.ia[m + 1]; ++r)
+        if (c.ja[r] == p) { c.isym[q] = r; break; }
+    }
+  int ipos = 0;
+  for (int p = 0; p < n; ++p)
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q)
+      if (c.ja[q] > p) c.jas[q] = ipos++;
+  for (int p = 0; p < n; ++p)
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q)
+      if (c.ja[q] < p) c.jas[q] = c.jas[c.isym[q]];
+  c.njas = ipos;
+  c.ihc.assign(ipos, 0);
+  c.cl1.assign(ipos, 0.0);
+  c.cl2.assign(ipos, 0.0);
+  c.hwva.assign(ipos, 0.0);
+  int s = 0;
+  for (int k = 0; k < nlay; ++k)
+    for (int i = 0; i < nrow; ++i)
+      for (int j = 0; j < ncol; ++j) {
+        long long p = j + (long long)i * ncol + k * nrc;
+        if (j < ncol - 1) { c.ihc[s] = 1; c.cl1[s] = 0.5 * delr[j]; c.cl2[s] = 0.5 * delr[j + 1]; c.hwva[s] = delc[i]; ++s; }
+        if (i < nrow - 1) { c.ihc[s] = 1; c.cl1[s] = 0.5 * delc[i]; c.cl2[s] = 0.5 * delc[i + 1]; c.hwva[s] = delr[j]; ++s; }
+        if (k < nlay - 1) {
+          long long m = p + nrc;
+          c.ihc[s] = 0; c.cl1[s] = 0.5 * (top[p] - bot[p]); c.cl2[s] = 0.5 * (top[m] - bot[m]);
+          c.hwva[s] = delr[j] * delc[i]; ++s;
+        }
+      }
 }
-extern "C" int gbnpf_get_condsat(gbnpf_handle *, double *) { return GBIMS_ERR_UNSUPPORTED; }
-extern "C" int gbnpf_destroy(gbnpf_handle *) { return GBIMS_OK; }
-extern "C" int gbsln_create(const gbsln_model *, const gbnpf_options *, const gbims_settings *,
-                            const gbsln_nonlinear *, const double *, gbsln_handle **out) {
-  if (out) *out = nullptr;
-  return GBIMS_ERR_UNSUPPORTED;
+
+struct NpfStore {
+  int *ia = nullptr, *ja = nullptr, *jas = nullptr, *isym = nullptr, *ihc = nullptr, *icelltype = nullptr;
+  double *cl1 = nullptr, *cl2 = nullptr, *hwva = nullptr, *top = nullptr, *bot = nullptr,
+         *k11 = nullptr, *k33 = nullptr, *condsat = nullptr, *sat = nullptr;
+  NpfDev view() const {
+    NpfDev g;
+    g.ia = ia; g.ja = ja; g.jas = jas; g.isym = isym; g.ihc = ihc;
+    g.cl1 = cl1; g.cl2 = cl2; g.hwva = hwva; g.top = top; g.bot = bot; g.k11 = k11; g.k33 = k33;
+    g.icelltype = icelltype;
+    g.inewton = 0; g.ivarcv = 0; g.idewatcv = 0; g.icellavg = 0; g.satomega = 1.0e-6;
+    return g;
+  }
+  void release() {
+    void *p[] = {ia, ja, jas, isym, ihc, icelltype, cl1, cl2, hwva, top, bot, k11, k33, condsat, sat};
+    for (void *q : p)
+      if (q) cudaFree(q);
+  }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// gbnpf
+// ---------------------------------------------------------------------------
+struct gbnpf_handle {
+  gbnpf_options o{};
+  int nodes = 0, nja = 0, njas = 0;
+  NpfStore d;
+  NpfDev g{};
+  int *zero_ptr = nullptr;  // nodes+1 zeros: empty boundary lists
+  cudaStream_t st = nullptr;
+  std::string err;
+};
+
+extern "C" int gbnpf_create(const gbnpf_options *opt, int nodes, int nja, int njas, const int *ia,
+                            const int *ja, const int *jas, const int *isym, const int *ihc,
+                            const double *cl1, const double *cl2, const double *hwva,
+                            const double *top, const double *bot, const double *k11,
+                            const double *k33, const int *icelltype, gbnpf_handle **out) {
+  if (!out) return GBIMS_ERR_ARG;
+  *out = nullptr;
+  if (!opt || nodes <= 0 || nja < nodes || njas < 0 || !ia || !ja || !jas || !isym || !ihc ||
+      !cl1 || !cl2 || !hwva || !top || !bot || !k11 || !k33 || !icelltype)
+    return GBIMS_ERR_ARG;
+  gbnpf_handle *h = new (std::nothrow) gbnpf_handle();
+  if (!h) return GBIMS_ERR_NOMEM;
+  *out = h;
+  h->o = *opt;
+  h->nodes = nodes;
+  h->nja = nja;
+  h->njas = njas;
+  int b = opt->index_base ? 1 : 0;
+  std::vector<int> ia0(ia, ia + nodes + 1), ja0(ja, ja + nja), jas0(jas, jas + nja), isym0(isym, isym + nja);
+  for (auto &v : ia0) v -= b;
+  for (auto &v : ja0) v -= b;
+  for (auto &v : jas0) v -= b;  // the diagonal's 0 (Fortran) becomes -1
+  for (auto &v : isym0) v -= b;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
+  chk(up(&h->d.ia, ia0.data(), ia0.size()));
+  chk(up(&h->d.ja, ja0.data(), ja0.size()));
+  chk(up(&h->d.jas, jas0.data(), jas0.size()));
+  chk(up(&h->d.isym, isym0.data(), isym0.size()));
+  chk(up(&h->d.ihc, ihc, (size_t)njas));
+  chk(up(&h->d.cl1, cl1, (size_t)njas));
+  chk(up(&h->d.cl2, cl2, (size_t)njas));
+  chk(up(&h->d.hwva, hwva, (size_t)njas));
+  chk(up(&h->d.top, top, (size_t)nodes));
+  chk(up(&h->d.bot, bot, (size_t)nodes));
+  chk(up(&h->d.k11, k11, (size_t)nodes));
+  chk(up(&h->d.k33, k33, (size_t)nodes));
+  chk(up(&h->d.icelltype, icelltype, (size_t)nodes));
+  chk(up<double>(&h->d.condsat, nullptr, (size_t)njas));
+  chk(up<double>(&h->d.sat, nullptr, (size_t)nodes));
+  chk(up<int>(&h->zero_ptr, nullptr, (size_t)nodes + 1));
+  if (h->zero_ptr) chk(cudaMemset(h->zero_ptr, 0, sizeof(int) * (nodes + 1)));
+  chk(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+  if (e != cudaSuccess) {
+    h->err = cudaGetErrorString(e);
+    return GBIMS_ERR_CUDA;
+  }
+  h->g = h->d.view();
+  h->g.inewton = opt->inewton;
+  h->g.ivarcv = opt->ivarcv;
+  h->g.idewatcv = opt->idewatcv;
+  h->g.icellavg = opt->icellavg;
+  h->g.satomega = opt->satomega > 0 ? opt->satomega : 1.0e-6;
+  cudaMemset(h->d.sat, 0, sizeof(double) * nodes);
+  gwf_condsat(nodes, h->g, h->d.condsat, h->st);
+  e = cudaStreamSynchronize(h->st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    h->err = cudaGetErrorString(e);
+    return GBIMS_ERR_CUDA;
+  }
+  return GBIMS_OK;
 }
-extern "C" int gbsln_timestep(gbsln_handle *, int, int, double, gbsln_stats *) { return GBIMS_ERR_UNSUPPORTED; }
-extern "C" int gbsln_get_heads(gbsln_handle *, double *) { return GBIMS_ERR_UNSUPPORTED; }
-extern "C" int gbsln_set_heads(gbsln_handle *, const double *) { return GBIMS_ERR_UNSUPPORTED; }
-extern "C" gbims_handle *gbsln_ims(gbsln_handle *) { return nullptr; }
-extern "C" int gbsln_destroy(gbsln_handle *) { return GBIMS_OK; }
+
+extern "C" int gbnpf_fill(gbnpf_handle *h, const int *d_ibound, const double *d_hnew,
+                          double *d_amat, double *d_rhs) {
+  if (!h || !d_ibound || !d_hnew || !d_amat || !d_rhs) return GBIMS_ERR_ARG;
+  // NPF terms only: no storage, empty boundary lists
+  FillDev f;
+  memset(&f, 0, sizeof(f));
+  f.bnd_ptr = h->zero_ptr;
+  gwf_npf_cf(h->nodes, h->g, d_ibound, d_hnew, h->d.sat, h->st);
+  gwf_fill(h->nodes, h->g, f, d_ibound, d_hnew, d_hnew, h->d.sat, h->d.condsat, d_amat, d_rhs, h->st);
+  cudaError_t e = cudaStreamSynchronize(h->st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    h->err = cudaGetErrorString(e);
+    return GBIMS_ERR_CUDA;
+  }
+  return GBIMS_OK;
+}
+
+extern "C" int gbnpf_get_condsat(gbnpf_handle *h, double *condsat) {
+  if (!h || !condsat) return GBIMS_ERR_ARG;
+  if (cudaMemcpy(condsat, h->d.condsat, sizeof(double) * h->njas, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GBIMS_ERR_CUDA;
+  return GBIMS_OK;
+}
+
+extern "C" int gbnpf_destroy(gbnpf_handle *h) {
+  if (!h) return GBIMS_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  h->d.release();
+  if (h->zero_ptr) cudaFree(h->zero_ptr);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return GBIMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// gbsln
+// ---------------------------------------------------------------------------
+struct gbsln_handle {
+  int nlay = 0, nrow = 0, ncol = 0, n = 0, nja = 0;
+  gbsln_nonlinear nl{};
+  gbims_settings ims_s{};
+  NpfStore d;
+  NpfDev g{};
+  double *strt = nullptr;  // initial heads (IC STRT), kept for gbsln_restart
+  double *ss = nullptr, *sy = nullptr, *area = nullptr, *vol = nullptr, *xold = nullptr,
+         *xtemp = nullptr, *wsave = nullptr, *hchold = nullptr, *deold = nullptr,
+         *dxold = nullptr, *part = nullptr, *bnd_val = nullptr, *chd_head = nullptr;
+  int *ibound = nullptr, *bnd_ptr = nullptr, *chd_node = nullptr, *flag = nullptr;
+  int nchd = 0, G = 1;
+  bool has_sto = false;
+  gbims_handle *ims = nullptr;
+  double *amat = nullptr, *rhs = nullptr, *x = nullptr;  // inside the IMS handle
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  // outer-loop state
+  double bigch = 0, bigchold = 0, relaxold = 0, l2norm0_ptc = 0, ptcdel = 0;
+  std::vector<double> hpart;
+  std::string err;
+};
+
+#define SLN_CUDA(h, call)                                                   \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) {                                                \
+      (h)->err = std::string(#call) + ": " + cudaGetErrorString(e_);        \
+      return GBIMS_ERR_CUDA;                                                \
+    }                                                                       \
+  } while (0)
+
+__global__ void k_set_chd(int nchd, const int *__restrict__ node, const double *__restrict__ head,
+                          double *x, double *xold) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nchd) {
+    x[node[i]] = head[i];
+    xold[node[i]] = head[i];
+  }
+}
+
+extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
+                            const gbims_settings *ims, const gbsln_nonlinear *nl,
+                            const double *strt, gbsln_handle **out) {
+  if (!out) return GBIMS_ERR_ARG;
+  *out = nullptr;
+  if (!m || !npf || !ims || !nl || !strt || m->nlay <= 0 || m->nrow <= 0 || m->ncol <= 0 ||
+      !m->delr || !m->delc || !m->top || !m->botm || !m->k11 || !m->k33 || !m->icelltype)
+    return GBIMS_ERR_ARG;
+  gbsln_handle *h = new (std::nothrow) gbsln_handle();
+  if (!h) return GBIMS_ERR_NOMEM;
+  *out = h;
+  h->nlay = m->nlay; h->nrow = m->nrow; h->ncol = m->ncol;
+  const long long nrc = (long long)m->nrow * m->ncol;
+  const long long nn = nrc * m->nlay;
+  if (nn > 400000000LL) { h->err = "grid too large"; return GBIMS_ERR_UNSUPPORTED; }
+  const int n = (int)nn;
+  h->n = n;
+  h->nl = *nl;
+  h->ims_s = *ims;
+  h->ims_s.index_base = 0;
+  h->ims_s.nlay = m->nlay; h->ims_s.nrow = m->nrow; h->ims_s.ncol = m->ncol;
+  // cell geometry (Dis.f90: top of layer 1 is TOP, of layer k>1 the bottom above)
+  std::vector<double> top(n), bot(m->botm, m->botm + n), area(n), vol(n);
+  for (long long p = 0; p < nn; ++p) {
+    top[p] = (p < nrc) ? m->top[p] : m->botm[p - nrc];
+    long long rem = p % nrc;
+    int i = (int)(rem / m->ncol), j = (int)(rem % m->ncol);
+    area[p] = m->delc[i] * m->delr[j];
+    vol[p] = area[p] * (top[p] - bot[p]);
+  }
+  Conn c;
+  build_connections(m->nlay, m->nrow, m->ncol, m->delr, m->delc, top, bot, c);
+  h->nja = (int)c.ja.size();
+  std::vector<int> ibound(n, 1);
+  for (int i = 0; i < m->nchd; ++i) {
+    int node = m->chd_node[i];
+    if (node < 0 || node >= n) { h->err = "CHD node out of range"; return GBIMS_ERR_ARG; }
+    ibound[node] = -1;
+  }
+  // boundary values per node: WEL q, then RCH rate*area (package order)
+  std::vector<std::vector<double>> per(n);
+  for (int i = 0; i < m->nwel; ++i) {
+    int node = m->wel_node[i];
+    if (node < 0 || node >= n) { h->err = "WEL node out of range"; return GBIMS_ERR_ARG; }
+    per[node].push_back(m->wel_q[i]);
+  }
+  for (int i = 0; i < m->nrch; ++i) {
+    int node = m->rch_node[i];
+    if (node < 0 || node >= n) { h->err = "RCH node out of range"; return GBIMS_ERR_ARG; }
+    per[node].push_back(m->rch_rate[i] * area[node]);
+  }
+  std::vector<int> bptr(n + 1, 0);
+  std::vector<double> bval;
+  for (int p = 0; p < n; ++p) {
+    bptr[p] = (int)bval.size();
+    for (double v : per[p]) bval.push_back(v);
+  }
+  bptr[n] = (int)bval.size();
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
+  chk(up(&h->d.ia, c.ia.data(), c.ia.size()));
+  chk(up(&h->d.ja, c.ja.data(), c.ja.size()));
+  chk(up(&h->d.jas, c.jas.data(), c.jas.size()));
+  chk(up(&h->d.isym, c.isym.data(), c.isym.size()));
+  chk(up(&h->d.ihc, c.ihc.data(), c.ihc.size()));
+  chk(up(&h->d.cl1, c.cl1.data(), c.cl1.size()));
+  chk(up(&h->d.cl2, c.cl2.data(), c.cl2.size()));
+  chk(up(&h->d.hwva, c.hwva.data(), c.hwva.size()));
+  chk(up(&h->d.top, top.data(), top.size()));
+  chk(up(&h->d.bot, bot.data(), bot.size()));
+  chk(up(&h->d.k11, m->k11, (size_t)n));
+  chk(up(&h->d.k33, m->k33, (size_t)n));
+  chk(up(&h->d.icelltype, m->icelltype, (size_t)n));
+  chk(up<double>(&h->d.condsat, nullptr, c.cl1.size()));
+  chk(up<double>(&h->d.sat, nullptr, (size_t)n));
+  h->has_sto = (m->ss != nullptr && m->sy != nullptr);
+  if (h->has_sto) {
+    chk(up(&h->ss, m->ss, (size_t)n));
+    chk(up(&h->sy, m->sy, (size_t)n));
+  }
+  chk(up(&h->area, area.data(), area.size()));
+  chk(up(&h->vol, vol.data(), vol.size()));
+  chk(up(&h->ibound, ibound.data(), ibound.size()));
+  chk(up(&h->bnd_ptr, bptr.data(), bptr.size()));
+  chk(up(&h->bnd_val, bval.data(), bval.size()));
+  h->nchd = m->nchd;
+  chk(up(&h->chd_node, m->chd_node, (size_t)m->nchd));
+  chk(up(&h->chd_head, m->chd_head, (size_t)m->nchd));
+  double **wv[] = {&h->xold, &h->xtemp, &h->wsave, &h->hchold, &h->deold, &h->dxold};
+  for (double **p : wv) chk(up<double>(p, nullptr, (size_t)n));
+  h->G = std::max(1, std::min(2 * kNumSM * 2, (n + 255) / 256));
+  chk(up<double>(&h->part, nullptr, (size_t)h->G * 2));
+  chk(up<int>(&h->flag, nullptr, 4));
+  chk(up(&h->strt, strt, (size_t)n));
+  if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GBIMS_ERR_CUDA; }
+  for (double **p : wv) cudaMemset(*p, 0, sizeof(double) * n);
+  cudaMemset(h->d.sat, 0, sizeof(double) * n);
+  h->hpart.resize((size_t)h->G * 2);
+  // IMS handle (imslinear_allocate) on the same connectivity
+  int rc = gbims_create(&h->ims_s, n, h->nja, c.ia.data(), c.ja.data(), &h->ims);
+  if (rc < 0) {
+    h->err = std::string("IMS: ") + (h->ims ? gbims_last_error(h->ims) : "create failed");
+    return rc;
+  }
+  ims_buffers(h->ims, &h->amat, &h->rhs, &h->x);
+  h->st = ims_stream(h->ims);
+  SLN_CUDA(h, cudaEventCreate(&h->e0));
+  SLN_CUDA(h, cudaEventCreate(&h->e1));
+  SLN_CUDA(h, cudaEventCreate(&h->e2));
+  h->g = h->d.view();
+  h->g.inewton = npf->inewton;
+  h->g.ivarcv = npf->ivarcv;
+  h->g.idewatcv = npf->idewatcv;
+  h->g.icellavg = npf->icellavg;
+  h->g.satomega = npf->satomega > 0 ? npf->satomega : 1.0e-6;
+  SLN_CUDA(h, cudaMemcpyAsync(h->x, strt, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
+  gwf_condsat(n, h->g, h->d.condsat, h->st);
+  SLN_CUDA(h, cudaStreamSynchronize(h->st));
+  SLN_CUDA(h, cudaGetLastError());
+  return GBIMS_OK;
+}
+
+static int read_dxmax(gbsln_handle *h, double *hncg, int *loc) {
+  gwf_dxmax(h->n, h->ibound, h->x, h->xtemp, h->part, h->G, h->st);
+  SLN_CUDA(h, cudaMemcpyAsync(h->hpart.data(), h->part, sizeof(double) * 2 * h->G,
+                              cudaMemcpyDeviceToHost, h->st));
+  SLN_CUDA(h, cudaStreamSynchronize(h->st));
+  double best = 0.0;
+  long long bi = -1;
+  for (int b = 0; b < h->G; ++b) {
+    double v = h->hpart[2 * b];
+    long long i = (long long)h->hpart[2 * b + 1];
+    if (i < 0) continue;
+    if (fabs(v) > fabs(best) || (fabs(v) == fabs(best) && (bi < 0 || i < bi))) {
+      best = v;
+      bi = i;
+    }
+  }
+  *hncg = best;
+  if (loc) *loc = (int)bi;
+  return GBIMS_OK;
+}
+
+static int reduce_host(gbsln_handle *h, bool max_not_sum, double *out) {
+  SLN_CUDA(h, cudaMemcpyAsync(h->hpart.data(), h->part, sizeof(double) * h->G,
+                              cudaMemcpyDeviceToHost, h->st));
+  SLN_CUDA(h, cudaStreamSynchronize(h->st));
+  double a = 0.0;
+  for (int b = 0; b < h->G; ++b) a = max_not_sum ? std::max(a, h->hpart[b]) : a + h->hpart[b];
+  *out = a;
+  return GBIMS_OK;
+}
+
+extern "C" int gbsln_timestep(gbsln_handle *h, int kper, int kstp, double delt, gbsln_stats *st) {
+  if (!h || !h->ims) return GBIMS_ERR_ARG;
+  const int n = h->n;
+  const bool transient = (delt > 0.0) && h->has_sto;
+  gbsln_stats s;
+  memset(&s, 0, sizeof(s));
+  float fill_ms = 0.f, solve_ms = 0.f;
+  SLN_CUDA(h, cudaEventRecord(h->e0, h->st));
+  // prepareSolve: gwf_ad (xold = x) and chd_ad (x = xold = head)
+  SLN_CUDA(h, cudaMemcpyAsync(h->xold, h->x, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->st));
+  if (h->nchd > 0)
+    k_set_chd<<<(h->nchd + 255) / 256, 256, 0, h->st>>>(h->nchd, h->chd_node, h->chd_head, h->x, h->xold);
+  FillDev f;
+  f.transient = transient ? 1 : 0;
+  f.tled = transient ? 1.0 / delt : 0.0;
+  f.ss = h->ss;
+  f.sy = h->sy;
+  f.area = h->area;
+  f.bnd_ptr = h->bnd_ptr;
+  f.bnd_val = h->bnd_val;
+  const int isymmetric = (h->ims_s.ilinmeth == 1) ? 1 : 0;
+  const bool steady_newton = !transient && h->g.inewton;
+  bool converged = false;
+  double hncg = 0.0;
+  for (int kiter = 1; kiter <= h->nl.mxiter; ++kiter) {
+    cudaEvent_t f0, f1;
+    cudaEventCreate(&f0);
+    cudaEventCreate(&f1);
+    cudaEventRecord(f0, h->st);
+    // sln_buildsystem: amat = rhs = 0, npf_cf, gwf_fc
+    SLN_CUDA(h, cudaMemsetAsync(h->amat, 0, sizeof(double) * h->nja, h->st));
+    SLN_CUDA(h, cudaMemsetAsync(h->rhs, 0, sizeof(double) * n, h->st));
+    gwf_npf_cf(n, h->g, h->ibound, h->x, h->d.sat, h->st);
+    gwf_fill(n, h->g, f, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, h->amat, h->rhs, h->st);
+    cudaEventRecord(f1, h->st);
+    // sln_calc_ptc -> gwf_ptc (steady-state Newton models)
+    int iptc = 0;
+    double ptcf = 0.0;
+    if (steady_newton) {
+      gwf_ptc_resid(n, h->d.ia, h->d.ja, h->amat, h->x, h->rhs, h->ibound, h->vol, h->part, h->G, h->st);
+      int rc = reduce_host(h, true, &ptcf);
+      if (rc < 0) return rc;
+      if (ptcf == 0.0) ptcf = 1.0 / (delt * 10.0);
+      iptc = 1;
+    }
+    // sln_ls: loose ends, then pseudo-transient continuation
+    gwf_fixups(n, h->d.ia, h->d.ja, h->ibound, isymmetric, h->amat, h->rhs, h->x, h->xtemp, h->st);
+    int iallowptc = h->nl.iallowptc;
+    if (iallowptc < 0) iallowptc = (kper > 1) ? 1 : 0;
+    if (iptc * iallowptc != 0) {
+      gwf_l2_resid(n, h->d.ia, h->d.ja, h->amat, h->x, h->rhs, h->ibound, h->part, h->G, h->st);
+      double ss2 = 0.0;
+      int rc = reduce_host(h, false, &ss2);
+      if (rc < 0) return rc;
+      double l2norm = sqrt(ss2);
+      if (kiter == 1) {
+        if ((kper > 1 || kstp > 1) && l2norm <= h->l2norm0_ptc) iptc = 0;
+      } else {
+        double a = l2norm, b = h->l2norm0_ptc;
+        bool same = (a == b) || fabs(a - b) <= 100.0 * 2.220446049250313e-16 * std::max(fabs(a), fabs(b));
+        if (same) iptc = 0;
+      }
+      if (iptc * iallowptc != 0) {
+        if (kiter == 1) h->ptcdel = 1.0 / ptcf;
+        else h->ptcdel = (l2norm > 0.0) ? h->ptcdel * (h->l2norm0_ptc / l2norm) : 0.0;
+        double ptcval = (h->ptcdel > 0.0) ? 1.0 / h->ptcdel : 1.0;
+        gwf_ptc_apply(n, h->d.ia, h->ibound, ptcval, h->amat, h->rhs, h->x, h->st);
+        h->l2norm0_ptc = l2norm;
+      }
+    }
+    // IMS apply (in place on the handle's buffers)
+    int icnvg = 0, in_iter = 0;
+    gbims_summary sm;
+    int rc = ims_apply_inplace(h->ims, kstp, kiter, &icnvg, &in_iter, &sm);
+    cudaEventElapsedTime(&fill_ms, f0, f1);
+    cudaEventDestroy(f0);
+    cudaEventDestroy(f1);
+    s.fill_ms += fill_ms;
+    s.solve_ms += sm.solve_ms;
+    if (rc < 0) {
+      h->err = std::string("IMS: ") + ims_error(h->ims);
+      return rc;
+    }
+    s.inner_total += in_iter;
+    s.pivot_retries += sm.pivot_retries;
+    s.outer = kiter;
+    rc = read_dxmax(h, &hncg, nullptr);
+    if (rc < 0) return rc;
+    bool cnvg = fabs(hncg) <= h->nl.dvclose;
+    if (!cnvg) {
+      if (h->nl.nonmeth == 1 || h->nl.nonmeth == 3) {
+        gwf_underrelax(n, h->nl.nonmeth, kiter, h->nl.theta, h->nl.akappa, h->nl.gamma,
+                       h->nl.amomentum, h->ibound, h->x, h->xtemp, h->wsave, h->hchold, h->deold,
+                       h->dxold, h->st);
+      } else if (h->nl.nonmeth == 2) {
+        double relax;
+        h->bigch = hncg;
+        if (kiter == 1) {
+          relax = 1.0;
+          h->relaxold = 1.0;
+          h->bigchold = hncg;
+        } else {
+          double es = h->bigch / (h->bigchold * h->relaxold);
+          double aes = fabs(es);
+          relax = (es < -1.0) ? 0.5 / aes : (3.0 + es) / (3.0 + aes);
+        }
+        h->relaxold = relax;
+        h->bigchold = (1.0 - h->nl.gamma) * h->bigch + h->nl.gamma * h->bigchold;
+        if (relax < 1.0) gwf_relax_scale(n, relax, h->ibound, h->x, h->xtemp, h->dxold, h->st);
+      } else {
+        gwf_calcdx(n, h->ibound, h->x, h->xtemp, h->dxold, h->st);
+      }
+      if (h->g.inewton) {
+        SLN_CUDA(h, cudaMemsetAsync(h->flag, 0, sizeof(int), h->st));
+        gwf_npf_nur(n, (int)((long long)h->nrow * h->ncol), h->nlay, h->g, h->ibound, h->x,
+                    h->xtemp, h->dxold, h->flag, h->st);
+        int flag = 0;
+        SLN_CUDA(h, cudaMemcpyAsync(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+        SLN_CUDA(h, cudaStreamSynchronize(h->st));
+        if (flag) {
+          // sln_maxval over dxold, then sln_nur_has_converged
+          std::vector<double> dx(n);
+          SLN_CUDA(h, cudaMemcpy(dx.data(), h->dxold, sizeof(double) * n, cudaMemcpyDeviceToHost));
+          double vmax = dx[0];
+          for (int q = 1; q < n; ++q) {
+            double denom = fabs(vmax);
+            if (denom == 0.0) denom = 2.220446049250313e-16;
+            if (fabs(dx[q]) / denom > 1.0) vmax = dx[q];
+          }
+          if (fabs(vmax) <= h->nl.dvclose && fabs(hncg) <= h->nl.dvclose) {
+            cnvg = true;
+            rc = read_dxmax(h, &hncg, nullptr);
+            if (rc < 0) return rc;
+          }
+        }
+      }
+    }
+    if (cnvg) {
+      converged = true;
+      break;
+    }
+  }
+  SLN_CUDA(h, cudaEventRecord(h->e1, h->st));
+  SLN_CUDA(h, cudaEventSynchronize(h->e1));
+  float tot = 0.f;
+  cudaEventElapsedTime(&tot, h->e0, h->e1);
+  s.total_ms = tot;
+  s.converged = converged ? 1 : 0;
+  s.dxmax = hncg;
+  (void)solve_ms;
+  if (st) *st = s;
+  return GBIMS_OK;
+}
+
+extern "C" int gbsln_formulate(gbsln_handle *h, double delt, const double *hold, double *amat,
+                               double *rhs) {
+  if (!h || !amat || !rhs) return GBIMS_ERR_ARG;
+  const int n = h->n;
+  const bool transient = (delt > 0.0) && h->has_sto;
+  if (transient && !hold) return GBIMS_ERR_ARG;
+  if (hold) SLN_CUDA(h, cudaMemcpyAsync(h->xold, hold, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
+  FillDev f;
+  f.transient = transient ? 1 : 0;
+  f.tled = transient ? 1.0 / delt : 0.0;
+  f.ss = h->ss;
+  f.sy = h->sy;
+  f.area = h->area;
+  f.bnd_ptr = h->bnd_ptr;
+  f.bnd_val = h->bnd_val;
+  SLN_CUDA(h, cudaMemsetAsync(h->amat, 0, sizeof(double) * h->nja, h->st));
+  SLN_CUDA(h, cudaMemsetAsync(h->rhs, 0, sizeof(double) * n, h->st));
+  gwf_npf_cf(n, h->g, h->ibound, h->x, h->d.sat, h->st);
+  gwf_fill(n, h->g, f, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, h->amat, h->rhs, h->st);
+  SLN_CUDA(h, cudaGetLastError());
+  SLN_CUDA(h, cudaMemcpyAsync(amat, h->amat, sizeof(double) * h->nja, cudaMemcpyDeviceToHost, h->st));
+  SLN_CUDA(h, cudaMemcpyAsync(rhs, h->rhs, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+  SLN_CUDA(h, cudaStreamSynchronize(h->st));
+  return GBIMS_OK;
+}
+
+extern "C" const char *gbsln_last_error(const gbsln_handle *h) {
+  return h ? h->err.c_str() : "null handle";
+}
+
+extern "C" int gbsln_restart(gbsln_handle *h) {
+  if (!h) return GBIMS_ERR_ARG;
+  SLN_CUDA(h, cudaMemcpyAsync(h->x, h->strt, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
+  SLN_CUDA(h, cudaStreamSynchronize(h->st));
+  h->bigch = h->bigchold = h->relaxold = h->l2norm0_ptc = h->ptcdel = 0.0;
+  return GBIMS_OK;
+}
+
+extern "C" int gbsln_get_heads(gbsln_handle *h, double *x) {
+  if (!h || !x) return GBIMS_ERR_ARG;
+  SLN_CUDA(h, cudaStreamSynchronize(h->st));
+  SLN_CUDA(h, cudaMemcpy(x, h->x, sizeof(double) * h->n, cudaMemcpyDeviceToHost));
+  return GBIMS_OK;
+}
+
+extern "C" int gbsln_set_heads(gbsln_handle *h, const double *x) {
+  if (!h || !x) return GBIMS_ERR_ARG;
+  SLN_CUDA(h, cudaStreamSynchronize(h->st));
+  SLN_CUDA(h, cudaMemcpy(h->x, x, sizeof(double) * h->n, cudaMemcpyHostToDevice));
+  return GBIMS_OK;
+}
+
+extern "C" gbims_handle *gbsln_ims(gbsln_handle *h) { return h ? h->ims : nullptr; }
+
+extern "C" int gbsln_destroy(gbsln_handle *h) {
+  if (!h) return GBIMS_OK;
+  if (h->ims) gbims_destroy(h->ims);
+  h->d.release();
+  void *p[] = {h->strt, h->ss, h->sy, h->area, h->vol, h->xold, h->xtemp, h->wsave, h->hchold, h->deold,
+               h->dxold, h->part, h->bnd_val, h->chd_head, h->ibound, h->bnd_ptr, h->chd_node,
+               h->flag};
+  for (void *q : p)
+    if (q) cudaFree(q);
+  if (h->e0) cudaEventDestroy(h->e0);
+  if (h->e1) cudaEventDestroy(h->e1);
+  if (h->e2) cudaEventDestroy(h->e2);
+  delete h;
+  return GBIMS_OK;
+}

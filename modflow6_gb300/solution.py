@@ -1,0 +1,179 @@
+"""Device-resident NumericalSolution for one GWF DIS model (gbsln_* C ABI).
+
+`GwfSolution` mirrors the per-time-step use of NumericalSolutionType
+(src/Solution/NumericalSolution.f90: sln_ca :1287, solve :1482-1837) for a
+single GWF model with the DIS, IC, NPF, STO, CHD, WEL and RCH packages: the
+fill, the sln_ls fix-ups, the IMS apply, dxmax and under-relaxation all run in
+HBM; only per-outer-iteration scalars return to the host.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .dis import GwfDisModel
+from .ims import ImsLinearSettings
+
+
+@dataclass
+class Nonlinear:
+    """IMS NONLINEAR block (defaults: COMPLEXITY SIMPLE, sln_setouter :2626-2637)."""
+
+    dvclose: float = 1.0e-3   # OUTER_DVCLOSE
+    mxiter: int = 25          # OUTER_MAXIMUM
+    nonmeth: int = 0          # UNDER_RELAXATION: 0 none, 1 simple, 2 cooley, 3 dbd
+    theta: float = 1.0
+    akappa: float = 0.0
+    gamma: float = 1.0
+    amomentum: float = 0.0
+    iallowptc: int = 1
+
+    @classmethod
+    def preset(cls, complexity: str, **kw) -> "Nonlinear":
+        c = complexity.upper()
+        if c == "SIMPLE":
+            n = cls(1e-3, 25, 0, 1.0, 0.0, 1.0, 0.0)
+        elif c == "MODERATE":
+            n = cls(1e-2, 50, 3, 0.9, 1e-4, 0.0, 0.0)
+        elif c == "COMPLEX":
+            n = cls(1e-1, 100, 3, 0.8, 1e-4, 0.0, 0.0)
+        else:
+            raise ValueError(complexity)
+        for k, v in kw.items():
+            setattr(n, k, v)
+        return n
+
+
+def sln_ls_fixups(ia, ja, active, amat, rhs, x, isymmetric=True):
+    """Host form of the sln_ls loose ends (NumericalSolution.f90:2434-2478) for
+    callers that assemble on the host and call the C ABI with host arrays."""
+    amat = amat.copy()
+    rhs = rhs.copy()
+    n = ia.size - 1
+    diag = ia[:-1]
+    act = active > 0
+    small = act & (np.abs(amat[diag]) < 1e-15)
+    amat[diag[small]] = -1.0
+    rhs[small] = rhs[small] + (-1.0) * x[small]
+    rows = np.repeat(np.arange(n), np.diff(ia))
+    inactive = ~act
+    off = rows != ja
+    kill = inactive[rows] & off
+    amat[kill] = 0.0
+    amat[diag[inactive]] = 1.0
+    rhs[inactive] = x[inactive]
+    if isymmetric:
+        elim = off & act[rows] & (active[ja] < 0)
+        idx = np.flatnonzero(elim)
+        # per row, in JA order: rhs -= a * x(col)
+        for p in idx:
+            r = rows[p]
+            rhs[r] = rhs[r] - amat[p] * x[ja[p]]
+        amat[idx] = 0.0
+    return amat, rhs
+
+
+def _f(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class GwfSolution:
+    def __init__(self, m: GwfDisModel, ims: ImsLinearSettings, nl: Nonlinear,
+                 satomega: float = 1.0e-6):
+        lib = _lib.load()
+        self.m = m
+        keep = dict(delr=_f(m.delr), delc=_f(m.delc), top=_f(m.top), botm=_f(m.botm),
+                    k11=_f(m.k11), k33=_f(m.k33), ict=_i(m.icelltype),
+                    chd_node=_i(m.chd_node), chd_head=_f(m.chd_head), wel_node=_i(m.wel_node),
+                    wel_q=_f(m.wel_q), rch_node=_i(m.rch_node), rch_rate=_f(m.rch_rate),
+                    strt=_f(m.strt))
+        ss = sy = None
+        if m.ss is not None and m.sy is not None:
+            keep["ss"], keep["sy"] = _f(m.ss), _f(m.sy)
+            ss, sy = _lib.dptr(keep["ss"]), _lib.dptr(keep["sy"])
+        self._keep = keep
+        cm = _lib.GbslnModel(m.nlay, m.nrow, m.ncol, _lib.dptr(keep["delr"]), _lib.dptr(keep["delc"]),
+                             _lib.dptr(keep["top"]), _lib.dptr(keep["botm"]), _lib.dptr(keep["k11"]),
+                             _lib.dptr(keep["k33"]), _lib.iptr(keep["ict"]), ss, sy,
+                             int(m.chd_node.size), _lib.iptr(keep["chd_node"]), _lib.dptr(keep["chd_head"]),
+                             int(m.wel_node.size), _lib.iptr(keep["wel_node"]), _lib.dptr(keep["wel_q"]),
+                             int(m.rch_node.size), _lib.iptr(keep["rch_node"]), _lib.dptr(keep["rch_rate"]))
+        npf = _lib.GbnpfOptions(int(m.inewton), 0, 0, 0, satomega, 0)
+        cs = ims.to_c(0)
+        cnl = _lib.GbslnNonlinear(nl.dvclose, nl.mxiter, nl.nonmeth, nl.theta, nl.akappa, nl.gamma,
+                                  nl.amomentum, nl.iallowptc)
+        self._h = C.c_void_p()
+        rc = lib.gbsln_create(C.byref(cm), C.byref(npf), C.byref(cs), C.byref(cnl),
+                              _lib.dptr(keep["strt"]), C.byref(self._h))
+        if rc < 0:
+            msg = lib.gbsln_last_error(self._h).decode() if self._h else ""
+            lib.gbsln_destroy(self._h)
+            self._h = C.c_void_p()
+            raise _lib.GbimsError(rc, msg)
+        self.nodes = m.nodes
+
+    def timestep(self, kper: int = 1, kstp: int = 1, delt: float = 1.0) -> dict:
+        lib = _lib.load()
+        st = _lib.GbslnStats()
+        rc = lib.gbsln_timestep(self._h, kper, kstp, delt, C.byref(st))
+        if rc < 0:
+            raise _lib.GbimsError(rc, lib.gbsln_last_error(self._h).decode())
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def formulate(self, delt: float = 0.0, hold: np.ndarray | None = None):
+        """Assembled (amat, rhs) at the current heads, before the sln_ls fix-ups."""
+        lib = _lib.load()
+        nja = int(self.m.connections()["nja"]) if not hasattr(self, "_nja") else self._nja
+        self._nja = nja
+        amat = np.zeros(nja)
+        rhs = np.zeros(self.nodes)
+        hp = _lib.dptr(_f(hold)) if hold is not None else None
+        if hold is not None:
+            self._hold = _f(hold)
+            hp = _lib.dptr(self._hold)
+        rc = lib.gbsln_formulate(self._h, delt, hp, _lib.dptr(amat), _lib.dptr(rhs))
+        if rc < 0:
+            raise _lib.GbimsError(rc, lib.gbsln_last_error(self._h).decode())
+        return amat, rhs
+
+    @property
+    def heads(self) -> np.ndarray:
+        x = np.zeros(self.nodes)
+        rc = _lib.load().gbsln_get_heads(self._h, _lib.dptr(x))
+        if rc < 0:
+            raise _lib.GbimsError(rc, "get_heads")
+        return x
+
+    @heads.setter
+    def heads(self, x: np.ndarray):
+        x = _f(x)
+        rc = _lib.load().gbsln_set_heads(self._h, _lib.dptr(x))
+        if rc < 0:
+            raise _lib.GbimsError(rc, "set_heads")
+
+    def restart(self):
+        """Heads back to IC STRT on the device (gbsln_restart)."""
+        rc = _lib.load().gbsln_restart(self._h)
+        if rc < 0:
+            raise _lib.GbimsError(rc, "restart")
+
+    def ims_handle(self) -> C.c_void_p:
+        return C.c_void_p(_lib.load().gbsln_ims(self._h))
+
+    def close(self):
+        if self._h:
+            _lib.load().gbsln_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

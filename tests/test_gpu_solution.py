@@ -1,0 +1,82 @@
+"""Device-resident GWF assembly and outer loop against the oracle.
+
+The fill (NPF fc/fn, STO fc/fn, WEL, RCH) is compared bit for bit; the time
+step (fill, sln_ls fix-ups, IMS, dxmax, under-relaxation) at closure.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from modflow6_gb300.dis import make_config
+from modflow6_gb300.ims import ImsLinearSettings
+from modflow6_gb300.solution import GwfSolution, Nonlinear
+from test_oracle_known_answers import chd01_model, newton01_model
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name,scale", [("c1", 1.0), ("c2", 0.05), ("c3", 0.04), ("c5", 0.1)])
+def test_formulate_bitexact(gblib, name, scale):
+    m = make_config(name, seed=2, scale=scale)
+    g = oracle.Gwf(m, oracle.settings())
+    sol = GwfSolution(m, ImsLinearSettings(), Nonlinear())
+    rng = np.random.default_rng(3)
+    h = m.strt + rng.uniform(-3.0, 3.0, m.nodes)
+    hold = m.strt + rng.uniform(-3.0, 3.0, m.nodes)
+    transient = m.ss is not None
+    delt = 2.5 if transient else 0.0
+    sol.heads = h
+    amat, rhs = sol.formulate(delt=delt, hold=hold if transient else None)
+    ao, ro = g.assemble(h, hold=hold, delt=delt, transient=transient)
+    np.testing.assert_array_equal(amat, ao)
+    np.testing.assert_array_equal(rhs, ro)
+
+
+def test_timestep_c1_matches_oracle(gblib):
+    m = make_config("c1", seed=0)
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=1000)
+    g = oracle.Gwf(m, oracle.settings(**tol))
+    so = g.timestep(kper=1, kstp=1, delt=1.0, dvclose=1e-8, mxiter=10)
+    sol = GwfSolution(m, ImsLinearSettings(structure=(1, 100, 100), **tol), Nonlinear(dvclose=1e-8, mxiter=10))
+    sg = sol.timestep(1, 1, 1.0)
+    assert sg["converged"] == 1 and so["converged"] == 1
+    assert sg["outer"] == so["outer"]
+    assert np.max(np.abs(sol.heads - g.x)) <= 0.1 * tol["dvclose"]
+
+
+def test_chd01_known_answer_gpu(gblib):
+    m = chd01_model()
+    sol = GwfSolution(m, ImsLinearSettings(dvclose=1e-6, rclose=1e-6, iter1=300),
+                      Nonlinear(dvclose=1e-6, mxiter=100))
+    st = sol.timestep(1, 1, 5.0)
+    assert st["converged"] == 1
+    np.testing.assert_allclose(sol.heads, np.linspace(1, 0, 100), rtol=1e-5, atol=1e-8)
+
+
+def test_newton01_known_answer_gpu(gblib):
+    m = newton01_model()
+    ims = ImsLinearSettings(dvclose=1e-9, rclose=0.1, iter1=500, ilinmeth=2, north=2)
+    sol = GwfSolution(m, ims, Nonlinear.preset("COMPLEX", dvclose=1e-9))
+    st = sol.timestep(1, 1, 1.0)
+    assert st["converged"] == 1
+    x = sol.heads
+    assert np.isclose(x[4], 8.0), x[4]
+    assert np.isclose(x[13], 7.0), x[13]
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_c3_small_transient_newton(gblib, precision):
+    m = make_config("c3", seed=1, scale=0.04)
+    tol = dict(dvclose=1e-6, rclose=1e-3, iter1=500, ilinmeth=2)
+    g = oracle.Gwf(m, oracle.settings(**tol))
+    nl = Nonlinear.preset("MODERATE", dvclose=1e-6, mxiter=50)
+    sol = GwfSolution(m, ImsLinearSettings(precision=precision, structure=(m.nlay, m.nrow, m.ncol), **tol), nl)
+    delt = 10.0
+    for kstp in range(1, 4):
+        so = g.timestep(kper=1, kstp=kstp, delt=delt, transient=True, dvclose=nl.dvclose,
+                        mxiter=nl.mxiter, nonmeth=nl.nonmeth, theta=nl.theta, akappa=nl.akappa,
+                        gamma=nl.gamma, amomentum=nl.amomentum)
+        sg = sol.timestep(1, kstp, delt)
+        assert so["converged"] == 1 and sg["converged"] == 1
+        delt *= 1.2
+    assert np.max(np.abs(sol.heads - g.x)) <= 1e-5

@@ -1,0 +1,79 @@
+"""Structured 7-point wavefront sweeps (DIS grids) against the oracle.
+
+The forward sweep keeps the reference's summation order; the backward sweep
+uses inverse-pivot-scaled upper factors, equal in exact arithmetic, so the
+preconditioner output is compared at 1e-12 relative to its scale, and solves
+at closure (heads within 0.1 x INNER_DVCLOSE of the oracle's IMS solve).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from modflow6_gb300 import _lib
+from modflow6_gb300.dis import GwfDisModel, lognormal_field, make_config
+from modflow6_gb300.ims import ImsLinear, ImsLinearSettings
+
+pytestmark = pytest.mark.gpu
+
+
+def dis_system(nlay, nrow, ncol, seed=0, isym=True):
+    rng = np.random.default_rng(seed)
+    nrc = nrow * ncol
+    n = nlay * nrc
+    k = np.exp(rng.normal(0.0, 1.0, n))
+    m = GwfDisModel(nlay, nrow, ncol, np.full(ncol, 10.0), np.full(nrow, 10.0),
+                    np.full(nrc, 10.0 * nlay), np.repeat(10.0 * (nlay - 1 - np.arange(nlay)), nrc),
+                    k, 0.1 * k, np.zeros(n, np.int32), np.full(n, 5.0))
+    m.chd_node = np.array([0], np.int32)
+    m.chd_head = np.array([1.0])
+    m.wel_node = np.array([n - 1], np.int32)
+    m.wel_q = np.array([-3.0])
+    g = oracle.Gwf(m, oracle.settings())
+    x0 = g.x.copy()
+    x0[m.chd_node] = m.chd_head
+    amat, rhs = g.assemble(x0)
+    amat, rhs = g.fixups(amat, rhs, x0, isymmetric=isym)
+    return m, g.con, amat, rhs, x0
+
+
+SHAPES = [(1, 1, 7), (3, 1, 1), (1, 5, 1), (2, 3, 4), (1, 33, 5), (2, 65, 3), (3, 40, 41), (10, 70, 64)]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_structured_precondition_matches_oracle(gblib, shape):
+    m, con, amat, rhs, x0 = dis_system(*shape)
+    ims = ImsLinear(ImsLinearSettings(structure=shape)).imslinear_allocate(m.nodes, con["ia"], con["ja"])
+    assert gblib.gbims_factor(ims._h, _lib.dptr(amat), None) == 0
+    v = np.random.default_rng(5).standard_normal(m.nodes)
+    z = np.zeros_like(v)
+    assert gblib.gbims_precondition(ims._h, _lib.dptr(v), _lib.dptr(z)) == 0
+    o = oracle.Ims(oracle.settings(), con["ia"], con["ja"])
+    o.apply(amat.copy(), rhs.copy(), x0.copy())
+    zo = oracle.ilu0a(o.apc(), o.iapc(), o.japc(), v, fma=True)
+    scale = np.max(np.abs(zo))
+    assert np.max(np.abs(z - zo)) <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("ilinmeth", [1, 2])
+@pytest.mark.parametrize("precision", [_lib.GBIMS_FP64, _lib.GBIMS_MIXED])
+def test_structured_solve_c2_small(gblib, ilinmeth, precision):
+    m = make_config("c2", seed=4, scale=0.06)
+    g = oracle.Gwf(m, oracle.settings())
+    x0 = g.x.copy()
+    x0[m.chd_node] = m.chd_head
+    amat, rhs = g.assemble(x0)
+    amat, rhs = g.fixups(amat, rhs, x0, isymmetric=(ilinmeth == 1))
+    tol = dict(dvclose=1e-8, rclose=1e-4, iter1=2000)
+    o = oracle.Ims(oracle.settings(ilinmeth=ilinmeth, **tol), g.con["ia"], g.con["ja"])
+    xo = x0.copy()
+    icnvg_o, it_o, _ = o.apply(amat.copy(), rhs.copy(), xo)
+    s = ImsLinearSettings(ilinmeth=ilinmeth, precision=precision,
+                          structure=(m.nlay, m.nrow, m.ncol), **tol)
+    ims = ImsLinear(s).imslinear_allocate(m.nodes, g.con["ia"], g.con["ja"])
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.summary["structured"] == 1
+    assert r.icnvg == 1 and icnvg_o == 1
+    assert np.max(np.abs(x - xo)) <= 0.1 * tol["dvclose"], np.max(np.abs(x - xo))
+    if precision == _lib.GBIMS_FP64:
+        assert abs(r.in_iter - it_o) <= max(2, int(0.05 * it_o)), (r.in_iter, it_o)
