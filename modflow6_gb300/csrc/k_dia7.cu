@@ -8,17 +8,25 @@
 // seven length-n arrays (no index arrays).
 //
 // Wavefront: a "line" is the ncol cells of one grid row (k,i).  One warp
-// (one CTA) owns 32 consecutive lines i0..i0+31 of one layer k; lane l walks
-// its line in column order, two steps behind lane l-1, so the value it needs
-// from line i-1 was produced two steps earlier and arrives by a register
-// shuffle, and the only dependency that is fresh at each step is the lane's
-// own previous column (one FMA on the critical path).  Lines of the previous
-// warp (i0-1) and of the layer above (k-1) come through global memory; each
-// warp publishes its progress after every chunk of C steps with a release
-// store, consumers wait with acquire loads bounded by the global timer (a
-// wait that runs out sets an error flag and Ctl::done, it never hangs).
-// Warps take a ticket in launch order and depend only on smaller tickets, so
-// the wait chain always ends.
+// (one CTA) owns W consecutive lines i0..i0+W-1 of one layer k; lane l walks
+// its line in column order one step behind lane l-1, so the value it needs
+// from line i-1 is the one lane l-1 produced in the previous step and
+// arrives by a register shuffle.  Lines of the previous warp (i0-1) and of
+// the layer above (k-1) come through global memory: every warp publishes its
+// progress after each chunk of C steps with a release store; consumers wait
+// with acquire loads bounded by the global timer (a wait that runs out sets
+// an error flag and Ctl::done; it never hangs).  All loads of chunk c+1 --
+// the local factors and right-hand side and the neighbour warps' results --
+// are issued at the start of chunk c into registers, so memory latency is
+// hidden behind one chunk of arithmetic; the price is a lag of one more
+// chunk between a warp and the warps it depends on.  Warps take a ticket in
+// launch order and depend only on smaller tickets, so the wait chain always
+// ends.
+//
+// W < 32 leaves lanes idle on purpose: on GB300 the FP64 pipe of an SM
+// sub-partition retires about half a lane-FMA per clock, so a 32-lane FP64
+// FMA occupies it for ~67 cycles and the wavefront step time scales with
+// the number of active lanes.
 //
 // Forward sweep: y = r - Lz*y(k-1) - Ly*y(i-1) - Lx*y(j-1), in the reference's
 // order (ascending column), bit-identical to the level kernel.
@@ -32,7 +40,7 @@ namespace gb {
 
 namespace {
 
-constexpr int kChunk = 16;
+constexpr int kChunk = 8;
 constexpr unsigned long long kWaitNs = 2000000000ULL;  // 2 s per wait
 
 __device__ __forceinline__ unsigned long long gtimer() {
@@ -51,7 +59,7 @@ __device__ __forceinline__ void st_release(int *p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Wait (lane 0) until *flag >= need; returns false if the wait ran out.
+// Wait until *flag >= need; false if the wait ran out.
 __device__ __forceinline__ bool wait_flag(const int *flag, int need) {
   if (ld_acquire(flag) >= need) return true;
   unsigned long long t0 = gtimer();
@@ -62,132 +70,129 @@ __device__ __forceinline__ bool wait_flag(const int *flag, int need) {
 }
 
 template <typename T>
-__device__ __forceinline__ T ldc(const T *p) { return __ldcg(p); }
-
-template <typename T>
 struct Fac {
   const T *lz, *ly, *lx, *ux, *uy, *uz, *dinv;
 };
 
+// Loads of one chunk for one lane.
 template <typename T>
-__global__ void __launch_bounds__(32) k_dia7_fwd(int nlay, int nrow, int ncol, Fac<T> f,
-                                                  const T *__restrict__ r, T *y, int *flags,
-                                                  int *err, Ctl *ctl) {
-  if (ctl && ctl->done) return;
-  const int lane = threadIdx.x;
-  int id = 0;
-  if (lane == 0) id = atomicAdd(&flags[0], 1);
-  id = __shfl_sync(0xffffffffu, id, 0);
-  const int k = id % nlay, b = id / nlay;
-  const int i = 32 * b + lane;
-  const long long nrc = (long long)nrow * ncol;
-  const int nsteps = ncol + 62;
-  const int nchunks = (nsteps + kChunk - 1) / kChunk;
-  const int total = nchunks * kChunk;
-  int *prog = flags + 1;
-  const int *pb = (b > 0) ? prog + (id - nlay) : nullptr;
-  const int *pu = (k > 0) ? prog + (id - 1) : nullptr;
-  const bool line_ok = i < nrow;
-  const long long base = k * nrc + (long long)i * ncol;
-  T out1 = T(0), out2 = T(0);
-  for (int c = 0; c < nchunks; ++c) {
-    int ok = 1;
-    if (lane == 0) {
-      if (pb && !wait_flag(pb, min((c + 1) * kChunk + 62, total))) ok = 0;
-      if (ok && pu && !wait_flag(pu, (c + 1) * kChunk)) ok = 0;
-      if (!ok) {
-        atomicExch(err, 1);
-        if (ctl) ctl->done = 1;
-      }
-    }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) return;
-#pragma unroll 4
-    for (int t = 0; t < kChunk; ++t) {
-      const int g = c * kChunk + t;
-      const int j = g - 2 * lane;
-      const bool valid = line_ok && j >= 0 && j < ncol;
-      T yb = __shfl_up_sync(0xffffffffu, out2, 1);
-      T tv = T(0);
-      if (valid) {
-        const long long n = base + j;
-        tv = r[n];
-        if (k > 0) tv = fma(-__ldg(f.lz + n), ldc(y + n - nrc), tv);
-        if (i > 0) {
-          if (lane == 0) yb = ldc(y + n - ncol);
-          tv = fma(-__ldg(f.ly + n), yb, tv);
-        }
-        if (j > 0) tv = fma(-__ldg(f.lx + n), out1, tv);
-        y[n] = tv;
-      }
-      out2 = out1;
-      out1 = tv;
-    }
-    __syncwarp();
-    if (lane == 0) {
-      __threadfence();
-      st_release(prog + id, (c + 1) * kChunk);
-    }
-  }
-}
+struct Chunk {
+  T r[kChunk], a[kChunk], b[kChunk], c[kChunk], zn[kChunk], yn[kChunk];
+};
 
-template <typename T>
-__global__ void __launch_bounds__(32) k_dia7_bwd(int nlay, int nrow, int ncol, Fac<T> f,
-                                                  const T *y, T *z, int *flags, int *err,
-                                                  Ctl *ctl) {
+// DIR = +1: forward sweep (lines ascending, columns left to right).
+// DIR = -1: backward sweep (lines descending, columns right to left).
+template <typename T, int W, int DIR>
+__global__ void __launch_bounds__(32) k_dia7_sweep(int nlay, int nrow, int ncol, Fac<T> f,
+                                                    const T *__restrict__ rin, T *out,
+                                                    int *flags, int *err, Ctl *ctl) {
   if (ctl && ctl->done) return;
   const int lane = threadIdx.x;
   int id = 0;
   if (lane == 0) id = atomicAdd(&flags[0], 1);
   id = __shfl_sync(0xffffffffu, id, 0);
-  const int nb = (nrow + 31) / 32;
-  // tickets run from the last line block and the bottom layer upwards
-  const int k = nlay - 1 - (id % nlay), b = nb - 1 - id / nlay;
-  const int l = 31 - lane;  // lane 0 holds the highest line of the block
-  const int i = 32 * b + l;
+  const int nb = (nrow + W - 1) / W;
+  int k, b;
+  if (DIR > 0) {
+    k = id % nlay;
+    b = id / nlay;
+  } else {
+    k = nlay - 1 - (id % nlay);
+    b = nb - 1 - id / nlay;
+  }
+  // lane l walks line i: ascending lines for the forward sweep, descending
+  // for the backward sweep, so lane l-1 always holds the line it depends on
+  const int l = lane;
+  const int i = (DIR > 0) ? (b * W + l) : (b * W + (W - 1 - l));
+  const bool active = (l < W);
+  const bool line_ok = active && i >= 0 && i < nrow;
   const long long nrc = (long long)nrow * ncol;
-  const int nsteps = ncol + 62;
+  const int nsteps = ncol + (W - 1);
   const int nchunks = (nsteps + kChunk - 1) / kChunk;
   const int total = nchunks * kChunk;
   int *prog = flags + 1;
-  const int *pb = (b < nb - 1) ? prog + (id - nlay) : nullptr;  // block i0+32
-  const int *pu = (k < nlay - 1) ? prog + (id - 1) : nullptr;   // layer k+1
-  const bool line_ok = i < nrow;
-  const bool has_next_line = (i + 1 < nrow);
+  const bool has_blk = (DIR > 0) ? (b > 0) : (b < nb - 1);  // neighbour line block
+  const bool has_lay = (DIR > 0) ? (k > 0) : (k < nlay - 1);  // neighbour layer
+  const int *pb = has_blk ? prog + (id - nlay) : nullptr;
+  const int *pu = has_lay ? prog + (id - 1) : nullptr;
   const long long base = k * nrc + (long long)i * ncol;
-  T out1 = T(0), out2 = T(0);
-  for (int c = 0; c < nchunks; ++c) {
+  const long long dz = DIR * nrc;      // neighbour in the next/previous layer
+  const long long dyl = DIR * (long long)ncol;  // neighbour line
+  // the neighbour line of lane 0 lives in the other block; it exists unless
+  // this is the first line of the sweep
+  const bool lane0_has_y = (DIR > 0) ? (i > 0) : (i + 1 < nrow);
+  const bool y_exists = line_ok && ((DIR > 0) ? (i > 0) : (i + 1 < nrow));
+  // per-lane element of step g: column index along the walk
+  auto col_of = [&](int g) { int jj = g - l; return (DIR > 0) ? jj : (ncol - 1 - jj); };
+  auto walk_of = [&](int g) { return g - l; };
+
+  auto load_chunk = [&](int c, Chunk<T> &ch) {
+#pragma unroll
+    for (int t = 0; t < kChunk; ++t) {
+      const int g = c * kChunk + t;
+      const int jj = walk_of(g);
+      const bool valid = line_ok && jj >= 0 && jj < ncol;
+      T r = T(0), a = T(0), bb = T(0), cc = T(0), zn = T(0), yn = T(0);
+      if (valid) {
+        const int j = col_of(g);
+        const long long n = base + j;
+        if (DIR > 0) {
+          r = __ldg(rin + n);
+          a = __ldg(f.lz + n);
+          bb = __ldg(f.ly + n);
+          cc = __ldg(f.lx + n);
+        } else {
+          r = __ldg(f.dinv + n) * out[n];  // dinv * y (own cell, written by the forward sweep)
+          a = __ldg(f.uz + n);
+          bb = __ldg(f.uy + n);
+          cc = __ldg(f.ux + n);
+        }
+        if (has_lay) zn = __ldcg(out + n - dz);
+        if (lane == 0 && lane0_has_y) yn = __ldcg(out + n - dyl);
+      }
+      ch.r[t] = r; ch.a[t] = a; ch.b[t] = bb; ch.c[t] = cc; ch.zn[t] = zn; ch.yn[t] = yn;
+    }
+  };
+  // data for chunk c needs: neighbour block progress >= (c+1)*C + W - 1 (its
+  // last lane) ... capped by its total; neighbour layer progress >= (c+1)*C
+  auto wait_for = [&](int c) -> bool {
     int ok = 1;
     if (lane == 0) {
-      if (pb && !wait_flag(pb, min((c + 1) * kChunk + 62, total))) ok = 0;
-      if (ok && pu && !wait_flag(pu, (c + 1) * kChunk)) ok = 0;
+      if (pb && !wait_flag(pb, min((c + 1) * kChunk + (W - 1), total))) ok = 0;
+      if (ok && pu && !wait_flag(pu, min((c + 1) * kChunk, total))) ok = 0;
       if (!ok) {
         atomicExch(err, 1);
         if (ctl) ctl->done = 1;
       }
     }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    if (!ok) return;
-#pragma unroll 4
+    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+  };
+
+  Chunk<T> cur, nxt;
+  if (!wait_for(0)) return;
+  load_chunk(0, cur);
+  T out1 = T(0);  // this lane's previous result (x neighbour)
+  for (int c = 0; c < nchunks; ++c) {
+    const bool more = (c + 1 < nchunks);
+    if (more) {
+      if (!wait_for(c + 1)) return;
+      load_chunk(c + 1, nxt);
+    }
+#pragma unroll
     for (int t = 0; t < kChunk; ++t) {
       const int g = c * kChunk + t;
-      const int jj = g - 2 * lane;        // steps taken along the line
-      const int j = ncol - 1 - jj;        // column, walked right to left
+      const int jj = walk_of(g);
       const bool valid = line_ok && jj >= 0 && jj < ncol;
-      T zb = __shfl_up_sync(0xffffffffu, out2, 1);
+      T yprev = __shfl_up_sync(0xffffffffu, out1, 1);  // lane l-1, previous step = same column
+      if (lane == 0) yprev = cur.yn[t];
       T tv = T(0);
       if (valid) {
-        const long long n = base + j;
-        tv = __ldg(f.dinv + n) * y[n];
-        if (k < nlay - 1) tv = fma(-__ldg(f.uz + n), ldc(z + n + nrc), tv);
-        if (has_next_line) {
-          if (lane == 0) zb = ldc(z + n + ncol);
-          tv = fma(-__ldg(f.uy + n), zb, tv);
-        }
-        if (j < ncol - 1) tv = fma(-__ldg(f.ux + n), out1, tv);
-        z[n] = tv;
+        tv = cur.r[t];
+        if (has_lay) tv = fma(-cur.a[t], cur.zn[t], tv);
+        if (y_exists) tv = fma(-cur.b[t], yprev, tv);
+        if (jj > 0) tv = fma(-cur.c[t], out1, tv);
+        out[base + col_of(g)] = tv;
       }
-      out2 = out1;
       out1 = tv;
     }
     __syncwarp();
@@ -195,6 +200,7 @@ __global__ void __launch_bounds__(32) k_dia7_bwd(int nlay, int nrow, int ncol, F
       __threadfence();
       st_release(prog + id, (c + 1) * kChunk);
     }
+    if (more) cur = nxt;
   }
 }
 
@@ -267,30 +273,41 @@ void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_j
                                                 D.f_dinv);
 }
 
+// Lines per warp: FP64 steps are bounded by the FP64 pipe (fewer lanes per
+// warp, shorter steps), FP32 steps by latency (full warps).
 template <typename T>
-static void apply_t(const Dia7 &D, Fac<T> f, const T *r, T *z, T *ywork, const Ctl *ctl,
-                    cudaStream_t st) {
-  int nb = (D.nrow + 31) / 32;
+struct LinesPerWarp;
+template <>
+struct LinesPerWarp<double> { static constexpr int W = 16; };
+template <>
+struct LinesPerWarp<float> { static constexpr int W = 32; };
+
+template <typename T>
+static void apply_t(const Dia7 &D, Fac<T> f, const T *r, T *z, const Ctl *ctl, cudaStream_t st) {
+  constexpr int W = LinesPerWarp<T>::W;
+  int nb = (D.nrow + W - 1) / W;
   int nct = nb * D.nlay;
   cudaMemsetAsync(D.d_flags, 0, sizeof(int) * (nct + 1), st);
-  k_dia7_fwd<T><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, r, ywork, D.d_flags, D.d_err,
-                                    const_cast<Ctl *>(ctl));
+  k_dia7_sweep<T, W, 1><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, r, z, D.d_flags, D.d_err,
+                                            const_cast<Ctl *>(ctl));
   cudaMemsetAsync(D.d_flags, 0, sizeof(int) * (nct + 1), st);
-  k_dia7_bwd<T><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, ywork, z, D.d_flags, D.d_err,
-                                    const_cast<Ctl *>(ctl));
+  k_dia7_sweep<T, W, -1><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, nullptr, z, D.d_flags,
+                                             D.d_err, const_cast<Ctl *>(ctl));
 }
+
+int dia7_nflags(int nlay, int nrow) { return nlay * ((nrow + 15) / 16) + 2; }
 
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
                          cudaStream_t st) {
   Fac<double> f{D.d_lz, D.d_ly, D.d_lx, D.d_ux, D.d_uy, D.d_uz, D.d_dinv};
   // the forward result is written into z and swept backwards in place
-  apply_t<double>(D, f, r, z, z, ctl, st);
+  apply_t<double>(D, f, r, z, ctl, st);
 }
 
 void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
                          cudaStream_t st) {
   Fac<float> f{D.f_lz, D.f_ly, D.f_lx, D.f_ux, D.f_uy, D.f_uz, D.f_dinv};
-  apply_t<float>(D, f, r, z, z, ctl, st);
+  apply_t<float>(D, f, r, z, ctl, st);
 }
 
 }  // namespace gb
