@@ -8,25 +8,27 @@
 // seven length-n arrays (no index arrays).
 //
 // Wavefront: a "line" is the ncol cells of one grid row (k,i).  One warp
-// (one CTA) owns W consecutive lines i0..i0+W-1 of one layer k; lane l walks
-// its line in column order one step behind lane l-1, so the value it needs
-// from line i-1 is the one lane l-1 produced in the previous step and
-// arrives by a register shuffle.  Lines of the previous warp (i0-1) and of
-// the layer above (k-1) come through global memory: every warp publishes its
-// progress after each chunk of C steps with a release store; consumers wait
-// with acquire loads bounded by the global timer (a wait that runs out sets
-// an error flag and Ctl::done; it never hangs).  All loads of chunk c+1 --
-// the local factors and right-hand side and the neighbour warps' results --
-// are issued at the start of chunk c into registers, so memory latency is
-// hidden behind one chunk of arithmetic; the price is a lag of one more
-// chunk between a warp and the warps it depends on.  Warps take a ticket in
-// launch order and depend only on smaller tickets, so the wait chain always
-// ends.
+// (one CTA) owns W consecutive lines of one layer; lane l walks its line
+// S steps behind lane l-1, so the value it needs from the neighbour line was
+// produced S steps earlier by lane l-1 and arrives by a register shuffle.
+// With S = 2 (FP64) the only operation on the critical path of a step is the
+// FMA with the lane's own previous column; with S = 1 (FP32, short FMA
+// latency) the neighbour-line FMA joins it.  Lines of the neighbour block and
+// of the neighbour layer come through global memory: each warp publishes its
+// progress after every chunk of C steps; a consumer reads the producers'
+// progress words early (relaxed loads that complete behind a chunk of
+// arithmetic) and spins only when they are short, with a wait bounded by the
+// global timer (a wait that runs out sets an error flag and Ctl::done; it
+// never hangs).  The factors, the right-hand side and the neighbour results
+// of chunk c+1 are loaded at the start of chunk c through per-lane running
+// pointers, so memory latency hides behind one chunk of arithmetic.  Warps
+// take a ticket in launch order and depend only on smaller tickets, so the
+// wait chain always ends.
 //
 // W < 32 leaves lanes idle on purpose: on GB300 the FP64 pipe of an SM
 // sub-partition retires about half a lane-FMA per clock, so a 32-lane FP64
-// FMA occupies it for ~67 cycles and the wavefront step time scales with
-// the number of active lanes.
+// FMA occupies it for ~67 cycles and the wavefront step time scales with the
+// number of active lanes.
 //
 // Forward sweep: y = r - Lz*y(k-1) - Ly*y(i-1) - Lx*y(j-1), in the reference's
 // order (ascending column), bit-identical to the level kernel.
@@ -40,7 +42,6 @@ namespace gb {
 
 namespace {
 
-constexpr int kChunk = 8;
 constexpr unsigned long long kWaitNs = 2000000000ULL;  // 2 s per wait
 
 __device__ __forceinline__ unsigned long long gtimer() {
@@ -49,24 +50,14 @@ __device__ __forceinline__ unsigned long long gtimer() {
   return t;
 }
 
-__device__ __forceinline__ int ld_acquire(const int *p) {
+__device__ __forceinline__ int ld_relaxed(const int *p) {
   int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 
-__device__ __forceinline__ void st_release(int *p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-// Wait until *flag >= need; false if the wait ran out.
-__device__ __forceinline__ bool wait_flag(const int *flag, int need) {
-  if (ld_acquire(flag) >= need) return true;
-  unsigned long long t0 = gtimer();
-  while (ld_acquire(flag) < need) {
-    if (gtimer() - t0 > kWaitNs) return false;
-  }
-  return true;
+__device__ __forceinline__ void st_relaxed(int *p, int v) {
+  asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 template <typename T>
@@ -74,15 +65,14 @@ struct Fac {
   const T *lz, *ly, *lx, *ux, *uy, *uz, *dinv;
 };
 
-// Loads of one chunk for one lane.
-template <typename T>
+template <typename T, int C>
 struct Chunk {
-  T r[kChunk], a[kChunk], b[kChunk], c[kChunk], zn[kChunk], yn[kChunk];
+  T r[C], a[C], b[C], x[C], zn[C], yn[C];
 };
 
 // DIR = +1: forward sweep (lines ascending, columns left to right).
 // DIR = -1: backward sweep (lines descending, columns right to left).
-template <typename T, int W, int DIR>
+template <typename T, int W, int S, int C, int DIR>
 __global__ void __launch_bounds__(32) k_dia7_sweep(int nlay, int nrow, int ncol, Fac<T> f,
                                                     const T *__restrict__ rin, T *out,
                                                     int *flags, int *err, Ctl *ctl) {
@@ -92,113 +82,115 @@ __global__ void __launch_bounds__(32) k_dia7_sweep(int nlay, int nrow, int ncol,
   if (lane == 0) id = atomicAdd(&flags[0], 1);
   id = __shfl_sync(0xffffffffu, id, 0);
   const int nb = (nrow + W - 1) / W;
-  int k, b;
-  if (DIR > 0) {
-    k = id % nlay;
-    b = id / nlay;
-  } else {
-    k = nlay - 1 - (id % nlay);
-    b = nb - 1 - id / nlay;
-  }
-  // lane l walks line i: ascending lines for the forward sweep, descending
-  // for the backward sweep, so lane l-1 always holds the line it depends on
-  const int l = lane;
-  const int i = (DIR > 0) ? (b * W + l) : (b * W + (W - 1 - l));
-  const bool active = (l < W);
-  const bool line_ok = active && i >= 0 && i < nrow;
+  const int k = (DIR > 0) ? id % nlay : nlay - 1 - (id % nlay);
+  const int b = (DIR > 0) ? id / nlay : nb - 1 - id / nlay;
+  const int i = (DIR > 0) ? (b * W + lane) : (b * W + (W - 1 - lane));
+  const bool line_ok = lane < W && i >= 0 && i < nrow;
   const long long nrc = (long long)nrow * ncol;
-  const int nsteps = ncol + (W - 1);
-  const int nchunks = (nsteps + kChunk - 1) / kChunk;
-  const int total = nchunks * kChunk;
+  const int nch = (ncol + S * (W - 1) + C - 1) / C;
+  const int total = nch * C;
   int *prog = flags + 1;
-  const bool has_blk = (DIR > 0) ? (b > 0) : (b < nb - 1);  // neighbour line block
-  const bool has_lay = (DIR > 0) ? (k > 0) : (k < nlay - 1);  // neighbour layer
+  const bool has_blk = (DIR > 0) ? (b > 0) : (b < nb - 1);
+  const bool has_lay = (DIR > 0) ? (k > 0) : (k < nlay - 1);
   const int *pb = has_blk ? prog + (id - nlay) : nullptr;
   const int *pu = has_lay ? prog + (id - 1) : nullptr;
-  const long long base = k * nrc + (long long)i * ncol;
-  const long long dz = DIR * nrc;      // neighbour in the next/previous layer
-  const long long dyl = DIR * (long long)ncol;  // neighbour line
-  // the neighbour line of lane 0 lives in the other block; it exists unless
-  // this is the first line of the sweep
-  const bool lane0_has_y = (DIR > 0) ? (i > 0) : (i + 1 < nrow);
-  const bool y_exists = line_ok && ((DIR > 0) ? (i > 0) : (i + 1 < nrow));
-  // per-lane element of step g: column index along the walk
-  auto col_of = [&](int g) { int jj = g - l; return (DIR > 0) ? jj : (ncol - 1 - jj); };
-  auto walk_of = [&](int g) { return g - l; };
+  // neighbour line exists for this lane (lane 0's lives in the other block)
+  const bool has_y = line_ok && ((DIR > 0) ? (i > 0) : (i + 1 < nrow));
+  const bool y_from_mem = has_y && lane == 0;
+  const bool z_on = line_ok && has_lay;
+  // element of step g: e(g) = e0 + DIR*g; walk index jj(g) = g - S*lane
+  const long long base = k * nrc + (long long)(line_ok ? i : 0) * ncol;
+  const long long e0 = (DIR > 0) ? base - (long long)S * lane : base + ncol - 1 + (long long)S * lane;
+  const long long zoff = -(long long)DIR * nrc;
+  const long long yoff = -(long long)DIR * ncol;
+  const T *A = (DIR > 0) ? f.lz : f.uz;
+  const T *B = (DIR > 0) ? f.ly : f.uy;
+  const T *X = (DIR > 0) ? f.lx : f.ux;
+  int seen_b = 0, seen_u = 0;
 
-  auto load_chunk = [&](int c, Chunk<T> &ch) {
-#pragma unroll
-    for (int t = 0; t < kChunk; ++t) {
-      const int g = c * kChunk + t;
-      const int jj = walk_of(g);
-      const bool valid = line_ok && jj >= 0 && jj < ncol;
-      T r = T(0), a = T(0), bb = T(0), cc = T(0), zn = T(0), yn = T(0);
-      if (valid) {
-        const int j = col_of(g);
-        const long long n = base + j;
-        if (DIR > 0) {
-          r = __ldg(rin + n);
-          a = __ldg(f.lz + n);
-          bb = __ldg(f.ly + n);
-          cc = __ldg(f.lx + n);
-        } else {
-          r = __ldg(f.dinv + n) * out[n];  // dinv * y (own cell, written by the forward sweep)
-          a = __ldg(f.uz + n);
-          bb = __ldg(f.uy + n);
-          cc = __ldg(f.ux + n);
-        }
-        if (has_lay) zn = __ldcg(out + n - dz);
-        if (lane == 0 && lane0_has_y) yn = __ldcg(out + n - dyl);
-      }
-      ch.r[t] = r; ch.a[t] = a; ch.b[t] = bb; ch.c[t] = cc; ch.zn[t] = zn; ch.yn[t] = yn;
-    }
-  };
-  // data for chunk c needs: neighbour block progress >= (c+1)*C + W - 1 (its
-  // last lane) ... capped by its total; neighbour layer progress >= (c+1)*C
-  auto wait_for = [&](int c) -> bool {
+  // make sure the producers have published what chunk c needs
+  auto ensure = [&](int c) -> bool {
     int ok = 1;
     if (lane == 0) {
-      if (pb && !wait_flag(pb, min((c + 1) * kChunk + (W - 1), total))) ok = 0;
-      if (ok && pu && !wait_flag(pu, min((c + 1) * kChunk, total))) ok = 0;
+      const int nb_need = min((c + 1) * C + S * (W - 1), total);
+      const int nu_need = min((c + 1) * C, total);
+      if (pb && seen_b < nb_need) {
+        unsigned long long t0 = gtimer();
+        while ((seen_b = ld_relaxed(pb)) < nb_need)
+          if (gtimer() - t0 > kWaitNs) { ok = 0; break; }
+      }
+      if (ok && pu && seen_u < nu_need) {
+        unsigned long long t0 = gtimer();
+        while ((seen_u = ld_relaxed(pu)) < nu_need)
+          if (gtimer() - t0 > kWaitNs) { ok = 0; break; }
+      }
       if (!ok) {
         atomicExch(err, 1);
         if (ctl) ctl->done = 1;
       }
+      // early reads for the next check; they complete behind a chunk of work
+      if (ok && pb) seen_b = ld_relaxed(pb);
+      if (ok && pu) seen_u = ld_relaxed(pu);
     }
+    __syncwarp();
     return __shfl_sync(0xffffffffu, ok, 0) != 0;
   };
 
-  Chunk<T> cur, nxt;
-  if (!wait_for(0)) return;
-  load_chunk(0, cur);
-  T out1 = T(0);  // this lane's previous result (x neighbour)
-  for (int c = 0; c < nchunks; ++c) {
-    const bool more = (c + 1 < nchunks);
-    if (more) {
-      if (!wait_for(c + 1)) return;
-      load_chunk(c + 1, nxt);
-    }
+  auto load = [&](int c, Chunk<T, C> &q) {
+    const long long ec = e0 + (long long)DIR * c * C;
+    const int jc = c * C - S * lane;
 #pragma unroll
-    for (int t = 0; t < kChunk; ++t) {
-      const int g = c * kChunk + t;
-      const int jj = walk_of(g);
-      const bool valid = line_ok && jj >= 0 && jj < ncol;
-      T yprev = __shfl_up_sync(0xffffffffu, out1, 1);  // lane l-1, previous step = same column
-      if (lane == 0) yprev = cur.yn[t];
-      T tv = T(0);
-      if (valid) {
-        tv = cur.r[t];
-        if (has_lay) tv = fma(-cur.a[t], cur.zn[t], tv);
-        if (y_exists) tv = fma(-cur.b[t], yprev, tv);
-        if (jj > 0) tv = fma(-cur.c[t], out1, tv);
-        out[base + col_of(g)] = tv;
+    for (int t = 0; t < C; ++t) {
+      const long long e = ec + DIR * t;
+      const bool v = line_ok && (unsigned)(jc + t) < (unsigned)ncol;
+      T r = T(0), a = T(0), bb = T(0), x = T(0), zn = T(0), yn = T(0);
+      if (v) {
+        if (DIR > 0) r = __ldg(rin + e);
+        else r = __ldg(f.dinv + e) * out[e];  // dinv * y: own cell, still the forward value
+        bb = __ldg(B + e);
+        x = __ldg(X + e);
+        if (z_on) {
+          a = __ldg(A + e);
+          zn = __ldcg(out + e + zoff);
+        }
+        if (y_from_mem) yn = __ldcg(out + e + yoff);
       }
-      out1 = tv;
+      q.r[t] = r; q.a[t] = a; q.b[t] = bb; q.x[t] = x; q.zn[t] = zn; q.yn[t] = yn;
+    }
+  };
+
+  Chunk<T, C> cur, nxt;
+  if (!ensure(0)) return;
+  load(0, cur);
+  T h1 = T(0), h2 = T(0);  // this lane's results of the last two steps
+  for (int c = 0; c < nch; ++c) {
+    const bool more = (c + 1 < nch);
+    if (more) {
+      if (!ensure(c + 1)) return;
+      load(c + 1, nxt);
+    }
+    const long long ec = e0 + (long long)DIR * c * C;
+    const int jc = c * C - S * lane;
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+      // neighbour line, same column: lane-1's result S steps ago
+      T yv = __shfl_up_sync(0xffffffffu, (S == 1) ? h1 : h2, 1);
+      if (lane == 0) yv = cur.yn[t];
+      const int jj = jc + t;
+      T tv = cur.r[t];
+      tv = fma(-cur.a[t], cur.zn[t], tv);
+      if (has_y) tv = fma(-cur.b[t], yv, tv);
+      if (jj > 0) tv = fma(-cur.x[t], h1, tv);
+      const bool v = line_ok && (unsigned)jj < (unsigned)ncol;
+      if (v) out[ec + DIR * t] = tv;
+      else tv = T(0);
+      h2 = h1;
+      h1 = tv;
     }
     __syncwarp();
     if (lane == 0) {
       __threadfence();
-      st_release(prog + id, (c + 1) * kChunk);
+      st_relaxed(prog + id, (c + 1) * C);
     }
     if (more) cur = nxt;
   }
@@ -273,29 +265,28 @@ void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_j
                                                 D.f_dinv);
 }
 
-// Lines per warp: FP64 steps are bounded by the FP64 pipe (fewer lanes per
-// warp, shorter steps), FP32 steps by latency (full warps).
+// Wavefront shape per precision: lines per warp W, lane skew S, chunk C.
 template <typename T>
-struct LinesPerWarp;
+struct Shape;
 template <>
-struct LinesPerWarp<double> { static constexpr int W = 16; };
+struct Shape<double> { static constexpr int W = 16, S = 2, C = 8; };
 template <>
-struct LinesPerWarp<float> { static constexpr int W = 32; };
+struct Shape<float> { static constexpr int W = 32, S = 1, C = 8; };
 
 template <typename T>
 static void apply_t(const Dia7 &D, Fac<T> f, const T *r, T *z, const Ctl *ctl, cudaStream_t st) {
-  constexpr int W = LinesPerWarp<T>::W;
-  int nb = (D.nrow + W - 1) / W;
+  using P = Shape<T>;
+  int nb = (D.nrow + P::W - 1) / P::W;
   int nct = nb * D.nlay;
   cudaMemsetAsync(D.d_flags, 0, sizeof(int) * (nct + 1), st);
-  k_dia7_sweep<T, W, 1><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, r, z, D.d_flags, D.d_err,
-                                            const_cast<Ctl *>(ctl));
+  k_dia7_sweep<T, P::W, P::S, P::C, 1><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, r, z,
+                                                           D.d_flags, D.d_err,
+                                                           const_cast<Ctl *>(ctl));
   cudaMemsetAsync(D.d_flags, 0, sizeof(int) * (nct + 1), st);
-  k_dia7_sweep<T, W, -1><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, nullptr, z, D.d_flags,
-                                             D.d_err, const_cast<Ctl *>(ctl));
+  k_dia7_sweep<T, P::W, P::S, P::C, -1><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, nullptr, z,
+                                                            D.d_flags, D.d_err,
+                                                            const_cast<Ctl *>(ctl));
 }
-
-int dia7_nflags(int nlay, int nrow) { return nlay * ((nrow + 15) / 16) + 2; }
 
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
                          cudaStream_t st) {

@@ -75,12 +75,11 @@ def test_structured_solve_c2_small(gblib, ilinmeth, precision):
     r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
     assert r.summary["structured"] == 1
     assert r.icnvg == 1 and icnvg_o == 1
-    direct = ilinmeth == 1 and precision == _lib.GBIMS_FP64
-    x_star = None
-    if not direct:
-        ts = oracle.settings(ilinmeth=ilinmeth, dvclose=1e-13, rclose=1e-11, iter1=20000)
-        x_star = x0.copy()
-        oracle.Ims(ts, g.con["ia"], g.con["ja"]).apply(amat.copy(), rhs.copy(), x_star)
-    assert_closure_parity(x, xo, x_star, tol["dvclose"], direct)
+    # the structured backward sweep rounds differently from ilu0a, so even
+    # PCG stops an iteration or so apart: compare accuracy, not iterates
+    ts = oracle.settings(ilinmeth=ilinmeth, dvclose=1e-13, rclose=1e-11, iter1=20000)
+    x_star = x0.copy()
+    oracle.Ims(ts, g.con["ia"], g.con["ja"]).apply(amat.copy(), rhs.copy(), x_star)
+    assert_closure_parity(x, xo, x_star, tol["dvclose"], False)
     if precision == _lib.GBIMS_FP64:
         assert abs(r.in_iter - it_o) <= max(2, int(0.05 * it_o)), (r.in_iter, it_o)
