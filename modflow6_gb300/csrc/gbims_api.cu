@@ -319,24 +319,26 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
     h->D.nlay = s->nlay;
     h->D.nrow = s->nrow;
     h->D.ncol = s->ncol;
-    size_t nn = (size_t)neq;
+    dia7_geometry(s->nlay, s->nrow, s->ncol, h->mixed, &h->D.nb, &h->D.G, &h->D.slots);
+    size_t nn = (size_t)h->D.slots;
     if (!h->mixed) {
-      GB_CUDA(h, dalloc(&h->D.d_lz, nn)); GB_CUDA(h, dalloc(&h->D.d_ly, nn)); GB_CUDA(h, dalloc(&h->D.d_lx, nn));
-      GB_CUDA(h, dalloc(&h->D.d_ux, nn)); GB_CUDA(h, dalloc(&h->D.d_uy, nn)); GB_CUDA(h, dalloc(&h->D.d_uz, nn));
-      GB_CUDA(h, dalloc(&h->D.d_dinv, nn));
+      double **a[] = {&h->D.d_lz, &h->D.d_ly, &h->D.d_lx, &h->D.d_ux, &h->D.d_uy, &h->D.d_uz,
+                      &h->D.d_dinv, &h->D.d_rsk, &h->D.d_ysk, &h->D.d_zsk};
+      for (double **p : a) GB_CUDA(h, dalloc(p, nn));
     } else {
-      GB_CUDA(h, dalloc(&h->D.f_lz, nn)); GB_CUDA(h, dalloc(&h->D.f_ly, nn)); GB_CUDA(h, dalloc(&h->D.f_lx, nn));
-      GB_CUDA(h, dalloc(&h->D.f_ux, nn)); GB_CUDA(h, dalloc(&h->D.f_uy, nn)); GB_CUDA(h, dalloc(&h->D.f_uz, nn));
-      GB_CUDA(h, dalloc(&h->D.f_dinv, nn));
+      float **a[] = {&h->D.f_lz, &h->D.f_ly, &h->D.f_lx, &h->D.f_ux, &h->D.f_uy, &h->D.f_uz,
+                     &h->D.f_dinv, &h->D.f_rsk, &h->D.f_ysk, &h->D.f_zsk};
+      for (float **p : a) GB_CUDA(h, dalloc(p, nn));
     }
-    h->D.nflags = s->nlay * s->nrow + 64;
+    // one 128-byte progress line per CTA plus the ticket line
+    h->D.nflags = (s->nlay * h->D.nb + 2) * 32;
     GB_CUDA(h, dalloc(&h->D.d_flags, h->D.nflags));
     GB_CUDA(h, dalloc(&h->D.d_err, 4));
     GB_CUDA(h, cudaMemset(h->D.d_err, 0, sizeof(int) * 4));
     h->structured = true;
   }
-  // vectors
-  size_t nn = (size_t)neq;
+  // vectors (with slack after the last cell for the sweeps' aligned copies)
+  size_t nn = (size_t)neq + kVecPad;
   GB_CUDA(h, dalloc(&h->d_amat, nja));
   GB_CUDA(h, dalloc(&h->d_rhs, nn));
   GB_CUDA(h, dalloc(&h->d_x, nn));
@@ -664,6 +666,7 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->S.d_col, h->S.d_src, h->S.d_val, h->S.d_val32, h->F.d_rows, h->B.d_rows,
                   h->D.d_lz, h->D.d_ly, h->D.d_lx, h->D.d_ux, h->D.d_uy, h->D.d_uz, h->D.d_dinv,
                   h->D.f_lz, h->D.f_ly, h->D.f_lx, h->D.f_ux, h->D.f_uy, h->D.f_uz, h->D.f_dinv,
+                  h->D.d_rsk, h->D.d_ysk, h->D.d_zsk, h->D.f_rsk, h->D.f_ysk, h->D.f_zsk,
                   h->D.d_flags, h->D.d_err, h->d_amat, h->d_rhs, h->d_x, h->v_d, h->v_p, h->v_q,
                   h->v_z, h->v_t, h->v_v, h->v_dhat, h->v_phat, h->v_qhat, h->f_d, h->f_p,
                   h->f_q, h->f_z, h->f_t, h->f_v, h->f_dhat, h->f_phat, h->f_qhat, h->d_part,

@@ -93,20 +93,30 @@ struct Levels {
   int maxwidth = 0;
 };
 
-// Structured 7-point DIS layout of the ILU0 factors for the wavefront sweeps.
+// Structured 7-point DIS layout of the ILU0 factors for the wavefront sweeps:
+// per block of lines, G x W tiles (row = wavefront step, column = lane).
 struct Dia7 {
   int nlay = 0, nrow = 0, ncol = 0;
-  // lower coefficients L (unit diagonal) per row: z (layer above), y (row
-  // behind), x (column left); upper U: x, y, z; inverse pivot.  Length n each,
-  // 0 where the neighbour does not exist.
+  int nb = 0, G = 0;       // blocks per layer, padded steps per block
+  long long slots = 0;     // nlay * nb * G * W elements per array
+  // forward tiles: lower coefficients (unit diagonal) z (layer above),
+  // y (row behind), x (column left); backward tiles: dinv*U for z, y, x and
+  // dinv; zero where the neighbour or the cell does not exist
   double *d_lz = nullptr, *d_ly = nullptr, *d_lx = nullptr;
   double *d_ux = nullptr, *d_uy = nullptr, *d_uz = nullptr, *d_dinv = nullptr;
+  double *d_rsk = nullptr, *d_ysk = nullptr, *d_zsk = nullptr;  // skewed input and results
   float *f_lz = nullptr, *f_ly = nullptr, *f_lx = nullptr;
   float *f_ux = nullptr, *f_uy = nullptr, *f_uz = nullptr, *f_dinv = nullptr;
-  int *d_flags = nullptr;  // wavefront progress counters
+  float *f_rsk = nullptr, *f_ysk = nullptr, *f_zsk = nullptr;
+  int *d_flags = nullptr;  // wavefront progress words, one per 128-byte line
   int nflags = 0;
   int *d_err = nullptr;    // wait-limit error flag
 };
+
+// Elements of slack after every n-vector: the structured sweeps copy 16-byte
+// aligned segments that can run past the last cell.
+constexpr int kVecPad = 256;
+void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, long long *slots);
 
 // ---------------------------------------------------------------------------
 // kernel launchers (implemented in the .cu files)

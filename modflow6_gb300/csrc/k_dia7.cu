@@ -4,38 +4,46 @@
 // (src/Solution/LinearMethods/ImsLinearBase.f90:1049-1092) when the CSR
 // pattern is that of a full DIS grid in natural order (node = j + i*ncol +
 // k*nrow*ncol).  Row n then has at most three lower neighbours, (k-1,i,j),
-// (k,i-1,j), (k,i,j-1), and three upper ones, so the factors are stored as
-// seven length-n arrays (no index arrays).
+// (k,i-1,j), (k,i,j-1), and three upper ones.
 //
-// Wavefront: a "line" is the ncol cells of one grid row (k,i).  One warp
-// (one CTA) owns W consecutive lines of one layer; lane l walks its line
-// S steps behind lane l-1, so the value it needs from the neighbour line was
-// produced S steps earlier by lane l-1 and arrives by a register shuffle.
-// With S = 2 (FP64) the only operation on the critical path of a step is the
-// FMA with the lane's own previous column; with S = 1 (FP32, short FMA
-// latency) the neighbour-line FMA joins it.  Lines of the neighbour block and
-// of the neighbour layer come through global memory: each warp publishes its
-// progress after every chunk of C steps; a consumer reads the producers'
-// progress words early (relaxed loads that complete behind a chunk of
-// arithmetic) and spins only when they are short, with a wait bounded by the
-// global timer (a wait that runs out sets an error flag and Ctl::done; it
-// never hangs).  The factors, the right-hand side and the neighbour results
-// of chunk c+1 are loaded at the start of chunk c through per-lane running
-// pointers, so memory latency hides behind one chunk of arithmetic.  Warps
+// Wavefront.  A "line" is the ncol cells of one grid row (k,i).  A CTA owns W
+// consecutive lines of one layer (a "block").  Lane l of its compute warp
+// walks line l of the block S steps behind lane l-1, so the value it needs
+// from the neighbour line was produced S steps earlier and arrives by a
+// register shuffle; with S = 2 (FP64) only the FMA with the lane's own
+// previous column is on the critical path of a step.  The neighbour block
+// (line i0-1) and the neighbour layer are other CTAs.
+//
+// Skewed layout.  The factors and the intermediate results are stored per
+// block as G x W tiles, row g = wavefront step, column l = lane (element
+// (g,l) is the cell lane l handles at step g; slots outside the grid hold
+// zero).  A chunk of C steps of one array is then one contiguous C*W tile.
+//
+// Three warps per CTA, so that no fence ever stalls the arithmetic:
+//  * warp 1 (copy) waits for the producer CTAs' progress words and stages the
+//    chunks into a ring of NS shared-memory buffers with TMA bulk copies
+//    (cp.async.bulk), one "full" mbarrier per buffer;
+//  * warp 0 (compute) waits on the full mbarrier, computes C steps, writes the
+//    C x W result tile to shared memory and sends it out with one bulk store,
+//    then frees the buffer through its "empty" mbarrier; it tracks its bulk
+//    stores with cp.async.bulk.wait_group and reports completed chunks in
+//    shared memory;
+//  * warp 2 (publish) turns completed chunks into this CTA's progress word:
+//    proxy fence, gpu-scope fence, store.  On GB300 a gpu-scope fence costs
+//    on the order of a microsecond, which is why it lives in a warp of its own.
+// Every wait is bounded by the global timer; a wait that runs out sets an
+// error flag and Ctl::done, drains the copies in flight and returns.  CTAs
 // take a ticket in launch order and depend only on smaller tickets, so the
-// wait chain always ends.
-//
-// W < 32 leaves lanes idle on purpose: on GB300 the FP64 pipe of an SM
-// sub-partition retires about half a lane-FMA per clock, so a 32-lane FP64
-// FMA occupies it for ~67 cycles and the wavefront step time scales with the
-// number of active lanes.
+// chain of waits always ends.
 //
 // Forward sweep: y = r - Lz*y(k-1) - Ly*y(i-1) - Lx*y(j-1), in the reference's
-// order (ascending column), bit-identical to the level kernel.
+// order (ascending column), so it rounds exactly like ilu0a with FMA.
 // Backward sweep: z = dinv*y - Uz'*z(k+1) - Uy'*z(i+1) - Ux'*z(j+1) with the
 // upper factors pre-scaled by the inverse pivot (U' = dinv*U), equal in exact
-// arithmetic to the reference's (y - sum U z)*dinv with one FMA, not two
-// dependent operations, on the critical path.
+// arithmetic to the reference's (y - sum U z)*dinv with one FMA instead of two
+// dependent operations on the critical path.  The forward input and the
+// backward output are in natural order: k_dia7_skew / k_dia7_unskew permute
+// them with coalesced row accesses.
 #include "gbims_internal.cuh"
 
 namespace gb {
@@ -43,188 +51,399 @@ namespace gb {
 namespace {
 
 constexpr unsigned long long kWaitNs = 2000000000ULL;  // 2 s per wait
+constexpr int kFlagStride = 32;                        // one progress word per 128-byte line
+constexpr int kOut = 8;                                // result tiles buffered per CTA
 
 __device__ __forceinline__ unsigned long long gtimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-
 __device__ __forceinline__ int ld_relaxed(const int *p) {
   int v;
   asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-
 __device__ __forceinline__ void st_relaxed(int *p, int v) {
   asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ int ld_acquire_cta(const int *p) {
+  int v;
+  asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"((unsigned)__cvta_generic_to_shared(p)) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_cta(int *p, int v) {
+  asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for phase `parity` of an mbarrier, bounded; false if it ran out or
+// the CTA is aborting.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity,
+                                          volatile int *abort_flag) {
+  if (mbar_test(b, parity)) return true;
+  unsigned long long t0 = gtimer();
+  while (!mbar_test(b, parity)) {
+    if (*abort_flag || gtimer() - t0 > kWaitNs) return false;
+  }
+  return true;
+}
+// 1-D bulk copy global -> shared (16-byte aligned addresses, size a multiple
+// of 16), completion counted on the mbarrier.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         unsigned long long *b) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(b))
+      : "memory");
+}
 
 template <typename T>
-struct Fac {
-  const T *lz, *ly, *lx, *ux, *uy, *uz, *dinv;
+struct SweepArgs {
+  int nlay, nrow, ncol, nb, G;
+  const T *A, *B, *X, *D;  // skewed factors (forward: Lz Ly Lx -, backward: Uz' Uy' Ux' dinv)
+  const T *rsk;            // forward: right-hand side, skewed
+  T *ysk;                  // forward result, skewed (written forward, read backward)
+  T *zsk;                  // backward result, skewed (written and read backward)
+  int *flags, *err;
+  Ctl *ctl;
 };
 
-template <typename T, int C>
-struct Chunk {
-  T r[C], a[C], b[C], x[C], zn[C], yn[C];
+template <typename T, int W, int C>
+struct Stage {
+  T a[C * W], b[C * W], x[C * W], d[C * W], r[C * W], zn[C * W], yn[C * W];
 };
 
-// DIR = +1: forward sweep (lines ascending, columns left to right).
-// DIR = -1: backward sweep (lines descending, columns right to left).
-template <typename T, int W, int S, int C, int DIR>
-__global__ void __launch_bounds__(32) k_dia7_sweep(int nlay, int nrow, int ncol, Fac<T> f,
-                                                    const T *__restrict__ rin, T *out,
-                                                    int *flags, int *err, Ctl *ctl) {
-  if (ctl && ctl->done) return;
-  const int lane = threadIdx.x;
-  int id = 0;
-  if (lane == 0) id = atomicAdd(&flags[0], 1);
-  id = __shfl_sync(0xffffffffu, id, 0);
-  const int nb = (nrow + W - 1) / W;
+// DIR = +1 forward, -1 backward.
+template <typename T, int W, int S, int C, int NS, int DIR>
+__global__ void __launch_bounds__(96) k_dia7_sweep(SweepArgs<T> p) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Stage<T, W, C> *stg = reinterpret_cast<Stage<T, W, C> *>(smem_raw);
+  T *outring = reinterpret_cast<T *>(smem_raw + NS * sizeof(Stage<T, W, C>));
+  unsigned long long *full = reinterpret_cast<unsigned long long *>(
+      smem_raw + NS * sizeof(Stage<T, W, C>) + kOut * C * W * sizeof(T));
+  unsigned long long *empty = full + NS;
+  __shared__ int s_id, s_ready, s_freed, s_abort;
+  if (p.ctl && p.ctl->done) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    s_id = atomicAdd(&p.flags[0], 1);
+    s_ready = 0;
+    s_freed = 0;
+    s_abort = 0;
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int id = s_id;
+  const int nlay = p.nlay, nrow = p.nrow, nb = p.nb, G = p.G;
   const int k = (DIR > 0) ? id % nlay : nlay - 1 - (id % nlay);
   const int b = (DIR > 0) ? id / nlay : nb - 1 - id / nlay;
-  const int i = (DIR > 0) ? (b * W + lane) : (b * W + (W - 1 - lane));
-  const bool line_ok = lane < W && i >= 0 && i < nrow;
-  const long long nrc = (long long)nrow * ncol;
-  const int nch = (ncol + S * (W - 1) + C - 1) / C;
-  const int total = nch * C;
-  int *prog = flags + 1;
+  const int nch = G / C;
   const bool has_blk = (DIR > 0) ? (b > 0) : (b < nb - 1);
   const bool has_lay = (DIR > 0) ? (k > 0) : (k < nlay - 1);
-  const int *pb = has_blk ? prog + (id - nlay) : nullptr;
-  const int *pu = has_lay ? prog + (id - 1) : nullptr;
-  // neighbour line exists for this lane (lane 0's lives in the other block)
-  const bool has_y = line_ok && ((DIR > 0) ? (i > 0) : (i + 1 < nrow));
-  const bool y_from_mem = has_y && lane == 0;
-  const bool z_on = line_ok && has_lay;
-  // element of step g: e(g) = e0 + DIR*g; walk index jj(g) = g - S*lane
-  const long long base = k * nrc + (long long)(line_ok ? i : 0) * ncol;
-  const long long e0 = (DIR > 0) ? base - (long long)S * lane : base + ncol - 1 + (long long)S * lane;
-  const long long zoff = -(long long)DIR * nrc;
-  const long long yoff = -(long long)DIR * ncol;
-  const T *A = (DIR > 0) ? f.lz : f.uz;
-  const T *B = (DIR > 0) ? f.ly : f.uy;
-  const T *X = (DIR > 0) ? f.lx : f.ux;
-  int seen_b = 0, seen_u = 0;
+  int *prog = p.flags + kFlagStride;
+  auto tile = [&](int kk, int bb) -> long long { return ((long long)kk * nb + bb) * G * W; };
+  volatile int *v_abort = &s_abort;
 
-  // make sure the producers have published what chunk c needs
-  auto ensure = [&](int c) -> bool {
-    int ok = 1;
+  if (warp == 2) {
+    // ---------------- store + publish warp ----------------
+    // Takes every result tile the compute warp has finished, sends each out
+    // with a bulk store, frees its slot once the store has read it, and then
+    // publishes the batch: stores complete, proxy fence, gpu-scope fence,
+    // progress word.  Batching spreads the cost of the fence over all the
+    // chunks that finished meanwhile.
     if (lane == 0) {
-      const int nb_need = min((c + 1) * C + S * (W - 1), total);
-      const int nu_need = min((c + 1) * C, total);
-      if (pb && seen_b < nb_need) {
-        unsigned long long t0 = gtimer();
-        while ((seen_b = ld_relaxed(pb)) < nb_need)
-          if (gtimer() - t0 > kWaitNs) { ok = 0; break; }
-      }
-      if (ok && pu && seen_u < nu_need) {
-        unsigned long long t0 = gtimer();
-        while ((seen_u = ld_relaxed(pu)) < nu_need)
-          if (gtimer() - t0 > kWaitNs) { ok = 0; break; }
-      }
-      if (!ok) {
-        atomicExch(err, 1);
-        if (ctl) ctl->done = 1;
-      }
-      // early reads for the next check; they complete behind a chunk of work
-      if (ok && pb) seen_b = ld_relaxed(pb);
-      if (ok && pu) seen_u = ld_relaxed(pu);
-    }
-    __syncwarp();
-    return __shfl_sync(0xffffffffu, ok, 0) != 0;
-  };
-
-  auto load = [&](int c, Chunk<T, C> &q) {
-    const long long ec = e0 + (long long)DIR * c * C;
-    const int jc = c * C - S * lane;
-#pragma unroll
-    for (int t = 0; t < C; ++t) {
-      const long long e = ec + DIR * t;
-      const bool v = line_ok && (unsigned)(jc + t) < (unsigned)ncol;
-      T r = T(0), a = T(0), bb = T(0), x = T(0), zn = T(0), yn = T(0);
-      if (v) {
-        if (DIR > 0) r = __ldg(rin + e);
-        else r = __ldg(f.dinv + e) * out[e];  // dinv * y: own cell, still the forward value
-        bb = __ldg(B + e);
-        x = __ldg(X + e);
-        if (z_on) {
-          a = __ldg(A + e);
-          zn = __ldcg(out + e + zoff);
+      int stored = 0;
+      unsigned long long t0 = gtimer();
+      unsigned ns = 32;
+      T *dstbase = ((DIR > 0) ? p.ysk : p.zsk) + tile(k, b);
+      while (stored < nch && !*v_abort) {
+        const int r = ld_acquire_cta(&s_ready);
+        if (r > stored) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          for (int c = stored; c < r; ++c) {
+            const T *src = outring + (c % kOut) * (C * W);
+            asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(
+                             dstbase + (long long)c * C * W),
+                         "r"(smem_u32(src)), "r"((unsigned)(C * W * sizeof(T)))
+                         : "memory");
+          }
+          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          st_release_cta(&s_freed, r);  // result slots may be reused
+          asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+          asm volatile("fence.proxy.async.global;" ::: "memory");
+          __threadfence();
+          st_relaxed(prog + (size_t)id * kFlagStride, r * C);
+          stored = r;
+          t0 = gtimer();
+          ns = 32;
+        } else {
+          __nanosleep(ns);
+          if (ns < 256) ns <<= 1;
+          if (gtimer() - t0 > kWaitNs) {
+            *v_abort = 1;
+            atomicExch(p.err, 1);
+            if (p.ctl) p.ctl->done = 1;
+          }
         }
-        if (y_from_mem) yn = __ldcg(out + e + yoff);
       }
-      q.r[t] = r; q.a[t] = a; q.b[t] = bb; q.x[t] = x; q.zn[t] = zn; q.yn[t] = yn;
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     }
-  };
+    return;
+  }
 
-  Chunk<T, C> cur, nxt;
-  if (!ensure(0)) return;
-  load(0, cur);
-  T h1 = T(0), h2 = T(0);  // this lane's results of the last two steps
-  for (int c = 0; c < nch; ++c) {
-    const bool more = (c + 1 < nch);
-    if (more) {
-      if (!ensure(c + 1)) return;
-      load(c + 1, nxt);
+  if (warp == 1) {
+    // ---------------- copy warp ----------------
+    const int *pb = has_blk ? prog + (size_t)(id - nlay) * kFlagStride : nullptr;
+    const int *pu = has_lay ? prog + (size_t)(id - 1) * kFlagStride : nullptr;
+    int seen_b = 0, seen_u = 0, issued = 0;
+    bool ok = true;
+    const unsigned tileb = C * W * sizeof(T);
+    for (int c = 0; c < nch; ++c) {
+      const int s = c % NS;
+      if (lane == 0) {
+        // the buffer's previous chunk (c - NS) has been consumed
+        if (c >= NS && !mbar_wait(&empty[s], ((c / NS) - 1) & 1, v_abort)) ok = false;
+        // producers: neighbour block (its last lane) and neighbour layer
+        const int nb_need = min((c + 1) * C + S * (W - 1), G);
+        const int nu_need = min((c + 1) * C, G);
+        if (ok && ((pb && seen_b < nb_need) || (pu && seen_u < nu_need))) {
+          unsigned long long t0 = gtimer();
+          while ((pb && seen_b < nb_need) || (pu && seen_u < nu_need)) {
+            if (pb && seen_b < nb_need) seen_b = ld_relaxed(pb);
+            if (pu && seen_u < nu_need) seen_u = ld_relaxed(pu);
+            if (*v_abort || gtimer() - t0 > kWaitNs) { ok = false; break; }
+          }
+          // the data behind the progress just observed is read by the async proxy
+          asm volatile("fence.proxy.async.global;" ::: "memory");
+        }
+      }
+      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+      if (!ok) break;
+      if (lane == 0) {
+        Stage<T, W, C> &st = stg[s];
+        const int g0 = c * C;
+        const int yrow0 = g0 + S * (W - 1);
+        const int yrows = has_blk ? max(0, min(C, G - yrow0)) : 0;
+        int plo = 0, prows = 0, pskip = 0;
+        if (DIR < 0) {  // own forward result, rows P descending
+          const int phi = p.ncol - 1 + S * (W - 1) - g0;
+          const int pl = phi - (C - 1);
+          const int lo = max(pl, 0), hi = min(phi, G - 1);
+          plo = lo;
+          prows = max(0, hi - lo + 1);
+          pskip = lo - pl;
+        }
+        unsigned bytes = 3 * tileb;
+        bytes += (DIR > 0) ? tileb : tileb + prows * W * (unsigned)sizeof(T);
+        if (has_lay) bytes += tileb;
+        bytes += yrows * W * (unsigned)sizeof(T);
+        mbar_expect_tx(&full[s], bytes);
+        const long long tb = tile(k, b) + (long long)g0 * W;
+        bulk_g2s(st.a, p.A + tb, tileb, &full[s]);
+        bulk_g2s(st.b, p.B + tb, tileb, &full[s]);
+        bulk_g2s(st.x, p.X + tb, tileb, &full[s]);
+        if (DIR > 0) {
+          bulk_g2s(st.r, p.rsk + tb, tileb, &full[s]);
+        } else {
+          bulk_g2s(st.d, p.D + tb, tileb, &full[s]);
+          if (prows > 0)
+            bulk_g2s(st.r + pskip * W, p.ysk + tile(k, b) + (long long)plo * W,
+                     prows * W * sizeof(T), &full[s]);
+        }
+        const T *nbr = (DIR > 0) ? p.ysk : p.zsk;
+        if (has_lay) bulk_g2s(st.zn, nbr + tile(k - DIR, b) + (long long)g0 * W, tileb, &full[s]);
+        if (yrows > 0)
+          bulk_g2s(st.yn, nbr + tile(k, b - DIR) + (long long)yrow0 * W, yrows * W * sizeof(T),
+                   &full[s]);
+      }
+      issued = c + 1;
     }
-    const long long ec = e0 + (long long)DIR * c * C;
-    const int jc = c * C - S * lane;
+    if (!ok && lane == 0) {
+      atomicExch(p.err, 1);
+      if (p.ctl) p.ctl->done = 1;
+      *v_abort = 1;
+      // drain the copies still in flight before the CTA's shared memory goes
+      for (int c = max(0, issued - NS); c < issued; ++c) {
+        unsigned long long t0 = gtimer();
+        while (!mbar_test(&full[c % NS], (c / NS) & 1))
+          if (gtimer() - t0 > kWaitNs) break;
+      }
+    }
+    return;
+  }
+
+  // ---------------- compute warp ----------------
+  const int i = (DIR > 0) ? (b * W + lane) : (b * W + (W - 1 - lane));
+  const bool line_ok = lane < W && i >= 0 && i < nrow;
+  const bool has_y = line_ok && ((DIR > 0) ? (i > 0) : (i + 1 < nrow));
+  const int ncol = p.ncol;
+  const int l = lane < W ? lane : 0;
+  T h1 = T(0), h2 = T(0);
+  for (int c = 0; c < nch; ++c) {
+    const int s = c % NS;
+    const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort);
+    if (!__all_sync(0xffffffffu, got)) {
+      if (lane == 0) {
+        *v_abort = 1;
+        asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+      }
+      return;
+    }
+    const Stage<T, W, C> &st = stg[s];
+    T *ot = outring + (c % kOut) * (C * W);
+    if (c >= kOut) {
+      // the slot's previous tile (chunk c - kOut) must have left for global memory
+      bool freed = true;
+      if (lane == 0 && ld_acquire_cta(&s_freed) < c - kOut + 1) {
+        unsigned long long t0 = gtimer();
+        while (ld_acquire_cta(&s_freed) < c - kOut + 1)
+          if (*v_abort || gtimer() - t0 > kWaitNs) { freed = false; break; }
+      }
+      if (!__shfl_sync(0xffffffffu, freed ? 1 : 0, 0)) {
+        if (lane == 0) *v_abort = 1;
+        return;
+      }
+    }
+    const int g0 = c * C;
+    const int jc = g0 - S * lane;
 #pragma unroll
     for (int t = 0; t < C; ++t) {
-      // neighbour line, same column: lane-1's result S steps ago
       T yv = __shfl_up_sync(0xffffffffu, (S == 1) ? h1 : h2, 1);
-      if (lane == 0) yv = cur.yn[t];
+      if (lane == 0) yv = st.yn[t * W + (W - 1)];
       const int jj = jc + t;
-      T tv = cur.r[t];
-      tv = fma(-cur.a[t], cur.zn[t], tv);
-      if (has_y) tv = fma(-cur.b[t], yv, tv);
-      if (jj > 0) tv = fma(-cur.x[t], h1, tv);
       const bool v = line_ok && (unsigned)jj < (unsigned)ncol;
-      if (v) out[ec + DIR * t] = tv;
-      else tv = T(0);
+      T tv;
+      if (DIR > 0) tv = st.r[t * W + l];
+      else tv = st.d[t * W + l] * st.r[(C - 1 - t) * W + (W - 1 - l)];
+      if (has_lay) tv = fma(-st.a[t * W + l], st.zn[t * W + l], tv);
+      if (has_y) tv = fma(-st.b[t * W + l], yv, tv);
+      if (jj > 0) tv = fma(-st.x[t * W + l], h1, tv);
+      if (!v) tv = T(0);
+      if (lane < W) ot[t * W + lane] = tv;
       h2 = h1;
       h1 = tv;
     }
+    // hand the result tile to the store warp and the input buffer back to
+    // the copy warp
     __syncwarp();
     if (lane == 0) {
-      __threadfence();
-      st_relaxed(prog + id, (c + 1) * C);
+      st_release_cta(&s_ready, c + 1);
+      mbar_arrive(&empty[s]);
     }
-    if (more) cur = nxt;
   }
 }
 
-// APC/JAPC -> seven arrays; U pre-scaled by the inverse pivot.
+// Natural order -> skewed tiles (forward input) and back (backward output).
+// A 32 x 8 thread block covers 32 columns of 8 lines: the natural-order side
+// is whole rows, and the skewed side falls in a few rows of one tile.
+template <typename T, int W, int S, int DIR>
+__global__ void k_dia7_permute(int nrow, int ncol, int nb, int G, const T *__restrict__ src,
+                               T *__restrict__ dst, const Ctl *__restrict__ ctl) {
+  if (ctl && ctl->done) return;
+  const int j = blockIdx.x * 32 + threadIdx.x;
+  const int i = blockIdx.y * 8 + threadIdx.y;
+  const int k = blockIdx.z;
+  if (j >= ncol || i >= nrow) return;
+  const int b = i / W;
+  const int l = (DIR > 0) ? (i - b * W) : (W - 1 - (i - b * W));
+  const int g = ((DIR > 0) ? j : (ncol - 1 - j)) + S * l;
+  const long long sk = (((long long)k * nb + b) * G + g) * W + l;
+  const long long nat = ((long long)k * nrow + i) * ncol + j;
+  if (DIR > 0) dst[sk] = src[nat];  // skew (forward input)
+  else dst[nat] = src[sk];          // unskew (backward output)
+}
+
+// APC/JAPC -> skewed tiles.  Forward tiles hold Lz, Ly, Lx of the cell that
+// lane l visits at step g; backward tiles hold dinv*Uz, dinv*Uy, dinv*Ux and
+// dinv.  Slots outside the grid are zero.
 template <typename T>
-__global__ void k_dia7_extract(int nlay, int nrow, int ncol, const int *__restrict__ iapc,
-                               const int *__restrict__ japc, const double *__restrict__ apc,
-                               T *lz, T *ly, T *lx, T *ux, T *uy, T *uz, T *dinv) {
-  long long nn = (long long)nlay * nrow * ncol;
-  long long nrc = (long long)nrow * ncol;
-  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nn;
-       n += (long long)gridDim.x * blockDim.x) {
-    int k = (int)(n / nrc);
-    int rem = (int)(n - k * nrc);
-    int i = rem / ncol, j = rem - i * ncol;
-    double vz = 0, vy = 0, vx = 0, wx = 0, wy = 0, wz = 0;
-    for (int p = iapc[n]; p < iapc[n + 1]; ++p) {
-      long long c = japc[p];
-      double a = apc[p];
-      if (k > 0 && c == n - nrc) vz = a;
-      else if (i > 0 && c == n - ncol) vy = a;
-      else if (j > 0 && c == n - 1) vx = a;
-      else if (j < ncol - 1 && c == n + 1) wx = a;
-      else if (i < nrow - 1 && c == n + ncol) wy = a;
-      else if (k < nlay - 1 && c == n + nrc) wz = a;
+__global__ void k_dia7_extract(int nlay, int nrow, int ncol, int nb, int G, int W, int S, int dir,
+                               const int *__restrict__ iapc, const int *__restrict__ japc,
+                               const double *__restrict__ apc, T *A, T *B, T *X, T *D) {
+  const long long nslot = (long long)nlay * nb * G * W;
+  const long long nrc = (long long)nrow * ncol;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nslot;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int l = (int)(q % W);
+    const long long r1 = q / W;
+    const int g = (int)(r1 % G);
+    const long long kb = r1 / G;
+    const int b = (int)(kb % nb), k = (int)(kb / nb);
+    const int jj = g - S * l;
+    const int i = (dir > 0) ? b * W + l : b * W + (W - 1 - l);
+    double va = 0, vb = 0, vx = 0, vd = 0;
+    if (i < nrow && jj >= 0 && jj < ncol) {
+      const int j = (dir > 0) ? jj : ncol - 1 - jj;
+      const long long n = k * nrc + (long long)i * ncol + j;
+      const double d = apc[n];
+      for (int pp = iapc[n]; pp < iapc[n + 1]; ++pp) {
+        const long long c = japc[pp];
+        const double a = apc[pp];
+        if (dir > 0) {
+          if (k > 0 && c == n - nrc) va = a;
+          else if (i > 0 && c == n - ncol) vb = a;
+          else if (j > 0 && c == n - 1) vx = a;
+        } else {
+          if (k < nlay - 1 && c == n + nrc) va = d * a;
+          else if (i < nrow - 1 && c == n + ncol) vb = d * a;
+          else if (j < ncol - 1 && c == n + 1) vx = d * a;
+        }
+      }
+      vd = d;
     }
-    double d = apc[n];
-    lz[n] = (T)vz; ly[n] = (T)vy; lx[n] = (T)vx;
-    ux[n] = (T)(d * wx); uy[n] = (T)(d * wy); uz[n] = (T)(d * wz);
-    dinv[n] = (T)d;
+    A[q] = (T)va;
+    B[q] = (T)vb;
+    X[q] = (T)vx;
+    if (D) D[q] = (T)vd;
   }
 }
+
+// Wavefront shape per precision: lines per block W, lane skew S, chunk C,
+// buffers NS.
+template <typename T>
+struct Shape;
+template <>
+struct Shape<double> { static constexpr int W = 16, S = 2, C = 8, NS = 5; };
+template <>
+struct Shape<float> { static constexpr int W = 32, S = 1, C = 8, NS = 5; };
+
+template <typename T>
+constexpr size_t stage_bytes() {
+  using P = Shape<T>;
+  return P::NS * sizeof(Stage<T, P::W, P::C>) + kOut * P::C * P::W * sizeof(T) +
+         2 * P::NS * sizeof(unsigned long long);
+}
+static_assert(stage_bytes<double>() < 48 * 1024, "FP64 stage ring too large");
+static_assert(stage_bytes<float>() < 48 * 1024, "FP32 stage ring too large");
 
 }  // namespace
 
@@ -252,53 +471,74 @@ bool dia7_matches(int nlay, int nrow, int ncol, int n, const std::vector<int> &i
   return true;
 }
 
-void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_japc,
-                         const double *d_apc, bool mixed, cudaStream_t st) {
-  int grid = std::min((n + 255) / 256, 8 * kNumSM);
-  if (!mixed)
-    k_dia7_extract<double><<<grid, 256, 0, st>>>(D.nlay, D.nrow, D.ncol, d_iapc, d_japc, d_apc,
-                                                 D.d_lz, D.d_ly, D.d_lx, D.d_ux, D.d_uy, D.d_uz,
-                                                 D.d_dinv);
-  else
-    k_dia7_extract<float><<<grid, 256, 0, st>>>(D.nlay, D.nrow, D.ncol, d_iapc, d_japc, d_apc,
-                                                D.f_lz, D.f_ly, D.f_lx, D.f_ux, D.f_uy, D.f_uz,
-                                                D.f_dinv);
+// Geometry of the skewed layout of one precision.
+void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, long long *slots) {
+  int W = fp32 ? Shape<float>::W : Shape<double>::W;
+  int S = fp32 ? Shape<float>::S : Shape<double>::S;
+  int C = fp32 ? Shape<float>::C : Shape<double>::C;
+  *nb = (nrow + W - 1) / W;
+  *G = ((ncol + S * (W - 1) + C - 1) / C) * C;
+  *slots = (long long)nlay * (*nb) * (*G) * W;
 }
 
-// Wavefront shape per precision: lines per warp W, lane skew S, chunk C.
 template <typename T>
-struct Shape;
-template <>
-struct Shape<double> { static constexpr int W = 16, S = 2, C = 8; };
-template <>
-struct Shape<float> { static constexpr int W = 32, S = 1, C = 8; };
+static void extract_t(const Dia7 &D, const int *d_iapc, const int *d_japc, const double *d_apc,
+                      T *const *arr, cudaStream_t st) {
+  using P = Shape<T>;
+  long long nslot = (long long)D.nlay * D.nb * D.G * P::W;
+  int grid = (int)std::min<long long>((nslot + 255) / 256, 8LL * kNumSM);
+  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.nb, D.G, P::W, P::S, 1, d_iapc,
+                                          d_japc, d_apc, arr[0], arr[1], arr[2], nullptr);
+  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.nb, D.G, P::W, P::S, -1, d_iapc,
+                                          d_japc, d_apc, arr[3], arr[4], arr[5], arr[6]);
+}
+
+void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_japc,
+                         const double *d_apc, bool mixed, cudaStream_t st) {
+  (void)n;
+  if (!mixed) {
+    double *arr[7] = {D.d_lz, D.d_ly, D.d_lx, D.d_uz, D.d_uy, D.d_ux, D.d_dinv};
+    extract_t<double>(D, d_iapc, d_japc, d_apc, arr, st);
+    cudaMemsetAsync(D.d_rsk, 0, sizeof(double) * D.slots, st);  // padding slots stay zero
+  } else {
+    float *arr[7] = {D.f_lz, D.f_ly, D.f_lx, D.f_uz, D.f_uy, D.f_ux, D.f_dinv};
+    extract_t<float>(D, d_iapc, d_japc, d_apc, arr, st);
+    cudaMemsetAsync(D.f_rsk, 0, sizeof(float) * D.slots, st);
+  }
+}
 
 template <typename T>
-static void apply_t(const Dia7 &D, Fac<T> f, const T *r, T *z, const Ctl *ctl, cudaStream_t st) {
+static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, T *ysk, T *zsk, const T *r, T *z,
+                    const Ctl *ctl, cudaStream_t st) {
   using P = Shape<T>;
-  int nb = (D.nrow + P::W - 1) / P::W;
-  int nct = nb * D.nlay;
-  cudaMemsetAsync(D.d_flags, 0, sizeof(int) * (nct + 1), st);
-  k_dia7_sweep<T, P::W, P::S, P::C, 1><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, r, z,
-                                                           D.d_flags, D.d_err,
-                                                           const_cast<Ctl *>(ctl));
-  cudaMemsetAsync(D.d_flags, 0, sizeof(int) * (nct + 1), st);
-  k_dia7_sweep<T, P::W, P::S, P::C, -1><<<nct, 32, 0, st>>>(D.nlay, D.nrow, D.ncol, f, nullptr, z,
-                                                            D.d_flags, D.d_err,
-                                                            const_cast<Ctl *>(ctl));
+  const int nct = D.nb * D.nlay;
+  const size_t fbytes = sizeof(int) * (size_t)(nct + 1) * kFlagStride;
+  constexpr size_t sm = stage_bytes<T>();
+  const dim3 pb(32, 8), pg((D.ncol + 31) / 32, (D.nrow + 7) / 8, D.nlay);
+  SweepArgs<T> a;
+  a.nlay = D.nlay; a.nrow = D.nrow; a.ncol = D.ncol; a.nb = D.nb; a.G = D.G;
+  a.rsk = rsk; a.ysk = ysk; a.zsk = zsk;
+  a.flags = D.d_flags; a.err = D.d_err; a.ctl = const_cast<Ctl *>(ctl);
+  a.A = arr[0]; a.B = arr[1]; a.X = arr[2]; a.D = nullptr;
+  k_dia7_permute<T, P::W, P::S, 1><<<pg, pb, 0, st>>>(D.nrow, D.ncol, D.nb, D.G, r, rsk, ctl);
+  cudaMemsetAsync(D.d_flags, 0, fbytes, st);
+  k_dia7_sweep<T, P::W, P::S, P::C, P::NS, 1><<<nct, 96, sm, st>>>(a);
+  a.A = arr[3]; a.B = arr[4]; a.X = arr[5]; a.D = arr[6];
+  cudaMemsetAsync(D.d_flags, 0, fbytes, st);
+  k_dia7_sweep<T, P::W, P::S, P::C, P::NS, -1><<<nct, 96, sm, st>>>(a);
+  k_dia7_permute<T, P::W, P::S, -1><<<pg, pb, 0, st>>>(D.nrow, D.ncol, D.nb, D.G, zsk, z, ctl);
 }
 
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
                          cudaStream_t st) {
-  Fac<double> f{D.d_lz, D.d_ly, D.d_lx, D.d_ux, D.d_uy, D.d_uz, D.d_dinv};
-  // the forward result is written into z and swept backwards in place
-  apply_t<double>(D, f, r, z, ctl, st);
+  const double *arr[7] = {D.d_lz, D.d_ly, D.d_lx, D.d_uz, D.d_uy, D.d_ux, D.d_dinv};
+  apply_t<double>(D, arr, D.d_rsk, D.d_ysk, D.d_zsk, r, z, ctl, st);
 }
 
 void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
                          cudaStream_t st) {
-  Fac<float> f{D.f_lz, D.f_ly, D.f_lx, D.f_ux, D.f_uy, D.f_uz, D.f_dinv};
-  apply_t<float>(D, f, r, z, ctl, st);
+  const float *arr[7] = {D.f_lz, D.f_ly, D.f_lx, D.f_uz, D.f_uy, D.f_ux, D.f_dinv};
+  apply_t<float>(D, arr, D.f_rsk, D.f_ysk, D.f_zsk, r, z, ctl, st);
 }
 
 }  // namespace gb
