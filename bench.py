@@ -4,7 +4,7 @@
 Workload (1000x1000x10 DIS, 7-point, 10,000,000 cells, 67,960,000 nonzeros):
 per-layer lognormal Kh (ln K ~ N(0, 1.5^2), 20-cell correlation), Kv = 0.1 Kh,
 CHD 20 m / 0 m on the west / east faces, 5,000 wells U(-500, -50) m3/d,
-seeded synthetic data.  PCG + ILU0, INNER_DVCLOSE 1e-6 m, INNER_RCLOSE 1e-2,
+seeded synthetic data.  PCG + ILU0, INNER_DVCLOSE 1e-6 m, INNER_RCLOSE 1e-4,
 OUTER_DVCLOSE 1e-6 m.
 
 A step is one steady-state time step from the initial heads to closure: the
@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernels", action="store_true",
+                    help="per-kernel device times on direct launches (no solve)")
     return ap.parse_args()
 
 
@@ -56,6 +58,19 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     lrank = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, lrank
+
+
+def max_over_ranks(v: float, ws: int) -> float:
+    """The slowest rank's time: every rank times its own replica of the step;
+    the job's time is the maximum (NCCL on GPUs, gloo on CPU)."""
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def workload_config(a, m):
@@ -251,11 +266,7 @@ def gb_arm(a):
             torch.distributed.barrier()
 
     def maxr(v):
-        if ws > 1:
-            t = torch.tensor([v], device="cuda", dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return v
+        return max_over_ranks(v, ws)
 
     def run_form(precision, clocks=False):
         sol = GwfSolution(m, ImsLinearSettings(precision=precision, structure=shape, **C2_IMS), nl)
@@ -297,6 +308,8 @@ def gb_arm(a):
     spmv_gbs = kt.spmv_bytes / (kt.spmv_ms * 1e-3) / 1e9
     pre_gbs = kt.precond_bytes / (kt.precond_ms * 1e-3) / 1e9
     traffic = ncu_traffic()
+    pre_name = ("k_dia7_sweep<double> forward + backward (structured wavefront ILU0, "
+                "with the skew/unskew permutes)")
     mixed = None
     if not a.no_mixed:
         solm, msm, stm, lm, _, hm = run_form(_lib.GBIMS_MIXED)
@@ -367,11 +380,18 @@ def gb_arm(a):
         "fill_ms_per_step": float(np.mean([s["fill_ms"] for s in st64])),
         "mixed": mixed, "mixed_s": mixed["value"] if mixed else None, "warmstart_s": None,
         "spmv_gbs": spmv_gbs,
-        "roofline": {"kernel": "k_sell_spmv<double> (FP64 SpMV, SELL-32)", "bound": "hbm",
-                     "achieved": spmv_gbs, "peak": peak, "unit": "GB/s", "frac": spmv_gbs / peak,
-                     "peak_kind": f"{peak_kind} copy bandwidth",
-                     "algorithmic_bytes_per_launch": kt.spmv_bytes, "launch_ms": kt.spmv_ms,
-                     "traffic": traffic.get("spmv_fp64_bytes_per_launch")},
+        # dominant kernel of an inner iteration: the ILU0 application
+        "roofline": {"kernel": pre_name, "bound": "hbm", "achieved": pre_gbs, "peak": peak,
+                     "unit": "GB/s", "frac": pre_gbs / peak, "peak_kind": f"{peak_kind} copy bandwidth",
+                     "algorithmic_bytes_per_launch": kt.precond_bytes, "launch_ms": kt.precond_ms,
+                     "traffic": traffic.get("precond_fp64_bytes_per_launch"),
+                     "limiter": "wavefront dependency chain: per-step FP64 latency/issue and "
+                                "inter-CTA hand-off, not bandwidth"},
+        "roofline_spmv": {"kernel": "k_sell_spmv<double> (FP64 SpMV, SELL-32)", "bound": "hbm",
+                          "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
+                          "frac": spmv_gbs / peak, "peak_kind": f"{peak_kind} copy bandwidth",
+                          "algorithmic_bytes_per_launch": kt.spmv_bytes, "launch_ms": kt.spmv_ms,
+                          "traffic": traffic.get("spmv_fp64_bytes_per_launch")},
         "kernels": {"spmv_ms": kt.spmv_ms, "spmv_gbs": spmv_gbs, "precond_ms": kt.precond_ms,
                     "precond_gbs": pre_gbs, "dot_ms": kt.dot_ms, "update_ms": kt.update_ms},
         "e2e": e2e, "gpu_launches": int(launches64), "clocks": clocks,
@@ -384,9 +404,59 @@ def gb_arm(a):
         torch.distributed.destroy_process_group()
 
 
+def kernels_arm(a):
+    """Per-kernel device times of one inner iteration's kernels (SpMV,
+    ILU0 application, dot, update) on direct stream launches, for both
+    precisions: one system assembled on the GPU, factored, then each kernel
+    launched `--steps` times after one warm-up (gbims_time_kernels)."""
+    import ctypes as C
+
+    import torch
+    from modflow6_gb300 import _lib, build
+    build.build()
+    from modflow6_gb300.dis import make_config
+    from modflow6_gb300.ims import ImsLinear, ImsLinearSettings
+    from modflow6_gb300.solution import GwfSolution, Nonlinear, sln_ls_fixups
+    from modflow6_gb300.workloads import C2_IMS
+
+    torch.cuda.set_device(0)
+    lib = _lib.load()
+    m = make_config("c2", seed=a.seed, scale=a.scale)
+    shape = (m.nlay, m.nrow, m.ncol)
+    con = m.connections()
+    sol = GwfSolution(m, ImsLinearSettings(structure=shape, **C2_IMS), Nonlinear())
+    x0 = m.strt.copy()
+    x0[m.chd_node] = m.chd_head
+    sol.heads = x0
+    amat, rhs = sol.formulate(0.0)
+    sol.close()
+    amat, rhs = sln_ls_fixups(con["ia"], con["ja"], m.ibound, amat, rhs, x0, isymmetric=True)
+    out = {"workload": workload_config(a, m)["workload"], "reps": a.steps}
+    # the full-grid (index-free SpMV, wavefront sweeps) forms, then the
+    # general-pattern form (SELL-32 SpMV, level-scheduled sweeps) in FP64
+    for name, prec, st in (("fp64", _lib.GBIMS_FP64, shape), ("mixed", _lib.GBIMS_MIXED, shape),
+                           ("fp64_general", _lib.GBIMS_FP64, None)):
+        ims = ImsLinear(ImsLinearSettings(precision=prec, structure=st, **C2_IMS))
+        ims.imslinear_allocate(m.nodes, con["ia"], con["ja"])
+        rc = lib.gbims_factor(ims._h, _lib.dptr(amat), None)
+        assert rc >= 0, lib.gbims_last_error(ims._h)
+        kt = _lib.GbimsKernelTimes()
+        rc = lib.gbims_time_kernels(ims._h, max(1, a.steps), C.byref(kt))
+        assert rc == 0, lib.gbims_last_error(ims._h)
+        out[name] = {"spmv_ms": kt.spmv_ms, "precond_ms": kt.precond_ms, "dot_ms": kt.dot_ms,
+                     "update_ms": kt.update_ms,
+                     "spmv_gbs": kt.spmv_bytes / (kt.spmv_ms * 1e-3) / 1e9,
+                     "precond_gbs": kt.precond_bytes / (kt.precond_ms * 1e-3) / 1e9,
+                     "spmv_bytes": kt.spmv_bytes, "precond_bytes": kt.precond_bytes}
+        ims.imslinear_da()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     a = parse()
-    if a.impl == "reference":
+    if a.kernels:
+        kernels_arm(a)
+    elif a.impl == "reference":
         reference_arm(a)
     else:
         gb_arm(a)
