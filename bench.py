@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--kernels", action="store_true",
                     help="per-kernel device times on direct launches (no solve)")
     return ap.parse_args()
@@ -369,6 +370,7 @@ def gb_arm(a):
                "d2h_bytes_per_step": int(no * x0.nbytes),
                "path": "gbims_apply (C ABI, pinned host amat/rhs/x) per outer iteration"}
         ims.imslinear_da()
+    ens = None if a.no_ensemble else ensemble_form(a, lib, barrier, maxr)
     last = st64[-1]
     line = {
         "metric": METRIC, "value": ms64 / 1e3, "unit": "s", "n_gpus": ws, "steps": a.steps,
@@ -387,14 +389,15 @@ def gb_arm(a):
                      "traffic": traffic.get("precond_fp64_bytes_per_launch"),
                      "limiter": "wavefront dependency chain: per-step FP64 latency/issue and "
                                 "inter-CTA hand-off, not bandwidth"},
-        "roofline_spmv": {"kernel": "k_sell_spmv<double> (FP64 SpMV, SELL-32)", "bound": "hbm",
+        "roofline_spmv": {"kernel": "k_dia7_spmv<double> (FP64 SpMV, index-free 7-point)",
+                          "bound": "hbm",
                           "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
                           "frac": spmv_gbs / peak, "peak_kind": f"{peak_kind} copy bandwidth",
                           "algorithmic_bytes_per_launch": kt.spmv_bytes, "launch_ms": kt.spmv_ms,
                           "traffic": traffic.get("spmv_fp64_bytes_per_launch")},
         "kernels": {"spmv_ms": kt.spmv_ms, "spmv_gbs": spmv_gbs, "precond_ms": kt.precond_ms,
                     "precond_gbs": pre_gbs, "dot_ms": kt.dot_ms, "update_ms": kt.update_ms},
-        "e2e": e2e, "gpu_launches": int(launches64), "clocks": clocks,
+        "e2e": e2e, "gpu_launches": int(launches64), "clocks": clocks, "ensemble": ens,
     }
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_sample(m, last["inner_total"], last["outer"])
@@ -402,6 +405,55 @@ def gb_arm(a):
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def ensemble_form(a, lib, barrier, maxr) -> dict:
+    """The 256-member batched ensemble (C4): every member assembled on the
+    GPU (gbnpf_fill + sln_ls fix-ups), concatenated, and solved to its own
+    closure by one batched PCG + ILU0 (gbims_batch_apply_device, the
+    wavefront preconditioner over all members).  Inputs stay in HBM; each
+    timed step restores x and solves all members."""
+    import torch
+    from modflow6_gb300.ensemble import (EnsembleLinear, assemble_member, concat_systems,
+                                         make_ensemble)
+    from modflow6_gb300.ims import ImsLinearSettings
+    from modflow6_gb300.workloads import C4_IMS
+
+    count = 256 if a.scale == 1.0 else 16
+    members = make_ensemble(count, seed=a.seed, scale=a.scale)
+    systems = [assemble_member(m) for m in members]
+    mrow, ia, ja, amat, rhs, x0 = concat_systems([s[0] for s in systems], [s[1] for s in systems],
+                                                 [s[2] for s in systems], [s[3] for s in systems])
+    del systems
+    shapes = [(m.nlay, m.nrow, m.ncol) for m in members]
+    ens = EnsembleLinear(ImsLinearSettings(**C4_IMS)).allocate(mrow, ia, ja, shapes)
+    dev = torch.device("cuda")
+    d_amat, d_rhs = torch.from_numpy(amat).to(dev), torch.from_numpy(rhs).to(dev)
+    d_x0 = torch.from_numpy(x0).to(dev)
+    d_x = d_x0.clone()
+    res = None
+    for _ in range(a.warmup):
+        d_x.copy_(d_x0)
+        res = ens.apply_device(d_amat.data_ptr(), d_rhs.data_ptr(), d_x.data_ptr())
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.steps):
+        d_x.copy_(d_x0)
+        res = ens.apply_device(d_amat.data_ptr(), d_rhs.data_ptr(), d_x.data_ptr())
+    e1.record()
+    barrier()
+    ms = maxr(e0.elapsed_time(e1) / max(1, a.steps))
+    its = np.array([r.in_iter for r in res])
+    conv = int(sum(r.icnvg for r in res))
+    ens.close()
+    cells = int(mrow[-1])
+    return {"workload": f"{count} DIS members, nrow/ncol U{{50..450}} x scale {a.scale}, nlay U{{1..5}}",
+            "members": count, "cells": cells, "nonzeros": int(ia[-1]), "value": ms / 1e3, "unit": "s",
+            "members_per_s": count / (ms / 1e3), "converged": conv,
+            "inner_iterations": {"min": int(its.min()), "mean": float(its.mean()),
+                                 "max": int(its.max())},
+            "form": "FP64 batched PCG + wavefront ILU0, one CUDA graph for all members"}
 
 
 def kernels_arm(a):
@@ -435,7 +487,7 @@ def kernels_arm(a):
     # the full-grid (index-free SpMV, wavefront sweeps) forms, then the
     # general-pattern form (SELL-32 SpMV, level-scheduled sweeps) in FP64
     for name, prec, st in (("fp64", _lib.GBIMS_FP64, shape), ("mixed", _lib.GBIMS_MIXED, shape),
-                           ("fp64_general", _lib.GBIMS_FP64, None)):
+                           ("fp64_general", _lib.GBIMS_FP64, (0, 0, 0))):
         ims = ImsLinear(ImsLinearSettings(precision=prec, structure=st, **C2_IMS))
         ims.imslinear_allocate(m.nodes, con["ia"], con["ja"])
         rc = lib.gbims_factor(ims._h, _lib.dptr(amat), None)

@@ -102,6 +102,29 @@ int gbims_apply_device(gbims_handle *h, double *d_amat, double *d_rhs, double *d
 /* Replaces ImsLinearDataType%imslinear_da. */
 int gbims_destroy(gbims_handle *h);
 
+/* Batched ensembles (no counterpart in the reference, which solves one
+ * simulation at a time): nmembers independent systems concatenated into one
+ * block-diagonal system.  member_rows (nmembers+1, index_base) gives each
+ * member's first row; ia/ja are the concatenated CSR with global column
+ * numbers, which must stay inside the member's own rows.  One apply solves
+ * every member to its own closure with its own PCG iteration
+ * (ImsLinearBase.f90:30-240): per-member Krylov scalars, convergence test and
+ * exit, all members advanced by the same kernel launches.  icnvg, in_iter and
+ * summaries (may be NULL) have nmembers entries; locdv/locr are member-local
+ * rows.  shapes (3 * nmembers: nlay, nrow, ncol per member) may be NULL;
+ * when given, every member must be a full DIS grid of that shape and the
+ * preconditioner runs as one wavefront launch over all members (otherwise the
+ * level schedule of the whole batch).  FP64 PCG only (GBIMS_ERR_UNSUPPORTED
+ * otherwise); the handle is released with gbims_destroy. */
+int gbims_batch_create(const gbims_settings *settings, int nmembers, const int *member_rows,
+                       int neq, int nja, const int *ia, const int *ja, const int *shapes,
+                       gbims_handle **out);
+int gbims_batch_apply(gbims_handle *h, double *amat, double *rhs, double *x, int kstp,
+                      int kiter, int *icnvg, int *in_iter, gbims_summary *summaries);
+int gbims_batch_apply_device(gbims_handle *h, double *d_amat, double *d_rhs, double *d_x,
+                             int kstp, int kiter, int *icnvg, int *in_iter,
+                             gbims_summary *summaries);
+
 /* Building blocks of apply, exposed for callers that drive their own loop
  * and for kernel-level checks (host arrays):
  *  gbims_factor       preconditioner update, ims_base_pcu + ims_base_pcilu0
@@ -134,6 +157,7 @@ long long gbims_kernel_launches(const gbims_handle *h);
 /* Message of the last error on this handle (never NULL). */
 const char *gbims_last_error(const gbims_handle *h);
 const char *gbims_status_string(int status);
+
 
 /* ---- GWF NPF conductance fill (gwf-npf.f90:474-698) ---------------------- */
 

@@ -93,6 +93,12 @@ _SIGS = {
     "gbims_apply": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int, _ip, _ip, C.POINTER(GbimsSummary)]),
     "gbims_apply_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, _ip, _ip, C.POINTER(GbimsSummary)]),
     "gbims_destroy": (C.c_int, [C.c_void_p]),
+    "gbims_batch_create": (C.c_int, [C.POINTER(GbimsSettings), C.c_int, _ip, C.c_int, C.c_int, _ip,
+                                     _ip, _ip, C.POINTER(C.c_void_p)]),
+    "gbims_batch_apply": (C.c_int, [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int, _ip, _ip,
+                                    C.POINTER(GbimsSummary)]),
+    "gbims_batch_apply_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                           C.c_int, _ip, _ip, C.POINTER(GbimsSummary)]),
     "gbims_time_kernels": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "gbims_factor": (C.c_int, [C.c_void_p, _dp, _ip]),
     "gbims_get_apc": (C.c_int, [C.c_void_p, _dp]),

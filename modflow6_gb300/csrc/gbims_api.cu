@@ -14,6 +14,7 @@
 #include "k_krylov.cuh"
 #include <algorithm>
 #include <climits>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -30,7 +31,8 @@ struct gbims_handle {
   Sell S;
   Levels F, B;
   Dia7 D;
-  bool structured = false;
+  bool structured = false;  // wavefront sweeps (one or more full DIS grids)
+  bool dia_spmv = false;    // index-free SpMV (a single full DIS grid)
   // owned FP64 buffers
   double *d_amat = nullptr, *d_rhs = nullptr, *d_x = nullptr;
   double *v_d = nullptr, *v_p = nullptr, *v_q = nullptr, *v_z = nullptr, *v_t = nullptr,
@@ -38,6 +40,9 @@ struct gbims_handle {
   // FP32 inner vectors (mixed)
   float *f_d = nullptr, *f_p = nullptr, *f_q = nullptr, *f_z = nullptr, *f_t = nullptr,
         *f_v = nullptr, *f_dhat = nullptr, *f_phat = nullptr, *f_qhat = nullptr;
+  // SCALING_METHOD: DSCALE, DSCALE2 and the column position map (L2NORM)
+  double *d_dscale = nullptr, *d_dscale2 = nullptr;
+  int *d_cptr = nullptr, *d_cpos = nullptr;
   double *d_part = nullptr;
   int G = 1;
   Ctl *d_ctl = nullptr, *h_ctl = nullptr;
@@ -48,6 +53,13 @@ struct gbims_handle {
   bool graph_tried = false, graph_ok = false;
   double refine_factor = 1.0e-5;
   bool factored = false;
+  // batched ensemble (nm > 0): members concatenated into one block-diagonal
+  // system, one control block per member, the handle's Ctl = all done
+  int nm = 0;
+  std::vector<int> mrow;  // member -> first row (nm + 1)
+  int *d_bcm = nullptr, *d_bcr = nullptr, *d_bmc = nullptr, *d_bmr = nullptr;
+  Ctl *d_ctls = nullptr, *h_ctls = nullptr;
+  BatchDev bd;
   long long launches = 0;  // kernels launched by this handle (graph bodies counted per body)
   int body_kernels = 0;    // kernel nodes in one inner-loop body
   std::string err;
@@ -87,70 +99,101 @@ static void precond32(gbims_handle *h, const float *r, float *z) {
   else launch_ilu_apply_levels32(h->n, h->d_iapc, h->d_japc, h->d_apc32, h->F, h->B, r, z, h->d_ctl, h->st);
 }
 
+// A*x and b - A*x: index-free on full DIS grids, SELL-32 otherwise.
+static void spmv64(gbims_handle *h, const double *x, double *y, const Ctl *c) {
+  if (h->dia_spmv) launch_dia7_spmv64(h->D, x, y, c, h->st);
+  else launch_spmv64(h->S, x, y, c, h->st);
+}
+
+static void spmv32(gbims_handle *h, const float *x, float *y, const Ctl *c) {
+  if (h->dia_spmv) launch_dia7_spmv32(h->D, x, y, c, h->st);
+  else launch_spmv32(h->S, x, y, c, h->st);
+}
+
+static void residual64(gbims_handle *h, const Ctl *c, int only_if_north_due) {
+  if (h->dia_spmv) launch_dia7_residual64(h->D, h->d_x, h->d_rhs, h->v_d, c, only_if_north_due, h->st);
+  else launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, c, only_if_north_due, h->st);
+}
+
 static void enqueue_iteration(gbims_handle *h, unsigned long long cond, int use_cond) {
   const int n = h->n, G = h->G;
   Ctl *c = h->d_ctl;
   cudaStream_t st = h->st;
   double *part = h->d_part;
+  if (h->nm > 0) {
+    // batched ensemble, PCG: every member's iteration in the same launches
+    const BatchDev &B = h->bd;
+    precond64(h, h->v_d, h->v_z);
+    kb_dot64(B, h->v_d, h->v_z, part, st);
+    kb_ctl_cg_rho(B, part, st);
+    kb_cg_pupdate64(B, h->v_z, h->v_p, st);
+    spmv64(h, h->v_p, h->v_q, c);
+    kb_dot64(B, h->v_p, h->v_q, part, st);
+    kb_ctl_alpha(B, part, st);
+    kb_cg_update64(B, h->d_x, h->v_d, h->v_p, h->v_q, part, st);
+    kb_ctl_cg_cnvg(B, part, st);
+    kb_all_done(B, c, cond, use_cond, 1, st);
+    return;
+  }
   if (!h->mixed && !h->bcgs) {
     // ims_base_cg, ImsLinearBase.f90:100-236
     precond64(h, h->v_d, h->v_z);
     kr_dot64(n, h->v_d, h->v_z, part, G, c, st);
     kr_ctl_cg_rho(c, part, G, st);
     kr_cg_pupdate64(n, h->v_z, h->v_p, c, st);
-    launch_spmv64(h->S, h->v_p, h->v_q, c, st);
+    spmv64(h, h->v_p, h->v_q, c);
     kr_dot64(n, h->v_p, h->v_q, part, G, c, st);
     kr_ctl_alpha(c, part, G, st);
     kr_cg_update64(n, h->d_x, h->v_d, h->v_p, h->v_q, part, G, c, st);
     kr_ctl_cg_cnvg(c, part, G, cond, use_cond, st);
-    launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, c, 1, st);
+    residual64(h, c, 1);
   } else if (!h->mixed && h->bcgs) {
     // ims_base_bcgs, ImsLinearBase.f90:338-545
     kr_dot64(n, h->v_dhat, h->v_d, part, G, c, st);
     kr_ctl_bcgs_rho(c, part, G, st);
     kr_bcgs_p64(n, h->v_d, h->v_p, h->v_v, c, st);
     precond64(h, h->v_p, h->v_phat);
-    launch_spmv64(h->S, h->v_phat, h->v_v, c, st);
+    spmv64(h, h->v_phat, h->v_v, c);
     kr_dot64(n, h->v_dhat, h->v_v, part, G, c, st);
     kr_ctl_alpha(c, part, G, st);
     kr_bcgs_q64(n, h->v_d, h->v_v, h->v_q, c, st);
     precond64(h, h->v_q, h->v_qhat);
-    launch_spmv64(h->S, h->v_qhat, h->v_t, c, st);
+    spmv64(h, h->v_qhat, h->v_t, c);
     kr_dot_tq_tt64(n, h->v_t, h->v_q, part, G, c, st);
     kr_ctl_omega(c, part, G, st);
-    kr_bcgs_update64(n, h->d_x, h->v_d, h->v_phat, h->v_qhat, h->v_q, h->v_t, nullptr, part, G, c, st);
+    kr_bcgs_update64(n, h->d_x, h->v_d, h->v_phat, h->v_qhat, h->v_q, h->v_t, h->d_dscale, part, G, c, st);
     kr_ctl_bcgs_cnvg(c, part, G, cond, use_cond, st);
-    launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, c, 1, st);
+    residual64(h, c, 1);
   } else if (h->mixed && !h->bcgs) {
     precond32(h, h->f_d, h->f_z);
     kr_dot32(n, h->f_d, h->f_z, part, G, c, st);
     kr_ctl_cg_rho(c, part, G, st);
     kr_cg_pupdate32(n, h->f_z, h->f_p, c, st);
-    launch_spmv32(h->S, h->f_p, h->f_q, c, st);
+    spmv32(h, h->f_p, h->f_q, c);
     kr_dot32(n, h->f_p, h->f_q, part, G, c, st);
     kr_ctl_alpha(c, part, G, st);
     kr_cg_update_mixed(n, h->d_x, h->f_d, h->f_p, h->f_q, part, G, c, st);
     kr_ctl_mixed_inner(c, part, G, 0, h->refine_factor, st);
-    launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, c, 1, st);
-    kr_true_resid_stats(n, h->v_d, h->f_d, nullptr, part, G, c, st);
+    residual64(h, c, 1);
+    kr_true_resid_stats(n, h->v_d, h->f_d, nullptr, nullptr, part, G, c, st);
     kr_ctl_refine(c, part, G, cond, use_cond, st);
   } else {
     kr_dot32(n, h->f_dhat, h->f_d, part, G, c, st);
     kr_ctl_bcgs_rho(c, part, G, st);
     kr_bcgs_p32(n, h->f_d, h->f_p, h->f_v, c, st);
     precond32(h, h->f_p, h->f_phat);
-    launch_spmv32(h->S, h->f_phat, h->f_v, c, st);
+    spmv32(h, h->f_phat, h->f_v, c);
     kr_dot32(n, h->f_dhat, h->f_v, part, G, c, st);
     kr_ctl_alpha(c, part, G, st);
     kr_bcgs_q32(n, h->f_d, h->f_v, h->f_q, c, st);
     precond32(h, h->f_q, h->f_qhat);
-    launch_spmv32(h->S, h->f_qhat, h->f_t, c, st);
+    spmv32(h, h->f_qhat, h->f_t, c);
     kr_dot_tq_tt32(n, h->f_t, h->f_q, part, G, c, st);
     kr_ctl_omega(c, part, G, st);
-    kr_bcgs_update32(n, h->d_x, h->f_d, h->f_phat, h->f_qhat, h->f_q, h->f_t, nullptr, part, G, c, st);
+    kr_bcgs_update32(n, h->d_x, h->f_d, h->f_phat, h->f_qhat, h->f_q, h->f_t, h->d_dscale, part, G, c, st);
     kr_ctl_mixed_inner(c, part, G, 1, h->refine_factor, st);
-    launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, c, 1, st);
-    kr_true_resid_stats(n, h->v_d, h->f_d, h->f_dhat, part, G, c, st);
+    residual64(h, c, 1);
+    kr_true_resid_stats(n, h->v_d, h->f_d, h->f_dhat, h->d_dscale, part, G, c, st);
     kr_ctl_refine(c, part, G, cond, use_cond, st);
   }
 }
@@ -215,6 +258,33 @@ static bool build_graph(gbims_handle *h) {
 // ---------------------------------------------------------------------------
 // create
 // ---------------------------------------------------------------------------
+// Wavefront-sweep buffers for members of the given DIS shapes (nlay, nrow,
+// ncol per member) whose rows start at row0.
+static int setup_structured(gbims_handle *h, const std::vector<int> &shapes,
+                            const std::vector<long long> &row0) {
+  dia7_layout(h->D, shapes, row0, h->mixed);
+  const size_t nn = (size_t)h->D.slots;
+  if (!h->mixed) {
+    double **a[] = {&h->D.d_lz, &h->D.d_ly, &h->D.d_lx, &h->D.d_ux, &h->D.d_uy, &h->D.d_uz,
+                    &h->D.d_dinv, &h->D.d_rsk, &h->D.d_ysk, &h->D.d_zsk};
+    for (double **p : a) GB_CUDA(h, dalloc(p, nn));
+  } else {
+    float **a[] = {&h->D.f_lz, &h->D.f_ly, &h->D.f_lx, &h->D.f_ux, &h->D.f_uy, &h->D.f_uz,
+                   &h->D.f_dinv, &h->D.f_rsk, &h->D.f_ysk, &h->D.f_zsk};
+    for (float **p : a) GB_CUDA(h, dalloc(p, nn));
+  }
+  GB_CUDA(h, dalloc(&h->D.d_geo, h->D.geo.size()));
+  GB_CUDA(h, cudaMemcpy(h->D.d_geo, h->D.geo.data(), sizeof(Dia7Geo) * h->D.geo.size(),
+                        cudaMemcpyHostToDevice));
+  // one 128-byte progress line per CTA plus the ticket line
+  h->D.nflags = (h->D.ntickets + 2) * 32;
+  GB_CUDA(h, dalloc(&h->D.d_flags, h->D.nflags));
+  GB_CUDA(h, dalloc(&h->D.d_err, 4));
+  GB_CUDA(h, cudaMemset(h->D.d_err, 0, sizeof(int) * 4));
+  h->structured = true;
+  return GBIMS_OK;
+}
+
 extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int *ia,
                             const int *ja, gbims_handle **out) {
   if (!out) return GBIMS_ERR_ARG;
@@ -238,10 +308,13 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   if (s->relax > 1.0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RELAX MUST BE <= 1.0"); }
   if (h->ipc >= 3) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "ILUT/MILUT (PRECONDITIONER_LEVELS/DROP_TOLERANCE > 0) is not supported"); }
   if (s->iord != 0) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "REORDERING_METHOD RCM/MD is not supported"); }
-  if (s->iscl != 0) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "SCALING_METHOD other than NONE is not supported"); }
   if (s->precision != GBIMS_FP64 && s->precision != GBIMS_MIXED) { *out = h; return fail(h, GBIMS_ERR_ARG, "precision must be GBIMS_FP64 or GBIMS_MIXED"); }
   h->mixed = (s->precision == GBIMS_MIXED);
   h->bcgs = (s->ilinmeth == 2);
+  // GBIMS_GRAPH=0: the inner loop is driven from the host (the same kernels,
+  // launched one by one), for profilers that do not see kernel nodes inside
+  // conditional graphs
+  if (const char *g = std::getenv("GBIMS_GRAPH")) h->graph_tried = (g[0] == '0');
   // 0-based copies and checks: diagonal first in every row
   int base = s->index_base ? 1 : 0;
   h->ia.resize(neq + 1);
@@ -293,8 +366,19 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   GB_CUDA(h, cudaMemcpy(h->d_iapc, h->iapc.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemcpy(h->d_japc, h->japc.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemset(h->d_apc, 0, sizeof(double) * nja));
-  // SELL-32 layout of A
-  {
+  // optional structured 7-point sweeps (and the index-free SpMV)
+  if (s->nlay > 0 && s->nrow > 0 && s->ncol > 0 &&
+      dia7_matches(s->nlay, s->nrow, s->ncol, neq, h->ia, h->ja)) {
+    std::vector<int> shape = {s->nlay, s->nrow, s->ncol};
+    int rc = setup_structured(h, shape, std::vector<long long>{0});
+    if (rc != GBIMS_OK) return rc;
+    GB_CUDA(h, dalloc(&h->D.d_sv, (size_t)7 * neq));
+    if (h->mixed) GB_CUDA(h, dalloc(&h->D.f_sv, (size_t)7 * neq));
+    h->dia_spmv = true;
+  }
+  // SELL-32 layout of A (unstructured patterns; a single full DIS grid uses
+  // the index-free product)
+  if (!h->dia_spmv) {
     std::vector<int> ptr, col, src;
     sell_build_host(neq, h->ia, h->ja, ptr, col, src);
     if ((long long)col.size() > INT_MAX) return fail(h, GBIMS_ERR_UNSUPPORTED, "matrix too large for 32-bit SELL offsets");
@@ -313,30 +397,6 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   // level schedules of the triangular sweeps and the factorisation
   levels_build_host(neq, h->iapc, h->japc, true, h->F);
   levels_build_host(neq, h->iapc, h->japc, false, h->B);
-  // optional structured 7-point sweeps
-  if (s->nlay > 0 && s->nrow > 0 && s->ncol > 0 &&
-      dia7_matches(s->nlay, s->nrow, s->ncol, neq, h->ia, h->ja)) {
-    h->D.nlay = s->nlay;
-    h->D.nrow = s->nrow;
-    h->D.ncol = s->ncol;
-    dia7_geometry(s->nlay, s->nrow, s->ncol, h->mixed, &h->D.nb, &h->D.G, &h->D.slots);
-    size_t nn = (size_t)h->D.slots;
-    if (!h->mixed) {
-      double **a[] = {&h->D.d_lz, &h->D.d_ly, &h->D.d_lx, &h->D.d_ux, &h->D.d_uy, &h->D.d_uz,
-                      &h->D.d_dinv, &h->D.d_rsk, &h->D.d_ysk, &h->D.d_zsk};
-      for (double **p : a) GB_CUDA(h, dalloc(p, nn));
-    } else {
-      float **a[] = {&h->D.f_lz, &h->D.f_ly, &h->D.f_lx, &h->D.f_ux, &h->D.f_uy, &h->D.f_uz,
-                     &h->D.f_dinv, &h->D.f_rsk, &h->D.f_ysk, &h->D.f_zsk};
-      for (float **p : a) GB_CUDA(h, dalloc(p, nn));
-    }
-    // one 128-byte progress line per CTA plus the ticket line
-    h->D.nflags = (s->nlay * h->D.nb + 2) * 32;
-    GB_CUDA(h, dalloc(&h->D.d_flags, h->D.nflags));
-    GB_CUDA(h, dalloc(&h->D.d_err, 4));
-    GB_CUDA(h, cudaMemset(h->D.d_err, 0, sizeof(int) * 4));
-    h->structured = true;
-  }
   // vectors (with slack after the last cell for the sweeps' aligned copies)
   size_t nn = (size_t)neq + kVecPad;
   GB_CUDA(h, dalloc(&h->d_amat, nja));
@@ -360,6 +420,20 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
       GB_CUDA(h, dalloc(&h->f_t, nn)); GB_CUDA(h, dalloc(&h->f_v, nn));
       GB_CUDA(h, dalloc(&h->f_dhat, nn)); GB_CUDA(h, dalloc(&h->f_phat, nn));
       GB_CUDA(h, dalloc(&h->f_qhat, nn));
+    }
+  }
+  // SCALING_METHOD (ImsLinear.f90:222-224): DSCALE/DSCALE2 only when scaling;
+  // BiCGSTAB reads DSCALE in its convergence maxima (null without scaling)
+  if (s->iscl != 0) {
+    GB_CUDA(h, dalloc(&h->d_dscale, nn));
+    GB_CUDA(h, dalloc(&h->d_dscale2, nn));
+    if (s->iscl == 2) {
+      std::vector<int> cptr, cpos;
+      scale_colmap_host(neq, h->ia, h->ja, cptr, cpos);
+      GB_CUDA(h, dalloc(&h->d_cptr, cptr.size()));
+      GB_CUDA(h, dalloc(&h->d_cpos, cpos.size()));
+      GB_CUDA(h, cudaMemcpy(h->d_cptr, cptr.data(), sizeof(int) * cptr.size(), cudaMemcpyHostToDevice));
+      GB_CUDA(h, cudaMemcpy(h->d_cpos, cpos.data(), sizeof(int) * cpos.size(), cudaMemcpyHostToDevice));
     }
   }
   h->G = std::max(1, std::min(kMaxRedBlocks, (neq + kRedBlock - 1) / kRedBlock));
@@ -395,7 +469,8 @@ __global__ void k_zero_vec(int n, double *a, double *b, double *c, double *d) {
 static int factor_core(gbims_handle *h) {
   const int n = h->n;
   cudaStream_t st = h->st;
-  launch_sell_fill(h->S, h->d_amat, st);
+  if (h->dia_spmv) launch_dia7_vfill(h->D, h->d_ia, h->d_amat, st);
+  else launch_sell_fill(h->S, h->d_amat, st);
   h->launches += 1;
   int ipcflag = 0, icount = 0;
   double delta = 0.0;
@@ -436,6 +511,10 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
   cudaStream_t st = h->st;
   (void)kiter;
   GB_CUDA(h, cudaEventRecord(h->ev0, st));
+  // SCALE PROBLEM (ImsLinear.f90:644-650)
+  if (h->s.iscl != 0)
+    h->launches += launch_scale(h->s.iscl, n, h->d_ia, h->d_ja, h->d_cptr, h->d_cpos, h->d_amat,
+                                h->d_x, h->d_rhs, h->d_dscale, h->d_dscale2, st);
   int icount = factor_core(h);
   if (icount < 0) return icount;
   // control block
@@ -456,7 +535,7 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
   // D, P, Q, Z = 0 ; D = B - A X ; L2NORM0 (ImsLinear.f90:686-703)
   int eg = std::min(4 * kNumSM, (n + 255) / 256);
   k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
-  launch_residual64(h->S, h->d_x, h->d_rhs, h->v_d, nullptr, 0, st);
+  residual64(h, nullptr, 0);
   kr_sumsq64(n, h->v_d, h->d_part, h->G, st);
   kr_ctl_set_l2norm0(h->d_ctl, h->d_part, h->G, st);
   if (h->bcgs && !h->mixed) GB_CUDA(h, cudaMemcpyAsync(h->v_dhat, h->v_d, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
@@ -484,6 +563,12 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
       if (h->h_ctl->done || total > 4 * (h->s.iter1 + 2)) break;
       batch = std::min(batch * 2, 32);
     }
+  }
+  // UNSCALE the solution (ImsLinear.f90:739-745); amat and rhs are the
+  // handle's own copies and are refilled by the next apply
+  if (h->s.iscl != 0) {
+    launch_unscale_x(n, h->d_x, h->d_dscale2, st);
+    h->launches += 1;
   }
   GB_CUDA(h, cudaEventRecord(h->ev1, st));
   GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
@@ -526,6 +611,7 @@ extern "C" int gbims_apply(gbims_handle *h, double *amat, double *rhs, double *x
                            int kiter, int *icnvg, int *in_iter, gbims_summary *summary) {
   if (!h || !amat || !rhs || !x || !icnvg || !in_iter) return GBIMS_ERR_ARG;
   if (!h->d_ctl) return fail(h, GBIMS_ERR_STATE, "handle was not created successfully");
+  if (h->nm > 0) return fail(h, GBIMS_ERR_STATE, "batch handle: use gbims_batch_apply");
   GB_CUDA(h, cudaMemcpyAsync(h->d_amat, amat, sizeof(double) * h->nja, cudaMemcpyHostToDevice, h->st));
   GB_CUDA(h, cudaMemcpyAsync(h->d_rhs, rhs, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
   GB_CUDA(h, cudaMemcpyAsync(h->d_x, x, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
@@ -541,6 +627,7 @@ extern "C" int gbims_apply_device(gbims_handle *h, double *d_amat, double *d_rhs
                                   gbims_summary *summary) {
   if (!h || !d_amat || !d_rhs || !d_x || !icnvg || !in_iter) return GBIMS_ERR_ARG;
   if (!h->d_ctl) return fail(h, GBIMS_ERR_STATE, "handle was not created successfully");
+  if (h->nm > 0) return fail(h, GBIMS_ERR_STATE, "batch handle: use gbims_batch_apply_device");
   GB_CUDA(h, cudaMemcpyAsync(h->d_amat, d_amat, sizeof(double) * h->nja, cudaMemcpyDeviceToDevice, h->st));
   GB_CUDA(h, cudaMemcpyAsync(h->d_rhs, d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
   GB_CUDA(h, cudaMemcpyAsync(h->d_x, d_x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
@@ -575,7 +662,7 @@ extern "C" int gbims_matvec(gbims_handle *h, const double *x, double *y) {
   if (!h || !x || !y) return GBIMS_ERR_ARG;
   if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no matrix: call gbims_factor or gbims_apply first");
   GB_CUDA(h, cudaMemcpyAsync(h->v_d, x, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
-  launch_spmv64(h->S, h->v_d, h->d_rhs, nullptr, h->st);
+  spmv64(h, h->v_d, h->d_rhs, nullptr);
   GB_CUDA(h, cudaGetLastError());
   GB_CUDA(h, cudaMemcpyAsync(y, h->d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
   GB_CUDA(h, cudaStreamSynchronize(h->st));
@@ -637,23 +724,28 @@ extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times 
     return ms / reps;
   };
   if (!h->mixed) {
-    t->spmv_ms = time_it([&] { launch_spmv64(h->S, h->v_p, h->v_q, h->d_ctl, st); });
+    t->spmv_ms = time_it([&] { spmv64(h, h->v_p, h->v_q, h->d_ctl); });
     t->precond_ms = time_it([&] { precond64(h, h->v_p, h->v_z); });
     t->dot_ms = time_it([&] { kr_dot64(n, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
     t->update_ms = time_it([&] { kr_cg_update64(n, h->v_z, h->v_d, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
   } else {
-    t->spmv_ms = time_it([&] { launch_spmv32(h->S, h->f_p, h->f_q, h->d_ctl, st); });
+    t->spmv_ms = time_it([&] { spmv32(h, h->f_p, h->f_q, h->d_ctl); });
     t->precond_ms = time_it([&] { precond32(h, h->f_p, h->f_z); });
     t->dot_ms = time_it([&] { kr_dot32(n, h->f_p, h->f_q, h->d_part, h->G, h->d_ctl, st); });
     t->update_ms = time_it([&] { kr_cg_update_mixed(n, h->v_d, h->f_d, h->f_p, h->f_q, h->d_part, h->G, h->d_ctl, st); });
   }
   GB_CUDA(h, cudaGetLastError());
   // algorithmic bytes: CSR values + column indices + row pointers, x read
-  // once, y written once; preconditioner: APC + JAPC + IAPC, r read, z
-  // written, plus one intermediate vector written and read back.
+  // once, y written once (the index-free product of a full DIS grid: values,
+  // x and y only); preconditioner: every factor value once, r read
+  // and z written once, plus JAPC/IAPC for the unstructured sweeps (the
+  // structured sweeps need no indices).  The forward result kept between
+  // the two sweeps is not counted.
   double vb = h->mixed ? 4.0 : 8.0;
-  t->spmv_bytes = (vb + 4.0) * h->nja + 4.0 * (n + 1) + 2.0 * vb * n;
-  t->precond_bytes = (vb + 4.0) * h->nja + 4.0 * (n + 1) + 4.0 * vb * n;
+  t->spmv_bytes = h->dia_spmv ? vb * h->nja + 2.0 * vb * n
+                                 : (vb + 4.0) * h->nja + 4.0 * (n + 1) + 2.0 * vb * n;
+  t->precond_bytes = vb * h->nja + 2.0 * vb * n;
+  if (!h->structured) t->precond_bytes += 4.0 * h->nja + 4.0 * (n + 1);
   return GBIMS_OK;
 }
 
@@ -670,10 +762,12 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->D.d_flags, h->D.d_err, h->d_amat, h->d_rhs, h->d_x, h->v_d, h->v_p, h->v_q,
                   h->v_z, h->v_t, h->v_v, h->v_dhat, h->v_phat, h->v_qhat, h->f_d, h->f_p,
                   h->f_q, h->f_z, h->f_t, h->f_v, h->f_dhat, h->f_phat, h->f_qhat, h->d_part,
-                  h->d_ctl};
+                  h->d_dscale, h->d_dscale2, h->d_cptr, h->d_cpos, h->D.d_sv, h->D.f_sv,
+                  h->d_bcm, h->d_bcr, h->d_bmc, h->d_bmr, h->d_ctls, h->D.d_geo, h->d_ctl};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
+  if (h->h_ctls) cudaFreeHost(h->h_ctls);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->st) cudaStreamDestroy(h->st);
@@ -700,6 +794,216 @@ extern "C" const char *gbims_status_string(int status) {
   case GBIMS_ERR_STATE: return "invalid handle state";
   default: return "unknown status";
   }
+}
+
+// ---------------------------------------------------------------------------
+// batched ensemble
+// ---------------------------------------------------------------------------
+extern "C" int gbims_batch_create(const gbims_settings *settings, int nmembers,
+                                  const int *member_rows, int neq, int nja, const int *ia,
+                                  const int *ja, const int *shapes, gbims_handle **out) {
+  if (!out) return GBIMS_ERR_ARG;
+  *out = nullptr;
+  if (!settings || !member_rows || nmembers <= 0 || neq <= 0) return GBIMS_ERR_ARG;
+  const int base = settings->index_base ? 1 : 0;
+  std::vector<int> mrow(nmembers + 1);
+  for (int m = 0; m <= nmembers; ++m) mrow[m] = member_rows[m] - base;
+  if (mrow[0] != 0 || mrow[nmembers] != neq) return GBIMS_ERR_ARG;
+  for (int m = 0; m < nmembers; ++m)
+    if (mrow[m + 1] <= mrow[m]) return GBIMS_ERR_ARG;
+  gbims_settings s = *settings;
+  s.nlay = s.nrow = s.ncol = 0;  // members are swept by the level schedule of the whole batch
+  int rc = gbims_create(&s, neq, nja, ia, ja, out);
+  gbims_handle *h = *out;
+  if (rc != GBIMS_OK) return rc;
+  if (h->mixed || h->bcgs || s.north > 0)
+    return fail(h, GBIMS_ERR_UNSUPPORTED, "batched ensembles: FP64 PCG without NORTH");
+  // block-diagonal: every column of a member's rows lies inside the member
+  for (int m = 0; m < nmembers; ++m)
+    for (int r = mrow[m]; r < mrow[m + 1]; ++r)
+      for (int k = h->ia[r]; k < h->ia[r + 1]; ++k)
+        if (h->ja[k] < mrow[m] || h->ja[k] >= mrow[m + 1])
+          return fail(h, GBIMS_ERR_ARG, "member rows couple to another member (not block-diagonal)");
+  // chunks of kChunkRows rows inside each member
+  std::vector<int> cm, cr, mc(nmembers + 1, 0);
+  for (int m = 0; m < nmembers; ++m) {
+    mc[m] = (int)cm.size();
+    for (int r = mrow[m]; r < mrow[m + 1]; r += kChunkRows) {
+      cm.push_back(m);
+      cr.push_back(r);
+    }
+  }
+  mc[nmembers] = (int)cm.size();
+  cr.push_back(neq);
+  const int nchunks = (int)cm.size();
+  h->nm = nmembers;
+  h->mrow = mrow;
+  GB_CUDA(h, dalloc(&h->d_bcm, cm.size()));
+  GB_CUDA(h, dalloc(&h->d_bcr, cr.size()));
+  GB_CUDA(h, dalloc(&h->d_bmc, mc.size()));
+  GB_CUDA(h, dalloc(&h->d_bmr, mrow.size()));
+  GB_CUDA(h, dalloc(&h->d_ctls, (size_t)nmembers));
+  GB_CUDA(h, cudaMallocHost((void **)&h->h_ctls, sizeof(Ctl) * nmembers));
+  GB_CUDA(h, cudaMemcpy(h->d_bcm, cm.data(), sizeof(int) * cm.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(h, cudaMemcpy(h->d_bcr, cr.data(), sizeof(int) * cr.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(h, cudaMemcpy(h->d_bmc, mc.data(), sizeof(int) * mc.size(), cudaMemcpyHostToDevice));
+  GB_CUDA(h, cudaMemcpy(h->d_bmr, mrow.data(), sizeof(int) * mrow.size(), cudaMemcpyHostToDevice));
+  // partials: 8 slots per chunk
+  if ((size_t)nchunks > (size_t)h->G) {
+    cudaFree(h->d_part);
+    h->d_part = nullptr;
+    GB_CUDA(h, dalloc(&h->d_part, (size_t)nchunks * 8));
+  }
+  h->bd.nm = nmembers;
+  h->bd.nchunks = nchunks;
+  h->bd.cm = h->d_bcm;
+  h->bd.cr = h->d_bcr;
+  h->bd.mc = h->d_bmc;
+  h->bd.mr = h->d_bmr;
+  h->bd.ctls = h->d_ctls;
+  // full DIS grids: the wavefront sweeps run every member's layers and
+  // blocks as the CTAs of one launch
+  if (shapes) {
+    std::vector<int> sh(shapes, shapes + 3 * nmembers);
+    std::vector<long long> row0(nmembers);
+    std::vector<int> lia, lja;
+    for (int m = 0; m < nmembers; ++m) {
+      const int r0 = mrow[m], nr = mrow[m + 1] - mrow[m];
+      lia.assign(nr + 1, 0);
+      lja.clear();
+      for (int r = 0; r < nr; ++r) {
+        for (int k = h->ia[r0 + r]; k < h->ia[r0 + r + 1]; ++k) lja.push_back(h->ja[k] - r0);
+        lia[r + 1] = (int)lja.size();
+      }
+      if (sh[3 * m] <= 0 || sh[3 * m + 1] <= 0 || sh[3 * m + 2] <= 0 ||
+          !dia7_matches(sh[3 * m], sh[3 * m + 1], sh[3 * m + 2], nr, lia, lja))
+        return fail(h, GBIMS_ERR_ARG, "member " + std::to_string(m) +
+                                          ": pattern is not the full DIS grid of its shape");
+      row0[m] = r0;
+    }
+    int rc2 = setup_structured(h, sh, row0);
+    if (rc2 != GBIMS_OK) return rc2;
+  }
+  return GBIMS_OK;
+}
+
+static int batch_apply_core(gbims_handle *h, int kstp, int *icnvg, int *in_iter,
+                            gbims_summary *summaries) {
+  const int n = h->n, nm = h->nm;
+  cudaStream_t st = h->st;
+  GB_CUDA(h, cudaEventRecord(h->ev0, st));
+  if (h->s.iscl != 0)
+    h->launches += launch_scale(h->s.iscl, n, h->d_ia, h->d_ja, h->d_cptr, h->d_cpos, h->d_amat,
+                                h->d_x, h->d_rhs, h->d_dscale, h->d_dscale2, st);
+  int icount = factor_core(h);
+  if (icount < 0) return icount;
+  Ctl c;
+  memset(&c, 0, sizeof(c));
+  c.itmax = h->s.iter1;
+  c.icnvgopt = h->s.icnvgopt;
+  c.iscl = h->s.iscl;
+  c.dvclose = h->s.dvclose;
+  c.rclose = h->s.rclose;
+  c.epfact = epfact_of(h->s.icnvgopt, kstp);
+  c.iter = 1;
+  c.first = 1;
+  c.pivot_fail = INT_MAX;
+  for (int m = 0; m < nm; ++m) h->h_ctls[m] = c;
+  *h->h_ctl = c;  // the batch's own block: done = every member done
+  GB_CUDA(h, cudaMemcpyAsync(h->d_ctls, h->h_ctls, sizeof(Ctl) * nm, cudaMemcpyHostToDevice, st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+  int eg = std::min(4 * kNumSM, (n + 255) / 256);
+  k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
+  residual64(h, nullptr, 0);
+  kb_sumsq64(h->bd, h->v_d, h->d_part, st);
+  kb_ctl_set_l2norm0(h->bd, h->d_part, st);
+  kb_all_done(h->bd, h->d_ctl, 0ULL, 0, 0, st);
+  GB_CUDA(h, cudaGetLastError());
+  if (!h->graph_tried) build_graph(h);
+  if (h->graph_ok) {
+    GB_CUDA(h, cudaGraphLaunch(h->exec, st));
+  } else {
+    int batch = 1, total = 0;
+    for (;;) {
+      for (int b = 0; b < batch; ++b) enqueue_iteration(h, 0ULL, 0);
+      total += batch;
+      GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+      GB_CUDA(h, cudaStreamSynchronize(st));
+      if (h->h_ctl->done || total > 4 * (h->s.iter1 + 2)) break;
+      batch = std::min(batch * 2, 32);
+    }
+  }
+  if (h->s.iscl != 0) {
+    launch_unscale_x(n, h->d_x, h->d_dscale2, st);
+    h->launches += 1;
+  }
+  GB_CUDA(h, cudaEventRecord(h->ev1, st));
+  GB_CUDA(h, cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(h, cudaMemcpyAsync(h->h_ctls, h->d_ctls, sizeof(Ctl) * nm, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(h, cudaStreamSynchronize(st));
+  GB_CUDA(h, cudaGetLastError());
+  h->launches += 4 + (long long)h->body_kernels * h->h_ctl->bodies;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  bool nonfinite = false;
+  for (int m = 0; m < nm; ++m) {
+    const Ctl &r = h->h_ctls[m];
+    const int iters = (r.l2norm0 == 0.0 || h->s.iter1 <= 0) ? 0 : r.iter;
+    if (icnvg) icnvg[m] = r.icnvg;
+    if (in_iter) in_iter[m] = iters;
+    nonfinite = nonfinite || r.nonfinite;
+    if (summaries) {
+      gbims_summary &sm = summaries[m];
+      sm.iter_cnt = iters;
+      sm.icnvg = r.icnvg;
+      sm.pivot_retries = icount;
+      sm.exit_reason = r.exit_reason;
+      sm.dvmax = r.deltax;
+      sm.locdv = (int)r.xloc;
+      sm.rmax = r.rmax;
+      sm.locr = (int)r.rloc;
+      sm.l2norm0 = r.l2norm0;
+      sm.l2norm = r.l2norm;
+      sm.solve_ms = ms;
+      sm.refinements = 0;
+      sm.structured = h->structured ? 1 : 0;
+    }
+  }
+  if (nonfinite) return fail(h, GBIMS_ERR_NONFINITE, "non-finite values in a member's residual or head change");
+  if (h->h_ctl->guard_tripped) return fail(h, GBIMS_ERR_STATE, "inner loop cut by the body limit");
+  return icount > 0 ? GBIMS_WARN_PIVOT : GBIMS_OK;
+}
+
+extern "C" int gbims_batch_apply(gbims_handle *h, double *amat, double *rhs, double *x, int kstp,
+                                 int kiter, int *icnvg, int *in_iter, gbims_summary *summaries) {
+  (void)kiter;
+  if (!h || !amat || !rhs || !x || !icnvg || !in_iter) return GBIMS_ERR_ARG;
+  if (h->nm <= 0) return fail(h, GBIMS_ERR_STATE, "not a batch handle (gbims_batch_create)");
+  GB_CUDA(h, cudaMemcpyAsync(h->d_amat, amat, sizeof(double) * h->nja, cudaMemcpyHostToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_rhs, rhs, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_x, x, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  int rc = batch_apply_core(h, kstp, icnvg, in_iter, summaries);
+  if (rc < 0 && rc != GBIMS_ERR_NONFINITE) return rc;
+  cudaError_t e = cudaMemcpy(x, h->d_x, sizeof(double) * h->n, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(h, GBIMS_ERR_CUDA, cudaGetErrorString(e));
+  return rc;
+}
+
+extern "C" int gbims_batch_apply_device(gbims_handle *h, double *d_amat, double *d_rhs,
+                                        double *d_x, int kstp, int kiter, int *icnvg,
+                                        int *in_iter, gbims_summary *summaries) {
+  (void)kiter;
+  if (!h || !d_amat || !d_rhs || !d_x || !icnvg || !in_iter) return GBIMS_ERR_ARG;
+  if (h->nm <= 0) return fail(h, GBIMS_ERR_STATE, "not a batch handle (gbims_batch_create)");
+  GB_CUDA(h, cudaMemcpyAsync(h->d_amat, d_amat, sizeof(double) * h->nja, cudaMemcpyDeviceToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_rhs, d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_x, d_x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
+  int rc = batch_apply_core(h, kstp, icnvg, in_iter, summaries);
+  if (rc < 0 && rc != GBIMS_ERR_NONFINITE) return rc;
+  cudaError_t e = cudaMemcpyAsync(d_x, h->d_x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) return fail(h, GBIMS_ERR_CUDA, cudaGetErrorString(e));
+  return rc;
 }
 
 // Accessors used by the device-resident solution (gbsln_*): the solution

@@ -13,7 +13,7 @@ namespace gb {
 
 constexpr int kNumSM = 152;       // GB300: 2 dies x 76 SMs
 constexpr int kRedBlock = 256;    // threads per reduction block
-constexpr int kMaxRedBlocks = 2 * kNumSM * 2;  // grid of reduction kernels
+constexpr int kMaxRedBlocks = 8 * kNumSM;  // grid of reduction kernels: 8 x 256 threads per SM
 constexpr int kSell = 32;         // SELL slice height (one warp)
 constexpr int kMaxRowLen = 64;    // ILU0 factor: longest supported CSR row
 
@@ -42,7 +42,20 @@ struct Ctl {
   int nonfinite;
   int bodies;         // loop bodies executed in this solve
   int guard_tripped;  // the body limit ended the loop
+  int restart_due;    // mixed form: the pending true-residual check restarts the recurrence
 };
+
+// A batched ensemble on the device: members concatenated into one
+// block-diagonal system; rows cut into chunks that never straddle members.
+struct BatchDev {
+  int nm = 0, nchunks = 0;
+  const int *cm = nullptr;  // chunk -> member (nchunks)
+  const int *cr = nullptr;  // chunk -> first row (nchunks + 1)
+  const int *mc = nullptr;  // member -> first chunk (nm + 1)
+  const int *mr = nullptr;  // member -> first row (nm + 1)
+  Ctl *ctls = nullptr;      // one control block per member
+};
+constexpr int kChunkRows = 2048;  // rows per chunk (8 per thread of a 256-thread block)
 
 // Reduction partial layout: value slots per block.
 struct MaxLoc {
@@ -93,12 +106,27 @@ struct Levels {
   int maxwidth = 0;
 };
 
+// One full DIS grid ("member") of the wavefront layout.  A single model is
+// one member; a batched ensemble has one per model, laid end to end.
+struct Dia7Geo {
+  int nlay, nrow, ncol;
+  int nb, G;          // blocks of W lines per layer, padded steps per block
+  int ticket0;        // first CTA ticket (local ticket = b * nlay + k)
+  int ptile0;         // first 32 x 8 permute tile
+  long long slot0;    // first slot of the member's skewed tiles
+  long long row0;     // first row of the member in the natural-order vectors
+};
+
 // Structured 7-point DIS layout of the ILU0 factors for the wavefront sweeps:
 // per block of lines, G x W tiles (row = wavefront step, column = lane).
 struct Dia7 {
-  int nlay = 0, nrow = 0, ncol = 0;
-  int nb = 0, G = 0;       // blocks per layer, padded steps per block
-  long long slots = 0;     // nlay * nb * G * W elements per array
+  int nlay = 0, nrow = 0, ncol = 0;  // single model: its shape (index-free SpMV)
+  int nb = 0, G = 0;       // single model: blocks per layer, padded steps per block
+  long long slots = 0;     // total elements per skewed array (all members)
+  int nm = 0;              // members
+  std::vector<Dia7Geo> geo;
+  Dia7Geo *d_geo = nullptr;
+  int ntickets = 0, nptiles = 0;
   // forward tiles: lower coefficients (unit diagonal) z (layer above),
   // y (row behind), x (column left); backward tiles: dinv*U for z, y, x and
   // dinv; zero where the neighbour or the cell does not exist
@@ -108,6 +136,10 @@ struct Dia7 {
   float *f_lz = nullptr, *f_ly = nullptr, *f_lx = nullptr;
   float *f_ux = nullptr, *f_uy = nullptr, *f_uz = nullptr, *f_dinv = nullptr;
   float *f_rsk = nullptr, *f_ysk = nullptr, *f_zsk = nullptr;
+  // matrix values for the index-free SpMV: 7 slots of n (FP64; FP32 copy in
+  // the mixed form), slot order = CSR order of a row
+  double *d_sv = nullptr;
+  float *f_sv = nullptr;
   int *d_flags = nullptr;  // wavefront progress words, one per 128-byte line
   int nflags = 0;
   int *d_err = nullptr;    // wait-limit error flag
@@ -117,6 +149,10 @@ struct Dia7 {
 // aligned segments that can run past the last cell.
 constexpr int kVecPad = 256;
 void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, long long *slots);
+// Members (nlay, nrow, ncol) and their first rows -> D.geo, D.slots,
+// D.ntickets, D.nptiles (host side; the caller uploads D.geo to D.d_geo).
+void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long long> &row0,
+                 bool fp32);
 
 // ---------------------------------------------------------------------------
 // kernel launchers (implemented in the .cu files)
@@ -150,6 +186,23 @@ void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *c
                          cudaStream_t st);
 void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
                          cudaStream_t st);
+void launch_dia7_vfill(const Dia7 &D, const int *d_ia, const double *d_amat, cudaStream_t st);
+void launch_dia7_spmv64(const Dia7 &D, const double *x, double *y, const Ctl *ctl,
+                        cudaStream_t st);
+void launch_dia7_spmv32(const Dia7 &D, const float *x, float *y, const Ctl *ctl,
+                        cudaStream_t st);
+void launch_dia7_residual64(const Dia7 &D, const double *x, const double *b, double *d,
+                            const Ctl *ctl, int only_if_north_due, cudaStream_t st);
+
+// ims_base_scale (k_scale.cu): the column-major position map used by the
+// L2-norm column sums, the scaling before a solve (returns its kernel count)
+// and the unscaling of x after it.
+void scale_colmap_host(int n, const std::vector<int> &ia, const std::vector<int> &ja,
+                       std::vector<int> &cptr, std::vector<int> &cpos);
+int launch_scale(int iscl, int n, const int *ia, const int *ja, const int *cptr, const int *cpos,
+                 double *amat, double *x, double *b, double *dscale, double *dscale2,
+                 cudaStream_t st);
+void launch_unscale_x(int n, double *x, const double *dscale2, cudaStream_t st);
 
 // IMS handle internals shared with the device-resident solution.
 void ims_buffers(gbims_handle *h, double **amat, double **rhs, double **x);

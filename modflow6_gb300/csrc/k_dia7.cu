@@ -19,18 +19,23 @@
 // (g,l) is the cell lane l handles at step g; slots outside the grid hold
 // zero).  A chunk of C steps of one array is then one contiguous C*W tile.
 //
-// Three warps per CTA, so that no fence ever stalls the arithmetic:
-//  * warp 1 (copy) waits for the producer CTAs' progress words and stages the
-//    chunks into a ring of NS shared-memory buffers with TMA bulk copies
+// Four warps per CTA, so that no fence and no off-chain arithmetic ever
+// stalls the dependent chain:
+//  * copy: waits for the producer CTAs' progress words and stages the chunks
+//    into a ring of NS shared-memory buffers with TMA bulk copies
 //    (cp.async.bulk), one "full" mbarrier per buffer;
-//  * warp 0 (compute) waits on the full mbarrier, computes C steps, writes the
-//    C x W result tile to shared memory and sends it out with one bulk store,
-//    then frees the buffer through its "empty" mbarrier; it tracks its bulk
-//    stores with cp.async.bulk.wait_group and reports completed chunks in
-//    shared memory;
-//  * warp 2 (publish) turns completed chunks into this CTA's progress word:
-//    proxy fence, gpu-scope fence, store.  On GB300 a gpu-scope fence costs
-//    on the order of a microsecond, which is why it lives in a warp of its own.
+//  * pre-compute: once a buffer is full, folds the right-hand side and the
+//    layer-neighbour term (r - Lz*zn; backward dinv*y - Uz'*zn) into one
+//    tile and releases it through a "prep" mbarrier;
+//  * compute: per step one shuffle and the two FMAs of the row and column
+//    neighbours; writes the C x W result tile to a shared-memory ring and
+//    frees the buffer through its "empty" mbarrier;
+//  * store: sends finished result tiles out with bulk stores and publishes
+//    the CTA's progress word (bulk-store completion, proxy fence, gpu-scope
+//    fence, store).  On GB300 a gpu-scope fence costs on the order of a
+//    microsecond, which is why it lives in a warp of its own.
+// The roles rotate with the CTA's hardware warp slot so that compute warps
+// of co-resident CTAs land on different SM sub-partitions (FP64 pipes).
 // Every wait is bounded by the global timer; a wait that runs out sets an
 // error flag and Ctl::done, drains the copies in flight and returns.  CTAs
 // take a ticket in launch order and depend only on smaller tickets, so the
@@ -123,7 +128,8 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
 
 template <typename T>
 struct SweepArgs {
-  int nlay, nrow, ncol, nb, G;
+  const Dia7Geo *geo;  // members, in ticket order
+  int nm;
   const T *A, *B, *X, *D;  // skewed factors (forward: Lz Ly Lx -, backward: Uz' Uy' Ux' dinv)
   const T *rsk;            // forward: right-hand side, skewed
   T *ysk;                  // forward result, skewed (written forward, read backward)
@@ -137,42 +143,95 @@ struct Stage {
   T a[C * W], b[C * W], x[C * W], d[C * W], r[C * W], zn[C * W], yn[C * W];
 };
 
+// Warp roles of a sweep CTA.
+enum { kRoleCompute = 0, kRoleCopy = 1, kRoleStore = 2, kRolePre = 3 };
+
 // DIR = +1 forward, -1 backward.
 template <typename T, int W, int S, int C, int NS, int DIR>
-__global__ void __launch_bounds__(96) k_dia7_sweep(SweepArgs<T> p) {
+__global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Stage<T, W, C> *stg = reinterpret_cast<Stage<T, W, C> *>(smem_raw);
   T *outring = reinterpret_cast<T *>(smem_raw + NS * sizeof(Stage<T, W, C>));
   unsigned long long *full = reinterpret_cast<unsigned long long *>(
       smem_raw + NS * sizeof(Stage<T, W, C>) + kOut * C * W * sizeof(T));
   unsigned long long *empty = full + NS;
-  __shared__ int s_id, s_ready, s_freed, s_abort;
+  unsigned long long *prep = full + 2 * NS;
+  __shared__ int s_id, s_ready, s_freed, s_abort, s_rot, s_m;
   if (p.ctl && p.ctl->done) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     s_id = atomicAdd(&p.flags[0], 1);
+    // the member this ticket belongs to (members own contiguous tickets)
+    int lo = 0, hi = p.nm - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (p.geo[mid].ticket0 <= s_id) lo = mid;
+      else hi = mid - 1;
+    }
+    s_m = lo;
     s_ready = 0;
     s_freed = 0;
     s_abort = 0;
+    // Rotate the roles by the CTA's warp-slot group on the SM, so that the
+    // compute warps of co-resident CTAs sit on different SM sub-partitions
+    // (each has its own FP64 pipe) and apart from their own pre-compute warp.
+    unsigned hw;
+    asm volatile("mov.u32 %0, %%warpid;" : "=r"(hw));
+    s_rot = (int)((hw >> 2) & 3u);
     for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
+      mbar_init(&prep[s], 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  const int role = (warp + s_rot) & 3;
   const int id = s_id;
-  const int nlay = p.nlay, nrow = p.nrow, nb = p.nb, G = p.G;
-  const int k = (DIR > 0) ? id % nlay : nlay - 1 - (id % nlay);
-  const int b = (DIR > 0) ? id / nlay : nb - 1 - id / nlay;
+  const Dia7Geo geo = p.geo[s_m];
+  const int lid = id - geo.ticket0;
+  const int nlay = geo.nlay, nrow = geo.nrow, nb = geo.nb, G = geo.G;
+  const int k = (DIR > 0) ? lid % nlay : nlay - 1 - (lid % nlay);
+  const int b = (DIR > 0) ? lid / nlay : nb - 1 - lid / nlay;
   const int nch = G / C;
   const bool has_blk = (DIR > 0) ? (b > 0) : (b < nb - 1);
   const bool has_lay = (DIR > 0) ? (k > 0) : (k < nlay - 1);
   int *prog = p.flags + kFlagStride;
-  auto tile = [&](int kk, int bb) -> long long { return ((long long)kk * nb + bb) * G * W; };
+  const long long slot0 = geo.slot0;
+  auto tile = [&](int kk, int bb) -> long long { return slot0 + ((long long)kk * nb + bb) * G * W; };
   volatile int *v_abort = &s_abort;
 
-  if (warp == 2) {
+  if (role == kRolePre) {
+    // ---------------- pre-compute warp ----------------
+    // The terms of a step that do not depend on the wavefront: forward
+    // r - Lz*y(k-1), backward dinv*y - Uz'*z(k+1), in the same order and
+    // rounding as the full step.  Written over the stage's `a` tile (each
+    // element is read and written by one thread), released through the
+    // stage's prep mbarrier.
+    for (int c = 0; c < nch; ++c) {
+      const int s = c % NS;
+      const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort);
+      if (!__all_sync(0xffffffffu, got)) {
+        if (lane == 0) *v_abort = 1;
+        return;
+      }
+      Stage<T, W, C> &st = stg[s];
+#pragma unroll
+      for (int e = lane; e < C * W; e += 32) {
+        T t0 = (DIR > 0) ? st.r[e] : st.d[e] * st.r[C * W - 1 - e];
+        if (has_lay) t0 = fma(-st.a[e], st.zn[e], t0);
+        st.a[e] = t0;
+      }
+      // the buffer is refilled by the async proxy after the compute warp
+      // has released it: order these generic writes before that
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&prep[s]);
+    }
+    return;
+  }
+
+  if (role == kRoleStore) {
     // ---------------- store + publish warp ----------------
     // Takes every result tile the compute warp has finished, sends each out
     // with a bulk store, frees its slot once the store has read it, and then
@@ -220,7 +279,7 @@ __global__ void __launch_bounds__(96) k_dia7_sweep(SweepArgs<T> p) {
     return;
   }
 
-  if (warp == 1) {
+  if (role == kRoleCopy) {
     // ---------------- copy warp ----------------
     const int *pb = has_blk ? prog + (size_t)(id - nlay) * kFlagStride : nullptr;
     const int *pu = has_lay ? prog + (size_t)(id - 1) * kFlagStride : nullptr;
@@ -255,7 +314,7 @@ __global__ void __launch_bounds__(96) k_dia7_sweep(SweepArgs<T> p) {
         const int yrows = has_blk ? max(0, min(C, G - yrow0)) : 0;
         int plo = 0, prows = 0, pskip = 0;
         if (DIR < 0) {  // own forward result, rows P descending
-          const int phi = p.ncol - 1 + S * (W - 1) - g0;
+          const int phi = geo.ncol - 1 + S * (W - 1) - g0;
           const int pl = phi - (C - 1);
           const int lo = max(pl, 0), hi = min(phi, G - 1);
           plo = lo;
@@ -305,17 +364,15 @@ __global__ void __launch_bounds__(96) k_dia7_sweep(SweepArgs<T> p) {
   const int i = (DIR > 0) ? (b * W + lane) : (b * W + (W - 1 - lane));
   const bool line_ok = lane < W && i >= 0 && i < nrow;
   const bool has_y = line_ok && ((DIR > 0) ? (i > 0) : (i + 1 < nrow));
-  const int ncol = p.ncol;
+  const int ncol = geo.ncol;
   const int l = lane < W ? lane : 0;
   T h1 = T(0), h2 = T(0);
   for (int c = 0; c < nch; ++c) {
     const int s = c % NS;
-    const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort);
+    const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort) &&
+                     mbar_wait(&prep[s], (c / NS) & 1, v_abort);
     if (!__all_sync(0xffffffffu, got)) {
-      if (lane == 0) {
-        *v_abort = 1;
-        asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-      }
+      if (lane == 0) *v_abort = 1;
       return;
     }
     const Stage<T, W, C> &st = stg[s];
@@ -341,10 +398,7 @@ __global__ void __launch_bounds__(96) k_dia7_sweep(SweepArgs<T> p) {
       if (lane == 0) yv = st.yn[t * W + (W - 1)];
       const int jj = jc + t;
       const bool v = line_ok && (unsigned)jj < (unsigned)ncol;
-      T tv;
-      if (DIR > 0) tv = st.r[t * W + l];
-      else tv = st.d[t * W + l] * st.r[(C - 1 - t) * W + (W - 1 - l)];
-      if (has_lay) tv = fma(-st.a[t * W + l], st.zn[t * W + l], tv);
+      T tv = st.a[t * W + l];  // pre-computed r - Lz*zn (backward: dinv*y - Uz'*zn)
       if (has_y) tv = fma(-st.b[t * W + l], yv, tv);
       if (jj > 0) tv = fma(-st.x[t * W + l], h1, tv);
       if (!v) tv = T(0);
@@ -366,18 +420,30 @@ __global__ void __launch_bounds__(96) k_dia7_sweep(SweepArgs<T> p) {
 // A 32 x 8 thread block covers 32 columns of 8 lines: the natural-order side
 // is whole rows, and the skewed side falls in a few rows of one tile.
 template <typename T, int W, int S, int DIR>
-__global__ void k_dia7_permute(int nrow, int ncol, int nb, int G, const T *__restrict__ src,
+__global__ void k_dia7_permute(const Dia7Geo *__restrict__ geos, int nm, const T *__restrict__ src,
                                T *__restrict__ dst, const Ctl *__restrict__ ctl) {
   if (ctl && ctl->done) return;
-  const int j = blockIdx.x * 32 + threadIdx.x;
-  const int i = blockIdx.y * 8 + threadIdx.y;
-  const int k = blockIdx.z;
-  if (j >= ncol || i >= nrow) return;
+  // member of this 32 x 8 tile
+  const int t = blockIdx.x;
+  int lo = 0, hi = nm - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (geos[mid].ptile0 <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const Dia7Geo g = geos[lo];
+  const int tx = (g.ncol + 31) / 32, ty = (g.nrow + 7) / 8;
+  const int lt = t - g.ptile0;
+  const int k = lt / (tx * ty);
+  const int rem = lt - k * tx * ty;
+  const int j = (rem % tx) * 32 + threadIdx.x;
+  const int i = (rem / tx) * 8 + threadIdx.y;
+  if (j >= g.ncol || i >= g.nrow) return;
   const int b = i / W;
   const int l = (DIR > 0) ? (i - b * W) : (W - 1 - (i - b * W));
-  const int g = ((DIR > 0) ? j : (ncol - 1 - j)) + S * l;
-  const long long sk = (((long long)k * nb + b) * G + g) * W + l;
-  const long long nat = ((long long)k * nrow + i) * ncol + j;
+  const int gg = ((DIR > 0) ? j : (g.ncol - 1 - j)) + S * l;
+  const long long sk = g.slot0 + (((long long)k * g.nb + b) * g.G + gg) * W + l;
+  const long long nat = g.row0 + ((long long)k * g.nrow + i) * g.ncol + j;
   if (DIR > 0) dst[sk] = src[nat];  // skew (forward input)
   else dst[nat] = src[sk];          // unskew (backward output)
 }
@@ -386,36 +452,44 @@ __global__ void k_dia7_permute(int nrow, int ncol, int nb, int G, const T *__res
 // lane l visits at step g; backward tiles hold dinv*Uz, dinv*Uy, dinv*Ux and
 // dinv.  Slots outside the grid are zero.
 template <typename T>
-__global__ void k_dia7_extract(int nlay, int nrow, int ncol, int nb, int G, int W, int S, int dir,
-                               const int *__restrict__ iapc, const int *__restrict__ japc,
-                               const double *__restrict__ apc, T *A, T *B, T *X, T *D) {
-  const long long nslot = (long long)nlay * nb * G * W;
-  const long long nrc = (long long)nrow * ncol;
+__global__ void k_dia7_extract(const Dia7Geo *__restrict__ geos, int nm, long long nslot, int W,
+                               int S, int dir, const int *__restrict__ iapc,
+                               const int *__restrict__ japc, const double *__restrict__ apc,
+                               T *A, T *B, T *X, T *D) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nslot;
        q += (long long)gridDim.x * blockDim.x) {
-    const int l = (int)(q % W);
-    const long long r1 = q / W;
-    const int g = (int)(r1 % G);
-    const long long kb = r1 / G;
-    const int b = (int)(kb % nb), k = (int)(kb / nb);
-    const int jj = g - S * l;
+    int lo = 0, hi = nm - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (geos[mid].slot0 <= q) lo = mid;
+      else hi = mid - 1;
+    }
+    const Dia7Geo g = geos[lo];
+    const long long lq = q - g.slot0;
+    const long long nrc = (long long)g.nrow * g.ncol;
+    const int l = (int)(lq % W);
+    const long long r1 = lq / W;
+    const int gg = (int)(r1 % g.G);
+    const long long kb = r1 / g.G;
+    const int b = (int)(kb % g.nb), k = (int)(kb / g.nb);
+    const int jj = gg - S * l;
     const int i = (dir > 0) ? b * W + l : b * W + (W - 1 - l);
     double va = 0, vb = 0, vx = 0, vd = 0;
-    if (i < nrow && jj >= 0 && jj < ncol) {
-      const int j = (dir > 0) ? jj : ncol - 1 - jj;
-      const long long n = k * nrc + (long long)i * ncol + j;
+    if (i < g.nrow && jj >= 0 && jj < g.ncol) {
+      const int j = (dir > 0) ? jj : g.ncol - 1 - jj;
+      const long long n = g.row0 + k * nrc + (long long)i * g.ncol + j;
       const double d = apc[n];
       for (int pp = iapc[n]; pp < iapc[n + 1]; ++pp) {
         const long long c = japc[pp];
         const double a = apc[pp];
         if (dir > 0) {
           if (k > 0 && c == n - nrc) va = a;
-          else if (i > 0 && c == n - ncol) vb = a;
+          else if (i > 0 && c == n - g.ncol) vb = a;
           else if (j > 0 && c == n - 1) vx = a;
         } else {
-          if (k < nlay - 1 && c == n + nrc) va = d * a;
-          else if (i < nrow - 1 && c == n + ncol) vb = d * a;
-          else if (j < ncol - 1 && c == n + 1) vx = d * a;
+          if (k < g.nlay - 1 && c == n + nrc) va = d * a;
+          else if (i < g.nrow - 1 && c == n + g.ncol) vb = d * a;
+          else if (j < g.ncol - 1 && c == n + 1) vx = d * a;
         }
       }
       vd = d;
@@ -440,7 +514,7 @@ template <typename T>
 constexpr size_t stage_bytes() {
   using P = Shape<T>;
   return P::NS * sizeof(Stage<T, P::W, P::C>) + kOut * P::C * P::W * sizeof(T) +
-         2 * P::NS * sizeof(unsigned long long);
+         3 * P::NS * sizeof(unsigned long long);
 }
 static_assert(stage_bytes<double>() < 48 * 1024, "FP64 stage ring too large");
 static_assert(stage_bytes<float>() < 48 * 1024, "FP32 stage ring too large");
@@ -481,16 +555,49 @@ void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, lon
   *slots = (long long)nlay * (*nb) * (*G) * W;
 }
 
+void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long long> &row0,
+                 bool fp32) {
+  D.nm = (int)row0.size();
+  D.geo.resize(D.nm);
+  long long slots = 0;
+  int tickets = 0, ptiles = 0;
+  for (int m = 0; m < D.nm; ++m) {
+    Dia7Geo &g = D.geo[m];
+    g.nlay = shapes[3 * m];
+    g.nrow = shapes[3 * m + 1];
+    g.ncol = shapes[3 * m + 2];
+    long long ms = 0;
+    dia7_geometry(g.nlay, g.nrow, g.ncol, fp32, &g.nb, &g.G, &ms);
+    g.ticket0 = tickets;
+    g.ptile0 = ptiles;
+    g.slot0 = slots;
+    g.row0 = row0[m];
+    tickets += g.nlay * g.nb;
+    ptiles += g.nlay * ((g.ncol + 31) / 32) * ((g.nrow + 7) / 8);
+    slots += ms;  // a multiple of C*W elements: every member starts 16-byte aligned
+  }
+  D.slots = slots;
+  D.ntickets = tickets;
+  D.nptiles = ptiles;
+  if (D.nm == 1) {
+    D.nlay = D.geo[0].nlay;
+    D.nrow = D.geo[0].nrow;
+    D.ncol = D.geo[0].ncol;
+    D.nb = D.geo[0].nb;
+    D.G = D.geo[0].G;
+  }
+}
+
 template <typename T>
 static void extract_t(const Dia7 &D, const int *d_iapc, const int *d_japc, const double *d_apc,
                       T *const *arr, cudaStream_t st) {
   using P = Shape<T>;
-  long long nslot = (long long)D.nlay * D.nb * D.G * P::W;
+  const long long nslot = D.slots;
   int grid = (int)std::min<long long>((nslot + 255) / 256, 8LL * kNumSM);
-  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.nb, D.G, P::W, P::S, 1, d_iapc,
-                                          d_japc, d_apc, arr[0], arr[1], arr[2], nullptr);
-  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.nb, D.G, P::W, P::S, -1, d_iapc,
-                                          d_japc, d_apc, arr[3], arr[4], arr[5], arr[6]);
+  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.d_geo, D.nm, nslot, P::W, P::S, 1, d_iapc, d_japc,
+                                          d_apc, arr[0], arr[1], arr[2], nullptr);
+  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.d_geo, D.nm, nslot, P::W, P::S, -1, d_iapc, d_japc,
+                                          d_apc, arr[3], arr[4], arr[5], arr[6]);
 }
 
 void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_japc,
@@ -511,22 +618,23 @@ template <typename T>
 static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, T *ysk, T *zsk, const T *r, T *z,
                     const Ctl *ctl, cudaStream_t st) {
   using P = Shape<T>;
-  const int nct = D.nb * D.nlay;
+  const int nct = D.ntickets;
   const size_t fbytes = sizeof(int) * (size_t)(nct + 1) * kFlagStride;
   constexpr size_t sm = stage_bytes<T>();
-  const dim3 pb(32, 8), pg((D.ncol + 31) / 32, (D.nrow + 7) / 8, D.nlay);
+  const dim3 pb(32, 8);
   SweepArgs<T> a;
-  a.nlay = D.nlay; a.nrow = D.nrow; a.ncol = D.ncol; a.nb = D.nb; a.G = D.G;
+  a.geo = D.d_geo;
+  a.nm = D.nm;
   a.rsk = rsk; a.ysk = ysk; a.zsk = zsk;
   a.flags = D.d_flags; a.err = D.d_err; a.ctl = const_cast<Ctl *>(ctl);
   a.A = arr[0]; a.B = arr[1]; a.X = arr[2]; a.D = nullptr;
-  k_dia7_permute<T, P::W, P::S, 1><<<pg, pb, 0, st>>>(D.nrow, D.ncol, D.nb, D.G, r, rsk, ctl);
+  k_dia7_permute<T, P::W, P::S, 1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, r, rsk, ctl);
   cudaMemsetAsync(D.d_flags, 0, fbytes, st);
-  k_dia7_sweep<T, P::W, P::S, P::C, P::NS, 1><<<nct, 96, sm, st>>>(a);
+  k_dia7_sweep<T, P::W, P::S, P::C, P::NS, 1><<<nct, 128, sm, st>>>(a);
   a.A = arr[3]; a.B = arr[4]; a.X = arr[5]; a.D = arr[6];
   cudaMemsetAsync(D.d_flags, 0, fbytes, st);
-  k_dia7_sweep<T, P::W, P::S, P::C, P::NS, -1><<<nct, 96, sm, st>>>(a);
-  k_dia7_permute<T, P::W, P::S, -1><<<pg, pb, 0, st>>>(D.nrow, D.ncol, D.nb, D.G, zsk, z, ctl);
+  k_dia7_sweep<T, P::W, P::S, P::C, P::NS, -1><<<nct, 128, sm, st>>>(a);
+  k_dia7_permute<T, P::W, P::S, -1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, zsk, z, ctl);
 }
 
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,

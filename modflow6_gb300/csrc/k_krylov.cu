@@ -99,8 +99,17 @@ __global__ void __launch_bounds__(kRedBlock) k_dot(int n, const TA *__restrict__
                                                     const Ctl *__restrict__ ctl) {
   if (ctl->done) return;
   double v[1] = {0.0};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    v[0] = fma(to_d(a[i]), to_d(b[i]), v[0]);
+  // two rows per trip, loads first: the same summation order as one row per
+  // trip, with twice the loads in flight
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    const double a0 = to_d(a[i]), b0 = to_d(b[i]);
+    const double a1 = to_d(a[i + stride]), b1 = to_d(b[i + stride]);
+    v[0] = fma(a0, b0, v[0]);
+    v[0] = fma(a1, b1, v[0]);
+  }
+  if (i < n) v[0] = fma(to_d(a[i]), to_d(b[i]), v[0]);
   block_sum<1>(v);
   if (threadIdx.x == 0) part[blockIdx.x] = v[0];
 }
@@ -205,7 +214,7 @@ __device__ __forceinline__ void set_loop(Ctl *ctl, unsigned long long cond, int 
 // ---------------------------------------------------------------------------
 // PCG
 // ---------------------------------------------------------------------------
-__global__ void k_ctl_cg_rho(Ctl *ctl, const double *part, int G) {
+__device__ void ctl_cg_rho(Ctl *ctl, const double *part, int G) {
   if (ctl->done) return;
   double s = ctl_reduce_sum(part, G);
   if (threadIdx.x == 0) {
@@ -213,14 +222,20 @@ __global__ void k_ctl_cg_rho(Ctl *ctl, const double *part, int G) {
     ctl->beta = ctl->first ? 0.0 : s / ctl->rho0;
   }
 }
+__global__ void k_ctl_cg_rho(Ctl *ctl, const double *part, int G) {
+  ctl_cg_rho(ctl, part, G);
+}
 
-__global__ void k_ctl_alpha(Ctl *ctl, const double *part, int G) {
+__device__ void ctl_alpha(Ctl *ctl, const double *part, int G) {
   if (ctl->done) return;
   double s = ctl_reduce_sum(part, G);
   if (threadIdx.x == 0) {
     double den = s + sign_dprec(s);
     ctl->alpha = ctl->rho / den;
   }
+}
+__global__ void k_ctl_alpha(Ctl *ctl, const double *part, int G) {
+  ctl_alpha(ctl, part, G);
 }
 
 template <typename T>
@@ -264,16 +279,27 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__rest
   double v[2] = {0.0, 0.0};
   MaxLoc m[2];
   m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double tv = alpha * p[i];
-    x[i] = x[i] + tv;
+  auto row = [&](int i, double pi, double xi, double qi, double dI) {
+    double tv = alpha * pi;
+    x[i] = xi + tv;
     if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i; }
-    double di = fma(-alpha, q[i], d[i]);
+    double di = fma(-alpha, qi, dI);
     d[i] = di;
     if (absgt(di, m[1].val)) { m[1].val = di; m[1].idx = i; }
     v[0] = fma(di, di, v[0]);
     if (!isfinite(di) || !isfinite(tv)) v[1] += 1.0;
+  };
+  // two rows per trip, loads first (same order of rows as one per trip)
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    const int j = i + stride;
+    const double p0 = p[i], x0 = x[i], q0 = q[i], d0 = d[i];
+    const double p1 = p[j], x1 = x[j], q1 = q[j], d1 = d[j];
+    row(i, p0, x0, q0, d0);
+    row(j, p1, x1, q1, d1);
   }
+  if (i < n) row(i, p[i], x[i], q[i], d[i]);
   block_sum<2>(v);
   block_maxloc<2>(m);
   if (threadIdx.x == 0) {
@@ -298,17 +324,29 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update_mixed(int n, double *__
   double v[2] = {0.0, 0.0};
   MaxLoc m[2];
   m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double tv = alpha * (double)p[i];
-    x[i] = x[i] + tv;
+  auto row = [&](int i, float pi, double xi, float qi, float dI) {
+    double tv = alpha * (double)pi;
+    x[i] = xi + tv;
     if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i; }
-    float di = fmaf(-alphaf, q[i], d[i]);
+    float di = fmaf(-alphaf, qi, dI);
     d[i] = di;
     double dd = (double)di;
     if (absgt(dd, m[1].val)) { m[1].val = dd; m[1].idx = i; }
     v[0] = fma(dd, dd, v[0]);
     if (!isfinite(di) || !isfinite(tv)) v[1] += 1.0;
+  };
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    const int j = i + stride;
+    const float p0 = p[i], q0 = q[i], d0 = d[i];
+    const double x0 = x[i];
+    const float p1 = p[j], q1 = q[j], d1 = d[j];
+    const double x1 = x[j];
+    row(i, p0, x0, q0, d0);
+    row(j, p1, x1, q1, d1);
   }
+  if (i < n) row(i, p[i], x[i], q[i], d[i]);
   block_sum<2>(v);
   block_maxloc<2>(m);
   if (threadIdx.x == 0) {
@@ -337,7 +375,7 @@ __device__ void ctl_finish_update(Ctl *ctl, const double *part, int G) {
 }
 
 // End of a PCG iteration: closure test and loop control (ImsLinearBase.f90:196-236).
-__global__ void k_ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond,
+__device__ void ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond,
                               int use_cond) {
   if (ctl->done) {
     if (threadIdx.x == 0) set_loop(ctl, cond, use_cond);
@@ -380,17 +418,24 @@ __global__ void k_ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long
   if (ctl->done && ctl->icnvg < 0) ctl->icnvg = 0;
   set_loop(ctl, cond, use_cond);
 }
+__global__ void k_ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond,
+                              int use_cond) {
+  ctl_cg_cnvg(ctl, part, G, cond, use_cond);
+}
 
 // ---------------------------------------------------------------------------
 // BiCGSTAB
 // ---------------------------------------------------------------------------
-__global__ void k_ctl_bcgs_rho(Ctl *ctl, const double *part, int G) {
+__device__ void ctl_bcgs_rho(Ctl *ctl, const double *part, int G) {
   if (ctl->done) return;
   double s = ctl_reduce_sum(part, G);
   if (threadIdx.x == 0) {
     ctl->rho = s;
     if (!ctl->first) ctl->beta = (s / ctl->rho0) * (ctl->alpha0 / ctl->omega0);
   }
+}
+__global__ void k_ctl_bcgs_rho(Ctl *ctl, const double *part, int G) {
+  ctl_bcgs_rho(ctl, part, G);
 }
 
 template <typename T>
@@ -418,7 +463,7 @@ __global__ void __launch_bounds__(256) k_bcgs_q(int n, const T *__restrict__ d, 
   q[i] = fma(-(T)ctl->alpha, v[i], d[i]);
 }
 
-__global__ void k_ctl_omega(Ctl *ctl, const double *part, int G) {
+__device__ void ctl_omega(Ctl *ctl, const double *part, int G) {
   if (ctl->done) return;
   double num = ctl_reduce_sum(part, G);
   double den = ctl_reduce_sum(part + G, G);
@@ -426,6 +471,9 @@ __global__ void k_ctl_omega(Ctl *ctl, const double *part, int G) {
     den = den + sign_dprec(den);
     ctl->omega = num / den;
   }
+}
+__global__ void k_ctl_omega(Ctl *ctl, const double *part, int G) {
+  ctl_omega(ctl, part, G);
 }
 
 // x += alpha*phat + omega*qhat ; d = q - omega*t (ImsLinearBase.f90:428-480).
@@ -470,7 +518,7 @@ __global__ void __launch_bounds__(kRedBlock) k_bcgs_update(int n, double *__rest
 }
 
 // End of a BiCGSTAB iteration (ImsLinearBase.f90:498-545).
-__global__ void k_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond,
+__device__ void ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond,
                                 int use_cond) {
   if (ctl->done) {
     if (threadIdx.x == 0) set_loop(ctl, cond, use_cond);
@@ -516,6 +564,10 @@ __global__ void k_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned lo
   if (ctl->done && ctl->icnvg < 0) ctl->icnvg = 0;
   set_loop(ctl, cond, use_cond);
 }
+__global__ void k_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond,
+                                int use_cond) {
+  ctl_bcgs_cnvg(ctl, part, G, cond, use_cond);
+}
 
 // ---------------------------------------------------------------------------
 // Mixed precision: FP64 iterative refinement around the FP32 inner loop
@@ -525,7 +577,7 @@ __global__ void k_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned lo
 // residual; when it passes, or the recursive residual has dropped by
 // refine_factor since the last refinement, the next true-residual check is
 // requested (Ctl::north_due = 2) instead of stopping.
-__global__ void k_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
+__device__ void ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
                                   double refine_factor) {
   if (ctl->done) return;
   ctl_finish_update(ctl, part, G);
@@ -547,6 +599,11 @@ __global__ void k_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
   }
   if (icnvg != 0 || ctl->l2norm <= refine_factor * ctl->scratch[0] || stag || zero) {
     ctl->north_due = 2;  // request the FP64 true residual
+    // Every refinement restarts the recurrence from the true residual: with
+    // FP32 search directions, continuing after a residual replacement costs
+    // more iterations than a restart (measured on the 10M-cell case)
+    (void)bcgs;
+    ctl->restart_due = 1;
     ctl->scratch[1] = ctl->deltax;
     ctl->scratch[2] = (double)ctl->xloc;
   }
@@ -556,6 +613,7 @@ __global__ void k_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
   if (ctl->north_due != 2) {
     if (ctl->iter >= ctl->itmax) {
       ctl->north_due = 2;  // final true-residual check at the iteration limit
+      ctl->restart_due = 0;
       ctl->scratch[1] = ctl->deltax;
       ctl->scratch[2] = (double)ctl->xloc;
     } else {
@@ -564,12 +622,17 @@ __global__ void k_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
     }
   }
 }
+__global__ void k_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
+                                  double refine_factor) {
+  ctl_mixed_inner(ctl, part, G, bcgs, refine_factor);
+}
 
 // True residual r = b - A x in FP64 with its max|r| and L2, only when
 // requested; the FP32 residual is reset from it.
 __global__ void __launch_bounds__(kRedBlock) k_true_resid_stats(int n, const double *__restrict__ r,
                                                                  float *__restrict__ d32,
                                                                  float *__restrict__ dhat32,
+                                                                 const double *__restrict__ dscale,
                                                                  double *__restrict__ part,
                                                                  const Ctl *__restrict__ ctl) {
   if (ctl->done || ctl->north_due != 2) return;
@@ -579,7 +642,8 @@ __global__ void __launch_bounds__(kRedBlock) k_true_resid_stats(int n, const dou
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double ri = r[i];
     d32[i] = (float)ri;
-    if (dhat32) dhat32[i] = (float)ri;  // BiCGSTAB shadow residual restarts too
+    if (dhat32 && ctl->restart_due) dhat32[i] = (float)ri;  // BiCGSTAB shadow, on a restart
+    if (dscale) ri = ri / dscale[i];    // BiCGSTAB reports the unscaled residual
     if (absgt(ri, m[1].val)) { m[1].val = ri; m[1].idx = i; }
     v[0] = fma(ri, ri, v[0]);
     if (!isfinite(ri)) v[1] += 1.0;
@@ -596,7 +660,7 @@ __global__ void __launch_bounds__(kRedBlock) k_true_resid_stats(int n, const dou
 }
 
 // Closure test on the FP64 true residual; restart the inner loop if needed.
-__global__ void k_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond,
+__device__ void ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond,
                              int use_cond) {
   if (ctl->done || ctl->north_due != 2) {
     if (threadIdx.x == 0) set_loop(ctl, cond, use_cond);
@@ -626,16 +690,27 @@ __global__ void k_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long 
     ctl->done = 1;
     ctl->exit_reason = kExitItmax;
   } else {
-    // restart the inner Krylov recurrence from the true residual
+    // The FP32 recurrence residual is replaced by the FP64 true residual and
+    // the recurrence restarts from it (restart_due); a recurrence that
+    // carried on instead, like the reference's NORTH residual refresh
+    // (ImsLinearBase.f90:221-227), would keep its search direction.
     ctl->scratch[0] = ctl->l2norm;
     ctl->scratch[3] += 1.0;  // refinement count
-    ctl->first = 1;
-    ctl->rho0 = 0.0;
-    ctl->alpha0 = 0.0;
-    ctl->omega0 = 0.0;
+    if (ctl->restart_due) {
+      ctl->first = 1;
+      ctl->rho0 = 0.0;
+      ctl->alpha0 = 0.0;
+      ctl->omega0 = 0.0;
+    } else {
+      ctl->first = 0;
+    }
     ctl->iter += 1;
   }
   set_loop(ctl, cond, use_cond);
+}
+__global__ void k_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond,
+                             int use_cond) {
+  ctl_refine(ctl, part, G, cond, use_cond);
 }
 
 // ---------------------------------------------------------------------------
@@ -646,7 +721,7 @@ __global__ void k_convert(int n, const TS *__restrict__ s, TD *__restrict__ d) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) d[i] = (TD)s[i];
 }
 
-__global__ void k_ctl_set_l2norm0(Ctl *ctl, const double *part, int G) {
+__device__ void ctl_set_l2norm0(Ctl *ctl, const double *part, int G) {
   double s = ctl_reduce_sum(part, G);
   if (threadIdx.x == 0) {
     ctl->l2norm0 = sqrt(s);
@@ -662,6 +737,141 @@ __global__ void k_ctl_set_l2norm0(Ctl *ctl, const double *part, int G) {
       ctl->nonfinite = 1;
       ctl->done = 1;
     }
+  }
+}
+__global__ void k_ctl_set_l2norm0(Ctl *ctl, const double *part, int G) {
+  ctl_set_l2norm0(ctl, part, G);
+}
+
+// ---------------------------------------------------------------------------
+// Batched ensemble: independent systems ("members") concatenated into one
+// block-diagonal system and iterated in lockstep.  Rows are cut into chunks
+// that never straddle two members; one chunk is one block of the vector
+// kernels and owns one reduction partial per slot.  Member m's partials are
+// laid out like a single solve's (slot k of its b-th chunk at
+// part[8*mc[m] + k*Gm + b], Gm = its chunk count), so the per-member control
+// logic is exactly the single-solve code above, run by block m.  A member
+// whose Ctl is done skips all of its chunks; the loop ends when every member
+// is done.
+// ---------------------------------------------------------------------------
+struct ChunkRef {
+  int m, b, G, r0, r1;
+};
+
+__device__ __forceinline__ ChunkRef chunk_of(const BatchDev &B, int c) {
+  ChunkRef r;
+  r.m = B.cm[c];
+  const int c0 = B.mc[r.m];
+  r.b = c - c0;
+  r.G = B.mc[r.m + 1] - c0;
+  r.r0 = B.cr[c];
+  r.r1 = B.cr[c + 1];
+  return r;
+}
+
+__device__ __forceinline__ double *member_part(double *part, const BatchDev &B, int m) {
+  return part + 8LL * B.mc[m];
+}
+
+template <typename TA, typename TB>
+__global__ void __launch_bounds__(kRedBlock) k_b_dot(BatchDev B, const TA *__restrict__ a,
+                                                     const TB *__restrict__ b,
+                                                     double *__restrict__ part) {
+  const ChunkRef c = chunk_of(B, blockIdx.x);
+  if (B.ctls[c.m].done) return;
+  double v[1] = {0.0};
+  for (int i = c.r0 + threadIdx.x; i < c.r1; i += blockDim.x) v[0] = fma(to_d(a[i]), to_d(b[i]), v[0]);
+  block_sum<1>(v);
+  if (threadIdx.x == 0) member_part(part, B, c.m)[c.b] = v[0];
+}
+
+__global__ void __launch_bounds__(kRedBlock) k_b_sumsq(BatchDev B, const double *__restrict__ a,
+                                                       double *__restrict__ part) {
+  const ChunkRef c = chunk_of(B, blockIdx.x);
+  double v[1] = {0.0};
+  for (int i = c.r0 + threadIdx.x; i < c.r1; i += blockDim.x) v[0] = fma(a[i], a[i], v[0]);
+  block_sum<1>(v);
+  if (threadIdx.x == 0) member_part(part, B, c.m)[c.b] = v[0];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRedBlock) k_b_cg_pupdate(BatchDev B, const T *__restrict__ z,
+                                                            T *__restrict__ p) {
+  const ChunkRef c = chunk_of(B, blockIdx.x);
+  const Ctl &ctl = B.ctls[c.m];
+  if (ctl.done) return;
+  const bool first = ctl.first;
+  const double beta = ctl.beta;
+  for (int i = c.r0 + threadIdx.x; i < c.r1; i += blockDim.x)
+    p[i] = first ? z[i] : (T)fma((double)(T)beta, (double)p[i], (double)z[i]);
+}
+
+// x += alpha*p ; d -= alpha*q with the same partial slots as k_cg_update64.
+__global__ void __launch_bounds__(kRedBlock) k_b_cg_update64(BatchDev B, double *__restrict__ x,
+                                                             double *__restrict__ d,
+                                                             const double *__restrict__ p,
+                                                             const double *__restrict__ q,
+                                                             double *__restrict__ part) {
+  const ChunkRef c = chunk_of(B, blockIdx.x);
+  const Ctl &ctl = B.ctls[c.m];
+  if (ctl.done) return;
+  const double alpha = ctl.alpha;
+  double v[2] = {0.0, 0.0};
+  MaxLoc m[2];
+  m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
+  const int row0 = B.mr[c.m];  // member-local row numbers for the maxima
+  for (int i = c.r0 + threadIdx.x; i < c.r1; i += blockDim.x) {
+    double tv = alpha * p[i];
+    x[i] = x[i] + tv;
+    if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i - row0; }
+    double di = fma(-alpha, q[i], d[i]);
+    d[i] = di;
+    if (absgt(di, m[1].val)) { m[1].val = di; m[1].idx = i - row0; }
+    v[0] = fma(di, di, v[0]);
+    if (!isfinite(di) || !isfinite(tv)) v[1] += 1.0;
+  }
+  block_sum<2>(v);
+  block_maxloc<2>(m);
+  if (threadIdx.x == 0) {
+    double *pm = member_part(part, B, c.m);
+    const int G = c.G, b = c.b;
+    pm[b] = v[0];
+    pm[G + b] = m[0].val; pm[2 * G + b] = (double)m[0].idx;
+    pm[3 * G + b] = m[1].val; pm[4 * G + b] = (double)m[1].idx;
+    pm[5 * G + b] = v[1];
+  }
+}
+
+__global__ void k_b_ctl_set_l2norm0(BatchDev B, const double *part) {
+  const int m = blockIdx.x;
+  ctl_set_l2norm0(B.ctls + m, part + 8LL * B.mc[m], B.mc[m + 1] - B.mc[m]);
+}
+__global__ void k_b_ctl_cg_rho(BatchDev B, const double *part) {
+  const int m = blockIdx.x;
+  ctl_cg_rho(B.ctls + m, part + 8LL * B.mc[m], B.mc[m + 1] - B.mc[m]);
+}
+__global__ void k_b_ctl_alpha(BatchDev B, const double *part) {
+  const int m = blockIdx.x;
+  ctl_alpha(B.ctls + m, part + 8LL * B.mc[m], B.mc[m + 1] - B.mc[m]);
+}
+__global__ void k_b_ctl_cg_cnvg(BatchDev B, const double *part) {
+  const int m = blockIdx.x;
+  ctl_cg_cnvg(B.ctls + m, part + 8LL * B.mc[m], B.mc[m + 1] - B.mc[m], 0ULL, 0);
+}
+
+// The batch's own control block gets done = every member done; it gates the
+// shared kernels (SpMV, preconditioner) and drives the WHILE condition.
+__global__ void k_b_all_done(BatchDev B, Ctl *gctl, unsigned long long cond, int use_cond,
+                            int count_body) {
+  __shared__ int s_any;
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  for (int m = threadIdx.x; m < B.nm; m += blockDim.x)
+    if (!B.ctls[m].done) atomicOr(&s_any, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (!s_any) gctl->done = 1;
+    if (count_body) set_loop(gctl, cond, use_cond);
   }
 }
 
@@ -748,9 +958,9 @@ void kr_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs, double re
                         cudaStream_t st) {
   k_ctl_mixed_inner<<<1, kRedBlock, 0, st>>>(ctl, part, G, bcgs, refine_factor);
 }
-void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, double *part, int G,
-                         const Ctl *ctl, cudaStream_t st) {
-  k_true_resid_stats<<<G, kRedBlock, 0, st>>>(n, r, d32, dhat32, part, ctl);
+void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, const double *dscale,
+                         double *part, int G, const Ctl *ctl, cudaStream_t st) {
+  k_true_resid_stats<<<G, kRedBlock, 0, st>>>(n, r, d32, dhat32, dscale, part, ctl);
 }
 void kr_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
                    cudaStream_t st) {
@@ -761,6 +971,38 @@ void kr_f64_to_f32(int n, const double *s, float *d, cudaStream_t st) {
 }
 void kr_f32_to_f64(int n, const float *s, double *d, cudaStream_t st) {
   k_convert<double, float><<<std::min(egrid(n), 4 * kNumSM), 256, 0, st>>>(n, s, d);
+}
+
+
+// batched ensemble launchers
+void kb_dot64(const BatchDev &B, const double *a, const double *b, double *part, cudaStream_t st) {
+  k_b_dot<double, double><<<B.nchunks, kRedBlock, 0, st>>>(B, a, b, part);
+}
+void kb_sumsq64(const BatchDev &B, const double *a, double *part, cudaStream_t st) {
+  k_b_sumsq<<<B.nchunks, kRedBlock, 0, st>>>(B, a, part);
+}
+void kb_cg_pupdate64(const BatchDev &B, const double *z, double *p, cudaStream_t st) {
+  k_b_cg_pupdate<double><<<B.nchunks, kRedBlock, 0, st>>>(B, z, p);
+}
+void kb_cg_update64(const BatchDev &B, double *x, double *d, const double *p, const double *q,
+                    double *part, cudaStream_t st) {
+  k_b_cg_update64<<<B.nchunks, kRedBlock, 0, st>>>(B, x, d, p, q, part);
+}
+void kb_ctl_set_l2norm0(const BatchDev &B, const double *part, cudaStream_t st) {
+  k_b_ctl_set_l2norm0<<<B.nm, kRedBlock, 0, st>>>(B, part);
+}
+void kb_ctl_cg_rho(const BatchDev &B, const double *part, cudaStream_t st) {
+  k_b_ctl_cg_rho<<<B.nm, kRedBlock, 0, st>>>(B, part);
+}
+void kb_ctl_alpha(const BatchDev &B, const double *part, cudaStream_t st) {
+  k_b_ctl_alpha<<<B.nm, kRedBlock, 0, st>>>(B, part);
+}
+void kb_ctl_cg_cnvg(const BatchDev &B, const double *part, cudaStream_t st) {
+  k_b_ctl_cg_cnvg<<<B.nm, kRedBlock, 0, st>>>(B, part);
+}
+void kb_all_done(const BatchDev &B, Ctl *gctl, unsigned long long cond, int use_cond,
+                 int count_body, cudaStream_t st) {
+  k_b_all_done<<<1, kRedBlock, 0, st>>>(B, gctl, cond, use_cond, count_body);
 }
 
 }  // namespace gb

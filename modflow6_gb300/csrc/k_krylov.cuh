@@ -26,8 +26,20 @@ void kr_bcgs_update64(int n, double *x, double *d, const double *phat, const dou
 void kr_bcgs_update32(int n, double *x, float *d, const float *phat, const float *qhat, const float *q, const float *t, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st);
 void kr_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond, cudaStream_t st);
 void kr_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs, double refine_factor, cudaStream_t st);
-void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, double *part, int G, const Ctl *ctl, cudaStream_t st);
+void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st);
 void kr_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond, cudaStream_t st);
 void kr_f64_to_f32(int n, const double *s, float *d, cudaStream_t st);
 void kr_f32_to_f64(int n, const float *s, double *d, cudaStream_t st);
+// batched ensemble (one block-diagonal system, per-member control blocks)
+void kb_dot64(const BatchDev &B, const double *a, const double *b, double *part, cudaStream_t st);
+void kb_sumsq64(const BatchDev &B, const double *a, double *part, cudaStream_t st);
+void kb_cg_pupdate64(const BatchDev &B, const double *z, double *p, cudaStream_t st);
+void kb_cg_update64(const BatchDev &B, double *x, double *d, const double *p, const double *q,
+                    double *part, cudaStream_t st);
+void kb_ctl_set_l2norm0(const BatchDev &B, const double *part, cudaStream_t st);
+void kb_ctl_cg_rho(const BatchDev &B, const double *part, cudaStream_t st);
+void kb_ctl_alpha(const BatchDev &B, const double *part, cudaStream_t st);
+void kb_ctl_cg_cnvg(const BatchDev &B, const double *part, cudaStream_t st);
+void kb_all_done(const BatchDev &B, Ctl *gctl, unsigned long long cond, int use_cond,
+                 int count_body, cudaStream_t st);
 }  // namespace gb

@@ -121,6 +121,94 @@ __global__ void __launch_bounds__(256) k_sell_spmv(int n, const int *__restrict_
 
 static inline int rows_grid(int n) { return (n + 255) / 256; }
 
+// ---------------------------------------------------------------------------
+// Full DIS grids (7-point, natural order): the same products without index
+// arrays.  Value slot s of row r sits at v[s*n + r], slots in CSR (JA) order
+// (diagonal, k-1, i-1, j-1, j+1, i+1, k+1); absent neighbours hold zero and
+// are skipped, so every row sums exactly the entries of its CSR row in JA
+// order, like the SELL kernel.
+// ---------------------------------------------------------------------------
+__global__ void k_dia7_vfill(int nlay, int nrow, int ncol, const int *__restrict__ ia,
+                             const double *__restrict__ amat, double *__restrict__ v,
+                             float *__restrict__ v32) {
+  const long long nrc = (long long)nrow * ncol, n = nrc * nlay;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
+       r += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(r / nrc);
+    const int rem = (int)(r - k * nrc);
+    const int i = rem / ncol, j = rem - i * ncol;
+    const bool has[7] = {true, k > 0, i > 0, j > 0, j < ncol - 1, i < nrow - 1, k < nlay - 1};
+    int p = ia[r];
+#pragma unroll
+    for (int s = 0; s < 7; ++s) {
+      const double a = has[s] ? amat[p++] : 0.0;
+      if (v) v[s * n + r] = a;
+      if (v32) v32[s * n + r] = (float)a;
+    }
+  }
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_dia7_spmv(int nlay, int nrow, int ncol,
+                                                   const T *__restrict__ v,
+                                                   const T *__restrict__ x,
+                                                   const T *__restrict__ b, T *__restrict__ y,
+                                                   const Ctl *__restrict__ ctl,
+                                                   int only_if_north_due) {
+  if (ctl) {
+    if (ctl->done) return;
+    if (only_if_north_due && !ctl->north_due) return;
+  }
+  const int nrc = nrow * ncol, n = nrc * nlay;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int k = r / nrc;
+  const int rem = r - k * nrc;
+  const int i = rem / ncol, j = rem - i * ncol;
+  const bool has[7] = {true, k > 0, i > 0, j > 0, j < ncol - 1, i < nrow - 1, k < nlay - 1};
+  const int off[7] = {0, -nrc, -ncol, -1, 1, ncol, nrc};
+  T vv[7], xx[7];
+#pragma unroll
+  for (int s = 0; s < 7; ++s)
+    if (has[s]) vv[s] = ld_stream(v + (size_t)s * n + r);
+#pragma unroll
+  for (int s = 0; s < 7; ++s)
+    if (has[s]) xx[s] = __ldg(x + r + off[s]);
+  T t = T(0);
+#pragma unroll
+  for (int s = 0; s < 7; ++s)
+    if (has[s]) t = mac<T>(vv[s], xx[s], t);
+  if (MODE == 0) y[r] = t;
+  else y[r] = b[r] - t;
+}
+
+void launch_dia7_vfill(const Dia7 &D, const int *d_ia, const double *d_amat, cudaStream_t st) {
+  const long long n = (long long)D.nlay * D.nrow * D.ncol;
+  const int grid = (int)std::min<long long>((n + 255) / 256, 8LL * kNumSM);
+  k_dia7_vfill<<<grid, 256, 0, st>>>(D.nlay, D.nrow, D.ncol, d_ia, d_amat, D.d_sv, D.f_sv);
+}
+
+void launch_dia7_spmv64(const Dia7 &D, const double *x, double *y, const Ctl *ctl,
+                        cudaStream_t st) {
+  const int n = D.nlay * D.nrow * D.ncol;
+  k_dia7_spmv<double, 0><<<rows_grid(n), 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.d_sv, x,
+                                                        nullptr, y, ctl, 0);
+}
+
+void launch_dia7_spmv32(const Dia7 &D, const float *x, float *y, const Ctl *ctl,
+                        cudaStream_t st) {
+  const int n = D.nlay * D.nrow * D.ncol;
+  k_dia7_spmv<float, 0><<<rows_grid(n), 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.f_sv, x,
+                                                       nullptr, y, ctl, 0);
+}
+
+void launch_dia7_residual64(const Dia7 &D, const double *x, const double *b, double *d,
+                            const Ctl *ctl, int only_if_north_due, cudaStream_t st) {
+  const int n = D.nlay * D.nrow * D.ncol;
+  k_dia7_spmv<double, 1><<<rows_grid(n), 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.d_sv, x, b,
+                                                        d, ctl, only_if_north_due);
+}
+
 void launch_spmv64(const Sell &S, const double *x, double *y, const Ctl *ctl, cudaStream_t st) {
   if (S.n == 0) return;
   k_sell_spmv<double, 0><<<rows_grid(S.n), 256, 0, st>>>(S.n, S.d_ptr, S.d_col, S.d_val, x,

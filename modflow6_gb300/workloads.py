@@ -10,3 +10,6 @@ C1_IMS = dict(dvclose=1e-8, rclose=1e-6, iter1=1000, ilinmeth=1)
 C1_OUTER = dict(dvclose=1e-8, mxiter=10)
 C2_IMS = dict(dvclose=1e-6, rclose=1e-4, iter1=20000, ilinmeth=1)
 C2_OUTER = dict(dvclose=1e-6, mxiter=10)
+# C4 (256-member ensemble of confined steady-state DIS grids): PCG + ILU0
+# with the C2 closures, every member to its own closure.
+C4_IMS = dict(dvclose=1e-6, rclose=1e-4, iter1=20000, ilinmeth=1)

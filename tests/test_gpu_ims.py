@@ -2,9 +2,11 @@
 
 Bit-exact: the ILU0/MILU0 factor (ims_base_pcilu0 order, no FMA), the SpMV
 (amux order, FMA) and the preconditioner sweeps (ims_base_ilu0a order, FMA).
-Closure parity: heads within 0.1 x INNER_DVCLOSE of the oracle's IMS solve,
-inner-iteration counts within 2 (Krylov scalars are reduced in a different
-order on the GPU, so iterates differ in the last bits).
+Closure parity: heads within 0.1 x INNER_DVCLOSE of the oracle's IMS solve
+(PCG), or as accurate as the oracle's against a tight solution; inner-
+iteration counts within 2 or 10 % for PCG, and for BiCGSTAB within the
+oracle's own spread under last-bit perturbations (Krylov scalars are reduced
+in a different order on the GPU, so iterates differ in the last bits).
 """
 import ctypes as C
 
@@ -114,7 +116,26 @@ CASES = [
     dict(ilinmeth=2, north=2),
     dict(ilinmeth=1, icnvgopt=2),
     dict(ilinmeth=2, icnvgopt=4),
+    dict(ilinmeth=1, iscl=1),
+    # L2-norm scaling makes the system nonsymmetric: BiCGSTAB only (with CG
+    # the oracle itself stops at INNER_MAXIMUM)
+    dict(ilinmeth=2, iscl=1),
+    dict(ilinmeth=2, iscl=2),
 ]
+
+
+@pytest.mark.parametrize("iscl", [1, 2])
+def test_scaled_factor_bitexact(gblib, iscl):
+    """SCALING_METHOD DIAGONAL / L2NORM: the factor of the scaled matrix
+    (ims_base_scale then ims_base_pcilu0) is bit-identical to the oracle's."""
+    con, amat, rhs, x0 = c1_system()
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=1, iscl=iscl)
+    _, _, _, o = oracle_solve(con, amat, rhs, x0, **tol)
+    ims = gpu_ims(con, **tol)
+    ims.imslinear_apply(amat.copy(), rhs.copy(), x0.copy())
+    apc = np.zeros(con["nja"])
+    assert gblib.gbims_get_apc(ims._h, _lib.dptr(apc)) == 0
+    np.testing.assert_array_equal(apc, o.apc())
 
 
 @pytest.mark.parametrize("kw", CASES, ids=lambda k: "-".join(f"{a}{b}" for a, b in k.items()))
@@ -130,10 +151,22 @@ def test_solve_parity_c1(gblib, kw):
     assert r.icnvg == icnvg_o
     if kw.get("icnvgopt", 0) in (0, 1):
         assert r.icnvg == 1
-    assert iters_close(r.in_iter, it_o), (r.in_iter, it_o)
+    if kw["ilinmeth"] == 1:
+        assert iters_close(r.in_iter, it_o), (r.in_iter, it_o)
+    else:
+        lo, hi = oracle_iteration_spread(con, amat, rhs, x0, **tol, **kw)
+        assert lo - 3 <= r.in_iter <= hi + 3 or iters_close(r.in_iter, it_o), (r.in_iter, lo, hi)
     direct = kw["ilinmeth"] == 1 and kw.get("icnvgopt", 0) in (0, 1)
     x_star = None if direct else tight_solution(con, amat, rhs, x0, kw["ilinmeth"])
     assert_closure_parity(x, xo, x_star, tol["dvclose"], direct)
+
+
+def oracle_iteration_spread(con, amat, rhs, x0, **kw):
+    """BiCGSTAB's iteration count moves with last-bit changes of its inputs:
+    the range of the oracle's counts over right-hand sides perturbed by
+    k * 2.2e-16 relative (k = 0..5)."""
+    its = [oracle_solve(con, amat, rhs * (1.0 + k * 2.2e-16), x0, **kw)[2] for k in range(6)]
+    return min(its), max(its)
 
 
 def iters_close(a, b):

@@ -82,3 +82,27 @@ def test_c3_small_transient_newton(gblib, precision):
         assert so["converged"] == 1 and sg["converged"] == 1
         delt *= 1.2
     assert np.max(np.abs(sol.heads - g.x)) <= 1e-5
+
+
+def test_c2_full_size_matches_oracle_record(gblib):
+    """The 10M-cell steady-state case at full size against the oracle's own
+    full solve (tests/golden/c2_oracle_reference.json, made by
+    tests/golden/make_c2_reference.py): the same outer/inner iteration
+    counts, and heads that agree through size-independent statistics (mean
+    within 1e-5 m, minimum and maximum within 1e-4 m)."""
+    import json
+    from pathlib import Path
+    from modflow6_gb300.workloads import C2_IMS, C2_OUTER
+    rec = json.loads((Path(__file__).parent / "golden" / "c2_oracle_reference.json").read_text())
+    m = make_config("c2", seed=0, scale=1.0)
+    assert m.nodes == rec["nodes"]
+    sol = GwfSolution(m, ImsLinearSettings(structure=(m.nlay, m.nrow, m.ncol), **C2_IMS),
+                      Nonlinear(dvclose=C2_OUTER["dvclose"], mxiter=C2_OUTER["mxiter"]))
+    st = sol.timestep(1, 1, 1.0)
+    h = sol.heads
+    sol.close()
+    assert st["converged"] == 1
+    assert st["outer"] == rec["stats"]["outer"]
+    assert abs(st["inner_total"] - rec["stats"]["inner_total"]) <= 2, st["inner_total"]
+    assert abs(h.sum() - rec["head_checksum"]) <= 1e-5 * m.nodes
+    assert abs(h.min() - rec["head_min"]) <= 1e-4 and abs(h.max() - rec["head_max"]) <= 1e-4

@@ -55,6 +55,19 @@ def test_structured_precondition_matches_oracle(gblib, shape):
     assert np.max(np.abs(z - zo)) <= 1e-12 * scale
 
 
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_structured_matvec_bitexact(gblib, shape):
+    """The index-free product of a full DIS grid sums every CSR row in JA
+    order with FMA, exactly like amux."""
+    m, con, amat, rhs, x0 = dis_system(*shape)
+    ims = ImsLinear(ImsLinearSettings(structure=shape)).imslinear_allocate(m.nodes, con["ia"], con["ja"])
+    assert gblib.gbims_factor(ims._h, _lib.dptr(amat), None) == 0
+    v = np.random.default_rng(6).standard_normal(m.nodes)
+    y = np.zeros_like(v)
+    assert gblib.gbims_matvec(ims._h, _lib.dptr(v), _lib.dptr(y)) == 0
+    np.testing.assert_array_equal(y, oracle.amux_fma(con["ia"], con["ja"], amat, v))
+
+
 @pytest.mark.parametrize("ilinmeth", [1, 2])
 @pytest.mark.parametrize("precision", [_lib.GBIMS_FP64, _lib.GBIMS_MIXED])
 def test_structured_solve_c2_small(gblib, ilinmeth, precision):
