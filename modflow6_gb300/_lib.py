@@ -107,6 +107,10 @@ _SIGS = {
     "gbims_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "gbims_last_error": (C.c_char_p, [C.c_void_p]),
     "gbims_status_string": (C.c_char_p, [C.c_int]),
+    "gbims_residual_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                         C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_int)]),
     "gbnpf_create": (C.c_int, [C.POINTER(GbnpfOptions), C.c_int, C.c_int, C.c_int, _ip, _ip, _ip, _ip, _ip,
                                _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip, C.POINTER(C.c_void_p)]),
     "gbnpf_fill": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

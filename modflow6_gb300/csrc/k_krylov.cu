@@ -876,8 +876,64 @@ __global__ void k_b_all_done(BatchDev B, Ctl *gctl, unsigned long long cond, int
 }
 
 // ---------------------------------------------------------------------------
+// residual d = b - A x with its L2 norm and signed max|d| from CSR device
+// arrays, one row per thread (ims_base_residual + dnrm2, ImsLinearBase.f90:
+// 1291-1312; the row sum in amux order with FMA).  With one 256-row block per
+// partial, the sum of squares rounds exactly like k_sumsq + k_ctl_set_l2norm0
+// on a vector of at most kMaxRedBlocks * 256 rows.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kRedBlock) k_resid_rows(int n, const int *__restrict__ ia,
+                                                           const int *__restrict__ ja, int base,
+                                                           const double *__restrict__ amat,
+                                                           const double *__restrict__ x,
+                                                           const double *__restrict__ b,
+                                                           double *__restrict__ resid,
+                                                           double *__restrict__ part) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[1] = {0.0};
+  MaxLoc m[1];
+  m[0].val = 0.0;
+  m[0].idx = -1;
+  if (i < n) {
+    double t = 0.0;
+    const int k1 = ia[i + 1] - base;
+    for (int k = ia[i] - base; k < k1; ++k) t = fma(amat[k], x[ja[k] - base], t);
+    const double d = b[i] - t;
+    if (resid) resid[i] = d;
+    v[0] = fma(d, d, v[0]);
+    if (absgt(d, m[0].val)) { m[0].val = d; m[0].idx = i; }
+  }
+  block_sum<1>(v);
+  block_maxloc<1>(m);
+  if (threadIdx.x == 0) {
+    const int G = gridDim.x;
+    part[blockIdx.x] = v[0];
+    part[G + blockIdx.x] = m[0].val;
+    part[2 * G + blockIdx.x] = (double)m[0].idx;
+  }
+}
+
+// out[0] = L2 norm, out[1] = signed max|d|, out[2] = its row.
+__global__ void k_resid_final(const double *__restrict__ part, int G, double *__restrict__ out) {
+  const double s = ctl_reduce_sum(part, G);
+  const MaxLoc m = ctl_reduce_maxloc(part + G, part + 2 * G, G);
+  if (threadIdx.x == 0) {
+    out[0] = sqrt(s);
+    out[1] = m.val;
+    out[2] = (double)m.idx;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host launch wrappers
 // ---------------------------------------------------------------------------
+void kr_residual_rows(int n, const int *ia, const int *ja, int base, const double *amat,
+                      const double *x, const double *b, double *resid, double *part,
+                      double *out, cudaStream_t st) {
+  const int G = (n + kRedBlock - 1) / kRedBlock;
+  k_resid_rows<<<G, kRedBlock, 0, st>>>(n, ia, ja, base, amat, x, b, resid, part);
+  k_resid_final<<<1, kRedBlock, 0, st>>>(part, G, out);
+}
 static inline int egrid(int n) { return std::max(1, (n + 255) / 256); }
 
 void kr_dot64(int n, const double *a, const double *b, double *part, int G, const Ctl *ctl, cudaStream_t st) {

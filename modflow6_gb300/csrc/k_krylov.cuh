@@ -29,6 +29,11 @@ void kr_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs, double re
 void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st);
 void kr_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond, cudaStream_t st);
 void kr_f64_to_f32(int n, const double *s, float *d, cudaStream_t st);
+// d = b - A x (CSR, one row per thread; n <= kMaxRedBlocks * kRedBlock) with
+// part (3 * ceil(n/256) doubles) and out (3 doubles: L2, signed max, row).
+void kr_residual_rows(int n, const int *ia, const int *ja, int base, const double *amat,
+                      const double *x, const double *b, double *resid, double *part,
+                      double *out, cudaStream_t st);
 void kr_f32_to_f64(int n, const float *s, double *d, cudaStream_t st);
 // batched ensemble (one block-diagonal system, per-member control blocks)
 void kb_dot64(const BatchDev &B, const double *a, const double *b, double *part, cudaStream_t st);
