@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-warmstart", action="store_true")
     ap.add_argument("--kernels", action="store_true",
                     help="per-kernel device times on direct launches (no solve)")
     return ap.parse_args()
@@ -371,6 +372,7 @@ def gb_arm(a):
                "path": "gbims_apply (C ABI, pinned host amat/rhs/x) per outer iteration"}
         ims.imslinear_da()
     ens = None if a.no_ensemble else ensemble_form(a, lib, barrier, maxr)
+    ws_res = None if a.no_warmstart else warmstart_form(a)
     last = st64[-1]
     line = {
         "metric": METRIC, "value": ms64 / 1e3, "unit": "s", "n_gpus": ws, "steps": a.steps,
@@ -398,6 +400,7 @@ def gb_arm(a):
         "kernels": {"spmv_ms": kt.spmv_ms, "spmv_gbs": spmv_gbs, "precond_ms": kt.precond_ms,
                     "precond_gbs": pre_gbs, "dot_ms": kt.dot_ms, "update_ms": kt.update_ms},
         "e2e": e2e, "gpu_launches": int(launches64), "clocks": clocks, "ensemble": ens,
+        "warm_start": ws_res,
     }
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_sample(m, last["inner_total"], last["outer"])
@@ -454,6 +457,36 @@ def ensemble_form(a, lib, barrier, maxr) -> dict:
             "inner_iterations": {"min": int(its.min()), "mean": float(its.mean()),
                                  "max": int(its.max())},
             "form": "FP64 batched PCG + wavefront ILU0, one CUDA graph for all members"}
+
+
+def warmstart_form(a) -> dict:
+    """The learned warm start on the transient 256x256x3 workload (C5): the
+    network is trained on the GPU (its own BF16 tensor-core kernels) on heads
+    the plain solver produces for seeded training models, then every time step
+    of held-out models is solved from the previous heads and from the
+    network's guess, to the same closure."""
+    import time as _t
+    from modflow6_gb300.warmstart import WarmStartNet, evaluate, generate, train
+
+    full = a.scale == 1.0
+    ntrain, nheld, steps = (24, 4, 20) if full else (4, 2, 8)
+    sc = 1.0 if full else 0.1
+    t0 = _t.perf_counter()
+    data, dh_scale = generate(range(1000, 1000 + ntrain), steps=steps, scale=sc)
+    t_gen = _t.perf_counter() - t0
+    net = WarmStartNet(data[0][0], seed=a.seed)
+    t0 = _t.perf_counter()
+    hist = train(net, data, dh_scale, epochs=4, lr=1e-3)
+    t_train = _t.perf_counter() - t0
+    del data
+    res = evaluate(net, range(5000, 5000 + nheld), steps=steps, scale=sc)
+    net.close()
+    return {"workload": f"DIS 3x{int(256 * sc)}x{int(256 * sc)} transient, {steps} steps of 0.5 d, "
+                        f"50 wells; PCG + ILU0 to INNER_DVCLOSE 1e-6, INNER_RCLOSE 1e-4",
+            "train_models": ntrain, "train_samples": ntrain * steps, "data_s": t_gen,
+            "head_change_scale_m": dh_scale,
+            "train_s": t_train, "epochs": 4, "loss_per_epoch": hist, "heldout": res,
+            "network": "8-layer message passing, hidden 64, BF16 mma.sync GEMMs, FP32 Adam"}
 
 
 def kernels_arm(a):

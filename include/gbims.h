@@ -33,8 +33,10 @@ extern "C" {
 
 /* precision modes */
 #define GBIMS_FP64 0  /* FP64 everywhere: the plain drop-in */
-#define GBIMS_MIXED 1 /* FP32 matrix, factors and inner vectors; FP64 true
-                         residual, Krylov scalars, head update and closure */
+#define GBIMS_MIXED 1 /* FP32 matrix and ILU0 factors (FP32 triangular
+                         sweeps); FP64 Krylov vectors and scalars, FP64 true
+                         residual, head update and closure, with iterative
+                         refinement between the two */
 
 /* IMS LINEAR block options, with the meaning of
  * src/Solution/LinearMethods/ImsLinearSettings.f90:10-253 and
@@ -269,6 +271,12 @@ int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,
  * step length used by the pseudo-transient continuation default
  * (gwf.f90:625-687). */
 int gbsln_timestep(gbsln_handle *h, int kper, int kstp, double delt, gbsln_stats *st);
+/* The same time step started from a guess (d_guess: device array, nodes):
+ * the first outer iterate of every active cell is the guess instead of the
+ * previous heads, which stay the storage reference (xold).  The closure is
+ * unchanged, so a guess only changes how many iterations it takes. */
+int gbsln_timestep_guess(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
+                         gbsln_stats *st);
 /* sln_buildsystem at the current heads (hold: previous-step heads, needed for
  * a transient step): the assembled amat (nja, CSR order of the DIS grid) and
  * rhs before the sln_ls fix-ups, copied to the host.  The reference writes
@@ -282,6 +290,31 @@ int gbsln_get_heads(gbsln_handle *h, double *x);
 int gbsln_set_heads(gbsln_handle *h, const double *x);
 gbims_handle *gbsln_ims(gbsln_handle *h);
 int gbsln_destroy(gbsln_handle *h);
+
+/* ---- Learned warm start (no counterpart in the reference) ----------------
+ * A message-passing network over the graph of the IMS matrix (hidden width
+ * 64, 8 layers, 16 input features per cell) that predicts a time step's head
+ * change; trained and evaluated on the GPU (BF16 tensor-core GEMMs, FP32
+ * accumulation, FP32 Adam).  Device arrays: features nodes x 16 (row-major
+ * FP32), targets, masks and outputs nodes (FP32).  The loss is
+ * inv_count * sum(((y - target) * mask)^2). */
+typedef struct gbmpnn_handle gbmpnn_handle;
+long long gbmpnn_param_count(void);
+int gbmpnn_create(int nodes, int nja, const int *ia, const int *ja, unsigned long long seed,
+                  gbmpnn_handle **out);
+/* Edge weights from an assembled matrix (device amat, nja, the CSR of create). */
+int gbmpnn_set_graph(gbmpnn_handle *h, const double *d_amat);
+int gbmpnn_forward(gbmpnn_handle *h, const float *d_x, float *d_y);
+/* Loss and (grad != NULL) the gradient, both to the host, without an update. */
+int gbmpnn_gradients(gbmpnn_handle *h, const float *d_x, const float *d_target,
+                     const float *d_mask, float inv_count, float *loss, float *grad);
+/* One Adam step (learning rate lr) on one sample; the loss before the step. */
+int gbmpnn_train_step(gbmpnn_handle *h, const float *d_x, const float *d_target,
+                      const float *d_mask, float inv_count, float lr, float *loss);
+int gbmpnn_get_params(gbmpnn_handle *h, float *params);
+int gbmpnn_set_params(gbmpnn_handle *h, const float *params);
+const char *gbmpnn_last_error(const gbmpnn_handle *h);
+int gbmpnn_destroy(gbmpnn_handle *h);
 
 #ifdef __cplusplus
 }

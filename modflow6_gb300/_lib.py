@@ -119,6 +119,8 @@ _SIGS = {
     "gbsln_create": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbnpfOptions), C.POINTER(GbimsSettings),
                                C.POINTER(GbslnNonlinear), _dp, C.POINTER(C.c_void_p)]),
     "gbsln_timestep": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.POINTER(GbslnStats)]),
+    "gbsln_timestep_guess": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_void_p,
+                                       C.POINTER(GbslnStats)]),
     "gbsln_formulate": (C.c_int, [C.c_void_p, C.c_double, _dp, _dp, _dp]),
     "gbsln_last_error": (C.c_char_p, [C.c_void_p]),
     "gbsln_restart": (C.c_int, [C.c_void_p]),
@@ -126,6 +128,18 @@ _SIGS = {
     "gbsln_set_heads": (C.c_int, [C.c_void_p, _dp]),
     "gbsln_ims": (C.c_void_p, [C.c_void_p]),
     "gbsln_destroy": (C.c_int, [C.c_void_p]),
+    "gbmpnn_param_count": (C.c_longlong, []),
+    "gbmpnn_create": (C.c_int, [C.c_int, C.c_int, _ip, _ip, C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    "gbmpnn_set_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gbmpnn_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gbmpnn_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
+                                   C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "gbmpnn_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
+                                    C.c_float, C.POINTER(C.c_float)]),
+    "gbmpnn_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "gbmpnn_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "gbmpnn_last_error": (C.c_char_p, [C.c_void_p]),
+    "gbmpnn_destroy": (C.c_int, [C.c_void_p]),
 }
 
 EXPORTED = tuple(_SIGS)

@@ -30,12 +30,18 @@ def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu"))
 
 
-def _compile(src: Path, verbose: bool) -> Path:
+def extra_flags() -> list[str]:
+    """Build-time tuning definitions from GBIMS_NVCC_EXTRA (for example
+    "-DGB_DIA64_S=1"); a change of them rebuilds every object."""
+    return os.environ.get("GBIMS_NVCC_EXTRA", "").split()
+
+
+def _compile(src: Path, verbose: bool, stale: bool) -> Path:
     out = OBJ / (src.stem + ".o")
     deps = [src] + sorted(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "gbims.h"]
-    if out.exists() and out.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+    if not stale and out.exists() and out.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
         return out
-    cmd = [nvcc(), *ARCH, *FLAGS, "-c", str(src), "-o", str(out)]
+    cmd = [nvcc(), *ARCH, *FLAGS, *extra_flags(), "-c", str(src), "-o", str(out)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -50,10 +56,14 @@ def build(verbose: bool = False) -> Path:
     """Compiles every .cu under csrc/ and links libgbims.so; returns its path."""
     OBJ.mkdir(exist_ok=True)
     srcs = sources()
+    stamp = OBJ / "flags.txt"
+    flags = " ".join(extra_flags())
+    stale = not stamp.exists() or stamp.read_text() != flags
     with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
+        objs = list(ex.map(lambda s: _compile(s, verbose, stale), srcs))
+    stamp.write_text(flags)
     newest = max(o.stat().st_mtime for o in objs)
-    if not LIB.exists() or LIB.stat().st_mtime < newest:
+    if stale or not LIB.exists() or LIB.stat().st_mtime < newest:
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -51,7 +51,7 @@ struct gbims_handle {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool graph_tried = false, graph_ok = false;
-  double refine_factor = 1.0e-5;
+  double refine_factor = 1.0e-5;  // 1e-4 saves 3 % of the iterations but loses accuracy with BiCGSTAB
   bool factored = false;
   // batched ensemble (nm > 0): members concatenated into one block-diagonal
   // system, one control block per member, the handle's Ctl = all done
@@ -94,9 +94,17 @@ static void precond64(gbims_handle *h, const double *r, double *z) {
   else launch_ilu_apply_levels(h->n, h->d_iapc, h->d_japc, h->d_apc, h->F, h->B, r, z, h->d_ctl, h->st);
 }
 
-static void precond32(gbims_handle *h, const float *r, float *z) {
-  if (h->structured) launch_dia7_apply32(h->D, r, z, h->d_ctl, h->st);
-  else launch_ilu_apply_levels32(h->n, h->d_iapc, h->d_japc, h->d_apc32, h->F, h->B, r, z, h->d_ctl, h->st);
+// The mixed form's preconditioner: FP64 vectors, FP32 factors and FP32
+// sweeps (the skew/unskew permutes convert on the wavefront path).
+static void precond_mixed(gbims_handle *h, const double *r, double *z) {
+  if (h->structured) {
+    launch_dia7_apply_mixed(h->D, r, z, h->d_ctl, h->st);
+  } else {
+    kr_f64_to_f32(h->n, r, h->f_d, h->st);
+    launch_ilu_apply_levels32(h->n, h->d_iapc, h->d_japc, h->d_apc32, h->F, h->B, h->f_d, h->f_z,
+                              h->d_ctl, h->st);
+    kr_f32_to_f64(h->n, h->f_z, z, h->st);
+  }
 }
 
 // A*x and b - A*x: index-free on full DIS grids, SELL-32 otherwise.
@@ -105,9 +113,10 @@ static void spmv64(gbims_handle *h, const double *x, double *y, const Ctl *c) {
   else launch_spmv64(h->S, x, y, c, h->st);
 }
 
-static void spmv32(gbims_handle *h, const float *x, float *y, const Ctl *c) {
-  if (h->dia_spmv) launch_dia7_spmv32(h->D, x, y, c, h->st);
-  else launch_spmv32(h->S, x, y, c, h->st);
+// The mixed form's product: FP32 matrix values, FP64 vectors.
+static void spmv_mixed(gbims_handle *h, const double *x, double *y, const Ctl *c) {
+  if (h->dia_spmv) launch_dia7_spmv_mixed(h->D, x, y, c, h->st);
+  else launch_spmv_mixed(h->S, x, y, c, h->st);
 }
 
 static void residual64(gbims_handle *h, const Ctl *c, int only_if_north_due) {
@@ -165,35 +174,38 @@ static void enqueue_iteration(gbims_handle *h, unsigned long long cond, int use_
     kr_ctl_bcgs_cnvg(c, part, G, cond, use_cond, st);
     residual64(h, c, 1);
   } else if (h->mixed && !h->bcgs) {
-    precond32(h, h->f_d, h->f_z);
-    kr_dot32(n, h->f_d, h->f_z, part, G, c, st);
+    // PCG on the FP32 matrix with FP64 vectors and an FP32 preconditioner;
+    // the FP64 true residual replaces the recurrence's at each refinement
+    precond_mixed(h, h->v_d, h->v_z);
+    kr_dot64(n, h->v_d, h->v_z, part, G, c, st);
     kr_ctl_cg_rho(c, part, G, st);
-    kr_cg_pupdate32(n, h->f_z, h->f_p, c, st);
-    spmv32(h, h->f_p, h->f_q, c);
-    kr_dot32(n, h->f_p, h->f_q, part, G, c, st);
+    kr_cg_pupdate64(n, h->v_z, h->v_p, c, st);
+    spmv_mixed(h, h->v_p, h->v_q, c);
+    kr_dot64(n, h->v_p, h->v_q, part, G, c, st);
     kr_ctl_alpha(c, part, G, st);
-    kr_cg_update_mixed(n, h->d_x, h->f_d, h->f_p, h->f_q, part, G, c, st);
+    kr_cg_update64(n, h->d_x, h->v_d, h->v_p, h->v_q, part, G, c, st);
     kr_ctl_mixed_inner(c, part, G, 0, h->refine_factor, st);
     residual64(h, c, 1);
-    kr_true_resid_stats(n, h->v_d, h->f_d, nullptr, nullptr, part, G, c, st);
+    kr_true_resid_stats(n, h->v_d, nullptr, nullptr, nullptr, nullptr, part, G, c, st);
     kr_ctl_refine(c, part, G, cond, use_cond, st);
   } else {
-    kr_dot32(n, h->f_dhat, h->f_d, part, G, c, st);
+    // BiCGSTAB, same precision split
+    kr_dot64(n, h->v_dhat, h->v_d, part, G, c, st);
     kr_ctl_bcgs_rho(c, part, G, st);
-    kr_bcgs_p32(n, h->f_d, h->f_p, h->f_v, c, st);
-    precond32(h, h->f_p, h->f_phat);
-    spmv32(h, h->f_phat, h->f_v, c);
-    kr_dot32(n, h->f_dhat, h->f_v, part, G, c, st);
+    kr_bcgs_p64(n, h->v_d, h->v_p, h->v_v, c, st);
+    precond_mixed(h, h->v_p, h->v_phat);
+    spmv_mixed(h, h->v_phat, h->v_v, c);
+    kr_dot64(n, h->v_dhat, h->v_v, part, G, c, st);
     kr_ctl_alpha(c, part, G, st);
-    kr_bcgs_q32(n, h->f_d, h->f_v, h->f_q, c, st);
-    precond32(h, h->f_q, h->f_qhat);
-    spmv32(h, h->f_qhat, h->f_t, c);
-    kr_dot_tq_tt32(n, h->f_t, h->f_q, part, G, c, st);
+    kr_bcgs_q64(n, h->v_d, h->v_v, h->v_q, c, st);
+    precond_mixed(h, h->v_q, h->v_qhat);
+    spmv_mixed(h, h->v_qhat, h->v_t, c);
+    kr_dot_tq_tt64(n, h->v_t, h->v_q, part, G, c, st);
     kr_ctl_omega(c, part, G, st);
-    kr_bcgs_update32(n, h->d_x, h->f_d, h->f_phat, h->f_qhat, h->f_q, h->f_t, h->d_dscale, part, G, c, st);
+    kr_bcgs_update64(n, h->d_x, h->v_d, h->v_phat, h->v_qhat, h->v_q, h->v_t, h->d_dscale, part, G, c, st);
     kr_ctl_mixed_inner(c, part, G, 1, h->refine_factor, st);
     residual64(h, c, 1);
-    kr_true_resid_stats(n, h->v_d, h->f_d, h->f_dhat, h->d_dscale, part, G, c, st);
+    kr_true_resid_stats(n, h->v_d, nullptr, nullptr, h->v_dhat, h->d_dscale, part, G, c, st);
     kr_ctl_refine(c, part, G, cond, use_cond, st);
   }
 }
@@ -315,6 +327,11 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   // launched one by one), for profilers that do not see kernel nodes inside
   // conditional graphs
   if (const char *g = std::getenv("GBIMS_GRAPH")) h->graph_tried = (g[0] == '0');
+  // GBIMS_REFINE: the mixed form's relative L2 reduction per refinement
+  if (const char *r = std::getenv("GBIMS_REFINE")) {
+    const double v = std::atof(r);
+    if (v > 0.0 && v < 1.0) h->refine_factor = v;
+  }
   // 0-based copies and checks: diagonal first in every row
   int base = s->index_base ? 1 : 0;
   h->ia.resize(neq + 1);
@@ -403,24 +420,19 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   GB_CUDA(h, dalloc(&h->d_rhs, nn));
   GB_CUDA(h, dalloc(&h->d_x, nn));
   GB_CUDA(h, dalloc(&h->v_d, nn));
-  if (!h->mixed) {
-    GB_CUDA(h, dalloc(&h->v_p, nn));
-    GB_CUDA(h, dalloc(&h->v_q, nn));
-    GB_CUDA(h, dalloc(&h->v_z, nn));
-    if (h->bcgs) {
-      GB_CUDA(h, dalloc(&h->v_t, nn)); GB_CUDA(h, dalloc(&h->v_v, nn));
-      GB_CUDA(h, dalloc(&h->v_dhat, nn)); GB_CUDA(h, dalloc(&h->v_phat, nn));
-      GB_CUDA(h, dalloc(&h->v_qhat, nn));
-    }
-  } else {
+  GB_CUDA(h, dalloc(&h->v_p, nn));
+  GB_CUDA(h, dalloc(&h->v_q, nn));
+  GB_CUDA(h, dalloc(&h->v_z, nn));
+  if (h->bcgs) {
+    GB_CUDA(h, dalloc(&h->v_t, nn)); GB_CUDA(h, dalloc(&h->v_v, nn));
+    GB_CUDA(h, dalloc(&h->v_dhat, nn)); GB_CUDA(h, dalloc(&h->v_phat, nn));
+    GB_CUDA(h, dalloc(&h->v_qhat, nn));
+  }
+  if (h->mixed) {
+    // FP32 factors; FP32 input and output of the level-scheduled sweeps
     GB_CUDA(h, dalloc(&h->d_apc32, nja));
-    GB_CUDA(h, dalloc(&h->f_d, nn)); GB_CUDA(h, dalloc(&h->f_p, nn));
-    GB_CUDA(h, dalloc(&h->f_q, nn)); GB_CUDA(h, dalloc(&h->f_z, nn));
-    if (h->bcgs) {
-      GB_CUDA(h, dalloc(&h->f_t, nn)); GB_CUDA(h, dalloc(&h->f_v, nn));
-      GB_CUDA(h, dalloc(&h->f_dhat, nn)); GB_CUDA(h, dalloc(&h->f_phat, nn));
-      GB_CUDA(h, dalloc(&h->f_qhat, nn));
-    }
+    GB_CUDA(h, dalloc(&h->f_d, nn));
+    GB_CUDA(h, dalloc(&h->f_z, nn));
   }
   // SCALING_METHOD (ImsLinear.f90:222-224): DSCALE/DSCALE2 only when scaling;
   // BiCGSTAB reads DSCALE in its convergence maxima (null without scaling)
@@ -538,15 +550,7 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
   residual64(h, nullptr, 0);
   kr_sumsq64(n, h->v_d, h->d_part, h->G, st);
   kr_ctl_set_l2norm0(h->d_ctl, h->d_part, h->G, st);
-  if (h->bcgs && !h->mixed) GB_CUDA(h, cudaMemcpyAsync(h->v_dhat, h->v_d, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-  if (h->mixed) {
-    kr_f64_to_f32(n, h->v_d, h->f_d, st);
-    GB_CUDA(h, cudaMemsetAsync(h->f_p, 0, sizeof(float) * n, st));
-    if (h->bcgs) {
-      GB_CUDA(h, cudaMemcpyAsync(h->f_dhat, h->f_d, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
-      GB_CUDA(h, cudaMemsetAsync(h->f_v, 0, sizeof(float) * n, st));
-    }
-  }
+  if (h->bcgs) GB_CUDA(h, cudaMemcpyAsync(h->v_dhat, h->v_d, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   GB_CUDA(h, cudaGetLastError());
   // inner loop
   if (!h->graph_tried) build_graph(h);
@@ -576,7 +580,7 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
   GB_CUDA(h, cudaGetLastError());
   const Ctl &r = *h->h_ctl;
   // zero, residual, sum of squares, L2NORM0 control (+ FP32 copy), then the loop bodies
-  h->launches += 4 + (h->mixed ? 1 : 0) + (long long)h->body_kernels * r.bodies;
+  h->launches += 4 + (long long)h->body_kernels * r.bodies;
   int iters = (r.l2norm0 == 0.0 || h->s.iter1 <= 0) ? 0 : r.iter;
   *icnvg = r.icnvg;
   *in_iter = iters;
@@ -679,13 +683,8 @@ extern "C" int gbims_precondition(gbims_handle *h, const double *r, double *z) {
   c.pivot_fail = INT_MAX;
   *h->h_ctl = c;
   GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->st));
-  if (!h->mixed) {
-    precond64(h, h->v_d, h->d_rhs);
-  } else {
-    kr_f64_to_f32(h->n, h->v_d, h->f_d, h->st);
-    precond32(h, h->f_d, h->f_z);
-    kr_f32_to_f64(h->n, h->f_z, h->d_rhs, h->st);
-  }
+  if (!h->mixed) precond64(h, h->v_d, h->d_rhs);
+  else precond_mixed(h, h->v_d, h->d_rhs);
   GB_CUDA(h, cudaGetLastError());
   GB_CUDA(h, cudaMemcpyAsync(z, h->d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
   GB_CUDA(h, cudaStreamSynchronize(h->st));
@@ -705,14 +704,8 @@ extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times 
   GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
   int eg = std::min(4 * kNumSM, (n + 255) / 256);
   // deterministic, finite operands
-  if (!h->mixed) {
-    k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
-    GB_CUDA(h, cudaMemcpyAsync(h->v_p, h->d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-  } else {
-    kr_f64_to_f32(n, h->d_x, h->f_p, st);
-    GB_CUDA(h, cudaMemsetAsync(h->f_q, 0, sizeof(float) * n, st));
-    GB_CUDA(h, cudaMemsetAsync(h->f_d, 0, sizeof(float) * n, st));
-  }
+  k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
+  GB_CUDA(h, cudaMemcpyAsync(h->v_p, h->d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
   auto time_it = [&](auto &&fn) -> double {
     fn();
     cudaEventRecord(h->ev0, st);
@@ -729,10 +722,10 @@ extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times 
     t->dot_ms = time_it([&] { kr_dot64(n, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
     t->update_ms = time_it([&] { kr_cg_update64(n, h->v_z, h->v_d, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
   } else {
-    t->spmv_ms = time_it([&] { spmv32(h, h->f_p, h->f_q, h->d_ctl); });
-    t->precond_ms = time_it([&] { precond32(h, h->f_p, h->f_z); });
-    t->dot_ms = time_it([&] { kr_dot32(n, h->f_p, h->f_q, h->d_part, h->G, h->d_ctl, st); });
-    t->update_ms = time_it([&] { kr_cg_update_mixed(n, h->v_d, h->f_d, h->f_p, h->f_q, h->d_part, h->G, h->d_ctl, st); });
+    t->spmv_ms = time_it([&] { spmv_mixed(h, h->v_p, h->v_q, h->d_ctl); });
+    t->precond_ms = time_it([&] { precond_mixed(h, h->v_p, h->v_z); });
+    t->dot_ms = time_it([&] { kr_dot64(n, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
+    t->update_ms = time_it([&] { kr_cg_update64(n, h->v_z, h->v_d, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
   }
   GB_CUDA(h, cudaGetLastError());
   // algorithmic bytes: CSR values + column indices + row pointers, x read
@@ -741,10 +734,11 @@ extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times 
   // and z written once, plus JAPC/IAPC for the unstructured sweeps (the
   // structured sweeps need no indices).  The forward result kept between
   // the two sweeps is not counted.
-  double vb = h->mixed ? 4.0 : 8.0;
-  t->spmv_bytes = h->dia_spmv ? vb * h->nja + 2.0 * vb * n
-                                 : (vb + 4.0) * h->nja + 4.0 * (n + 1) + 2.0 * vb * n;
-  t->precond_bytes = vb * h->nja + 2.0 * vb * n;
+  // The mixed form: FP32 matrix and factors, FP64 vectors.
+  const double mb = h->mixed ? 4.0 : 8.0, vb = 8.0;
+  t->spmv_bytes = h->dia_spmv ? mb * h->nja + 2.0 * vb * n
+                              : (mb + 4.0) * h->nja + 4.0 * (n + 1) + 2.0 * vb * n;
+  t->precond_bytes = mb * h->nja + 2.0 * vb * n;
   if (!h->structured) t->precond_bytes += 4.0 * h->nja + 4.0 * (n + 1);
   return GBIMS_OK;
 }
@@ -763,7 +757,8 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->v_z, h->v_t, h->v_v, h->v_dhat, h->v_phat, h->v_qhat, h->f_d, h->f_p,
                   h->f_q, h->f_z, h->f_t, h->f_v, h->f_dhat, h->f_phat, h->f_qhat, h->d_part,
                   h->d_dscale, h->d_dscale2, h->d_cptr, h->d_cpos, h->D.d_sv, h->D.f_sv,
-                  h->d_bcm, h->d_bcr, h->d_bmc, h->d_bmr, h->d_ctls, h->D.d_geo, h->d_ctl};
+                  h->d_bcm, h->d_bcr, h->d_bmc, h->d_bmr, h->d_ctls, h->D.d_geo, h->S.d_slm,
+                  h->d_ctl};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
@@ -861,6 +856,21 @@ extern "C" int gbims_batch_create(const gbims_settings *settings, int nmembers,
   h->bd.mc = h->d_bmc;
   h->bd.mr = h->d_bmr;
   h->bd.ctls = h->d_ctls;
+  // the products skip the rows of members that are done: per SELL slice its
+  // member, or -1 where a member boundary falls inside the slice
+  if (h->S.nslices > 0) {
+    std::vector<int> slm(h->S.nslices);
+    for (int sl = 0, m = 0; sl < h->S.nslices; ++sl) {
+      const int r0 = sl * kSell, r1 = std::min(neq, r0 + kSell) - 1;
+      while (mrow[m + 1] <= r0) ++m;
+      slm[sl] = (r1 < mrow[m + 1]) ? m : -1;
+    }
+    GB_CUDA(h, dalloc(&h->S.d_slm, slm.size()));
+    GB_CUDA(h, cudaMemcpy(h->S.d_slm, slm.data(), sizeof(int) * slm.size(), cudaMemcpyHostToDevice));
+    h->S.d_mrow = h->d_bmr;
+    h->S.nm = nmembers;
+    h->S.mctl = h->d_ctls;
+  }
   // full DIS grids: the wavefront sweeps run every member's layers and
   // blocks as the CTAs of one launch
   if (shapes) {
@@ -883,6 +893,7 @@ extern "C" int gbims_batch_create(const gbims_settings *settings, int nmembers,
     }
     int rc2 = setup_structured(h, sh, row0);
     if (rc2 != GBIMS_OK) return rc2;
+    h->D.mctl = h->d_ctls;
   }
   return GBIMS_OK;
 }

@@ -96,6 +96,11 @@ struct Sell {
   int *d_src = nullptr;   // nstored, CSR position or -1 for padding
   double *d_val = nullptr;
   float *d_val32 = nullptr;
+  // batched ensembles: the products skip the rows of members that are done
+  int *d_slm = nullptr;         // per slice: its member, or -1 if it straddles two
+  const int *d_mrow = nullptr;  // member -> first row (nm + 1)
+  const Ctl *mctl = nullptr;    // member control blocks (null: single system)
+  int nm = 0;
 };
 
 // Level schedule of a triangular sweep: rows grouped by level.
@@ -126,6 +131,7 @@ struct Dia7 {
   int nm = 0;              // members
   std::vector<Dia7Geo> geo;
   Dia7Geo *d_geo = nullptr;
+  const Ctl *mctl = nullptr;  // batched ensembles: members that are done are skipped
   int ntickets = 0, nptiles = 0;
   // forward tiles: lower coefficients (unit diagonal) z (layer above),
   // y (row behind), x (column left); backward tiles: dinv*U for z, y, x and
@@ -161,9 +167,14 @@ void sell_build_host(int n, const std::vector<int> &ia, const std::vector<int> &
                      std::vector<int> &ptr, std::vector<int> &col, std::vector<int> &src);
 void launch_sell_fill(const Sell &S, const double *d_amat, cudaStream_t st);
 void launch_spmv64(const Sell &S, const double *x, double *y, const Ctl *ctl, cudaStream_t st);
-void launch_spmv32(const Sell &S, const float *x, float *y, const Ctl *ctl, cudaStream_t st);
 void launch_residual64(const Sell &S, const double *x, const double *b, double *d,
                        const Ctl *ctl, int only_if_north_due, cudaStream_t st);
+// FP32 matrix values, FP64 vectors and accumulation (the mixed form)
+void launch_spmv_mixed(const Sell &S, const double *x, double *y, const Ctl *ctl, cudaStream_t st);
+void launch_dia7_spmv_mixed(const Dia7 &D, const double *x, double *y, const Ctl *ctl,
+                            cudaStream_t st);
+void launch_dia7_apply_mixed(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
+                             cudaStream_t st);
 
 void levels_build_host(int n, const std::vector<int> &iapc, const std::vector<int> &japc,
                        bool forward, Levels &L);
@@ -184,12 +195,8 @@ void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_j
                          const double *d_apc, bool mixed, cudaStream_t st);
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
                          cudaStream_t st);
-void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
-                         cudaStream_t st);
 void launch_dia7_vfill(const Dia7 &D, const int *d_ia, const double *d_amat, cudaStream_t st);
 void launch_dia7_spmv64(const Dia7 &D, const double *x, double *y, const Ctl *ctl,
-                        cudaStream_t st);
-void launch_dia7_spmv32(const Dia7 &D, const float *x, float *y, const Ctl *ctl,
                         cudaStream_t st);
 void launch_dia7_residual64(const Dia7 &D, const double *x, const double *b, double *d,
                             const Ctl *ctl, int only_if_north_due, cudaStream_t st);

@@ -261,6 +261,13 @@ struct gbsln_handle {
     }                                                                       \
   } while (0)
 
+// Warm start: the first outer iterate of active cells from a guess.
+__global__ void k_apply_guess(int n, const int *__restrict__ ibound, const double *__restrict__ guess,
+                              double *__restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (ibound[i] > 0) x[i] = guess[i];
+}
+
 __global__ void k_set_chd(int nchd, const int *__restrict__ node, const double *__restrict__ head,
                           double *x, double *xold) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -423,7 +430,21 @@ static int reduce_host(gbsln_handle *h, bool max_not_sum, double *out) {
   return GBIMS_OK;
 }
 
+static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
+                         gbsln_stats *st);
+
 extern "C" int gbsln_timestep(gbsln_handle *h, int kper, int kstp, double delt, gbsln_stats *st) {
+  return timestep_core(h, kper, kstp, delt, nullptr, st);
+}
+
+extern "C" int gbsln_timestep_guess(gbsln_handle *h, int kper, int kstp, double delt,
+                                    const double *d_guess, gbsln_stats *st) {
+  if (!d_guess) return GBIMS_ERR_ARG;
+  return timestep_core(h, kper, kstp, delt, d_guess, st);
+}
+
+static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
+                         gbsln_stats *st) {
   if (!h || !h->ims) return GBIMS_ERR_ARG;
   const int n = h->n;
   const bool transient = (delt > 0.0) && h->has_sto;
@@ -433,6 +454,10 @@ extern "C" int gbsln_timestep(gbsln_handle *h, int kper, int kstp, double delt, 
   SLN_CUDA(h, cudaEventRecord(h->e0, h->st));
   // prepareSolve: gwf_ad (xold = x) and chd_ad (x = xold = head)
   SLN_CUDA(h, cudaMemcpyAsync(h->xold, h->x, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->st));
+  // warm start: the guess replaces the previous heads as the first iterate
+  // (xold, the storage reference, keeps the previous heads)
+  if (d_guess)
+    k_apply_guess<<<std::min(4 * kNumSM, (n + 255) / 256), 256, 0, h->st>>>(n, h->ibound, d_guess, h->x);
   if (h->nchd > 0)
     k_set_chd<<<(h->nchd + 255) / 256, 256, 0, h->st>>>(h->nchd, h->chd_node, h->chd_head, h->x, h->xold);
   FillDev f;

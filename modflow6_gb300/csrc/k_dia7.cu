@@ -10,9 +10,11 @@
 // consecutive lines of one layer (a "block").  Lane l of its compute warp
 // walks line l of the block S steps behind lane l-1, so the value it needs
 // from the neighbour line was produced S steps earlier and arrives by a
-// register shuffle; with S = 2 (FP64) only the FMA with the lane's own
-// previous column is on the critical path of a step.  The neighbour block
-// (line i0-1) and the neighbour layer are other CTAs.
+// register shuffle (with S >= 2 only the FMA with the lane's own previous
+// column is on a step's dependency chain; with S = 1, the default, the
+// shuffle and the row-neighbour FMA are too, but the blocks lag each other
+// by half as many steps).  The neighbour block (line i0-1) and the
+// neighbour layer are other CTAs.
 //
 // Skewed layout.  The factors and the intermediate results are stored per
 // block as G x W tiles, row g = wavefront step, column l = lane (element
@@ -130,6 +132,7 @@ template <typename T>
 struct SweepArgs {
   const Dia7Geo *geo;  // members, in ticket order
   int nm;
+  const Ctl *mctl;     // per-member control blocks (batched ensembles) or null
   const T *A, *B, *X, *D;  // skewed factors (forward: Lz Ly Lx -, backward: Uz' Uy' Ux' dinv)
   const T *rsk;            // forward: right-hand side, skewed
   T *ysk;                  // forward result, skewed (written forward, read backward)
@@ -186,6 +189,9 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  // a member of a batch that has reached its closure is not swept; its CTAs
+  // only depend on one another, so none of them waits for it
+  if (p.mctl && p.mctl[s_m].done) return;
   const int role = (warp + s_rot) & 3;
   const int id = s_id;
   const Dia7Geo geo = p.geo[s_m];
@@ -419,9 +425,10 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
 // Natural order -> skewed tiles (forward input) and back (backward output).
 // A 32 x 8 thread block covers 32 columns of 8 lines: the natural-order side
 // is whole rows, and the skewed side falls in a few rows of one tile.
-template <typename T, int W, int S, int DIR>
-__global__ void k_dia7_permute(const Dia7Geo *__restrict__ geos, int nm, const T *__restrict__ src,
-                               T *__restrict__ dst, const Ctl *__restrict__ ctl) {
+template <typename TS, typename TD, int W, int S, int DIR>
+__global__ void k_dia7_permute(const Dia7Geo *__restrict__ geos, int nm, const TS *__restrict__ src,
+                               TD *__restrict__ dst, const Ctl *__restrict__ ctl,
+                               const Ctl *__restrict__ mctl) {
   if (ctl && ctl->done) return;
   // member of this 32 x 8 tile
   const int t = blockIdx.x;
@@ -431,6 +438,7 @@ __global__ void k_dia7_permute(const Dia7Geo *__restrict__ geos, int nm, const T
     if (geos[mid].ptile0 <= t) lo = mid;
     else hi = mid - 1;
   }
+  if (mctl && mctl[lo].done) return;
   const Dia7Geo g = geos[lo];
   const int tx = (g.ncol + 31) / 32, ty = (g.nrow + 7) / 8;
   const int lt = t - g.ptile0;
@@ -444,8 +452,8 @@ __global__ void k_dia7_permute(const Dia7Geo *__restrict__ geos, int nm, const T
   const int gg = ((DIR > 0) ? j : (g.ncol - 1 - j)) + S * l;
   const long long sk = g.slot0 + (((long long)k * g.nb + b) * g.G + gg) * W + l;
   const long long nat = g.row0 + ((long long)k * g.nrow + i) * g.ncol + j;
-  if (DIR > 0) dst[sk] = src[nat];  // skew (forward input)
-  else dst[nat] = src[sk];          // unskew (backward output)
+  if (DIR > 0) dst[sk] = (TD)src[nat];  // skew (forward input)
+  else dst[nat] = (TD)src[sk];          // unskew (backward output)
 }
 
 // APC/JAPC -> skewed tiles.  Forward tiles hold Lz, Ly, Lx of the cell that
@@ -502,11 +510,27 @@ __global__ void k_dia7_extract(const Dia7Geo *__restrict__ geos, int nm, long lo
 }
 
 // Wavefront shape per precision: lines per block W, lane skew S, chunk C,
-// buffers NS.
+// buffers NS.  The FP64 shape can be set at build time (GB_DIA64_W/S/NS) to
+// tune it on a new part; W <= 32 (one warp), S >= 1, C a multiple of 2.
+// Measured on GB300 (10M-cell case, one ILU0 application): W16/S2 1.83 ms,
+// W16/S1 1.50 ms, W32/S1 (NS 4, three CTAs per SM) 1.20 ms -- the sweep is
+// bound by the hand-off chain, so fewer, wider blocks win although each
+// step then carries the y-term shuffle on its dependency chain.
+#ifndef GB_DIA64_W
+#define GB_DIA64_W 32
+#endif
+#ifndef GB_DIA64_S
+#define GB_DIA64_S 1
+#endif
+#ifndef GB_DIA64_NS
+#define GB_DIA64_NS 4
+#endif
 template <typename T>
 struct Shape;
 template <>
-struct Shape<double> { static constexpr int W = 16, S = 2, C = 8, NS = 5; };
+struct Shape<double> {
+  static constexpr int W = GB_DIA64_W, S = GB_DIA64_S, C = 8, NS = GB_DIA64_NS;
+};
 template <>
 struct Shape<float> { static constexpr int W = 32, S = 1, C = 8, NS = 5; };
 
@@ -516,8 +540,9 @@ constexpr size_t stage_bytes() {
   return P::NS * sizeof(Stage<T, P::W, P::C>) + kOut * P::C * P::W * sizeof(T) +
          3 * P::NS * sizeof(unsigned long long);
 }
-static_assert(stage_bytes<double>() < 48 * 1024, "FP64 stage ring too large");
-static_assert(stage_bytes<float>() < 48 * 1024, "FP32 stage ring too large");
+static_assert(Shape<double>::W <= 32 && Shape<double>::S >= 1, "FP64 wavefront shape");
+static_assert(stage_bytes<double>() <= 200 * 1024, "FP64 stage ring too large");
+static_assert(stage_bytes<float>() <= 200 * 1024, "FP32 stage ring too large");
 
 }  // namespace
 
@@ -614,8 +639,11 @@ void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_j
   }
 }
 
-template <typename T>
-static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, T *ysk, T *zsk, const T *r, T *z,
+// One ILU0 application on the skewed layout: skew r (natural order, type TV)
+// into the sweep type T, forward and backward wavefront sweeps, unskew z
+// back to TV (TV = double, T = float: FP32 factors inside FP64 vectors).
+template <typename T, typename TV = T>
+static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, T *ysk, T *zsk, const TV *r, TV *z,
                     const Ctl *ctl, cudaStream_t st) {
   using P = Shape<T>;
   const int nct = D.ntickets;
@@ -625,16 +653,27 @@ static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, T *ysk, T *zsk, 
   SweepArgs<T> a;
   a.geo = D.d_geo;
   a.nm = D.nm;
+  a.mctl = D.mctl;
   a.rsk = rsk; a.ysk = ysk; a.zsk = zsk;
   a.flags = D.d_flags; a.err = D.d_err; a.ctl = const_cast<Ctl *>(ctl);
   a.A = arr[0]; a.B = arr[1]; a.X = arr[2]; a.D = nullptr;
-  k_dia7_permute<T, P::W, P::S, 1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, r, rsk, ctl);
+  if (sm > 48 * 1024) {  // opt in to more than 48 KB of dynamic shared memory, once
+    static bool opted = false;
+    if (!opted) {
+      cudaFuncSetAttribute(k_dia7_sweep<T, P::W, P::S, P::C, P::NS, 1>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      cudaFuncSetAttribute(k_dia7_sweep<T, P::W, P::S, P::C, P::NS, -1>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      opted = true;
+    }
+  }
+  k_dia7_permute<TV, T, P::W, P::S, 1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, r, rsk, ctl, D.mctl);
   cudaMemsetAsync(D.d_flags, 0, fbytes, st);
   k_dia7_sweep<T, P::W, P::S, P::C, P::NS, 1><<<nct, 128, sm, st>>>(a);
   a.A = arr[3]; a.B = arr[4]; a.X = arr[5]; a.D = arr[6];
   cudaMemsetAsync(D.d_flags, 0, fbytes, st);
   k_dia7_sweep<T, P::W, P::S, P::C, P::NS, -1><<<nct, 128, sm, st>>>(a);
-  k_dia7_permute<T, P::W, P::S, -1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, zsk, z, ctl);
+  k_dia7_permute<T, TV, P::W, P::S, -1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, zsk, z, ctl, D.mctl);
 }
 
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
@@ -643,10 +682,11 @@ void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *c
   apply_t<double>(D, arr, D.d_rsk, D.d_ysk, D.d_zsk, r, z, ctl, st);
 }
 
-void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
-                         cudaStream_t st) {
+
+void launch_dia7_apply_mixed(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
+                             cudaStream_t st) {
   const float *arr[7] = {D.f_lz, D.f_ly, D.f_lx, D.f_uz, D.f_uy, D.f_ux, D.f_dinv};
-  apply_t<float>(D, arr, D.f_rsk, D.f_ysk, D.f_zsk, r, z, ctl, st);
+  apply_t<float, double>(D, arr, D.f_rsk, D.f_ysk, D.f_zsk, r, z, ctl, st);
 }
 
 }  // namespace gb

@@ -89,6 +89,16 @@ __device__ __forceinline__ void block_maxloc(MaxLoc (&m)[NM]) {
 __device__ __forceinline__ double to_d(double v) { return v; }
 __device__ __forceinline__ double to_d(float v) { return (double)v; }
 
+// 1 if v is Inf or NaN, tested on the exponent bits with integer
+// instructions: on GB300 every FP64 instruction (a compare included) goes
+// through the narrow FP64 pipe, which bounds the vector updates otherwise.
+__device__ __forceinline__ unsigned nonfinite(double v) {
+  return ((unsigned)__double2hiint(v) & 0x7ff00000u) == 0x7ff00000u;
+}
+__device__ __forceinline__ unsigned nonfinite(float v) {
+  return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u;
+}
+
 // ---------------------------------------------------------------------------
 // dot products: partial[b] (and partial[G+b])
 // ---------------------------------------------------------------------------
@@ -238,15 +248,6 @@ __global__ void k_ctl_alpha(Ctl *ctl, const double *part, int G) {
   ctl_alpha(ctl, part, G);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_cg_pupdate(int n, const T *__restrict__ z, T *__restrict__ p,
-                                                    const Ctl *__restrict__ ctl) {
-  if (ctl->done) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (ctl->first) p[i] = z[i];
-  else p[i] = (T)fma((double)(T)ctl->beta, (double)p[i], (double)z[i]);
-}
 
 __global__ void __launch_bounds__(256) k_cg_pupdate64(int n, const double *__restrict__ z,
                                                       double *__restrict__ p,
@@ -257,14 +258,6 @@ __global__ void __launch_bounds__(256) k_cg_pupdate64(int n, const double *__res
   p[i] = ctl->first ? z[i] : fma(ctl->beta, p[i], z[i]);
 }
 
-__global__ void __launch_bounds__(256) k_cg_pupdate32(int n, const float *__restrict__ z,
-                                                      float *__restrict__ p,
-                                                      const Ctl *__restrict__ ctl) {
-  if (ctl->done) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  p[i] = ctl->first ? z[i] : fmaf((float)ctl->beta, p[i], z[i]);
-}
 
 // x += alpha*p ; d -= alpha*q ; max|alpha p|, max|d|, sum d^2 (FP64 path).
 // partial slots: [0]=l2, [1]=dx val, [2]=dx idx, [3]=r val, [4]=r idx, [5]=nonfinite
@@ -277,6 +270,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__rest
   if (ctl->done) return;
   const double alpha = ctl->alpha;
   double v[2] = {0.0, 0.0};
+  unsigned nf = 0;
   MaxLoc m[2];
   m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
   auto row = [&](int i, double pi, double xi, double qi, double dI) {
@@ -287,7 +281,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__rest
     d[i] = di;
     if (absgt(di, m[1].val)) { m[1].val = di; m[1].idx = i; }
     v[0] = fma(di, di, v[0]);
-    if (!isfinite(di) || !isfinite(tv)) v[1] += 1.0;
+    nf |= nonfinite(di) | nonfinite(tv);
   };
   // two rows per trip, loads first (same order of rows as one per trip)
   const int stride = gridDim.x * blockDim.x;
@@ -300,6 +294,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__rest
     row(j, p1, x1, q1, d1);
   }
   if (i < n) row(i, p[i], x[i], q[i], d[i]);
+  v[1] = (double)nf;
   block_sum<2>(v);
   block_maxloc<2>(m);
   if (threadIdx.x == 0) {
@@ -311,52 +306,6 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__rest
   }
 }
 
-// Mixed inner update: x (FP64) += alpha*p (FP32 promoted); d32 -= alpha*q32.
-__global__ void __launch_bounds__(kRedBlock) k_cg_update_mixed(int n, double *__restrict__ x,
-                                                                float *__restrict__ d,
-                                                                const float *__restrict__ p,
-                                                                const float *__restrict__ q,
-                                                                double *__restrict__ part,
-                                                                const Ctl *__restrict__ ctl) {
-  if (ctl->done) return;
-  const double alpha = ctl->alpha;
-  const float alphaf = (float)alpha;
-  double v[2] = {0.0, 0.0};
-  MaxLoc m[2];
-  m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
-  auto row = [&](int i, float pi, double xi, float qi, float dI) {
-    double tv = alpha * (double)pi;
-    x[i] = xi + tv;
-    if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i; }
-    float di = fmaf(-alphaf, qi, dI);
-    d[i] = di;
-    double dd = (double)di;
-    if (absgt(dd, m[1].val)) { m[1].val = dd; m[1].idx = i; }
-    v[0] = fma(dd, dd, v[0]);
-    if (!isfinite(di) || !isfinite(tv)) v[1] += 1.0;
-  };
-  const int stride = gridDim.x * blockDim.x;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + stride < n; i += 2 * stride) {
-    const int j = i + stride;
-    const float p0 = p[i], q0 = q[i], d0 = d[i];
-    const double x0 = x[i];
-    const float p1 = p[j], q1 = q[j], d1 = d[j];
-    const double x1 = x[j];
-    row(i, p0, x0, q0, d0);
-    row(j, p1, x1, q1, d1);
-  }
-  if (i < n) row(i, p[i], x[i], q[i], d[i]);
-  block_sum<2>(v);
-  block_maxloc<2>(m);
-  if (threadIdx.x == 0) {
-    int G = gridDim.x, b = blockIdx.x;
-    part[b] = v[0];
-    part[G + b] = m[0].val; part[2 * G + b] = (double)m[0].idx;
-    part[3 * G + b] = m[1].val; part[4 * G + b] = (double)m[1].idx;
-    part[5 * G + b] = v[1];
-  }
-}
 
 // Finalise an update reduction into ctl (deltax, rmax, l2norm, nonfinite).
 __device__ void ctl_finish_update(Ctl *ctl, const double *part, int G) {
@@ -491,6 +440,7 @@ __global__ void __launch_bounds__(kRedBlock) k_bcgs_update(int n, double *__rest
   const double alpha = ctl->alpha, omega = ctl->omega;
   const T omegat = (T)omega;
   double v[2] = {0.0, 0.0};
+  unsigned nf = 0;
   MaxLoc m[2];
   m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -504,8 +454,9 @@ __global__ void __launch_bounds__(kRedBlock) k_bcgs_update(int n, double *__rest
     if (dscale) rv = rv / dscale[i];
     if (absgt(rv, m[1].val)) { m[1].val = rv; m[1].idx = i; }
     v[0] = fma(rv, rv, v[0]);
-    if (!isfinite(rv) || !isfinite(tv)) v[1] += 1.0;
+    nf |= nonfinite(rv) | nonfinite(tv);
   }
+  v[1] = (double)nf;
   block_sum<2>(v);
   block_maxloc<2>(m);
   if (threadIdx.x == 0) {
@@ -599,11 +550,10 @@ __device__ void ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
   }
   if (icnvg != 0 || ctl->l2norm <= refine_factor * ctl->scratch[0] || stag || zero) {
     ctl->north_due = 2;  // request the FP64 true residual
-    // Every refinement restarts the recurrence from the true residual: with
-    // FP32 search directions, continuing after a residual replacement costs
-    // more iterations than a restart (measured on the 10M-cell case)
-    (void)bcgs;
-    ctl->restart_due = 1;
+    // BiCGSTAB restarts from the true residual at every refinement (its
+    // shadow residual is tied to the recurrence); PCG keeps its search
+    // direction unless it stagnated or broke down
+    ctl->restart_due = (bcgs || stag || zero) ? 1 : 0;
     ctl->scratch[1] = ctl->deltax;
     ctl->scratch[2] = (double)ctl->xloc;
   }
@@ -632,22 +582,28 @@ __global__ void k_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
 __global__ void __launch_bounds__(kRedBlock) k_true_resid_stats(int n, const double *__restrict__ r,
                                                                  float *__restrict__ d32,
                                                                  float *__restrict__ dhat32,
+                                                                 double *__restrict__ dhat64,
                                                                  const double *__restrict__ dscale,
                                                                  double *__restrict__ part,
                                                                  const Ctl *__restrict__ ctl) {
   if (ctl->done || ctl->north_due != 2) return;
   double v[2] = {0.0, 0.0};
+  unsigned nf = 0;
   MaxLoc m[2];
   m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double ri = r[i];
-    d32[i] = (float)ri;
-    if (dhat32 && ctl->restart_due) dhat32[i] = (float)ri;  // BiCGSTAB shadow, on a restart
+    if (d32) d32[i] = (float)ri;
+    if (ctl->restart_due) {  // BiCGSTAB shadow residual, on a restart
+      if (dhat32) dhat32[i] = (float)ri;
+      if (dhat64) dhat64[i] = ri;
+    }
     if (dscale) ri = ri / dscale[i];    // BiCGSTAB reports the unscaled residual
     if (absgt(ri, m[1].val)) { m[1].val = ri; m[1].idx = i; }
     v[0] = fma(ri, ri, v[0]);
-    if (!isfinite(ri)) v[1] += 1.0;
+    nf |= nonfinite(ri);
   }
+  v[1] = (double)nf;
   block_sum<2>(v);
   block_maxloc<2>(m);
   if (threadIdx.x == 0) {
@@ -690,10 +646,10 @@ __device__ void ctl_refine(Ctl *ctl, const double *part, int G, unsigned long lo
     ctl->done = 1;
     ctl->exit_reason = kExitItmax;
   } else {
-    // The FP32 recurrence residual is replaced by the FP64 true residual and
-    // the recurrence restarts from it (restart_due); a recurrence that
-    // carried on instead, like the reference's NORTH residual refresh
-    // (ImsLinearBase.f90:221-227), would keep its search direction.
+    // The recurrence residual (of the FP32 matrix) is replaced by the FP64
+    // true residual.  PCG carries on with its search direction, like the
+    // reference's NORTH residual refresh (ImsLinearBase.f90:221-227);
+    // BiCGSTAB, and PCG after a stagnation or breakdown, restart from it.
     ctl->scratch[0] = ctl->l2norm;
     ctl->scratch[3] += 1.0;  // refinement count
     if (ctl->restart_due) {
@@ -817,6 +773,7 @@ __global__ void __launch_bounds__(kRedBlock) k_b_cg_update64(BatchDev B, double 
   if (ctl.done) return;
   const double alpha = ctl.alpha;
   double v[2] = {0.0, 0.0};
+  unsigned nf = 0;
   MaxLoc m[2];
   m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
   const int row0 = B.mr[c.m];  // member-local row numbers for the maxima
@@ -828,8 +785,9 @@ __global__ void __launch_bounds__(kRedBlock) k_b_cg_update64(BatchDev B, double 
     d[i] = di;
     if (absgt(di, m[1].val)) { m[1].val = di; m[1].idx = i - row0; }
     v[0] = fma(di, di, v[0]);
-    if (!isfinite(di) || !isfinite(tv)) v[1] += 1.0;
+    nf |= nonfinite(di) | nonfinite(tv);
   }
+  v[1] = (double)nf;
   block_sum<2>(v);
   block_maxloc<2>(m);
   if (threadIdx.x == 0) {
@@ -939,14 +897,8 @@ static inline int egrid(int n) { return std::max(1, (n + 255) / 256); }
 void kr_dot64(int n, const double *a, const double *b, double *part, int G, const Ctl *ctl, cudaStream_t st) {
   k_dot<double, double><<<G, kRedBlock, 0, st>>>(n, a, b, part, ctl);
 }
-void kr_dot32(int n, const float *a, const float *b, double *part, int G, const Ctl *ctl, cudaStream_t st) {
-  k_dot<float, float><<<G, kRedBlock, 0, st>>>(n, a, b, part, ctl);
-}
 void kr_dot_tq_tt64(int n, const double *t, const double *q, double *part, int G, const Ctl *ctl, cudaStream_t st) {
   k_dot_tq_tt<double><<<G, kRedBlock, 0, st>>>(n, t, q, part, ctl);
-}
-void kr_dot_tq_tt32(int n, const float *t, const float *q, double *part, int G, const Ctl *ctl, cudaStream_t st) {
-  k_dot_tq_tt<float><<<G, kRedBlock, 0, st>>>(n, t, q, part, ctl);
 }
 void kr_sumsq64(int n, const double *a, double *part, int G, cudaStream_t st) {
   k_sumsq<double><<<G, kRedBlock, 0, st>>>(n, a, part);
@@ -963,16 +915,9 @@ void kr_ctl_alpha(Ctl *ctl, const double *part, int G, cudaStream_t st) {
 void kr_cg_pupdate64(int n, const double *z, double *p, const Ctl *ctl, cudaStream_t st) {
   k_cg_pupdate64<<<egrid(n), 256, 0, st>>>(n, z, p, ctl);
 }
-void kr_cg_pupdate32(int n, const float *z, float *p, const Ctl *ctl, cudaStream_t st) {
-  k_cg_pupdate32<<<egrid(n), 256, 0, st>>>(n, z, p, ctl);
-}
 void kr_cg_update64(int n, double *x, double *d, const double *p, const double *q, double *part,
                     int G, const Ctl *ctl, cudaStream_t st) {
   k_cg_update64<<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
-}
-void kr_cg_update_mixed(int n, double *x, float *d, const float *p, const float *q, double *part,
-                        int G, const Ctl *ctl, cudaStream_t st) {
-  k_cg_update_mixed<<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
 }
 void kr_ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
                     cudaStream_t st) {
@@ -984,14 +929,8 @@ void kr_ctl_bcgs_rho(Ctl *ctl, const double *part, int G, cudaStream_t st) {
 void kr_bcgs_p64(int n, const double *d, double *p, const double *v, const Ctl *ctl, cudaStream_t st) {
   k_bcgs_p<double><<<egrid(n), 256, 0, st>>>(n, d, p, v, ctl);
 }
-void kr_bcgs_p32(int n, const float *d, float *p, const float *v, const Ctl *ctl, cudaStream_t st) {
-  k_bcgs_p<float><<<egrid(n), 256, 0, st>>>(n, d, p, v, ctl);
-}
 void kr_bcgs_q64(int n, const double *d, const double *v, double *q, const Ctl *ctl, cudaStream_t st) {
   k_bcgs_q<double><<<egrid(n), 256, 0, st>>>(n, d, v, q, ctl);
-}
-void kr_bcgs_q32(int n, const float *d, const float *v, float *q, const Ctl *ctl, cudaStream_t st) {
-  k_bcgs_q<float><<<egrid(n), 256, 0, st>>>(n, d, v, q, ctl);
 }
 void kr_ctl_omega(Ctl *ctl, const double *part, int G, cudaStream_t st) {
   k_ctl_omega<<<1, kRedBlock, 0, st>>>(ctl, part, G);
@@ -1001,11 +940,6 @@ void kr_bcgs_update64(int n, double *x, double *d, const double *phat, const dou
                       const Ctl *ctl, cudaStream_t st) {
   k_bcgs_update<double><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
 }
-void kr_bcgs_update32(int n, double *x, float *d, const float *phat, const float *qhat,
-                      const float *q, const float *t, const double *dscale, double *part, int G,
-                      const Ctl *ctl, cudaStream_t st) {
-  k_bcgs_update<float><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
-}
 void kr_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
                       cudaStream_t st) {
   k_ctl_bcgs_cnvg<<<1, kRedBlock, 0, st>>>(ctl, part, G, cond, use_cond);
@@ -1014,9 +948,10 @@ void kr_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs, double re
                         cudaStream_t st) {
   k_ctl_mixed_inner<<<1, kRedBlock, 0, st>>>(ctl, part, G, bcgs, refine_factor);
 }
-void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, const double *dscale,
-                         double *part, int G, const Ctl *ctl, cudaStream_t st) {
-  k_true_resid_stats<<<G, kRedBlock, 0, st>>>(n, r, d32, dhat32, dscale, part, ctl);
+void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, double *dhat64,
+                         const double *dscale, double *part, int G, const Ctl *ctl,
+                         cudaStream_t st) {
+  k_true_resid_stats<<<G, kRedBlock, 0, st>>>(n, r, d32, dhat32, dhat64, dscale, part, ctl);
 }
 void kr_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
                    cudaStream_t st) {

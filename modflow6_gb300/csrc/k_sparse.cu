@@ -73,15 +73,20 @@ __device__ __forceinline__ double mac<double>(double a, double x, double t) { re
 template <>
 __device__ __forceinline__ float mac<float>(float a, float x, float t) { return fmaf(a, x, t); }
 
-// y = A*x (MODE 0), or d = b - A*x (MODE 1).
-template <typename T, int MODE>
+// y = A*x (MODE 0), or d = b - A*x (MODE 1).  Matrix values TM, vectors and
+// accumulation T (TM = float, T = double: the mixed form's FP32 matrix with
+// FP64 vectors).
+template <typename T, int MODE, typename TM = T>
 __global__ void __launch_bounds__(256) k_sell_spmv(int n, const int *__restrict__ ptr,
                                                     const int *__restrict__ col,
-                                                    const T *__restrict__ val,
+                                                    const TM *__restrict__ val,
                                                     const T *__restrict__ x,
                                                     const T *__restrict__ b, T *__restrict__ y,
                                                     const Ctl *__restrict__ ctl,
-                                                    int only_if_north_due) {
+                                                    int only_if_north_due,
+                                                    const int *__restrict__ slm,
+                                                    const int *__restrict__ mrow, int nm,
+                                                    const Ctl *__restrict__ mctl) {
   if (ctl) {
     if (ctl->done) return;
     if (only_if_north_due && !ctl->north_due) return;
@@ -89,15 +94,28 @@ __global__ void __launch_bounds__(256) k_sell_spmv(int n, const int *__restrict_
   int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= n) return;
   int s = row / kSell, lane = row % kSell;
+  if (mctl) {  // batched ensemble: rows of a member that is done are skipped
+    int m = slm[s];
+    if (m < 0) {
+      int lo = 0, hi = nm - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (mrow[mid] <= row) lo = mid;
+        else hi = mid - 1;
+      }
+      m = lo;
+    }
+    if (mctl[m].done) return;
+  }
   int p0 = ptr[s];
   int w = (ptr[s + 1] - p0) / kSell;
   const int *c = col + p0 + lane;
-  const T *v = val + p0 + lane;
+  const TM *v = val + p0 + lane;
   T t = T(0);
   if (w <= 8) {
     // the common 5/7-point case: issue all loads first, then the gathers
     int cc[8];
-    T vv[8];
+    TM vv[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       if (k < w) {
@@ -111,9 +129,10 @@ __global__ void __launch_bounds__(256) k_sell_spmv(int n, const int *__restrict_
       if (k < w) xx[k] = __ldg(x + cc[k]);
 #pragma unroll
     for (int k = 0; k < 8; ++k)
-      if (k < w) t = mac<T>(vv[k], xx[k], t);
+      if (k < w) t = mac<T>((T)vv[k], xx[k], t);
   } else {
-    for (int k = 0; k < w; ++k) t = mac<T>(ld_stream(v + k * kSell), __ldg(x + ld_stream(c + k * kSell)), t);
+    for (int k = 0; k < w; ++k)
+      t = mac<T>((T)ld_stream(v + k * kSell), __ldg(x + ld_stream(c + k * kSell)), t);
   }
   if (MODE == 0) y[row] = t;
   else y[row] = b[row] - t;
@@ -148,9 +167,9 @@ __global__ void k_dia7_vfill(int nlay, int nrow, int ncol, const int *__restrict
   }
 }
 
-template <typename T, int MODE>
+template <typename T, int MODE, typename TM = T>
 __global__ void __launch_bounds__(256) k_dia7_spmv(int nlay, int nrow, int ncol,
-                                                   const T *__restrict__ v,
+                                                   const TM *__restrict__ v,
                                                    const T *__restrict__ x,
                                                    const T *__restrict__ b, T *__restrict__ y,
                                                    const Ctl *__restrict__ ctl,
@@ -167,7 +186,8 @@ __global__ void __launch_bounds__(256) k_dia7_spmv(int nlay, int nrow, int ncol,
   const int i = rem / ncol, j = rem - i * ncol;
   const bool has[7] = {true, k > 0, i > 0, j > 0, j < ncol - 1, i < nrow - 1, k < nlay - 1};
   const int off[7] = {0, -nrc, -ncol, -1, 1, ncol, nrc};
-  T vv[7], xx[7];
+  TM vv[7];
+  T xx[7];
 #pragma unroll
   for (int s = 0; s < 7; ++s)
     if (has[s]) vv[s] = ld_stream(v + (size_t)s * n + r);
@@ -177,7 +197,7 @@ __global__ void __launch_bounds__(256) k_dia7_spmv(int nlay, int nrow, int ncol,
   T t = T(0);
 #pragma unroll
   for (int s = 0; s < 7; ++s)
-    if (has[s]) t = mac<T>(vv[s], xx[s], t);
+    if (has[s]) t = mac<T>((T)vv[s], xx[s], t);
   if (MODE == 0) y[r] = t;
   else y[r] = b[r] - t;
 }
@@ -195,11 +215,12 @@ void launch_dia7_spmv64(const Dia7 &D, const double *x, double *y, const Ctl *ct
                                                         nullptr, y, ctl, 0);
 }
 
-void launch_dia7_spmv32(const Dia7 &D, const float *x, float *y, const Ctl *ctl,
-                        cudaStream_t st) {
+
+void launch_dia7_spmv_mixed(const Dia7 &D, const double *x, double *y, const Ctl *ctl,
+                            cudaStream_t st) {
   const int n = D.nlay * D.nrow * D.ncol;
-  k_dia7_spmv<float, 0><<<rows_grid(n), 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.f_sv, x,
-                                                       nullptr, y, ctl, 0);
+  k_dia7_spmv<double, 0, float><<<rows_grid(n), 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.f_sv, x,
+                                                               nullptr, y, ctl, 0);
 }
 
 void launch_dia7_residual64(const Dia7 &D, const double *x, const double *b, double *d,
@@ -212,20 +233,24 @@ void launch_dia7_residual64(const Dia7 &D, const double *x, const double *b, dou
 void launch_spmv64(const Sell &S, const double *x, double *y, const Ctl *ctl, cudaStream_t st) {
   if (S.n == 0) return;
   k_sell_spmv<double, 0><<<rows_grid(S.n), 256, 0, st>>>(S.n, S.d_ptr, S.d_col, S.d_val, x,
-                                                          nullptr, y, ctl, 0);
+                                                          nullptr, y, ctl, 0, S.d_slm, S.d_mrow,
+                                                          S.nm, S.mctl);
 }
 
-void launch_spmv32(const Sell &S, const float *x, float *y, const Ctl *ctl, cudaStream_t st) {
+
+void launch_spmv_mixed(const Sell &S, const double *x, double *y, const Ctl *ctl, cudaStream_t st) {
   if (S.n == 0) return;
-  k_sell_spmv<float, 0><<<rows_grid(S.n), 256, 0, st>>>(S.n, S.d_ptr, S.d_col, S.d_val32, x,
-                                                         nullptr, y, ctl, 0);
+  k_sell_spmv<double, 0, float><<<rows_grid(S.n), 256, 0, st>>>(S.n, S.d_ptr, S.d_col, S.d_val32,
+                                                                x, nullptr, y, ctl, 0, S.d_slm,
+                                                                S.d_mrow, S.nm, S.mctl);
 }
 
 void launch_residual64(const Sell &S, const double *x, const double *b, double *d,
                        const Ctl *ctl, int only_if_north_due, cudaStream_t st) {
   if (S.n == 0) return;
   k_sell_spmv<double, 1><<<rows_grid(S.n), 256, 0, st>>>(S.n, S.d_ptr, S.d_col, S.d_val, x, b,
-                                                          d, ctl, only_if_north_due);
+                                                          d, ctl, only_if_north_due, S.d_slm,
+                                                          S.d_mrow, S.nm, S.mctl);
 }
 
 }  // namespace gb

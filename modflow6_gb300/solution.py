@@ -119,10 +119,17 @@ class GwfSolution:
             raise _lib.GbimsError(rc, msg)
         self.nodes = m.nodes
 
-    def timestep(self, kper: int = 1, kstp: int = 1, delt: float = 1.0) -> dict:
+    def timestep(self, kper: int = 1, kstp: int = 1, delt: float = 1.0, guess=None) -> dict:
+        """One time step to closure.  `guess`: optional device address (int)
+        of a float64 array of initial heads for the active cells (a warm
+        start, gbsln_timestep_guess); the previous heads stay the storage
+        reference."""
         lib = _lib.load()
         st = _lib.GbslnStats()
-        rc = lib.gbsln_timestep(self._h, kper, kstp, delt, C.byref(st))
+        if guess is None:
+            rc = lib.gbsln_timestep(self._h, kper, kstp, delt, C.byref(st))
+        else:
+            rc = lib.gbsln_timestep_guess(self._h, kper, kstp, delt, C.c_void_p(guess), C.byref(st))
         if rc < 0:
             raise _lib.GbimsError(rc, lib.gbsln_last_error(self._h).decode())
         return {f: getattr(st, f) for f, _ in st._fields_}

@@ -1,0 +1,298 @@
+"""Learned warm start for transient time steps (gbmpnn_* + gbsln_timestep_guess).
+
+MODFLOW 6 starts every time step's outer loop from the previous heads.  Here
+a message-passing network over the graph of the IMS matrix (hidden width 64,
+8 layers, BF16 tensor-core GEMMs, trained on the GPU by the library's own
+forward and backward kernels) predicts the head change of the step from the
+cell's K, the previous heads, the previous step's head change, the well
+rates and the boundary mask.  The
+prediction is only an initial guess: PCG + ILU0 still runs to the same
+INNER_DVCLOSE / INNER_RCLOSE closure, so the plain solver stays the judge.
+A guess that costs more inner iterations than the previous heads is
+discarded (the fallback rule `evaluate` reports).
+
+`Graph.features` builds the 16 input features of the cells, `generate` the
+training samples (heads from the plain solver), `WarmStartNet` wraps the C
+ABI, `train` runs Adam on the GPU and `evaluate` compares inner iterations
+with and without the network on held-out models.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .dis import GwfDisModel, make_config
+from .ims import ImsLinearSettings
+from .solution import GwfSolution, Nonlinear
+
+NFEAT = 16
+HEAD_REF, HEAD_SCALE = 22.5, 5.0   # c5 CHD heads are 25 m (west) and 20 m (east)
+Q_SCALE = 100.0                    # well rate scale, m3/d
+DH_SOFT = 0.01                     # m: head changes are learnt as asinh(dh / DH_SOFT)
+
+
+def to_unit(dh):
+    """Head change (m) -> network units: asinh(dh / DH_SOFT), so that the
+    error of a prediction scales with the size of the change (near-zero far
+    from the wells, relative near them) instead of being spread evenly."""
+    import torch
+    return torch.asinh(dh / DH_SOFT)
+
+
+def from_unit(y):
+    import torch
+    return torch.sinh(y) * DH_SOFT
+
+
+class Graph:
+    """Static per-model inputs on the device: standardised ln K, well rate,
+    CHD mask, layer position, the active-cell mask and the CSR pattern."""
+
+    def __init__(self, m: GwfDisModel, device="cuda"):
+        import torch
+
+        self.m = m
+        n = m.nodes
+        lnk = np.log(m.k11)
+        lnk = (lnk - lnk.mean()) / (lnk.std() + 1e-12)
+        q = np.zeros(n)
+        np.add.at(q, m.wel_node, m.wel_q)
+        chd = np.zeros(n)
+        chd[m.chd_node] = 1.0
+        lay = np.repeat(np.arange(m.nlay) / max(1, m.nlay - 1), m.nrow * m.ncol)
+        static = np.zeros((n, NFEAT), np.float32)
+        static[:, 0] = lnk
+        static[:, 2] = q / Q_SCALE
+        static[:, 3] = chd
+        static[:, 4] = lay
+        static[:, 5] = 1.0
+        self.static = torch.from_numpy(static).to(device)
+        self.active = torch.from_numpy((m.ibound > 0).astype(np.float32)).to(device)
+        self.active64 = self.active.double()
+        con = m.connections()
+        self.ia, self.ja = con["ia"], con["ja"]
+        self.nja = int(con["nja"])
+
+    def features(self, h_prev, dh_prev, dh_scale: float):
+        """Device float64 previous heads and previous step's head change
+        (nodes) -> float32 features (nodes x 16)."""
+        x = self.static.clone()
+        x[:, 1] = ((h_prev - HEAD_REF) / HEAD_SCALE).float()
+        x[:, 6] = (to_unit(dh_prev) / dh_scale).float()
+        return x
+
+
+def c5_model(seed: int, scale: float = 1.0) -> GwfDisModel:
+    return make_config("c5", seed=seed, scale=scale)
+
+
+C5_IMS = dict(dvclose=1e-6, rclose=1e-4, iter1=2000, ilinmeth=1)
+C5_DELT = 0.5      # days per time step
+C5_STEPS = 20
+
+
+def new_solution(m: GwfDisModel) -> GwfSolution:
+    return GwfSolution(m, ImsLinearSettings(structure=(m.nlay, m.nrow, m.ncol), **C5_IMS),
+                       Nonlinear(dvclose=C5_IMS["dvclose"], mxiter=25))
+
+
+@dataclass
+class Sample:
+    x: object        # features (device, nodes x 16, float32)
+    target: object   # scaled head change (device, nodes, float32)
+
+
+def generate(seeds, steps: int = C5_STEPS, scale: float = 1.0, delt: float = C5_DELT):
+    """Training data from the plain solver: per model its Graph, its
+    assembled matrix (device, for the edge weights) and one Sample per step,
+    and the scale (standard deviation over the active cells of every step of
+    the asinh-transformed head change) that normalises the targets and the
+    previous-change feature."""
+    import torch
+
+    runs = []
+    for s in seeds:
+        m = c5_model(s, scale)
+        g = Graph(m)
+        sol = new_solution(m)
+        amat, _ = sol.formulate(delt, hold=m.strt)
+        d_amat = torch.from_numpy(amat).cuda()
+        hs = [torch.from_numpy(sol.heads).cuda()]
+        for kstp in range(1, steps + 1):
+            sol.timestep(1, kstp, delt)
+            hs.append(torch.from_numpy(sol.heads).cuda())
+        sol.close()
+        runs.append((g, d_amat, hs))
+    sq, cnt = 0.0, 0.0
+    for g, _, hs in runs:
+        for k in range(1, len(hs)):
+            d = to_unit(hs[k] - hs[k - 1]) * g.active64
+            sq += float((d * d).sum().item())
+            cnt += float(g.active64.sum().item())
+    dh_scale = max(1e-3, (sq / max(1.0, cnt)) ** 0.5)
+    data = []
+    for g, d_amat, hs in runs:
+        samples = []
+        for k in range(1, len(hs)):
+            dh_prev = hs[k - 1] - hs[k - 2] if k >= 2 else torch.zeros_like(hs[0])
+            x = g.features(hs[k - 1], dh_prev * g.active64, dh_scale)
+            t = (to_unit(hs[k] - hs[k - 1]) / dh_scale * g.active64).float()
+            samples.append(Sample(x, t))
+        data.append((g, d_amat, samples))
+    return data, dh_scale
+
+
+class WarmStartNet:
+    def __init__(self, g: Graph, seed: int = 0):
+        self._lib = _lib.load()
+        self._h = C.c_void_p()
+        ia = np.ascontiguousarray(g.ia, np.int32)
+        ja = np.ascontiguousarray(g.ja, np.int32)
+        rc = self._lib.gbmpnn_create(g.m.nodes, g.nja, _lib.iptr(ia), _lib.iptr(ja), seed,
+                                     C.byref(self._h))
+        if rc < 0:
+            raise _lib.GbimsError(rc, self._err())
+        self.nodes = g.m.nodes
+        self.nparams = int(self._lib.gbmpnn_param_count())
+        self.dh_scale = 1.0  # output scale in asinh units, set by training
+
+    def _err(self):
+        return self._lib.gbmpnn_last_error(self._h).decode() if self._h else ""
+
+    def _chk(self, rc):
+        if rc < 0:
+            raise _lib.GbimsError(rc, self._err())
+
+    def set_graph(self, d_amat):
+        self._chk(self._lib.gbmpnn_set_graph(self._h, C.c_void_p(d_amat.data_ptr())))
+
+    def predict(self, x):
+        import torch
+        y = torch.empty(self.nodes, dtype=torch.float32, device=x.device)
+        torch.cuda.synchronize()
+        self._chk(self._lib.gbmpnn_forward(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr())))
+        return y
+
+    def train_step(self, x, target, mask, lr: float) -> float:
+        import torch
+        inv = 1.0 / max(1.0, float(mask.sum().item()))
+        loss = C.c_float()
+        torch.cuda.synchronize()
+        self._chk(self._lib.gbmpnn_train_step(self._h, C.c_void_p(x.data_ptr()),
+                                              C.c_void_p(target.data_ptr()),
+                                              C.c_void_p(mask.data_ptr()), inv, lr, C.byref(loss)))
+        return loss.value
+
+    def gradients(self, x, target, mask, inv_count: float):
+        import torch
+        loss = C.c_float()
+        g = np.zeros(self.nparams, np.float32)
+        torch.cuda.synchronize()
+        self._chk(self._lib.gbmpnn_gradients(self._h, C.c_void_p(x.data_ptr()),
+                                             C.c_void_p(target.data_ptr()),
+                                             C.c_void_p(mask.data_ptr()), inv_count, C.byref(loss),
+                                             g.ctypes.data_as(C.POINTER(C.c_float))))
+        return loss.value, g
+
+    @property
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.nparams, np.float32)
+        self._chk(self._lib.gbmpnn_get_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))))
+        return p
+
+    @params.setter
+    def params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        self._chk(self._lib.gbmpnn_set_params(self._h, p.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def close(self):
+        if self._h:
+            self._lib.gbmpnn_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def train(net: WarmStartNet, data, dh_scale: float, epochs: int = 4,
+          lr: float = 1e-3) -> list[float]:
+    """Adam over every sample of every model, `epochs` times, the learning
+    rate halved each epoch; mean loss per epoch."""
+    net.dh_scale = dh_scale
+    hist = []
+    for ep in range(epochs):
+        tot, cnt = 0.0, 0
+        for g, d_amat, samples in data:
+            net.set_graph(d_amat)
+            for s in samples:
+                tot += net.train_step(s.x, s.target, g.active, lr * (0.5 ** ep))
+                cnt += 1
+        hist.append(tot / max(1, cnt))
+    return hist
+
+
+def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0,
+             delt: float = C5_DELT) -> dict:
+    """Held-out models: every step solved from the previous heads and, in a
+    second solution of the same model, from the network's guess, both to the
+    same closure.  Reported: inner iterations of both; the iterations with the
+    fallback rule (per step, the guess is discarded when it cost more
+    iterations than the previous heads); the RMS and maximum error of the
+    guess and of the previous heads against the converged heads; device time."""
+    import torch
+
+    it_prev, it_warm = [], []
+    rms_g, rms_p, max_g, max_p = [], [], [], []
+    ms_prev, ms_warm, ms_net = 0.0, 0.0, 0.0
+    converged = True
+    dsc = net.dh_scale
+    for s in seeds:
+        m = c5_model(s, scale)
+        g = Graph(m)
+        base, warm = new_solution(m), new_solution(m)
+        amat, _ = base.formulate(delt, hold=m.strt)
+        net.set_graph(torch.from_numpy(amat).cuda())
+        nact = float(g.active64.sum().item())
+        dh_last = torch.zeros(m.nodes, dtype=torch.float64, device="cuda")
+        for kstp in range(1, steps + 1):
+            st_b = base.timestep(1, kstp, delt)
+            h_prev = torch.from_numpy(warm.heads).cuda()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dh = from_unit(net.predict(g.features(h_prev, dh_last, dsc)).double() * dsc)
+            guess = (h_prev + dh * g.active64).contiguous()
+            e1.record()
+            e1.synchronize()
+            ms_net += e0.elapsed_time(e1)
+            st_w = warm.timestep(1, kstp, delt, guess=guess.data_ptr())
+            h_true = torch.from_numpy(warm.heads).cuda()
+            eg = (guess - h_true) * g.active64
+            ep = (h_prev - h_true) * g.active64
+            rms_g.append(float(torch.sqrt((eg * eg).sum() / nact).item()))
+            rms_p.append(float(torch.sqrt((ep * ep).sum() / nact).item()))
+            max_g.append(float(eg.abs().max().item()))
+            max_p.append(float(ep.abs().max().item()))
+            dh_last = (h_true - h_prev) * g.active64
+            it_prev.append(st_b["inner_total"])
+            it_warm.append(st_w["inner_total"])
+            ms_prev += st_b["total_ms"]
+            ms_warm += st_w["total_ms"]
+            converged = converged and st_b["converged"] == 1 and st_w["converged"] == 1
+        base.close()
+        warm.close()
+    ip, iw = np.array(it_prev), np.array(it_warm)
+    return {"models": len(seeds), "steps": int(ip.size), "all_converged": converged,
+            "inner_prev_heads": int(ip.sum()), "inner_warm": int(iw.sum()),
+            "inner_with_fallback": int(np.minimum(ip, iw).sum()),
+            "steps_guess_better": int((iw < ip).sum()), "steps_guess_worse": int((iw > ip).sum()),
+            "iteration_ratio": float(iw.sum() / max(1, ip.sum())),
+            "solve_ms_prev_heads": ms_prev, "solve_ms_warm": ms_warm, "inference_ms": ms_net,
+            "time_ratio": (ms_warm + ms_net) / max(1e-9, ms_prev),
+            "rms_err_guess": float(np.mean(rms_g)), "rms_err_prev_heads": float(np.mean(rms_p)),
+            "max_err_guess": float(np.max(max_g)), "max_err_prev_heads": float(np.max(max_p))}

@@ -10,7 +10,7 @@ ROOT = Path(__file__).resolve().parents[1]
 
 def header_symbols():
     text = (ROOT / "include" / "gbims.h").read_text()
-    return sorted(set(re.findall(r"\b(gb(?:ims|npf|sln)_[a-z_0-9]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(gb(?:ims|npf|sln|mpnn)_[a-z_0-9]+)\s*\(", text)))
 
 
 def test_header_symbols_bound_in_python():
