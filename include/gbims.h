@@ -283,6 +283,28 @@ int gbsln_timestep_guess(gbsln_handle *h, int kper, int kstp, double delt, const
  * the same system with its itestmat switch (NumericalSolution.f90:2581-2599). */
 int gbsln_formulate(gbsln_handle *h, double delt, const double *hold, double *amat, double *rhs);
 const char *gbsln_last_error(const gbsln_handle *h);
+
+/* Model budget of the last time step (or formulate): gwf_cq then gwf_bd
+ * (gwf.f90:741-830).  Rates in L^3/T, entries in the order STO-SS, STO-SY,
+ * CHD, WEL, RCH (sto_bd, then the packages, gwf-sto.f90:572-595,
+ * gwf-chd.f90:324-346, BoundaryPackage bnd_bd); the percent difference is
+ * that of Budget.f90:258-266. */
+typedef struct gbsln_budget_table {
+  double rate_in[5];
+  double rate_out[5];
+  double total_in, total_out;
+  double percent_discrepancy;  /* 100 (in - out) / ((in + out) / 2), 0 when in + out = 0 */
+  double max_cell_imbalance;   /* max over active cells of |FLOW-JA-FACE diagonal|, the
+                                  net of a cell's storage, boundary and face flows */
+  int max_cell;                /* 0-based node of that cell, -1 if none */
+} gbsln_budget_table;
+/* Cell-by-cell flows (npf_cq, gwf-npf.f90:745-770; sto_cq :447-564 of
+ * gwf-sto.f90; bnd_cq; csr_diagsum, Sparse.f90:262-281; calc_chd_rate,
+ * gwf-chd.f90:264-320) and the model budget at the current heads, with the
+ * saturation of the last formulate, as the reference computes them after
+ * a converged time step.  flowja: host array of nja values (FLOW-JA-FACE,
+ * CSR order; the diagonal holds the cell's net flow) or NULL. */
+int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table *out);
 /* Restores the initial heads (IC STRT) on the device: the state at the start
  * of the simulation, for repeated runs of the same model. */
 int gbsln_restart(gbsln_handle *h);

@@ -87,6 +87,14 @@ class GbslnStats(C.Structure):
     ]
 
 
+class GbslnBudgetTable(C.Structure):
+    _fields_ = [
+        ("rate_in", C.c_double * 5), ("rate_out", C.c_double * 5), ("total_in", C.c_double),
+        ("total_out", C.c_double), ("percent_discrepancy", C.c_double),
+        ("max_cell_imbalance", C.c_double), ("max_cell", C.c_int),
+    ]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "gbims_create": (C.c_int, [C.POINTER(GbimsSettings), C.c_int, C.c_int, _ip, _ip, C.POINTER(C.c_void_p)]),
@@ -124,6 +132,7 @@ _SIGS = {
     "gbsln_formulate": (C.c_int, [C.c_void_p, C.c_double, _dp, _dp, _dp]),
     "gbsln_last_error": (C.c_char_p, [C.c_void_p]),
     "gbsln_restart": (C.c_int, [C.c_void_p]),
+    "gbsln_budget": (C.c_int, [C.c_void_p, _dp, C.POINTER(GbslnBudgetTable)]),
     "gbsln_get_heads": (C.c_int, [C.c_void_p, _dp]),
     "gbsln_set_heads": (C.c_int, [C.c_void_p, _dp]),
     "gbsln_ims": (C.c_void_p, [C.c_void_p]),

@@ -94,17 +94,10 @@ static void precond64(gbims_handle *h, const double *r, double *z) {
   else launch_ilu_apply_levels(h->n, h->d_iapc, h->d_japc, h->d_apc, h->F, h->B, r, z, h->d_ctl, h->st);
 }
 
-// The mixed form's preconditioner: FP64 vectors, FP32 factors and FP32
-// sweeps (the skew/unskew permutes convert on the wavefront path).
-static void precond_mixed(gbims_handle *h, const double *r, double *z) {
-  if (h->structured) {
-    launch_dia7_apply_mixed(h->D, r, z, h->d_ctl, h->st);
-  } else {
-    kr_f64_to_f32(h->n, r, h->f_d, h->st);
-    launch_ilu_apply_levels32(h->n, h->d_iapc, h->d_japc, h->d_apc32, h->F, h->B, h->f_d, h->f_z,
-                              h->d_ctl, h->st);
-    kr_f32_to_f64(h->n, h->f_z, z, h->st);
-  }
+// The mixed form's preconditioner: FP32 factors, vectors and sweeps.
+static void precond32(gbims_handle *h, const float *r, float *z) {
+  if (h->structured) launch_dia7_apply32(h->D, r, z, h->d_ctl, h->st);
+  else launch_ilu_apply_levels32(h->n, h->d_iapc, h->d_japc, h->d_apc32, h->F, h->B, r, z, h->d_ctl, h->st);
 }
 
 // A*x and b - A*x: index-free on full DIS grids, SELL-32 otherwise.
@@ -113,10 +106,10 @@ static void spmv64(gbims_handle *h, const double *x, double *y, const Ctl *c) {
   else launch_spmv64(h->S, x, y, c, h->st);
 }
 
-// The mixed form's product: FP32 matrix values, FP64 vectors.
-static void spmv_mixed(gbims_handle *h, const double *x, double *y, const Ctl *c) {
-  if (h->dia_spmv) launch_dia7_spmv_mixed(h->D, x, y, c, h->st);
-  else launch_spmv_mixed(h->S, x, y, c, h->st);
+// The mixed form's product: FP32 matrix values and vectors.
+static void spmv32(gbims_handle *h, const float *x, float *y, const Ctl *c) {
+  if (h->dia_spmv) launch_dia7_spmv32(h->D, x, y, c, h->st);
+  else launch_spmv32(h->S, x, y, c, h->st);
 }
 
 static void residual64(gbims_handle *h, const Ctl *c, int only_if_north_due) {
@@ -174,38 +167,39 @@ static void enqueue_iteration(gbims_handle *h, unsigned long long cond, int use_
     kr_ctl_bcgs_cnvg(c, part, G, cond, use_cond, st);
     residual64(h, c, 1);
   } else if (h->mixed && !h->bcgs) {
-    // PCG on the FP32 matrix with FP64 vectors and an FP32 preconditioner;
-    // the FP64 true residual replaces the recurrence's at each refinement
-    precond_mixed(h, h->v_d, h->v_z);
-    kr_dot64(n, h->v_d, h->v_z, part, G, c, st);
+    // PCG on the FP32 matrix with FP32 vectors and preconditioner, FP64
+    // scalars and heads; the FP64 true residual restarts the recurrence at
+    // each refinement
+    precond32(h, h->f_d, h->f_z);
+    kr_dot32(n, h->f_d, h->f_z, part, G, c, st);
     kr_ctl_cg_rho(c, part, G, st);
-    kr_cg_pupdate64(n, h->v_z, h->v_p, c, st);
-    spmv_mixed(h, h->v_p, h->v_q, c);
-    kr_dot64(n, h->v_p, h->v_q, part, G, c, st);
+    kr_cg_pupdate32(n, h->f_z, h->f_p, c, st);
+    spmv32(h, h->f_p, h->f_q, c);
+    kr_dot32(n, h->f_p, h->f_q, part, G, c, st);
     kr_ctl_alpha(c, part, G, st);
-    kr_cg_update64(n, h->d_x, h->v_d, h->v_p, h->v_q, part, G, c, st);
+    kr_cg_update_mixed(n, h->d_x, h->f_d, h->f_p, h->f_q, part, G, c, st);
     kr_ctl_mixed_inner(c, part, G, 0, h->refine_factor, st);
     residual64(h, c, 1);
-    kr_true_resid_stats(n, h->v_d, nullptr, nullptr, nullptr, nullptr, part, G, c, st);
+    kr_true_resid_stats(n, h->v_d, h->f_d, nullptr, nullptr, nullptr, part, G, c, st);
     kr_ctl_refine(c, part, G, cond, use_cond, st);
   } else {
     // BiCGSTAB, same precision split
-    kr_dot64(n, h->v_dhat, h->v_d, part, G, c, st);
+    kr_dot32(n, h->f_dhat, h->f_d, part, G, c, st);
     kr_ctl_bcgs_rho(c, part, G, st);
-    kr_bcgs_p64(n, h->v_d, h->v_p, h->v_v, c, st);
-    precond_mixed(h, h->v_p, h->v_phat);
-    spmv_mixed(h, h->v_phat, h->v_v, c);
-    kr_dot64(n, h->v_dhat, h->v_v, part, G, c, st);
+    kr_bcgs_p32(n, h->f_d, h->f_p, h->f_v, c, st);
+    precond32(h, h->f_p, h->f_phat);
+    spmv32(h, h->f_phat, h->f_v, c);
+    kr_dot32(n, h->f_dhat, h->f_v, part, G, c, st);
     kr_ctl_alpha(c, part, G, st);
-    kr_bcgs_q64(n, h->v_d, h->v_v, h->v_q, c, st);
-    precond_mixed(h, h->v_q, h->v_qhat);
-    spmv_mixed(h, h->v_qhat, h->v_t, c);
-    kr_dot_tq_tt64(n, h->v_t, h->v_q, part, G, c, st);
+    kr_bcgs_q32(n, h->f_d, h->f_v, h->f_q, c, st);
+    precond32(h, h->f_q, h->f_qhat);
+    spmv32(h, h->f_qhat, h->f_t, c);
+    kr_dot_tq_tt32(n, h->f_t, h->f_q, part, G, c, st);
     kr_ctl_omega(c, part, G, st);
-    kr_bcgs_update64(n, h->d_x, h->v_d, h->v_phat, h->v_qhat, h->v_q, h->v_t, h->d_dscale, part, G, c, st);
+    kr_bcgs_update32(n, h->d_x, h->f_d, h->f_phat, h->f_qhat, h->f_q, h->f_t, h->d_dscale, part, G, c, st);
     kr_ctl_mixed_inner(c, part, G, 1, h->refine_factor, st);
     residual64(h, c, 1);
-    kr_true_resid_stats(n, h->v_d, nullptr, nullptr, h->v_dhat, h->d_dscale, part, G, c, st);
+    kr_true_resid_stats(n, h->v_d, h->f_d, h->f_dhat, nullptr, h->d_dscale, part, G, c, st);
     kr_ctl_refine(c, part, G, cond, use_cond, st);
   }
 }
@@ -278,19 +272,26 @@ static int setup_structured(gbims_handle *h, const std::vector<int> &shapes,
   const size_t nn = (size_t)h->D.slots;
   if (!h->mixed) {
     double **a[] = {&h->D.d_lz, &h->D.d_ly, &h->D.d_lx, &h->D.d_ux, &h->D.d_uy, &h->D.d_uz,
-                    &h->D.d_dinv, &h->D.d_rsk, &h->D.d_ysk, &h->D.d_zsk};
+                    &h->D.d_dinv, &h->D.d_rsk};
     for (double **p : a) GB_CUDA(h, dalloc(p, nn));
   } else {
     float **a[] = {&h->D.f_lz, &h->D.f_ly, &h->D.f_lx, &h->D.f_ux, &h->D.f_uy, &h->D.f_uz,
-                   &h->D.f_dinv, &h->D.f_rsk, &h->D.f_ysk, &h->D.f_zsk};
+                   &h->D.f_dinv, &h->D.f_rsk};
     for (float **p : a) GB_CUDA(h, dalloc(p, nn));
+  }
+  // result words: zero, so that no word carries the epoch of a sweep yet
+  const size_t llb = nn * (h->mixed ? 8 : 16);
+  for (void **p : {&h->D.ll_y, &h->D.ll_z}) {
+    GB_CUDA(h, dalloc((unsigned char **)p, llb));
+    GB_CUDA(h, cudaMemset(*p, 0, llb));
   }
   GB_CUDA(h, dalloc(&h->D.d_geo, h->D.geo.size()));
   GB_CUDA(h, cudaMemcpy(h->D.d_geo, h->D.geo.data(), sizeof(Dia7Geo) * h->D.geo.size(),
                         cudaMemcpyHostToDevice));
-  // one 128-byte progress line per CTA plus the ticket line
-  h->D.nflags = (h->D.ntickets + 2) * 32;
+  // the forward and backward ticket counters, one 128-byte line each
+  h->D.nflags = 2 * 32;
   GB_CUDA(h, dalloc(&h->D.d_flags, h->D.nflags));
+  GB_CUDA(h, cudaMemset(h->D.d_flags, 0, sizeof(int) * h->D.nflags));
   GB_CUDA(h, dalloc(&h->D.d_err, 4));
   GB_CUDA(h, cudaMemset(h->D.d_err, 0, sizeof(int) * 4));
   h->structured = true;
@@ -420,19 +421,25 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   GB_CUDA(h, dalloc(&h->d_rhs, nn));
   GB_CUDA(h, dalloc(&h->d_x, nn));
   GB_CUDA(h, dalloc(&h->v_d, nn));
-  GB_CUDA(h, dalloc(&h->v_p, nn));
-  GB_CUDA(h, dalloc(&h->v_q, nn));
-  GB_CUDA(h, dalloc(&h->v_z, nn));
-  if (h->bcgs) {
-    GB_CUDA(h, dalloc(&h->v_t, nn)); GB_CUDA(h, dalloc(&h->v_v, nn));
-    GB_CUDA(h, dalloc(&h->v_dhat, nn)); GB_CUDA(h, dalloc(&h->v_phat, nn));
-    GB_CUDA(h, dalloc(&h->v_qhat, nn));
-  }
-  if (h->mixed) {
-    // FP32 factors; FP32 input and output of the level-scheduled sweeps
+  if (!h->mixed) {
+    GB_CUDA(h, dalloc(&h->v_p, nn));
+    GB_CUDA(h, dalloc(&h->v_q, nn));
+    GB_CUDA(h, dalloc(&h->v_z, nn));
+    if (h->bcgs) {
+      GB_CUDA(h, dalloc(&h->v_t, nn)); GB_CUDA(h, dalloc(&h->v_v, nn));
+      GB_CUDA(h, dalloc(&h->v_dhat, nn)); GB_CUDA(h, dalloc(&h->v_phat, nn));
+      GB_CUDA(h, dalloc(&h->v_qhat, nn));
+    }
+  } else {
+    // FP32 factors and inner vectors; FP64 heads and true residual
     GB_CUDA(h, dalloc(&h->d_apc32, nja));
-    GB_CUDA(h, dalloc(&h->f_d, nn));
-    GB_CUDA(h, dalloc(&h->f_z, nn));
+    GB_CUDA(h, dalloc(&h->f_d, nn)); GB_CUDA(h, dalloc(&h->f_p, nn));
+    GB_CUDA(h, dalloc(&h->f_q, nn)); GB_CUDA(h, dalloc(&h->f_z, nn));
+    if (h->bcgs) {
+      GB_CUDA(h, dalloc(&h->f_t, nn)); GB_CUDA(h, dalloc(&h->f_v, nn));
+      GB_CUDA(h, dalloc(&h->f_dhat, nn)); GB_CUDA(h, dalloc(&h->f_phat, nn));
+      GB_CUDA(h, dalloc(&h->f_qhat, nn));
+    }
   }
   // SCALING_METHOD (ImsLinear.f90:222-224): DSCALE/DSCALE2 only when scaling;
   // BiCGSTAB reads DSCALE in its convergence maxima (null without scaling)
@@ -550,7 +557,15 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
   residual64(h, nullptr, 0);
   kr_sumsq64(n, h->v_d, h->d_part, h->G, st);
   kr_ctl_set_l2norm0(h->d_ctl, h->d_part, h->G, st);
-  if (h->bcgs) GB_CUDA(h, cudaMemcpyAsync(h->v_dhat, h->v_d, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if (h->bcgs && !h->mixed) GB_CUDA(h, cudaMemcpyAsync(h->v_dhat, h->v_d, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if (h->mixed) {
+    kr_f64_to_f32(n, h->v_d, h->f_d, st);
+    GB_CUDA(h, cudaMemsetAsync(h->f_p, 0, sizeof(float) * n, st));
+    if (h->bcgs) {
+      GB_CUDA(h, cudaMemcpyAsync(h->f_dhat, h->f_d, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+      GB_CUDA(h, cudaMemsetAsync(h->f_v, 0, sizeof(float) * n, st));
+    }
+  }
   GB_CUDA(h, cudaGetLastError());
   // inner loop
   if (!h->graph_tried) build_graph(h);
@@ -580,7 +595,7 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
   GB_CUDA(h, cudaGetLastError());
   const Ctl &r = *h->h_ctl;
   // zero, residual, sum of squares, L2NORM0 control (+ FP32 copy), then the loop bodies
-  h->launches += 4 + (long long)h->body_kernels * r.bodies;
+  h->launches += 4 + (h->mixed ? 1 : 0) + (long long)h->body_kernels * r.bodies;
   int iters = (r.l2norm0 == 0.0 || h->s.iter1 <= 0) ? 0 : r.iter;
   *icnvg = r.icnvg;
   *in_iter = iters;
@@ -683,8 +698,13 @@ extern "C" int gbims_precondition(gbims_handle *h, const double *r, double *z) {
   c.pivot_fail = INT_MAX;
   *h->h_ctl = c;
   GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, h->st));
-  if (!h->mixed) precond64(h, h->v_d, h->d_rhs);
-  else precond_mixed(h, h->v_d, h->d_rhs);
+  if (!h->mixed) {
+    precond64(h, h->v_d, h->d_rhs);
+  } else {
+    kr_f64_to_f32(h->n, h->v_d, h->f_d, h->st);
+    precond32(h, h->f_d, h->f_z);
+    kr_f32_to_f64(h->n, h->f_z, h->d_rhs, h->st);
+  }
   GB_CUDA(h, cudaGetLastError());
   GB_CUDA(h, cudaMemcpyAsync(z, h->d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToHost, h->st));
   GB_CUDA(h, cudaStreamSynchronize(h->st));
@@ -704,8 +724,14 @@ extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times 
   GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
   int eg = std::min(4 * kNumSM, (n + 255) / 256);
   // deterministic, finite operands
-  k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
-  GB_CUDA(h, cudaMemcpyAsync(h->v_p, h->d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  if (!h->mixed) {
+    k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
+    GB_CUDA(h, cudaMemcpyAsync(h->v_p, h->d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  } else {
+    kr_f64_to_f32(n, h->d_x, h->f_p, st);
+    GB_CUDA(h, cudaMemsetAsync(h->f_q, 0, sizeof(float) * n, st));
+    GB_CUDA(h, cudaMemsetAsync(h->f_d, 0, sizeof(float) * n, st));
+  }
   auto time_it = [&](auto &&fn) -> double {
     fn();
     cudaEventRecord(h->ev0, st);
@@ -722,10 +748,10 @@ extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times 
     t->dot_ms = time_it([&] { kr_dot64(n, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
     t->update_ms = time_it([&] { kr_cg_update64(n, h->v_z, h->v_d, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
   } else {
-    t->spmv_ms = time_it([&] { spmv_mixed(h, h->v_p, h->v_q, h->d_ctl); });
-    t->precond_ms = time_it([&] { precond_mixed(h, h->v_p, h->v_z); });
-    t->dot_ms = time_it([&] { kr_dot64(n, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
-    t->update_ms = time_it([&] { kr_cg_update64(n, h->v_z, h->v_d, h->v_p, h->v_q, h->d_part, h->G, h->d_ctl, st); });
+    t->spmv_ms = time_it([&] { spmv32(h, h->f_p, h->f_q, h->d_ctl); });
+    t->precond_ms = time_it([&] { precond32(h, h->f_p, h->f_z); });
+    t->dot_ms = time_it([&] { kr_dot32(n, h->f_p, h->f_q, h->d_part, h->G, h->d_ctl, st); });
+    t->update_ms = time_it([&] { kr_cg_update_mixed(n, h->v_d, h->f_d, h->f_p, h->f_q, h->d_part, h->G, h->d_ctl, st); });
   }
   GB_CUDA(h, cudaGetLastError());
   // algorithmic bytes: CSR values + column indices + row pointers, x read
@@ -734,11 +760,10 @@ extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times 
   // and z written once, plus JAPC/IAPC for the unstructured sweeps (the
   // structured sweeps need no indices).  The forward result kept between
   // the two sweeps is not counted.
-  // The mixed form: FP32 matrix and factors, FP64 vectors.
-  const double mb = h->mixed ? 4.0 : 8.0, vb = 8.0;
-  t->spmv_bytes = h->dia_spmv ? mb * h->nja + 2.0 * vb * n
-                              : (mb + 4.0) * h->nja + 4.0 * (n + 1) + 2.0 * vb * n;
-  t->precond_bytes = mb * h->nja + 2.0 * vb * n;
+  double vb = h->mixed ? 4.0 : 8.0;
+  t->spmv_bytes = h->dia_spmv ? vb * h->nja + 2.0 * vb * n
+                              : (vb + 4.0) * h->nja + 4.0 * (n + 1) + 2.0 * vb * n;
+  t->precond_bytes = vb * h->nja + 2.0 * vb * n;
   if (!h->structured) t->precond_bytes += 4.0 * h->nja + 4.0 * (n + 1);
   return GBIMS_OK;
 }
@@ -752,7 +777,7 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->S.d_col, h->S.d_src, h->S.d_val, h->S.d_val32, h->F.d_rows, h->B.d_rows,
                   h->D.d_lz, h->D.d_ly, h->D.d_lx, h->D.d_ux, h->D.d_uy, h->D.d_uz, h->D.d_dinv,
                   h->D.f_lz, h->D.f_ly, h->D.f_lx, h->D.f_ux, h->D.f_uy, h->D.f_uz, h->D.f_dinv,
-                  h->D.d_rsk, h->D.d_ysk, h->D.d_zsk, h->D.f_rsk, h->D.f_ysk, h->D.f_zsk,
+                  h->D.d_rsk, h->D.ll_y, h->D.ll_z, h->D.f_rsk,
                   h->D.d_flags, h->D.d_err, h->d_amat, h->d_rhs, h->d_x, h->v_d, h->v_p, h->v_q,
                   h->v_z, h->v_t, h->v_v, h->v_dhat, h->v_phat, h->v_qhat, h->f_d, h->f_p,
                   h->f_q, h->f_z, h->f_t, h->f_v, h->f_dhat, h->f_phat, h->f_qhat, h->d_part,

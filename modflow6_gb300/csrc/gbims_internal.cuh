@@ -138,15 +138,18 @@ struct Dia7 {
   // dinv; zero where the neighbour or the cell does not exist
   double *d_lz = nullptr, *d_ly = nullptr, *d_lx = nullptr;
   double *d_ux = nullptr, *d_uy = nullptr, *d_uz = nullptr, *d_dinv = nullptr;
-  double *d_rsk = nullptr, *d_ysk = nullptr, *d_zsk = nullptr;  // skewed input and results
+  double *d_rsk = nullptr;  // skewed right-hand side
   float *f_lz = nullptr, *f_ly = nullptr, *f_lx = nullptr;
   float *f_ux = nullptr, *f_uy = nullptr, *f_uz = nullptr, *f_dinv = nullptr;
-  float *f_rsk = nullptr, *f_ysk = nullptr, *f_zsk = nullptr;
+  float *f_rsk = nullptr;
+  // forward and backward results, skewed, as words that carry the epoch of
+  // the sweep that wrote them (16 bytes per element in FP64, 8 in FP32)
+  void *ll_y = nullptr, *ll_z = nullptr;
   // matrix values for the index-free SpMV: 7 slots of n (FP64; FP32 copy in
   // the mixed form), slot order = CSR order of a row
   double *d_sv = nullptr;
   float *f_sv = nullptr;
-  int *d_flags = nullptr;  // wavefront progress words, one per 128-byte line
+  int *d_flags = nullptr;  // the sweeps' ticket counters (forward, backward), one 128-byte line each
   int nflags = 0;
   int *d_err = nullptr;    // wait-limit error flag
 };
@@ -169,12 +172,12 @@ void launch_sell_fill(const Sell &S, const double *d_amat, cudaStream_t st);
 void launch_spmv64(const Sell &S, const double *x, double *y, const Ctl *ctl, cudaStream_t st);
 void launch_residual64(const Sell &S, const double *x, const double *b, double *d,
                        const Ctl *ctl, int only_if_north_due, cudaStream_t st);
-// FP32 matrix values, FP64 vectors and accumulation (the mixed form)
-void launch_spmv_mixed(const Sell &S, const double *x, double *y, const Ctl *ctl, cudaStream_t st);
-void launch_dia7_spmv_mixed(const Dia7 &D, const double *x, double *y, const Ctl *ctl,
-                            cudaStream_t st);
-void launch_dia7_apply_mixed(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
-                             cudaStream_t st);
+// The mixed form's inner loop: FP32 matrix values, vectors and factors.
+void launch_spmv32(const Sell &S, const float *x, float *y, const Ctl *ctl, cudaStream_t st);
+void launch_dia7_spmv32(const Dia7 &D, const float *x, float *y, const Ctl *ctl,
+                        cudaStream_t st);
+void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
+                         cudaStream_t st);
 
 void levels_build_host(int n, const std::vector<int> &iapc, const std::vector<int> &japc,
                        bool forward, Levels &L);

@@ -240,8 +240,11 @@ struct gbsln_handle {
          *xtemp = nullptr, *wsave = nullptr, *hchold = nullptr, *deold = nullptr,
          *dxold = nullptr, *part = nullptr, *bnd_val = nullptr, *chd_head = nullptr;
   int *ibound = nullptr, *bnd_ptr = nullptr, *chd_node = nullptr, *flag = nullptr;
+  int *bnd_kind = nullptr;  // per boundary entry: 0 WEL, 1 RCH
+  double *bpart = nullptr;  // budget partials (kGwfBudgetSlots per block)
   int nchd = 0, G = 1;
   bool has_sto = false;
+  double last_delt = 0.0;   // the last time step (or formulate) the budget refers to
   gbims_handle *ims = nullptr;
   double *amat = nullptr, *rhs = nullptr, *x = nullptr;  // inside the IMS handle
   cudaStream_t st = nullptr;
@@ -317,22 +320,25 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
     ibound[node] = -1;
   }
   // boundary values per node: WEL q, then RCH rate*area (package order)
-  std::vector<std::vector<double>> per(n);
+  std::vector<std::vector<std::pair<double, int>>> per(n);
   for (int i = 0; i < m->nwel; ++i) {
     int node = m->wel_node[i];
     if (node < 0 || node >= n) { h->err = "WEL node out of range"; return GBIMS_ERR_ARG; }
-    per[node].push_back(m->wel_q[i]);
+    per[node].push_back({m->wel_q[i], 0});
   }
   for (int i = 0; i < m->nrch; ++i) {
     int node = m->rch_node[i];
     if (node < 0 || node >= n) { h->err = "RCH node out of range"; return GBIMS_ERR_ARG; }
-    per[node].push_back(m->rch_rate[i] * area[node]);
+    per[node].push_back({m->rch_rate[i] * area[node], 1});
   }
-  std::vector<int> bptr(n + 1, 0);
+  std::vector<int> bptr(n + 1, 0), bkind;
   std::vector<double> bval;
   for (int p = 0; p < n; ++p) {
     bptr[p] = (int)bval.size();
-    for (double v : per[p]) bval.push_back(v);
+    for (const auto &v : per[p]) {
+      bval.push_back(v.first);
+      bkind.push_back(v.second);
+    }
   }
   bptr[n] = (int)bval.size();
   cudaError_t e = cudaSuccess;
@@ -362,6 +368,7 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
   chk(up(&h->ibound, ibound.data(), ibound.size()));
   chk(up(&h->bnd_ptr, bptr.data(), bptr.size()));
   chk(up(&h->bnd_val, bval.data(), bval.size()));
+  chk(up(&h->bnd_kind, bkind.data(), bkind.size()));
   h->nchd = m->nchd;
   chk(up(&h->chd_node, m->chd_node, (size_t)m->nchd));
   chk(up(&h->chd_head, m->chd_head, (size_t)m->nchd));
@@ -448,6 +455,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
   if (!h || !h->ims) return GBIMS_ERR_ARG;
   const int n = h->n;
   const bool transient = (delt > 0.0) && h->has_sto;
+  h->last_delt = delt;
   gbsln_stats s;
   memset(&s, 0, sizeof(s));
   float fill_ms = 0.f, solve_ms = 0.f;
@@ -608,6 +616,7 @@ extern "C" int gbsln_formulate(gbsln_handle *h, double delt, const double *hold,
   const int n = h->n;
   const bool transient = (delt > 0.0) && h->has_sto;
   if (transient && !hold) return GBIMS_ERR_ARG;
+  h->last_delt = delt;
   if (hold) SLN_CUDA(h, cudaMemcpyAsync(h->xold, hold, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
   FillDev f;
   f.transient = transient ? 1 : 0;
@@ -625,6 +634,60 @@ extern "C" int gbsln_formulate(gbsln_handle *h, double delt, const double *hold,
   SLN_CUDA(h, cudaMemcpyAsync(amat, h->amat, sizeof(double) * h->nja, cudaMemcpyDeviceToHost, h->st));
   SLN_CUDA(h, cudaMemcpyAsync(rhs, h->rhs, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
   SLN_CUDA(h, cudaStreamSynchronize(h->st));
+  return GBIMS_OK;
+}
+
+extern "C" int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table *out) {
+  if (!h || !out) return GBIMS_ERR_ARG;
+  const int n = h->n;
+  const bool transient = (h->last_delt > 0.0) && h->has_sto;
+  if (!h->bpart) SLN_CUDA(h, cudaMalloc((void **)&h->bpart, sizeof(double) * kGwfBudgetSlots * h->G));
+  double *dflow = nullptr;
+  if (flowja) SLN_CUDA(h, cudaMallocAsync((void **)&dflow, sizeof(double) * h->nja, h->st));
+  FillDev f;
+  f.transient = transient ? 1 : 0;
+  f.tled = transient ? 1.0 / h->last_delt : 0.0;
+  f.ss = h->ss;
+  f.sy = h->sy;
+  f.area = h->area;
+  f.bnd_ptr = h->bnd_ptr;
+  f.bnd_val = h->bnd_val;
+  gwf_budget(n, h->g, f, h->bnd_kind, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, dflow,
+             h->bpart, h->G, h->st);
+  std::vector<double> part((size_t)kGwfBudgetSlots * h->G);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(part.data(), h->bpart, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess && flowja)
+    e = cudaMemcpyAsync(flowja, dflow, sizeof(double) * h->nja, cudaMemcpyDeviceToHost, h->st);
+  if (dflow) cudaFreeAsync(dflow, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) {
+    h->err = std::string("gbsln_budget: ") + cudaGetErrorString(e);
+    return GBIMS_ERR_CUDA;
+  }
+  // block partials in block order, then the entries in budget order
+  double t[10] = {0};
+  double best = 0.0, row = -1.0;
+  for (int b = 0; b < h->G; ++b) {
+    const double *pb = part.data() + (size_t)b * kGwfBudgetSlots;
+    for (int k = 0; k < 10; ++k) t[k] += pb[k];
+    if (pb[10] > best) {
+      best = pb[10];
+      row = pb[11];
+    }
+  }
+  memset(out, 0, sizeof(*out));
+  for (int k = 0; k < 5; ++k) {
+    out->rate_in[k] = t[2 * k];
+    out->rate_out[k] = t[2 * k + 1];
+    out->total_in += t[2 * k];
+    out->total_out += t[2 * k + 1];
+  }
+  const double avg = (out->total_in + out->total_out) / 2.0;
+  out->percent_discrepancy = (avg != 0.0) ? 100.0 * (out->total_in - out->total_out) / avg : 0.0;
+  out->max_cell_imbalance = best;
+  out->max_cell = (int)row;
   return GBIMS_OK;
 }
 
@@ -662,6 +725,7 @@ extern "C" int gbsln_destroy(gbsln_handle *h) {
   h->d.release();
   void *p[] = {h->strt, h->ss, h->sy, h->area, h->vol, h->xold, h->xtemp, h->wsave, h->hchold, h->deold,
                h->dxold, h->part, h->bnd_val, h->chd_head, h->ibound, h->bnd_ptr, h->chd_node,
+               h->bnd_kind, h->bpart,
                h->flag};
   for (void *q : p)
     if (q) cudaFree(q);

@@ -58,29 +58,11 @@ namespace gb {
 namespace {
 
 constexpr unsigned long long kWaitNs = 2000000000ULL;  // 2 s per wait
-constexpr int kFlagStride = 32;                        // one progress word per 128-byte line
-constexpr int kOut = 8;                                // result tiles buffered per CTA
 
 __device__ __forceinline__ unsigned long long gtimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
-}
-__device__ __forceinline__ int ld_relaxed(const int *p) {
-  int v;
-  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_relaxed(int *p, int v) {
-  asm volatile("st.relaxed.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ int ld_acquire_cta(const int *p) {
-  int v;
-  asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"((unsigned)__cvta_generic_to_shared(p)) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_cta(int *p, int v) {
-  asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"((unsigned)__cvta_generic_to_shared(p)), "r"(v) : "memory");
 }
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
@@ -128,6 +110,47 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
       : "memory");
 }
 
+// One result element with its sweep epoch.  The epoch travels in the same
+// naturally aligned 8-byte access as the data it guards (FP64: both halves
+// carry it), so a consumer that reads the current epoch holds the value:
+// no fence and no progress counter stand between producer and consumer.
+template <typename T>
+struct LLWord;
+template <>
+struct alignas(16) LLWord<double> { unsigned long long v[2]; };
+template <>
+struct alignas(8) LLWord<float> { unsigned long long v; };
+
+__device__ __forceinline__ void ll_put(LLWord<double> *p, double x, unsigned ep) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long f = (unsigned long long)ep << 32;
+  asm volatile("st.relaxed.gpu.global.v2.b64 [%0], {%1, %2};" ::"l"(p), "l"((b & 0xffffffffULL) | f),
+               "l"((b >> 32) | f)
+               : "memory");
+}
+__device__ __forceinline__ void ll_put(LLWord<float> *p, float x, unsigned ep) {
+  const unsigned long long v = (unsigned long long)__float_as_uint(x) | ((unsigned long long)ep << 32);
+  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ bool ll_get(const LLWord<double> *p, unsigned ep, double &x) {
+  unsigned long long a, b;
+  asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+  x = __longlong_as_double((long long)((a & 0xffffffffULL) | (b << 32)));
+  return (unsigned)(a >> 32) == ep && (unsigned)(b >> 32) == ep;
+}
+__device__ __forceinline__ bool ll_get(const LLWord<float> *p, unsigned ep, float &x) {
+  unsigned long long a;
+  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(a) : "l"(p) : "memory");
+  x = __uint_as_float((unsigned)a);
+  return (unsigned)(a >> 32) == ep;
+}
+// The value of a word known to be complete (read by a later kernel, or
+// staged in shared memory after its kernel ended).
+__device__ __forceinline__ double ll_val(const LLWord<double> &w) {
+  return __longlong_as_double((long long)((w.v[0] & 0xffffffffULL) | (w.v[1] << 32)));
+}
+__device__ __forceinline__ float ll_val(const LLWord<float> &w) { return __uint_as_float((unsigned)w.v); }
+
 template <typename T>
 struct SweepArgs {
   const Dia7Geo *geo;  // members, in ticket order
@@ -135,35 +158,68 @@ struct SweepArgs {
   const Ctl *mctl;     // per-member control blocks (batched ensembles) or null
   const T *A, *B, *X, *D;  // skewed factors (forward: Lz Ly Lx -, backward: Uz' Uy' Ux' dinv)
   const T *rsk;            // forward: right-hand side, skewed
-  T *ysk;                  // forward result, skewed (written forward, read backward)
-  T *zsk;                  // backward result, skewed (written and read backward)
-  int *flags, *err;
+  LLWord<T> *ysk;          // forward result, skewed (written forward, read backward)
+  LLWord<T> *zsk;          // backward result, skewed (written and read backward)
+  unsigned long long *ticket;  // this direction's ticket counter (zeroed once, never reset)
+  int *err;
   Ctl *ctl;
 };
 
-template <typename T, int W, int C>
-struct Stage {
-  T a[C * W], b[C * W], x[C * W], d[C * W], r[C * W], zn[C * W], yn[C * W];
+// One ring buffer of a sweep CTA: C steps of the block's tiles (32 lanes).
+template <typename T, int C, int DIR>
+struct Stage;
+template <typename T, int C>
+struct alignas(16) Stage<T, C, 1> {
+  T a[C * 32], b[C * 32], x[C * 32], r[C * 32];
+  T yn[C];  // the neighbour block's last line, one value per step
+};
+template <typename T, int C>
+struct alignas(16) Stage<T, C, -1> {
+  T a[C * 32], b[C * 32], x[C * 32], d[C * 32];
+  LLWord<T> y[C * 32];  // own forward result, steps descending
+  T yn[C];
 };
 
 // Warp roles of a sweep CTA.
-enum { kRoleCompute = 0, kRoleCopy = 1, kRoleStore = 2, kRolePre = 3 };
+enum { kRoleCompute = 0, kRoleCopy = 1, kRoleEdge = 2, kRolePre = 3 };
 
-// DIR = +1 forward, -1 backward.
-template <typename T, int W, int S, int C, int NS, int DIR>
+// Poll result words of the current epoch, bounded; warp-uniform result.
+// `want` marks the lanes' words still missing (bit t = word t).
+template <typename T, int C>
+__device__ __forceinline__ bool ll_poll(const LLWord<T> *q, long long stride, unsigned want,
+                                        unsigned ep, T (&v)[C], volatile int *abort_flag) {
+  unsigned long long t0 = 0;
+  while (true) {
+#pragma unroll
+    for (int t = 0; t < C; ++t)
+      if ((want >> t) & 1u)
+        if (ll_get(q + t * stride, ep, v[t])) want &= ~(1u << t);
+    if (!__any_sync(0xffffffffu, want != 0)) return true;
+    if (t0 == 0) t0 = gtimer();
+    if (__any_sync(0xffffffffu, *abort_flag != 0 || gtimer() - t0 > kWaitNs)) return false;
+  }
+}
+
+// DIR = +1 forward, -1 backward.  A CTA is one block: 32 lines of one layer.
+template <typename T, int S, int C, int NS, int DIR>
 __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
+  constexpr int W = 32;
+  using St = Stage<T, C, DIR>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  Stage<T, W, C> *stg = reinterpret_cast<Stage<T, W, C> *>(smem_raw);
-  T *outring = reinterpret_cast<T *>(smem_raw + NS * sizeof(Stage<T, W, C>));
-  unsigned long long *full = reinterpret_cast<unsigned long long *>(
-      smem_raw + NS * sizeof(Stage<T, W, C>) + kOut * C * W * sizeof(T));
+  St *stg = reinterpret_cast<St *>(smem_raw);
+  unsigned long long *full = reinterpret_cast<unsigned long long *>(smem_raw + NS * sizeof(St));
   unsigned long long *empty = full + NS;
   unsigned long long *prep = full + 2 * NS;
-  __shared__ int s_id, s_ready, s_freed, s_abort, s_rot, s_m;
-  if (p.ctl && p.ctl->done) return;
+  __shared__ int s_id, s_abort, s_rot, s_m;
+  __shared__ unsigned s_ep;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    s_id = atomicAdd(&p.flags[0], 1);
+    // Every CTA of a launch takes its ticket, also one that returns at once,
+    // so that launch e (from 0) owns tickets [e*grid, (e+1)*grid): the local
+    // ticket orders the CTAs, the launch number is the epoch of its words.
+    const unsigned long long tk = atomicAdd(p.ticket, 1ULL);
+    s_id = (int)(tk % gridDim.x);
+    s_ep = (unsigned)(tk / gridDim.x) + 1u;
     // the member this ticket belongs to (members own contiguous tickets)
     int lo = 0, hi = p.nm - 1;
     while (lo < hi) {
@@ -172,28 +228,28 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       else hi = mid - 1;
     }
     s_m = lo;
-    s_ready = 0;
-    s_freed = 0;
     s_abort = 0;
     // Rotate the roles by the CTA's warp-slot group on the SM, so that the
     // compute warps of co-resident CTAs sit on different SM sub-partitions
-    // (each has its own FP64 pipe) and apart from their own pre-compute warp.
+    // (each has its own FP64 pipe).
     unsigned hw;
     asm volatile("mov.u32 %0, %%warpid;" : "=r"(hw));
     s_rot = (int)((hw >> 2) & 3u);
     for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
-      mbar_init(&prep[s], 1);
+      mbar_init(&prep[s], 2);  // pre-compute warp + edge warp
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  if (p.ctl && p.ctl->done) return;
   // a member of a batch that has reached its closure is not swept; its CTAs
   // only depend on one another, so none of them waits for it
   if (p.mctl && p.mctl[s_m].done) return;
   const int role = (warp + s_rot) & 3;
   const int id = s_id;
+  const unsigned ep = s_ep;
   const Dia7Geo geo = p.geo[s_m];
   const int lid = id - geo.ticket0;
   const int nlay = geo.nlay, nrow = geo.nrow, nb = geo.nb, G = geo.G;
@@ -202,18 +258,27 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   const int nch = G / C;
   const bool has_blk = (DIR > 0) ? (b > 0) : (b < nb - 1);
   const bool has_lay = (DIR > 0) ? (k > 0) : (k < nlay - 1);
-  int *prog = p.flags + kFlagStride;
   const long long slot0 = geo.slot0;
   auto tile = [&](int kk, int bb) -> long long { return slot0 + ((long long)kk * nb + bb) * G * W; };
+  LLWord<T> *out = (DIR > 0) ? p.ysk : p.zsk;
   volatile int *v_abort = &s_abort;
+  auto fail = [&]() {
+    if (lane == 0) {
+      *v_abort = 1;
+      atomicExch(p.err, 1);
+      if (p.ctl) p.ctl->done = 1;
+    }
+  };
 
   if (role == kRolePre) {
     // ---------------- pre-compute warp ----------------
     // The terms of a step that do not depend on the wavefront: forward
     // r - Lz*y(k-1), backward dinv*y - Uz'*z(k+1), in the same order and
-    // rounding as the full step.  Written over the stage's `a` tile (each
-    // element is read and written by one thread), released through the
-    // stage's prep mbarrier.
+    // rounding as the full step.  The neighbour layer's words are polled
+    // straight from global memory; the sum is written over the stage's `a`
+    // tile (each element read and written by one thread) and released
+    // through the stage's prep mbarrier.
+    const LLWord<T> *zsrc = has_lay ? out + tile(k - DIR, b) + lane : nullptr;
     for (int c = 0; c < nch; ++c) {
       const int s = c % NS;
       const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort);
@@ -221,11 +286,19 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         if (lane == 0) *v_abort = 1;
         return;
       }
-      Stage<T, W, C> &st = stg[s];
+      St &st = stg[s];
+      T zn[C];
+      if (has_lay && !ll_poll<T, C>(zsrc + (long long)c * C * W, W, (1u << C) - 1u, ep, zn, v_abort)) {
+        fail();
+        return;
+      }
 #pragma unroll
-      for (int e = lane; e < C * W; e += 32) {
-        T t0 = (DIR > 0) ? st.r[e] : st.d[e] * st.r[C * W - 1 - e];
-        if (has_lay) t0 = fma(-st.a[e], st.zn[e], t0);
+      for (int t = 0; t < C; ++t) {
+        const int e = t * W + lane;
+        T t0;
+        if constexpr (DIR > 0) t0 = st.r[e];
+        else t0 = st.d[e] * ll_val(st.y[C * W - 1 - e]);
+        if (has_lay) t0 = fma(-st.a[e], zn[t], t0);
         st.a[e] = t0;
       }
       // the buffer is refilled by the async proxy after the compute warp
@@ -237,126 +310,82 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     return;
   }
 
-  if (role == kRoleStore) {
-    // ---------------- store + publish warp ----------------
-    // Takes every result tile the compute warp has finished, sends each out
-    // with a bulk store, frees its slot once the store has read it, and then
-    // publishes the batch: stores complete, proxy fence, gpu-scope fence,
-    // progress word.  Batching spreads the cost of the fence over all the
-    // chunks that finished meanwhile.
-    if (lane == 0) {
-      int stored = 0;
-      unsigned long long t0 = gtimer();
-      unsigned ns = 32;
-      T *dstbase = ((DIR > 0) ? p.ysk : p.zsk) + tile(k, b);
-      while (stored < nch && !*v_abort) {
-        const int r = ld_acquire_cta(&s_ready);
-        if (r > stored) {
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          for (int c = stored; c < r; ++c) {
-            const T *src = outring + (c % kOut) * (C * W);
-            asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(
-                             dstbase + (long long)c * C * W),
-                         "r"(smem_u32(src)), "r"((unsigned)(C * W * sizeof(T)))
-                         : "memory");
-          }
-          asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-          st_release_cta(&s_freed, r);  // result slots may be reused
-          asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
-          asm volatile("fence.proxy.async.global;" ::: "memory");
-          __threadfence();
-          st_relaxed(prog + (size_t)id * kFlagStride, r * C);
-          stored = r;
-          t0 = gtimer();
-          ns = 32;
-        } else {
-          __nanosleep(ns);
-          if (ns < 256) ns <<= 1;
-          if (gtimer() - t0 > kWaitNs) {
-            *v_abort = 1;
-            atomicExch(p.err, 1);
-            if (p.ctl) p.ctl->done = 1;
-          }
+  if (role == kRoleEdge) {
+    // ---------------- edge warp ----------------
+    // The neighbour block's last line: lane t < C polls the word of step t
+    // of the chunk (the neighbour's lane 31 reaches column g at its step
+    // g + S*31) and leaves it in the stage's `yn`.
+    const LLWord<T> *ysrc = has_blk ? out + tile(k, b - DIR) + (W - 1) : nullptr;
+    for (int c = 0; c < nch; ++c) {
+      const int s = c % NS;
+      if (c >= NS) {
+        const bool got = mbar_wait(&empty[s], ((c / NS) - 1) & 1, v_abort);
+        if (!__all_sync(0xffffffffu, got)) {
+          if (lane == 0) *v_abort = 1;
+          return;
         }
       }
-      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+      if (has_blk) {
+        const int yrow = c * C + S * (W - 1) + lane;
+        T v[1] = {T(0)};
+        const bool need = lane < C && yrow < G;
+        if (!ll_poll<T, 1>(ysrc + (long long)(need ? yrow : 0) * W, 0, need ? 1u : 0u, ep, v,
+                           v_abort)) {
+          fail();
+          return;
+        }
+        if (lane < C) stg[s].yn[lane] = need ? v[0] : T(0);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&prep[s]);
     }
     return;
   }
 
   if (role == kRoleCopy) {
     // ---------------- copy warp ----------------
-    const int *pb = has_blk ? prog + (size_t)(id - nlay) * kFlagStride : nullptr;
-    const int *pu = has_lay ? prog + (size_t)(id - 1) * kFlagStride : nullptr;
-    int seen_b = 0, seen_u = 0, issued = 0;
+    // The block's own tiles have no producer in this launch: they stream
+    // into the ring as fast as buffers free up.
+    int issued = 0;
     bool ok = true;
     const unsigned tileb = C * W * sizeof(T);
     for (int c = 0; c < nch; ++c) {
       const int s = c % NS;
-      if (lane == 0) {
-        // the buffer's previous chunk (c - NS) has been consumed
-        if (c >= NS && !mbar_wait(&empty[s], ((c / NS) - 1) & 1, v_abort)) ok = false;
-        // producers: neighbour block (its last lane) and neighbour layer
-        const int nb_need = min((c + 1) * C + S * (W - 1), G);
-        const int nu_need = min((c + 1) * C, G);
-        if (ok && ((pb && seen_b < nb_need) || (pu && seen_u < nu_need))) {
-          unsigned long long t0 = gtimer();
-          while ((pb && seen_b < nb_need) || (pu && seen_u < nu_need)) {
-            if (pb && seen_b < nb_need) seen_b = ld_relaxed(pb);
-            if (pu && seen_u < nu_need) seen_u = ld_relaxed(pu);
-            if (*v_abort || gtimer() - t0 > kWaitNs) { ok = false; break; }
-          }
-          // the data behind the progress just observed is read by the async proxy
-          asm volatile("fence.proxy.async.global;" ::: "memory");
-        }
+      if (c >= NS) {
+        const bool got = mbar_wait(&empty[s], ((c / NS) - 1) & 1, v_abort);
+        ok = __all_sync(0xffffffffu, got);
+        if (!ok) break;
       }
-      ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
-      if (!ok) break;
       if (lane == 0) {
-        Stage<T, W, C> &st = stg[s];
+        St &st = stg[s];
         const int g0 = c * C;
-        const int yrow0 = g0 + S * (W - 1);
-        const int yrows = has_blk ? max(0, min(C, G - yrow0)) : 0;
-        int plo = 0, prows = 0, pskip = 0;
-        if (DIR < 0) {  // own forward result, rows P descending
+        const long long tb = tile(k, b) + (long long)g0 * W;
+        if constexpr (DIR > 0) {
+          mbar_expect_tx(&full[s], 4 * tileb);
+          bulk_g2s(st.r, p.rsk + tb, tileb, &full[s]);
+        } else {
+          // own forward result, steps P descending
           const int phi = geo.ncol - 1 + S * (W - 1) - g0;
           const int pl = phi - (C - 1);
           const int lo = max(pl, 0), hi = min(phi, G - 1);
-          plo = lo;
-          prows = max(0, hi - lo + 1);
-          pskip = lo - pl;
+          const int prows = max(0, hi - lo + 1);
+          const int pskip = lo - pl;
+          const unsigned ybytes = prows * W * (unsigned)sizeof(LLWord<T>);
+          mbar_expect_tx(&full[s], 4 * tileb + ybytes);
+          bulk_g2s(st.d, p.D + tb, tileb, &full[s]);
+          if (prows > 0)
+            bulk_g2s(st.y + pskip * W, p.ysk + tile(k, b) + (long long)lo * W, ybytes, &full[s]);
         }
-        unsigned bytes = 3 * tileb;
-        bytes += (DIR > 0) ? tileb : tileb + prows * W * (unsigned)sizeof(T);
-        if (has_lay) bytes += tileb;
-        bytes += yrows * W * (unsigned)sizeof(T);
-        mbar_expect_tx(&full[s], bytes);
-        const long long tb = tile(k, b) + (long long)g0 * W;
         bulk_g2s(st.a, p.A + tb, tileb, &full[s]);
         bulk_g2s(st.b, p.B + tb, tileb, &full[s]);
         bulk_g2s(st.x, p.X + tb, tileb, &full[s]);
-        if (DIR > 0) {
-          bulk_g2s(st.r, p.rsk + tb, tileb, &full[s]);
-        } else {
-          bulk_g2s(st.d, p.D + tb, tileb, &full[s]);
-          if (prows > 0)
-            bulk_g2s(st.r + pskip * W, p.ysk + tile(k, b) + (long long)plo * W,
-                     prows * W * sizeof(T), &full[s]);
-        }
-        const T *nbr = (DIR > 0) ? p.ysk : p.zsk;
-        if (has_lay) bulk_g2s(st.zn, nbr + tile(k - DIR, b) + (long long)g0 * W, tileb, &full[s]);
-        if (yrows > 0)
-          bulk_g2s(st.yn, nbr + tile(k, b - DIR) + (long long)yrow0 * W, yrows * W * sizeof(T),
-                   &full[s]);
       }
       issued = c + 1;
     }
-    if (!ok && lane == 0) {
-      atomicExch(p.err, 1);
-      if (p.ctl) p.ctl->done = 1;
-      *v_abort = 1;
-      // drain the copies still in flight before the CTA's shared memory goes
+    if (!ok) fail();
+    if (lane == 0) {
+      // every copy issued has landed before this warp, and so the CTA, ends
+      // (the other warps may have left early on an abort)
       for (int c = max(0, issued - NS); c < issued; ++c) {
         unsigned long long t0 = gtimer();
         while (!mbar_test(&full[c % NS], (c / NS) & 1))
@@ -367,11 +396,13 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   }
 
   // ---------------- compute warp ----------------
+  // Per step one shuffle and the two FMAs of the row and column neighbours;
+  // each result goes straight out as a word of this epoch.
   const int i = (DIR > 0) ? (b * W + lane) : (b * W + (W - 1 - lane));
-  const bool line_ok = lane < W && i >= 0 && i < nrow;
+  const bool line_ok = i >= 0 && i < nrow;
   const bool has_y = line_ok && ((DIR > 0) ? (i > 0) : (i + 1 < nrow));
   const int ncol = geo.ncol;
-  const int l = lane < W ? lane : 0;
+  LLWord<T> *outt = out + tile(k, b) + lane;
   T h1 = T(0), h2 = T(0);
   for (int c = 0; c < nch; ++c) {
     const int s = c % NS;
@@ -381,52 +412,35 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       if (lane == 0) *v_abort = 1;
       return;
     }
-    const Stage<T, W, C> &st = stg[s];
-    T *ot = outring + (c % kOut) * (C * W);
-    if (c >= kOut) {
-      // the slot's previous tile (chunk c - kOut) must have left for global memory
-      bool freed = true;
-      if (lane == 0 && ld_acquire_cta(&s_freed) < c - kOut + 1) {
-        unsigned long long t0 = gtimer();
-        while (ld_acquire_cta(&s_freed) < c - kOut + 1)
-          if (*v_abort || gtimer() - t0 > kWaitNs) { freed = false; break; }
-      }
-      if (!__shfl_sync(0xffffffffu, freed ? 1 : 0, 0)) {
-        if (lane == 0) *v_abort = 1;
-        return;
-      }
-    }
+    const St &st = stg[s];
     const int g0 = c * C;
     const int jc = g0 - S * lane;
 #pragma unroll
     for (int t = 0; t < C; ++t) {
       T yv = __shfl_up_sync(0xffffffffu, (S == 1) ? h1 : h2, 1);
-      if (lane == 0) yv = st.yn[t * W + (W - 1)];
+      if (lane == 0) yv = st.yn[t];
       const int jj = jc + t;
       const bool v = line_ok && (unsigned)jj < (unsigned)ncol;
-      T tv = st.a[t * W + l];  // pre-computed r - Lz*zn (backward: dinv*y - Uz'*zn)
-      if (has_y) tv = fma(-st.b[t * W + l], yv, tv);
-      if (jj > 0) tv = fma(-st.x[t * W + l], h1, tv);
+      T tv = st.a[t * W + lane];  // pre-computed r - Lz*zn (backward: dinv*y - Uz'*zn)
+      if (has_y) tv = fma(-st.b[t * W + lane], yv, tv);
+      if (jj > 0) tv = fma(-st.x[t * W + lane], h1, tv);
       if (!v) tv = T(0);
-      if (lane < W) ot[t * W + lane] = tv;
+      ll_put(outt + (long long)(g0 + t) * W, tv, ep);
       h2 = h1;
       h1 = tv;
     }
-    // hand the result tile to the store warp and the input buffer back to
-    // the copy warp
+    // the input buffer goes back to the copy and edge warps
     __syncwarp();
-    if (lane == 0) {
-      st_release_cta(&s_ready, c + 1);
-      mbar_arrive(&empty[s]);
-    }
+    if (lane == 0) mbar_arrive(&empty[s]);
   }
 }
 
 // Natural order -> skewed tiles (forward input) and back (backward output).
 // A 32 x 8 thread block covers 32 columns of 8 lines: the natural-order side
 // is whole rows, and the skewed side falls in a few rows of one tile.
+// The backward source holds result words (LLWord<TS>).
 template <typename TS, typename TD, int W, int S, int DIR>
-__global__ void k_dia7_permute(const Dia7Geo *__restrict__ geos, int nm, const TS *__restrict__ src,
+__global__ void k_dia7_permute(const Dia7Geo *__restrict__ geos, int nm, const void *__restrict__ src,
                                TD *__restrict__ dst, const Ctl *__restrict__ ctl,
                                const Ctl *__restrict__ mctl) {
   if (ctl && ctl->done) return;
@@ -452,8 +466,8 @@ __global__ void k_dia7_permute(const Dia7Geo *__restrict__ geos, int nm, const T
   const int gg = ((DIR > 0) ? j : (g.ncol - 1 - j)) + S * l;
   const long long sk = g.slot0 + (((long long)k * g.nb + b) * g.G + gg) * W + l;
   const long long nat = g.row0 + ((long long)k * g.nrow + i) * g.ncol + j;
-  if (DIR > 0) dst[sk] = (TD)src[nat];  // skew (forward input)
-  else dst[nat] = (TD)src[sk];          // unskew (backward output)
+  if (DIR > 0) dst[sk] = (TD)static_cast<const TS *>(src)[nat];  // skew (forward input)
+  else dst[nat] = (TD)ll_val(static_cast<const LLWord<TS> *>(src)[sk]);  // unskew (backward output)
 }
 
 // APC/JAPC -> skewed tiles.  Forward tiles hold Lz, Ly, Lx of the cell that
@@ -534,15 +548,17 @@ struct Shape<double> {
 template <>
 struct Shape<float> { static constexpr int W = 32, S = 1, C = 8, NS = 5; };
 
-template <typename T>
+template <typename T, int DIR>
 constexpr size_t stage_bytes() {
   using P = Shape<T>;
-  return P::NS * sizeof(Stage<T, P::W, P::C>) + kOut * P::C * P::W * sizeof(T) +
-         3 * P::NS * sizeof(unsigned long long);
+  return P::NS * sizeof(Stage<T, P::C, DIR>) + 3 * P::NS * sizeof(unsigned long long);
 }
-static_assert(Shape<double>::W <= 32 && Shape<double>::S >= 1, "FP64 wavefront shape");
-static_assert(stage_bytes<double>() <= 200 * 1024, "FP64 stage ring too large");
-static_assert(stage_bytes<float>() <= 200 * 1024, "FP32 stage ring too large");
+static_assert(Shape<double>::W == 32 && Shape<float>::W == 32, "a sweep block is one warp of lines");
+static_assert((Shape<double>::S == 1 || Shape<double>::S == 2) &&
+                  (Shape<float>::S == 1 || Shape<float>::S == 2),
+              "lane skew 1 or 2");
+static_assert(stage_bytes<double, -1>() <= 200 * 1024, "FP64 stage ring too large");
+static_assert(stage_bytes<float, -1>() <= 200 * 1024, "FP32 stage ring too large");
 
 }  // namespace
 
@@ -641,52 +657,59 @@ void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_j
 
 // One ILU0 application on the skewed layout: skew r (natural order, type TV)
 // into the sweep type T, forward and backward wavefront sweeps, unskew z
-// back to TV (TV = double, T = float: FP32 factors inside FP64 vectors).
+// back to TV.
+// No memory is reset between applications: each sweep launch writes its
+// words with a new epoch.
 template <typename T, typename TV = T>
-static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, T *ysk, T *zsk, const TV *r, TV *z,
-                    const Ctl *ctl, cudaStream_t st) {
+static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, const TV *r, TV *z, const Ctl *ctl,
+                    cudaStream_t st) {
   using P = Shape<T>;
   const int nct = D.ntickets;
-  const size_t fbytes = sizeof(int) * (size_t)(nct + 1) * kFlagStride;
-  constexpr size_t sm = stage_bytes<T>();
+  constexpr size_t smf = stage_bytes<T, 1>(), smb = stage_bytes<T, -1>();
   const dim3 pb(32, 8);
   SweepArgs<T> a;
   a.geo = D.d_geo;
   a.nm = D.nm;
   a.mctl = D.mctl;
-  a.rsk = rsk; a.ysk = ysk; a.zsk = zsk;
-  a.flags = D.d_flags; a.err = D.d_err; a.ctl = const_cast<Ctl *>(ctl);
+  a.rsk = rsk;
+  a.ysk = static_cast<LLWord<T> *>(D.ll_y);
+  a.zsk = static_cast<LLWord<T> *>(D.ll_z);
+  a.err = D.d_err;
+  a.ctl = const_cast<Ctl *>(ctl);
   a.A = arr[0]; a.B = arr[1]; a.X = arr[2]; a.D = nullptr;
-  if (sm > 48 * 1024) {  // opt in to more than 48 KB of dynamic shared memory, once
+  a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags);
+  {  // opt in to more than 48 KB of dynamic shared memory, once
     static bool opted = false;
     if (!opted) {
-      cudaFuncSetAttribute(k_dia7_sweep<T, P::W, P::S, P::C, P::NS, 1>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      cudaFuncSetAttribute(k_dia7_sweep<T, P::W, P::S, P::C, P::NS, -1>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (smf > 48 * 1024)
+        cudaFuncSetAttribute(k_dia7_sweep<T, P::S, P::C, P::NS, 1>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+      if (smb > 48 * 1024)
+        cudaFuncSetAttribute(k_dia7_sweep<T, P::S, P::C, P::NS, -1>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb);
       opted = true;
     }
   }
   k_dia7_permute<TV, T, P::W, P::S, 1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, r, rsk, ctl, D.mctl);
-  cudaMemsetAsync(D.d_flags, 0, fbytes, st);
-  k_dia7_sweep<T, P::W, P::S, P::C, P::NS, 1><<<nct, 128, sm, st>>>(a);
+  k_dia7_sweep<T, P::S, P::C, P::NS, 1><<<nct, 128, smf, st>>>(a);
   a.A = arr[3]; a.B = arr[4]; a.X = arr[5]; a.D = arr[6];
-  cudaMemsetAsync(D.d_flags, 0, fbytes, st);
-  k_dia7_sweep<T, P::W, P::S, P::C, P::NS, -1><<<nct, 128, sm, st>>>(a);
-  k_dia7_permute<T, TV, P::W, P::S, -1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, zsk, z, ctl, D.mctl);
+  a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags + 32);
+  k_dia7_sweep<T, P::S, P::C, P::NS, -1><<<nct, 128, smb, st>>>(a);
+  k_dia7_permute<T, TV, P::W, P::S, -1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, D.ll_z, z, ctl,
+                                                                 D.mctl);
 }
 
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
                          cudaStream_t st) {
   const double *arr[7] = {D.d_lz, D.d_ly, D.d_lx, D.d_uz, D.d_uy, D.d_ux, D.d_dinv};
-  apply_t<double>(D, arr, D.d_rsk, D.d_ysk, D.d_zsk, r, z, ctl, st);
+  apply_t<double>(D, arr, D.d_rsk, r, z, ctl, st);
 }
 
 
-void launch_dia7_apply_mixed(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
-                             cudaStream_t st) {
+void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
+                         cudaStream_t st) {
   const float *arr[7] = {D.f_lz, D.f_ly, D.f_lx, D.f_uz, D.f_uy, D.f_ux, D.f_dinv};
-  apply_t<float, double>(D, arr, D.f_rsk, D.f_ysk, D.f_zsk, r, z, ctl, st);
+  apply_t<float>(D, arr, D.f_rsk, r, z, ctl, st);
 }
 
 }  // namespace gb

@@ -302,6 +302,140 @@ __global__ void k_gwf_fill(int nodes, NpfDev g, FillDev f, const int *__restrict
   }
 }
 
+// Cell-by-cell flows and the model budget of one time step (gwf_cq and
+// gwf_bd, gwf.f90:741-830), one row per thread in gather form:
+//  * sto_cq (gwf-sto.f90:447-564, SsTerms/SyTerms rates,
+//    GwfStorageUtils.f90:32-134) into the flowja diagonal;
+//  * bnd_cq_simrate (BoundaryPackage.f90:583-619) for WEL then RCH:
+//    rate = hcof*h - rhs with hcof = 0, for active cells;
+//  * npf_cq (gwf-npf.f90:745-770, qcalc :800-865): q = cond*(h_m - h_n)
+//    into the lower-numbered cell n, -q into m; csr_diagsum
+//    (Sparse.f90:262-281) adds the row's flows to the diagonal in JA order;
+//  * calc_chd_rate (gwf-chd.f90:264-320) for CHD cells: rate = -sum q, and
+//    the in/out split over connections to active cells.
+// Per block: the in/out sums of STO-SS, STO-SY, CHD, WEL, RCH (the
+// rate_accumulator of Budget.f90:631-648) and the largest |flowja diagonal|
+// of an active cell (its row as a double).  flowja may be null.
+__global__ void __launch_bounds__(256) k_gwf_budget(int nodes, NpfDev g, FillDev f,
+                                                    const int *__restrict__ bnd_kind,
+                                                    const int *__restrict__ ibound,
+                                                    const double *__restrict__ h,
+                                                    const double *__restrict__ hold,
+                                                    const double *__restrict__ sat,
+                                                    const double *__restrict__ condsat,
+                                                    double *flowja, double *part) {
+  double acc[kGwfBudgetSlots];
+#pragma unroll
+  for (int t = 0; t < kGwfBudgetSlots; ++t) acc[t] = 0.0;
+  acc[11] = -1.0;
+  auto inout = [&](int slot, double r) {
+    if (r < 0.0) acc[2 * slot + 1] = DSUB(acc[2 * slot + 1], r);
+    else acc[2 * slot] = DADD(acc[2 * slot], r);
+  };
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nodes; p += gridDim.x * blockDim.x) {
+    const int i0 = g.ia[p], i1 = g.ia[p + 1];
+    double diag = 0.0;
+    // STO
+    if (f.transient && ibound[p] > 0) {
+      const double tp = g.top[p], bt = g.bot[p];
+      const int iconvert = g.icelltype[p];
+      double snold = 1.0, snnew = 1.0;
+      if (iconvert != 0) {
+        snold = d_sqsat(tp, bt, hold[p], g.satomega);
+        snnew = d_sqsat(tp, bt, h[p], g.satomega);
+      }
+      const double sc1 = DMUL(DMUL(f.ss[p], DSUB(tp, bt)), f.area[p]);
+      const double rho1 = DMUL(sc1, f.tled);
+      const double aterm = DMUL(-rho1, snnew);
+      double rhsterm;
+      if (iconvert != 0) {
+        const double tthk = DSUB(tp, bt);
+        const double zold = DADD(bt, DMUL(DMUL(0.5, tthk), snold));
+        const double znew = DADD(bt, DMUL(DMUL(0.5, tthk), snnew));
+        rhsterm = DSUB(DMUL(DMUL(-rho1, snold), DSUB(hold[p], zold)), DMUL(DMUL(rho1, snnew), znew));
+      } else {
+        rhsterm = DMUL(DMUL(-rho1, snold), hold[p]);
+      }
+      const double rss = DSUB(DMUL(aterm, h[p]), rhsterm);
+      diag = DADD(diag, rss);
+      inout(0, rss);
+      double rsy = 0.0;
+      if (iconvert != 0) {
+        const double rho2 = DMUL(DMUL(f.sy[p], f.area[p]), f.tled);
+        const double tthk = DSUB(tp, bt);
+        rsy = DSUB(DMUL(DMUL(rho2, tthk), snold), DMUL(DMUL(rho2, tthk), snnew));
+      }
+      diag = DADD(diag, rsy);
+      inout(1, rsy);
+    }
+    // WEL, RCH: rhs = -v, hcof = 0
+    for (int e = f.bnd_ptr[p]; e < f.bnd_ptr[p + 1]; ++e) {
+      double rr = 0.0;
+      if (ibound[p] > 0) rr = DSUB(DMUL(0.0, h[p]), -f.bnd_val[e]);
+      diag = DADD(diag, rr);
+      inout(3 + bnd_kind[e], rr);
+    }
+    // NPF flows, diagonal sum, CHD
+    const bool chd = ibound[p] < 0;
+    double crate = 0.0, cin = 0.0, cout = 0.0;
+    for (int ii = i0 + 1; ii < i1; ++ii) {
+      const int q = g.ja[ii];
+      const int n = min(p, q), m = max(p, q);
+      const double cond = conn_cond(g, ibound, h, sat, condsat, n, m, g.jas[ii]);
+      const double qnm = DMUL(cond, DSUB(h[m], h[n]));
+      const double fj = (p == n) ? qnm : -qnm;
+      if (flowja) flowja[ii] = fj;
+      diag = DADD(diag, fj);
+      if (chd) {
+        crate = DSUB(crate, fj);
+        if (ibound[q] > 0) {
+          if (fj < 0.0) cin = DSUB(cin, fj);
+          else cout = DADD(cout, fj);
+        }
+      }
+    }
+    if (chd) {
+      diag = DADD(diag, crate);
+      acc[4] = DADD(acc[4], cin);
+      acc[5] = DADD(acc[5], cout);
+    }
+    if (flowja) flowja[i0] = diag;
+    if (ibound[p] > 0 && fabs(diag) > acc[10]) {
+      acc[10] = fabs(diag);
+      acc[11] = (double)p;
+    }
+  }
+  // block reduction: sums of slots 0-9, max (with row) of slot 10
+  __shared__ double sh[8][kGwfBudgetSlots];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t < 10; ++t)
+    for (int o = 16; o > 0; o >>= 1) acc[t] += __shfl_xor_sync(0xffffffffu, acc[t], o);
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v = __shfl_xor_sync(0xffffffffu, acc[10], o);
+    const double r = __shfl_xor_sync(0xffffffffu, acc[11], o);
+    if (v > acc[10] || (v == acc[10] && r >= 0.0 && (acc[11] < 0.0 || r < acc[11]))) {
+      acc[10] = v;
+      acc[11] = r;
+    }
+  }
+  if (lane == 0)
+    for (int t = 0; t < kGwfBudgetSlots; ++t) sh[w][t] = acc[t];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double out[kGwfBudgetSlots];
+    for (int t = 0; t < kGwfBudgetSlots; ++t) out[t] = sh[0][t];
+    for (int v = 1; v < (int)(blockDim.x >> 5); ++v) {
+      for (int t = 0; t < 10; ++t) out[t] += sh[v][t];
+      if (sh[v][10] > out[10]) {
+        out[10] = sh[v][10];
+        out[11] = sh[v][11];
+      }
+    }
+    for (int t = 0; t < kGwfBudgetSlots; ++t) part[(size_t)blockIdx.x * kGwfBudgetSlots + t] = out[t];
+  }
+}
+
 // sln_calc_residual + gwf_ptc (NumericalSolution.f90:2966-2982, gwf.f90:625-687):
 // per block, max over active cells of |A x - b| / cell volume.
 __global__ void k_ptc_resid(int nodes, const int *__restrict__ ia, const int *__restrict__ ja,
@@ -547,6 +681,12 @@ void gwf_calcdx(int nodes, const int *active, const double *x, const double *xte
 void gwf_npf_nur(int nodes, int nrc, int nlay, const NpfDev &g, const int *ibound, double *x,
                  const double *xtemp, double *dx, int *flag, cudaStream_t st) {
   k_npf_nur<<<g_grid(nodes), 256, 0, st>>>(nodes, nrc, nlay, g, ibound, x, xtemp, dx, flag);
+}
+
+void gwf_budget(int nodes, const NpfDev &g, const FillDev &f, const int *bnd_kind,
+                const int *ibound, const double *h, const double *hold, const double *sat,
+                const double *condsat, double *flowja, double *part, int G, cudaStream_t st) {
+  k_gwf_budget<<<G, 256, 0, st>>>(nodes, g, f, bnd_kind, ibound, h, hold, sat, condsat, flowja, part);
 }
 
 }  // namespace gb

@@ -51,5 +51,11 @@ void gwf_calcdx(int nodes, const int *active, const double *x, const double *xte
                 cudaStream_t st);
 void gwf_npf_nur(int nodes, int nrc, int nlay, const NpfDev &g, const int *ibound, double *x,
                  const double *xtemp, double *dx, int *flag, cudaStream_t st);
+// Flows and model budget terms; part holds kGwfBudgetSlots doubles per block
+// (in/out of STO-SS, STO-SY, CHD, WEL, RCH; max |flowja diagonal|, its row).
+constexpr int kGwfBudgetSlots = 12;
+void gwf_budget(int nodes, const NpfDev &g, const FillDev &f, const int *bnd_kind,
+                const int *ibound, const double *h, const double *hold, const double *sat,
+                const double *condsat, double *flowja, double *part, int G, cudaStream_t st);
 
 }  // namespace gb

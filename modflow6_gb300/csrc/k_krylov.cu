@@ -259,6 +259,15 @@ __global__ void __launch_bounds__(256) k_cg_pupdate64(int n, const double *__res
 }
 
 
+__global__ void __launch_bounds__(256) k_cg_pupdate32(int n, const float *__restrict__ z,
+                                                      float *__restrict__ p,
+                                                      const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  p[i] = ctl->first ? z[i] : fmaf((float)ctl->beta, p[i], z[i]);
+}
+
 // x += alpha*p ; d -= alpha*q ; max|alpha p|, max|d|, sum d^2 (FP64 path).
 // partial slots: [0]=l2, [1]=dx val, [2]=dx idx, [3]=r val, [4]=r idx, [5]=nonfinite
 __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__restrict__ x,
@@ -306,6 +315,55 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__rest
   }
 }
 
+
+// Mixed inner update: x (FP64) += alpha*p (FP32 promoted); d32 -= alpha*q32.
+__global__ void __launch_bounds__(kRedBlock) k_cg_update_mixed(int n, double *__restrict__ x,
+                                                                float *__restrict__ d,
+                                                                const float *__restrict__ p,
+                                                                const float *__restrict__ q,
+                                                                double *__restrict__ part,
+                                                                const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  const double alpha = ctl->alpha;
+  const float alphaf = (float)alpha;
+  double v[2] = {0.0, 0.0};
+  unsigned nf = 0;
+  MaxLoc m[2];
+  m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
+  auto row = [&](int i, float pi, double xi, float qi, float dI) {
+    double tv = alpha * (double)pi;
+    x[i] = xi + tv;
+    if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i; }
+    float di = fmaf(-alphaf, qi, dI);
+    d[i] = di;
+    double dd = (double)di;
+    if (absgt(dd, m[1].val)) { m[1].val = dd; m[1].idx = i; }
+    v[0] = fma(dd, dd, v[0]);
+    nf |= nonfinite(di) | nonfinite(tv);
+  };
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    const int j = i + stride;
+    const float p0 = p[i], q0 = q[i], d0 = d[i];
+    const double x0 = x[i];
+    const float p1 = p[j], q1 = q[j], d1 = d[j];
+    const double x1 = x[j];
+    row(i, p0, x0, q0, d0);
+    row(j, p1, x1, q1, d1);
+  }
+  if (i < n) row(i, p[i], x[i], q[i], d[i]);
+  v[1] = (double)nf;
+  block_sum<2>(v);
+  block_maxloc<2>(m);
+  if (threadIdx.x == 0) {
+    int G = gridDim.x, b = blockIdx.x;
+    part[b] = v[0];
+    part[G + b] = m[0].val; part[2 * G + b] = (double)m[0].idx;
+    part[3 * G + b] = m[1].val; part[4 * G + b] = (double)m[1].idx;
+    part[5 * G + b] = v[1];
+  }
+}
 
 // Finalise an update reduction into ctl (deltax, rmax, l2norm, nonfinite).
 __device__ void ctl_finish_update(Ctl *ctl, const double *part, int G) {
@@ -550,10 +608,11 @@ __device__ void ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs,
   }
   if (icnvg != 0 || ctl->l2norm <= refine_factor * ctl->scratch[0] || stag || zero) {
     ctl->north_due = 2;  // request the FP64 true residual
-    // BiCGSTAB restarts from the true residual at every refinement (its
-    // shadow residual is tied to the recurrence); PCG keeps its search
-    // direction unless it stagnated or broke down
-    ctl->restart_due = (bcgs || stag || zero) ? 1 : 0;
+    // Every refinement restarts the recurrence from the true residual: with
+    // FP32 search directions, continuing after a residual replacement costs
+    // more iterations than a restart (measured on the 10M-cell case)
+    (void)bcgs;
+    ctl->restart_due = 1;
     ctl->scratch[1] = ctl->deltax;
     ctl->scratch[2] = (double)ctl->xloc;
   }
@@ -646,10 +705,10 @@ __device__ void ctl_refine(Ctl *ctl, const double *part, int G, unsigned long lo
     ctl->done = 1;
     ctl->exit_reason = kExitItmax;
   } else {
-    // The recurrence residual (of the FP32 matrix) is replaced by the FP64
-    // true residual.  PCG carries on with its search direction, like the
-    // reference's NORTH residual refresh (ImsLinearBase.f90:221-227);
-    // BiCGSTAB, and PCG after a stagnation or breakdown, restart from it.
+    // The FP32 recurrence residual is replaced by the FP64 true residual and
+    // the recurrence restarts from it (restart_due); a recurrence that
+    // carried on instead, like the reference's NORTH residual refresh
+    // (ImsLinearBase.f90:221-227), would keep its search direction.
     ctl->scratch[0] = ctl->l2norm;
     ctl->scratch[3] += 1.0;  // refinement count
     if (ctl->restart_due) {
@@ -900,6 +959,12 @@ void kr_dot64(int n, const double *a, const double *b, double *part, int G, cons
 void kr_dot_tq_tt64(int n, const double *t, const double *q, double *part, int G, const Ctl *ctl, cudaStream_t st) {
   k_dot_tq_tt<double><<<G, kRedBlock, 0, st>>>(n, t, q, part, ctl);
 }
+void kr_dot32(int n, const float *a, const float *b, double *part, int G, const Ctl *ctl, cudaStream_t st) {
+  k_dot<float, float><<<G, kRedBlock, 0, st>>>(n, a, b, part, ctl);
+}
+void kr_dot_tq_tt32(int n, const float *t, const float *q, double *part, int G, const Ctl *ctl, cudaStream_t st) {
+  k_dot_tq_tt<float><<<G, kRedBlock, 0, st>>>(n, t, q, part, ctl);
+}
 void kr_sumsq64(int n, const double *a, double *part, int G, cudaStream_t st) {
   k_sumsq<double><<<G, kRedBlock, 0, st>>>(n, a, part);
 }
@@ -919,6 +984,13 @@ void kr_cg_update64(int n, double *x, double *d, const double *p, const double *
                     int G, const Ctl *ctl, cudaStream_t st) {
   k_cg_update64<<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
 }
+void kr_cg_pupdate32(int n, const float *z, float *p, const Ctl *ctl, cudaStream_t st) {
+  k_cg_pupdate32<<<egrid(n), 256, 0, st>>>(n, z, p, ctl);
+}
+void kr_cg_update_mixed(int n, double *x, float *d, const float *p, const float *q, double *part,
+                        int G, const Ctl *ctl, cudaStream_t st) {
+  k_cg_update_mixed<<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
+}
 void kr_ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
                     cudaStream_t st) {
   k_ctl_cg_cnvg<<<1, kRedBlock, 0, st>>>(ctl, part, G, cond, use_cond);
@@ -932,6 +1004,12 @@ void kr_bcgs_p64(int n, const double *d, double *p, const double *v, const Ctl *
 void kr_bcgs_q64(int n, const double *d, const double *v, double *q, const Ctl *ctl, cudaStream_t st) {
   k_bcgs_q<double><<<egrid(n), 256, 0, st>>>(n, d, v, q, ctl);
 }
+void kr_bcgs_p32(int n, const float *d, float *p, const float *v, const Ctl *ctl, cudaStream_t st) {
+  k_bcgs_p<float><<<egrid(n), 256, 0, st>>>(n, d, p, v, ctl);
+}
+void kr_bcgs_q32(int n, const float *d, const float *v, float *q, const Ctl *ctl, cudaStream_t st) {
+  k_bcgs_q<float><<<egrid(n), 256, 0, st>>>(n, d, v, q, ctl);
+}
 void kr_ctl_omega(Ctl *ctl, const double *part, int G, cudaStream_t st) {
   k_ctl_omega<<<1, kRedBlock, 0, st>>>(ctl, part, G);
 }
@@ -939,6 +1017,11 @@ void kr_bcgs_update64(int n, double *x, double *d, const double *phat, const dou
                       const double *q, const double *t, const double *dscale, double *part, int G,
                       const Ctl *ctl, cudaStream_t st) {
   k_bcgs_update<double><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
+}
+void kr_bcgs_update32(int n, double *x, float *d, const float *phat, const float *qhat,
+                      const float *q, const float *t, const double *dscale, double *part, int G,
+                      const Ctl *ctl, cudaStream_t st) {
+  k_bcgs_update<float><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
 }
 void kr_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
                       cudaStream_t st) {

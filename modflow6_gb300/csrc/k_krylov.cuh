@@ -21,6 +21,14 @@ void kr_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long co
 void kr_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs, double refine_factor, cudaStream_t st);
 void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, double *dhat64, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st);
 void kr_ctl_refine(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond, cudaStream_t st);
+// the mixed form's FP32 inner vectors (FP64 reductions and scalars)
+void kr_dot32(int n, const float *a, const float *b, double *part, int G, const Ctl *ctl, cudaStream_t st);
+void kr_dot_tq_tt32(int n, const float *t, const float *q, double *part, int G, const Ctl *ctl, cudaStream_t st);
+void kr_cg_pupdate32(int n, const float *z, float *p, const Ctl *ctl, cudaStream_t st);
+void kr_cg_update_mixed(int n, double *x, float *d, const float *p, const float *q, double *part, int G, const Ctl *ctl, cudaStream_t st);
+void kr_bcgs_p32(int n, const float *d, float *p, const float *v, const Ctl *ctl, cudaStream_t st);
+void kr_bcgs_q32(int n, const float *d, const float *v, float *q, const Ctl *ctl, cudaStream_t st);
+void kr_bcgs_update32(int n, double *x, float *d, const float *phat, const float *qhat, const float *q, const float *t, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st);
 void kr_f64_to_f32(int n, const double *s, float *d, cudaStream_t st);
 // d = b - A x (CSR, one row per thread; n <= kMaxRedBlocks * kRedBlock) with
 // part (3 * ceil(n/256) doubles) and out (3 doubles: L2, signed max, row).

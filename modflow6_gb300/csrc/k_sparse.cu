@@ -73,9 +73,7 @@ __device__ __forceinline__ double mac<double>(double a, double x, double t) { re
 template <>
 __device__ __forceinline__ float mac<float>(float a, float x, float t) { return fmaf(a, x, t); }
 
-// y = A*x (MODE 0), or d = b - A*x (MODE 1).  Matrix values TM, vectors and
-// accumulation T (TM = float, T = double: the mixed form's FP32 matrix with
-// FP64 vectors).
+// y = A*x (MODE 0), or d = b - A*x (MODE 1).
 template <typename T, int MODE, typename TM = T>
 __global__ void __launch_bounds__(256) k_sell_spmv(int n, const int *__restrict__ ptr,
                                                     const int *__restrict__ col,
@@ -215,12 +213,11 @@ void launch_dia7_spmv64(const Dia7 &D, const double *x, double *y, const Ctl *ct
                                                         nullptr, y, ctl, 0);
 }
 
-
-void launch_dia7_spmv_mixed(const Dia7 &D, const double *x, double *y, const Ctl *ctl,
-                            cudaStream_t st) {
+void launch_dia7_spmv32(const Dia7 &D, const float *x, float *y, const Ctl *ctl,
+                        cudaStream_t st) {
   const int n = D.nlay * D.nrow * D.ncol;
-  k_dia7_spmv<double, 0, float><<<rows_grid(n), 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.f_sv, x,
-                                                               nullptr, y, ctl, 0);
+  k_dia7_spmv<float, 0><<<rows_grid(n), 256, 0, st>>>(D.nlay, D.nrow, D.ncol, D.f_sv, x,
+                                                       nullptr, y, ctl, 0);
 }
 
 void launch_dia7_residual64(const Dia7 &D, const double *x, const double *b, double *d,
@@ -237,12 +234,11 @@ void launch_spmv64(const Sell &S, const double *x, double *y, const Ctl *ctl, cu
                                                           S.nm, S.mctl);
 }
 
-
-void launch_spmv_mixed(const Sell &S, const double *x, double *y, const Ctl *ctl, cudaStream_t st) {
+void launch_spmv32(const Sell &S, const float *x, float *y, const Ctl *ctl, cudaStream_t st) {
   if (S.n == 0) return;
-  k_sell_spmv<double, 0, float><<<rows_grid(S.n), 256, 0, st>>>(S.n, S.d_ptr, S.d_col, S.d_val32,
-                                                                x, nullptr, y, ctl, 0, S.d_slm,
-                                                                S.d_mrow, S.nm, S.mctl);
+  k_sell_spmv<float, 0><<<rows_grid(S.n), 256, 0, st>>>(S.n, S.d_ptr, S.d_col, S.d_val32, x,
+                                                         nullptr, y, ctl, 0, S.d_slm, S.d_mrow,
+                                                         S.nm, S.mctl);
 }
 
 void launch_residual64(const Sell &S, const double *x, const double *b, double *d,

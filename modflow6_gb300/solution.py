@@ -150,6 +150,27 @@ class GwfSolution:
             raise _lib.GbimsError(rc, lib.gbsln_last_error(self._h).decode())
         return amat, rhs
 
+    BUDGET_ENTRIES = ("STO-SS", "STO-SY", "CHD", "WEL", "RCH")
+
+    def budget(self, flowja: bool = False):
+        """Model budget of the last time step (gbsln_budget): rates in/out per
+        entry, totals, percent discrepancy and the largest cell imbalance;
+        with flowja=True also FLOW-JA-FACE (nja, CSR order)."""
+        lib = _lib.load()
+        t = _lib.GbslnBudgetTable()
+        m = self.m
+        njas = (m.nlay * (m.nrow * (m.ncol - 1) + m.ncol * (m.nrow - 1))
+                + (m.nlay - 1) * m.nrow * m.ncol)
+        fj = np.zeros(m.nodes + 2 * njas) if flowja else None
+        rc = lib.gbsln_budget(self._h, _lib.dptr(fj) if fj is not None else None, C.byref(t))
+        if rc < 0:
+            raise _lib.GbimsError(rc, lib.gbsln_last_error(self._h).decode())
+        out = dict(rate_in=np.array(t.rate_in[:]), rate_out=np.array(t.rate_out[:]),
+                   total_in=t.total_in, total_out=t.total_out,
+                   percent_discrepancy=t.percent_discrepancy,
+                   max_cell_imbalance=t.max_cell_imbalance, max_cell=t.max_cell)
+        return (fj, out) if flowja else out
+
     @property
     def heads(self) -> np.ndarray:
         x = np.zeros(self.nodes)

@@ -158,6 +158,7 @@ class WarmStartNet:
         self.nodes = g.m.nodes
         self.nparams = int(self._lib.gbmpnn_param_count())
         self.dh_scale = 1.0  # output scale in asinh units, set by training
+        self.unit_max = 0.0  # bound on |output| (normalised units), set by training; 0 = none
 
     def _err(self):
         return self._lib.gbmpnn_last_error(self._h).decode() if self._h else ""
@@ -225,6 +226,13 @@ def train(net: WarmStartNet, data, dh_scale: float, epochs: int = 4,
     """Adam over every sample of every model, `epochs` times, the learning
     rate halved each epoch; mean loss per epoch."""
     net.dh_scale = dh_scale
+    # predictions are bounded by the largest change seen in training (with a
+    # margin): the network does not extrapolate beyond its data
+    tmax = 0.0
+    for g, _, samples in data:
+        for s in samples:
+            tmax = max(tmax, float(s.target.abs().max().item()))
+    net.unit_max = 1.25 * tmax
     hist = []
     for ep in range(epochs):
         tot, cnt = 0.0, 0
@@ -265,7 +273,10 @@ def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0
             h_prev = torch.from_numpy(warm.heads).cuda()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            dh = from_unit(net.predict(g.features(h_prev, dh_last, dsc)).double() * dsc)
+            y = net.predict(g.features(h_prev, dh_last, dsc))
+            if net.unit_max > 0.0:
+                y = y.clamp(-net.unit_max, net.unit_max)
+            dh = from_unit(y.double() * dsc)
             guess = (h_prev + dh * g.active64).contiguous()
             e1.record()
             e1.synchronize()

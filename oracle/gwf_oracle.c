@@ -482,6 +482,125 @@ void or_bnd_fc(const or_gwf_model *m, const int *ibound, double *amat, double *r
   }
 }
 
+/* gwf.f90:741-830 (gwf_cq, then gwf_bd's csr_diagsum and CHD rates) and the
+ * model budget entries, in package order STO-SS, STO-SY, CHD, WEL, RCH:
+ *  - npf_cq, gwf-npf.f90:745-770 (qcalc :800-865, no perched option);
+ *  - sto_cq, gwf-sto.f90:447-564 (SsTerms/SyTerms rates,
+ *    GwfStorageUtils.f90:32-134);
+ *  - bnd_cq_simrate, BoundaryPackage.f90:583-619 (WEL, then RCH);
+ *  - csr_diagsum, Sparse.f90:262-281;
+ *  - calc_chd_rate, gwf-chd.f90:264-320;
+ *  - rate_accumulator, Budget.f90:631-648.
+ * terms[2k], terms[2k+1]: rate in and out of entry k.  flowja: nja values. */
+void or_gwf_budget(const or_gwf_model *m, const int *ibound, const double *condsat,
+                   const double *sat, double delt, int transient, const double *hold,
+                   const double *hnew, double *flowja, double *terms) {
+  for (int k = 0; k < 10; ++k) terms[k] = 0.0;
+  for (int k = 0; k < m->nja; ++k) flowja[k] = 0.0;
+  /* npf_cq */
+  for (int n = 0; n < m->nodes; ++n) {
+    for (int ii = m->ia[n] + 1; ii < m->ia[n + 1]; ++ii) {
+      int mm = m->ja[ii];
+      if (mm < n) continue;
+      int jj = m->jas[ii];
+      double cond;
+      if (m->ihc[jj] == 0) {
+        cond = vcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm], m->ivarcv,
+                     m->idewatcv, condsat[jj], hnew[n], hnew[mm], m->k33[n], m->k33[mm], sat[n],
+                     sat[mm], m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->hwva[jj]);
+      } else {
+        cond = hcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm], m->inewton,
+                     m->icellavg, condsat[jj], hnew[n], hnew[mm], sat[n], sat[mm], m->k11[n],
+                     m->k11[mm], m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->cl1[jj],
+                     m->cl2[jj], m->hwva[jj]);
+      }
+      double qnm = cond * (hnew[mm] - hnew[n]);
+      flowja[ii] = qnm;
+      flowja[m->isym[ii]] = -qnm;
+    }
+  }
+  /* sto_cq */
+  if (transient) {
+    double tled = 1.0 / delt;
+    for (int n = 0; n < m->nodes; ++n) {
+      if (ibound[n] <= 0) continue;
+      double tp = m->top[n], bt = m->bot[n];
+      int iconvert = m->iconvert[n];
+      double snold = 1.0, snnew = 1.0;
+      if (iconvert != 0) {
+        snold = or_squadratic_sat(tp, bt, hold[n], m->satomega);
+        snnew = or_squadratic_sat(tp, bt, hnew[n], m->satomega);
+      }
+      double sc1 = m->ss[n] * (tp - bt) * m->area[n];
+      double rho1 = sc1 * tled;
+      double rho1old = rho1;
+      double aterm = -rho1 * snnew;
+      double rhsterm;
+      if (iconvert != 0) {
+        double tthk = tp - bt;
+        double zold = bt + 0.5 * tthk * snold;
+        double znew = bt + 0.5 * tthk * snnew;
+        rhsterm = -rho1old * snold * (hold[n] - zold) - rho1 * snnew * znew;
+      } else {
+        rhsterm = -rho1old * snold * hold[n];
+      }
+      double rate = aterm * hnew[n] - rhsterm;
+      int idiag = m->ia[n];
+      flowja[idiag] = flowja[idiag] + rate;
+      if (rate < 0.0) terms[1] = terms[1] - rate;
+      else terms[0] = terms[0] + rate;
+      rate = 0.0;
+      if (iconvert != 0) {
+        double rho2 = m->sy[n] * m->area[n] * tled;
+        double rho2old = rho2;
+        double tthk = tp - bt;
+        rate = rho2old * tthk * snold - rho2 * tthk * snnew;
+      }
+      flowja[idiag] = flowja[idiag] + rate;
+      if (rate < 0.0) terms[3] = terms[3] - rate;
+      else terms[2] = terms[2] + rate;
+    }
+  }
+  /* bnd_cq: WEL, RCH (hcof = 0, rhs as in or_bnd_fc) */
+  for (int i = 0; i < m->nwel; ++i) {
+    int node = m->wel_node[i];
+    double rrate = 0.0;
+    if (ibound[node] > 0) rrate = 0.0 * hnew[node] - (-m->wel_q[i]);
+    flowja[m->ia[node]] = flowja[m->ia[node]] + rrate;
+    if (rrate < 0.0) terms[7] = terms[7] - rrate;
+    else terms[6] = terms[6] + rrate;
+  }
+  for (int i = 0; i < m->nrch; ++i) {
+    int node = m->rch_node[i];
+    double rrate = 0.0;
+    if (ibound[node] > 0) rrate = 0.0 * hnew[node] - (-m->rch_rate[i] * m->area[node]);
+    flowja[m->ia[node]] = flowja[m->ia[node]] + rrate;
+    if (rrate < 0.0) terms[9] = terms[9] - rrate;
+    else terms[8] = terms[8] + rrate;
+  }
+  /* csr_diagsum */
+  for (int n = 0; n < m->nodes; ++n)
+    for (int ii = m->ia[n] + 1; ii < m->ia[n + 1]; ++ii)
+      flowja[m->ia[n]] = flowja[m->ia[n]] + flowja[ii];
+  /* calc_chd_rate */
+  for (int i = 0; i < m->nchd; ++i) {
+    int node = m->chd_node[i];
+    int idiag = m->ia[node];
+    double rate = 0.0, ratein = 0.0, rateout = 0.0;
+    for (int ii = m->ia[node] + 1; ii < m->ia[node + 1]; ++ii) {
+      double q = flowja[ii];
+      rate = rate - q;
+      if (ibound[m->ja[ii]] > 0) {
+        if (q < 0.0) ratein = ratein - q;
+        else rateout = rateout + q;
+      }
+    }
+    flowja[idiag] = flowja[idiag] + rate;
+    terms[4] = terms[4] + ratein;
+    terms[5] = terms[5] + rateout;
+  }
+}
+
 /* gwf.f90:466-555, gwf_fc order for the packages restated here:
  * NPF fc, STO fc, BND fc, then NPF fn, STO fn.  amat and rhs must be zero on
  * entry (NumericalSolution sln_reset). */

@@ -80,6 +80,9 @@ double or_sln_get_dxmax(int neq, const int *active, const double *x, const doubl
                         int *lrch);
 void or_sln_underrelax(or_nonlinear *nl, int kiter, double bigch, int neq,
                        const int *active, double *x, const double *xtemp);
+void or_gwf_budget(const or_gwf_model *m, const int *ibound, const double *condsat,
+                   const double *sat, double delt, int transient, const double *hold,
+                   const double *hnew, double *flowja, double *terms);
 int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
                     const double *condsat, int *ibound, int kper, int kstp, double delt,
                     int transient, double *x, double *xold, or_timestep_stats *st);

@@ -109,6 +109,9 @@ def load():
         lib.or_npf_condsat.argtypes = [C.POINTER(GwfModel), _dp]
         lib.or_gwf_fc.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, C.c_double, C.c_int, _dp, _dp, _dp, _dp]
         lib.or_sln_ls_fixups.argtypes = [C.c_int, _ip, _ip, _ip, C.c_int, _dp, _dp, _dp, _dp]
+        lib.or_npf_cf.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp]
+        lib.or_gwf_budget.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, C.c_double, C.c_int, _dp,
+                                      _dp, _dp, _dp]
         lib.or_gwf_timestep.argtypes = [C.POINTER(GwfModel), C.c_void_p, C.POINTER(Nonlinear), _dp, _ip,
                                         C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp,
                                         C.POINTER(TimestepStats)]
@@ -274,6 +277,39 @@ class Gwf:
         self.lib.or_sln_ls_fixups(x.size, ip(self.con["ia"]), ip(self.con["ja"]), ip(self.ibound),
                                   int(isymmetric), dp(amat), dp(rhs), dp(x), dp(xtemp))
         return amat, rhs
+
+    def sat(self, hnew):
+        """npf_cf: cell saturation at the given heads."""
+        s = np.zeros(self.m.nodes)
+        h = np.ascontiguousarray(hnew, np.float64)
+        self.lib.or_npf_cf(C.byref(self.model), ip(self.ibound), dp(h), dp(s))
+        return s
+
+    def budget(self, hnew, hold=None, delt=0.0, transient=False, sat=None):
+        """gwf_cq + gwf_bd (or_gwf_budget): FLOW-JA-FACE and the model budget
+        (entries STO-SS, STO-SY, CHD, WEL, RCH; totals and percent difference
+        summed in entry order, Budget.f90:250-266).  sat defaults to npf_cf at
+        hnew."""
+        hnew = np.ascontiguousarray(hnew, np.float64)
+        hold = np.ascontiguousarray(hnew if hold is None else hold, np.float64)
+        sat = self.sat(hnew) if sat is None else np.ascontiguousarray(sat, np.float64)
+        flowja = np.zeros(self.con["nja"])
+        terms = np.zeros(10)
+        self.lib.or_gwf_budget(C.byref(self.model), ip(self.ibound), dp(self.condsat), dp(sat), delt,
+                               int(transient), dp(hold), dp(hnew), dp(flowja), dp(terms))
+        rin, rout = terms[0::2].copy(), terms[1::2].copy()
+        tin = tout = 0.0
+        for k in range(5):
+            tin += rin[k]
+            tout += rout[k]
+        avg = (tin + tout) / 2.0
+        pd = 100.0 * (tin - tout) / avg if avg != 0.0 else 0.0
+        act = self.ibound > 0
+        diag = flowja[self.con["ia"][:-1]]
+        imb = np.abs(np.where(act, diag, 0.0))
+        return flowja, dict(rate_in=rin, rate_out=rout, total_in=tin, total_out=tout,
+                            percent_discrepancy=pd, max_cell_imbalance=float(imb.max()),
+                            max_cell=int(imb.argmax()) if imb.max() > 0 else -1)
 
     def timestep(self, kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-3, mxiter=25,
                  nonmeth=0, theta=1.0, akappa=0.0, gamma=1.0, amomentum=0.0, iallowptc=1):

@@ -106,3 +106,55 @@ def test_c2_full_size_matches_oracle_record(gblib):
     assert abs(st["inner_total"] - rec["stats"]["inner_total"]) <= 2, st["inner_total"]
     assert abs(h.sum() - rec["head_checksum"]) <= 1e-5 * m.nodes
     assert abs(h.min() - rec["head_min"]) <= 1e-4 and abs(h.max() - rec["head_max"]) <= 1e-4
+
+
+def _budget_pair(m, sol, g, delt, hold):
+    """GPU budget at the solution's heads (saturation from a formulate at
+    those heads) beside the oracle's on the same heads."""
+    x = sol.heads
+    transient = m.ss is not None and delt > 0.0
+    sol.formulate(delt=delt, hold=hold if transient else None)
+    fj, bg = sol.budget(flowja=True)
+    fo, bo = g.budget(x, hold=hold, delt=delt, transient=transient)
+    return fj, bg, fo, bo
+
+
+@pytest.mark.parametrize("name,scale", [("c1", 1.0), ("c3", 0.04)])
+def test_budget_bitexact(gblib, name, scale):
+    """FLOW-JA-FACE bit for bit (npf_cq, sto_cq, bnd_cq, csr_diagsum, CHD
+    rates in the reference's order); the model budget entries to rounding
+    of the reduction order."""
+    m = make_config(name, seed=4, scale=scale)
+    g = oracle.Gwf(m, oracle.settings())
+    sol = GwfSolution(m, ImsLinearSettings(), Nonlinear())
+    rng = np.random.default_rng(5)
+    sol.heads = m.strt + rng.uniform(-2.0, 2.0, m.nodes)
+    hold = m.strt + rng.uniform(-2.0, 2.0, m.nodes)
+    delt = 3.0 if m.ss is not None else 0.0
+    fj, bg, fo, bo = _budget_pair(m, sol, g, delt, hold)
+    np.testing.assert_array_equal(fj, fo)
+    scale_in = max(bo["total_in"], 1e-300)
+    np.testing.assert_allclose(bg["rate_in"], bo["rate_in"], rtol=1e-12, atol=1e-12 * scale_in)
+    np.testing.assert_allclose(bg["rate_out"], bo["rate_out"], rtol=1e-12, atol=1e-12 * scale_in)
+    assert bg["max_cell"] == bo["max_cell"]
+    assert bg["max_cell_imbalance"] == bo["max_cell_imbalance"]
+    sol.close()
+
+
+def test_budget_after_solve_within_reference_discrepancy(gblib):
+    """After a converged time step the model budget of the GPU solution is as
+    closed as the oracle's own: percent discrepancy within 10x the oracle's
+    (plus 1e-6 %), entries within the tolerance the head closure allows."""
+    m = make_config("c1", seed=0)
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=1000)
+    g = oracle.Gwf(m, oracle.settings(**tol))
+    g.timestep(kper=1, kstp=1, delt=1.0, dvclose=1e-8, mxiter=10)
+    _, bo = g.budget(g.x)
+    sol = GwfSolution(m, ImsLinearSettings(structure=(1, 100, 100), **tol), Nonlinear(dvclose=1e-8, mxiter=10))
+    assert sol.timestep(1, 1, 1.0)["converged"] == 1
+    bg = sol.budget()
+    print(bg["percent_discrepancy"], bo["percent_discrepancy"])
+    assert abs(bg["percent_discrepancy"]) <= 10.0 * abs(bo["percent_discrepancy"]) + 1e-6
+    np.testing.assert_allclose(bg["rate_in"], bo["rate_in"], rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(bg["rate_out"], bo["rate_out"], rtol=1e-6, atol=1e-9)
+    sol.close()
