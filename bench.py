@@ -273,10 +273,16 @@ def gb_arm(a):
     def run_form(precision, clocks=False):
         sol = GwfSolution(m, ImsLinearSettings(precision=precision, structure=shape, **C2_IMS), nl)
         stats = []
-        for _ in range(a.warmup):
+        tuning = None
+        for i in range(a.warmup):
             sol.restart()
             st = sol.timestep(1, 1, 1.0)
             assert st["converged"] == 1, st
+            if i == 0:
+                # the autotuner picks the sweep tiling and reduction grid on
+                # the factored system; the later warm-up steps re-capture
+                # the inner-loop graph with them
+                tuning = autotune(lib, sol.ims_handle())
         ims_h = sol.ims_handle()
         l0 = lib.gbims_kernel_launches(ims_h)
         barrier()
@@ -298,9 +304,9 @@ def gb_arm(a):
         # fix-ups, dxmax per outer iteration, CHD reset per step
         launches += sum(4 * s["outer"] + 1 for s in stats)
         heads = sol.heads
-        return sol, ms, stats, launches, sampler.summary() if sampler else None, heads
+        return sol, ms, stats, launches, sampler.summary() if sampler else None, heads, tuning
 
-    sol64, ms64, st64, launches64, clocks, h64 = run_form(_lib.GBIMS_FP64, clocks=True)
+    sol64, ms64, st64, launches64, clocks, h64, tune64 = run_form(_lib.GBIMS_FP64, clocks=True)
     ms64 = maxr(ms64)
     # per-kernel device times (CUDA events on the library stream) for the roofline
     kt = _lib.GbimsKernelTimes()
@@ -314,7 +320,7 @@ def gb_arm(a):
                 "with the skew/unskew permutes)")
     mixed = None
     if not a.no_mixed:
-        solm, msm, stm, lm, _, hm = run_form(_lib.GBIMS_MIXED)
+        solm, msm, stm, lm, _, hm, tunem = run_form(_lib.GBIMS_MIXED)
         msm = maxr(msm)
         ktm = _lib.GbimsKernelTimes()
         lib.gbims_time_kernels(solm.ims_handle(), 20, C.byref(ktm))
@@ -322,7 +328,8 @@ def gb_arm(a):
                  "outer_iterations": stm[-1]["outer"],
                  "max_head_diff_vs_fp64": float(np.max(np.abs(hm - h64))),
                  "spmv_fp32_gbs": ktm.spmv_bytes / (ktm.spmv_ms * 1e-3) / 1e9,
-                 "precond_fp32_ms": ktm.precond_ms, "spmv_fp32_ms": ktm.spmv_ms}
+                 "precond_fp32_ms": ktm.precond_ms, "spmv_fp32_ms": ktm.spmv_ms,
+                 "tuning": tunem}
         solm.close()
     # e2e: the same FP64 step through the C ABI with host buffers
     e2e = None
@@ -399,7 +406,8 @@ def gb_arm(a):
                           "traffic": traffic.get("spmv_fp64_bytes_per_launch")},
         "kernels": {"spmv_ms": kt.spmv_ms, "spmv_gbs": spmv_gbs, "precond_ms": kt.precond_ms,
                     "precond_gbs": pre_gbs, "dot_ms": kt.dot_ms, "update_ms": kt.update_ms},
-        "e2e": e2e, "gpu_launches": int(launches64), "clocks": clocks, "ensemble": ens,
+        "e2e": e2e, "gpu_launches": int(launches64), "clocks": clocks, "tuning": tune64,
+        "ensemble": ens,
         "warm_start": ws_res,
     }
     if rank == 0 and not a.no_cpu:
@@ -408,6 +416,26 @@ def gb_arm(a):
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def autotune(lib, h, reps=5):
+    """gbims_autotune on a factored handle: the chosen wavefront tiling and
+    reduction grid, with the time of every tiling tried."""
+    import ctypes as C
+    from modflow6_gb300 import _lib
+    t = _lib.GbimsTuning()
+    rc = lib.gbims_autotune(h, reps, C.byref(t))
+    assert rc == 0, lib.gbims_last_error(h)
+    out = {"reduction_blocks": t.reduction_blocks}
+    if t.level_mode >= 0:
+        out.update(level_mode=("sync-free" if t.level_mode == 1 else "per-level launches"),
+                   level_ms=[round(t.level_ms[0], 4), round(t.level_ms[1], 4)])
+    if t.sweep_config >= 0:
+        out.update(sweep_chunk=t.sweep_chunk, sweep_ring=t.sweep_ring,
+                   sweep_prefetch=t.sweep_prefetch, sweep_occupancy=t.sweep_occupancy,
+                   precond_ms=t.precond_ms,
+                   candidates_ms=[round(t.candidate_ms[i], 4) for i in range(t.ncandidates)])
+    return out
 
 
 def ensemble_form(a, lib, barrier, maxr) -> dict:
@@ -435,9 +463,12 @@ def ensemble_form(a, lib, barrier, maxr) -> dict:
     d_x0 = torch.from_numpy(x0).to(dev)
     d_x = d_x0.clone()
     res = None
-    for _ in range(a.warmup):
+    tuning = None
+    for i in range(a.warmup):
         d_x.copy_(d_x0)
         res = ens.apply_device(d_amat.data_ptr(), d_rhs.data_ptr(), d_x.data_ptr())
+        if i == 0:
+            tuning = autotune(lib, ens._h, reps=3)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -456,7 +487,8 @@ def ensemble_form(a, lib, barrier, maxr) -> dict:
             "members_per_s": count / (ms / 1e3), "converged": conv,
             "inner_iterations": {"min": int(its.min()), "mean": float(its.mean()),
                                  "max": int(its.max())},
-            "form": "FP64 batched PCG + wavefront ILU0, one CUDA graph for all members"}
+            "form": "FP64 batched PCG + wavefront ILU0, one CUDA graph for all members",
+            "tuning": tuning}
 
 
 def warmstart_form(a) -> dict:
@@ -525,6 +557,7 @@ def kernels_arm(a):
         ims.imslinear_allocate(m.nodes, con["ia"], con["ja"])
         rc = lib.gbims_factor(ims._h, _lib.dptr(amat), None)
         assert rc >= 0, lib.gbims_last_error(ims._h)
+        tuning = autotune(lib, ims._h)
         kt = _lib.GbimsKernelTimes()
         rc = lib.gbims_time_kernels(ims._h, max(1, a.steps), C.byref(kt))
         assert rc == 0, lib.gbims_last_error(ims._h)
@@ -532,7 +565,8 @@ def kernels_arm(a):
                      "update_ms": kt.update_ms,
                      "spmv_gbs": kt.spmv_bytes / (kt.spmv_ms * 1e-3) / 1e9,
                      "precond_gbs": kt.precond_bytes / (kt.precond_ms * 1e-3) / 1e9,
-                     "spmv_bytes": kt.spmv_bytes, "precond_bytes": kt.precond_bytes}
+                     "spmv_bytes": kt.spmv_bytes, "precond_bytes": kt.precond_bytes,
+                     "tuning": tuning}
         ims.imslinear_da()
     print(json.dumps(out), flush=True)
 

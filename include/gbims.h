@@ -147,6 +147,34 @@ typedef struct gbims_kernel_times {
 } gbims_kernel_times;
 int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times *t);
 
+/* Autotuner (no counterpart in the reference, which has no tunable kernels):
+ * on the handle's own factored system it times every wavefront tiling of
+ * the structured sweeps (chunk of steps per ring buffer, ring depth,
+ * neighbour-word prefetch depth, CTAs per SM), the form of the level-
+ * scheduled sweeps of other patterns, and the thread-block count of the
+ * dot/update reductions, and keeps the fastest for the following applies.
+ * The tiling does not change any cell's arithmetic; the reduction grid only
+ * changes the order in which the partial sums are added.  Batched handles
+ * tune the tiling only.  reps: timed applications per candidate. */
+typedef struct gbims_tuning {
+  int sweep_config;                 /* chosen tiling, -1 when the handle has no wavefront sweeps */
+  int sweep_chunk, sweep_ring, sweep_prefetch;
+  int sweep_occupancy;              /* 0: as many sweep CTAs per SM as fit; 2: at most two */
+  int reduction_blocks;             /* chosen reduction grid (0: batched handle) */
+  int level_mode;                   /* level-scheduled sweeps (handles without wavefront
+                                       sweeps): 0 one launch per level, 1 one sync-free
+                                       launch per sweep; -1 not applicable */
+  double level_ms[2];               /* one ILU0 application in each level mode */
+  int ncandidates;                  /* tilings timed */
+  double candidate_ms[16];          /* one ILU0 application per tiling */
+  double precond_ms;                /* of the chosen tiling */
+  double vector_ms;                 /* dot + update at the chosen grid */
+} gbims_tuning;
+int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out);
+/* Applies a tuning found earlier (sweep_config < 0, reduction_blocks <= 0 or
+ * level_mode < 0 leave that part unchanged). */
+int gbims_set_tuning(gbims_handle *h, int sweep_config, int reduction_blocks, int level_mode);
+
 int gbims_factor(gbims_handle *h, const double *amat, int *pivot_retries);
 int gbims_get_apc(gbims_handle *h, double *apc);
 int gbims_matvec(gbims_handle *h, const double *x, double *y);

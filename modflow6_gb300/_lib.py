@@ -87,6 +87,15 @@ class GbslnStats(C.Structure):
     ]
 
 
+class GbimsTuning(C.Structure):
+    _fields_ = [
+        ("sweep_config", C.c_int), ("sweep_chunk", C.c_int), ("sweep_ring", C.c_int),
+        ("sweep_prefetch", C.c_int), ("sweep_occupancy", C.c_int), ("reduction_blocks", C.c_int),
+        ("level_mode", C.c_int), ("level_ms", C.c_double * 2), ("ncandidates", C.c_int),
+        ("candidate_ms", C.c_double * 16), ("precond_ms", C.c_double), ("vector_ms", C.c_double),
+    ]
+
+
 class GbslnBudgetTable(C.Structure):
     _fields_ = [
         ("rate_in", C.c_double * 5), ("rate_out", C.c_double * 5), ("total_in", C.c_double),
@@ -133,6 +142,8 @@ _SIGS = {
     "gbsln_last_error": (C.c_char_p, [C.c_void_p]),
     "gbsln_restart": (C.c_int, [C.c_void_p]),
     "gbsln_budget": (C.c_int, [C.c_void_p, _dp, C.POINTER(GbslnBudgetTable)]),
+    "gbims_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(GbimsTuning)]),
+    "gbims_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "gbsln_get_heads": (C.c_int, [C.c_void_p, _dp]),
     "gbsln_set_heads": (C.c_int, [C.c_void_p, _dp]),
     "gbsln_ims": (C.c_void_p, [C.c_void_p]),

@@ -51,6 +51,9 @@ struct gbims_handle {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   bool graph_tried = false, graph_ok = false;
+  bool no_graph = false;   // GBIMS_GRAPH=0: the host drives the loop
+  LevelWords LW;           // the level-scheduled sweeps' result words (unstructured handles)
+  int G_alloc = 0;         // reduction blocks the partials were sized for
   double refine_factor = 1.0e-5;  // 1e-4 saves 3 % of the iterations but loses accuracy with BiCGSTAB
   bool factored = false;
   // batched ensemble (nm > 0): members concatenated into one block-diagonal
@@ -89,15 +92,40 @@ static int fail(gbims_handle *h, int code, const std::string &msg) {
 // ---------------------------------------------------------------------------
 // graph body: one inner iteration
 // ---------------------------------------------------------------------------
+// The sync-free level sweeps' words, allocated (zeroed) before their first
+// use; a handle with wavefront sweeps never needs them.
+static int ensure_level_words(gbims_handle *h) {
+  if (h->structured || h->LW.fwd) return GBIMS_OK;
+  const size_t wb = (size_t)h->n * (h->mixed ? 8 : 16);
+  GB_CUDA(h, cudaMalloc(&h->LW.fwd, wb));
+  GB_CUDA(h, cudaMalloc(&h->LW.bwd, wb));
+  GB_CUDA(h, cudaMalloc((void **)&h->LW.ticket, 256));
+  GB_CUDA(h, cudaMalloc((void **)&h->LW.err, sizeof(int)));
+  GB_CUDA(h, cudaMemset(h->LW.fwd, 0, wb));
+  GB_CUDA(h, cudaMemset(h->LW.bwd, 0, wb));
+  GB_CUDA(h, cudaMemset(h->LW.ticket, 0, 256));
+  GB_CUDA(h, cudaMemset(h->LW.err, 0, sizeof(int)));
+  return GBIMS_OK;
+}
+
+// A level sweep whose wait ran out (reported by the kernels' error word).
+static int level_words_error(gbims_handle *h) {
+  if (h->structured || !h->LW.err) return GBIMS_OK;
+  int e = 0;
+  GB_CUDA(h, cudaMemcpy(&e, h->LW.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return fail(h, GBIMS_ERR_CUDA, "level sweep wait limit reached");
+  return GBIMS_OK;
+}
+
 static void precond64(gbims_handle *h, const double *r, double *z) {
   if (h->structured) launch_dia7_apply64(h->D, r, z, h->d_ctl, h->st);
-  else launch_ilu_apply_levels(h->n, h->d_iapc, h->d_japc, h->d_apc, h->F, h->B, r, z, h->d_ctl, h->st);
+  else launch_ilu_apply_levels(h->n, h->d_iapc, h->d_japc, h->d_apc, h->F, h->B, h->LW, r, z, h->d_ctl, h->st);
 }
 
 // The mixed form's preconditioner: FP32 factors, vectors and sweeps.
 static void precond32(gbims_handle *h, const float *r, float *z) {
   if (h->structured) launch_dia7_apply32(h->D, r, z, h->d_ctl, h->st);
-  else launch_ilu_apply_levels32(h->n, h->d_iapc, h->d_japc, h->d_apc32, h->F, h->B, r, z, h->d_ctl, h->st);
+  else launch_ilu_apply_levels32(h->n, h->d_iapc, h->d_japc, h->d_apc32, h->F, h->B, h->LW, r, z, h->d_ctl, h->st);
 }
 
 // A*x and b - A*x: index-free on full DIS grids, SELL-32 otherwise.
@@ -327,7 +355,8 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   // GBIMS_GRAPH=0: the inner loop is driven from the host (the same kernels,
   // launched one by one), for profilers that do not see kernel nodes inside
   // conditional graphs
-  if (const char *g = std::getenv("GBIMS_GRAPH")) h->graph_tried = (g[0] == '0');
+  if (const char *g = std::getenv("GBIMS_GRAPH")) h->no_graph = (g[0] == '0');
+  h->graph_tried = h->no_graph;
   // GBIMS_REFINE: the mixed form's relative L2 reduction per refinement
   if (const char *r = std::getenv("GBIMS_REFINE")) {
     const double v = std::atof(r);
@@ -456,6 +485,7 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
     }
   }
   h->G = std::max(1, std::min(kMaxRedBlocks, (neq + kRedBlock - 1) / kRedBlock));
+  h->G_alloc = h->G;
   GB_CUDA(h, dalloc(&h->d_part, (size_t)h->G * 8));
   GB_CUDA(h, dalloc(&h->d_ctl, 1));
   GB_CUDA(h, cudaMallocHost((void **)&h->h_ctl, sizeof(Ctl)));
@@ -526,6 +556,7 @@ static int factor_core(gbims_handle *h) {
 
 static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_iter,
                       gbims_summary *summary) {
+  if (int rc = ensure_level_words(h)) return rc;
   const int n = h->n;
   cudaStream_t st = h->st;
   (void)kiter;
@@ -623,6 +654,7 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
     GB_CUDA(h, cudaMemcpy(&derr, h->D.d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (derr) return fail(h, GBIMS_ERR_CUDA, "structured sweep wait limit reached");
   }
+  if (int rc = level_words_error(h)) return rc;
   return icount > 0 ? GBIMS_WARN_PIVOT : GBIMS_OK;
 }
 
@@ -690,6 +722,7 @@ extern "C" int gbims_matvec(gbims_handle *h, const double *x, double *y) {
 
 extern "C" int gbims_precondition(gbims_handle *h, const double *r, double *z) {
   if (!h || !r || !z) return GBIMS_ERR_ARG;
+  if (int rc = ensure_level_words(h)) return rc;
   if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no factor: call gbims_factor or gbims_apply first");
   GB_CUDA(h, cudaMemcpyAsync(h->v_d, r, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
   // a control block with done = 0 lets the gated sweep kernels run
@@ -711,8 +744,164 @@ extern "C" int gbims_precondition(gbims_handle *h, const double *r, double *z) {
   return GBIMS_OK;
 }
 
+// The inner-loop graph holds launch parameters (reduction blocks, sweep
+// tiling): after a change it is captured again at the next apply.
+static void drop_graph(gbims_handle *h) {
+  if (h->exec) cudaGraphExecDestroy(h->exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  h->exec = nullptr;
+  h->graph = nullptr;
+  h->graph_ok = false;
+  h->graph_tried = h->no_graph;
+}
+
+// Times the wavefront tilings and the reduction grid on the handle's own
+// (factored) system and keeps the fastest.  Neither choice changes the
+// arithmetic of a cell: the sweeps compute every cell in the same order
+// whatever the tiling; the reduction grid changes only the order in which
+// dot-product partials are summed.
+extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
+  if (!h || !out || reps <= 0) return GBIMS_ERR_ARG;
+  if (int rc = ensure_level_words(h)) return rc;
+  if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no factor: call gbims_factor or an apply first");
+  memset(out, 0, sizeof(*out));
+  out->sweep_config = -1;
+  const int n = h->n;
+  cudaStream_t st = h->st;
+  // control blocks that let every kernel run (batch members included)
+  Ctl c;
+  memset(&c, 0, sizeof(c));
+  c.pivot_fail = INT_MAX;
+  c.alpha = 1.0e-30;  // keeps x unchanged to rounding in the update timing
+  *h->h_ctl = c;
+  GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+  if (h->nm > 0) GB_CUDA(h, cudaMemsetAsync(h->d_ctls, 0, sizeof(Ctl) * h->nm, st));
+  const int eg = std::min(4 * kNumSM, (n + 255) / 256);
+  if (!h->mixed) {
+    k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
+    GB_CUDA(h, cudaMemcpyAsync(h->v_p, h->d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  } else {
+    kr_f64_to_f32(n, h->d_x, h->f_p, st);
+    GB_CUDA(h, cudaMemsetAsync(h->f_q, 0, sizeof(float) * n, st));
+    GB_CUDA(h, cudaMemsetAsync(h->f_d, 0, sizeof(float) * n, st));
+  }
+  auto time_it = [&](auto &&fn) -> double {
+    fn();
+    cudaEventRecord(h->ev0, st);
+    for (int r = 0; r < reps; ++r) fn();
+    cudaEventRecord(h->ev1, st);
+    cudaEventSynchronize(h->ev1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    return ms / reps;
+  };
+  if (h->structured) {
+    const int nc = std::min(dia7_num_cfgs(), (int)(sizeof(out->candidate_ms) / sizeof(double)));
+    int best = 0;
+    double bt = 1e300;
+    for (int i = 0; i < nc; ++i) {
+      h->D.cfg = i;
+      const double ms = time_it([&] {
+        if (!h->mixed) precond64(h, h->v_p, h->v_z);
+        else precond32(h, h->f_p, h->f_z);
+      });
+      out->candidate_ms[i] = ms;
+      if (ms < bt) {
+        bt = ms;
+        best = i;
+      }
+    }
+    int err = 0;
+    GB_CUDA(h, cudaMemcpy(&err, h->D.d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+      cudaMemset(h->D.d_err, 0, sizeof(int));
+      return fail(h, GBIMS_ERR_CUDA, "structured sweep wait limit reached while tuning");
+    }
+    h->D.cfg = best;
+    out->ncandidates = nc;
+    out->sweep_config = best;
+    dia7_cfg(best, &out->sweep_chunk, &out->sweep_ring, &out->sweep_prefetch, &out->sweep_occupancy);
+    out->precond_ms = bt;
+  }
+  out->level_mode = -1;
+  if (!h->structured) {
+    // level-scheduled sweeps: one launch per level, or one sync-free launch
+    // per sweep
+    double bt = 1e300;
+    int best = 1;
+    for (int mode = 0; mode < 2; ++mode) {
+      h->LW.mode = mode;
+      const double ms = time_it([&] {
+        if (!h->mixed) precond64(h, h->v_p, h->v_z);
+        else precond32(h, h->f_p, h->f_z);
+      });
+      out->level_ms[mode] = ms;
+      if (ms < bt) {
+        bt = ms;
+        best = mode;
+      }
+    }
+    if (int rc = level_words_error(h)) return rc;
+    h->LW.mode = best;
+    out->level_mode = best;
+    out->precond_ms = bt;
+  }
+  if (h->nm == 0) {
+    // reduction blocks: multiples of the SM count up to the allocated grid
+    int best = h->G;
+    double bt = 1e300;
+    std::vector<int> cand;
+    for (int g = kNumSM; g < h->G_alloc; g *= 2) cand.push_back(g);
+    cand.push_back(h->G_alloc);
+    for (int g : cand) {
+      const double ms = time_it([&] {
+        if (!h->mixed) {
+          kr_dot64(n, h->v_p, h->v_q, h->d_part, g, h->d_ctl, st);
+          kr_cg_update64(n, h->v_z, h->v_d, h->v_p, h->v_q, h->d_part, g, h->d_ctl, st);
+        } else {
+          kr_dot32(n, h->f_p, h->f_q, h->d_part, g, h->d_ctl, st);
+          kr_cg_update_mixed(n, h->v_d, h->f_d, h->f_p, h->f_q, h->d_part, g, h->d_ctl, st);
+        }
+      });
+      if (ms < bt) {
+        bt = ms;
+        best = g;
+      }
+    }
+    h->G = best;
+    out->reduction_blocks = best;
+    out->vector_ms = bt;
+  }
+  GB_CUDA(h, cudaGetLastError());
+  drop_graph(h);
+  return GBIMS_OK;
+}
+
+extern "C" int gbims_set_tuning(gbims_handle *h, int sweep_config, int reduction_blocks,
+                                int level_mode) {
+  if (!h) return GBIMS_ERR_ARG;
+  if (level_mode >= 0) {
+    if (h->structured || level_mode > 1)
+      return fail(h, GBIMS_ERR_ARG, "level mode out of range (or a structured handle)");
+    h->LW.mode = level_mode;
+  }
+  if (sweep_config >= 0) {
+    if (!h->structured || sweep_config >= dia7_num_cfgs())
+      return fail(h, GBIMS_ERR_ARG, "sweep configuration out of range (or not a structured handle)");
+    h->D.cfg = sweep_config;
+  }
+  if (reduction_blocks > 0) {
+    if (h->nm > 0 || reduction_blocks > h->G_alloc)
+      return fail(h, GBIMS_ERR_ARG, "reduction blocks out of range (or a batch handle)");
+    h->G = reduction_blocks;
+  }
+  drop_graph(h);
+  return GBIMS_OK;
+}
+
 extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times *t) {
   if (!h || !t || reps <= 0) return GBIMS_ERR_ARG;
+  if (int rc = ensure_level_words(h)) return rc;
   if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no factor: call gbims_factor or gbims_apply first");
   const int n = h->n;
   cudaStream_t st = h->st;
@@ -783,7 +972,7 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->f_q, h->f_z, h->f_t, h->f_v, h->f_dhat, h->f_phat, h->f_qhat, h->d_part,
                   h->d_dscale, h->d_dscale2, h->d_cptr, h->d_cpos, h->D.d_sv, h->D.f_sv,
                   h->d_bcm, h->d_bcr, h->d_bmc, h->d_bmr, h->d_ctls, h->D.d_geo, h->S.d_slm,
-                  h->d_ctl};
+                  h->LW.fwd, h->LW.bwd, h->LW.ticket, h->LW.err, h->d_ctl};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
@@ -925,6 +1114,7 @@ extern "C" int gbims_batch_create(const gbims_settings *settings, int nmembers,
 
 static int batch_apply_core(gbims_handle *h, int kstp, int *icnvg, int *in_iter,
                             gbims_summary *summaries) {
+  if (int rc = ensure_level_words(h)) return rc;
   const int n = h->n, nm = h->nm;
   cudaStream_t st = h->st;
   GB_CUDA(h, cudaEventRecord(h->ev0, st));

@@ -111,6 +111,17 @@ struct Levels {
   int maxwidth = 0;
 };
 
+// The level-scheduled sweeps' form: mode 0 launches one kernel per level;
+// mode 1 runs each sweep as one sync-free launch over result words tagged
+// with the launch's epoch (fwd, bwd: n words each, 16 bytes in FP64, 8 in
+// FP32, zeroed once; ticket: two counters, 128 bytes apart, zeroed once).
+struct LevelWords {
+  int mode = 1;
+  void *fwd = nullptr, *bwd = nullptr;
+  unsigned long long *ticket = nullptr;
+  int *err = nullptr;
+};
+
 // One full DIS grid ("member") of the wavefront layout.  A single model is
 // one member; a batched ensemble has one per model, laid end to end.
 struct Dia7Geo {
@@ -133,6 +144,7 @@ struct Dia7 {
   Dia7Geo *d_geo = nullptr;
   const Ctl *mctl = nullptr;  // batched ensembles: members that are done are skipped
   int ntickets = 0, nptiles = 0;
+  int cfg = 0;  // sweep configuration (chunk, ring, prefetch): an index of dia7_cfg
   // forward tiles: lower coefficients (unit diagonal) z (layer above),
   // y (row behind), x (column left); backward tiles: dinv*U for z, y, x and
   // dinv; zero where the neighbour or the cell does not exist
@@ -158,6 +170,10 @@ struct Dia7 {
 // aligned segments that can run past the last cell.
 constexpr int kVecPad = 256;
 void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, long long *slots);
+// The wavefront sweep configurations: chunk C, ring depth NS, prefetch PF,
+// occupancy cap OCC (0: as many CTAs per SM as fit, 2: at most two).
+int dia7_num_cfgs();
+void dia7_cfg(int i, int *C, int *NS, int *PF, int *OCC);
 // Members (nlay, nrow, ncol) and their first rows -> D.geo, D.slots,
 // D.ntickets, D.nptiles (host side; the caller uploads D.geo to D.d_geo).
 void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long long> &row0,
@@ -187,10 +203,12 @@ void launch_ilu_factor(int n, const int *d_ia, const int *d_ja, const double *d_
                        Ctl *ctl, cudaStream_t st);
 void launch_ilu_apply_levels(int n, const int *d_iapc, const int *d_japc,
                              const double *d_apc, const Levels &F, const Levels &B,
-                             const double *r, double *d, const Ctl *ctl, cudaStream_t st);
+                             const LevelWords &Wd, const double *r, double *d, const Ctl *ctl,
+                             cudaStream_t st);
 void launch_ilu_apply_levels32(int n, const int *d_iapc, const int *d_japc,
                                const float *d_apc32, const Levels &F, const Levels &B,
-                               const float *r, float *d, const Ctl *ctl, cudaStream_t st);
+                               const LevelWords &Wd, const float *r, float *d, const Ctl *ctl,
+                               cudaStream_t st);
 
 bool dia7_matches(int nlay, int nrow, int ncol, int n, const std::vector<int> &ia,
                   const std::vector<int> &ja);

@@ -51,19 +51,17 @@
 // dependent operations on the critical path.  The forward input and the
 // backward output are in natural order: k_dia7_skew / k_dia7_unskew permute
 // them with coalesced row accesses.
+#include <algorithm>
+#include <cstdlib>
+
 #include "gbims_internal.cuh"
+#include "k_llword.cuh"
 
 namespace gb {
 
 namespace {
 
-constexpr unsigned long long kWaitNs = 2000000000ULL;  // 2 s per wait
 
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);
 }
@@ -110,46 +108,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
       : "memory");
 }
 
-// One result element with its sweep epoch.  The epoch travels in the same
-// naturally aligned 8-byte access as the data it guards (FP64: both halves
-// carry it), so a consumer that reads the current epoch holds the value:
-// no fence and no progress counter stand between producer and consumer.
-template <typename T>
-struct LLWord;
-template <>
-struct alignas(16) LLWord<double> { unsigned long long v[2]; };
-template <>
-struct alignas(8) LLWord<float> { unsigned long long v; };
-
-__device__ __forceinline__ void ll_put(LLWord<double> *p, double x, unsigned ep) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned long long f = (unsigned long long)ep << 32;
-  asm volatile("st.relaxed.gpu.global.v2.b64 [%0], {%1, %2};" ::"l"(p), "l"((b & 0xffffffffULL) | f),
-               "l"((b >> 32) | f)
-               : "memory");
-}
-__device__ __forceinline__ void ll_put(LLWord<float> *p, float x, unsigned ep) {
-  const unsigned long long v = (unsigned long long)__float_as_uint(x) | ((unsigned long long)ep << 32);
-  asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-__device__ __forceinline__ bool ll_get(const LLWord<double> *p, unsigned ep, double &x) {
-  unsigned long long a, b;
-  asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
-  x = __longlong_as_double((long long)((a & 0xffffffffULL) | (b << 32)));
-  return (unsigned)(a >> 32) == ep && (unsigned)(b >> 32) == ep;
-}
-__device__ __forceinline__ bool ll_get(const LLWord<float> *p, unsigned ep, float &x) {
-  unsigned long long a;
-  asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(a) : "l"(p) : "memory");
-  x = __uint_as_float((unsigned)a);
-  return (unsigned)(a >> 32) == ep;
-}
-// The value of a word known to be complete (read by a later kernel, or
-// staged in shared memory after its kernel ended).
-__device__ __forceinline__ double ll_val(const LLWord<double> &w) {
-  return __longlong_as_double((long long)((w.v[0] & 0xffffffffULL) | (w.v[1] << 32)));
-}
-__device__ __forceinline__ float ll_val(const LLWord<float> &w) { return __uint_as_float((unsigned)w.v); }
 
 template <typename T>
 struct SweepArgs {
@@ -181,7 +139,7 @@ struct alignas(16) Stage<T, C, -1> {
 };
 
 // Warp roles of a sweep CTA.
-enum { kRoleCompute = 0, kRoleCopy = 1, kRoleEdge = 2, kRolePre = 3 };
+enum { kRoleCompute = 0, kRolePre = 1, kRoleCopy = 2, kRoleEdge = 3 };
 
 // Poll result words of the current epoch, bounded; warp-uniform result.
 // `want` marks the lanes' words still missing (bit t = word t).
@@ -201,7 +159,8 @@ __device__ __forceinline__ bool ll_poll(const LLWord<T> *q, long long stride, un
 }
 
 // DIR = +1 forward, -1 backward.  A CTA is one block: 32 lines of one layer.
-template <typename T, int S, int C, int NS, int DIR>
+// PF: chunks of neighbour words whose loads are in flight ahead of use.
+template <typename T, int S, int C, int NS, int DIR, int PF>
 __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   constexpr int W = 32;
   using St = Stage<T, C, DIR>;
@@ -229,12 +188,16 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     }
     s_m = lo;
     s_abort = 0;
-    // Rotate the roles by the CTA's warp-slot group on the SM, so that the
-    // compute warps of co-resident CTAs sit on different SM sub-partitions
-    // (each has its own FP64 pipe).
+    // Place the roles on the SM sub-partitions (each has its own FP64
+    // pipe; warp w of the CTA is taken to sit on sub-partition
+    // (slot of warp 0 + w) mod 4): the compute warp on sub-partition 2p and
+    // the pre-compute warp on 2p+1, p the parity of the CTA's 4-slot group,
+    // so that two co-resident CTAs keep their FP64 warps apart.  The roles
+    // are a rotation of the warps in any case.
     unsigned hw;
     asm volatile("mov.u32 %0, %%warpid;" : "=r"(hw));
-    s_rot = (int)((hw >> 2) & 3u);
+    const int w0 = (int)(hw & 3u), par = (int)((hw >> 2) & 1u);
+    s_rot = (2 * par - w0) & 3;  // the warp that computes
     for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
@@ -247,7 +210,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   // a member of a batch that has reached its closure is not swept; its CTAs
   // only depend on one another, so none of them waits for it
   if (p.mctl && p.mctl[s_m].done) return;
-  const int role = (warp + s_rot) & 3;
+  const int role = (warp - s_rot) & 3;
   const int id = s_id;
   const unsigned ep = s_ep;
   const Dia7Geo geo = p.geo[s_m];
@@ -279,33 +242,61 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     // tile (each element read and written by one thread) and released
     // through the stage's prep mbarrier.
     const LLWord<T> *zsrc = has_lay ? out + tile(k - DIR, b) + lane : nullptr;
-    for (int c = 0; c < nch; ++c) {
-      const int s = c % NS;
-      const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort);
-      if (!__all_sync(0xffffffffu, got)) {
-        if (lane == 0) *v_abort = 1;
-        return;
-      }
-      St &st = stg[s];
-      T zn[C];
-      if (has_lay && !ll_poll<T, C>(zsrc + (long long)c * C * W, W, (1u << C) - 1u, ep, zn, v_abort)) {
-        fail();
-        return;
-      }
+    // loads of chunk c sit in slot c % PF, issued PF chunks ahead
+    LLRaw zr[PF][C];
+    if (has_lay) {
 #pragma unroll
-      for (int t = 0; t < C; ++t) {
-        const int e = t * W + lane;
-        T t0;
-        if constexpr (DIR > 0) t0 = st.r[e];
-        else t0 = st.d[e] * ll_val(st.y[C * W - 1 - e]);
-        if (has_lay) t0 = fma(-st.a[e], zn[t], t0);
-        st.a[e] = t0;
+      for (int j = 0; j < PF; ++j)
+        if (j < nch)
+#pragma unroll
+          for (int t = 0; t < C; ++t) ll_issue(zsrc + (long long)(j * C + t) * W, zr[j][t]);
+    }
+    for (int c0 = 0; c0 < nch; c0 += PF) {
+#pragma unroll
+      for (int j = 0; j < PF; ++j) {
+        const int c = c0 + j;
+        if (c >= nch) break;
+        const int s = c % NS;
+        const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort);
+        if (!__all_sync(0xffffffffu, got)) {
+          if (lane == 0) *v_abort = 1;
+          return;
+        }
+        St &st = stg[s];
+        T zn[C];
+        if (has_lay) {
+          // words that were not yet written when their load was issued are
+          // polled again
+          unsigned want = 0;
+#pragma unroll
+          for (int t = 0; t < C; ++t) {
+            if (ll_ready<T>(zr[j][t], ep)) ll_take(zr[j][t], zn[t]);
+            else want |= 1u << t;
+          }
+          if (__any_sync(0xffffffffu, want != 0) &&
+              !ll_poll<T, C>(zsrc + (long long)c * C * W, W, want, ep, zn, v_abort)) {
+            fail();
+            return;
+          }
+          if (c + PF < nch)
+#pragma unroll
+            for (int t = 0; t < C; ++t) ll_issue(zsrc + (long long)((c + PF) * C + t) * W, zr[j][t]);
+        }
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+          const int e = t * W + lane;
+          T t0;
+          if constexpr (DIR > 0) t0 = st.r[e];
+          else t0 = st.d[e] * ll_val(st.y[C * W - 1 - e]);
+          if (has_lay) t0 = fma(-st.a[e], zn[t], t0);
+          st.a[e] = t0;
+        }
+        // the buffer is refilled by the async proxy after the compute warp
+        // has released it: order these generic writes before that
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&prep[s]);
       }
-      // the buffer is refilled by the async proxy after the compute warp
-      // has released it: order these generic writes before that
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&prep[s]);
     }
     return;
   }
@@ -316,28 +307,46 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     // of the chunk (the neighbour's lane 31 reaches column g at its step
     // g + S*31) and leaves it in the stage's `yn`.
     const LLWord<T> *ysrc = has_blk ? out + tile(k, b - DIR) + (W - 1) : nullptr;
-    for (int c = 0; c < nch; ++c) {
-      const int s = c % NS;
-      if (c >= NS) {
-        const bool got = mbar_wait(&empty[s], ((c / NS) - 1) & 1, v_abort);
-        if (!__all_sync(0xffffffffu, got)) {
-          if (lane == 0) *v_abort = 1;
-          return;
+    // lane t < C: the word of step t of a chunk; loads PF chunks ahead
+    auto yrow_of = [&](int c) { return c * C + S * (W - 1) + lane; };
+    auto needs = [&](int c) { return has_blk && lane < C && yrow_of(c) < G; };
+    LLRaw yr[PF];
+#pragma unroll
+    for (int j = 0; j < PF; ++j)
+      if (j < nch && needs(j)) ll_issue(ysrc + (long long)yrow_of(j) * W, yr[j]);
+    for (int c0 = 0; c0 < nch; c0 += PF) {
+#pragma unroll
+      for (int j = 0; j < PF; ++j) {
+        const int c = c0 + j;
+        if (c >= nch) break;
+        const int s = c % NS;
+        if (c >= NS) {
+          const bool got = mbar_wait(&empty[s], ((c / NS) - 1) & 1, v_abort);
+          if (!__all_sync(0xffffffffu, got)) {
+            if (lane == 0) *v_abort = 1;
+            return;
+          }
         }
-      }
-      if (has_blk) {
-        const int yrow = c * C + S * (W - 1) + lane;
-        T v[1] = {T(0)};
-        const bool need = lane < C && yrow < G;
-        if (!ll_poll<T, 1>(ysrc + (long long)(need ? yrow : 0) * W, 0, need ? 1u : 0u, ep, v,
-                           v_abort)) {
-          fail();
-          return;
+        if (has_blk) {
+          const bool need = needs(c);
+          T v[1] = {T(0)};
+          unsigned want = 0;
+          if (need) {
+            if (ll_ready<T>(yr[j], ep)) ll_take(yr[j], v[0]);
+            else want = 1u;
+          }
+          if (__any_sync(0xffffffffu, want != 0) &&
+              !ll_poll<T, 1>(ysrc + (long long)(need ? yrow_of(c) : 0) * W, 0, want, ep, v,
+                             v_abort)) {
+            fail();
+            return;
+          }
+          if (lane < C) stg[s].yn[lane] = need ? v[0] : T(0);
+          if (c + PF < nch && needs(c + PF)) ll_issue(ysrc + (long long)yrow_of(c + PF) * W, yr[j]);
         }
-        if (lane < C) stg[s].yn[lane] = need ? v[0] : T(0);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&prep[s]);
       }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&prep[s]);
     }
     return;
   }
@@ -523,42 +532,41 @@ __global__ void k_dia7_extract(const Dia7Geo *__restrict__ geos, int nm, long lo
   }
 }
 
-// Wavefront shape per precision: lines per block W, lane skew S, chunk C,
-// buffers NS.  The FP64 shape can be set at build time (GB_DIA64_W/S/NS) to
-// tune it on a new part; W <= 32 (one warp), S >= 1, C a multiple of 2.
-// Measured on GB300 (10M-cell case, one ILU0 application): W16/S2 1.83 ms,
-// W16/S1 1.50 ms, W32/S1 (NS 4, three CTAs per SM) 1.20 ms -- the sweep is
-// bound by the hand-off chain, so fewer, wider blocks win although each
-// step then carries the y-term shuffle on its dependency chain.
-#ifndef GB_DIA64_W
-#define GB_DIA64_W 32
+// Wavefront shape: W = 32 lines per block (one warp), lane skew S = 1.  A
+// sweep's chunk C (steps per ring buffer), ring depth NS and prefetch depth
+// PF are run-time choices among the configurations below: the padded step
+// count G is a multiple of 16, so every C fits the same layout, and
+// gbims_autotune times them on the handle's own system.
+// The FP32 lane skew can be set at build time (GB_DIA32_S, 1 or 2): with
+// S = 2 the shuffle leaves a step's dependency chain at the price of twice
+// the lag between neighbour blocks.
+#ifndef GB_DIA32_S
+#define GB_DIA32_S 1
 #endif
-#ifndef GB_DIA64_S
-#define GB_DIA64_S 1
-#endif
-#ifndef GB_DIA64_NS
-#define GB_DIA64_NS 4
-#endif
+constexpr int kW = 32, kGPad = 16;
 template <typename T>
-struct Shape;
+constexpr int kSOf = 1;
 template <>
-struct Shape<double> {
-  static constexpr int W = GB_DIA64_W, S = GB_DIA64_S, C = 8, NS = GB_DIA64_NS;
+constexpr int kSOf<float> = GB_DIA32_S;
+static_assert(GB_DIA32_S == 1 || GB_DIA32_S == 2, "lane skew 1 or 2");
+// OCC 2: the CTA asks for enough shared memory that at most two share an
+// SM, so that each compute warp has a sub-partition's FP64 pipe to itself.
+struct SweepCfg {
+  int C, NS, PF, OCC;
 };
-template <>
-struct Shape<float> { static constexpr int W = 32, S = 1, C = 8, NS = 5; };
+constexpr SweepCfg kSweepCfgs[] = {{8, 4, 1, 0},  {8, 4, 2, 0},  {4, 8, 1, 0},  {4, 8, 2, 0},
+                                   {16, 2, 1, 0}, {16, 2, 2, 0}, {8, 4, 1, 2},  {8, 4, 2, 2},
+                                   {4, 8, 1, 2},  {4, 8, 2, 2},  {16, 2, 1, 2}, {16, 2, 2, 2}};
+constexpr size_t kOcc2Smem = 80 * 1024;
+constexpr int kNumSweepCfgs = sizeof(kSweepCfgs) / sizeof(kSweepCfgs[0]);
 
-template <typename T, int DIR>
+template <typename T, int C, int NS, int DIR>
 constexpr size_t stage_bytes() {
-  using P = Shape<T>;
-  return P::NS * sizeof(Stage<T, P::C, DIR>) + 3 * P::NS * sizeof(unsigned long long);
+  return NS * sizeof(Stage<T, C, DIR>) + 3 * NS * sizeof(unsigned long long);
 }
-static_assert(Shape<double>::W == 32 && Shape<float>::W == 32, "a sweep block is one warp of lines");
-static_assert((Shape<double>::S == 1 || Shape<double>::S == 2) &&
-                  (Shape<float>::S == 1 || Shape<float>::S == 2),
-              "lane skew 1 or 2");
-static_assert(stage_bytes<double, -1>() <= 200 * 1024, "FP64 stage ring too large");
-static_assert(stage_bytes<float, -1>() <= 200 * 1024, "FP32 stage ring too large");
+static_assert(stage_bytes<double, 16, 2, -1>() <= 72 * 1024 && stage_bytes<double, 4, 8, -1>() <= 72 * 1024 &&
+                  stage_bytes<double, 8, 4, -1>() <= 72 * 1024,
+              "three sweep CTAs per SM");
 
 }  // namespace
 
@@ -588,12 +596,18 @@ bool dia7_matches(int nlay, int nrow, int ncol, int n, const std::vector<int> &i
 
 // Geometry of the skewed layout of one precision.
 void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, long long *slots) {
-  int W = fp32 ? Shape<float>::W : Shape<double>::W;
-  int S = fp32 ? Shape<float>::S : Shape<double>::S;
-  int C = fp32 ? Shape<float>::C : Shape<double>::C;
-  *nb = (nrow + W - 1) / W;
-  *G = ((ncol + S * (W - 1) + C - 1) / C) * C;
-  *slots = (long long)nlay * (*nb) * (*G) * W;
+  const int S = fp32 ? kSOf<float> : kSOf<double>;
+  *nb = (nrow + kW - 1) / kW;
+  *G = ((ncol + S * (kW - 1) + kGPad - 1) / kGPad) * kGPad;
+  *slots = (long long)nlay * (*nb) * (*G) * kW;
+}
+
+int dia7_num_cfgs() { return kNumSweepCfgs; }
+void dia7_cfg(int i, int *C, int *NS, int *PF, int *OCC) {
+  *C = kSweepCfgs[i].C;
+  *NS = kSweepCfgs[i].NS;
+  *PF = kSweepCfgs[i].PF;
+  *OCC = kSweepCfgs[i].OCC;
 }
 
 void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long long> &row0,
@@ -615,7 +629,7 @@ void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long
     g.row0 = row0[m];
     tickets += g.nlay * g.nb;
     ptiles += g.nlay * ((g.ncol + 31) / 32) * ((g.nrow + 7) / 8);
-    slots += ms;  // a multiple of C*W elements: every member starts 16-byte aligned
+    slots += ms;  // a multiple of 16*W elements: every member starts 16-byte aligned
   }
   D.slots = slots;
   D.ntickets = tickets;
@@ -632,12 +646,11 @@ void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long
 template <typename T>
 static void extract_t(const Dia7 &D, const int *d_iapc, const int *d_japc, const double *d_apc,
                       T *const *arr, cudaStream_t st) {
-  using P = Shape<T>;
   const long long nslot = D.slots;
   int grid = (int)std::min<long long>((nslot + 255) / 256, 8LL * kNumSM);
-  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.d_geo, D.nm, nslot, P::W, P::S, 1, d_iapc, d_japc,
+  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.d_geo, D.nm, nslot, kW, kSOf<T>, 1, d_iapc, d_japc,
                                           d_apc, arr[0], arr[1], arr[2], nullptr);
-  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.d_geo, D.nm, nslot, P::W, P::S, -1, d_iapc, d_japc,
+  k_dia7_extract<T><<<grid, 256, 0, st>>>(D.d_geo, D.nm, nslot, kW, kSOf<T>, -1, d_iapc, d_japc,
                                           d_apc, arr[3], arr[4], arr[5], arr[6]);
 }
 
@@ -655,17 +668,35 @@ void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_j
   }
 }
 
+// The two sweeps of one configuration (opting in to more than 48 KB of
+// dynamic shared memory once per kernel).
+template <typename T, int C, int NS, int PF>
+static void sweep_pair(SweepArgs<T> a, const T *const *arr, const Dia7 &D, int occ,
+                       cudaStream_t st) {
+  constexpr size_t bf = stage_bytes<T, C, NS, 1>(), bb = stage_bytes<T, C, NS, -1>();
+  static bool opted = false;
+  if (!opted) {  // allow up to the two-per-SM request
+    cudaFuncSetAttribute(k_dia7_sweep<T, kSOf<T>, C, NS, 1, PF>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(bf, kOcc2Smem));
+    cudaFuncSetAttribute(k_dia7_sweep<T, kSOf<T>, C, NS, -1, PF>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(bb, kOcc2Smem));
+    opted = true;
+  }
+  const size_t smf = (occ == 2) ? std::max(bf, kOcc2Smem) : bf;
+  const size_t smb = (occ == 2) ? std::max(bb, kOcc2Smem) : bb;
+  k_dia7_sweep<T, kSOf<T>, C, NS, 1, PF><<<D.ntickets, 128, smf, st>>>(a);
+  a.A = arr[3]; a.B = arr[4]; a.X = arr[5]; a.D = arr[6];
+  a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags + 32);
+  k_dia7_sweep<T, kSOf<T>, C, NS, -1, PF><<<D.ntickets, 128, smb, st>>>(a);
+}
+
 // One ILU0 application on the skewed layout: skew r (natural order, type TV)
-// into the sweep type T, forward and backward wavefront sweeps, unskew z
-// back to TV.
-// No memory is reset between applications: each sweep launch writes its
-// words with a new epoch.
+// into the sweep type T, forward and backward wavefront sweeps in the
+// handle's configuration, unskew z back to TV.  No memory is reset between
+// applications: each sweep launch writes its words with a new epoch.
 template <typename T, typename TV = T>
 static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, const TV *r, TV *z, const Ctl *ctl,
                     cudaStream_t st) {
-  using P = Shape<T>;
-  const int nct = D.ntickets;
-  constexpr size_t smf = stage_bytes<T, 1>(), smb = stage_bytes<T, -1>();
   const dim3 pb(32, 8);
   SweepArgs<T> a;
   a.geo = D.d_geo;
@@ -678,25 +709,18 @@ static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, const TV *r, TV 
   a.ctl = const_cast<Ctl *>(ctl);
   a.A = arr[0]; a.B = arr[1]; a.X = arr[2]; a.D = nullptr;
   a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags);
-  {  // opt in to more than 48 KB of dynamic shared memory, once
-    static bool opted = false;
-    if (!opted) {
-      if (smf > 48 * 1024)
-        cudaFuncSetAttribute(k_dia7_sweep<T, P::S, P::C, P::NS, 1>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
-      if (smb > 48 * 1024)
-        cudaFuncSetAttribute(k_dia7_sweep<T, P::S, P::C, P::NS, -1>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb);
-      opted = true;
-    }
+  k_dia7_permute<TV, T, kW, kSOf<T>, 1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, r, rsk, ctl, D.mctl);
+  const int occ = kSweepCfgs[D.cfg].OCC;
+  switch (D.cfg % 6) {
+    case 1: sweep_pair<T, 8, 4, 2>(a, arr, D, occ, st); break;
+    case 2: sweep_pair<T, 4, 8, 1>(a, arr, D, occ, st); break;
+    case 3: sweep_pair<T, 4, 8, 2>(a, arr, D, occ, st); break;
+    case 4: sweep_pair<T, 16, 2, 1>(a, arr, D, occ, st); break;
+    case 5: sweep_pair<T, 16, 2, 2>(a, arr, D, occ, st); break;
+    default: sweep_pair<T, 8, 4, 1>(a, arr, D, occ, st); break;
   }
-  k_dia7_permute<TV, T, P::W, P::S, 1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, r, rsk, ctl, D.mctl);
-  k_dia7_sweep<T, P::S, P::C, P::NS, 1><<<nct, 128, smf, st>>>(a);
-  a.A = arr[3]; a.B = arr[4]; a.X = arr[5]; a.D = arr[6];
-  a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags + 32);
-  k_dia7_sweep<T, P::S, P::C, P::NS, -1><<<nct, 128, smb, st>>>(a);
-  k_dia7_permute<T, TV, P::W, P::S, -1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, D.ll_z, z, ctl,
-                                                                 D.mctl);
+  k_dia7_permute<T, TV, kW, kSOf<T>, -1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, D.ll_z, z, ctl,
+                                                               D.mctl);
 }
 
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,

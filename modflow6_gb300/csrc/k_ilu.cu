@@ -12,6 +12,8 @@
 // backward sweep D = (D - U*D) * APC(n).  Rows of a level are independent; one
 // launch per level.  Entries are summed in JAPC order with FMA.
 #include "gbims_internal.cuh"
+#include "k_llword.cuh"
+#include <algorithm>
 #include <climits>
 
 namespace gb {
@@ -182,6 +184,96 @@ __global__ void k_ilu_bwd_level(const int *__restrict__ rows, int nrows,
   d[n] = tv * apc[n];
 }
 
+// Sync-free sweeps: one launch per sweep instead of one per level.  Every
+// thread walks the level-ordered row list with a grid stride; a row reads the
+// rows it depends on as result words tagged with the launch's epoch and
+// waits (bounded) for those not written yet.  Rows depend only on rows of
+// lower levels, which come earlier in the list, and the grid is sized so
+// that all of its CTAs are resident: the lowest unfinished row of the list
+// can always proceed, so every wait ends.  Each row sums its entries in
+// JAPC order with FMA, as the per-level kernels do (bit-identical results).
+template <typename T, int DIR>
+__global__ void __launch_bounds__(256) k_ilu_sweep_sf(int n, const int *__restrict__ rows,
+                                                      const int *__restrict__ iapc,
+                                                      const int *__restrict__ japc,
+                                                      const T *__restrict__ apc,
+                                                      const T *__restrict__ r,
+                                                      const LLWord<T> *__restrict__ yin,
+                                                      LLWord<T> *out, T *d,
+                                                      unsigned long long *ticket, int *err,
+                                                      Ctl *ctl) {
+  __shared__ unsigned s_ep;
+  if (threadIdx.x == 0) {
+    // every CTA takes a ticket, so launch e owns tickets [e*grid, (e+1)*grid)
+    const unsigned long long tk = atomicAdd(ticket, 1ULL);
+    s_ep = (unsigned)(tk / gridDim.x) + 1u;
+  }
+  __syncthreads();
+  if (ctl && ctl->done) return;
+  const unsigned ep = s_ep;
+  volatile int *vdone = ctl ? &ctl->done : nullptr;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int row = rows[q];
+    T tv;
+    int j0, j1;
+    if (DIR > 0) {
+      tv = r[row];
+      j0 = iapc[row];
+      j1 = japc[row];
+    } else {
+      tv = ll_val(yin[row]);
+      j0 = japc[row];
+      j1 = iapc[row + 1];
+    }
+    for (int j = j0; j < j1; ++j) {
+      const LLWord<T> *w = out + japc[j];
+      T v;
+      if (!ll_get(w, ep, v)) {
+        const unsigned long long t0 = gtimer();
+        while (!ll_get(w, ep, v)) {
+          if ((vdone && *vdone) || gtimer() - t0 > kWaitNs) {
+            atomicExch(err, 1);
+            if (ctl) ctl->done = 1;
+            return;
+          }
+        }
+      }
+      tv = fms<T>(apc[j], v, tv);
+    }
+    if (DIR < 0) {
+      tv = tv * apc[row];
+      d[row] = tv;
+    }
+    ll_put(out + row, tv, ep);
+  }
+}
+
+// Grid of the sync-free sweeps: every CTA resident at once.
+template <typename T, int DIR>
+static int sf_grid(int n) {
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_sweep_sf<T, DIR>, 256, 0);
+    per_sm = std::max(1, per_sm);
+  }
+  return std::max(1, std::min((n + 255) / 256, per_sm * kNumSM));
+}
+
+template <typename T>
+static void apply_sf(int n, const int *d_iapc, const int *d_japc, const T *d_apc, const Levels &F,
+                     const Levels &B, const LevelWords &Wd, const T *r, T *d, Ctl *ctl,
+                     cudaStream_t st) {
+  LLWord<T> *yf = static_cast<LLWord<T> *>(Wd.fwd);
+  LLWord<T> *zb = static_cast<LLWord<T> *>(Wd.bwd);
+  k_ilu_sweep_sf<T, 1><<<sf_grid<T, 1>(n), 256, 0, st>>>(n, F.d_rows, d_iapc, d_japc, d_apc, r,
+                                                          nullptr, yf, nullptr, Wd.ticket,
+                                                          Wd.err, ctl);
+  k_ilu_sweep_sf<T, -1><<<sf_grid<T, -1>(n), 256, 0, st>>>(n, B.d_rows, d_iapc, d_japc, d_apc,
+                                                            nullptr, yf, zb, d, Wd.ticket + 16,
+                                                            Wd.err, ctl);
+}
+
 template <typename T>
 static void apply_levels(const int *d_iapc, const int *d_japc, const T *d_apc,
                          const Levels &F, const Levels &B, const T *r, T *d, const Ctl *ctl,
@@ -199,17 +291,22 @@ static void apply_levels(const int *d_iapc, const int *d_japc, const T *d_apc,
 }
 
 void launch_ilu_apply_levels(int n, const int *d_iapc, const int *d_japc, const double *d_apc,
-                             const Levels &F, const Levels &B, const double *r, double *d,
-                             const Ctl *ctl, cudaStream_t st) {
-  (void)n;
-  apply_levels<double>(d_iapc, d_japc, d_apc, F, B, r, d, ctl, st);
+                             const Levels &F, const Levels &B, const LevelWords &Wd,
+                             const double *r, double *d, const Ctl *ctl, cudaStream_t st) {
+  if (Wd.mode == 1)
+    apply_sf<double>(n, d_iapc, d_japc, d_apc, F, B, Wd, r, d, const_cast<Ctl *>(ctl), st);
+  else
+    apply_levels<double>(d_iapc, d_japc, d_apc, F, B, r, d, ctl, st);
 }
 
 void launch_ilu_apply_levels32(int n, const int *d_iapc, const int *d_japc,
                                const float *d_apc32, const Levels &F, const Levels &B,
-                               const float *r, float *d, const Ctl *ctl, cudaStream_t st) {
-  (void)n;
-  apply_levels<float>(d_iapc, d_japc, d_apc32, F, B, r, d, ctl, st);
+                               const LevelWords &Wd, const float *r, float *d, const Ctl *ctl,
+                               cudaStream_t st) {
+  if (Wd.mode == 1)
+    apply_sf<float>(n, d_iapc, d_japc, d_apc32, F, B, Wd, r, d, const_cast<Ctl *>(ctl), st);
+  else
+    apply_levels<float>(d_iapc, d_japc, d_apc32, F, B, r, d, ctl, st);
 }
 
 }  // namespace gb

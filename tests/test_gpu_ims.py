@@ -269,3 +269,31 @@ def test_repeated_apply_is_reproducible(gblib):
     rb = ims.imslinear_apply(amat.copy(), rhs.copy(), xb)
     assert ra.in_iter == rb.in_iter
     np.testing.assert_array_equal(xa, xb)
+
+
+def test_level_sweep_modes_bitexact_and_autotune(gblib):
+    """The level-scheduled sweeps in both forms (one launch per level; one
+    sync-free launch per sweep over epoch-tagged words) give the oracle's
+    ilu0a bit for bit; the autotuner times both and keeps one."""
+    m, con, amat, rhs, x0 = c2_small_system()
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=1000)
+    ims = gpu_ims(con, **tol)
+    assert gblib.gbims_factor(ims._h, _lib.dptr(amat), None) == 0
+    o = oracle.Ims(oracle.settings(), con["ia"], con["ja"])
+    o.apply(amat.copy(), rhs.copy(), x0.copy())
+    v = np.random.default_rng(11).standard_normal(con["nodes"])
+    zo = oracle.ilu0a(o.apc(), o.iapc(), o.japc(), v, fma=True)
+    for mode in (0, 1, 1, 0):
+        assert gblib.gbims_set_tuning(ims._h, -1, 0, mode) == 0
+        z = np.zeros_like(v)
+        assert gblib.gbims_precondition(ims._h, _lib.dptr(v), _lib.dptr(z)) == 0
+        np.testing.assert_array_equal(z, zo)
+    t = _lib.GbimsTuning()
+    assert gblib.gbims_autotune(ims._h, 2, C.byref(t)) == 0, gblib.gbims_last_error(ims._h)
+    assert t.level_mode in (0, 1) and t.sweep_config == -1
+    assert t.level_ms[0] > 0.0 and t.level_ms[1] > 0.0
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.icnvg == 1
+    xo, _, _, _ = oracle_solve(con, amat, rhs, x0, ilinmeth=1, **tol)
+    assert np.max(np.abs(x - xo)) <= 5e-7

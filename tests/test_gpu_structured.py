@@ -96,3 +96,48 @@ def test_structured_solve_c2_small(gblib, ilinmeth, precision):
     assert_closure_parity(x, xo, x_star, tol["dvclose"], False)
     if precision == _lib.GBIMS_FP64:
         assert abs(r.in_iter - it_o) <= max(2, int(0.05 * it_o)), (r.in_iter, it_o)
+
+
+@pytest.mark.parametrize("precision", [_lib.GBIMS_FP64, _lib.GBIMS_MIXED])
+@pytest.mark.parametrize("shape", [(2, 65, 3), (3, 40, 41), (4, 97, 150)], ids=lambda s: "x".join(map(str, s)) if isinstance(s, tuple) else str(s))
+def test_every_sweep_tiling_gives_the_same_result(gblib, shape, precision):
+    """The wavefront tilings (chunk, ring depth, prefetch depth) the
+    autotuner chooses among compute every cell in the same order: the
+    preconditioner output is bit for bit the same under each."""
+    import ctypes as C
+    m, con, amat, rhs, x0 = dis_system(*shape)
+    ims = ImsLinear(ImsLinearSettings(structure=shape, precision=precision)).imslinear_allocate(
+        m.nodes, con["ia"], con["ja"])
+    assert gblib.gbims_factor(ims._h, _lib.dptr(amat), None) == 0
+    v = np.random.default_rng(9).standard_normal(m.nodes)
+    ref = None
+    t = _lib.GbimsTuning()
+    assert gblib.gbims_autotune(ims._h, 2, C.byref(t)) == 0, gblib.gbims_last_error(ims._h)
+    assert t.ncandidates >= 2 and 0 <= t.sweep_config < t.ncandidates
+    assert all(t.candidate_ms[i] > 0.0 for i in range(t.ncandidates))
+    assert t.reduction_blocks > 0 and t.precond_ms == min(t.candidate_ms[:t.ncandidates])
+    for cfg in range(t.ncandidates):
+        assert gblib.gbims_set_tuning(ims._h, cfg, 0, -1) == 0
+        z = np.zeros_like(v)
+        assert gblib.gbims_precondition(ims._h, _lib.dptr(v), _lib.dptr(z)) == 0
+        if ref is None:
+            ref = z
+        else:
+            np.testing.assert_array_equal(z, ref)
+
+
+def test_autotuned_solve_reaches_the_same_closure(gblib):
+    import ctypes as C
+    shape = (3, 40, 41)
+    m, con, amat, rhs, x0 = dis_system(*shape)
+    tol = dict(dvclose=1e-9, rclose=1e-7, iter1=2000)
+    ims = ImsLinear(ImsLinearSettings(structure=shape, **tol)).imslinear_allocate(m.nodes, con["ia"], con["ja"])
+    x1 = x0.copy()
+    r1 = ims.imslinear_apply(amat.copy(), rhs.copy(), x1)
+    t = _lib.GbimsTuning()
+    assert gblib.gbims_autotune(ims._h, 3, C.byref(t)) == 0, gblib.gbims_last_error(ims._h)
+    x2 = x0.copy()
+    r2 = ims.imslinear_apply(amat.copy(), rhs.copy(), x2)
+    assert r1.icnvg == 1 and r2.icnvg == 1
+    assert abs(r1.in_iter - r2.in_iter) <= 2
+    assert np.max(np.abs(x1 - x2)) <= 0.1 * tol["dvclose"]
