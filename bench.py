@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-warmstart", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the library's default sweep tiling and reduction grid")
     ap.add_argument("--kernels", action="store_true",
                     help="per-kernel device times on direct launches (no solve)")
     return ap.parse_args()
@@ -278,7 +280,7 @@ def gb_arm(a):
             sol.restart()
             st = sol.timestep(1, 1, 1.0)
             assert st["converged"] == 1, st
-            if i == 0:
+            if i == 0 and not a.no_tune:
                 # the autotuner picks the sweep tiling and reduction grid on
                 # the factored system; the later warm-up steps re-capture
                 # the inner-loop graph with them
@@ -467,7 +469,7 @@ def ensemble_form(a, lib, barrier, maxr) -> dict:
     for i in range(a.warmup):
         d_x.copy_(d_x0)
         res = ens.apply_device(d_amat.data_ptr(), d_rhs.data_ptr(), d_x.data_ptr())
-        if i == 0:
+        if i == 0 and not a.no_tune:
             tuning = autotune(lib, ens._h, reps=3)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -557,7 +559,7 @@ def kernels_arm(a):
         ims.imslinear_allocate(m.nodes, con["ia"], con["ja"])
         rc = lib.gbims_factor(ims._h, _lib.dptr(amat), None)
         assert rc >= 0, lib.gbims_last_error(ims._h)
-        tuning = autotune(lib, ims._h)
+        tuning = None if a.no_tune else autotune(lib, ims._h)
         kt = _lib.GbimsKernelTimes()
         rc = lib.gbims_time_kernels(ims._h, max(1, a.steps), C.byref(kt))
         assert rc == 0, lib.gbims_last_error(ims._h)

@@ -248,16 +248,20 @@ __global__ void __launch_bounds__(256) k_ilu_sweep_sf(int n, const int *__restri
   }
 }
 
-// Grid of the sync-free sweeps: every CTA resident at once.
+// Grid of the sync-free sweeps: about one thread per row of the widest
+// level, so that a thread's next row is about one level ahead of the front
+// (more threads only add threads spinning far ahead of it), and never more
+// CTAs than are resident at once.
 template <typename T, int DIR>
-static int sf_grid(int n) {
+static int sf_grid(int n, int maxwidth) {
   static int per_sm = -1;
   if (per_sm < 0) {
     per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_sweep_sf<T, DIR>, 256, 0);
     per_sm = std::max(1, per_sm);
   }
-  return std::max(1, std::min((n + 255) / 256, per_sm * kNumSM));
+  const int want = (std::max(1, std::min(n, maxwidth)) + 255) / 256;
+  return std::max(1, std::min(want, per_sm * kNumSM));
 }
 
 template <typename T>
@@ -266,10 +270,10 @@ static void apply_sf(int n, const int *d_iapc, const int *d_japc, const T *d_apc
                      cudaStream_t st) {
   LLWord<T> *yf = static_cast<LLWord<T> *>(Wd.fwd);
   LLWord<T> *zb = static_cast<LLWord<T> *>(Wd.bwd);
-  k_ilu_sweep_sf<T, 1><<<sf_grid<T, 1>(n), 256, 0, st>>>(n, F.d_rows, d_iapc, d_japc, d_apc, r,
+  k_ilu_sweep_sf<T, 1><<<sf_grid<T, 1>(n, F.maxwidth), 256, 0, st>>>(n, F.d_rows, d_iapc, d_japc, d_apc, r,
                                                           nullptr, yf, nullptr, Wd.ticket,
                                                           Wd.err, ctl);
-  k_ilu_sweep_sf<T, -1><<<sf_grid<T, -1>(n), 256, 0, st>>>(n, B.d_rows, d_iapc, d_japc, d_apc,
+  k_ilu_sweep_sf<T, -1><<<sf_grid<T, -1>(n, B.maxwidth), 256, 0, st>>>(n, B.d_rows, d_iapc, d_japc, d_apc,
                                                             nullptr, yf, zb, d, Wd.ticket + 16,
                                                             Wd.err, ctl);
 }

@@ -99,6 +99,30 @@ __device__ __forceinline__ unsigned nonfinite(float v) {
   return (__float_as_uint(v) & 0x7f800000u) == 0x7f800000u;
 }
 
+// Sums of FP32 products with FP64-like accuracy and no FP64 instruction per
+// element (on GB300 those run on a narrow pipe): each product is split
+// exactly into p + e (p = x*y rounded, e = fma(x, y, -p)), and the p are
+// added with Neumaier's compensated summation, their rounding errors and
+// the e collected in c.  The pair enters the FP64 reductions as
+// (double)s + (double)c.  Explicit _rn operations keep the compiler from
+// contracting the splitting steps.
+struct CSum {
+  float s, c;
+};
+__device__ __forceinline__ void csum_add(CSum &a, float p) {
+  const float t = __fadd_rn(a.s, p);
+  const float bp = __fsub_rn(t, a.s);
+  a.c = __fadd_rn(a.c, __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, bp)), __fsub_rn(p, bp)));
+  a.s = t;
+}
+__device__ __forceinline__ void csum_prod(CSum &a, float x, float y) {
+  const float p = __fmul_rn(x, y);
+  const float e = __fmaf_rn(x, y, -p);
+  csum_add(a, p);
+  a.c = __fadd_rn(a.c, e);
+}
+__device__ __forceinline__ double csum_value(const CSum &a) { return (double)a.s + (double)a.c; }
+
 // ---------------------------------------------------------------------------
 // dot products: partial[b] (and partial[G+b])
 // ---------------------------------------------------------------------------
@@ -122,6 +146,45 @@ __global__ void __launch_bounds__(kRedBlock) k_dot(int n, const TA *__restrict__
   if (i < n) v[0] = fma(to_d(a[i]), to_d(b[i]), v[0]);
   block_sum<1>(v);
   if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+// The mixed form's FP32 dot products, summed as above.
+__global__ void __launch_bounds__(kRedBlock) k_dot32c(int n, const float *__restrict__ a,
+                                                       const float *__restrict__ b,
+                                                       double *__restrict__ part,
+                                                       const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  CSum acc{0.f, 0.f};
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    const float a0 = a[i], b0 = b[i], a1 = a[i + stride], b1 = b[i + stride];
+    csum_prod(acc, a0, b0);
+    csum_prod(acc, a1, b1);
+  }
+  if (i < n) csum_prod(acc, a[i], b[i]);
+  double v[1] = {csum_value(acc)};
+  block_sum<1>(v);
+  if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+__global__ void __launch_bounds__(kRedBlock) k_dot_tq_tt32c(int n, const float *__restrict__ t,
+                                                             const float *__restrict__ q,
+                                                             double *__restrict__ part,
+                                                             const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  CSum tq{0.f, 0.f}, tt{0.f, 0.f};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float ti = t[i];
+    csum_prod(tq, ti, q[i]);
+    csum_prod(tt, ti, ti);
+  }
+  double v[2] = {csum_value(tq), csum_value(tt)};
+  block_sum<2>(v);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = v[0];
+    part[gridDim.x + blockIdx.x] = v[1];
+  }
 }
 
 // t.q and t.t in one pass (BiCGSTAB omega)
@@ -316,7 +379,10 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__rest
 }
 
 
-// Mixed inner update: x (FP64) += alpha*p (FP32 promoted); d32 -= alpha*q32.
+// Mixed inner update: the step alpha*p in FP32, added to the FP64 heads;
+// d32 -= alpha*q32; the maxima on FP32 magnitudes (integer compares of the
+// bit patterns) and the L2 sum compensated in FP32, so that the only FP64
+// instructions per row are the conversion of the step and the head update.
 __global__ void __launch_bounds__(kRedBlock) k_cg_update_mixed(int n, double *__restrict__ x,
                                                                 float *__restrict__ d,
                                                                 const float *__restrict__ p,
@@ -324,21 +390,22 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update_mixed(int n, double *__
                                                                 double *__restrict__ part,
                                                                 const Ctl *__restrict__ ctl) {
   if (ctl->done) return;
-  const double alpha = ctl->alpha;
-  const float alphaf = (float)alpha;
-  double v[2] = {0.0, 0.0};
+  const float alphaf = (float)ctl->alpha;
+  CSum l2{0.f, 0.f};
   unsigned nf = 0;
-  MaxLoc m[2];
-  m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
+  unsigned bdx = 0, brr = 0;  // largest magnitudes so far (bit patterns)
+  float vdx = 0.f, vrr = 0.f;
+  int idx_dx = -1, idx_rr = -1;
   auto row = [&](int i, float pi, double xi, float qi, float dI) {
-    double tv = alpha * (double)pi;
-    x[i] = xi + tv;
-    if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i; }
-    float di = fmaf(-alphaf, qi, dI);
+    const float tv = __fmul_rn(alphaf, pi);
+    x[i] = xi + (double)tv;
+    const unsigned at = __float_as_uint(tv) & 0x7fffffffu;
+    if (at > bdx) { bdx = at; vdx = tv; idx_dx = i; }
+    const float di = __fmaf_rn(-alphaf, qi, dI);
     d[i] = di;
-    double dd = (double)di;
-    if (absgt(dd, m[1].val)) { m[1].val = dd; m[1].idx = i; }
-    v[0] = fma(dd, dd, v[0]);
+    const unsigned ad = __float_as_uint(di) & 0x7fffffffu;
+    if (ad > brr) { brr = ad; vrr = di; idx_rr = i; }
+    csum_prod(l2, di, di);
     nf |= nonfinite(di) | nonfinite(tv);
   };
   const int stride = gridDim.x * blockDim.x;
@@ -353,7 +420,10 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update_mixed(int n, double *__
     row(j, p1, x1, q1, d1);
   }
   if (i < n) row(i, p[i], x[i], q[i], d[i]);
-  v[1] = (double)nf;
+  double v[2] = {csum_value(l2), (double)nf};
+  MaxLoc m[2];
+  m[0].val = (double)vdx; m[0].idx = idx_dx;
+  m[1].val = (double)vrr; m[1].idx = idx_rr;
   block_sum<2>(v);
   block_maxloc<2>(m);
   if (threadIdx.x == 0) {
@@ -960,10 +1030,10 @@ void kr_dot_tq_tt64(int n, const double *t, const double *q, double *part, int G
   k_dot_tq_tt<double><<<G, kRedBlock, 0, st>>>(n, t, q, part, ctl);
 }
 void kr_dot32(int n, const float *a, const float *b, double *part, int G, const Ctl *ctl, cudaStream_t st) {
-  k_dot<float, float><<<G, kRedBlock, 0, st>>>(n, a, b, part, ctl);
+  k_dot32c<<<G, kRedBlock, 0, st>>>(n, a, b, part, ctl);
 }
 void kr_dot_tq_tt32(int n, const float *t, const float *q, double *part, int G, const Ctl *ctl, cudaStream_t st) {
-  k_dot_tq_tt<float><<<G, kRedBlock, 0, st>>>(n, t, q, part, ctl);
+  k_dot_tq_tt32c<<<G, kRedBlock, 0, st>>>(n, t, q, part, ctl);
 }
 void kr_sumsq64(int n, const double *a, double *part, int G, cudaStream_t st) {
   k_sumsq<double><<<G, kRedBlock, 0, st>>>(n, a, part);
