@@ -318,8 +318,8 @@ def gb_arm(a):
     spmv_gbs = kt.spmv_bytes / (kt.spmv_ms * 1e-3) / 1e9
     pre_gbs = kt.precond_bytes / (kt.precond_ms * 1e-3) / 1e9
     traffic = ncu_traffic()
-    pre_name = ("k_dia7_sweep<double> forward + backward (structured wavefront ILU0, "
-                "with the skew/unskew permutes)")
+    pre_name = ("k_dia7_sweep<double> forward + backward (structured wavefront ILU0; "
+                "the forward sweep reads r and the backward sweep writes z in natural order)")
     mixed = None
     if not a.no_mixed:
         solm, msm, stm, lm, _, hm, tunem = run_form(_lib.GBIMS_MIXED)
@@ -518,7 +518,7 @@ def warmstart_form(a) -> dict:
     return {"workload": f"DIS 3x{int(256 * sc)}x{int(256 * sc)} transient, {steps} steps of 0.5 d, "
                         f"50 wells; PCG + ILU0 to INNER_DVCLOSE 1e-6, INNER_RCLOSE 1e-4",
             "train_models": ntrain, "train_samples": ntrain * steps, "data_s": t_gen,
-            "head_change_scale_m": dh_scale,
+            "head_change_scale_asinh_units": dh_scale,
             "train_s": t_train, "epochs": 4, "loss_per_epoch": hist, "heldout": res,
             "network": "8-layer message passing, hidden 64, BF16 mma.sync GEMMs, FP32 Adam"}
 

@@ -300,11 +300,11 @@ static int setup_structured(gbims_handle *h, const std::vector<int> &shapes,
   const size_t nn = (size_t)h->D.slots;
   if (!h->mixed) {
     double **a[] = {&h->D.d_lz, &h->D.d_ly, &h->D.d_lx, &h->D.d_ux, &h->D.d_uy, &h->D.d_uz,
-                    &h->D.d_dinv, &h->D.d_rsk};
+                    &h->D.d_dinv};
     for (double **p : a) GB_CUDA(h, dalloc(p, nn));
   } else {
     float **a[] = {&h->D.f_lz, &h->D.f_ly, &h->D.f_lx, &h->D.f_ux, &h->D.f_uy, &h->D.f_uz,
-                   &h->D.f_dinv, &h->D.f_rsk};
+                   &h->D.f_dinv};
     for (float **p : a) GB_CUDA(h, dalloc(p, nn));
   }
   // result words: zero, so that no word carries the epoch of a sweep yet
@@ -970,7 +970,7 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->S.d_col, h->S.d_src, h->S.d_val, h->S.d_val32, h->F.d_rows, h->B.d_rows,
                   h->D.d_lz, h->D.d_ly, h->D.d_lx, h->D.d_ux, h->D.d_uy, h->D.d_uz, h->D.d_dinv,
                   h->D.f_lz, h->D.f_ly, h->D.f_lx, h->D.f_ux, h->D.f_uy, h->D.f_uz, h->D.f_dinv,
-                  h->D.d_rsk, h->D.ll_y, h->D.ll_z, h->D.f_rsk,
+                  h->D.ll_y, h->D.ll_z,
                   h->D.d_flags, h->D.d_err, h->d_amat, h->d_rhs, h->d_x, h->v_d, h->v_p, h->v_q,
                   h->v_z, h->v_t, h->v_v, h->v_dhat, h->v_phat, h->v_qhat, h->f_d, h->f_p,
                   h->f_q, h->f_z, h->f_t, h->f_v, h->f_dhat, h->f_phat, h->f_qhat, h->d_part,

@@ -128,7 +128,6 @@ struct Dia7Geo {
   int nlay, nrow, ncol;
   int nb, G;          // blocks of W lines per layer, padded steps per block
   int ticket0;        // first CTA ticket (local ticket = b * nlay + k)
-  int ptile0;         // first 32 x 8 permute tile
   long long slot0;    // first slot of the member's skewed tiles
   long long row0;     // first row of the member in the natural-order vectors
 };
@@ -143,17 +142,15 @@ struct Dia7 {
   std::vector<Dia7Geo> geo;
   Dia7Geo *d_geo = nullptr;
   const Ctl *mctl = nullptr;  // batched ensembles: members that are done are skipped
-  int ntickets = 0, nptiles = 0;
+  int ntickets = 0;
   int cfg = 0;  // sweep configuration (chunk, ring, prefetch): an index of dia7_cfg
   // forward tiles: lower coefficients (unit diagonal) z (layer above),
   // y (row behind), x (column left); backward tiles: dinv*U for z, y, x and
   // dinv; zero where the neighbour or the cell does not exist
   double *d_lz = nullptr, *d_ly = nullptr, *d_lx = nullptr;
   double *d_ux = nullptr, *d_uy = nullptr, *d_uz = nullptr, *d_dinv = nullptr;
-  double *d_rsk = nullptr;  // skewed right-hand side
   float *f_lz = nullptr, *f_ly = nullptr, *f_lx = nullptr;
   float *f_ux = nullptr, *f_uy = nullptr, *f_uz = nullptr, *f_dinv = nullptr;
-  float *f_rsk = nullptr;
   // forward and backward results, skewed, as words that carry the epoch of
   // the sweep that wrote them (16 bytes per element in FP64, 8 in FP32)
   void *ll_y = nullptr, *ll_z = nullptr;
@@ -175,7 +172,7 @@ void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, lon
 int dia7_num_cfgs();
 void dia7_cfg(int i, int *C, int *NS, int *PF, int *OCC);
 // Members (nlay, nrow, ncol) and their first rows -> D.geo, D.slots,
-// D.ntickets, D.nptiles (host side; the caller uploads D.geo to D.d_geo).
+// D.ntickets (host side; the caller uploads D.geo to D.d_geo).
 void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long long> &row0,
                  bool fp32);
 

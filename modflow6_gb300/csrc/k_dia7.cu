@@ -6,40 +6,38 @@
 // k*nrow*ncol).  Row n then has at most three lower neighbours, (k-1,i,j),
 // (k,i-1,j), (k,i,j-1), and three upper ones.
 //
-// Wavefront.  A "line" is the ncol cells of one grid row (k,i).  A CTA owns W
-// consecutive lines of one layer (a "block").  Lane l of its compute warp
+// Wavefront.  A "line" is the ncol cells of one grid row (k,i).  A CTA owns
+// 32 consecutive lines of one layer (a "block").  Lane l of its compute warp
 // walks line l of the block S steps behind lane l-1, so the value it needs
 // from the neighbour line was produced S steps earlier and arrives by a
-// register shuffle (with S >= 2 only the FMA with the lane's own previous
-// column is on a step's dependency chain; with S = 1, the default, the
-// shuffle and the row-neighbour FMA are too, but the blocks lag each other
-// by half as many steps).  The neighbour block (line i0-1) and the
-// neighbour layer are other CTAs.
+// register shuffle.  The neighbour block (line i0-1) and the neighbour layer
+// are other CTAs.
 //
-// Skewed layout.  The factors and the intermediate results are stored per
-// block as G x W tiles, row g = wavefront step, column l = lane (element
-// (g,l) is the cell lane l handles at step g; slots outside the grid hold
-// zero).  A chunk of C steps of one array is then one contiguous C*W tile.
+// Skewed layout.  The factors and the results are stored per block as
+// G x 32 tiles, row g = wavefront step, column l = lane (element (g,l) is
+// the cell lane l handles at step g; slots outside the grid hold zero).  A
+// chunk of C steps of one array is then one contiguous C*32 tile.
 //
-// Four warps per CTA, so that no fence and no off-chain arithmetic ever
-// stalls the dependent chain:
-//  * copy: waits for the producer CTAs' progress words and stages the chunks
-//    into a ring of NS shared-memory buffers with TMA bulk copies
+// Hand-over.  Every result goes to global memory as a word tagged with the
+// epoch of its launch (k_llword.cuh): a consumer that reads the current
+// epoch has the value, with no fence or progress counter in between.  Four
+// warps per CTA, so that no wait stalls the dependent chain:
+//  * copy: streams the block's own factor tiles (and, backward, its forward
+//    result) into a ring of NS shared-memory buffers with bulk copies
 //    (cp.async.bulk), one "full" mbarrier per buffer;
-//  * pre-compute: once a buffer is full, folds the right-hand side and the
-//    layer-neighbour term (r - Lz*zn; backward dinv*y - Uz'*zn) into one
-//    tile and releases it through a "prep" mbarrier;
+//  * pre-compute: loads the layer neighbour's words (PF chunks ahead) and
+//    folds the right-hand side and the layer term (forward r - Lz*zn, with
+//    r read in natural order; backward dinv*y - Uz'*zn) into one tile,
+//    released through a "prep" mbarrier;
+//  * edge: loads the neighbour block's last line (PF chunks ahead) for the
+//    first lane;
 //  * compute: per step one shuffle and the two FMAs of the row and column
-//    neighbours; writes the C x W result tile to a shared-memory ring and
-//    frees the buffer through its "empty" mbarrier;
-//  * store: sends finished result tiles out with bulk stores and publishes
-//    the CTA's progress word (bulk-store completion, proxy fence, gpu-scope
-//    fence, store).  On GB300 a gpu-scope fence costs on the order of a
-//    microsecond, which is why it lives in a warp of its own.
-// The roles rotate with the CTA's hardware warp slot so that compute warps
-// of co-resident CTAs land on different SM sub-partitions (FP64 pipes).
-// Every wait is bounded by the global timer; a wait that runs out sets an
-// error flag and Ctl::done, drains the copies in flight and returns.  CTAs
+//    neighbours; writes each result word, and backward also the result in
+//    natural order, then frees the buffer through its "empty" mbarrier.
+// The compute and pre-compute warps sit on different SM sub-partitions, so
+// that their FP64 instructions do not share a pipe.  Every wait is bounded
+// by the global timer; a wait that runs out sets an error flag and
+// Ctl::done, the copies in flight are drained, and the CTA returns.  CTAs
 // take a ticket in launch order and depend only on smaller tickets, so the
 // chain of waits always ends.
 //
@@ -48,9 +46,7 @@
 // Backward sweep: z = dinv*y - Uz'*z(k+1) - Uy'*z(i+1) - Ux'*z(j+1) with the
 // upper factors pre-scaled by the inverse pivot (U' = dinv*U), equal in exact
 // arithmetic to the reference's (y - sum U z)*dinv with one FMA instead of two
-// dependent operations on the critical path.  The forward input and the
-// backward output are in natural order: k_dia7_skew / k_dia7_unskew permute
-// them with coalesced row accesses.
+// dependent operations on the critical path.
 #include <algorithm>
 #include <cstdlib>
 
@@ -115,7 +111,8 @@ struct SweepArgs {
   int nm;
   const Ctl *mctl;     // per-member control blocks (batched ensembles) or null
   const T *A, *B, *X, *D;  // skewed factors (forward: Lz Ly Lx -, backward: Uz' Uy' Ux' dinv)
-  const T *rsk;            // forward: right-hand side, skewed
+  const T *rnat;           // forward: right-hand side, natural order
+  T *znat;                 // backward: result, natural order
   LLWord<T> *ysk;          // forward result, skewed (written forward, read backward)
   LLWord<T> *zsk;          // backward result, skewed (written and read backward)
   unsigned long long *ticket;  // this direction's ticket counter (zeroed once, never reset)
@@ -128,7 +125,7 @@ template <typename T, int C, int DIR>
 struct Stage;
 template <typename T, int C>
 struct alignas(16) Stage<T, C, 1> {
-  T a[C * 32], b[C * 32], x[C * 32], r[C * 32];
+  T a[C * 32], b[C * 32], x[C * 32];
   T yn[C];  // the neighbour block's last line, one value per step
 };
 template <typename T, int C>
@@ -251,6 +248,24 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
 #pragma unroll
           for (int t = 0; t < C; ++t) ll_issue(zsrc + (long long)(j * C + t) * W, zr[j][t]);
     }
+    // forward: the right-hand side straight from natural order (lane l
+    // walks line b*W + l; step g is column g - S*l), in the same ring
+    const int ri = b * W + lane;
+    const bool rline = (DIR > 0) && ri < nrow;
+    const T *rrow = rline ? p.rnat + geo.row0 + ((long long)k * nrow + ri) * geo.ncol : nullptr;
+    auto rload = [&](int c, T (&dst)[C]) {
+#pragma unroll
+      for (int t = 0; t < C; ++t) {
+        const int jj = c * C + t - S * lane;
+        dst[t] = (rline && (unsigned)jj < (unsigned)geo.ncol) ? __ldg(rrow + jj) : T(0);
+      }
+    };
+    T rr[PF][C];
+    if constexpr (DIR > 0) {
+#pragma unroll
+      for (int j = 0; j < PF; ++j)
+        if (j < nch) rload(j, rr[j]);
+    }
     for (int c0 = 0; c0 < nch; c0 += PF) {
 #pragma unroll
       for (int j = 0; j < PF; ++j) {
@@ -286,10 +301,13 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         for (int t = 0; t < C; ++t) {
           const int e = t * W + lane;
           T t0;
-          if constexpr (DIR > 0) t0 = st.r[e];
+          if constexpr (DIR > 0) t0 = rr[j][t];
           else t0 = st.d[e] * ll_val(st.y[C * W - 1 - e]);
           if (has_lay) t0 = fma(-st.a[e], zn[t], t0);
           st.a[e] = t0;
+        }
+        if constexpr (DIR > 0) {
+          if (c + PF < nch) rload(c + PF, rr[j]);
         }
         // the buffer is refilled by the async proxy after the compute warp
         // has released it: order these generic writes before that
@@ -370,8 +388,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         const int g0 = c * C;
         const long long tb = tile(k, b) + (long long)g0 * W;
         if constexpr (DIR > 0) {
-          mbar_expect_tx(&full[s], 4 * tileb);
-          bulk_g2s(st.r, p.rsk + tb, tileb, &full[s]);
+          mbar_expect_tx(&full[s], 3 * tileb);
         } else {
           // own forward result, steps P descending
           const int phi = geo.ncol - 1 + S * (W - 1) - g0;
@@ -412,6 +429,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   const bool has_y = line_ok && ((DIR > 0) ? (i > 0) : (i + 1 < nrow));
   const int ncol = geo.ncol;
   LLWord<T> *outt = out + tile(k, b) + lane;
+  T *zrow = (DIR < 0 && line_ok) ? p.znat + geo.row0 + ((long long)k * nrow + i) * ncol : nullptr;
   T h1 = T(0), h2 = T(0);
   for (int c = 0; c < nch; ++c) {
     const int s = c % NS;
@@ -435,6 +453,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       if (jj > 0) tv = fma(-st.x[t * W + lane], h1, tv);
       if (!v) tv = T(0);
       ll_put(outt + (long long)(g0 + t) * W, tv, ep);
+      if (DIR < 0 && v) zrow[ncol - 1 - jj] = tv;  // the result in natural order
       h2 = h1;
       h1 = tv;
     }
@@ -442,41 +461,6 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
   }
-}
-
-// Natural order -> skewed tiles (forward input) and back (backward output).
-// A 32 x 8 thread block covers 32 columns of 8 lines: the natural-order side
-// is whole rows, and the skewed side falls in a few rows of one tile.
-// The backward source holds result words (LLWord<TS>).
-template <typename TS, typename TD, int W, int S, int DIR>
-__global__ void k_dia7_permute(const Dia7Geo *__restrict__ geos, int nm, const void *__restrict__ src,
-                               TD *__restrict__ dst, const Ctl *__restrict__ ctl,
-                               const Ctl *__restrict__ mctl) {
-  if (ctl && ctl->done) return;
-  // member of this 32 x 8 tile
-  const int t = blockIdx.x;
-  int lo = 0, hi = nm - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (geos[mid].ptile0 <= t) lo = mid;
-    else hi = mid - 1;
-  }
-  if (mctl && mctl[lo].done) return;
-  const Dia7Geo g = geos[lo];
-  const int tx = (g.ncol + 31) / 32, ty = (g.nrow + 7) / 8;
-  const int lt = t - g.ptile0;
-  const int k = lt / (tx * ty);
-  const int rem = lt - k * tx * ty;
-  const int j = (rem % tx) * 32 + threadIdx.x;
-  const int i = (rem / tx) * 8 + threadIdx.y;
-  if (j >= g.ncol || i >= g.nrow) return;
-  const int b = i / W;
-  const int l = (DIR > 0) ? (i - b * W) : (W - 1 - (i - b * W));
-  const int gg = ((DIR > 0) ? j : (g.ncol - 1 - j)) + S * l;
-  const long long sk = g.slot0 + (((long long)k * g.nb + b) * g.G + gg) * W + l;
-  const long long nat = g.row0 + ((long long)k * g.nrow + i) * g.ncol + j;
-  if (DIR > 0) dst[sk] = (TD)static_cast<const TS *>(src)[nat];  // skew (forward input)
-  else dst[nat] = (TD)ll_val(static_cast<const LLWord<TS> *>(src)[sk]);  // unskew (backward output)
 }
 
 // APC/JAPC -> skewed tiles.  Forward tiles hold Lz, Ly, Lx of the cell that
@@ -615,7 +599,7 @@ void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long
   D.nm = (int)row0.size();
   D.geo.resize(D.nm);
   long long slots = 0;
-  int tickets = 0, ptiles = 0;
+  int tickets = 0;
   for (int m = 0; m < D.nm; ++m) {
     Dia7Geo &g = D.geo[m];
     g.nlay = shapes[3 * m];
@@ -624,16 +608,13 @@ void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long
     long long ms = 0;
     dia7_geometry(g.nlay, g.nrow, g.ncol, fp32, &g.nb, &g.G, &ms);
     g.ticket0 = tickets;
-    g.ptile0 = ptiles;
     g.slot0 = slots;
     g.row0 = row0[m];
     tickets += g.nlay * g.nb;
-    ptiles += g.nlay * ((g.ncol + 31) / 32) * ((g.nrow + 7) / 8);
     slots += ms;  // a multiple of 16*W elements: every member starts 16-byte aligned
   }
   D.slots = slots;
   D.ntickets = tickets;
-  D.nptiles = ptiles;
   if (D.nm == 1) {
     D.nlay = D.geo[0].nlay;
     D.nrow = D.geo[0].nrow;
@@ -660,11 +641,9 @@ void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_j
   if (!mixed) {
     double *arr[7] = {D.d_lz, D.d_ly, D.d_lx, D.d_uz, D.d_uy, D.d_ux, D.d_dinv};
     extract_t<double>(D, d_iapc, d_japc, d_apc, arr, st);
-    cudaMemsetAsync(D.d_rsk, 0, sizeof(double) * D.slots, st);  // padding slots stay zero
   } else {
     float *arr[7] = {D.f_lz, D.f_ly, D.f_lx, D.f_uz, D.f_uy, D.f_ux, D.f_dinv};
     extract_t<float>(D, d_iapc, d_japc, d_apc, arr, st);
-    cudaMemsetAsync(D.f_rsk, 0, sizeof(float) * D.slots, st);
   }
 }
 
@@ -690,26 +669,25 @@ static void sweep_pair(SweepArgs<T> a, const T *const *arr, const Dia7 &D, int o
   k_dia7_sweep<T, kSOf<T>, C, NS, -1, PF><<<D.ntickets, 128, smb, st>>>(a);
 }
 
-// One ILU0 application on the skewed layout: skew r (natural order, type TV)
-// into the sweep type T, forward and backward wavefront sweeps in the
-// handle's configuration, unskew z back to TV.  No memory is reset between
+// One ILU0 application: the forward sweep reads r in natural order, the
+// backward sweep writes z in natural order; between them the results live
+// in the skewed layout as epoch-tagged words.  No memory is reset between
 // applications: each sweep launch writes its words with a new epoch.
-template <typename T, typename TV = T>
-static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, const TV *r, TV *z, const Ctl *ctl,
+template <typename T>
+static void apply_t(const Dia7 &D, const T *const *arr, const T *r, T *z, const Ctl *ctl,
                     cudaStream_t st) {
-  const dim3 pb(32, 8);
   SweepArgs<T> a;
   a.geo = D.d_geo;
   a.nm = D.nm;
   a.mctl = D.mctl;
-  a.rsk = rsk;
+  a.rnat = r;
+  a.znat = z;
   a.ysk = static_cast<LLWord<T> *>(D.ll_y);
   a.zsk = static_cast<LLWord<T> *>(D.ll_z);
   a.err = D.d_err;
   a.ctl = const_cast<Ctl *>(ctl);
   a.A = arr[0]; a.B = arr[1]; a.X = arr[2]; a.D = nullptr;
   a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags);
-  k_dia7_permute<TV, T, kW, kSOf<T>, 1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, r, rsk, ctl, D.mctl);
   const int occ = kSweepCfgs[D.cfg].OCC;
   switch (D.cfg % 6) {
     case 1: sweep_pair<T, 8, 4, 2>(a, arr, D, occ, st); break;
@@ -719,21 +697,19 @@ static void apply_t(const Dia7 &D, const T *const *arr, T *rsk, const TV *r, TV 
     case 5: sweep_pair<T, 16, 2, 2>(a, arr, D, occ, st); break;
     default: sweep_pair<T, 8, 4, 1>(a, arr, D, occ, st); break;
   }
-  k_dia7_permute<T, TV, kW, kSOf<T>, -1><<<D.nptiles, pb, 0, st>>>(D.d_geo, D.nm, D.ll_z, z, ctl,
-                                                               D.mctl);
 }
 
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
                          cudaStream_t st) {
   const double *arr[7] = {D.d_lz, D.d_ly, D.d_lx, D.d_uz, D.d_uy, D.d_ux, D.d_dinv};
-  apply_t<double>(D, arr, D.d_rsk, r, z, ctl, st);
+  apply_t<double>(D, arr, r, z, ctl, st);
 }
 
 
 void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl,
                          cudaStream_t st) {
   const float *arr[7] = {D.f_lz, D.f_ly, D.f_lx, D.f_uz, D.f_uy, D.f_ux, D.f_dinv};
-  apply_t<float>(D, arr, D.f_rsk, r, z, ctl, st);
+  apply_t<float>(D, arr, r, z, ctl, st);
 }
 
 }  // namespace gb

@@ -226,13 +226,16 @@ def train(net: WarmStartNet, data, dh_scale: float, epochs: int = 4,
     """Adam over every sample of every model, `epochs` times, the learning
     rate halved each epoch; mean loss per epoch."""
     net.dh_scale = dh_scale
-    # predictions are bounded by the largest change seen in training (with a
-    # margin): the network does not extrapolate beyond its data
+    # predictions are bounded by the largest head change seen in training,
+    # with a 25 % margin in metres (not in the asinh units, where the same
+    # margin would allow changes many times larger): the network does not
+    # extrapolate beyond its data
     tmax = 0.0
     for g, _, samples in data:
         for s in samples:
             tmax = max(tmax, float(s.target.abs().max().item()))
-    net.unit_max = 1.25 * tmax
+    dh_max = float(np.sinh(tmax * dh_scale)) * DH_SOFT
+    net.unit_max = float(np.arcsinh(1.25 * dh_max / DH_SOFT)) / dh_scale
     hist = []
     for ep in range(epochs):
         tot, cnt = 0.0, 0
