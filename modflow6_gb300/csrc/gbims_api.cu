@@ -322,10 +322,10 @@ static int setup_structured(gbims_handle *h, const std::vector<int> &shapes,
   GB_CUDA(h, cudaMemset(h->D.d_flags, 0, sizeof(int) * h->D.nflags));
   GB_CUDA(h, dalloc(&h->D.d_err, 4));
   GB_CUDA(h, cudaMemset(h->D.d_err, 0, sizeof(int) * 4));
-  // default tiling: the fastest on the 10M-cell case (FP64: chunk 4, ring
-  // 8, prefetch 1, two CTAs per SM; FP32: chunk 8, ring 4, prefetch 1, two
-  // CTAs per SM); gbims_autotune picks per system
-  h->D.cfg = h->mixed ? 6 : 8;
+  // default tiling: the fastest on the 10M-cell case in both precisions
+  // (chunk 8, ring 4, prefetch 2, two CTAs per SM); gbims_autotune picks
+  // per system
+  h->D.cfg = 7;
   h->structured = true;
   return GBIMS_OK;
 }
