@@ -361,6 +361,8 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
           }
           if (lane < C) stg[s].yn[lane] = need ? v[0] : T(0);
           if (c + PF < nch && needs(c + PF)) ll_issue(ysrc + (long long)yrow_of(c + PF) * W, yr[j]);
+        } else if (lane < C) {
+          stg[s].yn[lane] = T(0);  // an edge block of the layer: no neighbour line
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&prep[s]);
@@ -426,7 +428,6 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   // each result goes straight out as a word of this epoch.
   const int i = (DIR > 0) ? (b * W + lane) : (b * W + (W - 1 - lane));
   const bool line_ok = i >= 0 && i < nrow;
-  const bool has_y = line_ok && ((DIR > 0) ? (i > 0) : (i + 1 < nrow));
   const int ncol = geo.ncol;
   LLWord<T> *outt = out + tile(k, b) + lane;
   T *zrow = (DIR < 0 && line_ok) ? p.znat + geo.row0 + ((long long)k * nrow + i) * ncol : nullptr;
@@ -449,8 +450,11 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       const int jj = jc + t;
       const bool v = line_ok && (unsigned)jj < (unsigned)ncol;
       T tv = st.a[t * W + lane];  // pre-computed r - Lz*zn (backward: dinv*y - Uz'*zn)
-      if (has_y) tv = fma(-st.b[t * W + lane], yv, tv);
-      if (jj > 0) tv = fma(-st.x[t * W + lane], h1, tv);
+      // the coefficients of absent neighbours are zero (first line of the
+      // grid, first column, padding slots) and their values finite, so both
+      // products are taken unconditionally: no divergent lanes on the chain
+      tv = fma(-st.b[t * W + lane], yv, tv);
+      tv = fma(-st.x[t * W + lane], h1, tv);
       if (!v) tv = T(0);
       ll_put(outt + (long long)(g0 + t) * W, tv, ep);
       if (DIR < 0 && v) zrow[ncol - 1 - jj] = tv;  // the result in natural order
