@@ -604,17 +604,23 @@ void or_gwf_budget(const or_gwf_model *m, const int *ibound, const double *conds
 /* gwf.f90:466-555, gwf_fc order for the packages restated here:
  * NPF fc, STO fc, BND fc, then NPF fn, STO fn.  amat and rhs must be zero on
  * entry (NumericalSolution sln_reset). */
-void or_gwf_fc(const or_gwf_model *m, const int *ibound, const double *condsat,
-               double *sat, double delt, int transient, const double *hold,
-               const double *hnew, double *amat, double *rhs) {
+static void gwf_fc_flag(const or_gwf_model *m, const int *ibound, const double *condsat,
+                        double *sat, double delt, int transient, const double *hold,
+                        const double *hnew, double *amat, double *rhs, int inwtflag) {
   or_npf_cf(m, ibound, hnew, sat);
   or_npf_fc(m, ibound, condsat, sat, hnew, amat, rhs);
   if (transient) or_sto_fc(m, ibound, delt, hold, hnew, amat, rhs);
   or_bnd_fc(m, ibound, amat, rhs);
-  if (m->inewton) {
+  if (inwtflag && m->inewton) {
     or_npf_fn(m, ibound, condsat, hnew, amat, rhs);
     if (transient) or_sto_fn(m, ibound, delt, hnew, amat, rhs);
   }
+}
+
+void or_gwf_fc(const or_gwf_model *m, const int *ibound, const double *condsat,
+               double *sat, double delt, int transient, const double *hold,
+               const double *hnew, double *amat, double *rhs) {
+  gwf_fc_flag(m, ibound, condsat, sat, delt, transient, hold, hnew, amat, rhs, 1);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -792,6 +798,48 @@ int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
   int converged = 0;
   double l2norm0_ptc = 0.0, ptcdel = 0.0;
   for (int kiter = 1; kiter <= nl->mxiter; ++kiter) {
+    if (nl->numtrack > 0) {
+      /* sln_backtracking (NumericalSolution.f90:2680-2760): the system
+       * without Newton terms (sln_buildsystem with inewton = 0) and its
+       * residual L2 norm; from the second outer iteration on, while the
+       * norm exceeds BTOL x the previous one, the last change is cut by
+       * BREDUC (get_backtracking_flag :2795-2817, apply_backtracking
+       * :2823-2838) */
+      memset(amat, 0, sizeof(double) * nja);
+      memset(rhs, 0, sizeof(double) * neq);
+      gwf_fc_flag(m, ibound, condsat, sat, delt, transient, xold, x, amat, rhs, 0);
+      double l2 = sln_l2norm(neq, m->ia, m->ja, amat, x, rhs, ibound, work);
+      if (kiter == 1) {
+        nl->res_prev = l2;
+      } else {
+        nl->res_new = l2;
+        if (nl->res_new > nl->res_prev * nl->btol) {
+          for (int nb = 1; nb <= nl->numtrack; ++nb) {
+            double dx_abs_max = 0.0;
+            for (int n = 0; n < neq; ++n) {
+              if (ibound[n] < 1) continue;
+              double dx_abs = fabs(x[n] - xtemp[n]);
+              if (dx_abs > dx_abs_max) dx_abs_max = dx_abs;
+            }
+            if (!(nl->breduc * dx_abs_max >= nl->dvclose)) break;
+            for (int n = 0; n < neq; ++n) {
+              if (ibound[n] < 1) continue;
+              double delx = nl->breduc * (x[n] - xtemp[n]);
+              x[n] = xtemp[n] + delx;
+            }
+            st->backtracks += 1;
+            memset(amat, 0, sizeof(double) * nja);
+            memset(rhs, 0, sizeof(double) * neq);
+            gwf_fc_flag(m, ibound, condsat, sat, delt, transient, xold, x, amat, rhs, 0);
+            nl->res_new = sln_l2norm(neq, m->ia, m->ja, amat, x, rhs, ibound, work);
+            if (nb == nl->numtrack) break;
+            if (nl->res_new < nl->res_prev * nl->btol) break;
+            if (nl->res_new < nl->res_lim) break;
+          }
+        }
+        nl->res_prev = nl->res_new;
+      }
+    }
     memset(amat, 0, sizeof(double) * nja);
     memset(rhs, 0, sizeof(double) * neq);
     or_gwf_fc(m, ibound, condsat, sat, delt, transient, xold, x, amat, rhs);

@@ -44,11 +44,17 @@ typedef struct {
   double theta, akappa, gamma, amomentum;
   double bigch, bigchold, relaxold;
   double *wsave, *hchold, *deold, *dxold; /* length neq, caller-owned */
+  /* backtracking (BACKTRACKING_NUMBER, _TOLERANCE, _REDUCTION_FACTOR,
+   * _RESIDUAL_LIMIT); numtrack 0 switches it off */
+  int numtrack;
+  double btol, breduc, res_lim;
+  double res_prev, res_new; /* state */
 } or_nonlinear;
 
 typedef struct {
   int outer, inner_total, converged, pivot_retries;
   double last_dxmax;
+  int backtracks; /* backtracking steps taken in the time step */
 } or_timestep_stats;
 
 void or_dis_sizes(int nlay, int nrow, int ncol, int *nodes, int *nja, int *njas);

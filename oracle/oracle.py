@@ -59,12 +59,14 @@ class Nonlinear(C.Structure):
                 ("iallowptc", C.c_int), ("theta", C.c_double), ("akappa", C.c_double),
                 ("gamma", C.c_double), ("amomentum", C.c_double), ("bigch", C.c_double),
                 ("bigchold", C.c_double), ("relaxold", C.c_double),
-                ("wsave", _dp), ("hchold", _dp), ("deold", _dp), ("dxold", _dp)]
+                ("wsave", _dp), ("hchold", _dp), ("deold", _dp), ("dxold", _dp),
+                ("numtrack", C.c_int), ("btol", C.c_double), ("breduc", C.c_double),
+                ("res_lim", C.c_double), ("res_prev", C.c_double), ("res_new", C.c_double)]
 
 
 class TimestepStats(C.Structure):
     _fields_ = [("outer", C.c_int), ("inner_total", C.c_int), ("converged", C.c_int),
-                ("pivot_retries", C.c_int), ("last_dxmax", C.c_double)]
+                ("pivot_retries", C.c_int), ("last_dxmax", C.c_double), ("backtracks", C.c_int)]
 
 
 def load():
@@ -312,10 +314,12 @@ class Gwf:
                             max_cell=int(imb.argmax()) if imb.max() > 0 else -1)
 
     def timestep(self, kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-3, mxiter=25,
-                 nonmeth=0, theta=1.0, akappa=0.0, gamma=1.0, amomentum=0.0, iallowptc=1):
+                 nonmeth=0, theta=1.0, akappa=0.0, gamma=1.0, amomentum=0.0, iallowptc=1,
+                 numtrack=0, btol=0.0, breduc=0.0, res_lim=0.0):
         w = self._nlv
         nl = Nonlinear(dvclose, mxiter, nonmeth, iallowptc, theta, akappa, gamma, amomentum,
-                       0.0, 0.0, 0.0, dp(w[0]), dp(w[1]), dp(w[2]), dp(w[3]))
+                       0.0, 0.0, 0.0, dp(w[0]), dp(w[1]), dp(w[2]), dp(w[3]),
+                       numtrack, btol, breduc, res_lim, 0.0, 0.0)
         st = TimestepStats()
         rc = self.lib.or_gwf_timestep(C.byref(self.model), self.ims.h, C.byref(nl), dp(self.condsat),
                                       ip(self.ibound), kper, kstp, delt, int(transient), dp(self.x),
