@@ -278,6 +278,11 @@ typedef struct gbsln_nonlinear {
   int nonmeth;     /* UNDER_RELAXATION: 0 none, 1 simple, 2 cooley, 3 dbd */
   double theta, akappa, gamma, amomentum;
   int iallowptc;   /* 1 = pseudo-transient continuation allowed (default) */
+  /* backtracking (sln_backtracking, NumericalSolution.f90:2680-2838):
+   * BACKTRACKING_NUMBER (0 = off), _TOLERANCE, _REDUCTION_FACTOR,
+   * _RESIDUAL_LIMIT */
+  int numtrack;
+  double btol, breduc, res_lim;
 } gbsln_nonlinear;
 
 typedef struct gbsln_handle gbsln_handle;
@@ -289,6 +294,7 @@ typedef struct gbsln_stats {
   int pivot_retries;
   double dxmax;       /* last outer max head change */
   double fill_ms, solve_ms, total_ms; /* device time of the step */
+  int backtracks;     /* backtracking reductions taken in the step */
 } gbsln_stats;
 
 int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,

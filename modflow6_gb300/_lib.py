@@ -75,7 +75,8 @@ class GbslnNonlinear(C.Structure):
     _fields_ = [
         ("dvclose", C.c_double), ("mxiter", C.c_int), ("nonmeth", C.c_int),
         ("theta", C.c_double), ("akappa", C.c_double), ("gamma", C.c_double),
-        ("amomentum", C.c_double), ("iallowptc", C.c_int),
+        ("amomentum", C.c_double), ("iallowptc", C.c_int), ("numtrack", C.c_int),
+        ("btol", C.c_double), ("breduc", C.c_double), ("res_lim", C.c_double),
     ]
 
 
@@ -83,7 +84,7 @@ class GbslnStats(C.Structure):
     _fields_ = [
         ("outer", C.c_int), ("inner_total", C.c_int), ("converged", C.c_int),
         ("pivot_retries", C.c_int), ("dxmax", C.c_double), ("fill_ms", C.c_double),
-        ("solve_ms", C.c_double), ("total_ms", C.c_double),
+        ("solve_ms", C.c_double), ("total_ms", C.c_double), ("backtracks", C.c_int),
     ]
 
 

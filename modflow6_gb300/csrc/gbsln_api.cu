@@ -251,6 +251,7 @@ struct gbsln_handle {
   cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
   // outer-loop state
   double bigch = 0, bigchold = 0, relaxold = 0, l2norm0_ptc = 0, ptcdel = 0;
+  double res_prev = 0, res_new = 0;  // backtracking residual norms
   std::vector<double> hpart;
   std::string err;
 };
@@ -480,7 +481,49 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
   const bool steady_newton = !transient && h->g.inewton;
   bool converged = false;
   double hncg = 0.0;
+  // the system without Newton terms (sln_buildsystem with inewton = 0) and
+  // the L2 norm of its residual over active cells (sln_l2norm)
+  auto build_l2_nonewton = [&](double *l2) -> int {
+    FillDev f0 = f;
+    f0.fn = 0;
+    SLN_CUDA(h, cudaMemsetAsync(h->amat, 0, sizeof(double) * h->nja, h->st));
+    SLN_CUDA(h, cudaMemsetAsync(h->rhs, 0, sizeof(double) * n, h->st));
+    gwf_npf_cf(n, h->g, h->ibound, h->x, h->d.sat, h->st);
+    gwf_fill(n, h->g, f0, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, h->amat, h->rhs, h->st);
+    gwf_l2_resid(n, h->d.ia, h->d.ja, h->amat, h->x, h->rhs, h->ibound, h->part, h->G, h->st);
+    double ss = 0.0;
+    int rc = reduce_host(h, false, &ss);
+    *l2 = sqrt(ss);
+    return rc;
+  };
   for (int kiter = 1; kiter <= h->nl.mxiter; ++kiter) {
+    if (h->nl.numtrack > 0) {
+      // sln_backtracking (NumericalSolution.f90:2680-2760): from the second
+      // outer iteration on, while the residual norm exceeds BTOL times the
+      // previous one, the last change is cut by BREDUC
+      // (get_backtracking_flag :2795-2817, apply_backtracking :2823-2838)
+      double l2 = 0.0;
+      if (int rc = build_l2_nonewton(&l2)) return rc;
+      if (kiter == 1) {
+        h->res_prev = l2;
+      } else {
+        h->res_new = l2;
+        if (h->res_new > h->res_prev * h->nl.btol) {
+          for (int nb = 1; nb <= h->nl.numtrack; ++nb) {
+            double dxm = 0.0;
+            if (int rc = read_dxmax(h, &dxm, nullptr)) return rc;
+            if (!(h->nl.breduc * fabs(dxm) >= h->nl.dvclose)) break;
+            gwf_backtrack(n, h->nl.breduc, h->ibound, h->x, h->xtemp, h->st);
+            s.backtracks += 1;
+            if (int rc = build_l2_nonewton(&h->res_new)) return rc;
+            if (nb == h->nl.numtrack) break;
+            if (h->res_new < h->res_prev * h->nl.btol) break;
+            if (h->res_new < h->nl.res_lim) break;
+          }
+        }
+        h->res_prev = h->res_new;
+      }
+    }
     cudaEvent_t f0, f1;
     cudaEventCreate(&f0);
     cudaEventCreate(&f1);
@@ -700,6 +743,7 @@ extern "C" int gbsln_restart(gbsln_handle *h) {
   SLN_CUDA(h, cudaMemcpyAsync(h->x, h->strt, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
   SLN_CUDA(h, cudaStreamSynchronize(h->st));
   h->bigch = h->bigchold = h->relaxold = h->l2norm0_ptc = h->ptcdel = 0.0;
+  h->res_prev = h->res_new = 0.0;
   return GBIMS_OK;
 }
 

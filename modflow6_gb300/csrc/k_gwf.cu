@@ -243,7 +243,7 @@ __global__ void k_gwf_fill(int nodes, NpfDev g, FillDev f, const int *__restrict
       diag = DADD(diag, 0.0);
     }
     // NPF fn (gwf-npf.f90:578-698), gather form
-    if (g.inewton) {
+    if (g.inewton && f.fn) {
       for (int ii = i0 + 1; ii < i1; ++ii) {
         int q = g.ja[ii];
         int n = min(p, q), m = max(p, q);
@@ -279,7 +279,7 @@ __global__ void k_gwf_fill(int nodes, NpfDev g, FillDev f, const int *__restrict
       }
     }
     // STO fn (gwf-sto.f90:353-439)
-    if (g.inewton && f.transient && ibound[p] > 0 && g.icelltype[p] != 0) {
+    if (g.inewton && f.fn && f.transient && ibound[p] > 0 && g.icelltype[p] != 0) {
       double tp = g.top[p], bt = g.bot[p];
       double tthk = DSUB(tp, bt);
       double hp = h[p];
@@ -681,6 +681,21 @@ void gwf_calcdx(int nodes, const int *active, const double *x, const double *xte
 void gwf_npf_nur(int nodes, int nrc, int nlay, const NpfDev &g, const int *ibound, double *x,
                  const double *xtemp, double *dx, int *flag, cudaStream_t st) {
   k_npf_nur<<<g_grid(nodes), 256, 0, st>>>(nodes, nrc, nlay, g, ibound, x, xtemp, dx, flag);
+}
+
+// apply_backtracking (NumericalSolution.f90:2823-2838), the same two
+// roundings as the reference: delx = breduc*(x - xtemp); x = xtemp + delx.
+__global__ void k_backtrack(int nodes, double breduc, const int *__restrict__ active, double *x,
+                            const double *__restrict__ xtemp) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nodes; n += gridDim.x * blockDim.x) {
+    if (active[n] < 1) continue;
+    const double delx = DMUL(breduc, DSUB(x[n], xtemp[n]));
+    x[n] = DADD(xtemp[n], delx);
+  }
+}
+void gwf_backtrack(int nodes, double breduc, const int *active, double *x, const double *xtemp,
+                   cudaStream_t st) {
+  k_backtrack<<<g_grid(nodes), 256, 0, st>>>(nodes, breduc, active, x, xtemp);
 }
 
 void gwf_budget(int nodes, const NpfDev &g, const FillDev &f, const int *bnd_kind,

@@ -19,6 +19,7 @@ struct NpfDev {
 // the WEL q then the RCH rate*area values in package and list order.
 struct FillDev {
   int transient;
+  int fn = 1;   // add the Newton terms (npf_fn, sto_fn) when the model uses Newton
   double tled;  // 1/delt
   const double *ss, *sy, *area;
   const int *bnd_ptr;
@@ -51,6 +52,9 @@ void gwf_calcdx(int nodes, const int *active, const double *x, const double *xte
                 cudaStream_t st);
 void gwf_npf_nur(int nodes, int nrc, int nlay, const NpfDev &g, const int *ibound, double *x,
                  const double *xtemp, double *dx, int *flag, cudaStream_t st);
+// apply_backtracking: x = xtemp + breduc * (x - xtemp) on active cells
+void gwf_backtrack(int nodes, double breduc, const int *active, double *x, const double *xtemp,
+                   cudaStream_t st);
 // Flows and model budget terms; part holds kGwfBudgetSlots doubles per block
 // (in/out of STO-SS, STO-SY, CHD, WEL, RCH; max |flowja diagonal|, its row).
 constexpr int kGwfBudgetSlots = 12;

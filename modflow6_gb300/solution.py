@@ -30,6 +30,10 @@ class Nonlinear:
     gamma: float = 1.0
     amomentum: float = 0.0
     iallowptc: int = 1
+    numtrack: int = 0         # BACKTRACKING_NUMBER (0: no backtracking)
+    btol: float = 0.0         # BACKTRACKING_TOLERANCE
+    breduc: float = 0.0       # BACKTRACKING_REDUCTION_FACTOR
+    res_lim: float = 0.0      # BACKTRACKING_RESIDUAL_LIMIT
 
     @classmethod
     def preset(cls, complexity: str, **kw) -> "Nonlinear":
@@ -39,7 +43,8 @@ class Nonlinear:
         elif c == "MODERATE":
             n = cls(1e-2, 50, 3, 0.9, 1e-4, 0.0, 0.0)
         elif c == "COMPLEX":
-            n = cls(1e-1, 100, 3, 0.8, 1e-4, 0.0, 0.0)
+            # sln_setouter (NumericalSolution.f90:2657-2668), with backtracking
+            n = cls(1e-1, 100, 3, 0.8, 1e-4, 0.0, 0.0, 1, 20, 1.05, 0.1, 0.002)
         else:
             raise ValueError(complexity)
         for k, v in kw.items():
@@ -108,7 +113,8 @@ class GwfSolution:
         npf = _lib.GbnpfOptions(int(m.inewton), 0, 0, 0, satomega, 0)
         cs = ims.to_c(0)
         cnl = _lib.GbslnNonlinear(nl.dvclose, nl.mxiter, nl.nonmeth, nl.theta, nl.akappa, nl.gamma,
-                                  nl.amomentum, nl.iallowptc)
+                                  nl.amomentum, nl.iallowptc, nl.numtrack, nl.btol, nl.breduc,
+                                  nl.res_lim)
         self._h = C.c_void_p()
         rc = lib.gbsln_create(C.byref(cm), C.byref(npf), C.byref(cs), C.byref(cnl),
                               _lib.dptr(keep["strt"]), C.byref(self._h))

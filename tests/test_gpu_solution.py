@@ -161,3 +161,35 @@ def test_budget_after_solve_within_reference_discrepancy(gblib):
     np.testing.assert_allclose(bg["rate_in"], bo["rate_in"], rtol=1e-6, atol=1e-9)
     np.testing.assert_allclose(bg["rate_out"], bo["rate_out"], rtol=1e-6, atol=1e-9)
     sol.close()
+
+
+def test_backtracking_matches_oracle(gblib):
+    """sln_backtracking on a transient Newton case whose residual rises
+    between outer iterations (c3 grid at 20 x 20 x 5 with wells at a fifth
+    of the full rates): with the COMPLEX preset's backtracking options both
+    the oracle and the GPU solution cut steps, and they end at the same
+    heads."""
+    m = make_config("c3", seed=1, scale=0.04)
+    m.wel_q = m.wel_q * 0.2
+    tol = dict(dvclose=1e-6, rclose=1e-3, iter1=500, ilinmeth=2)
+    g = oracle.Gwf(m, oracle.settings(**tol))
+    nl = Nonlinear(dvclose=1e-5, mxiter=100, nonmeth=3, theta=0.8, akappa=1e-4, gamma=0.0,
+                   numtrack=20, btol=1.05, breduc=0.1, res_lim=0.002)
+    sol = GwfSolution(m, ImsLinearSettings(**tol), nl)
+    delt = 10.0
+    bt_o = bt_g = 0
+    for kstp in range(1, 4):
+        so = g.timestep(kper=1, kstp=kstp, delt=delt, transient=True, dvclose=nl.dvclose,
+                        mxiter=nl.mxiter, nonmeth=nl.nonmeth, theta=nl.theta, akappa=nl.akappa,
+                        gamma=nl.gamma, amomentum=nl.amomentum, numtrack=nl.numtrack,
+                        btol=nl.btol, breduc=nl.breduc, res_lim=nl.res_lim)
+        sg = sol.timestep(1, kstp, delt)
+        assert so["converged"] == 1 and sg["converged"] == 1, (so, sg)
+        assert abs(sg["outer"] - so["outer"]) <= 3, (sg, so)
+        bt_o += so["backtracks"]
+        bt_g += sg["backtracks"]
+        delt *= 1.2
+    assert bt_o > 0 and bt_g > 0, (bt_o, bt_g)
+    assert abs(bt_g - bt_o) <= max(3, bt_o // 4), (bt_g, bt_o)
+    assert np.max(np.abs(sol.heads - g.x)) <= 1e-4
+    sol.close()
