@@ -163,8 +163,8 @@ struct Dia7 {
   int *d_err = nullptr;    // wait-limit error flag
 };
 
-// Elements of slack after every n-vector: the structured sweeps copy 16-byte
-// aligned segments that can run past the last cell.
+// Elements of slack after every n-vector, so that a kernel may read or
+// write whole 16-byte aligned segments past the last cell.
 constexpr int kVecPad = 256;
 void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, long long *slots);
 // The wavefront sweep configurations: chunk C, ring depth NS, prefetch PF,

@@ -194,9 +194,9 @@ extern "C" int gbnpf_create(const gbnpf_options *opt, int nodes, int nja, int nj
 extern "C" int gbnpf_fill(gbnpf_handle *h, const int *d_ibound, const double *d_hnew,
                           double *d_amat, double *d_rhs) {
   if (!h || !d_ibound || !d_hnew || !d_amat || !d_rhs) return GBIMS_ERR_ARG;
-  // NPF terms only: no storage, empty boundary lists
-  FillDev f;
-  memset(&f, 0, sizeof(f));
+  // NPF terms only (with the Newton terms of a Newton model): no storage,
+  // empty boundary lists
+  FillDev f{};
   f.bnd_ptr = h->zero_ptr;
   gwf_npf_cf(h->nodes, h->g, d_ibound, d_hnew, h->d.sat, h->st);
   gwf_fill(h->nodes, h->g, f, d_ibound, d_hnew, d_hnew, h->d.sat, h->d.condsat, d_amat, d_rhs, h->st);
@@ -459,7 +459,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
   h->last_delt = delt;
   gbsln_stats s;
   memset(&s, 0, sizeof(s));
-  float fill_ms = 0.f, solve_ms = 0.f;
+  float fill_ms = 0.f;
   SLN_CUDA(h, cudaEventRecord(h->e0, h->st));
   // prepareSolve: gwf_ad (xold = x) and chd_ad (x = xold = head)
   SLN_CUDA(h, cudaMemcpyAsync(h->xold, h->x, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->st));
@@ -469,7 +469,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
     k_apply_guess<<<std::min(4 * kNumSM, (n + 255) / 256), 256, 0, h->st>>>(n, h->ibound, d_guess, h->x);
   if (h->nchd > 0)
     k_set_chd<<<(h->nchd + 255) / 256, 256, 0, h->st>>>(h->nchd, h->chd_node, h->chd_head, h->x, h->xold);
-  FillDev f;
+  FillDev f{};
   f.transient = transient ? 1 : 0;
   f.tled = transient ? 1.0 / delt : 0.0;
   f.ss = h->ss;
@@ -648,7 +648,6 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
   s.total_ms = tot;
   s.converged = converged ? 1 : 0;
   s.dxmax = hncg;
-  (void)solve_ms;
   if (st) *st = s;
   return GBIMS_OK;
 }
@@ -661,7 +660,7 @@ extern "C" int gbsln_formulate(gbsln_handle *h, double delt, const double *hold,
   if (transient && !hold) return GBIMS_ERR_ARG;
   h->last_delt = delt;
   if (hold) SLN_CUDA(h, cudaMemcpyAsync(h->xold, hold, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
-  FillDev f;
+  FillDev f{};
   f.transient = transient ? 1 : 0;
   f.tled = transient ? 1.0 / delt : 0.0;
   f.ss = h->ss;
@@ -687,7 +686,7 @@ extern "C" int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table 
   if (!h->bpart) SLN_CUDA(h, cudaMalloc((void **)&h->bpart, sizeof(double) * kGwfBudgetSlots * h->G));
   double *dflow = nullptr;
   if (flowja) SLN_CUDA(h, cudaMallocAsync((void **)&dflow, sizeof(double) * h->nja, h->st));
-  FillDev f;
+  FillDev f{};
   f.transient = transient ? 1 : 0;
   f.tled = transient ? 1.0 / h->last_delt : 0.0;
   f.ss = h->ss;
