@@ -150,6 +150,26 @@ static void enqueue_iteration(gbims_handle *h, unsigned long long cond, int use_
   Ctl *c = h->d_ctl;
   cudaStream_t st = h->st;
   double *part = h->d_part;
+  if (h->nm > 0 && h->mixed) {
+    // batched ensemble, mixed form: every member's FP32 PCG iteration and,
+    // where due, its FP64 refinement, in the same launches
+    const BatchDev &B = h->bd;
+    precond32(h, h->f_d, h->f_z);
+    kb_dot32(B, h->f_d, h->f_z, part, st);
+    kb_ctl_cg_rho(B, part, st);
+    kb_cg_pupdate32(B, h->f_z, h->f_p, st);
+    spmv32(h, h->f_p, h->f_q, c);
+    kb_dot32(B, h->f_p, h->f_q, part, st);
+    kb_ctl_alpha(B, part, st);
+    kb_cg_update_mixed(B, h->d_x, h->f_d, h->f_p, h->f_q, part, st);
+    kb_ctl_mixed_inner(B, part, h->refine_factor, st);
+    kb_any_due(B, c, st);
+    residual64(h, c, 1);
+    kb_true_resid_stats(B, h->v_d, h->f_d, part, st);
+    kb_ctl_refine(B, part, st);
+    kb_all_done(B, c, cond, use_cond, 1, st);
+    return;
+  }
   if (h->nm > 0) {
     // batched ensemble, PCG: every member's iteration in the same launches
     const BatchDev &B = h->bd;
@@ -1029,8 +1049,9 @@ extern "C" int gbims_batch_create(const gbims_settings *settings, int nmembers,
   int rc = gbims_create(&s, neq, nja, ia, ja, out);
   gbims_handle *h = *out;
   if (rc != GBIMS_OK) return rc;
-  if (h->mixed || h->bcgs || s.north > 0)
-    return fail(h, GBIMS_ERR_UNSUPPORTED, "batched ensembles: FP64 PCG without NORTH");
+  if (h->bcgs || s.north > 0 || (h->mixed && s.iscl != 0))
+    return fail(h, GBIMS_ERR_UNSUPPORTED,
+                "batched ensembles: PCG without NORTH (and without scaling in the mixed form)");
   // block-diagonal: every column of a member's rows lies inside the member
   for (int m = 0; m < nmembers; ++m)
     for (int r = mrow[m]; r < mrow[m + 1]; ++r)
@@ -1143,11 +1164,16 @@ static int batch_apply_core(gbims_handle *h, int kstp, int *icnvg, int *in_iter,
   GB_CUDA(h, cudaMemcpyAsync(h->d_ctls, h->h_ctls, sizeof(Ctl) * nm, cudaMemcpyHostToDevice, st));
   GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
   int eg = std::min(4 * kNumSM, (n + 255) / 256);
-  k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
+  if (!h->mixed) k_zero_vec<<<eg, 256, 0, st>>>(n, h->v_p, h->v_q, h->v_z, nullptr);
   residual64(h, nullptr, 0);
   kb_sumsq64(h->bd, h->v_d, h->d_part, st);
   kb_ctl_set_l2norm0(h->bd, h->d_part, st);
   kb_all_done(h->bd, h->d_ctl, 0ULL, 0, 0, st);
+  if (h->mixed) {
+    // the FP32 recurrence starts from the FP64 residual
+    kr_f64_to_f32(n, h->v_d, h->f_d, st);
+    GB_CUDA(h, cudaMemsetAsync(h->f_p, 0, sizeof(float) * n, st));
+  }
   GB_CUDA(h, cudaGetLastError());
   if (!h->graph_tried) build_graph(h);
   if (h->graph_ok) {
@@ -1172,7 +1198,7 @@ static int batch_apply_core(gbims_handle *h, int kstp, int *icnvg, int *in_iter,
   GB_CUDA(h, cudaMemcpyAsync(h->h_ctls, h->d_ctls, sizeof(Ctl) * nm, cudaMemcpyDeviceToHost, st));
   GB_CUDA(h, cudaStreamSynchronize(st));
   GB_CUDA(h, cudaGetLastError());
-  h->launches += 4 + (long long)h->body_kernels * h->h_ctl->bodies;
+  h->launches += 4 + (h->mixed ? 1 : 0) + (long long)h->body_kernels * h->h_ctl->bodies;
   float ms = 0.f;
   cudaEventElapsedTime(&ms, h->ev0, h->ev1);
   bool nonfinite = false;
@@ -1195,7 +1221,7 @@ static int batch_apply_core(gbims_handle *h, int kstp, int *icnvg, int *in_iter,
       sm.l2norm0 = r.l2norm0;
       sm.l2norm = r.l2norm;
       sm.solve_ms = ms;
-      sm.refinements = 0;
+      sm.refinements = h->mixed ? (int)r.scratch[3] : 0;
       sm.structured = h->structured ? 1 : 0;
     }
   }

@@ -963,6 +963,130 @@ __global__ void k_b_all_done(BatchDev B, Ctl *gctl, unsigned long long cond, int
 }
 
 // ---------------------------------------------------------------------------
+// Batched mixed form: the single solve's FP32 inner loop and FP64
+// refinement (k_dot32c, k_cg_pupdate32, k_cg_update_mixed,
+// ctl_mixed_inner, k_true_resid_stats, ctl_refine) per member.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kRedBlock) k_b_dot32c(BatchDev B, const float *__restrict__ a,
+                                                         const float *__restrict__ b,
+                                                         double *__restrict__ part) {
+  const ChunkRef c = chunk_of(B, blockIdx.x);
+  if (B.ctls[c.m].done) return;
+  CSum acc{0.f, 0.f};
+  for (int i = c.r0 + threadIdx.x; i < c.r1; i += blockDim.x) csum_prod(acc, a[i], b[i]);
+  double v[1] = {csum_value(acc)};
+  block_sum<1>(v);
+  if (threadIdx.x == 0) member_part(part, B, c.m)[c.b] = v[0];
+}
+
+__global__ void __launch_bounds__(kRedBlock) k_b_cg_pupdate32(BatchDev B, const float *__restrict__ z,
+                                                               float *__restrict__ p) {
+  const ChunkRef c = chunk_of(B, blockIdx.x);
+  const Ctl &ctl = B.ctls[c.m];
+  if (ctl.done) return;
+  const bool first = ctl.first;
+  const float beta = (float)ctl.beta;
+  for (int i = c.r0 + threadIdx.x; i < c.r1; i += blockDim.x) p[i] = first ? z[i] : fmaf(beta, p[i], z[i]);
+}
+
+__global__ void __launch_bounds__(kRedBlock) k_b_cg_update_mixed(BatchDev B, double *__restrict__ x,
+                                                                  float *__restrict__ d,
+                                                                  const float *__restrict__ p,
+                                                                  const float *__restrict__ q,
+                                                                  double *__restrict__ part) {
+  const ChunkRef c = chunk_of(B, blockIdx.x);
+  const Ctl &ctl = B.ctls[c.m];
+  if (ctl.done) return;
+  const float alphaf = (float)ctl.alpha;
+  const int row0 = B.mr[c.m];  // member-local row numbers for the maxima
+  CSum l2{0.f, 0.f};
+  unsigned nf = 0, bdx = 0, brr = 0;
+  float vdx = 0.f, vrr = 0.f;
+  int idx_dx = -1, idx_rr = -1;
+  for (int i = c.r0 + threadIdx.x; i < c.r1; i += blockDim.x) {
+    const float tv = __fmul_rn(alphaf, p[i]);
+    x[i] = x[i] + (double)tv;
+    const unsigned at = __float_as_uint(tv) & 0x7fffffffu;
+    if (at > bdx) { bdx = at; vdx = tv; idx_dx = i - row0; }
+    const float di = __fmaf_rn(-alphaf, q[i], d[i]);
+    d[i] = di;
+    const unsigned ad = __float_as_uint(di) & 0x7fffffffu;
+    if (ad > brr) { brr = ad; vrr = di; idx_rr = i - row0; }
+    csum_prod(l2, di, di);
+    nf |= nonfinite(di) | nonfinite(tv);
+  }
+  double v[2] = {csum_value(l2), (double)nf};
+  MaxLoc m[2];
+  m[0].val = (double)vdx; m[0].idx = idx_dx;
+  m[1].val = (double)vrr; m[1].idx = idx_rr;
+  block_sum<2>(v);
+  block_maxloc<2>(m);
+  if (threadIdx.x == 0) {
+    double *pm = member_part(part, B, c.m);
+    const int G = c.G, b = c.b;
+    pm[b] = v[0];
+    pm[G + b] = m[0].val; pm[2 * G + b] = (double)m[0].idx;
+    pm[3 * G + b] = m[1].val; pm[4 * G + b] = (double)m[1].idx;
+    pm[5 * G + b] = v[1];
+  }
+}
+
+__global__ void k_b_ctl_mixed_inner(BatchDev B, const double *part, double refine_factor) {
+  const int m = blockIdx.x;
+  ctl_mixed_inner(B.ctls + m, part + 8LL * B.mc[m], B.mc[m + 1] - B.mc[m], 0, refine_factor);
+}
+
+// The batch's own block asks for the FP64 true residual when any member
+// does (the residual kernel is gated on it; members that are not due
+// ignore it).
+__global__ void k_b_any_due(BatchDev B, Ctl *gctl) {
+  __shared__ int s_any;
+  if (threadIdx.x == 0) s_any = 0;
+  __syncthreads();
+  for (int m = threadIdx.x; m < B.nm; m += blockDim.x)
+    if (!B.ctls[m].done && B.ctls[m].north_due == 2) atomicOr(&s_any, 1);
+  __syncthreads();
+  if (threadIdx.x == 0) gctl->north_due = s_any ? 2 : 0;
+}
+
+__global__ void __launch_bounds__(kRedBlock) k_b_true_resid_stats(BatchDev B,
+                                                                   const double *__restrict__ r,
+                                                                   float *__restrict__ d32,
+                                                                   double *__restrict__ part) {
+  const ChunkRef c = chunk_of(B, blockIdx.x);
+  const Ctl &ctl = B.ctls[c.m];
+  if (ctl.done || ctl.north_due != 2) return;
+  const int row0 = B.mr[c.m];
+  double v[2] = {0.0, 0.0};
+  unsigned nf = 0;
+  MaxLoc m[2];
+  m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
+  for (int i = c.r0 + threadIdx.x; i < c.r1; i += blockDim.x) {
+    const double ri = r[i];
+    d32[i] = (float)ri;
+    if (absgt(ri, m[1].val)) { m[1].val = ri; m[1].idx = i - row0; }
+    v[0] = fma(ri, ri, v[0]);
+    nf |= nonfinite(ri);
+  }
+  v[1] = (double)nf;
+  block_sum<2>(v);
+  block_maxloc<2>(m);
+  if (threadIdx.x == 0) {
+    double *pm = member_part(part, B, c.m);
+    const int G = c.G, b = c.b;
+    pm[b] = v[0];
+    pm[G + b] = 0.0; pm[2 * G + b] = -1.0;
+    pm[3 * G + b] = m[1].val; pm[4 * G + b] = (double)m[1].idx;
+    pm[5 * G + b] = v[1];
+  }
+}
+
+__global__ void k_b_ctl_refine(BatchDev B, const double *part) {
+  const int m = blockIdx.x;
+  ctl_refine(B.ctls + m, part + 8LL * B.mc[m], B.mc[m + 1] - B.mc[m], 0ULL, 0);
+}
+
+// ---------------------------------------------------------------------------
 // residual d = b - A x with its L2 norm and signed max|d| from CSR device
 // arrays, one row per thread (ims_base_residual + dnrm2, ImsLinearBase.f90:
 // 1291-1312; the row sum in amux order with FMA).  With one 256-row block per
@@ -1147,6 +1271,30 @@ void kb_ctl_cg_cnvg(const BatchDev &B, const double *part, cudaStream_t st) {
 void kb_all_done(const BatchDev &B, Ctl *gctl, unsigned long long cond, int use_cond,
                  int count_body, cudaStream_t st) {
   k_b_all_done<<<1, kRedBlock, 0, st>>>(B, gctl, cond, use_cond, count_body);
+}
+void kb_dot32(const BatchDev &B, const float *a, const float *b, double *part, cudaStream_t st) {
+  k_b_dot32c<<<B.nchunks, kRedBlock, 0, st>>>(B, a, b, part);
+}
+void kb_cg_pupdate32(const BatchDev &B, const float *z, float *p, cudaStream_t st) {
+  k_b_cg_pupdate32<<<B.nchunks, kRedBlock, 0, st>>>(B, z, p);
+}
+void kb_cg_update_mixed(const BatchDev &B, double *x, float *d, const float *p, const float *q,
+                        double *part, cudaStream_t st) {
+  k_b_cg_update_mixed<<<B.nchunks, kRedBlock, 0, st>>>(B, x, d, p, q, part);
+}
+void kb_ctl_mixed_inner(const BatchDev &B, const double *part, double refine_factor,
+                        cudaStream_t st) {
+  k_b_ctl_mixed_inner<<<B.nm, kRedBlock, 0, st>>>(B, part, refine_factor);
+}
+void kb_any_due(const BatchDev &B, Ctl *gctl, cudaStream_t st) {
+  k_b_any_due<<<1, kRedBlock, 0, st>>>(B, gctl);
+}
+void kb_true_resid_stats(const BatchDev &B, const double *r, float *d32, double *part,
+                         cudaStream_t st) {
+  k_b_true_resid_stats<<<B.nchunks, kRedBlock, 0, st>>>(B, r, d32, part);
+}
+void kb_ctl_refine(const BatchDev &B, const double *part, cudaStream_t st) {
+  k_b_ctl_refine<<<B.nm, kRedBlock, 0, st>>>(B, part);
 }
 
 }  // namespace gb

@@ -48,4 +48,15 @@ void kb_ctl_alpha(const BatchDev &B, const double *part, cudaStream_t st);
 void kb_ctl_cg_cnvg(const BatchDev &B, const double *part, cudaStream_t st);
 void kb_all_done(const BatchDev &B, Ctl *gctl, unsigned long long cond, int use_cond,
                  int count_body, cudaStream_t st);
+// batched mixed form (FP32 inner loop, FP64 refinement per member)
+void kb_dot32(const BatchDev &B, const float *a, const float *b, double *part, cudaStream_t st);
+void kb_cg_pupdate32(const BatchDev &B, const float *z, float *p, cudaStream_t st);
+void kb_cg_update_mixed(const BatchDev &B, double *x, float *d, const float *p, const float *q,
+                        double *part, cudaStream_t st);
+void kb_ctl_mixed_inner(const BatchDev &B, const double *part, double refine_factor,
+                        cudaStream_t st);
+void kb_any_due(const BatchDev &B, Ctl *gctl, cudaStream_t st);
+void kb_true_resid_stats(const BatchDev &B, const double *r, float *d32, double *part,
+                         cudaStream_t st);
+void kb_ctl_refine(const BatchDev &B, const double *part, cudaStream_t st);
 }  // namespace gb

@@ -193,3 +193,49 @@ def test_backtracking_matches_oracle(gblib):
     assert abs(bt_g - bt_o) <= max(3, bt_o // 4), (bt_g, bt_o)
     assert np.max(np.abs(sol.heads - g.x)) <= 1e-4
     sol.close()
+
+
+def test_gbnpf_fill_newton_bitexact(gblib):
+    """gbnpf_fill (the NPF package alone on caller-owned device arrays) on a
+    Newton model: npf_cf, npf_fc and npf_fn against the oracle's, bit for
+    bit."""
+    import ctypes as C
+    import torch
+    from modflow6_gb300 import _lib
+    m = make_config("c3", seed=3, scale=0.04)
+    con = m.connections()
+    g = oracle.Gwf(m, oracle.settings())
+    lib = oracle.load()
+    dpp, ipp = C.POINTER(C.c_double), C.POINTER(C.c_int)
+    lib.or_npf_cf.argtypes = [C.POINTER(oracle.GwfModel), ipp, dpp, dpp]
+    lib.or_npf_fc.argtypes = [C.POINTER(oracle.GwfModel), ipp, dpp, dpp, dpp, dpp, dpp]
+    lib.or_npf_fn.argtypes = [C.POINTER(oracle.GwfModel), ipp, dpp, dpp, dpp, dpp]
+    rng = np.random.default_rng(4)
+    h = np.ascontiguousarray(m.strt + rng.uniform(-8.0, 3.0, m.nodes))
+    ib = np.ascontiguousarray(m.ibound, np.int32)
+    sat = np.zeros(m.nodes)
+    ao, ro = np.zeros(con["nja"]), np.zeros(m.nodes)
+    lib.or_npf_cf(C.byref(g.model), oracle.ip(ib), oracle.dp(h), oracle.dp(sat))
+    lib.or_npf_fc(C.byref(g.model), oracle.ip(ib), oracle.dp(g.condsat), oracle.dp(sat), oracle.dp(h),
+                  oracle.dp(ao), oracle.dp(ro))
+    lib.or_npf_fn(C.byref(g.model), oracle.ip(ib), oracle.dp(g.condsat), oracle.dp(h), oracle.dp(ao),
+                  oracle.dp(ro))
+    ip = lambda a: np.ascontiguousarray(a, dtype=np.int32).ctypes.data_as(C.POINTER(C.c_int))
+    dp = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(C.POINTER(C.c_double))
+    opt = _lib.GbnpfOptions(1, 0, 0, 0, 1.0e-6, 0)
+    hh = C.c_void_p()
+    keep = [np.ascontiguousarray(a) for a in (m.cell_top, m.cell_bot, m.k11, m.k33)]
+    assert gblib.gbnpf_create(C.byref(opt), m.nodes, con["nja"], con["njas"], ip(con["ia"]),
+                              ip(con["ja"]), ip(con["jas"]), ip(con["isym"]), ip(con["ihc"]),
+                              dp(con["cl1"]), dp(con["cl2"]), dp(con["hwva"]), dp(keep[0]),
+                              dp(keep[1]), dp(keep[2]), dp(keep[3]), ip(m.icelltype), C.byref(hh)) == 0
+    dev = torch.device("cuda")
+    d_amat = torch.zeros(con["nja"], dtype=torch.float64, device=dev)
+    d_rhs = torch.zeros(m.nodes, dtype=torch.float64, device=dev)
+    d_ib = torch.from_numpy(ib).to(dev)
+    d_h = torch.from_numpy(h).to(dev)
+    torch.cuda.synchronize()
+    assert gblib.gbnpf_fill(hh, d_ib.data_ptr(), d_h.data_ptr(), d_amat.data_ptr(), d_rhs.data_ptr()) == 0
+    gblib.gbnpf_destroy(hh)
+    np.testing.assert_array_equal(d_amat.cpu().numpy(), ao)
+    np.testing.assert_array_equal(d_rhs.cpu().numpy(), ro)
