@@ -447,8 +447,11 @@ def ensemble_form(a, lib, barrier, maxr) -> dict:
     GPU (gbnpf_fill + sln_ls fix-ups), concatenated, and solved to its own
     closure by one batched PCG + ILU0 (gbims_batch_apply_device, the
     wavefront preconditioner over all members).  Inputs stay in HBM; each
-    timed step restores x and solves all members."""
+    timed step restores x and solves all members.  The same members are then
+    solved in the mixed form (FP32 inner loop per member, FP64 refinement)
+    unless --no-mixed."""
     import torch
+    from modflow6_gb300 import _lib
     from modflow6_gb300.ensemble import (EnsembleLinear, assemble_member, concat_systems,
                                          make_ensemble)
     from modflow6_gb300.ims import ImsLinearSettings
@@ -461,38 +464,51 @@ def ensemble_form(a, lib, barrier, maxr) -> dict:
                                                  [s[2] for s in systems], [s[3] for s in systems])
     del systems
     shapes = [(m.nlay, m.nrow, m.ncol) for m in members]
-    ens = EnsembleLinear(ImsLinearSettings(**C4_IMS)).allocate(mrow, ia, ja, shapes)
     dev = torch.device("cuda")
     d_amat, d_rhs = torch.from_numpy(amat).to(dev), torch.from_numpy(rhs).to(dev)
     d_x0 = torch.from_numpy(x0).to(dev)
     d_x = d_x0.clone()
-    res = None
-    tuning = None
-    for i in range(a.warmup):
-        d_x.copy_(d_x0)
-        res = ens.apply_device(d_amat.data_ptr(), d_rhs.data_ptr(), d_x.data_ptr())
-        if i == 0 and not a.no_tune:
-            tuning = autotune(lib, ens._h, reps=3)
-    barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(a.steps):
-        d_x.copy_(d_x0)
-        res = ens.apply_device(d_amat.data_ptr(), d_rhs.data_ptr(), d_x.data_ptr())
-    e1.record()
-    barrier()
-    ms = maxr(e0.elapsed_time(e1) / max(1, a.steps))
-    its = np.array([r.in_iter for r in res])
-    conv = int(sum(r.icnvg for r in res))
-    ens.close()
-    cells = int(mrow[-1])
-    return {"workload": f"{count} DIS members, nrow/ncol U{{50..450}} x scale {a.scale}, nlay U{{1..5}}",
-            "members": count, "cells": cells, "nonzeros": int(ia[-1]), "value": ms / 1e3, "unit": "s",
-            "members_per_s": count / (ms / 1e3), "converged": conv,
-            "inner_iterations": {"min": int(its.min()), "mean": float(its.mean()),
-                                 "max": int(its.max())},
-            "form": "FP64 batched PCG + wavefront ILU0, one CUDA graph for all members",
-            "tuning": tuning}
+
+    def run(precision):
+        ens = EnsembleLinear(ImsLinearSettings(precision=precision, **C4_IMS)).allocate(
+            mrow, ia, ja, shapes)
+        res = None
+        tuning = None
+        for i in range(a.warmup):
+            d_x.copy_(d_x0)
+            res = ens.apply_device(d_amat.data_ptr(), d_rhs.data_ptr(), d_x.data_ptr())
+            if i == 0 and not a.no_tune:
+                tuning = autotune(lib, ens._h, reps=3)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(a.steps):
+            d_x.copy_(d_x0)
+            res = ens.apply_device(d_amat.data_ptr(), d_rhs.data_ptr(), d_x.data_ptr())
+        e1.record()
+        barrier()
+        ms = maxr(e0.elapsed_time(e1) / max(1, a.steps))
+        its = np.array([r.in_iter for r in res])
+        ens.close()
+        return {"value": ms / 1e3, "unit": "s", "members_per_s": count / (ms / 1e3),
+                "converged": int(sum(r.icnvg for r in res)),
+                "inner_iterations": {"min": int(its.min()), "mean": float(its.mean()),
+                                     "max": int(its.max())},
+                "refinements_max": int(max(r.summary["refinements"] for r in res)),
+                "tuning": tuning}
+
+    out = {"workload": f"{count} DIS members, nrow/ncol U{{50..450}} x scale {a.scale}, "
+                       f"nlay U{{1..5}}",
+           "members": count, "cells": int(mrow[-1]), "nonzeros": int(ia[-1]),
+           "form": "FP64 batched PCG + wavefront ILU0, one CUDA graph for all members"}
+    out.update(run(_lib.GBIMS_FP64))
+    if not a.no_mixed:
+        mixed = run(_lib.GBIMS_MIXED)
+        mixed["form"] = ("FP32 matrix, factors and inner loop per member inside FP64 "
+                         "refinement, same closure")
+        mixed["vs_fp64"] = mixed["value"] / out["value"]
+        out["mixed"] = mixed
+    return out
 
 
 def warmstart_form(a) -> dict:
