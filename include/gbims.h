@@ -50,9 +50,12 @@ typedef struct gbims_settings {
   int iscl;         /* SCALING_METHOD: 0 none, 1 diagonal, 2 L2 norm */
   int iord;         /* REORDERING_METHOD: 0 none (others: GBIMS_ERR_UNSUPPORTED) */
   int north;        /* NUMBER_ORTHOGONALIZATIONS */
-  double relax;     /* RELAXATION_FACTOR (> 0 selects MILU0) */
-  int level;        /* PRECONDITIONER_LEVELS (> 0: ILUT, unsupported) */
-  double droptol;   /* PRECONDITIONER_DROP_TOLERANCE (> 0: ILUT, unsupported) */
+  double relax;     /* RELAXATION_FACTOR (> 0 selects MILU0 / MILUT) */
+  int level;        /* PRECONDITIONER_LEVELS (> 0: ILUT with lfil = level) */
+  double droptol;   /* PRECONDITIONER_DROP_TOLERANCE (> 0: ILUT).  ILUT works
+                       on the general pattern (no wavefront sweeps) and on up
+                       to 256 candidates per row and triangle before dropping
+                       (GBIMS_ERR_UNSUPPORTED beyond) */
   int precision;    /* GBIMS_FP64 or GBIMS_MIXED */
   int index_base;   /* 0 (C) or 1 (Fortran) for ia/ja */
   int nlay, nrow, ncol; /* optional DIS shape; enables the structured
@@ -130,9 +133,18 @@ int gbims_batch_apply_device(gbims_handle *h, double *d_amat, double *d_rhs, dou
 /* Building blocks of apply, exposed for callers that drive their own loop
  * and for kernel-level checks (host arrays):
  *  gbims_factor       preconditioner update, ims_base_pcu + ims_base_pcilu0
- *                     (ImsLinearBase.f90:761-864, 928-1042), from amat (nja);
+ *                     (ImsLinearBase.f90:761-864, 928-1042) or, for IPC 3/4,
+ *                     ilut (sparskit2/ilut.f90:48-465), from amat (nja);
  *  gbims_get_apc      copies APC (nja, the reference's layout: APC(1:NEQ) the
  *                     inverse pivots, then the L\U entries in JAPC order);
+ *                     ILU0/MILU0 only;
+ *  gbims_get_factor   copies the preconditioner as IAPC (neq+1), JAPC and APC
+ *                     (njapc each; 0-based).  Row i's L entries are at
+ *                     [IAPC(i), JAPC(i)), its U entries at [JAPC(i), IAPC(i+1)),
+ *                     APC(0:neq) the inverse pivots.  For ILUT this is
+ *                     sparskit's MSR storage (ALU/JLU/JU of ImsLinear.f90)
+ *                     with JLU's row pointers in IAPC and JU in JAPC(0:neq).
+ *                     Null arrays: *njapc only;
  *  gbims_matvec       y = A*x, amux (sparsekit.f90:1-59), with the matrix of
  *                     the last gbims_factor or apply;
  *  gbims_precondition z = M^-1 r, ims_base_ilu0a (ImsLinearBase.f90:1049-1092),
@@ -177,6 +189,8 @@ int gbims_set_tuning(gbims_handle *h, int sweep_config, int reduction_blocks, in
 
 int gbims_factor(gbims_handle *h, const double *amat, int *pivot_retries);
 int gbims_get_apc(gbims_handle *h, double *apc);
+int gbims_get_factor(gbims_handle *h, int *iapc, int *japc, double *apc, int capacity,
+                     int *njapc);
 int gbims_matvec(gbims_handle *h, const double *x, double *y);
 int gbims_precondition(gbims_handle *h, const double *r, double *z);
 

@@ -56,6 +56,12 @@ struct gbims_handle {
   int G_alloc = 0;         // reduction blocks the partials were sized for
   double refine_factor = 1.0e-5;  // 1e-4 saves 3 % of the iterations but loses accuracy with BiCGSTAB
   bool factored = false;
+  // ILUT / MILUT (IPC 3/4): padded per-row factor, the reference's storage
+  // length iwk (ims_calc_pcdims) and the positions of IAPC/JAPC/APC in use
+  IlutDev I;
+  IlutStatus *h_ilut = nullptr;
+  long long ilut_iwk = 0;
+  int njapc = 0;
   // batched ensemble (nm > 0): members concatenated into one block-diagonal
   // system, one control block per member, the handle's Ctl = all done
   int nm = 0;
@@ -371,7 +377,7 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   if (s->rclose == 0.0 && s->icnvgopt != 3) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RCLOSE MUST > 0.0"); }
   if (s->relax < 0.0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RELAX MUST BE >= 0.0"); }
   if (s->relax > 1.0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RELAX MUST BE <= 1.0"); }
-  if (h->ipc >= 3) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "ILUT/MILUT (PRECONDITIONER_LEVELS/DROP_TOLERANCE > 0) is not supported"); }
+  if (s->level < 0) { *out = h; return fail(h, GBIMS_ERR_ARG, "ILUT: PRECONDITIONER_LEVELS must be >= 0"); }
   if (s->iord != 0) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "REORDERING_METHOD RCM/MD is not supported"); }
   if (s->precision != GBIMS_FP64 && s->precision != GBIMS_MIXED) { *out = h; return fail(h, GBIMS_ERR_ARG, "precision must be GBIMS_FP64 or GBIMS_MIXED"); }
   h->mixed = (s->precision == GBIMS_MIXED);
@@ -422,6 +428,24 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
         if (h->japc[j] > r) { h->japc[r] = j; break; }
     }
   }
+  h->njapc = nja;
+  long long ilut_cap = 0;
+  if (h->ipc >= 3) {
+    // ILUT keeps at most lfil L and lfil - 1 U entries per row; its storage
+    // starts after the n inverse pivots and one unused slot (sparskit's MSR)
+    const long long sl = s->level, su = std::max(0, s->level - 1);
+    ilut_cap = (long long)neq + 1 + (long long)neq * (sl + su);
+    if (ilut_cap > INT_MAX) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "ILUT storage exceeds 32-bit positions"); }
+    int maxrow = 0;
+    for (int r = 0; r < neq; ++r) maxrow = std::max(maxrow, h->ia[r + 1] - h->ia[r]);
+    h->ilut_iwk = s->level > 0 ? (long long)neq * (2LL * s->level + 1) : (long long)neq * maxrow;
+    h->japc.assign((size_t)ilut_cap, 0);
+    h->I.n = neq;
+    h->I.lfil = s->level;
+    h->I.sl = (int)sl;
+    h->I.su = (int)su;
+  }
+  const size_t npc = h->ipc >= 3 ? (size_t)ilut_cap : (size_t)nja;
   // device state
   *out = h;
   GB_CUDA(h, cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
@@ -430,15 +454,35 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   GB_CUDA(h, dalloc(&h->d_ia, neq + 1));
   GB_CUDA(h, dalloc(&h->d_ja, nja));
   GB_CUDA(h, dalloc(&h->d_iapc, neq + 1));
-  GB_CUDA(h, dalloc(&h->d_japc, nja));
-  GB_CUDA(h, dalloc(&h->d_apc, nja));
+  GB_CUDA(h, dalloc(&h->d_japc, npc));
+  GB_CUDA(h, dalloc(&h->d_apc, npc));
   GB_CUDA(h, cudaMemcpy(h->d_ia, h->ia.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemcpy(h->d_ja, h->ja.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemcpy(h->d_iapc, h->iapc.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemcpy(h->d_japc, h->japc.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
-  GB_CUDA(h, cudaMemset(h->d_apc, 0, sizeof(double) * nja));
-  // optional structured 7-point sweeps (and the index-free SpMV)
-  if (s->nlay > 0 && s->nrow > 0 && s->ncol > 0 &&
+  GB_CUDA(h, cudaMemset(h->d_apc, 0, sizeof(double) * npc));
+  if (h->ipc >= 3) {
+    IlutDev &I = h->I;
+    const size_t nsl = std::max<size_t>(1, (size_t)neq * I.sl);
+    const size_t nsu = std::max<size_t>(1, (size_t)neq * I.su);
+    GB_CUDA(h, dalloc(&I.lcol, nsl));
+    GB_CUDA(h, dalloc(&I.lval, nsl));
+    GB_CUDA(h, dalloc(&I.ucol, nsu));
+    GB_CUDA(h, dalloc(&I.uval, nsu));
+    GB_CUDA(h, dalloc(&I.nl, neq));
+    GB_CUDA(h, dalloc(&I.nu, neq));
+    GB_CUDA(h, dalloc(&I.dinv, neq));
+    GB_CUDA(h, dalloc(&I.rdone, neq));
+    GB_CUDA(h, dalloc(&I.stat, 1));
+    GB_CUDA(h, cudaMemset(I.rdone, 0, sizeof(unsigned) * neq));
+    GB_CUDA(h, cudaMemset(I.nl, 0, sizeof(int) * neq));
+    GB_CUDA(h, cudaMemset(I.nu, 0, sizeof(int) * neq));
+    GB_CUDA(h, cudaMemset(I.dinv, 0, sizeof(double) * neq));
+    GB_CUDA(h, cudaMallocHost((void **)&h->h_ilut, sizeof(IlutStatus)));
+  }
+  // optional structured 7-point sweeps (and the index-free SpMV); the
+  // wavefront sweeps carry the ILU0 pattern only
+  if (h->ipc < 3 && s->nlay > 0 && s->nrow > 0 && s->ncol > 0 &&
       dia7_matches(s->nlay, s->nrow, s->ncol, neq, h->ia, h->ja)) {
     std::vector<int> shape = {s->nlay, s->nrow, s->ncol};
     int rc = setup_structured(h, shape, std::vector<long long>{0});
@@ -485,7 +529,7 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
     }
   } else {
     // FP32 factors and inner vectors; FP64 heads and true residual
-    GB_CUDA(h, dalloc(&h->d_apc32, nja));
+    GB_CUDA(h, dalloc(&h->d_apc32, npc));
     GB_CUDA(h, dalloc(&h->f_d, nn)); GB_CUDA(h, dalloc(&h->f_p, nn));
     GB_CUDA(h, dalloc(&h->f_q, nn)); GB_CUDA(h, dalloc(&h->f_z, nn));
     if (h->bcgs) {
@@ -537,6 +581,97 @@ __global__ void k_zero_vec(int n, double *a, double *b, double *c, double *d) {
   }
 }
 
+static void drop_graph(gbims_handle *h);
+
+// ILUT / MILUT update (ims_base_pcu, IPC 3/4: ImsLinearBase.f90:812-864
+// around sparskit2/ilut.f90:48-465).  The pivot guard's retry loop is the
+// reference's; ilut leaves izero unchanged on success, so a factorisation
+// with izero 2 (delta 0.5) makes the reference repeat the same factorisation
+// until icount exceeds 10: that count is taken without the repeats.  The
+// pattern the factor kept is turned into IAPC/JAPC here, with the storage
+// checks of ilut (ierr -2/-3) at the reference's positions, and the level
+// schedules of the sweeps are rebuilt for it.
+static int ilut_factor_core(gbims_handle *h) {
+  const int n = h->n;
+  cudaStream_t st = h->st;
+  IlutDev &I = h->I;
+  int ipcflag = 0, icount = 0;
+  double delta = 0.0;
+  for (;;) {
+    I.epoch += 1;
+    if (I.epoch == 0) {  // completion words wrapped: clear them
+      GB_CUDA(h, cudaMemsetAsync(I.rdone, 0, sizeof(unsigned) * n, st));
+      I.epoch = 1;
+    }
+    IlutStatus init{0ULL, INT_MAX, kIlutOk, -1, 0};
+    *h->h_ilut = init;
+    GB_CUDA(h, cudaMemcpyAsync(I.stat, h->h_ilut, sizeof(IlutStatus), cudaMemcpyHostToDevice, st));
+    launch_ilut_factor(I, h->d_ia, h->d_ja, h->d_amat, h->s.droptol, h->s.relax, delta, ipcflag,
+                       st);
+    h->launches += 1;
+    GB_CUDA(h, cudaMemcpyAsync(h->h_ilut, I.stat, sizeof(IlutStatus), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(h, cudaStreamSynchronize(st));
+    GB_CUDA(h, cudaGetLastError());
+    const IlutStatus r = *h->h_ilut;
+    if (r.err == kIlutErrCap)
+      return fail(h, GBIMS_ERR_UNSUPPORTED,
+                  "ILUT: the working row of row " + std::to_string(r.err_row) + " exceeds " +
+                      std::to_string(kIlutCap) +
+                      " candidates (lower PRECONDITIONER_LEVELS or raise DROP_TOLERANCE)");
+    if (r.err == kIlutErrZeroRow)
+      return fail(h, GBIMS_ERR_ARG, "ILUT: zero row encountered (ilut ierr -5)");
+    if (r.err != kIlutOk) return fail(h, GBIMS_ERR_CUDA, "ILUT factorisation wait limit reached");
+    if (r.pivot_fail != INT_MAX) ipcflag = 1;
+    if (ipcflag < 1) break;
+    if (ipcflag == 2) {  // the repeats of an identical factorisation
+      icount = std::max(icount, 11);
+      break;
+    }
+    delta = 1.5 * delta + 1.0e-3;
+    ipcflag = 0;
+    if (delta > 0.5) {
+      delta = 0.5;
+      ipcflag = 2;
+    }
+    icount += 1;
+    if (icount > 10) break;
+  }
+  // the kept pattern as IAPC/JAPC, with ilut's storage checks
+  std::vector<int> nl(n), nu(n), lc((size_t)n * I.sl), uc((size_t)n * I.su);
+  GB_CUDA(h, cudaMemcpyAsync(nl.data(), I.nl, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  GB_CUDA(h, cudaMemcpyAsync(nu.data(), I.nu, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+  if (!lc.empty())
+    GB_CUDA(h, cudaMemcpyAsync(lc.data(), I.lcol, sizeof(int) * lc.size(), cudaMemcpyDeviceToHost, st));
+  if (!uc.empty())
+    GB_CUDA(h, cudaMemcpyAsync(uc.data(), I.ucol, sizeof(int) * uc.size(), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(h, cudaStreamSynchronize(st));
+  long long ju0 = (long long)n + 1;
+  h->iapc[0] = (int)ju0;
+  for (int r = 0; r < n; ++r) {
+    if (nl[r] < 0 || nl[r] > I.sl || nu[r] < 0 || nu[r] > I.su)
+      return fail(h, GBIMS_ERR_STATE, "ILUT: row counts out of range");
+    for (int k = 0; k < nl[r]; ++k) {
+      if (ju0 + 1 > h->ilut_iwk) return fail(h, GBIMS_ERR_ARG, "ILUT: L storage exceeded (ilut ierr -2)");
+      h->japc[ju0++] = lc[(size_t)r * I.sl + k];
+    }
+    h->japc[r] = (int)ju0;
+    const long long ilen = I.lfil > 0 ? nu[r] + 1 : 0;
+    if (ilen + ju0 + 1 > h->ilut_iwk) return fail(h, GBIMS_ERR_ARG, "ILUT: U storage exceeded (ilut ierr -3)");
+    for (int k = 0; k < nu[r]; ++k) h->japc[ju0++] = uc[(size_t)r * I.su + k];
+    h->iapc[r + 1] = (int)ju0;
+  }
+  h->njapc = (int)ju0;
+  GB_CUDA(h, cudaMemcpyAsync(h->d_iapc, h->iapc.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st));
+  GB_CUDA(h, cudaMemcpyAsync(h->d_japc, h->japc.data(), sizeof(int) * h->njapc, cudaMemcpyHostToDevice, st));
+  launch_ilut_scatter(I, h->d_iapc, h->d_japc, h->d_apc, st);
+  h->launches += 1;
+  levels_build_host(n, h->iapc, h->japc, true, h->F);
+  levels_build_host(n, h->iapc, h->japc, false, h->B);
+  drop_graph(h);  // the sweeps' level schedule is part of the captured loop
+  GB_CUDA(h, cudaStreamSynchronize(st));
+  return icount;
+}
+
 // Preconditioner update from h->d_amat: ims_base_pcu with its retry loop
 // (ImsLinearBase.f90:761-864).  Returns the retry count or a negative status.
 static int factor_core(gbims_handle *h) {
@@ -545,6 +680,17 @@ static int factor_core(gbims_handle *h) {
   if (h->dia_spmv) launch_dia7_vfill(h->D, h->d_ia, h->d_amat, st);
   else launch_sell_fill(h->S, h->d_amat, st);
   h->launches += 1;
+  if (h->ipc >= 3) {
+    int icount = ilut_factor_core(h);
+    if (icount < 0) return icount;
+    if (h->mixed) {
+      kr_f64_to_f32(h->njapc, h->d_apc, h->d_apc32, st);
+      h->launches += 1;
+    }
+    GB_CUDA(h, cudaGetLastError());
+    h->factored = true;
+    return icount;
+  }
   int ipcflag = 0, icount = 0;
   double delta = 0.0;
   for (;;) {
@@ -729,7 +875,22 @@ extern "C" int gbims_get_apc(gbims_handle *h, double *apc) {
   if (!h || !apc) return GBIMS_ERR_ARG;
   if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no factor: call gbims_factor or gbims_apply first");
   GB_CUDA(h, cudaStreamSynchronize(h->st));
+  if (h->ipc >= 3) return fail(h, GBIMS_ERR_STATE, "ILUT: the factor's pattern varies; use gbims_get_factor");
   GB_CUDA(h, cudaMemcpy(apc, h->d_apc, sizeof(double) * h->nja, cudaMemcpyDeviceToHost));
+  return GBIMS_OK;
+}
+
+extern "C" int gbims_get_factor(gbims_handle *h, int *iapc, int *japc, double *apc,
+                                int capacity, int *njapc) {
+  if (!h || !njapc) return GBIMS_ERR_ARG;
+  if (!h->factored) return fail(h, GBIMS_ERR_STATE, "no factor: call gbims_factor or gbims_apply first");
+  *njapc = h->njapc;
+  if (!iapc || !japc || !apc) return GBIMS_OK;  // size query
+  if (capacity < h->njapc) return fail(h, GBIMS_ERR_ARG, "capacity below the factor's storage");
+  GB_CUDA(h, cudaStreamSynchronize(h->st));
+  GB_CUDA(h, cudaMemcpy(iapc, h->d_iapc, sizeof(int) * (h->n + 1), cudaMemcpyDeviceToHost));
+  GB_CUDA(h, cudaMemcpy(japc, h->d_japc, sizeof(int) * h->njapc, cudaMemcpyDeviceToHost));
+  GB_CUDA(h, cudaMemcpy(apc, h->d_apc, sizeof(double) * h->njapc, cudaMemcpyDeviceToHost));
   return GBIMS_OK;
 }
 
@@ -996,10 +1157,13 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->f_q, h->f_z, h->f_t, h->f_v, h->f_dhat, h->f_phat, h->f_qhat, h->d_part,
                   h->d_dscale, h->d_dscale2, h->d_cptr, h->d_cpos, h->D.d_sv, h->D.f_sv,
                   h->d_bcm, h->d_bcr, h->d_bmc, h->d_bmr, h->d_ctls, h->D.d_geo, h->S.d_slm,
-                  h->LW.fwd, h->LW.bwd, h->LW.ticket, h->LW.err, h->d_ctl};
+                  h->LW.fwd, h->LW.bwd, h->LW.ticket, h->LW.err, h->d_ctl, h->I.lcol,
+                  h->I.lval, h->I.ucol, h->I.uval, h->I.nl, h->I.nu, h->I.dinv, h->I.rdone,
+                  h->I.stat};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
+  if (h->h_ilut) cudaFreeHost(h->h_ilut);
   if (h->h_ctls) cudaFreeHost(h->h_ctls);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -1049,9 +1213,10 @@ extern "C" int gbims_batch_create(const gbims_settings *settings, int nmembers,
   int rc = gbims_create(&s, neq, nja, ia, ja, out);
   gbims_handle *h = *out;
   if (rc != GBIMS_OK) return rc;
-  if (h->bcgs || s.north > 0 || (h->mixed && s.iscl != 0))
+  if (h->bcgs || s.north > 0 || (h->mixed && s.iscl != 0) || h->ipc >= 3)
     return fail(h, GBIMS_ERR_UNSUPPORTED,
-                "batched ensembles: PCG without NORTH (and without scaling in the mixed form)");
+                "batched ensembles: PCG with ILU0/MILU0 without NORTH (and without scaling in "
+                "the mixed form)");
   // block-diagonal: every column of a member's rows lies inside the member
   for (int m = 0; m < nmembers; ++m)
     for (int r = mrow[m]; r < mrow[m + 1]; ++r)

@@ -122,6 +122,33 @@ struct LevelWords {
   int *err = nullptr;
 };
 
+// ILUT / MILUT factorisation (k_ilut.cu).  kIlutCap bounds the working row
+// of one row (its L and its U candidates before dropping, each): ILUT with
+// PRECONDITIONER_LEVELS 5 and DROP_TOLERANCE 1e-4 on a 7-point grid reaches
+// about 125 L and 65 U candidates; PRECONDITIONER_LEVELS 10 about 230 and 165.
+constexpr int kIlutCap = 256;
+enum IlutError { kIlutOk = 0, kIlutErrWait = 1, kIlutErrCap = 2, kIlutErrZeroRow = 3 };
+
+struct IlutStatus {
+  unsigned long long next;  // next row to claim
+  int pivot_fail;           // lowest row whose pivot changed sign or vanished (INT_MAX: none)
+  int err;                  // IlutError
+  int err_row;
+  int pad;
+};
+
+// Per-row results in padded slots (sl = lfil L entries, su = lfil - 1 U
+// entries per row) and the completion word of each row (equal to epoch once
+// the row of the current attempt is stored).
+struct IlutDev {
+  int n = 0, lfil = 0, sl = 0, su = 0;
+  int *lcol = nullptr, *ucol = nullptr, *nl = nullptr, *nu = nullptr;
+  double *lval = nullptr, *uval = nullptr, *dinv = nullptr;
+  unsigned *rdone = nullptr;
+  IlutStatus *stat = nullptr;
+  unsigned epoch = 0;
+};
+
 // One full DIS grid ("member") of the wavefront layout.  A single model is
 // one member; a batched ensemble has one per model, laid end to end.
 struct Dia7Geo {
@@ -198,6 +225,10 @@ void launch_ilu_factor(int n, const int *d_ia, const int *d_ja, const double *d_
                        const int *d_iapc, const int *d_japc, double *d_apc,
                        const Levels &L, double relax, double delta, int ipcflag,
                        Ctl *ctl, cudaStream_t st);
+void launch_ilut_factor(const IlutDev &I, const int *d_ia, const int *d_ja, const double *d_amat,
+                        double droptol, double relax, double delta, int izero, cudaStream_t st);
+void launch_ilut_scatter(const IlutDev &I, const int *d_iapc, const int *d_japc, double *d_apc,
+                         cudaStream_t st);
 void launch_ilu_apply_levels(int n, const int *d_iapc, const int *d_japc,
                              const double *d_apc, const Levels &F, const Levels &B,
                              const LevelWords &Wd, const double *r, double *d, const Ctl *ctl,

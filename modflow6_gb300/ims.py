@@ -122,6 +122,25 @@ class ImsLinear:
             raise _lib.GbimsError(rc, lib.gbims_last_error(self._h).decode())
         return ApplyResult(icnvg.value, in_iter.value, rc, _summary(sm))
 
+    def get_factor(self):
+        """The preconditioner of the last factor or apply as (iapc, japc, apc),
+        0-based: row i's L entries at [iapc[i], japc[i]), its U entries at
+        [japc[i], iapc[i+1]), apc[:neq] the inverse pivots (ILU0's APC, or
+        ILUT's MSR storage with its row pointers in iapc)."""
+        lib = _lib.load()
+        njapc = C.c_int(0)
+        rc = lib.gbims_get_factor(self._h, None, None, None, 0, C.byref(njapc))
+        if rc < 0:
+            raise _lib.GbimsError(rc, lib.gbims_last_error(self._h).decode())
+        iapc = np.zeros(self.neq + 1, np.int32)
+        japc = np.zeros(njapc.value, np.int32)
+        apc = np.zeros(njapc.value)
+        rc = lib.gbims_get_factor(self._h, _lib.iptr(iapc), _lib.iptr(japc), _lib.dptr(apc),
+                                  njapc.value, C.byref(njapc))
+        if rc < 0:
+            raise _lib.GbimsError(rc, lib.gbims_last_error(self._h).decode())
+        return iapc, japc, apc
+
     def apply_device(self, d_amat: int, d_rhs: int, d_x: int, kstp: int = 1,
                      kiter: int = 1) -> ApplyResult:
         """imslinear_apply on device pointers (e.g. torch tensors' data_ptr())."""

@@ -259,7 +259,236 @@ int or_pcu(int nja, int neq, int ipc, double relax, const double *amat,
   return icount;
 }
 
-/* ImsLinearBase.f90:1049-1092, ims_base_ilu0a: forward then backward solve. */
+/* sparskit2/ilut.f90:515-579, qsplit: partial quick-sort of a[0..n) by
+ * decreasing magnitude so that the ncut-th entry (1-based, as in the
+ * reference) splits larger from smaller ones; ind moves with a. */
+static void or_qsplit(int n, double *a, int *ind, int ncut) {
+  int first = 0, last = n - 1, cut = ncut - 1;
+  if (cut < first || cut > last) return;
+  for (;;) {
+    int mid = first;
+    double abskey = fabs(a[mid]);
+    for (int j = first + 1; j <= last; ++j) {
+      if (fabs(a[j]) > abskey) {
+        ++mid;
+        double t = a[mid]; a[mid] = a[j]; a[j] = t;
+        int it = ind[mid]; ind[mid] = ind[j]; ind[j] = it;
+      }
+    }
+    double t = a[mid]; a[mid] = a[first]; a[first] = t;
+    int it = ind[mid]; ind[mid] = ind[first]; ind[first] = it;
+    if (mid == cut) return;
+    if (mid > cut) last = mid - 1;
+    else first = mid + 1;
+  }
+}
+
+/* sparskit2/ilut.f90:48-465, ilut: dual-threshold incomplete LU with the
+ * MODFLOW changes (relaxation of the dropped sum, MILUT; pivot guard through
+ * izero and delta).  Row ii keeps at most lfil L entries (|multiplier| above
+ * droptol) and lfil - 1 U entries (|u| above droptol x the row's mean |a|),
+ * the largest by qsplit, in qsplit's order.
+ *
+ * Layout: sparskit's modified sparse row storage with its row pointers moved
+ * out of jlu, so that the factor has the IAPC/JAPC/APC shape the ILU0
+ * application reads: alu[0..n) the inverse pivots; row ii's L entries at
+ * [iapc[ii], japc[ii]) and its U entries at [japc[ii], iapc[ii+1]), columns
+ * in japc and values in alu from position n + 1 on (sparskit's jlu(1) = n+2).
+ * iwk is the reference's storage length (ims_calc_pcdims,
+ * ImsLinearBase.f90:1148-1197); the arrays hold max(iwk, n + 1) entries.
+ * Work arrays: w (n), jw (n), jr (n).  Returns ierr: 0, -1 (row longer than
+ * n), -2/-3 (L/U storage), -4 (lfil < 0), -5 (zero row). */
+int or_ilut(int n, const double *a, const int *ja, const int *ia, int lfil, double droptol,
+            double *alu, int *iapc, int *japc, int iwk, double *w, int *jw, int *jr,
+            double relax, int *izero, double delta) {
+  if (lfil < 0) return -4;
+  int ju0 = n + 1; /* next free storage position */
+  iapc[0] = ju0;
+  for (int j = 0; j < n; ++j) jr[j] = -1;
+  for (int ii = 0; ii < n; ++ii) {
+    const int j1 = ia[ii], j2 = ia[ii + 1];
+    double dropsum = 0.0, tnorm = 0.0;
+    for (int k = j1; k < j2; ++k) tnorm = tnorm + fabs(a[k]);
+    if (tnorm == 0.0) return -5;
+    tnorm = tnorm / (double)(j2 - j1);
+    /* unpack: L part at [0, lenl), the diagonal at ii, U part at ii+1.. */
+    int lenu = 1, lenl = 0;
+    jw[ii] = ii;
+    w[ii] = 0.0;
+    jr[ii] = ii;
+    for (int j = j1; j < j2; ++j) {
+      const int k = ja[j];
+      const double t = a[j];
+      if (k < ii) {
+        jw[lenl] = k;
+        w[lenl] = t;
+        jr[k] = lenl;
+        ++lenl;
+      } else if (k == ii) {
+        w[ii] = t;
+      } else {
+        const int jpos = ii + lenu;
+        ++lenu;
+        jw[jpos] = k;
+        w[jpos] = t;
+        jr[k] = jpos;
+      }
+    }
+    /* eliminate the earlier rows, smallest column first */
+    int ilen = 0;
+    for (int jj = 0; jj < lenl; ++jj) {
+      int jrow = jw[jj], k = jj;
+      for (int j = jj + 1; j < lenl; ++j)
+        if (jw[j] < jrow) {
+          jrow = jw[j];
+          k = j;
+        }
+      if (k != jj) {
+        const int j = jw[jj];
+        jw[jj] = jw[k];
+        jw[k] = j;
+        jr[jrow] = jj;
+        jr[j] = k;
+        const double s = w[jj];
+        w[jj] = w[k];
+        w[k] = s;
+      }
+      jr[jrow] = -1;
+      const double fact = w[jj] * alu[jrow];
+      if (fabs(fact) <= droptol) {
+        dropsum = dropsum + w[jj];
+        continue;
+      }
+      for (int kk = japc[jrow]; kk < iapc[jrow + 1]; ++kk) {
+        const double s = fact * alu[kk];
+        const int j = japc[kk];
+        const int jpos = jr[j];
+        if (j >= ii) {
+          if (jpos < 0) {
+            if (lenu + 1 > n) return -1;
+            const int i = ii + lenu;
+            ++lenu;
+            jw[i] = j;
+            jr[j] = i;
+            w[i] = -s;
+          } else {
+            w[jpos] = w[jpos] - s;
+          }
+        } else {
+          if (jpos < 0) {
+            if (lenl + 1 > n) return -1;
+            jw[lenl] = j;
+            jr[j] = lenl;
+            w[lenl] = -s;
+            ++lenl;
+          } else {
+            w[jpos] = w[jpos] - s;
+          }
+        }
+      }
+      w[ilen] = fact;
+      jw[ilen] = jrow;
+      ++ilen;
+    }
+    for (int k = 0; k < lenu; ++k) jr[jw[ii + k]] = -1;
+    /* L: the lfil largest multipliers */
+    lenl = ilen;
+    ilen = lenl < lfil ? lenl : lfil;
+    or_qsplit(lenl, w, jw, ilen);
+    for (int k = 0; k < ilen; ++k) {
+      if (ju0 + 1 > iwk) return -2;
+      alu[ju0] = w[k];
+      japc[ju0] = jw[k];
+      ++ju0;
+    }
+    japc[ii] = ju0;
+    /* U: drop below droptol x tnorm, then the lfil - 1 largest */
+    ilen = 0;
+    for (int k = 1; k < lenu; ++k) {
+      if (fabs(w[ii + k]) > droptol * tnorm) {
+        ++ilen;
+        w[ii + ilen] = w[ii + k];
+        jw[ii + ilen] = jw[ii + k];
+      } else {
+        dropsum = dropsum + w[ii + k];
+      }
+    }
+    lenu = ilen + 1;
+    ilen = lenu < lfil ? lenu : lfil;
+    or_qsplit(lenu - 1, w + ii + 1, jw + ii + 1, ilen);
+    if (ilen + ju0 + 1 > iwk) return -3;
+    for (int k = ii + 1; k < ii + ilen; ++k) {
+      japc[ju0] = jw[k];
+      alu[ju0] = w[k];
+      ++ju0;
+    }
+    /* the pivot, guarded against a sign change or zero */
+    const double diag = w[ii];
+    double dw = (1.0 + delta) * diag + (relax * dropsum);
+    const double sc = f_sign(diag, dw);
+    if (sc != diag) {
+      if (*izero > 1) {
+        dw = f_sign(1.0, diag) * (1.0e-4 + droptol) * tnorm;
+      } else {
+        *izero = 1;
+        return 0; /* EXIT MAIN */
+      }
+    }
+    if (fabs(dw) == 0.0) {
+      if (*izero > 1) {
+        dw = f_sign(1.0, diag) * (1.0e-4 + droptol) * tnorm;
+      } else {
+        *izero = 1;
+        return 0;
+      }
+    }
+    w[ii] = dw;
+    alu[ii] = 1.0 / w[ii];
+    iapc[ii + 1] = ju0;
+  }
+  return 0;
+}
+
+/* ImsLinearBase.f90:761-864, ims_base_pcu for IPC 3/4.  ilut leaves izero
+ * as it found it on success, so once the retries reach delta = 0.5
+ * (ipcflag 2) the loop refactors until icount exceeds 10, as the reference
+ * does.  Returns icount, or ierr (< 0) from ilut. */
+int or_pcu_ilut(int neq, int lfil, double droptol, double relax, const double *amat,
+                const int *ia, const int *ja, double *alu, int *iapc, int *japc, int iwk,
+                double *w, int *jw, int *jr) {
+  int ipcflag = 0, icount = 0;
+  double delta = 0.0;
+  for (;;) {
+    int ierr = or_ilut(neq, amat, ja, ia, lfil, droptol, alu, iapc, japc, iwk, w, jw, jr,
+                       relax, &ipcflag, delta);
+    if (ierr != 0) return ierr;
+    if (ipcflag < 1) break;
+    delta = 1.5 * delta + DEM3;
+    ipcflag = 0;
+    if (delta > 0.5) {
+      delta = 0.5;
+      ipcflag = 2;
+    }
+    icount = icount + 1;
+    if (icount > 10) break;
+  }
+  return icount;
+}
+
+/* ImsLinearBase.f90:1148-1197, ims_calc_pcdims: the ILUT storage length. */
+int or_ilut_iwk(int neq, const int *ia, int level) {
+  if (level > 0) return neq * (level * 2 + 1);
+  int iwk = 0;
+  for (int n = 0; n < neq; ++n) {
+    int i = ia[n + 1] - ia[n];
+    if (i > iwk) iwk = i;
+  }
+  return neq * iwk;
+}
+
+/* ImsLinearBase.f90:1049-1092, ims_base_ilu0a: forward then backward solve.
+ * sparskit2/ilut.f90:467-513 (lusol, the ILUT application) is the same
+ * pair of sweeps over the ILUT storage. */
 void or_ilu0a(int nja, int neq, const double *apc, const int *iapc, const int *japc,
               const double *r, double *d) {
   (void)nja;
@@ -486,6 +715,9 @@ struct or_ims {
   int *iapc, *japc;
   double *apc, *w;
   int *iw;
+  int njapc, iwk;  /* storage of IAPC/JAPC/APC; ILUT: the reference's iwk */
+  int *jw, *jr;    /* ILUT work arrays */
+  int ilut_ierr;
   double *d, *p, *q, *z, *t, *v, *dhat, *phat, *qhat;
   double *dscale, *dscale2;
   double l2norm0, epfact;
@@ -505,9 +737,16 @@ or_ims *or_ims_create(const or_ims_settings *s, int neq, int nja, const int *ia,
   h->ja = (int *)malloc(sizeof(int) * nja);
   memcpy(h->ia, ia, sizeof(int) * (neq + 1));
   memcpy(h->ja, ja, sizeof(int) * nja);
+  h->njapc = nja;
+  if (h->ipc == 3 || h->ipc == 4) {
+    h->iwk = or_ilut_iwk(neq, ia, s->level);
+    h->njapc = h->iwk > neq + 1 ? h->iwk : neq + 1;
+    h->jw = (int *)calloc(neq, sizeof(int));
+    h->jr = (int *)calloc(neq, sizeof(int));
+  }
   h->iapc = (int *)calloc(neq + 1, sizeof(int));
-  h->japc = (int *)calloc(nja, sizeof(int));
-  h->apc = (double *)calloc(nja, sizeof(double));
+  h->japc = (int *)calloc(h->njapc, sizeof(int));
+  h->apc = (double *)calloc(h->njapc, sizeof(double));
   h->iw = (int *)calloc(neq, sizeof(int));
   h->w = (double *)calloc(neq, sizeof(double));
   double **vecs[] = {&h->d, &h->p, &h->q, &h->z, &h->t, &h->v, &h->dhat, &h->phat,
@@ -528,10 +767,13 @@ void or_ims_destroy(or_ims *h) {
   free(h->iw); free(h->w); free(h->d); free(h->p); free(h->q); free(h->z);
   free(h->t); free(h->v); free(h->dhat); free(h->phat); free(h->qhat);
   free(h->dscale); free(h->dscale2);
+  free(h->jw); free(h->jr);
   free(h);
 }
 
 int or_ims_ipc(const or_ims *h) { return h->ipc; }
+int or_ims_njapc(const or_ims *h) { return h->njapc; }
+int or_ims_ilut_ierr(const or_ims *h) { return h->ilut_ierr; }
 const int *or_ims_iapc(const or_ims *h) { return h->iapc; }
 const int *or_ims_japc(const or_ims *h) { return h->japc; }
 const double *or_ims_apc(const or_ims *h) { return h->apc; }
@@ -544,12 +786,20 @@ int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int 
   const or_ims_settings *s = &h->s;
   int neq = h->neq, nja = h->nja;
   if (s->iord != 0) return -2; /* reordering is not restated here */
-  if (h->ipc != 1 && h->ipc != 2) return -3; /* ILUT is not restated here */
   h->epfact = or_epfact(s->icnvgopt, kstp);
   if (s->iscl != 0)
     or_scale(0, s->iscl, neq, nja, h->ia, h->ja, amat, x, rhs, h->dscale, h->dscale2);
-  h->npivot_retries = or_pcu(nja, neq, h->ipc, s->relax, amat, h->ia, h->ja, h->apc,
-                             h->iapc, h->japc, h->iw, h->w);
+  if (h->ipc == 1 || h->ipc == 2) {
+    h->npivot_retries = or_pcu(nja, neq, h->ipc, s->relax, amat, h->ia, h->ja, h->apc,
+                               h->iapc, h->japc, h->iw, h->w);
+  } else {
+    int rc = or_pcu_ilut(neq, s->level, s->droptol, s->relax, amat, h->ia, h->ja, h->apc,
+                         h->iapc, h->japc, h->iwk, h->w, h->jw, h->jr);
+    /* ImsLinearBase.f90:822-834: an ilut error is fatal in the reference */
+    h->ilut_ierr = rc < 0 ? rc : 0;
+    if (rc < 0) return -4;
+    h->npivot_retries = rc;
+  }
   (void)kiter;
   *icnvg = 0;
   for (int n = 0; n < neq; ++n) {

@@ -54,6 +54,15 @@ void or_ims_destroy(or_ims *h);
 int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int kiter,
                  int *icnvg, int *in_iter, or_cnvg_record *rec, int nrec);
 int or_ims_ipc(const or_ims *h);
+int or_ims_njapc(const or_ims *h);
+int or_ims_ilut_ierr(const or_ims *h);
+int or_ilut(int n, const double *a, const int *ja, const int *ia, int lfil, double droptol,
+            double *alu, int *iapc, int *japc, int iwk, double *w, int *jw, int *jr,
+            double relax, int *izero, double delta);
+int or_pcu_ilut(int neq, int lfil, double droptol, double relax, const double *amat,
+                const int *ia, const int *ja, double *alu, int *iapc, int *japc, int iwk,
+                double *w, int *jw, int *jr);
+int or_ilut_iwk(int neq, const int *ia, int level);
 const int *or_ims_iapc(const or_ims *h);
 const int *or_ims_japc(const or_ims *h);
 const double *or_ims_apc(const or_ims *h);

@@ -88,6 +88,11 @@ def load():
         lib.or_ims_l2norm0.restype = C.c_double
         lib.or_ims_l2norm0.argtypes = [C.c_void_p]
         lib.or_ims_pivot_retries.argtypes = [C.c_void_p]
+        lib.or_ims_njapc.argtypes = [C.c_void_p]
+        lib.or_ims_ilut_ierr.argtypes = [C.c_void_p]
+        lib.or_ilut_iwk.argtypes = [C.c_int, _ip, C.c_int]
+        lib.or_pcu_ilut.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp, _ip, _ip, _dp,
+                                    _ip, _ip, C.c_int, _dp, _ip, _ip]
         lib.or_amux.argtypes = [C.c_int, _dp, _dp, _dp, _ip, _ip]
         lib.or_ilu0a.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, _dp, _dp]
         lib.or_amux_fma.argtypes = [C.c_int, _dp, _dp, _dp, _ip, _ip]
@@ -153,19 +158,30 @@ class Ims:
         rec = (CnvgRecord * max(nrec, 1))()
         rc = self.lib.or_ims_apply(self.h, dp(amat), dp(rhs), dp(x), kstp, kiter, C.byref(icnvg),
                                    C.byref(in_iter), rec if nrec else None, nrec)
+        if rc == -4:
+            raise RuntimeError(f"oracle ilut failed: ierr {self.lib.or_ims_ilut_ierr(self.h)}")
         if rc != 0:
             raise RuntimeError(f"oracle apply failed: {rc}")
         recs = [{f: getattr(rec[i], f) for f, _ in CnvgRecord._fields_} for i in range(min(nrec, in_iter.value))]
         return icnvg.value, in_iter.value, recs
 
     def apc(self) -> np.ndarray:
-        return np.ctypeslib.as_array(self.lib.or_ims_apc(self.h), shape=(self.nja,)).copy()
+        n = self.lib.or_ims_njapc(self.h)
+        return np.ctypeslib.as_array(self.lib.or_ims_apc(self.h), shape=(n,)).copy()
 
     def iapc(self) -> np.ndarray:
         return np.ctypeslib.as_array(self.lib.or_ims_iapc(self.h), shape=(self.neq + 1,)).copy()
 
     def japc(self) -> np.ndarray:
-        return np.ctypeslib.as_array(self.lib.or_ims_japc(self.h), shape=(self.nja,)).copy()
+        n = self.lib.or_ims_njapc(self.h)
+        return np.ctypeslib.as_array(self.lib.or_ims_japc(self.h), shape=(n,)).copy()
+
+    def factor(self):
+        """The preconditioner after the last apply as (iapc, japc, apc), cut
+        to the storage in use (ILUT: positions up to iapc[neq])."""
+        iapc = self.iapc()
+        used = int(iapc[-1]) if self.lib.or_ims_ipc(self.h) >= 3 else self.nja
+        return iapc, self.japc()[:used], self.apc()[:used]
 
     def l2norm0(self) -> float:
         return self.lib.or_ims_l2norm0(self.h)
@@ -178,6 +194,26 @@ class Ims:
             self.lib.or_ims_destroy(self.h)
         except Exception:
             pass
+
+
+def ilut(ia, ja, amat, level, droptol, relax=0.0):
+    """ims_base_pcu with ILUT/MILUT (sparskit2/ilut.f90) on one matrix:
+    returns (iapc, japc, apc, retries), storage cut to iapc[neq]."""
+    lib = load()
+    ia = np.ascontiguousarray(ia, np.int32)
+    ja = np.ascontiguousarray(ja, np.int32)
+    n = ia.size - 1
+    iwk = lib.or_ilut_iwk(n, ip(ia), level)
+    cap = max(iwk, n + 1)
+    alu, japc = np.zeros(cap), np.zeros(cap, np.int32)
+    iapc = np.zeros(n + 1, np.int32)
+    w, jw, jr = np.zeros(n), np.zeros(n, np.int32), np.zeros(n, np.int32)
+    rc = lib.or_pcu_ilut(n, level, droptol, relax, dp(np.ascontiguousarray(amat, float)), ip(ia),
+                         ip(ja), dp(alu), ip(iapc), ip(japc), iwk, dp(w), ip(jw), ip(jr))
+    if rc < 0:
+        raise RuntimeError(f"oracle ilut failed: ierr {rc}")
+    used = int(iapc[-1])
+    return iapc, japc[:used], alu[:used], rc
 
 
 def amux(ia, ja, a, x):

@@ -1,0 +1,189 @@
+"""ILUT / MILUT (IPC 3/4) on the GPU against the oracle, through the C ABI.
+
+The oracle restates sparskit2/ilut.f90 (ilut with MODFLOW's relaxation and
+pivot guard, qsplit) and the IPC 3/4 branch of ims_base_pcu
+(ImsLinearBase.f90:761-864); it is pinned by the newton01 known answer run
+with the whole COMPLEX preset (tests/test_oracle_known_answers.py).
+
+Bit-exact: the factor -- which entries survive the dual dropping, in
+qsplit's order, and their values -- for ILUT and MILUT at several
+PRECONDITIONER_LEVELS / DROP_TOLERANCE, with the pivot-guard retries; the
+application (lusol = the ilu0a sweeps, FMA).  Closure parity: PCG and
+BiCGSTAB solves; the mixed form; newton01 with the COMPLEX preset on the
+device-resident solution; a transient Newton run with backtracking.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from modflow6_gb300 import _lib
+from modflow6_gb300.dis import make_config
+from modflow6_gb300.ims import ImsLinear, ImsLinearSettings
+from modflow6_gb300.solution import GwfSolution, Nonlinear
+from test_gpu_ims import (assert_closure_parity, c1_system, gpu_ims, iters_close,
+                          oracle_iteration_spread, oracle_solve, tight_solution)
+from test_oracle_known_answers import newton01_model
+
+pytestmark = pytest.mark.gpu
+
+# (PRECONDITIONER_LEVELS, DROP_TOLERANCE, RELAXATION_FACTOR)
+FACTOR_CASES = [(5, 1e-4, 0.0), (5, 1e-4, 0.97), (1, 0.0, 0.0), (10, 1e-4, 0.0),
+                (0, 1e-3, 0.0), (3, 0.0, 0.0), (7, 1e-6, 1.0)]
+
+
+def gpu_factor(ims, amat):
+    retries = C.c_int(-1)
+    rc = _lib.load().gbims_factor(ims._h, _lib.dptr(amat), C.byref(retries))
+    assert rc >= 0, rc
+    return retries.value
+
+
+@pytest.mark.parametrize("isym", [True, False], ids=["sym", "nonsym"])
+@pytest.mark.parametrize("level,droptol,relax", FACTOR_CASES)
+def test_ilut_factor_bitexact(gblib, level, droptol, relax, isym):
+    con, amat, rhs, x0 = c1_system(isym=isym)
+    ims = gpu_ims(con, level=level, droptol=droptol, relax=relax)
+    retries = gpu_factor(ims, amat)
+    iapc, japc, apc = ims.get_factor()
+    io, jo, ao, ro = oracle.ilut(con["ia"], con["ja"], amat, level, droptol, relax)
+    assert retries == ro
+    np.testing.assert_array_equal(iapc, io)
+    np.testing.assert_array_equal(japc, jo)
+    np.testing.assert_array_equal(apc, ao)
+    # the caps: at most lfil L and lfil - 1 U entries per row
+    n = con["nodes"]
+    assert np.all(japc[:n] - iapc[:-1] <= level)
+    assert np.all(iapc[1:] - japc[:n] <= max(level - 1, 0))
+
+
+@pytest.mark.parametrize("relax", [0.0, 1.0])
+def test_ilut_pivot_retry_matches_oracle(gblib, relax):
+    # row 1 of [[1,1,0],[1,1,1],[0,1,3]] eliminates to a zero pivot: the
+    # pivot guard of ilut (izero / delta) retries with a growing delta
+    ia = np.array([0, 2, 5, 7], np.int32)
+    ja = np.array([0, 1, 1, 0, 2, 2, 1], np.int32)
+    amat = np.array([1.0, 1.0, 1.0, 1.0, 1.0, 3.0, 1.0])
+    ims = ImsLinear(ImsLinearSettings(level=2, droptol=0.0, relax=relax)).imslinear_allocate(3, ia, ja)
+    retries = gpu_factor(ims, amat)
+    iapc, japc, apc = ims.get_factor()
+    io, jo, ao, ro = oracle.ilut(ia, ja, amat, 2, 0.0, relax)
+    assert retries == ro and ro > 0
+    np.testing.assert_array_equal(iapc, io)
+    np.testing.assert_array_equal(japc, jo)
+    np.testing.assert_array_equal(apc, ao)
+
+
+def test_ilut_precondition_bitexact(gblib):
+    con, amat, rhs, x0 = c1_system()
+    ims = gpu_ims(con, level=5, droptol=1e-4)
+    gpu_factor(ims, amat)
+    iapc, japc, apc = ims.get_factor()
+    v = np.random.default_rng(0).standard_normal(con["nodes"])
+    z = np.zeros_like(v)
+    assert gblib.gbims_precondition(ims._h, _lib.dptr(v), _lib.dptr(z)) == 0
+    np.testing.assert_array_equal(z, oracle.ilu0a(apc, iapc, japc, v, fma=True))
+
+
+SOLVE_CASES = [dict(level=5, droptol=1e-4, north=2),
+               dict(level=3, droptol=1e-3, relax=0.97),
+               dict(level=10, droptol=1e-5),
+               dict(level=5, droptol=1e-4, iscl=1),
+               dict(level=5, droptol=1e-4, iscl=2)]
+
+
+@pytest.mark.parametrize("kw", SOLVE_CASES, ids=lambda k: "-".join(f"{a}{b}" for a, b in k.items()))
+def test_ilut_bicgstab_parity_c1(gblib, kw):
+    """BiCGSTAB, the accelerator the COMPLEX preset pairs with ILUT."""
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=500, ilinmeth=2)
+    con, amat, rhs, x0 = c1_system(isym=False)
+    xo, icnvg_o, it_o, _ = oracle_solve(con, amat, rhs, x0, **tol, **kw)
+    ims = gpu_ims(con, **tol, **kw)
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.icnvg == icnvg_o == 1
+    lo, hi = oracle_iteration_spread(con, amat, rhs, x0, **tol, **kw)
+    assert lo - 3 <= r.in_iter <= hi + 3 or iters_close(r.in_iter, it_o), (r.in_iter, lo, hi)
+    assert_closure_parity(x, xo, tight_solution(con, amat, rhs, x0, 2), tol["dvclose"], False)
+
+
+def test_ilut_pcg_parity_c1(gblib):
+    """PCG with ILUT.  ILUT drops L and U terms by different rules, so its
+    factor is not symmetric and PCG stalls short of tight closures (the
+    oracle stays near rmax 1e-2 after 500 iterations on this system, as the
+    reference's PCG would); at a closure it reaches, GPU and oracle agree."""
+    tol = dict(dvclose=1e-3, rclose=2e-2, iter1=500, ilinmeth=1, level=5, droptol=1e-4)
+    con, amat, rhs, x0 = c1_system()
+    xo, icnvg_o, it_o, _ = oracle_solve(con, amat, rhs, x0, **tol)
+    ims = gpu_ims(con, **tol)
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.icnvg == icnvg_o == 1
+    assert iters_close(r.in_iter, it_o), (r.in_iter, it_o)
+    assert_closure_parity(x, xo, tight_solution(con, amat, rhs, x0, 1), tol["dvclose"], False)
+
+
+def test_ilut_mixed_precision_closure(gblib):
+    """FP32 ILUT factors and inner vectors inside FP64 refinement reach the
+    FP64 closure."""
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=1000, ilinmeth=2)
+    con, amat, rhs, x0 = c1_system(isym=False)
+    xo, icnvg_o, it_o, _ = oracle_solve(con, amat, rhs, x0, level=5, droptol=1e-4, **tol)
+    ims = gpu_ims(con, level=5, droptol=1e-4, precision=_lib.GBIMS_MIXED, **tol)
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.icnvg == 1
+    resid = rhs - oracle.amux(con["ia"], con["ja"], amat, x)
+    assert np.max(np.abs(resid)) <= tol["rclose"] * 1.0001
+    assert_closure_parity(x, xo, tight_solution(con, amat, rhs, x0, 2), tol["dvclose"], False)
+
+
+def test_newton01_complex_preset_gpu(gblib):
+    """autotest/test_gwf_newton01.py:95-103 with the reference's own solver
+    configuration (COMPLEXITY COMPLEX: BiCGSTAB + ILUT 5 / 1e-4, NORTH 2, DBD,
+    backtracking) on the device-resident solution."""
+    m = newton01_model()
+    ims = ImsLinearSettings(dvclose=1e-9, rclose=0.1, iter1=500, ilinmeth=2, north=2, level=5,
+                            droptol=1e-4)
+    sol = GwfSolution(m, ims, Nonlinear.preset("COMPLEX", dvclose=1e-9))
+    st = sol.timestep(1, 1, 1.0)
+    assert st["converged"] == 1
+    x = sol.heads
+    assert np.isclose(x[4], 8.0), x[4]
+    assert np.isclose(x[13], 7.0), x[13]
+    sol.close()
+
+
+def test_ilut_transient_newton_matches_oracle(gblib):
+    """Three transient Newton steps (c3 grid at 20 x 20 x 5) with BiCGSTAB +
+    ILUT and the COMPLEX preset's outer options, oracle and GPU."""
+    m = make_config("c3", seed=1, scale=0.04)
+    m.wel_q = m.wel_q * 0.2
+    tol = dict(dvclose=1e-6, rclose=1e-3, iter1=500, ilinmeth=2, north=2, level=5, droptol=1e-4)
+    g = oracle.Gwf(m, oracle.settings(**tol))
+    nl = Nonlinear(dvclose=1e-5, mxiter=100, nonmeth=3, theta=0.8, akappa=1e-4, gamma=0.0,
+                   numtrack=20, btol=1.05, breduc=0.1, res_lim=0.002)
+    sol = GwfSolution(m, ImsLinearSettings(**tol), nl)
+    delt = 10.0
+    for kstp in range(1, 4):
+        so = g.timestep(kper=1, kstp=kstp, delt=delt, transient=True, dvclose=nl.dvclose,
+                        mxiter=nl.mxiter, nonmeth=nl.nonmeth, theta=nl.theta, akappa=nl.akappa,
+                        gamma=nl.gamma, amomentum=nl.amomentum, numtrack=nl.numtrack,
+                        btol=nl.btol, breduc=nl.breduc, res_lim=nl.res_lim)
+        sg = sol.timestep(1, kstp, delt)
+        assert so["converged"] == 1 and sg["converged"] == 1, (so, sg)
+        assert abs(sg["outer"] - so["outer"]) <= 3, (sg, so)
+        delt *= 1.2
+    assert np.max(np.abs(sol.heads - g.x)) <= 1e-4
+    sol.close()
+
+
+def test_ilut_rejected_in_batches(gblib):
+    from modflow6_gb300.ensemble import EnsembleLinear
+    ia = np.array([0, 1, 2], np.int32)
+    ja = np.array([0, 1], np.int32)
+    with pytest.raises(_lib.GbimsError) as e:
+        EnsembleLinear(ImsLinearSettings(level=5, droptol=1e-4)).allocate(
+            np.array([0, 1, 2], np.int32), ia, ja)
+    assert e.value.status == _lib.GBIMS_ERR_UNSUPPORTED

@@ -6,7 +6,7 @@
 * autotest/test_gwf_newton01.py:8-103: 2x3x3 convertible Newton model, CHD 7
   in layer 2, recharge 1 on layer 1; answers H1 = 8.0 at (0,1,1) and
   H2 = 7.0 at (1,1,1) (:95-103).  The reference runs COMPLEXITY COMPLEX
-  (BiCGSTAB + ILUT); the IMS path built here is ILU0, so the case is run with
+  (BiCGSTAB + ILUT, backtracking); the case is run both that way and with
   PRECONDITIONER_LEVELS 0 / DROP_TOLERANCE 0 (BiCGSTAB + ILU0), which must
   reach the same heads.
 """
@@ -68,6 +68,27 @@ def test_newton01_h1_h2():
     st = g.timestep(kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-9, mxiter=100,
                     nonmeth=3, theta=0.8, akappa=1e-4, gamma=0.0, amomentum=0.0)
     assert st["converged"] == 1
+    h1 = g.x[0 * 9 + 1 * 3 + 1]
+    h2 = g.x[1 * 9 + 1 * 3 + 1]
+    assert np.isclose(h1, 8.0), h1
+    assert np.isclose(h2, 7.0), h2
+
+
+def test_newton01_h1_h2_complex_preset():
+    """The reference's own configuration: COMPLEXITY COMPLEX as a whole
+    (ImsLinearSettings.f90:100-111 -- BiCGSTAB, ILUT with PRECONDITIONER_LEVELS
+    5 and DROP_TOLERANCE 1e-4, NORTH 2; sln_setouter
+    NumericalSolution.f90:2657-2669 -- DBD under-relaxation and backtracking)
+    with the test's INNER/OUTER_DVCLOSE 1e-9."""
+    m = newton01_model()
+    s = oracle.settings(dvclose=1e-9, rclose=0.1, iter1=500, ilinmeth=2, north=2, level=5,
+                        droptol=1e-4)
+    g = oracle.Gwf(m, s)
+    st = g.timestep(kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-9, mxiter=100,
+                    nonmeth=3, theta=0.8, akappa=1e-4, gamma=0.0, amomentum=0.0,
+                    numtrack=20, btol=1.05, breduc=0.1, res_lim=0.002)
+    assert st["converged"] == 1
+    assert g.ims.lib.or_ims_ipc(g.ims.h) == 3
     h1 = g.x[0 * 9 + 1 * 3 + 1]
     h2 = g.x[1 * 9 + 1 * 3 + 1]
     assert np.isclose(h1, 8.0), h1
