@@ -439,7 +439,11 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
     int maxrow = 0;
     for (int r = 0; r < neq; ++r) maxrow = std::max(maxrow, h->ia[r + 1] - h->ia[r]);
     h->ilut_iwk = s->level > 0 ? (long long)neq * (2LL * s->level + 1) : (long long)neq * maxrow;
+    // until the first factorisation: no L or U entries in any row
     h->japc.assign((size_t)ilut_cap, 0);
+    h->iapc.assign(neq + 1, neq + 1);
+    for (int r = 0; r < neq; ++r) h->japc[r] = neq + 1;
+    h->njapc = neq + 1;
     h->I.n = neq;
     h->I.lfil = s->level;
     h->I.sl = (int)sl;
@@ -459,7 +463,7 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   GB_CUDA(h, cudaMemcpy(h->d_ia, h->ia.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemcpy(h->d_ja, h->ja.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemcpy(h->d_iapc, h->iapc.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
-  GB_CUDA(h, cudaMemcpy(h->d_japc, h->japc.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
+  GB_CUDA(h, cudaMemcpy(h->d_japc, h->japc.data(), sizeof(int) * h->njapc, cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemset(h->d_apc, 0, sizeof(double) * npc));
   if (h->ipc >= 3) {
     IlutDev &I = h->I;
@@ -1137,8 +1141,8 @@ extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times 
   double vb = h->mixed ? 4.0 : 8.0;
   t->spmv_bytes = h->dia_spmv ? vb * h->nja + 2.0 * vb * n
                               : (vb + 4.0) * h->nja + 4.0 * (n + 1) + 2.0 * vb * n;
-  t->precond_bytes = vb * h->nja + 2.0 * vb * n;
-  if (!h->structured) t->precond_bytes += 4.0 * h->nja + 4.0 * (n + 1);
+  t->precond_bytes = vb * h->njapc + 2.0 * vb * n;
+  if (!h->structured) t->precond_bytes += 4.0 * h->njapc + 4.0 * (n + 1);
   return GBIMS_OK;
 }
 

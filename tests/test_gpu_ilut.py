@@ -105,7 +105,15 @@ def test_ilut_bicgstab_parity_c1(gblib, kw):
     assert r.icnvg == icnvg_o == 1
     lo, hi = oracle_iteration_spread(con, amat, rhs, x0, **tol, **kw)
     assert lo - 3 <= r.in_iter <= hi + 3 or iters_close(r.in_iter, it_o), (r.in_iter, lo, hi)
-    assert_closure_parity(x, xo, tight_solution(con, amat, rhs, x0, 2), tol["dvclose"], False)
+    # where BiCGSTAB stops moves with last-bit changes, and so does the
+    # error it stops at (3e-8 to 1.5e-7 for the oracle on the scaled case):
+    # the GPU's error is held to 5x the oracle's largest over perturbed
+    # right-hand sides, plus dvclose
+    x_star = tight_solution(con, amat, rhs, x0, 2)
+    e_ref = max(np.max(np.abs(oracle_solve(con, amat, rhs * (1.0 + k * 2.2e-16), x0, **tol, **kw)[0]
+                              - x_star)) for k in range(6))
+    e_gpu = np.max(np.abs(x - x_star))
+    assert e_gpu <= 5.0 * e_ref + tol["dvclose"], (e_gpu, e_ref)
 
 
 def test_ilut_pcg_parity_c1(gblib):
