@@ -105,15 +105,20 @@ def test_ilut_bicgstab_parity_c1(gblib, kw):
     assert r.icnvg == icnvg_o == 1
     lo, hi = oracle_iteration_spread(con, amat, rhs, x0, **tol, **kw)
     assert lo - 3 <= r.in_iter <= hi + 3 or iters_close(r.in_iter, it_o), (r.in_iter, lo, hi)
-    # where BiCGSTAB stops moves with last-bit changes, and so does the
-    # error it stops at (3e-8 to 1.5e-7 for the oracle on the scaled case):
-    # the GPU's error is held to 5x the oracle's largest over perturbed
-    # right-hand sides, plus dvclose
+    assert_within_oracle_error_spread(x, con, amat, rhs, x0, **tol, **kw)
+
+
+def assert_within_oracle_error_spread(x, con, amat, rhs, x0, **kw):
+    """Where BiCGSTAB stops moves with last-bit changes of its inputs, and so
+    does the error it stops at (3e-8 to 2.6e-7 for the oracle with ILUT on
+    c1 over right-hand sides perturbed by k x 2.2e-16, k = 0..7).  The GPU's
+    error against a tightly converged solution is held to 5x the oracle's
+    largest over those runs, plus dvclose."""
     x_star = tight_solution(con, amat, rhs, x0, 2)
-    e_ref = max(np.max(np.abs(oracle_solve(con, amat, rhs * (1.0 + k * 2.2e-16), x0, **tol, **kw)[0]
-                              - x_star)) for k in range(6))
+    e_ref = max(np.max(np.abs(oracle_solve(con, amat, rhs * (1.0 + k * 2.2e-16), x0, **kw)[0]
+                              - x_star)) for k in range(8))
     e_gpu = np.max(np.abs(x - x_star))
-    assert e_gpu <= 5.0 * e_ref + tol["dvclose"], (e_gpu, e_ref)
+    assert e_gpu <= 5.0 * e_ref + kw["dvclose"], (e_gpu, e_ref)
 
 
 def test_ilut_pcg_parity_c1(gblib):
@@ -137,14 +142,13 @@ def test_ilut_mixed_precision_closure(gblib):
     FP64 closure."""
     tol = dict(dvclose=1e-8, rclose=1e-6, iter1=1000, ilinmeth=2)
     con, amat, rhs, x0 = c1_system(isym=False)
-    xo, icnvg_o, it_o, _ = oracle_solve(con, amat, rhs, x0, level=5, droptol=1e-4, **tol)
     ims = gpu_ims(con, level=5, droptol=1e-4, precision=_lib.GBIMS_MIXED, **tol)
     x = x0.copy()
     r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
     assert r.icnvg == 1
     resid = rhs - oracle.amux(con["ia"], con["ja"], amat, x)
     assert np.max(np.abs(resid)) <= tol["rclose"] * 1.0001
-    assert_closure_parity(x, xo, tight_solution(con, amat, rhs, x0, 2), tol["dvclose"], False)
+    assert_within_oracle_error_spread(x, con, amat, rhs, x0, level=5, droptol=1e-4, **tol)
 
 
 def test_newton01_complex_preset_gpu(gblib):
