@@ -568,7 +568,9 @@ void or_scale(int iopt, int iscl, int neq, int nja, const int *ia, const int *ja
   }
 }
 
-/* ImsLinearBase.f90:30-240, ims_base_cg (single model, IPC 1/2). */
+/* ImsLinearBase.f90:30-240, ims_base_cg (single model).  The preconditioner
+ * is applied by or_ilu0a for every IPC: ilu0a for ILU0/MILU0 and lusol for
+ * ILUT/MILUT are the same sweeps over the IAPC/JAPC/APC storage. */
 static void or_cg(int *icnvg, int itmax, int *innerit, int neq, int nja, int icnvgopt,
                   int north, double dvclose, double rclose, double l2norm0,
                   double epfact, const int *ia0, const int *ja0, const double *a0,
@@ -630,7 +632,7 @@ static void or_cg(int *icnvg, int itmax, int *innerit, int neq, int nja, int icn
   if (*icnvg < 0) *icnvg = 0;
 }
 
-/* ImsLinearBase.f90:249-549, ims_base_bcgs (single model, IPC 1/2). */
+/* ImsLinearBase.f90:249-549, ims_base_bcgs (single model, every IPC). */
 static void or_bcgs(int *icnvg, int itmax, int *innerit, int neq, int nja, int icnvgopt,
                     int north, int iscl, const double *dscale, double dvclose,
                     double rclose, double l2norm0, double epfact, const int *ia0,
@@ -707,7 +709,8 @@ static void or_bcgs(int *icnvg, int itmax, int *innerit, int neq, int nja, int i
 }
 
 /* ImsLinear.f90:111-339 (imslinear_ar, the parts that do not read files):
- * choose IPC (:178-185) and build IAPC/JAPC (:267-270). */
+ * choose IPC (:178-185), build IAPC/JAPC for ILU0/MILU0 (:244-248) or size
+ * the ILUT storage (ims_calc_pcdims, :227-228). */
 struct or_ims {
   or_ims_settings s;
   int neq, nja, ipc;
