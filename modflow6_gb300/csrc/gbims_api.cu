@@ -62,6 +62,14 @@ struct gbims_handle {
   IlutStatus *h_ilut = nullptr;
   long long ilut_iwk = 0;
   int njapc = 0;
+  // REORDERING_METHOD RCM: the solve runs on the permuted system (A0, IA0,
+  // JA0 of imslinear_ap); callers' arrays, the scaling and the unscaling
+  // stay in the model's numbering (u_*), gathered in and out at each apply
+  bool reorder = false;
+  std::vector<int> lorder, ia_u, ja_u, asrc;
+  int *d_lorder = nullptr, *d_iorder = nullptr, *d_asrc = nullptr;
+  int *d_ia_u = nullptr, *d_ja_u = nullptr;
+  double *u_amat = nullptr, *u_rhs = nullptr, *u_x = nullptr;
   // batched ensemble (nm > 0): members concatenated into one block-diagonal
   // system, one control block per member, the handle's Ctl = all done
   int nm = 0;
@@ -378,7 +386,12 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   if (s->relax < 0.0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RELAX MUST BE >= 0.0"); }
   if (s->relax > 1.0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RELAX MUST BE <= 1.0"); }
   if (s->level < 0) { *out = h; return fail(h, GBIMS_ERR_ARG, "ILUT: PRECONDITIONER_LEVELS must be >= 0"); }
-  if (s->iord != 0) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "REORDERING_METHOD RCM/MD is not supported"); }
+  if (s->iord == 2) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "REORDERING_METHOD MD is not supported"); }
+  // With ILU0/MILU0 the reference factors the permuted matrix against the
+  // IAPC/JAPC of the unpermuted pattern (built at ImsLinear.f90:244-248,
+  // before the ordering at :333-336), carrying work-vector entries from row
+  // to row; that combination is declined rather than changed.
+  if (s->iord == 1 && h->ipc < 3) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "REORDERING_METHOD RCM is supported with ILUT/MILUT only (PRECONDITIONER_LEVELS or DROP_TOLERANCE > 0)"); }
   if (s->precision != GBIMS_FP64 && s->precision != GBIMS_MIXED) { *out = h; return fail(h, GBIMS_ERR_ARG, "precision must be GBIMS_FP64 or GBIMS_MIXED"); }
   h->mixed = (s->precision == GBIMS_MIXED);
   h->bcgs = (s->ilinmeth == 2);
@@ -405,6 +418,31 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
     if (h->ia[r + 1] - h->ia[r] > kMaxRowLen) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "CSR row longer than 64 entries"); }
     for (int k = h->ia[r]; k < h->ia[r + 1]; ++k)
       if (h->ja[k] < 0 || h->ja[k] >= neq) { *out = h; return fail(h, GBIMS_ERR_ARG, "column index out of range"); }
+  }
+  // REORDERING_METHOD RCM: LORDER (ims_base_calc_order) and the permuted
+  // pattern of dperm with job 1 (sparsekit.f90:249-447): row j becomes row
+  // LORDER(j), its entries kept in order, columns relabelled by LORDER --
+  // LORDER is the numbering's list of nodes, used as a new-index map, as
+  // imslinear_ap passes it (ImsLinear.f90:653-658)
+  if (s->iord == 1) {
+    h->reorder = true;
+    rcm_order(neq, h->ia, h->ja, h->lorder);
+    h->ia_u = h->ia;
+    h->ja_u = h->ja;
+    std::vector<int> iaro(neq + 1, 0), jaro(nja);
+    h->asrc.assign(nja, 0);
+    for (int j = 0; j < neq; ++j) iaro[h->lorder[j] + 1] = h->ia_u[j + 1] - h->ia_u[j];
+    for (int j = 0; j < neq; ++j) iaro[j + 1] += iaro[j];
+    for (int r = 0; r < neq; ++r) {
+      int ko = iaro[h->lorder[r]];
+      for (int k = h->ia_u[r]; k < h->ia_u[r + 1]; ++k) {
+        jaro[ko] = h->lorder[h->ja_u[k]];
+        h->asrc[ko] = k;
+        ++ko;
+      }
+    }
+    h->ia = iaro;
+    h->ja = jaro;
   }
   // ims_base_pccrs (ImsLinearBase.f90:1207-1261)
   h->iapc.assign(neq + 1, 0);
@@ -462,6 +500,23 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   GB_CUDA(h, dalloc(&h->d_apc, npc));
   GB_CUDA(h, cudaMemcpy(h->d_ia, h->ia.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemcpy(h->d_ja, h->ja.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
+  if (h->reorder) {
+    std::vector<int> iorder(neq);
+    for (int j = 0; j < neq; ++j) iorder[h->lorder[j]] = j;
+    GB_CUDA(h, dalloc(&h->d_lorder, neq));
+    GB_CUDA(h, dalloc(&h->d_iorder, neq));
+    GB_CUDA(h, dalloc(&h->d_asrc, nja));
+    GB_CUDA(h, dalloc(&h->d_ia_u, neq + 1));
+    GB_CUDA(h, dalloc(&h->d_ja_u, nja));
+    GB_CUDA(h, cudaMemcpy(h->d_lorder, h->lorder.data(), sizeof(int) * neq, cudaMemcpyHostToDevice));
+    GB_CUDA(h, cudaMemcpy(h->d_iorder, iorder.data(), sizeof(int) * neq, cudaMemcpyHostToDevice));
+    GB_CUDA(h, cudaMemcpy(h->d_asrc, h->asrc.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
+    GB_CUDA(h, cudaMemcpy(h->d_ia_u, h->ia_u.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
+    GB_CUDA(h, cudaMemcpy(h->d_ja_u, h->ja_u.data(), sizeof(int) * nja, cudaMemcpyHostToDevice));
+    GB_CUDA(h, dalloc(&h->u_amat, nja));
+    GB_CUDA(h, dalloc(&h->u_rhs, (size_t)neq + kVecPad));
+    GB_CUDA(h, dalloc(&h->u_x, (size_t)neq + kVecPad));
+  }
   GB_CUDA(h, cudaMemcpy(h->d_iapc, h->iapc.data(), sizeof(int) * (neq + 1), cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemcpy(h->d_japc, h->japc.data(), sizeof(int) * h->njapc, cudaMemcpyHostToDevice));
   GB_CUDA(h, cudaMemset(h->d_apc, 0, sizeof(double) * npc));
@@ -549,7 +604,9 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
     GB_CUDA(h, dalloc(&h->d_dscale2, nn));
     if (s->iscl == 2) {
       std::vector<int> cptr, cpos;
-      scale_colmap_host(neq, h->ia, h->ja, cptr, cpos);
+      // the scaling works in the model's numbering
+      scale_colmap_host(neq, h->reorder ? h->ia_u : h->ia, h->reorder ? h->ja_u : h->ja, cptr,
+                        cpos);
       GB_CUDA(h, dalloc(&h->d_cptr, cptr.size()));
       GB_CUDA(h, dalloc(&h->d_cpos, cpos.size()));
       GB_CUDA(h, cudaMemcpy(h->d_cptr, cptr.data(), sizeof(int) * cptr.size(), cudaMemcpyHostToDevice));
@@ -574,6 +631,33 @@ static double epfact_of(int icnvgopt, int kstp) {
   if (icnvgopt == 2) return (kstp == 1) ? (double)0.01f : (double)0.10f;
   if (icnvgopt == 4) return 1.0e-4;
   return 1.0;
+}
+
+// dst[i] = src[idx[i]]: the permutations of REORDERING_METHOD RCM (dperm and
+// dvperm of sparsekit, as gathers)
+__global__ void k_gather(int n, const int *__restrict__ idx, const double *__restrict__ src,
+                         double *__restrict__ dst) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    dst[i] = src[idx[i]];
+}
+
+static void gather(gbims_handle *h, int n, const int *idx, const double *src, double *dst) {
+  const int g = std::max(1, std::min(8 * kNumSM, (n + 255) / 256));
+  k_gather<<<g, 256, 0, h->st>>>(n, idx, src, dst);
+  h->launches += 1;
+}
+
+// The arrays a caller fills and reads back: the model's numbering.
+static double *in_amat(gbims_handle *h) { return h->reorder ? h->u_amat : h->d_amat; }
+static double *in_rhs(gbims_handle *h) { return h->reorder ? h->u_rhs : h->d_rhs; }
+static double *in_x(gbims_handle *h) { return h->reorder ? h->u_x : h->d_x; }
+
+// PERMUTE ROWS, COLUMNS, AND RHS (ImsLinear.f90:652-666): AMAT by dperm,
+// X and RHS by dvperm with LORDER (x0[LORDER(j)] = x[j]).
+static void permute_in(gbims_handle *h) {
+  gather(h, h->nja, h->d_asrc, h->u_amat, h->d_amat);
+  gather(h, h->n, h->d_iorder, h->u_x, h->d_x);
+  gather(h, h->n, h->d_iorder, h->u_rhs, h->d_rhs);
 }
 
 __global__ void k_zero_vec(int n, double *a, double *b, double *c, double *d) {
@@ -735,10 +819,14 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
   cudaStream_t st = h->st;
   (void)kiter;
   GB_CUDA(h, cudaEventRecord(h->ev0, st));
-  // SCALE PROBLEM (ImsLinear.f90:644-650)
+  // SCALE PROBLEM (ImsLinear.f90:644-650), in the model's numbering
   if (h->s.iscl != 0)
-    h->launches += launch_scale(h->s.iscl, n, h->d_ia, h->d_ja, h->d_cptr, h->d_cpos, h->d_amat,
-                                h->d_x, h->d_rhs, h->d_dscale, h->d_dscale2, st);
+    h->launches += launch_scale(h->s.iscl, n, h->reorder ? h->d_ia_u : h->d_ia,
+                                h->reorder ? h->d_ja_u : h->d_ja, h->d_cptr, h->d_cpos,
+                                in_amat(h), in_x(h), in_rhs(h), h->d_dscale, h->d_dscale2, st);
+  // PERMUTE (:652-666); BiCGSTAB reads DSCALE in the model's numbering at
+  // the permuted row index, as the reference does
+  if (h->reorder) permute_in(h);
   int icount = factor_core(h);
   if (icount < 0) return icount;
   // control block
@@ -788,10 +876,13 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
       batch = std::min(batch * 2, 32);
     }
   }
-  // UNSCALE the solution (ImsLinear.f90:739-745); amat and rhs are the
-  // handle's own copies and are refilled by the next apply
+  // BACK PERMUTE the solution (ImsLinear.f90:730-737: dvperm with IORDER,
+  // x[j] = x0[LORDER(j)]); amat and rhs are the handle's own copies and are
+  // refilled by the next apply
+  if (h->reorder) gather(h, n, h->d_lorder, h->d_x, h->u_x);
+  // UNSCALE the solution (ImsLinear.f90:739-745)
   if (h->s.iscl != 0) {
-    launch_unscale_x(n, h->d_x, h->d_dscale2, st);
+    launch_unscale_x(n, in_x(h), h->d_dscale2, st);
     h->launches += 1;
   }
   GB_CUDA(h, cudaEventRecord(h->ev1, st));
@@ -837,12 +928,12 @@ extern "C" int gbims_apply(gbims_handle *h, double *amat, double *rhs, double *x
   if (!h || !amat || !rhs || !x || !icnvg || !in_iter) return GBIMS_ERR_ARG;
   if (!h->d_ctl) return fail(h, GBIMS_ERR_STATE, "handle was not created successfully");
   if (h->nm > 0) return fail(h, GBIMS_ERR_STATE, "batch handle: use gbims_batch_apply");
-  GB_CUDA(h, cudaMemcpyAsync(h->d_amat, amat, sizeof(double) * h->nja, cudaMemcpyHostToDevice, h->st));
-  GB_CUDA(h, cudaMemcpyAsync(h->d_rhs, rhs, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
-  GB_CUDA(h, cudaMemcpyAsync(h->d_x, x, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(in_amat(h), amat, sizeof(double) * h->nja, cudaMemcpyHostToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(in_rhs(h), rhs, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(in_x(h), x, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->st));
   int rc = apply_core(h, kstp, kiter, icnvg, in_iter, summary);
   if (rc < 0 && rc != GBIMS_ERR_NONFINITE) return rc;
-  cudaError_t e = cudaMemcpy(x, h->d_x, sizeof(double) * h->n, cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpy(x, in_x(h), sizeof(double) * h->n, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return fail(h, GBIMS_ERR_CUDA, cudaGetErrorString(e));
   return rc;
 }
@@ -853,12 +944,12 @@ extern "C" int gbims_apply_device(gbims_handle *h, double *d_amat, double *d_rhs
   if (!h || !d_amat || !d_rhs || !d_x || !icnvg || !in_iter) return GBIMS_ERR_ARG;
   if (!h->d_ctl) return fail(h, GBIMS_ERR_STATE, "handle was not created successfully");
   if (h->nm > 0) return fail(h, GBIMS_ERR_STATE, "batch handle: use gbims_batch_apply_device");
-  GB_CUDA(h, cudaMemcpyAsync(h->d_amat, d_amat, sizeof(double) * h->nja, cudaMemcpyDeviceToDevice, h->st));
-  GB_CUDA(h, cudaMemcpyAsync(h->d_rhs, d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
-  GB_CUDA(h, cudaMemcpyAsync(h->d_x, d_x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(in_amat(h), d_amat, sizeof(double) * h->nja, cudaMemcpyDeviceToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(in_rhs(h), d_rhs, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(in_x(h), d_x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
   int rc = apply_core(h, kstp, kiter, icnvg, in_iter, summary);
   if (rc < 0 && rc != GBIMS_ERR_NONFINITE) return rc;
-  cudaError_t e = cudaMemcpyAsync(d_x, h->d_x, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st);
+  cudaError_t e = cudaMemcpyAsync(d_x, in_x(h), sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   if (e != cudaSuccess) return fail(h, GBIMS_ERR_CUDA, cudaGetErrorString(e));
   return rc;
@@ -867,7 +958,8 @@ extern "C" int gbims_apply_device(gbims_handle *h, double *d_amat, double *d_rhs
 extern "C" int gbims_factor(gbims_handle *h, const double *amat, int *pivot_retries) {
   if (!h || !amat) return GBIMS_ERR_ARG;
   if (!h->d_ctl) return fail(h, GBIMS_ERR_STATE, "handle was not created successfully");
-  GB_CUDA(h, cudaMemcpyAsync(h->d_amat, amat, sizeof(double) * h->nja, cudaMemcpyHostToDevice, h->st));
+  GB_CUDA(h, cudaMemcpyAsync(in_amat(h), amat, sizeof(double) * h->nja, cudaMemcpyHostToDevice, h->st));
+  if (h->reorder) gather(h, h->nja, h->d_asrc, h->u_amat, h->d_amat);  // factor the permuted matrix
   int icount = factor_core(h);
   if (icount < 0) return icount;
   GB_CUDA(h, cudaStreamSynchronize(h->st));
@@ -881,6 +973,28 @@ extern "C" int gbims_get_apc(gbims_handle *h, double *apc) {
   GB_CUDA(h, cudaStreamSynchronize(h->st));
   if (h->ipc >= 3) return fail(h, GBIMS_ERR_STATE, "ILUT: the factor's pattern varies; use gbims_get_factor");
   GB_CUDA(h, cudaMemcpy(apc, h->d_apc, sizeof(double) * h->nja, cudaMemcpyDeviceToHost));
+  return GBIMS_OK;
+}
+
+extern "C" int gbims_calc_order(int iord, int neq, int nja, const int *ia, const int *ja,
+                                int index_base, int *lorder, int *iorder) {
+  if (neq <= 0 || nja < neq || !ia || !ja || !lorder || !iorder) return GBIMS_ERR_ARG;
+  if (iord != 1) return GBIMS_ERR_UNSUPPORTED;
+  const int base = index_base ? 1 : 0;
+  std::vector<int> a(neq + 1), c(nja), lo;
+  for (int i = 0; i <= neq; ++i) a[i] = ia[i] - base;
+  if (a[0] != 0 || a[neq] != nja) return GBIMS_ERR_ARG;
+  for (int r = 0; r < neq; ++r)
+    if (a[r + 1] < a[r]) return GBIMS_ERR_ARG;
+  for (int k = 0; k < nja; ++k) {
+    c[k] = ja[k] - base;
+    if (c[k] < 0 || c[k] >= neq) return GBIMS_ERR_ARG;
+  }
+  rcm_order(neq, a, c, lo);
+  for (int i = 0; i < neq; ++i) {
+    lorder[i] = lo[i] + base;
+    iorder[lo[i]] = i + base;
+  }
   return GBIMS_OK;
 }
 
@@ -1163,7 +1277,8 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->d_bcm, h->d_bcr, h->d_bmc, h->d_bmr, h->d_ctls, h->D.d_geo, h->S.d_slm,
                   h->LW.fwd, h->LW.bwd, h->LW.ticket, h->LW.err, h->d_ctl, h->I.lcol,
                   h->I.lval, h->I.ucol, h->I.uval, h->I.nl, h->I.nu, h->I.dinv, h->I.rdone,
-                  h->I.stat};
+                  h->I.stat, h->d_lorder, h->d_iorder, h->d_asrc, h->d_ia_u, h->d_ja_u,
+                  h->u_amat, h->u_rhs, h->u_x};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
@@ -1435,9 +1550,9 @@ extern "C" int gbims_batch_apply_device(gbims_handle *h, double *d_amat, double 
 // assembles straight into the IMS handle's amat/rhs and keeps x there.
 namespace gb {
 void ims_buffers(gbims_handle *h, double **amat, double **rhs, double **x) {
-  *amat = h->d_amat;
-  *rhs = h->d_rhs;
-  *x = h->d_x;
+  *amat = in_amat(h);
+  *rhs = in_rhs(h);
+  *x = in_x(h);
 }
 cudaStream_t ims_stream(gbims_handle *h) { return h->st; }
 int ims_apply_inplace(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_iter,

@@ -221,6 +221,10 @@ void launch_dia7_apply32(const Dia7 &D, const float *r, float *z, const Ctl *ctl
 
 void levels_build_host(int n, const std::vector<int> &iapc, const std::vector<int> &japc,
                        bool forward, Levels &L);
+// REORDERING_METHOD RCM (h_rcm.cu): lorder[i] is the i-th node (0-based) of
+// the numbering genrcm gives for the 0-based CSR pattern ia/ja.
+void rcm_order(int n, const std::vector<int> &ia, const std::vector<int> &ja,
+               std::vector<int> &lorder);
 void launch_ilu_factor(int n, const int *d_ia, const int *d_ja, const double *d_amat,
                        const int *d_iapc, const int *d_japc, double *d_apc,
                        const Levels &L, double relax, double delta, int ipcflag,

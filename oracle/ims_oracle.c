@@ -475,6 +475,208 @@ int or_pcu_ilut(int neq, int lfil, double droptol, double relax, const double *a
   return icount;
 }
 
+/* ---- REORDERING_METHOD RCM: rcm/rcm.f90 (George & Liu's GENRCM as
+ * vendored in the reference).  The routines below keep the reference's
+ * 1-based node numbers internally (arrays of n + 1, index 0 unused) so each
+ * loop bound reads as in the source; the caller converts at the edges.
+ * A separate visited array stands in for degree's sign flips of adj_row. */
+
+/* rcm.f90:853-1001, degree: component of root among mask != 0 and each
+ * node's count of neighbours with mask != 0 (its own diagonal included). */
+static void rcm_degree(int root, const int *ia, const int *ja, const int *mask, int *deg,
+                       int *iccsze, int *ls, char *vis) {
+  ls[1] = root;
+  vis[root] = 1;
+  int lvlend = 0, cc = 1;
+  for (;;) {
+    const int lbegin = lvlend + 1;
+    lvlend = cc;
+    for (int i = lbegin; i <= lvlend; ++i) {
+      const int node = ls[i];
+      int ideg = 0;
+      for (int j = ia[node]; j <= ia[node + 1] - 1; ++j) {
+        const int nbr = ja[j];
+        if (mask[nbr] != 0) {
+          ++ideg;
+          if (!vis[nbr]) {
+            vis[nbr] = 1;
+            ++cc;
+            ls[cc] = nbr;
+          }
+        }
+      }
+      deg[node] = ideg;
+    }
+    if (cc - lvlend == 0) break;
+  }
+  for (int i = 1; i <= cc; ++i) vis[ls[i]] = 0;
+  *iccsze = cc;
+}
+
+/* rcm.f90:2188-2330, level_set: the rooted level structure of root's
+ * component; mask is restored to 1 on the component on exit. */
+static void rcm_level_set(int root, const int *ia, const int *ja, int *mask, int *level_num,
+                          int *level_row, int *level) {
+  mask[root] = 0;
+  level[1] = root;
+  int nl = 0, lvlend = 0, cc = 1;
+  for (;;) {
+    const int lbegin = lvlend + 1;
+    lvlend = cc;
+    ++nl;
+    level_row[nl] = lbegin;
+    for (int i = lbegin; i <= lvlend; ++i) {
+      const int node = level[i];
+      for (int j = ia[node]; j <= ia[node + 1] - 1; ++j) {
+        const int nbr = ja[j];
+        if (mask[nbr] != 0) {
+          ++cc;
+          level[cc] = nbr;
+          mask[nbr] = 0;
+        }
+      }
+    }
+    if (cc - lvlend <= 0) break;
+  }
+  level_row[nl + 1] = lvlend + 1;
+  for (int i = 1; i <= cc; ++i) mask[level[i]] = 1;
+  *level_num = nl;
+}
+
+/* rcm.f90:3121-3316, root_find: a pseudo-peripheral node of root's
+ * component (the minimum-degree node of the last level, while the level
+ * structure keeps growing). */
+static void rcm_root_find(int *root, const int *ia, const int *ja, int *mask, int *level_row,
+                          int *level) {
+  int level_num, level_num2;
+  rcm_level_set(*root, ia, ja, mask, &level_num, level_row, level);
+  const int iccsze = level_row[level_num + 1] - 1;
+  if (level_num == 1 || level_num == iccsze) return;
+  for (;;) {
+    int mindeg = iccsze;
+    const int jstrt = level_row[level_num];
+    *root = level[jstrt];
+    if (jstrt < iccsze) {
+      for (int j = jstrt; j <= iccsze; ++j) {
+        const int node = level[j];
+        int ndeg = 0;
+        for (int k = ia[node]; k <= ia[node + 1] - 1; ++k)
+          if (0 < mask[ja[k]]) ++ndeg;
+        if (ndeg < mindeg) {
+          *root = node;
+          mindeg = ndeg;
+        }
+      }
+    }
+    rcm_level_set(*root, ia, ja, mask, &level_num2, level_row, level);
+    if (level_num2 <= level_num) break;
+    level_num = level_num2;
+    if (iccsze <= level_num) break;
+  }
+}
+
+/* rcm.f90:2899-3120, rcm: breadth-first numbering of root's component,
+ * each node's new neighbours ordered by increasing degree with the
+ * insertion sort of the vendored source (its inner loop stops above the
+ * first new neighbour), then reversed. */
+static void rcm_number(int root, const int *ia, const int *ja, int *mask, int *perm,
+                       int *iccsze, int *deg, char *vis) {
+  rcm_degree(root, ia, ja, mask, deg, iccsze, perm, vis);
+  mask[root] = 0;
+  const int cc = *iccsze;
+  if (cc == 1) return;
+  int lvlend = 0, lnbr = 1;
+  while (lvlend < lnbr) {
+    const int lbegin = lvlend + 1;
+    lvlend = lnbr;
+    for (int i = lbegin; i <= lvlend; ++i) {
+      const int node = perm[i];
+      const int fnbr = lnbr + 1;
+      for (int j = ia[node]; j <= ia[node + 1] - 1; ++j) {
+        const int nbr = ja[j];
+        if (mask[nbr] != 0) {
+          ++lnbr;
+          mask[nbr] = 0;
+          perm[lnbr] = nbr;
+        }
+      }
+      if (lnbr <= fnbr) continue;
+      int k = fnbr;
+      while (k < lnbr) {
+        int l = k;
+        ++k;
+        const int nbr = perm[k];
+        while (fnbr < l) {
+          const int lperm = perm[l];
+          if (deg[lperm] <= deg[nbr]) break;
+          perm[l + 1] = lperm;
+          --l;
+        }
+        perm[l + 1] = nbr;
+      }
+    }
+  }
+  for (int i = 1; i <= cc / 2; ++i) {
+    const int t = perm[i];
+    perm[i] = perm[cc + 1 - i];
+    perm[cc + 1 - i] = t;
+  }
+}
+
+/* rcm.f90:1003-1107, genrcm, on a 0-based CSR pattern (the diagonal
+ * included, as IMS passes it): lorder[i] (0-based) is the i-th node of the
+ * RCM numbering. */
+void or_genrcm(int n, const int *ia0, const int *ja0, int *lorder) {
+  const int nja = ia0[n];
+  int *ia = (int *)malloc(sizeof(int) * (n + 2));
+  int *ja = (int *)malloc(sizeof(int) * (nja + 1));
+  for (int i = 0; i <= n; ++i) ia[i + 1] = ia0[i] + 1;
+  for (int k = 0; k < nja; ++k) ja[k + 1] = ja0[k] + 1;
+  int *mask = (int *)malloc(sizeof(int) * (n + 1));
+  int *perm = (int *)calloc(n + 2, sizeof(int));
+  int *level_row = (int *)calloc(n + 2, sizeof(int));
+  int *level = (int *)calloc(n + 2, sizeof(int));
+  int *deg = (int *)calloc(n + 1, sizeof(int));
+  char *vis = (char *)calloc(n + 1, 1);
+  for (int i = 1; i <= n; ++i) mask[i] = 1;
+  int num = 1;
+  for (int i = 1; i <= n; ++i) {
+    if (mask[i] != 0) {
+      int root = i, iccsze = 0;
+      rcm_root_find(&root, ia, ja, mask, level_row, level);
+      rcm_number(root, ia, ja, mask, perm + num - 1, &iccsze, deg, vis);
+      num += iccsze;
+      if (n < num) break;
+    }
+  }
+  for (int i = 1; i <= n; ++i) lorder[i - 1] = perm[i] - 1;
+  free(ia); free(ja); free(mask); free(perm); free(level_row); free(level); free(deg); free(vis);
+}
+
+/* sparsekit.f90:353-447 (dperm with job 1: rperm then cperm with the same
+ * permutation) -- row j of A becomes row perm[j] of B, its entries in the
+ * same order, columns relabelled by perm -- and :61-161 (dvperm):
+ * y[perm[j]] = x[j].  perm is IMS's LORDER as passed (ImsLinear.f90:653-658). */
+void or_dperm(int n, const double *a, const int *ja, const int *ia, double *ao, int *jao,
+              int *iao, const int *perm) {
+  for (int j = 0; j < n; ++j) iao[perm[j] + 1] = ia[j + 1] - ia[j];
+  iao[0] = 0;
+  for (int j = 0; j < n; ++j) iao[j + 1] += iao[j];
+  for (int ii = 0; ii < n; ++ii) {
+    int ko = iao[perm[ii]];
+    for (int k = ia[ii]; k < ia[ii + 1]; ++k) {
+      jao[ko] = perm[ja[k]];
+      if (a) ao[ko] = a[k];
+      ++ko;
+    }
+  }
+}
+
+static void or_dvperm(int n, double *x, const int *perm, double *tmp) {
+  for (int j = 0; j < n; ++j) tmp[perm[j]] = x[j];
+  memcpy(x, tmp, sizeof(double) * n);
+}
+
 /* ImsLinearBase.f90:1148-1197, ims_calc_pcdims: the ILUT storage length. */
 int or_ilut_iwk(int neq, const int *ia, int level) {
   if (level > 0) return neq * (level * 2 + 1);
@@ -721,6 +923,9 @@ struct or_ims {
   int njapc, iwk;  /* storage of IAPC/JAPC/APC; ILUT: the reference's iwk */
   int *jw, *jr;    /* ILUT work arrays */
   int ilut_ierr;
+  int *lorder, *iorder;  /* REORDERING_METHOD RCM: LORDER/IORDER */
+  int *iaro, *jaro;      /* the permuted pattern */
+  double *aro, *tmp;
   double *d, *p, *q, *z, *t, *v, *dhat, *phat, *qhat;
   double *dscale, *dscale2;
   double l2norm0, epfact;
@@ -761,8 +966,23 @@ or_ims *or_ims_create(const or_ims_settings *s, int neq, int nja, const int *ia,
     h->dscale2[n] = 1.0;
   }
   if (h->ipc == 1 || h->ipc == 2) or_pccrs(neq, nja, h->ia, h->ja, h->iapc, h->japc);
+  /* ims_base_calc_order (ImsLinearBase.f90:556-610), after the IAPC/JAPC
+   * above were built from the unpermuted pattern (ImsLinear.f90:244-248,
+   * 333-336) */
+  if (s->iord == 1) {
+    h->lorder = (int *)malloc(sizeof(int) * neq);
+    h->iorder = (int *)malloc(sizeof(int) * neq);
+    or_genrcm(neq, h->ia, h->ja, h->lorder);
+    for (int n = 0; n < neq; ++n) h->iorder[h->lorder[n]] = n;
+    h->iaro = (int *)calloc(neq + 1, sizeof(int));
+    h->jaro = (int *)calloc(nja, sizeof(int));
+    h->aro = (double *)calloc(nja, sizeof(double));
+    h->tmp = (double *)calloc(neq, sizeof(double));
+  }
   return h;
 }
+
+const int *or_ims_lorder(const or_ims *h) { return h->lorder; }
 
 void or_ims_destroy(or_ims *h) {
   if (!h) return;
@@ -771,6 +991,7 @@ void or_ims_destroy(or_ims *h) {
   free(h->t); free(h->v); free(h->dhat); free(h->phat); free(h->qhat);
   free(h->dscale); free(h->dscale2);
   free(h->jw); free(h->jr);
+  free(h->lorder); free(h->iorder); free(h->iaro); free(h->jaro); free(h->aro); free(h->tmp);
   free(h);
 }
 
@@ -783,20 +1004,32 @@ const double *or_ims_apc(const or_ims *h) { return h->apc; }
 double or_ims_l2norm0(const or_ims *h) { return h->l2norm0; }
 int or_ims_pivot_retries(const or_ims *h) { return h->npivot_retries; }
 
-/* ImsLinear.f90:617-750, imslinear_ap (no reordering: IORD = 0). */
+/* ImsLinear.f90:617-750, imslinear_ap (IORD 0 or 1). */
 int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int kiter,
                  int *icnvg, int *in_iter, or_cnvg_record *rec, int nrec) {
   const or_ims_settings *s = &h->s;
   int neq = h->neq, nja = h->nja;
-  if (s->iord != 0) return -2; /* reordering is not restated here */
+  if (s->iord == 2) return -2; /* minimum degree ordering is not restated here */
   h->epfact = or_epfact(s->icnvgopt, kstp);
   if (s->iscl != 0)
     or_scale(0, s->iscl, neq, nja, h->ia, h->ja, amat, x, rhs, h->dscale, h->dscale2);
+  /* PERMUTE ROWS, COLUMNS, AND RHS (:652-666): the solve works on
+   * A0/IA0/JA0; IAPC/JAPC stay those of the unpermuted pattern */
+  const int *ia0 = h->ia, *ja0 = h->ja;
+  const double *a0 = amat;
+  if (s->iord == 1) {
+    or_dperm(neq, amat, h->ja, h->ia, h->aro, h->jaro, h->iaro, h->lorder);
+    or_dvperm(neq, x, h->lorder, h->tmp);
+    or_dvperm(neq, rhs, h->lorder, h->tmp);
+    ia0 = h->iaro;
+    ja0 = h->jaro;
+    a0 = h->aro;
+  }
   if (h->ipc == 1 || h->ipc == 2) {
-    h->npivot_retries = or_pcu(nja, neq, h->ipc, s->relax, amat, h->ia, h->ja, h->apc,
+    h->npivot_retries = or_pcu(nja, neq, h->ipc, s->relax, a0, ia0, ja0, h->apc,
                                h->iapc, h->japc, h->iw, h->w);
   } else {
-    int rc = or_pcu_ilut(neq, s->level, s->droptol, s->relax, amat, h->ia, h->ja, h->apc,
+    int rc = or_pcu_ilut(neq, s->level, s->droptol, s->relax, a0, ia0, ja0, h->apc,
                          h->iapc, h->japc, h->iwk, h->w, h->jw, h->jr);
     /* ImsLinearBase.f90:822-834: an ilut error is fatal in the reference */
     h->ilut_ierr = rc < 0 ? rc : 0;
@@ -808,7 +1041,7 @@ int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int 
   for (int n = 0; n < neq; ++n) {
     h->d[n] = 0.0; h->p[n] = 0.0; h->q[n] = 0.0; h->z[n] = 0.0;
   }
-  or_residual(neq, x, rhs, h->d, amat, h->ia, h->ja);
+  or_residual(neq, x, rhs, h->d, a0, ia0, ja0);
   h->l2norm0 = or_dnrm2(neq, h->d);
   int itmax = s->iter1;
   if (h->l2norm0 == 0.0) {
@@ -818,13 +1051,19 @@ int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int 
   int innerit = 0;
   if (s->ilinmeth == 1) {
     or_cg(icnvg, itmax, &innerit, neq, nja, s->icnvgopt, s->north, s->dvclose,
-          s->rclose, h->l2norm0, h->epfact, h->ia, h->ja, amat, h->iapc, h->japc,
+          s->rclose, h->l2norm0, h->epfact, ia0, ja0, a0, h->iapc, h->japc,
           h->apc, x, rhs, h->d, h->p, h->q, h->z, rec, nrec);
   } else {
+    /* DSCALE keeps the unpermuted numbering, as in the reference */
     or_bcgs(icnvg, itmax, &innerit, neq, nja, s->icnvgopt, s->north, s->iscl,
-            h->dscale, s->dvclose, s->rclose, h->l2norm0, h->epfact, h->ia, h->ja,
-            amat, h->iapc, h->japc, h->apc, x, rhs, h->d, h->p, h->q, h->t, h->v,
+            h->dscale, s->dvclose, s->rclose, h->l2norm0, h->epfact, ia0, ja0,
+            a0, h->iapc, h->japc, h->apc, x, rhs, h->d, h->p, h->q, h->t, h->v,
             h->dhat, h->phat, h->qhat, rec, nrec);
+  }
+  /* BACK PERMUTE (:730-737); AMAT itself was not permuted in place */
+  if (s->iord == 1) {
+    or_dvperm(neq, x, h->iorder, h->tmp);
+    or_dvperm(neq, rhs, h->iorder, h->tmp);
   }
   if (s->iscl != 0)
     or_scale(1, s->iscl, neq, nja, h->ia, h->ja, amat, x, rhs, h->dscale, h->dscale2);

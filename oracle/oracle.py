@@ -91,6 +91,8 @@ def load():
         lib.or_ims_njapc.argtypes = [C.c_void_p]
         lib.or_ims_ilut_ierr.argtypes = [C.c_void_p]
         lib.or_ilut_iwk.argtypes = [C.c_int, _ip, C.c_int]
+        lib.or_genrcm.argtypes = [C.c_int, _ip, _ip, _ip]
+        lib.or_dperm.argtypes = [C.c_int, _dp, _ip, _ip, _dp, _ip, _ip, _ip]
         lib.or_pcu_ilut.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp, _ip, _ip, _dp,
                                     _ip, _ip, C.c_int, _dp, _ip, _ip]
         lib.or_amux.argtypes = [C.c_int, _dp, _dp, _dp, _ip, _ip]
@@ -214,6 +216,30 @@ def ilut(ia, ja, amat, level, droptol, relax=0.0):
         raise RuntimeError(f"oracle ilut failed: ierr {rc}")
     used = int(iapc[-1])
     return iapc, japc[:used], alu[:used], rc
+
+
+def genrcm(ia, ja):
+    """LORDER of REORDERING_METHOD RCM (rcm.f90 genrcm on the IMS pattern,
+    0-based): lorder[i] is the i-th node of the RCM numbering."""
+    lib = load()
+    ia = np.ascontiguousarray(ia, np.int32)
+    ja = np.ascontiguousarray(ja, np.int32)
+    lorder = np.zeros(ia.size - 1, np.int32)
+    lib.or_genrcm(ia.size - 1, ip(ia), ip(ja), ip(lorder))
+    return lorder
+
+
+def dperm(ia, ja, a, perm):
+    """sparsekit dperm (job 1): row j of A becomes row perm[j], columns
+    relabelled by perm, entries kept in order."""
+    lib = load()
+    ia = np.ascontiguousarray(ia, np.int32)
+    ja = np.ascontiguousarray(ja, np.int32)
+    perm = np.ascontiguousarray(perm, np.int32)
+    iao, jao, ao = np.zeros_like(ia), np.zeros_like(ja), np.zeros(ja.size)
+    lib.or_dperm(ia.size - 1, dp(np.ascontiguousarray(a, float)), ip(ja), ip(ia), dp(ao), ip(jao),
+                 ip(iao), ip(perm))
+    return iao, jao, ao
 
 
 def amux(ia, ja, a, x):

@@ -199,3 +199,73 @@ def test_ilut_rejected_in_batches(gblib):
         EnsembleLinear(ImsLinearSettings(level=5, droptol=1e-4)).allocate(
             np.array([0, 1, 2], np.int32), ia, ja)
     assert e.value.status == _lib.GBIMS_ERR_UNSUPPORTED
+
+
+# -- REORDERING_METHOD RCM (with ILUT/MILUT)
+
+@pytest.mark.parametrize("iscl", [0, 2])
+def test_rcm_ilut_matches_oracle(gblib, iscl):
+    """The permuted system (dperm / dvperm with genrcm's LORDER,
+    ImsLinear.f90:652-666) factored by ILUT: the GPU factor in the permuted
+    numbering is the oracle's bit for bit, and the BiCGSTAB solve reaches the
+    oracle's closure.  L2NORM scaling runs in the model's numbering, as in
+    the reference."""
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=500, ilinmeth=2, level=5, droptol=1e-4, iord=1,
+               iscl=iscl)
+    con, amat, rhs, x0 = c1_system(isym=False)
+    o = oracle.Ims(oracle.settings(**tol), con["ia"], con["ja"])
+    xo = x0.copy()
+    icnvg_o, it_o, _ = o.apply(amat.copy(), rhs.copy(), xo)
+    ims = gpu_ims(con, **tol)
+    x = x0.copy()
+    r = ims.imslinear_apply(amat.copy(), rhs.copy(), x)
+    assert r.icnvg == icnvg_o == 1
+    io, jo, ao = o.factor()
+    iapc, japc, apc = ims.get_factor()
+    np.testing.assert_array_equal(iapc, io)
+    np.testing.assert_array_equal(japc, jo)
+    np.testing.assert_array_equal(apc, ao)
+    lo, hi = oracle_iteration_spread(con, amat, rhs, x0, **tol)
+    assert lo - 3 <= r.in_iter <= hi + 3 or iters_close(r.in_iter, it_o), (r.in_iter, lo, hi)
+    assert_within_oracle_error_spread(x, con, amat, rhs, x0, **tol)
+
+
+def test_rcm_with_ilu0_declined(gblib):
+    con, amat, rhs, x0 = c1_system()
+    with pytest.raises(_lib.GbimsError) as e:
+        gpu_ims(con, iord=1)
+    assert e.value.status == _lib.GBIMS_ERR_UNSUPPORTED
+    with pytest.raises(_lib.GbimsError) as e:
+        gpu_ims(con, iord=2, level=5, droptol=1e-4)
+    assert e.value.status == _lib.GBIMS_ERR_UNSUPPORTED
+
+
+def test_rcm_reorder_autotest_on_gpu(gblib):
+    """autotest/test_gwf_ims_rcm_reorder.py on the device-resident solution:
+    2 x 5 x 30, CHD 10 and 5 on the ends of layer 1, ILUT level 10 and drop
+    tolerance 1e-6, inner closure 1e-12 -- RCM and natural order give the
+    same heads, and both match the oracle's."""
+    from modflow6_gb300.dis import GwfDisModel
+    nlay, nrow, ncol = 2, 5, 30
+    m = GwfDisModel(nlay, nrow, ncol, np.full(ncol, 100.0), np.full(nrow, 100.0),
+                    np.zeros(nrow * ncol), np.concatenate([np.full(nrow * ncol, -10.0),
+                                                           np.full(nrow * ncol, -20.0)]),
+                    np.ones(nlay * nrow * ncol), np.ones(nlay * nrow * ncol),
+                    np.zeros(nlay * nrow * ncol, np.int32), np.zeros(nlay * nrow * ncol))
+    m.chd_node = np.array([r * ncol for r in range(nrow)] + [r * ncol + ncol - 1 for r in range(nrow)],
+                          np.int32)
+    m.chd_head = np.array([10.0] * nrow + [5.0] * nrow)
+    heads = []
+    for iord in (0, 1):
+        ims = ImsLinearSettings(dvclose=1e-12, rclose=1e-6, iter1=100, ilinmeth=2, iord=iord,
+                                level=10, droptol=1e-6)
+        sol = GwfSolution(m, ims, Nonlinear(dvclose=1e-9, mxiter=100))
+        st = sol.timestep(1, 1, 1.0)
+        assert st["converged"] == 1
+        heads.append(sol.heads.copy())
+        sol.close()
+    assert np.max(np.abs(heads[0] - heads[1])) <= 1e-9
+    g = oracle.Gwf(m, oracle.settings(dvclose=1e-12, rclose=1e-6, iter1=100, ilinmeth=2, iord=1,
+                                      level=10, droptol=1e-6))
+    g.timestep(kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-9, mxiter=100)
+    assert np.max(np.abs(heads[1] - g.x)) <= 1e-9

@@ -1,0 +1,116 @@
+"""REORDERING_METHOD RCM on the CPU: the library's numbering (gbims_calc_order,
+host code) against the oracle's restatement of genrcm (rcm/rcm.f90), and
+the oracle's reordered IMS solve against its natural-order solve -- the
+property the reference's own test checks (autotest/test_gwf_ims_rcm_reorder.py:
+the same budgets with and without RCM, ILUT level 10, drop tolerance 1e-6).
+"""
+import ctypes as C
+import shutil
+
+import numpy as np
+import pytest
+
+import oracle
+from modflow6_gb300.dis import GwfDisModel, make_config
+
+
+def lib_or_skip():
+    from modflow6_gb300 import _lib
+    if not _lib.LIB_PATH.exists():
+        if shutil.which("nvcc") is None:
+            pytest.skip("library not built and nvcc not available")
+        from modflow6_gb300 import build
+        build.build()
+    return _lib
+
+
+def pattern(name, scale=1.0, seed=0):
+    g = oracle.Gwf(make_config(name, seed=seed, scale=scale), oracle.settings())
+    return g.con["ia"], g.con["ja"]
+
+
+def grid_pattern(nlay, nrow, ncol):
+    con = oracle.dis_connect(nlay, nrow, ncol, np.ones(ncol), np.ones(nrow), np.zeros(nrow * ncol),
+                             -np.arange(1, nlay + 1, dtype=float).repeat(nrow * ncol))
+    return con["ia"], con["ja"]
+
+
+def disconnected_pattern():
+    """Two grids side by side (the second numbered first in part) and three
+    isolated nodes: several components, each numbered on its own."""
+    ia1, ja1 = grid_pattern(1, 4, 7)
+    ia2, ja2 = grid_pattern(2, 3, 3)
+    n1, n2 = ia1.size - 1, ia2.size - 1
+    rows = [list(ja2[ia2[r]:ia2[r + 1]] + 2) for r in range(n2)]
+    rows = [[0], [1]] + rows + [list(ja1[ia1[r]:ia1[r + 1]] + 2 + n2) for r in range(n1)] + [[2 + n1 + n2]]
+    ia = np.cumsum([0] + [len(r) for r in rows]).astype(np.int32)
+    ja = np.concatenate([np.array(r, np.int32) for r in rows])
+    return ia, ja
+
+
+def lib_order(_lib, ia, ja, base=0):
+    n = ia.size - 1
+    lo, io = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    iab = np.ascontiguousarray(ia + base, np.int32)  # kept alive across the call
+    jab = np.ascontiguousarray(ja + base, np.int32)
+    rc = _lib.load().gbims_calc_order(1, n, int(ia[-1]), _lib.iptr(iab), _lib.iptr(jab), base,
+                                      _lib.iptr(lo), _lib.iptr(io))
+    assert rc == 0
+    return lo - base, io - base
+
+
+CASES = {
+    "c1": lambda: pattern("c1"),
+    "c2-small": lambda: pattern("c2", 0.05, 3),
+    "c3-small": lambda: pattern("c3", 0.04, 1),
+    "rcm-autotest-grid": lambda: grid_pattern(2, 5, 30),
+    "disconnected": disconnected_pattern,
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_library_rcm_matches_oracle(name):
+    _lib = lib_or_skip()
+    ia, ja = CASES[name]()
+    lo_ref = oracle.genrcm(ia, ja)
+    assert np.array_equal(np.sort(lo_ref), np.arange(ia.size - 1))
+    lo, io = lib_order(_lib, ia, ja)
+    np.testing.assert_array_equal(lo, lo_ref)
+    np.testing.assert_array_equal(io[lo], np.arange(ia.size - 1))
+    lo1, _ = lib_order(_lib, ia, ja, base=1)  # Fortran indexing gives the same numbering
+    np.testing.assert_array_equal(lo1, lo_ref)
+
+
+def test_rcm_numbering_reduces_the_profile():
+    """The RCM list itself is a bandwidth-reducing numbering of the
+    2 x 5 x 30 grid (natural bandwidth 150 -> RCM's at most 10)."""
+    ia, ja = grid_pattern(2, 5, 30)
+    lo = oracle.genrcm(ia, ja)
+    pos = np.empty_like(lo)
+    pos[lo] = np.arange(lo.size)
+    rows = np.repeat(np.arange(ia.size - 1), np.diff(ia))
+    assert np.max(np.abs(rows - ja)) == 150
+    assert np.max(np.abs(pos[rows] - pos[ja])) <= 10
+
+
+def test_reordered_solve_matches_natural_order():
+    """The reference's reorder test in the oracle: ILUT level 10, drop
+    tolerance 1e-6, inner closure 1e-12 -- the heads with and without RCM."""
+    nlay, nrow, ncol = 2, 5, 30
+    m = GwfDisModel(nlay, nrow, ncol, np.full(ncol, 100.0), np.full(nrow, 100.0),
+                    np.zeros(nrow * ncol), np.concatenate([np.full(nrow * ncol, -10.0),
+                                                           np.full(nrow * ncol, -20.0)]),
+                    np.ones(nlay * nrow * ncol), np.ones(nlay * nrow * ncol),
+                    np.zeros(nlay * nrow * ncol, np.int32), np.zeros(nlay * nrow * ncol))
+    m.chd_node = np.array([r * ncol for r in range(nrow)] + [r * ncol + ncol - 1 for r in range(nrow)],
+                          np.int32)
+    m.chd_head = np.array([10.0] * nrow + [5.0] * nrow)
+    heads = []
+    for iord in (0, 1):
+        s = oracle.settings(dvclose=1e-12, rclose=1e-6, iter1=100, ilinmeth=2, iord=iord, level=10,
+                            droptol=1e-6)
+        g = oracle.Gwf(m, s)
+        st = g.timestep(kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-9, mxiter=100)
+        assert st["converged"] == 1
+        heads.append(g.x.copy())
+    assert np.max(np.abs(heads[0] - heads[1])) <= 1e-9
