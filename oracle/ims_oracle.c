@@ -627,9 +627,11 @@ static void rcm_number(int root, const int *ia, const int *ja, int *mask, int *p
  * included, as IMS passes it): lorder[i] (0-based) is the i-th node of the
  * RCM numbering. */
 void or_genrcm(int n, const int *ia0, const int *ja0, int *lorder) {
+  if (n <= 0) return;
   const int nja = ia0[n];
-  int *ia = (int *)malloc(sizeof(int) * (n + 2));
-  int *ja = (int *)malloc(sizeof(int) * (nja + 1));
+  if (nja <= 0) return;
+  int *ia = (int *)malloc(sizeof(int) * ((size_t)n + 2));
+  int *ja = (int *)malloc(sizeof(int) * ((size_t)nja + 1));
   for (int i = 0; i <= n; ++i) ia[i + 1] = ia0[i] + 1;
   for (int k = 0; k < nja; ++k) ja[k + 1] = ja0[k] + 1;
   int *mask = (int *)malloc(sizeof(int) * (n + 1));
