@@ -48,8 +48,8 @@ typedef struct gbims_settings {
   int iter1;        /* INNER_MAXIMUM */
   int ilinmeth;     /* LINEAR_ACCELERATION: 1 CG, 2 BICGSTAB */
   int iscl;         /* SCALING_METHOD: 0 none, 1 diagonal, 2 L2 norm */
-  int iord;         /* REORDERING_METHOD: 0 none, 1 RCM (with ILUT/MILUT;
-                       with ILU0/MILU0 and for 2, MD: GBIMS_ERR_UNSUPPORTED) */
+  int iord;         /* REORDERING_METHOD: 0 none, 1 RCM, 2 MD (with
+                       ILUT/MILUT; with ILU0/MILU0: GBIMS_ERR_UNSUPPORTED) */
   int north;        /* NUMBER_ORTHOGONALIZATIONS */
   double relax;     /* RELAXATION_FACTOR (> 0 selects MILU0 / MILUT) */
   int level;        /* PRECONDITIONER_LEVELS (> 0: ILUT with lfil = level) */
@@ -193,11 +193,11 @@ int gbims_get_apc(gbims_handle *h, double *apc);
 int gbims_get_factor(gbims_handle *h, int *iapc, int *japc, double *apc, int capacity,
                      int *njapc);
 
-/* ims_base_calc_order (ImsLinearBase.f90:556-610) for IORD 1 (RCM, genrcm of
- * rcm/rcm.f90) on a CSR pattern: LORDER(i) is the i-th node of the
- * numbering and IORDER its inverse, in index_base.  Host only (no device
- * work); IORD 2 (minimum degree) returns GBIMS_ERR_UNSUPPORTED.  A handle
- * created with iord 1 applies LORDER as imslinear_ap does (dperm/dvperm,
+/* ims_base_calc_order (ImsLinearBase.f90:556-610) on a CSR pattern: IORD 1
+ * RCM (genrcm of rcm/rcm.f90), IORD 2 minimum degree (ims_odrv of
+ * ImsReordering.f90).  LORDER(i) is the i-th node of the numbering and
+ * IORDER its inverse, in index_base.  Host only (no device work).  A handle
+ * created with iord 1 or 2 applies LORDER as imslinear_ap does (dperm/dvperm,
  * ImsLinear.f90:652-666 and 730-737); its gbims_matvec, gbims_precondition
  * and gbims_get_factor then work in that permuted numbering. */
 int gbims_calc_order(int iord, int neq, int nja, const int *ia, const int *ja, int index_base,

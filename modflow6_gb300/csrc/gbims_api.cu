@@ -62,7 +62,7 @@ struct gbims_handle {
   IlutStatus *h_ilut = nullptr;
   long long ilut_iwk = 0;
   int njapc = 0;
-  // REORDERING_METHOD RCM: the solve runs on the permuted system (A0, IA0,
+  // REORDERING_METHOD RCM/MD: the solve runs on the permuted system (A0, IA0,
   // JA0 of imslinear_ap); callers' arrays, the scaling and the unscaling
   // stay in the model's numbering (u_*), gathered in and out at each apply
   bool reorder = false;
@@ -386,12 +386,11 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   if (s->relax < 0.0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RELAX MUST BE >= 0.0"); }
   if (s->relax > 1.0) { *out = h; return fail(h, GBIMS_ERR_ARG, "IMSLINEAR7AR RELAX MUST BE <= 1.0"); }
   if (s->level < 0) { *out = h; return fail(h, GBIMS_ERR_ARG, "ILUT: PRECONDITIONER_LEVELS must be >= 0"); }
-  if (s->iord == 2) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "REORDERING_METHOD MD is not supported"); }
   // With ILU0/MILU0 the reference factors the permuted matrix against the
   // IAPC/JAPC of the unpermuted pattern (built at ImsLinear.f90:244-248,
   // before the ordering at :333-336), carrying work-vector entries from row
   // to row; that combination is declined rather than changed.
-  if (s->iord == 1 && h->ipc < 3) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "REORDERING_METHOD RCM is supported with ILUT/MILUT only (PRECONDITIONER_LEVELS or DROP_TOLERANCE > 0)"); }
+  if (s->iord != 0 && h->ipc < 3) { *out = h; return fail(h, GBIMS_ERR_UNSUPPORTED, "REORDERING_METHOD RCM/MD is supported with ILUT/MILUT only (PRECONDITIONER_LEVELS or DROP_TOLERANCE > 0)"); }
   if (s->precision != GBIMS_FP64 && s->precision != GBIMS_MIXED) { *out = h; return fail(h, GBIMS_ERR_ARG, "precision must be GBIMS_FP64 or GBIMS_MIXED"); }
   h->mixed = (s->precision == GBIMS_MIXED);
   h->bcgs = (s->ilinmeth == 2);
@@ -419,14 +418,20 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
     for (int k = h->ia[r]; k < h->ia[r + 1]; ++k)
       if (h->ja[k] < 0 || h->ja[k] >= neq) { *out = h; return fail(h, GBIMS_ERR_ARG, "column index out of range"); }
   }
-  // REORDERING_METHOD RCM: LORDER (ims_base_calc_order) and the permuted
+  // REORDERING_METHOD RCM/MD: LORDER (ims_base_calc_order) and the permuted
   // pattern of dperm with job 1 (sparsekit.f90:249-447): row j becomes row
   // LORDER(j), its entries kept in order, columns relabelled by LORDER --
   // LORDER is the numbering's list of nodes, used as a new-index map, as
   // imslinear_ap passes it (ImsLinear.f90:653-658)
-  if (s->iord == 1) {
+  if (s->iord != 0) {
     h->reorder = true;
-    rcm_order(neq, h->ia, h->ja, h->lorder);
+    if (s->iord == 1) {
+      rcm_order(neq, h->ia, h->ja, h->lorder);
+    } else if (int flag = md_order(neq, h->ia, h->ja, h->lorder)) {
+      // ImsLinearBase.f90:590-595: fatal in the reference
+      *out = h;
+      return fail(h, GBIMS_ERR_ARG, "IMSLINEARSUB_CALC_ORDER error creating minimum degree order permutation (flag " + std::to_string(flag) + ")");
+    }
     h->ia_u = h->ia;
     h->ja_u = h->ja;
     std::vector<int> iaro(neq + 1, 0), jaro(nja);
@@ -633,7 +638,7 @@ static double epfact_of(int icnvgopt, int kstp) {
   return 1.0;
 }
 
-// dst[i] = src[idx[i]]: the permutations of REORDERING_METHOD RCM (dperm and
+// dst[i] = src[idx[i]]: the permutations of REORDERING_METHOD RCM/MD (dperm and
 // dvperm of sparsekit, as gathers)
 __global__ void k_gather(int n, const int *__restrict__ idx, const double *__restrict__ src,
                          double *__restrict__ dst) {
@@ -979,7 +984,7 @@ extern "C" int gbims_get_apc(gbims_handle *h, double *apc) {
 extern "C" int gbims_calc_order(int iord, int neq, int nja, const int *ia, const int *ja,
                                 int index_base, int *lorder, int *iorder) {
   if (neq <= 0 || nja < neq || !ia || !ja || !lorder || !iorder) return GBIMS_ERR_ARG;
-  if (iord != 1) return GBIMS_ERR_UNSUPPORTED;
+  if (iord != 1 && iord != 2) return GBIMS_ERR_ARG;
   const int base = index_base ? 1 : 0;
   std::vector<int> a(neq + 1), c(nja), lo;
   for (int i = 0; i <= neq; ++i) a[i] = ia[i] - base;
@@ -990,7 +995,8 @@ extern "C" int gbims_calc_order(int iord, int neq, int nja, const int *ia, const
     c[k] = ja[k] - base;
     if (c[k] < 0 || c[k] >= neq) return GBIMS_ERR_ARG;
   }
-  rcm_order(neq, a, c, lo);
+  if (iord == 1) rcm_order(neq, a, c, lo);
+  else if (md_order(neq, a, c, lo) != 0) return GBIMS_ERR_ARG;
   for (int i = 0; i < neq; ++i) {
     lorder[i] = lo[i] + base;
     iorder[lo[i]] = i + base;

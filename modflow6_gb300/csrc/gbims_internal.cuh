@@ -225,6 +225,10 @@ void levels_build_host(int n, const std::vector<int> &iapc, const std::vector<in
 // the numbering genrcm gives for the 0-based CSR pattern ia/ja.
 void rcm_order(int n, const std::vector<int> &ia, const std::vector<int> &ja,
                std::vector<int> &lorder);
+// REORDERING_METHOD MD (h_md.cu): lorder[i] is the i-th node eliminated by
+// the Yale minimum-degree ordering; returns odrv's flag (0 on success).
+int md_order(int n, const std::vector<int> &ia, const std::vector<int> &ja,
+             std::vector<int> &lorder);
 void launch_ilu_factor(int n, const int *d_ia, const int *d_ja, const double *d_amat,
                        const int *d_iapc, const int *d_japc, double *d_apc,
                        const Levels &L, double relax, double delta, int ipcflag,

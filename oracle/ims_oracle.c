@@ -655,6 +655,273 @@ void or_genrcm(int n, const int *ia0, const int *ja0, int *lorder) {
   free(ia); free(ja); free(mask); free(perm); free(level_row); free(level); free(deg); free(vis);
 }
 
+/* ---- REORDERING_METHOD MD: ImsReordering.f90 (the Yale sparse matrix
+ * package's minimum-degree ordering: odrv, md, mdi, mdm, mdp, mdu).  Arrays
+ * are 1-based as in the source; v doubles as mark (odrv passes isp(v) for
+ * both: mark lives in v(1:n), the list nodes from n + 1 on); vk and ek are
+ * one variable, as are vs and es.  The labels of the source are kept. */
+
+/* :359-461, mdi: element/vertex lists of the symmetric pattern and the
+ * degree lists. */
+static int md_init(int n, const int *ia, const int *ja, int mmax, int *v, int *l, int *head,
+                   int *last, int *next, int tag) {
+  int *mark = v;
+  for (int vi = 1; vi <= n; ++vi) {
+    mark[vi] = 1;
+    l[vi] = 0;
+    head[vi] = 0;
+  }
+  int sfs = n + 1;
+  for (int vi = 1; vi <= n; ++vi) {
+    const int jmin = ia[vi], jmax = ia[vi + 1] - 1;
+    for (int j = jmin; j <= jmax; ++j) {
+      const int vj = ja[j];
+      const int ieval = vj - vi;
+      if (ieval == 0) continue;
+      if (ieval < 0) {
+        int lvk = vi, found = 0;
+        const int kmax = mark[vi] - 1;
+        for (int k = 1; k <= kmax; ++k) {
+          lvk = l[lvk];
+          if (v[lvk] == vj) { found = 1; break; }
+        }
+        if (found) continue;
+      }
+      if (sfs >= mmax) return 9 * n + vi;
+      mark[vi] = mark[vi] + 1;
+      v[sfs] = vj;
+      l[sfs] = l[vi];
+      l[vi] = sfs;
+      sfs = sfs + 1;
+      mark[vj] = mark[vj] + 1;
+      v[sfs] = vi;
+      l[sfs] = l[vj];
+      l[vj] = sfs;
+      sfs = sfs + 1;
+    }
+  }
+  for (int vi = 1; vi <= n; ++vi) {
+    const int dvi = mark[vi];
+    next[vi] = head[dvi];
+    head[dvi] = vi;
+    last[vi] = -dvi;
+    const int nextvi = next[vi];
+    if (nextvi > 0) last[nextvi] = vi;
+    mark[vi] = tag;
+  }
+  return 0;
+}
+
+/* :463-540, mdm: the list of uneliminated vertices reachable from vk. */
+static void md_merge(int vk, int *tail, int *v, int *l, const int *last, const int *next) {
+  int *mark = v;
+  const int tag = mark[vk];
+  *tail = vk;
+  int ls = l[vk];
+  for (;;) {
+    const int s = ls;
+    if (s == 0) break;
+    ls = l[s];
+    const int vs = v[s];
+    if (next[vs] >= 0) {
+      mark[vs] = tag;
+      l[*tail] = s;
+      *tail = s;
+      continue;
+    }
+    const int es = vs;
+    int lb = l[es];
+    const int blpmax = last[es];
+    for (int blp = 1; blp <= blpmax; ++blp) {
+      const int b = lb;
+      lb = l[b];
+      const int vb = v[b];
+      if (mark[vb] >= tag) continue;
+      mark[vb] = tag;
+      l[*tail] = b;
+      *tail = b;
+    }
+    mark[es] = tag;
+  }
+  l[*tail] = 0;
+}
+
+/* :542-657, mdp: purges the reachable vertices' lists of the elements
+ * absorbed by ek and eliminates the vertices left with no other element. */
+static void md_purge(int *k, int ek, int tail, int *v, int *l, int *head, int *last, int *next) {
+  int *mark = v;
+  const int tag = mark[ek];
+  int li = ek, free_ = 0;
+  const int ilpmax = last[ek];
+  if (ilpmax <= 0) goto L12;
+  for (int ilp = 1; ilp <= ilpmax; ++ilp) {
+    int i = li, ls, s, lvi, evi;
+    li = l[i];
+    const int vi = v[li];
+    if (last[vi] == 0) goto L3;
+    if (last[vi] > 0) goto L1;
+    head[-last[vi]] = next[vi];
+    goto L2;
+  L1:
+    next[last[vi]] = next[vi];
+  L2:
+    if (next[vi] > 0) last[next[vi]] = last[vi];
+  L3:
+    ls = vi;
+  L4:
+    s = ls;
+    ls = l[s];
+    if (ls == 0) goto L6;
+    {
+      const int es = v[ls];
+      if (mark[es] < tag) goto L4;
+    }
+    free_ = ls;
+    l[s] = l[ls];
+    ls = s;
+    goto L4;
+  L6:
+    lvi = l[vi];
+    if (lvi != 0) goto L7;
+    l[i] = l[li];
+    li = i;
+    *k = *k + 1;
+    next[vi] = -*k;
+    last[ek] = last[ek] - 1;
+    continue;
+  L7:
+    if (l[lvi] != 0) goto L9;
+    evi = v[lvi];
+    if (next[evi] >= 0) goto L9;
+    if (mark[evi] < 0) goto L8;
+    last[vi] = evi;
+    mark[evi] = -1;
+    l[tail] = li;
+    tail = li;
+    l[i] = l[li];
+    li = i;
+    goto L10;
+  L8:
+    last[vi] = 0;
+    mark[evi] = mark[evi] - 1;
+    goto L10;
+  L9:
+    last[vi] = -ek;
+  L10:
+    v[free_] = ek;
+    l[free_] = l[vi];
+    l[vi] = free_;
+  }
+L12:
+  l[tail] = 0;
+}
+
+/* :659-772, mdu: new degrees of the vertices reachable from ek. */
+static void md_update(int ek, int *dmin, int *v, int *l, int *head, int *last, int *next) {
+  int *mark = v;
+  int tag = mark[ek] - last[ek];
+  int i = ek;
+  const int ilpmax = last[ek];
+  if (ilpmax <= 0) return;
+  for (int ilp = 1; ilp <= ilpmax; ++ilp) {
+    int vi, dvi, s, es, evi;
+    i = l[i];
+    vi = v[i];
+    if (last[vi] == 0) continue;
+    if (last[vi] > 0) goto L8;
+    tag = tag + 1;
+    dvi = last[ek];
+    s = l[vi];
+  L2:
+    s = l[s];
+    if (s == 0) goto L9;
+    es = v[s];
+    if (next[es] < 0) goto L3;
+    mark[es] = tag;
+    dvi = dvi + 1;
+    goto L2;
+  L3:
+    if (mark[es] < 0) goto L6;
+    {
+      int b = es;
+      const int blpmax = last[es];
+      for (int blp = 1; blp <= blpmax; ++blp) {
+        b = l[b];
+        const int vb = v[b];
+        if (mark[vb] >= tag) continue;
+        mark[vb] = tag;
+        dvi = dvi + 1;
+      }
+    }
+    goto L2;
+  L6:
+    last[vi] = 0;
+    mark[es] = mark[es] - 1;
+  L7:
+    s = l[s];
+    if (s == 0) continue;
+    es = v[s];
+    if (mark[es] < 0) mark[es] = mark[es] - 1;
+    goto L7;
+  L8:
+    evi = last[vi];
+    dvi = last[ek] + last[evi] + mark[evi];
+    mark[evi] = 0;
+  L9:
+    next[vi] = head[dvi];
+    head[dvi] = vi;
+    last[vi] = -dvi;
+    if (next[vi] > 0) last[next[vi]] = vi;
+    if (dvi < *dmin) *dmin = dvi;
+  }
+}
+
+/* :7-196 (odrv, path 1) and :198-357 (md) with the work length IMS gives
+ * (nsp = 3 NEQ + 4 NJA, ImsLinearBase.f90:585): lorder[i] (0-based) is the
+ * i-th eliminated node.  Returns odrv's flag (0 on success). */
+int or_genmd(int n, const int *ia0, const int *ja0, int *lorder) {
+  if (n <= 0) return 0;
+  const int nja = ia0[n];
+  const long long nsp = 3LL * n + 4LL * nja;
+  const int mmax = (int)((nsp - n) / 2);
+  if (mmax < n) return 10 * n + 1;
+  int *ia = (int *)malloc(sizeof(int) * ((size_t)n + 2));
+  int *ja = (int *)malloc(sizeof(int) * ((size_t)nja + 1));
+  for (int i = 0; i <= n; ++i) ia[i + 1] = ia0[i] + 1;
+  for (int k = 0; k < nja; ++k) ja[k + 1] = ja0[k] + 1;
+  int *v = (int *)calloc((size_t)mmax + 1, sizeof(int));
+  int *l = (int *)calloc((size_t)mmax + 1, sizeof(int));
+  int *head = (int *)calloc(2 * (size_t)n + 2, sizeof(int));
+  int *last = (int *)calloc((size_t)n + 1, sizeof(int));
+  int *next = (int *)calloc((size_t)n + 1, sizeof(int));
+  int tag = 0;
+  int flag = md_init(n, ia, ja, mmax, v, l, head, last, next, tag);
+  if (flag == 0) {
+    int k = 0, dmin = 1, tail = 0;
+    while (k < n) {
+      while (head[dmin] <= 0) dmin = dmin + 1;
+      const int vk = head[dmin];
+      head[dmin] = next[vk];
+      if (head[dmin] > 0) last[head[dmin]] = -dmin;
+      k = k + 1;
+      next[vk] = -k;
+      last[vk] = dmin - 1;
+      tag = tag + last[vk];
+      v[vk] = tag;
+      md_merge(vk, &tail, v, l, last, next);
+      md_purge(&k, vk, tail, v, l, head, last, next);
+      md_update(vk, &dmin, v, l, head, last, next);
+    }
+    for (int kk = 1; kk <= n; ++kk) {
+      next[kk] = -next[kk];
+      last[next[kk]] = kk;
+    }
+    for (int i = 1; i <= n; ++i) lorder[i - 1] = last[i] - 1;
+  }
+  free(ia); free(ja); free(v); free(l); free(head); free(last); free(next);
+  return flag;
+}
+
 /* sparsekit.f90:353-447 (dperm with job 1: rperm then cperm with the same
  * permutation) -- row j of A becomes row perm[j] of B, its entries in the
  * same order, columns relabelled by perm -- and :61-161 (dvperm):
@@ -927,6 +1194,7 @@ struct or_ims {
   int ilut_ierr;
   int *lorder, *iorder;  /* REORDERING_METHOD RCM: LORDER/IORDER */
   int *iaro, *jaro;      /* the permuted pattern */
+  int md_flag;           /* odrv's flag (MD) */
   double *aro, *tmp;
   double *d, *p, *q, *z, *t, *v, *dhat, *phat, *qhat;
   double *dscale, *dscale2;
@@ -971,10 +1239,11 @@ or_ims *or_ims_create(const or_ims_settings *s, int neq, int nja, const int *ia,
   /* ims_base_calc_order (ImsLinearBase.f90:556-610), after the IAPC/JAPC
    * above were built from the unpermuted pattern (ImsLinear.f90:244-248,
    * 333-336) */
-  if (s->iord == 1) {
+  if (s->iord == 1 || s->iord == 2) {
     h->lorder = (int *)malloc(sizeof(int) * neq);
     h->iorder = (int *)malloc(sizeof(int) * neq);
-    or_genrcm(neq, h->ia, h->ja, h->lorder);
+    if (s->iord == 1) or_genrcm(neq, h->ia, h->ja, h->lorder);
+    else h->md_flag = or_genmd(neq, h->ia, h->ja, h->lorder);
     for (int n = 0; n < neq; ++n) h->iorder[h->lorder[n]] = n;
     h->iaro = (int *)calloc(neq + 1, sizeof(int));
     h->jaro = (int *)calloc(nja, sizeof(int));
@@ -1011,7 +1280,8 @@ int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int 
                  int *icnvg, int *in_iter, or_cnvg_record *rec, int nrec) {
   const or_ims_settings *s = &h->s;
   int neq = h->neq, nja = h->nja;
-  if (s->iord == 2) return -2; /* minimum degree ordering is not restated here */
+  /* ImsLinearBase.f90:590-595: an MD failure is fatal in the reference */
+  if (s->iord == 2 && h->md_flag != 0) return -2;
   h->epfact = or_epfact(s->icnvgopt, kstp);
   if (s->iscl != 0)
     or_scale(0, s->iscl, neq, nja, h->ia, h->ja, amat, x, rhs, h->dscale, h->dscale2);
@@ -1019,7 +1289,7 @@ int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int 
    * A0/IA0/JA0; IAPC/JAPC stay those of the unpermuted pattern */
   const int *ia0 = h->ia, *ja0 = h->ja;
   const double *a0 = amat;
-  if (s->iord == 1) {
+  if (s->iord != 0) {
     or_dperm(neq, amat, h->ja, h->ia, h->aro, h->jaro, h->iaro, h->lorder);
     or_dvperm(neq, x, h->lorder, h->tmp);
     or_dvperm(neq, rhs, h->lorder, h->tmp);
@@ -1063,7 +1333,7 @@ int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int 
             h->dhat, h->phat, h->qhat, rec, nrec);
   }
   /* BACK PERMUTE (:730-737); AMAT itself was not permuted in place */
-  if (s->iord == 1) {
+  if (s->iord != 0) {
     or_dvperm(neq, x, h->iorder, h->tmp);
     or_dvperm(neq, rhs, h->iorder, h->tmp);
   }

@@ -64,6 +64,7 @@ int or_pcu_ilut(int neq, int lfil, double droptol, double relax, const double *a
                 double *w, int *jw, int *jr);
 int or_ilut_iwk(int neq, const int *ia, int level);
 void or_genrcm(int n, const int *ia0, const int *ja0, int *lorder);
+int or_genmd(int n, const int *ia0, const int *ja0, int *lorder);
 void or_dperm(int n, const double *a, const int *ja, const int *ia, double *ao, int *jao,
               int *iao, const int *perm);
 const int *or_ims_lorder(const or_ims *h);

@@ -92,6 +92,7 @@ def load():
         lib.or_ims_ilut_ierr.argtypes = [C.c_void_p]
         lib.or_ilut_iwk.argtypes = [C.c_int, _ip, C.c_int]
         lib.or_genrcm.argtypes = [C.c_int, _ip, _ip, _ip]
+        lib.or_genmd.argtypes = [C.c_int, _ip, _ip, _ip]
         lib.or_dperm.argtypes = [C.c_int, _dp, _ip, _ip, _dp, _ip, _ip, _ip]
         lib.or_pcu_ilut.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp, _ip, _ip, _dp,
                                     _ip, _ip, C.c_int, _dp, _ip, _ip]
@@ -226,6 +227,19 @@ def genrcm(ia, ja):
     ja = np.ascontiguousarray(ja, np.int32)
     lorder = np.zeros(ia.size - 1, np.int32)
     lib.or_genrcm(ia.size - 1, ip(ia), ip(ja), ip(lorder))
+    return lorder
+
+
+def genmd(ia, ja):
+    """LORDER of REORDERING_METHOD MD (ImsReordering.f90 odrv/md on the IMS
+    pattern, 0-based): lorder[i] is the i-th eliminated node."""
+    lib = load()
+    ia = np.ascontiguousarray(ia, np.int32)
+    ja = np.ascontiguousarray(ja, np.int32)
+    lorder = np.zeros(ia.size - 1, np.int32)
+    flag = lib.or_genmd(ia.size - 1, ip(ia), ip(ja), ip(lorder))
+    if flag != 0:
+        raise RuntimeError(f"oracle md failed: flag {flag}")
     return lorder
 
 

@@ -204,16 +204,18 @@ def test_ilut_rejected_in_batches(gblib):
 # -- REORDERING_METHOD RCM (with ILUT/MILUT)
 
 @pytest.mark.parametrize("iscl", [0, 2])
-def test_rcm_ilut_matches_oracle(gblib, iscl):
-    """The permuted system (dperm / dvperm with genrcm's LORDER,
-    ImsLinear.f90:652-666) factored by ILUT: the GPU factor in the permuted
-    numbering is the oracle's bit for bit, and the BiCGSTAB solve reaches the
-    oracle's closure.  L2NORM scaling runs in the model's numbering, as in
-    the reference.  IMS applies genrcm's list as a new-index map, which
-    numbers c1 with a bandwidth near 9,800: ILUT(5, 1e-4) then gathers 261
-    lower candidates in one row, past the 256 the GPU factor holds, so the
-    case runs ILUT(3, 1e-3) (62 at most)."""
-    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=500, ilinmeth=2, level=3, droptol=1e-3, iord=1,
+@pytest.mark.parametrize("iord", [1, 2], ids=["rcm", "md"])
+def test_rcm_ilut_matches_oracle(gblib, iscl, iord):
+    """The permuted system (dperm / dvperm with LORDER, ImsLinear.f90:652-666;
+    genrcm's for RCM, the minimum-degree package's for MD) factored by ILUT:
+    the GPU factor in the permuted numbering is the oracle's bit for bit, and
+    the BiCGSTAB solve reaches the oracle's closure.  L2NORM scaling runs in
+    the model's numbering, as in the reference.  IMS applies the ordering's
+    list as a new-index map, which numbers c1 with a bandwidth near 9,800:
+    ILUT(5, 1e-4) then gathers 261 (RCM) or 265 (MD) lower candidates in one
+    row, past the 256 the GPU factor holds, so the case runs ILUT(3, 1e-3)
+    (62 and 55 at most)."""
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=500, ilinmeth=2, level=3, droptol=1e-3, iord=iord,
                iscl=iscl)
     con, amat, rhs, x0 = c1_system(isym=False)
     o = oracle.Ims(oracle.settings(**tol), con["ia"], con["ja"])
@@ -239,7 +241,7 @@ def test_rcm_with_ilu0_declined(gblib):
         gpu_ims(con, iord=1)
     assert e.value.status == _lib.GBIMS_ERR_UNSUPPORTED
     with pytest.raises(_lib.GbimsError) as e:
-        gpu_ims(con, iord=2, level=5, droptol=1e-4)
+        gpu_ims(con, iord=2, relax=0.97)  # MD with MILU0
     assert e.value.status == _lib.GBIMS_ERR_UNSUPPORTED
 
 

@@ -1,10 +1,13 @@
-"""REORDERING_METHOD RCM on the CPU: the library's numbering (gbims_calc_order,
-host code) against the oracle's restatement of genrcm (rcm/rcm.f90), and
-the oracle's reordered IMS solve against its natural-order solve -- the
-property the reference's own test checks (autotest/test_gwf_ims_rcm_reorder.py:
-the same budgets with and without RCM, ILUT level 10, drop tolerance 1e-6).
+"""REORDERING_METHOD RCM and MD on the CPU: the library's numberings
+(gbims_calc_order, host code) against the oracle's restatements of genrcm
+(rcm/rcm.f90) and of the Yale minimum-degree ordering (ImsReordering.f90),
+and the oracle's reordered IMS solves against natural order -- the property
+the reference's own test checks (autotest/test_gwf_ims_rcm_reorder.py: the
+same budgets with and without RCM, ILUT level 10, drop tolerance 1e-6).
+The reference commits no orderings, so the numberings are pinned by the two
+restatements agreeing and by what the orderings are for (RCM's bandwidth,
+MD's fill).
 """
-import ctypes as C
 import shutil
 
 import numpy as np
@@ -114,3 +117,61 @@ def test_reordered_solve_matches_natural_order():
         assert st["converged"] == 1
         heads.append(g.x.copy())
     assert np.max(np.abs(heads[0] - heads[1])) <= 1e-9
+
+
+# -- REORDERING_METHOD MD (ImsReordering.f90: the Yale minimum-degree ordering)
+
+def lib_md_order(_lib, ia, ja):
+    n = ia.size - 1
+    lo, io = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    iab = np.ascontiguousarray(ia, np.int32)
+    jab = np.ascontiguousarray(ja, np.int32)
+    rc = _lib.load().gbims_calc_order(2, n, int(ia[-1]), _lib.iptr(iab), _lib.iptr(jab), 0,
+                                      _lib.iptr(lo), _lib.iptr(io))
+    assert rc == 0
+    return lo, io
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_library_md_matches_oracle(name):
+    _lib = lib_or_skip()
+    ia, ja = CASES[name]()
+    lo_ref = oracle.genmd(ia, ja)
+    assert np.array_equal(np.sort(lo_ref), np.arange(ia.size - 1))
+    lo, io = lib_md_order(_lib, ia, ja)
+    np.testing.assert_array_equal(lo, lo_ref)
+    np.testing.assert_array_equal(io[lo], np.arange(ia.size - 1))
+
+
+def test_md_numbering_cuts_the_fill():
+    """Eliminating in the MD list's order fills far less than the natural
+    order (symbolic LU of the 2 x 5 x 30 grid and of c1)."""
+    scipy_linalg = pytest.importorskip("scipy.sparse.linalg")
+    import scipy.sparse as sp
+    for ia, ja in (grid_pattern(2, 5, 30), pattern("c1")):
+        n = ia.size - 1
+        A = sp.csr_matrix((np.ones(ja.size), ja, ia), shape=(n, n)) + 10.0 * sp.eye(n)
+        lo = oracle.genmd(ia, ja)
+
+        def fill(M):
+            f = scipy_linalg.splu(M.tocsc(), permc_spec="NATURAL", diag_pivot_thresh=0.0,
+                                  options=dict(SymmetricMode=True))
+            return f.L.nnz + f.U.nnz
+        assert fill(A[lo][:, lo]) < 0.25 * fill(A)
+
+
+def test_md_reordered_solve_matches_natural_order():
+    """As the reference's reorder test, with MD: ILUT level 10 / 1e-6, the
+    heads with and without the ordering agree."""
+    from test_gpu_ims import c1_system  # the oracle-assembled c1 system (no GPU involved)
+    con, amat, rhs, x0 = c1_system(isym=False)
+    xs = []
+    for iord in (0, 2):
+        s = oracle.settings(dvclose=1e-10, rclose=1e-8, iter1=2000, ilinmeth=2, iord=iord,
+                            level=10, droptol=1e-6)
+        ims = oracle.Ims(s, con["ia"], con["ja"])
+        x = x0.copy()
+        icnvg, it, _ = ims.apply(amat.copy(), rhs.copy(), x)
+        assert icnvg == 1
+        xs.append(x)
+    assert np.max(np.abs(xs[0] - xs[1])) <= 1e-7
