@@ -135,7 +135,7 @@ int gbims_batch_apply_device(gbims_handle *h, double *d_amat, double *d_rhs, dou
  * and for kernel-level checks (host arrays):
  *  gbims_factor       preconditioner update, ims_base_pcu + ims_base_pcilu0
  *                     (ImsLinearBase.f90:761-864, 928-1042) or, for IPC 3/4,
- *                     ilut (sparskit2/ilut.f90:48-465), from amat (nja);
+ *                     ilut (sparskit2/ilut.f90:48-462), from amat (nja);
  *  gbims_get_apc      copies APC (nja, the reference's layout: APC(1:NEQ) the
  *                     inverse pivots, then the L\U entries in JAPC order);
  *                     ILU0/MILU0 only;

@@ -677,7 +677,7 @@ __global__ void k_zero_vec(int n, double *a, double *b, double *c, double *d) {
 static void drop_graph(gbims_handle *h);
 
 // ILUT / MILUT update (ims_base_pcu, IPC 3/4: ImsLinearBase.f90:812-864
-// around sparskit2/ilut.f90:48-465).  The pivot guard's retry loop is the
+// around sparskit2/ilut.f90:48-462).  The pivot guard's retry loop is the
 // reference's; ilut leaves izero unchanged on success, so a factorisation
 // with izero 2 (delta 0.5) makes the reference repeat the same factorisation
 // until icount exceeds 10: that count is taken without the repeats.  The

@@ -1,6 +1,6 @@
 // k_ilut.cu -- ILUT / MILUT factorisation on the GPU.
 //
-// ilut (src/Utilities/Libraries/sparskit2/ilut.f90:48-465, Saad's dual
+// ilut (src/Utilities/Libraries/sparskit2/ilut.f90:48-462, Saad's dual
 // threshold ILU with MODFLOW's relaxation of the dropped sum and its pivot
 // guard) restated for one thread per row.  Row ii depends only on the U rows
 // of the earlier rows it eliminates, and those are known only once its own
@@ -17,7 +17,7 @@
 // they entered the row (the row's own upper entries in JA order, then the
 // fill as it appears); dropped terms are summed in the reference's order; the
 // lfil largest multipliers and the lfil - 1 largest U entries are chosen by
-// the same partial quick-sort (qsplit, :515-579), whose output order is the
+// the same partial quick-sort (qsplit, :519-581), whose output order is the
 // storage order and so the summation order of the triangular solves.  Every
 // operation is rounded on its own (no FMA), as in the CPU code.
 //
@@ -25,7 +25,7 @@
 // kept columns and values, their counts and the inverse pivot.  The host
 // turns the counts into the IAPC/JAPC layout of the ILU0 preconditioner and
 // k_ilut_scatter moves the values there, so the level-scheduled sweeps apply
-// ILUT unchanged (lusol, :467-513, is the ilu0a pair of sweeps).
+// ILUT unchanged (lusol, :465-516, is the ilu0a pair of sweeps).
 #include "gbims_internal.cuh"
 #include "k_llword.cuh"
 #include <algorithm>

@@ -259,7 +259,7 @@ int or_pcu(int nja, int neq, int ipc, double relax, const double *amat,
   return icount;
 }
 
-/* sparskit2/ilut.f90:515-579, qsplit: partial quick-sort of a[0..n) by
+/* sparskit2/ilut.f90:519-581, qsplit: partial quick-sort of a[0..n) by
  * decreasing magnitude so that the ncut-th entry (1-based, as in the
  * reference) splits larger from smaller ones; ind moves with a. */
 static void or_qsplit(int n, double *a, int *ind, int ncut) {
@@ -283,7 +283,7 @@ static void or_qsplit(int n, double *a, int *ind, int ncut) {
   }
 }
 
-/* sparskit2/ilut.f90:48-465, ilut: dual-threshold incomplete LU with the
+/* sparskit2/ilut.f90:48-462, ilut: dual-threshold incomplete LU with the
  * MODFLOW changes (relaxation of the dropped sum, MILUT; pivot guard through
  * izero and delta).  Row ii keeps at most lfil L entries (|multiplier| above
  * droptol) and lfil - 1 U entries (|u| above droptol x the row's mean |a|),
@@ -958,7 +958,7 @@ int or_ilut_iwk(int neq, const int *ia, int level) {
 }
 
 /* ImsLinearBase.f90:1049-1092, ims_base_ilu0a: forward then backward solve.
- * sparskit2/ilut.f90:467-513 (lusol, the ILUT application) is the same
+ * sparskit2/ilut.f90:465-516 (lusol, the ILUT application) is the same
  * pair of sweeps over the ILUT storage. */
 void or_ilu0a(int nja, int neq, const double *apc, const int *iapc, const int *japc,
               const double *r, double *d) {
