@@ -419,7 +419,7 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
       if (h->ja[k] < 0 || h->ja[k] >= neq) { *out = h; return fail(h, GBIMS_ERR_ARG, "column index out of range"); }
   }
   // REORDERING_METHOD RCM/MD: LORDER (ims_base_calc_order) and the permuted
-  // pattern of dperm with job 1 (sparsekit.f90:249-447): row j becomes row
+  // pattern of dperm with job 1 (sparsekit.f90:163-447): row j becomes row
   // LORDER(j), its entries kept in order, columns relabelled by LORDER --
   // LORDER is the numbering's list of nodes, used as a new-index map, as
   // imslinear_ap passes it (ImsLinear.f90:653-658)
