@@ -16,7 +16,8 @@ namespace {
 struct MdWork {
   int n, mmax;
   std::vector<int> v, l, head, last, next;
-  int *mark;  // v(1:n)
+  int *mark;         // v(1:n)
+  bool bad = false;  // a degree out of range (malformed input)
   MdWork(int n_, int mmax_)
       : n(n_), mmax(mmax_), v(mmax_ + 1, 0), l(mmax_ + 1, 0), head(2 * n_ + 2, 0),
         last(n_ + 1, 0), next(n_ + 1, 0), mark(v.data()) {}
@@ -195,6 +196,10 @@ struct MdWork {
         }
         if (outmatched) continue;
       }
+      if (d < 1 || d > 2 * n) {  // a degree no quotient graph of n nodes has
+        bad = true;
+        return;
+      }
       next[w] = head[d];
       head[d] = w;
       last[w] = -d;
@@ -229,6 +234,7 @@ int md_order(int n, const std::vector<int> &ia, const std::vector<int> &ja,
     const int tail = W.merge(ek);
     W.purge(k, ek, tail);
     W.update(ek, dmin);
+    if (W.bad) return 8 * n + 2;
   }
   for (int u = 1; u <= n; ++u) lorder[-W.next[u] - 1] = u - 1;
   return 0;
