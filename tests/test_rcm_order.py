@@ -175,3 +175,24 @@ def test_md_reordered_solve_matches_natural_order():
         assert icnvg == 1
         xs.append(x)
     assert np.max(np.abs(xs[0] - xs[1])) <= 1e-7
+
+
+def test_calc_order_rejects_bad_arguments():
+    _lib = lib_or_skip()
+    lib = _lib.load()
+    ia, ja = grid_pattern(1, 3, 3)
+    n = ia.size - 1
+    lo, io = np.zeros(n, np.int32), np.zeros(n, np.int32)
+
+    def call(iord, ia_, ja_, nja=None):
+        iab = np.ascontiguousarray(ia_, np.int32)
+        jab = np.ascontiguousarray(ja_, np.int32)
+        return lib.gbims_calc_order(iord, n, int(ia_[-1]) if nja is None else nja, _lib.iptr(iab),
+                                    _lib.iptr(jab), 0, _lib.iptr(lo), _lib.iptr(io))
+
+    assert call(1, ia, ja) == 0 and call(2, ia, ja) == 0
+    assert call(3, ia, ja) == _lib.GBIMS_ERR_ARG                     # no such ordering
+    bad = ja.copy()
+    bad[3] = n                                                         # column out of range
+    assert call(1, ia, bad) == _lib.GBIMS_ERR_ARG
+    assert call(1, ia, ja, nja=int(ia[-1]) - 1) == _lib.GBIMS_ERR_ARG  # ia inconsistent with nja
