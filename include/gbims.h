@@ -214,9 +214,10 @@ const char *gbims_last_error(const gbims_handle *h);
 const char *gbims_status_string(int status);
 
 /* No counterpart in the reference: an entry point that allocates nothing,
- * for callers that must not allocate device memory (inside CUDA stream
- * capture, where cudaMalloc is not permitted, or a host whose device memory
- * is owned by its own memory manager).
+ * for callers that cannot call cudaMalloc themselves or through this library:
+ * a host whose device memory is owned by its own memory manager (an
+ * application that reserves the GPU's memory up front and hands out pieces of
+ * it, so that any further cudaMalloc would fail or fragment its pool).
  *
  * d = b - A x (the initial residual of an IMS solve, ims_base_residual,
  * ImsLinearBase.f90:1291-1312), its L2 norm (L2NORM0) and its signed max|d|
@@ -227,11 +228,12 @@ const char *gbims_status_string(int status);
  *
  * Limit: neq <= 155,648 rows (608 reduction blocks of 256 rows, held in a
  * static device array); larger systems get GBIMS_ERR_ARG.  Runs on `stream`
- * (a cudaStream_t, NULL = the legacy default stream) and returns after it
- * has finished.  The first call on a device looks up the static array and
- * loads the library's device code: make it before any stream capture.  The
- * static array is shared by all callers on a device: calls that overlap in
- * time (two host threads, or work on two streams in flight) race on it. */
+ * (a cudaStream_t, NULL = the legacy default stream); it copies its three
+ * results to the host and synchronizes `stream` before it returns.  The
+ * first call on a device looks up the static array and loads the library's
+ * device code: make it before any stream capture.  The static array is shared
+ * by all callers on a device: calls that overlap in time (two host threads,
+ * or work on two streams in flight) race on it. */
 int gbims_residual_noalloc(int neq, int nja, const int *d_ia, const int *d_ja,
                            const double *d_amat, const double *d_x, const double *d_rhs,
                            double *d_resid, int index_base, void *stream, double *l2norm,

@@ -405,7 +405,8 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
     if (v > 0.0 && v < 1.0) h->refine_factor = v;
   }
   // 0-based copies and checks: diagonal first in every row
-  int base = s->index_base ? 1 : 0;
+  if (s->index_base != 0 && s->index_base != 1) { *out = h; return fail(h, GBIMS_ERR_ARG, "index_base must be 0 or 1"); }
+  int base = s->index_base;
   h->ia.resize(neq + 1);
   h->ja.resize(nja);
   for (int i = 0; i <= neq; ++i) h->ia[i] = ia[i] - base;
@@ -985,7 +986,8 @@ extern "C" int gbims_calc_order(int iord, int neq, int nja, const int *ia, const
                                 int index_base, int *lorder, int *iorder) {
   if (neq <= 0 || nja < neq || !ia || !ja || !lorder || !iorder) return GBIMS_ERR_ARG;
   if (iord != 1 && iord != 2) return GBIMS_ERR_ARG;
-  const int base = index_base ? 1 : 0;
+  if (index_base != 0 && index_base != 1) return GBIMS_ERR_ARG;
+  const int base = index_base;
   std::vector<int> a(neq + 1), c(nja), lo;
   for (int i = 0; i <= neq; ++i) a[i] = ia[i] - base;
   if (a[0] != 0 || a[neq] != nja) return GBIMS_ERR_ARG;
@@ -1327,7 +1329,8 @@ extern "C" int gbims_batch_create(const gbims_settings *settings, int nmembers,
   if (!out) return GBIMS_ERR_ARG;
   *out = nullptr;
   if (!settings || !member_rows || nmembers <= 0 || neq <= 0) return GBIMS_ERR_ARG;
-  const int base = settings->index_base ? 1 : 0;
+  if (settings->index_base != 0 && settings->index_base != 1) return GBIMS_ERR_ARG;
+  const int base = settings->index_base;
   std::vector<int> mrow(nmembers + 1);
   for (int m = 0; m <= nmembers; ++m) mrow[m] = member_rows[m] - base;
   if (mrow[0] != 0 || mrow[nmembers] != neq) return GBIMS_ERR_ARG;

@@ -1,7 +1,11 @@
 // gbims_noalloc.cu -- gbims_residual_noalloc: the initial residual of an IMS
 // solve (d = b - A x, its L2 norm and signed max|d|; ims_base_residual and
 // dnrm2, src/Solution/LinearMethods/ImsLinearBase.f90:1291-1312) from the
-// caller's device arrays, allocating nothing.
+// caller's device arrays, allocating nothing.  It serves hosts whose device
+// memory is owned by their own memory manager (the GPU's memory reserved up
+// front and handed out in pieces), where a cudaMalloc by a library would fail
+// or fragment that pool.  The call copies its three results to the host and
+// synchronizes its stream before it returns.
 //
 // The reduction partials live in a file-scope device array sized for
 // kNoAllocBlocks blocks of 256 rows, so the call serves systems of at most

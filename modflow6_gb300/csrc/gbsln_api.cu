@@ -137,6 +137,7 @@ extern "C" int gbnpf_create(const gbnpf_options *opt, int nodes, int nja, int nj
   if (!opt || nodes <= 0 || nja < nodes || njas < 0 || !ia || !ja || !jas || !isym || !ihc ||
       !cl1 || !cl2 || !hwva || !top || !bot || !k11 || !k33 || !icelltype)
     return GBIMS_ERR_ARG;
+  if (opt->index_base != 0 && opt->index_base != 1) return GBIMS_ERR_ARG;
   gbnpf_handle *h = new (std::nothrow) gbnpf_handle();
   if (!h) return GBIMS_ERR_NOMEM;
   *out = h;
@@ -144,7 +145,7 @@ extern "C" int gbnpf_create(const gbnpf_options *opt, int nodes, int nja, int nj
   h->nodes = nodes;
   h->nja = nja;
   h->njas = njas;
-  int b = opt->index_base ? 1 : 0;
+  int b = opt->index_base;
   std::vector<int> ia0(ia, ia + nodes + 1), ja0(ja, ja + nja), jas0(jas, jas + nja), isym0(isym, isym + nja);
   for (auto &v : ia0) v -= b;
   for (auto &v : ja0) v -= b;

@@ -184,11 +184,12 @@ def test_calc_order_rejects_bad_arguments():
     n = ia.size - 1
     lo, io = np.zeros(n, np.int32), np.zeros(n, np.int32)
 
-    def call(iord, ia_, ja_, nja=None):
+    def call(iord, ia_, ja_, nja=None, base=0):
         iab = np.ascontiguousarray(ia_, np.int32)
         jab = np.ascontiguousarray(ja_, np.int32)
-        return lib.gbims_calc_order(iord, n, int(ia_[-1]) if nja is None else nja, _lib.iptr(iab),
-                                    _lib.iptr(jab), 0, _lib.iptr(lo), _lib.iptr(io))
+        return lib.gbims_calc_order(iord, n, int(ia_[-1]) - base if nja is None else nja,
+                                    _lib.iptr(iab), _lib.iptr(jab), base, _lib.iptr(lo),
+                                    _lib.iptr(io))
 
     assert call(1, ia, ja) == 0 and call(2, ia, ja) == 0
     assert call(3, ia, ja) == _lib.GBIMS_ERR_ARG                     # no such ordering
@@ -196,3 +197,5 @@ def test_calc_order_rejects_bad_arguments():
     bad[3] = n                                                         # column out of range
     assert call(1, ia, bad) == _lib.GBIMS_ERR_ARG
     assert call(1, ia, ja, nja=int(ia[-1]) - 1) == _lib.GBIMS_ERR_ARG  # ia inconsistent with nja
+    assert call(1, ia + 1, ja + 1, base=1) == 0                         # 1-based input
+    assert call(1, ia + 2, ja + 2, base=2) == _lib.GBIMS_ERR_ARG        # index_base neither 0 nor 1

@@ -3,7 +3,8 @@ handle-based entry points on the same system: its residual vector against
 b - gbims_matvec(x), its L2 norm against gbims_apply's L2NORM0, and its
 signed max|r| against the residual's own maximum -- bit for bit, on two
 calls in a row (the static scratch carries nothing from one call to the
-next).  Collected last so it also runs after every other GPU test.
+next) -- and the device's free memory unchanged across the second call.
+Collected last so it also runs after every other GPU test.
 """
 import ctypes as C
 
@@ -46,10 +47,17 @@ def test_residual_noalloc_matches_handle_entry_points(gblib, base):
            "rhs": torch.from_numpy(rhs).cuda(),
            "resid": torch.full((n,), np.nan, dtype=torch.float64, device="cuda")}
     torch.cuda.synchronize()
-    for _ in range(2):
+    for call in range(2):
         dev["resid"].fill_(np.nan)
+        torch.cuda.synchronize()
+        # the first call looks up the static array and loads the kernels; from
+        # the second on, the device's free memory must not move
+        free_before = torch.cuda.mem_get_info()[0]
         rc, l2, rmax, locr = _noalloc(gblib, n, nja, dev, base)
+        free_after = torch.cuda.mem_get_info()[0]
         assert rc == _lib.GBIMS_OK
+        if call > 0:
+            assert free_after == free_before
         np.testing.assert_array_equal(dev["resid"].cpu().numpy(), r_ref)
         assert l2 == l2_ref
         assert locr == loc_ref and rmax == r_ref[loc_ref]
