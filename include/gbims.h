@@ -59,9 +59,15 @@ typedef struct gbims_settings {
                        (GBIMS_ERR_UNSUPPORTED beyond) */
   int precision;    /* GBIMS_FP64 or GBIMS_MIXED */
   int index_base;   /* 0 (C) or 1 (Fortran) for ia/ja */
-  int nlay, nrow, ncol; /* optional DIS shape; enables the structured
-                           (7-point) triangular-sweep kernels when the CSR
-                           pattern matches a full DIS grid.  0 = none. */
+  int nlay, nrow, ncol; /* DIS shape for the structured (7-point) wavefront
+                           sweeps and the index-free product, used when the
+                           CSR pattern is that of a full DIS grid in natural
+                           order.  All three 0: the shape is found from the
+                           pattern (row 0's neighbour offsets 1, ncol,
+                           nrow*ncol, then every row checked), so a caller
+                           that passes only IA/JA, as imslinear_ar does,
+                           reaches the structured path.  nlay < 0: never (the
+                           level-scheduled sweeps on the general pattern). */
 } gbims_settings;
 
 /* Convergence summary of the last apply (ConvergenceSummary.f90 fields for a
@@ -249,6 +255,9 @@ typedef struct gbnpf_options {
   int icellavg;     /* ALTERNATIVE_CELL_AVERAGING: 0 harmonic, 1 log, 2 AMT-LMK, 3 AMT-HMK */
   double satomega;  /* Newton saturation smoothing (default 1e-6) */
   int index_base;   /* 0 or 1 for the index arrays */
+  int inewtonur;    /* NEWTON UNDER_RELAXATION (gwf.f90:181, gwf_nur :717): heads
+                       that fall below the bottom of their column are pulled back
+                       (npf_nur) by gbsln_timestep; needs inewton */
 } gbnpf_options;
 
 typedef struct gbnpf_handle gbnpf_handle;

@@ -57,6 +57,7 @@ class GbnpfOptions(C.Structure):
     _fields_ = [
         ("inewton", C.c_int), ("ivarcv", C.c_int), ("idewatcv", C.c_int),
         ("icellavg", C.c_int), ("satomega", C.c_double), ("index_base", C.c_int),
+        ("inewtonur", C.c_int),
     ]
 
 

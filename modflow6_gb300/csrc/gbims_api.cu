@@ -547,9 +547,14 @@ extern "C" int gbims_create(const gbims_settings *s, int neq, int nja, const int
   }
   // optional structured 7-point sweeps (and the index-free SpMV); the
   // wavefront sweeps carry the ILU0 pattern only
-  if (h->ipc < 3 && s->nlay > 0 && s->nrow > 0 && s->ncol > 0 &&
-      dia7_matches(s->nlay, s->nrow, s->ncol, neq, h->ia, h->ja)) {
-    std::vector<int> shape = {s->nlay, s->nrow, s->ncol};
+  int dl = s->nlay, dr = s->nrow, dc = s->ncol;
+  bool dis = false;
+  if (h->ipc < 3 && dl >= 0) {
+    if (dl == 0 && dr == 0 && dc == 0) dis = dia7_detect(neq, h->ia, h->ja, &dl, &dr, &dc);
+    else dis = dl > 0 && dr > 0 && dc > 0 && dia7_matches(dl, dr, dc, neq, h->ia, h->ja);
+  }
+  if (dis) {
+    std::vector<int> shape = {dl, dr, dc};
     int rc = setup_structured(h, shape, std::vector<long long>{0});
     if (rc != GBIMS_OK) return rc;
     GB_CUDA(h, dalloc(&h->D.d_sv, (size_t)7 * neq));
@@ -1337,7 +1342,8 @@ extern "C" int gbims_batch_create(const gbims_settings *settings, int nmembers,
   for (int m = 0; m < nmembers; ++m)
     if (mrow[m + 1] <= mrow[m]) return GBIMS_ERR_ARG;
   gbims_settings s = *settings;
-  s.nlay = s.nrow = s.ncol = 0;  // members are swept by the level schedule of the whole batch
+  s.nlay = -1;  // members are swept by the level schedule of the whole batch
+  s.nrow = s.ncol = 0;
   int rc = gbims_create(&s, neq, nja, ia, ja, out);
   gbims_handle *h = *out;
   if (rc != GBIMS_OK) return rc;

@@ -248,6 +248,10 @@ void launch_ilu_apply_levels32(int n, const int *d_iapc, const int *d_japc,
 
 bool dia7_matches(int nlay, int nrow, int ncol, int n, const std::vector<int> &ia,
                   const std::vector<int> &ja);
+// The DIS shape of a 0-based CSR pattern that is a full 7-point grid in
+// natural order (false if it is not one).
+bool dia7_detect(int n, const std::vector<int> &ia, const std::vector<int> &ja, int *nlay,
+                 int *nrow, int *ncol);
 void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_japc,
                          const double *d_apc, bool mixed, cudaStream_t st);
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,

@@ -233,6 +233,7 @@ extern "C" int gbnpf_destroy(gbnpf_handle *h) {
 struct gbsln_handle {
   int nlay = 0, nrow = 0, ncol = 0, n = 0, nja = 0;
   gbsln_nonlinear nl{};
+  bool inewtonur = false;  // NEWTON UNDER_RELAXATION
   gbims_settings ims_s{};
   NpfStore d;
   NpfDev g{};
@@ -401,6 +402,7 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
   h->g.idewatcv = npf->idewatcv;
   h->g.icellavg = npf->icellavg;
   h->g.satomega = npf->satomega > 0 ? npf->satomega : 1.0e-6;
+  h->inewtonur = npf->inewton && npf->inewtonur;
   SLN_CUDA(h, cudaMemcpyAsync(h->x, strt, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
   gwf_condsat(n, h->g, h->d.condsat, h->st);
   SLN_CUDA(h, cudaStreamSynchronize(h->st));
@@ -612,7 +614,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
       } else {
         gwf_calcdx(n, h->ibound, h->x, h->xtemp, h->dxold, h->st);
       }
-      if (h->g.inewton) {
+      if (h->inewtonur) {  // gwf_nur (gwf.f90:717): NEWTON UNDER_RELAXATION only
         SLN_CUDA(h, cudaMemsetAsync(h->flag, 0, sizeof(int), h->st));
         gwf_npf_nur(n, (int)((long long)h->nrow * h->ncol), h->nlay, h->g, h->ibound, h->x,
                     h->xtemp, h->dxold, h->flag, h->st);

@@ -582,6 +582,33 @@ bool dia7_matches(int nlay, int nrow, int ncol, int n, const std::vector<int> &i
   return true;
 }
 
+bool dia7_detect(int n, const std::vector<int> &ia, const std::vector<int> &ja, int *nlay,
+                 int *nrow, int *ncol) {
+  if (n < 2 || (int)ia.size() != n + 1) return false;
+  // row 0 of a natural-order DIS grid has only upper neighbours, at offsets
+  // 1 (next column), ncol (next row) and nrow*ncol (next layer), each present
+  // when its dimension exceeds one.  A grid with a dimension of one has the
+  // pattern of a smaller-rank grid, which the sweeps treat alike.
+  std::vector<long long> off;
+  for (int q = ia[0] + 1; q < ia[1]; ++q) off.push_back(ja[q]);
+  long long l = 1, r = 1, c = n;
+  if (off.size() == 1 && off[0] == 1) {
+    l = 1; r = 1; c = n;
+  } else if (off.size() == 2 && off[0] == 1 && off[1] > 1 && n % off[1] == 0) {
+    l = 1; r = n / off[1]; c = off[1];
+  } else if (off.size() == 3 && off[0] == 1 && off[1] > 1 && off[2] > off[1] &&
+             off[2] % off[1] == 0 && n % off[2] == 0) {
+    l = n / off[2]; r = off[2] / off[1]; c = off[1];
+  } else {
+    return false;
+  }
+  if (!dia7_matches((int)l, (int)r, (int)c, n, ia, ja)) return false;
+  *nlay = (int)l;
+  *nrow = (int)r;
+  *ncol = (int)c;
+  return true;
+}
+
 // Geometry of the skewed layout of one precision.
 void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, long long *slots) {
   const int S = fp32 ? kSOf<float> : kSOf<double>;

@@ -113,6 +113,10 @@ class GwfDisModel:
     rch_node: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     rch_rate: np.ndarray = field(default_factory=lambda: np.zeros(0))
     inewton: int = 0
+    inewtonur: int = 0      # NEWTON UNDER_RELAXATION (gwf.f90:181)
+    ivarcv: int = 0         # NPF VARIABLECV
+    idewatcv: int = 0       # NPF VARIABLECV DEWATERED
+    icellavg: int = 0       # ALTERNATIVE_CELL_AVERAGING: 0 harmonic, 1 LOGARITHMIC, 2 AMT-LMK, 3 AMT-HMK
     name: str = ""
 
     @property

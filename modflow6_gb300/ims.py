@@ -16,6 +16,8 @@ import numpy as np
 from . import _lib
 
 CG_METHOD = 1
+# `structure` value that keeps the level-scheduled sweeps on a DIS pattern
+GENERAL = (-1, 0, 0)
 BCGS_METHOD = 2
 
 EXIT_REASONS = {0: "none", 1: "closure", 2: "stagnation", 3: "itmax", 4: "exact", 5: "zero rho"}
@@ -37,7 +39,9 @@ class ImsLinearSettings:
     level: int = 0               # PRECONDITIONER_LEVELS
     droptol: float = 0.0         # PRECONDITIONER_DROP_TOLERANCE
     precision: int = _lib.GBIMS_FP64
-    structure: tuple = field(default=(0, 0, 0))  # optional (nlay, nrow, ncol) of a DIS grid
+    # (nlay, nrow, ncol) of a DIS grid for the wavefront sweeps; (0, 0, 0):
+    # found from the pattern; GENERAL: the level-scheduled sweeps always
+    structure: tuple = field(default=(0, 0, 0))
 
     @classmethod
     def preset_config(cls, complexity: str, **overrides) -> "ImsLinearSettings":

@@ -110,7 +110,8 @@ class GwfSolution:
                              int(m.chd_node.size), _lib.iptr(keep["chd_node"]), _lib.dptr(keep["chd_head"]),
                              int(m.wel_node.size), _lib.iptr(keep["wel_node"]), _lib.dptr(keep["wel_q"]),
                              int(m.rch_node.size), _lib.iptr(keep["rch_node"]), _lib.dptr(keep["rch_rate"]))
-        npf = _lib.GbnpfOptions(int(m.inewton), 0, 0, 0, satomega, 0)
+        npf = _lib.GbnpfOptions(int(m.inewton), int(m.ivarcv), int(m.idewatcv), int(m.icellavg),
+                                satomega, 0, int(m.inewtonur))
         cs = ims.to_c(0)
         cnl = _lib.GbslnNonlinear(nl.dvclose, nl.mxiter, nl.nonmeth, nl.theta, nl.akappa, nl.gamma,
                                   nl.amomentum, nl.iallowptc, nl.numtrack, nl.btol, nl.breduc,

@@ -911,7 +911,7 @@ int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
       if (nl->nonmeth > 0) or_sln_underrelax(nl, kiter, hncg, neq, ibound, x, xtemp);
       else
         for (int n = 0; n < neq; ++n) nl->dxold[n] = (ibound[n] < 1) ? 0.0 : x[n] - xtemp[n];
-      if (m->inewton) {
+      if (m->inewton && m->inewtonur) { /* gwf_nur, gwf.f90:717 */
         int inewtonur = 0, locmax = -1;
         double dxmax_nur = 0.0;
         or_npf_nur(m, ibound, x, xtemp, nl->dxold, &inewtonur, &dxmax_nur, &locmax);

@@ -22,6 +22,9 @@ typedef struct {
   const int *icelltype;
   int inewton, ivarcv, idewatcv, icellavg;
   double satomega;
+  /* NEWTON UNDER_RELAXATION (gwf.f90:181): npf_nur runs only when it is set
+   * together with inewton (gwf_nur, gwf.f90:717) */
+  int inewtonur;
   /* storage */
   const double *ss, *sy;
   const int *iconvert;

@@ -48,7 +48,7 @@ class GwfModel(C.Structure):
                 ("top", _dp), ("bot", _dp), ("area", _dp), ("k11", _dp), ("k33", _dp),
                 ("icelltype", _ip), ("inewton", C.c_int), ("ivarcv", C.c_int),
                 ("idewatcv", C.c_int), ("icellavg", C.c_int), ("satomega", C.c_double),
-                ("ss", _dp), ("sy", _dp), ("iconvert", _ip),
+                ("inewtonur", C.c_int), ("ss", _dp), ("sy", _dp), ("iconvert", _ip),
                 ("nwel", C.c_int), ("wel_node", _ip), ("wel_q", _dp),
                 ("nrch", C.c_int), ("rch_node", _ip), ("rch_rate", _dp),
                 ("nchd", C.c_int), ("chd_node", _ip), ("chd_head", _dp)]
@@ -325,7 +325,9 @@ class Gwf:
             i(con["ia"]), i(con["ja"]), i(con["isym"]), i(con["jas"]), i(con["ihc"]),
             d(con["cl1"]), d(con["cl2"]), d(con["hwva"]),
             d(m.cell_top), d(m.cell_bot), d(m.area), d(m.k11), d(m.k33), i(m.icelltype),
-            int(m.inewton), 0, 0, 0, satomega, d(ss), d(sy), i(m.icelltype),
+            int(m.inewton), int(getattr(m, "ivarcv", 0)), int(getattr(m, "idewatcv", 0)),
+            int(getattr(m, "icellavg", 0)), satomega, int(getattr(m, "inewtonur", 0)),
+            d(ss), d(sy), i(m.icelltype),
             int(m.wel_node.size), i(m.wel_node), d(m.wel_q),
             int(m.rch_node.size), i(m.rch_node), d(m.rch_rate),
             int(m.chd_node.size), i(m.chd_node), d(m.chd_head))

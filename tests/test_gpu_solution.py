@@ -8,9 +8,9 @@ import pytest
 
 import oracle
 from modflow6_gb300.dis import make_config
-from modflow6_gb300.ims import ImsLinearSettings
+from modflow6_gb300.ims import GENERAL, ImsLinearSettings
 from modflow6_gb300.solution import GwfSolution, Nonlinear
-from test_oracle_known_answers import chd01_model, newton01_model
+from test_oracle_known_answers import BUMP_IMS, BUMP_OUTER, bump_model, chd01_model, newton01_model
 
 pytestmark = pytest.mark.gpu
 
@@ -64,6 +64,31 @@ def test_newton01_known_answer_gpu(gblib):
     assert np.isclose(x[13], 7.0), x[13]
 
 
+@pytest.mark.parametrize("structured", [False, True])
+def test_newton_under_relaxation_bump_matches_mf6_heads_gpu(gblib, structured):
+    """The device time step against heads written by MODFLOW 6 itself
+    (autotest/test_gwf_newton_under_relaxation.py, case nr_ur01, with its own
+    np.allclose check), on the level-scheduled and the wavefront sweeps; and
+    against the oracle's heads."""
+    m, mf6_heads = bump_model()
+    shape = (m.nlay, m.nrow, m.ncol) if structured else GENERAL
+    o = dict(BUMP_OUTER)
+    nl = Nonlinear(dvclose=o["dvclose"], mxiter=o["mxiter"], nonmeth=o["nonmeth"],
+                   iallowptc=o["iallowptc"])
+    sol = GwfSolution(m, ImsLinearSettings(structure=shape, **BUMP_IMS), nl)
+    st = sol.timestep(1, 1, 1.0)
+    assert st["converged"] == 1
+    x = sol.heads
+    assert np.allclose(mf6_heads, x)
+    assert np.max(np.abs(x - mf6_heads)) <= 5e-8
+    g = oracle.Gwf(m, oracle.settings(**BUMP_IMS))
+    so = g.timestep(kper=1, kstp=1, delt=1.0, transient=False, **BUMP_OUTER)
+    # the GPU's reductions sum in another order, so the Newton path may take a
+    # few outer iterations more or fewer on the way to the same heads
+    assert so["converged"] == 1 and abs(st["outer"] - so["outer"]) <= 5
+    assert np.max(np.abs(x - g.x)) <= 5e-8
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_c3_small_transient_newton(gblib, precision):
     m = make_config("c3", seed=1, scale=0.04)
@@ -89,9 +114,12 @@ def test_c2_full_size_matches_oracle_record(gblib):
     full solve (tests/golden/c2_oracle_reference.json, made by
     tests/golden/make_c2_reference.py): the same outer iterations, inner
     iterations within 1 % (the wavefront's backward sweep rounds differently
-    from ilu0a, see the structured tests), and heads that agree through
+    from ilu0a, see the structured tests), heads that agree through
     size-independent statistics (mean within 1e-5 m, minimum and maximum
-    within 1e-4 m)."""
+    within 1e-4 m), and, cell by cell, heads within 0.1 x INNER_DVCLOSE of
+    the oracle's on the recorded sample (tests/golden/
+    c2_oracle_heads_sample.npz: every WEL cell, every cell beside a CHD face
+    and 100,000 further cells)."""
     import json
     from pathlib import Path
     from modflow6_gb300.workloads import C2_IMS, C2_OUTER
@@ -109,6 +137,10 @@ def test_c2_full_size_matches_oracle_record(gblib):
         (st["inner_total"], rec["stats"]["inner_total"])
     assert abs(h.sum() - rec["head_checksum"]) <= 1e-5 * m.nodes
     assert abs(h.min() - rec["head_min"]) <= 1e-4 and abs(h.max() - rec["head_max"]) <= 1e-4
+    smp = np.load(Path(__file__).parent / "golden" / "c2_oracle_heads_sample.npz")
+    assert np.isin(m.wel_node, smp["cells"]).all()
+    err = np.abs(h[smp["cells"]] - smp["heads"])
+    assert err.max() <= 0.1 * C2_IMS["dvclose"], (err.max(), int(smp["cells"][err.argmax()]))
 
 
 def _budget_pair(m, sol, g, delt, hold):
@@ -175,7 +207,7 @@ def test_backtracking_matches_oracle(gblib):
     g = oracle.Gwf(m, oracle.settings(**tol))
     nl = Nonlinear(dvclose=1e-5, mxiter=100, nonmeth=3, theta=0.8, akappa=1e-4, gamma=0.0,
                    numtrack=20, btol=1.05, breduc=0.1, res_lim=0.002)
-    sol = GwfSolution(m, ImsLinearSettings(**tol), nl)
+    sol = GwfSolution(m, ImsLinearSettings(structure=GENERAL, **tol), nl)
     delt = 10.0
     bt_o = bt_g = 0
     for kstp in range(1, 4):

@@ -141,3 +141,54 @@ def test_autotuned_solve_reaches_the_same_closure(gblib):
     assert r1.icnvg == 1 and r2.icnvg == 1
     assert abs(r1.in_iter - r2.in_iter) <= 2
     assert np.max(np.abs(x1 - x2)) <= 0.1 * tol["dvclose"]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_dis_shape_found_from_the_pattern(gblib, shape):
+    """A caller that passes only IA/JA (as imslinear_ar does) reaches the
+    wavefront sweeps: the shape is found from the pattern, and the
+    preconditioner equals, bit for bit, the one built with the shape given
+    (a grid with a dimension of one has the pattern of a smaller-rank grid,
+    which sweeps the same cells in the same order)."""
+    m, con, amat, rhs, x0 = dis_system(*shape)
+    v = np.random.default_rng(6).standard_normal(m.nodes)
+    out = []
+    for st in (shape, (0, 0, 0)):
+        ims = ImsLinear(ImsLinearSettings(structure=st)).imslinear_allocate(m.nodes, con["ia"], con["ja"])
+        assert gblib.gbims_factor(ims._h, _lib.dptr(amat), None) == 0
+        z = np.zeros_like(v)
+        assert gblib.gbims_precondition(ims._h, _lib.dptr(v), _lib.dptr(z)) == 0
+        r = ims.imslinear_apply(amat.copy(), rhs.copy(), x0.copy())
+        assert r.summary["structured"] == (1 if m.nodes > 1 else 0)
+        out.append(z)
+    np.testing.assert_array_equal(out[0], out[1])
+
+
+def test_reduced_pattern_keeps_the_level_sweeps(gblib):
+    """A pattern that is not a full DIS grid (one cell cut out, as IDOMAIN
+    does) keeps the level-scheduled sweeps; so does structure GENERAL on a
+    full grid."""
+    from modflow6_gb300.ims import GENERAL
+    m, con, amat, rhs, x0 = dis_system(2, 9, 8)
+    ia, ja = con["ia"], con["ja"]
+    cut = 37
+    keep = np.ones(m.nodes, bool)
+    keep[cut] = False
+    new = np.cumsum(keep) - 1
+    rows = []
+    for r in np.flatnonzero(keep):
+        cols = [new[c] for c in ja[ia[r]:ia[r + 1]] if keep[c]]
+        rows.append(cols)
+    ia2 = np.concatenate([[0], np.cumsum([len(c) for c in rows])]).astype(np.int32)
+    ja2 = np.concatenate(rows).astype(np.int32)
+    n2 = keep.sum()
+    a2 = np.zeros(ja2.size)
+    for r in range(n2):
+        a2[ia2[r]] = 6.0
+        a2[ia2[r] + 1:ia2[r + 1]] = -1.0
+    ims = ImsLinear(ImsLinearSettings(structure=(0, 0, 0))).imslinear_allocate(int(n2), ia2, ja2)
+    res = ims.imslinear_apply(a2, np.ones(n2), np.zeros(n2))
+    assert res.summary["structured"] == 0
+    ims = ImsLinear(ImsLinearSettings(structure=GENERAL)).imslinear_allocate(m.nodes, ia, ja)
+    res = ims.imslinear_apply(amat.copy(), rhs.copy(), x0.copy())
+    assert res.summary["structured"] == 0
