@@ -114,6 +114,31 @@ int gbims_apply_device(gbims_handle *h, double *d_amat, double *d_rhs, double *d
 /* Replaces ImsLinearDataType%imslinear_da. */
 int gbims_destroy(gbims_handle *h);
 
+/* Per-inner-iteration convergence records, the NCONV, CONVNMOD, CONVMODSTART
+ * and CACCEL arguments of imslinear_ap (ImsLinear.f90:617-633) and the rows
+ * ims_base_cg / ims_base_bcgs write into the solution's ConvergenceSummary
+ * (ImsLinearBase.f90:141-197, 431-493), which feed CSV_INNER_OUTPUT
+ * (NumericalSolution.f90:2060-2200).
+ *
+ * gbims_set_inner_records: from the next apply on, keep up to nconv records
+ * per apply (nconv = 0 switches them off).  convmodstart (convnmod + 1
+ * entries, in the handle's index_base) gives the first row of each model and
+ * ends at neq + index_base, as CONVMODSTART does.  FP64 PCG and BiCGSTAB on a
+ * single system (GBIMS_ERR_UNSUPPORTED for the mixed form and batches).
+ *
+ * gbims_get_inner_records: the records of the last apply, at most cap of
+ * them (*nrec gets the count): itinner (ITINNER, the inner iteration),
+ * alpha and omega (CACCEL: PCG alpha, omega 0; BiCGSTAB alpha and omega),
+ * and per model (arrays [nrec][convnmod], model fastest, the layout of the
+ * reference's convdvmax(im, n)): the signed largest head change dvmax with
+ * its row locdv and the signed largest residual rmax with its row locr, rows
+ * in the handle's index_base (index_base - 1 when no row of the model
+ * changed).  Rows are those of the system the solver iterates on (the
+ * permuted one under REORDERING_METHOD), as in the reference. */
+int gbims_set_inner_records(gbims_handle *h, int nconv, int convnmod, const int *convmodstart);
+int gbims_get_inner_records(gbims_handle *h, int cap, int *nrec, int *itinner, double *alpha,
+                            double *omega, int *locdv, double *dvmax, int *locr, double *rmax);
+
 /* Batched ensembles (no counterpart in the reference, which solves one
  * simulation at a time): nmembers independent systems concatenated into one
  * block-diagonal system.  member_rows (nmembers+1, index_base) gives each

@@ -122,6 +122,9 @@ _SIGS = {
     "gbims_factor": (C.c_int, [C.c_void_p, _dp, _ip]),
     "gbims_get_apc": (C.c_int, [C.c_void_p, _dp]),
     "gbims_get_factor": (C.c_int, [C.c_void_p, _ip, _ip, _dp, C.c_int, _ip]),
+    "gbims_set_inner_records": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _ip]),
+    "gbims_get_inner_records": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp, _dp, _ip, _dp, _ip,
+                                          _dp]),
     "gbims_calc_order": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, C.c_int, _ip, _ip]),
     "gbims_matvec": (C.c_int, [C.c_void_p, _dp, _dp]),
     "gbims_precondition": (C.c_int, [C.c_void_p, _dp, _dp]),

@@ -45,6 +45,13 @@ struct gbims_handle {
   int *d_cptr = nullptr, *d_cpos = nullptr;
   double *d_part = nullptr;
   int G = 1;
+  // per-inner-iteration records (gbims_set_inner_records): capacity per
+  // apply, models, their first rows (0-based, nmod+1), the record rows, the
+  // per-model partials and the locations carried between iterations
+  int rec_cap = 0, rec_nmod = 0, rec_G = 0;
+  int *d_modstart = nullptr;
+  double *d_rec = nullptr, *d_rec_part = nullptr;
+  long long *d_rec_loc = nullptr;
   Ctl *d_ctl = nullptr, *h_ctl = nullptr;
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -209,6 +216,9 @@ static void enqueue_iteration(gbims_handle *h, unsigned long long cond, int use_
     kr_dot64(n, h->v_p, h->v_q, part, G, c, st);
     kr_ctl_alpha(c, part, G, st);
     kr_cg_update64(n, h->d_x, h->v_d, h->v_p, h->v_q, part, G, c, st);
+    if (h->rec_cap > 0 && h->rec_nmod > 1)
+      kr_rec_models(false, h->rec_nmod, h->d_modstart, h->v_p, nullptr, h->v_d, nullptr,
+                    h->d_rec_part, h->rec_G, c, st);
     kr_ctl_cg_cnvg(c, part, G, cond, use_cond, st);
     residual64(h, c, 1);
   } else if (!h->mixed && h->bcgs) {
@@ -226,6 +236,9 @@ static void enqueue_iteration(gbims_handle *h, unsigned long long cond, int use_
     kr_dot_tq_tt64(n, h->v_t, h->v_q, part, G, c, st);
     kr_ctl_omega(c, part, G, st);
     kr_bcgs_update64(n, h->d_x, h->v_d, h->v_phat, h->v_qhat, h->v_q, h->v_t, h->d_dscale, part, G, c, st);
+    if (h->rec_cap > 0 && h->rec_nmod > 1)
+      kr_rec_models(true, h->rec_nmod, h->d_modstart, h->v_phat, h->v_qhat, h->v_d, h->d_dscale,
+                    h->d_rec_part, h->rec_G, c, st);
     kr_ctl_bcgs_cnvg(c, part, G, cond, use_cond, st);
     residual64(h, c, 1);
   } else if (h->mixed && !h->bcgs) {
@@ -853,6 +866,14 @@ static int apply_core(gbims_handle *h, int kstp, int kiter, int *icnvg, int *in_
   c.iter = 1;
   c.first = 1;
   c.pivot_fail = INT_MAX;
+  if (h->rec_cap > 0 && !h->mixed && h->nm == 0) {
+    c.rec = h->d_rec;
+    c.rec_part = h->d_rec_part;
+    c.rec_loc = h->d_rec_loc;
+    c.rec_cap = h->rec_cap;
+    c.rec_nmod = h->rec_nmod;
+    c.rec_G = h->rec_G;
+  }
   *h->h_ctl = c;
   GB_CUDA(h, cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
   // D, P, Q, Z = 0 ; D = B - A X ; L2NORM0 (ImsLinear.f90:686-703)
@@ -1273,6 +1294,82 @@ extern "C" int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times 
   return GBIMS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// per-inner-iteration records (imslinear_ap's NCONV, CONVNMOD, CONVMODSTART,
+// CACCEL and the ConvergenceSummary rows, ImsLinear.f90:617-633,
+// ImsLinearBase.f90:141-197 and :431-493)
+// ---------------------------------------------------------------------------
+extern "C" int gbims_set_inner_records(gbims_handle *h, int nconv, int convnmod,
+                                       const int *convmodstart) {
+  if (!h) return GBIMS_ERR_ARG;
+  if (!h->d_ctl) return fail(h, GBIMS_ERR_STATE, "handle was not created successfully");
+  if (nconv < 0) return fail(h, GBIMS_ERR_ARG, "nconv must be >= 0");
+  if (nconv > 0 && (h->mixed || h->nm > 0))
+    return fail(h, GBIMS_ERR_UNSUPPORTED, "inner records: single FP64 systems only");
+  std::vector<int> ms;
+  if (nconv > 0) {
+    if (convnmod < 1 || !convmodstart) return fail(h, GBIMS_ERR_ARG, "convnmod >= 1 and convmodstart are required");
+    const int base = h->s.index_base;
+    ms.resize(convnmod + 1);
+    for (int m = 0; m <= convnmod; ++m) ms[m] = convmodstart[m] - base;
+    if (ms[0] != 0 || ms[convnmod] != h->n)
+      return fail(h, GBIMS_ERR_ARG, "convmodstart must run from index_base to neq+index_base");
+    for (int m = 0; m < convnmod; ++m)
+      if (ms[m + 1] <= ms[m]) return fail(h, GBIMS_ERR_ARG, "convmodstart must increase");
+  }
+  GB_CUDA(h, cudaStreamSynchronize(h->st));
+  for (void *p : {(void *)h->d_modstart, (void *)h->d_rec, (void *)h->d_rec_part, (void *)h->d_rec_loc})
+    if (p) cudaFree(p);
+  h->d_modstart = nullptr;
+  h->d_rec = h->d_rec_part = nullptr;
+  h->d_rec_loc = nullptr;
+  h->rec_cap = h->rec_nmod = h->rec_G = 0;
+  drop_graph(h);  // the loop body gains or loses the record kernel
+  if (nconv == 0) return GBIMS_OK;
+  h->rec_nmod = convnmod;
+  h->rec_G = std::max(1, std::min(h->G, (h->n + kRedBlock - 1) / kRedBlock));
+  GB_CUDA(h, dalloc(&h->d_modstart, (size_t)convnmod + 1));
+  GB_CUDA(h, dalloc(&h->d_rec, (size_t)nconv * (3 + 4 * convnmod)));
+  GB_CUDA(h, dalloc(&h->d_rec_part, (size_t)4 * convnmod * h->rec_G));
+  GB_CUDA(h, dalloc(&h->d_rec_loc, (size_t)2 * convnmod));
+  GB_CUDA(h, cudaMemcpy(h->d_modstart, ms.data(), sizeof(int) * (convnmod + 1), cudaMemcpyHostToDevice));
+  std::vector<long long> none(2 * convnmod, -1);
+  GB_CUDA(h, cudaMemcpy(h->d_rec_loc, none.data(), sizeof(long long) * 2 * convnmod, cudaMemcpyHostToDevice));
+  h->rec_cap = nconv;
+  return GBIMS_OK;
+}
+
+extern "C" int gbims_get_inner_records(gbims_handle *h, int cap, int *nrec, int *itinner,
+                                       double *alpha, double *omega, int *locdv, double *dvmax,
+                                       int *locr, double *rmax) {
+  if (!h || !nrec || cap < 0) return GBIMS_ERR_ARG;
+  *nrec = 0;
+  if (h->rec_cap == 0 || !h->h_ctl) return GBIMS_OK;
+  const int nm = h->rec_nmod, stride = 3 + 4 * nm;
+  const int have = std::min(h->h_ctl->rec_count, h->rec_cap);
+  const int k = std::min(have, cap);
+  if (k > 0 && (!itinner || !alpha || !omega || !locdv || !dvmax || !locr || !rmax))
+    return fail(h, GBIMS_ERR_ARG, "record arrays are required");
+  std::vector<double> buf((size_t)k * stride);
+  if (k > 0)
+    GB_CUDA(h, cudaMemcpy(buf.data(), h->d_rec, sizeof(double) * buf.size(), cudaMemcpyDeviceToHost));
+  const int base = h->s.index_base;
+  for (int r = 0; r < k; ++r) {
+    const double *row = &buf[(size_t)r * stride];
+    itinner[r] = (int)row[0];
+    alpha[r] = row[1];
+    omega[r] = row[2];
+    for (int im = 0; im < nm; ++im) {
+      dvmax[r * nm + im] = row[3 + 4 * im];
+      locdv[r * nm + im] = (int)row[4 + 4 * im] + base;
+      rmax[r * nm + im] = row[5 + 4 * im];
+      locr[r * nm + im] = (int)row[6 + 4 * im] + base;
+    }
+  }
+  *nrec = k;
+  return GBIMS_OK;
+}
+
 extern "C" int gbims_destroy(gbims_handle *h) {
   if (!h) return GBIMS_OK;
   if (h->st) cudaStreamSynchronize(h->st);
@@ -1291,7 +1388,8 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->LW.fwd, h->LW.bwd, h->LW.ticket, h->LW.err, h->d_ctl, h->I.lcol,
                   h->I.lval, h->I.ucol, h->I.uval, h->I.nl, h->I.nu, h->I.dinv, h->I.rdone,
                   h->I.stat, h->d_lorder, h->d_iorder, h->d_asrc, h->d_ia_u, h->d_ja_u,
-                  h->u_amat, h->u_rhs, h->u_x};
+                  h->u_amat, h->u_rhs, h->u_x, h->d_modstart, h->d_rec, h->d_rec_part,
+                  h->d_rec_loc};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);

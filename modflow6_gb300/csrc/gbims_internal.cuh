@@ -43,6 +43,15 @@ struct Ctl {
   int bodies;         // loop bodies executed in this solve
   int guard_tripped;  // the body limit ended the loop
   int restart_due;    // mixed form: the pending true-residual check restarts the recurrence
+  // Per-inner-iteration records (gbims_set_inner_records; rec == nullptr:
+  // off).  Row r of rec (stride 3 + 4*rec_nmod): iteration, alpha, omega,
+  // then per model dvmax, locdv, rmax, locr.  rec_part holds the per-model
+  // block partials of k_rec_models (rec_nmod > 1); rec_loc the per-model
+  // locations carried from one iteration to the next (2*rec_nmod).
+  double *rec;
+  const double *rec_part;
+  long long *rec_loc;
+  int rec_cap, rec_nmod, rec_G, rec_count;
 };
 
 // A batched ensemble on the device: members concatenated into one

@@ -451,6 +451,98 @@ __device__ void ctl_finish_update(Ctl *ctl, const double *part, int G) {
   }
 }
 
+// Per-model maxima of one iteration for the inner records, when the solution
+// has more than one model (CONVNMOD > 1; ImsLinearBase.f90:141-182 for PCG,
+// :431-480 for BiCGSTAB): for each model's rows, the largest head change
+// (the step the update kernel added: PCG alpha*p, BiCGSTAB alpha*phat +
+// omega*qhat, times DSCALE when scaled) and the largest residual (divided by
+// DSCALE when scaled), signed, with its row.  The step is recomputed with the
+// update kernel's own expression, so the values are the ones the update
+// compared.  Partial slots per model im: [4im] dx value, [4im+1] its row,
+// [4im+2] r value, [4im+3] its row (G blocks each).
+template <bool BCGS>
+__global__ void __launch_bounds__(kRedBlock) k_rec_models(int nm, const int *__restrict__ modstart,
+                                                          const double *__restrict__ p,
+                                                          const double *__restrict__ q,
+                                                          const double *__restrict__ d,
+                                                          const double *__restrict__ dscale,
+                                                          double *__restrict__ part,
+                                                          const Ctl *__restrict__ ctl) {
+  if (ctl->done) return;
+  const double alpha = ctl->alpha, omega = ctl->omega;
+  const int G = gridDim.x, b = blockIdx.x;
+  for (int im = 0; im < nm; ++im) {
+    MaxLoc m[2];
+    m[0].val = 0.0; m[0].idx = -1; m[1].val = 0.0; m[1].idx = -1;
+    const int r0 = modstart[im], r1 = modstart[im + 1];
+    for (int i = r0 + b * blockDim.x + threadIdx.x; i < r1; i += G * blockDim.x) {
+      double tv;
+      if (BCGS) tv = fma(alpha, p[i], omega * q[i]);
+      else tv = alpha * p[i];
+      double rv = d[i];
+      if (BCGS && dscale) {
+        tv = tv * dscale[i];
+        rv = rv / dscale[i];
+      }
+      if (absgt(tv, m[0].val)) { m[0].val = tv; m[0].idx = i; }
+      if (absgt(rv, m[1].val)) { m[1].val = rv; m[1].idx = i; }
+    }
+    block_maxloc<2>(m);
+    if (threadIdx.x == 0) {
+      part[(4 * im) * G + b] = m[0].val;
+      part[(4 * im + 1) * G + b] = (double)m[0].idx;
+      part[(4 * im + 2) * G + b] = m[1].val;
+      part[(4 * im + 3) * G + b] = (double)m[1].idx;
+    }
+  }
+}
+
+// Writes this iteration's record (called by every thread of the control
+// block after ctl_finish_update, before the iteration count advances):
+// ITINNER, the CACCEL values (alpha; BiCGSTAB also omega) and per model
+// dvmax, locdv, rmax, locr.  With one model these are the update's own
+// maxima.  The reference resets the per-model locations every PCG iteration
+// but not every BiCGSTAB iteration (ImsLinearBase.f90:141-146 against
+// :432-435), so a BiCGSTAB model whose maxima stay zero keeps its last rows.
+__device__ void ctl_record(Ctl *ctl, bool bcgs) {
+  const int nm = ctl->rec_nmod, G = ctl->rec_G;
+  const int row = ctl->iter - 1;
+  const bool keep = row >= 0 && row < ctl->rec_cap;
+  double *r = ctl->rec + (size_t)(keep ? row : 0) * (3 + 4 * nm);
+  for (int im = 0; im < nm; ++im) {
+    MaxLoc dx, rm;
+    if (nm == 1) {
+      dx.val = ctl->deltax; dx.idx = ctl->xloc;
+      rm.val = ctl->rmax; rm.idx = ctl->rloc;
+    } else {
+      const double *pp = ctl->rec_part;
+      dx = ctl_reduce_maxloc(pp + (4 * im) * G, pp + (4 * im + 1) * G, G);
+      rm = ctl_reduce_maxloc(pp + (4 * im + 2) * G, pp + (4 * im + 3) * G, G);
+    }
+    if (threadIdx.x == 0) {
+      long long ldv = dx.idx, lr = rm.idx;
+      if (bcgs) {
+        if (ldv < 0) ldv = ctl->rec_loc[2 * im];
+        if (lr < 0) lr = ctl->rec_loc[2 * im + 1];
+      }
+      ctl->rec_loc[2 * im] = ldv;
+      ctl->rec_loc[2 * im + 1] = lr;
+      if (keep) {
+        r[3 + 4 * im] = dx.val;
+        r[4 + 4 * im] = (double)ldv;
+        r[5 + 4 * im] = rm.val;
+        r[6 + 4 * im] = (double)lr;
+      }
+    }
+  }
+  if (threadIdx.x == 0 && keep) {
+    r[0] = (double)ctl->iter;
+    r[1] = ctl->alpha;
+    r[2] = bcgs ? ctl->omega : 0.0;
+    ctl->rec_count = row + 1;
+  }
+}
+
 // End of a PCG iteration: closure test and loop control (ImsLinearBase.f90:196-236).
 __device__ void ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond,
                               int use_cond) {
@@ -459,6 +551,7 @@ __device__ void ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long l
     return;
   }
   ctl_finish_update(ctl, part, G);
+  if (ctl->rec) ctl_record(ctl, false);
   if (threadIdx.x != 0) return;
   double rcnvg = (ctl->icnvgopt == 2 || ctl->icnvgopt == 3 || ctl->icnvgopt == 4) ? ctl->l2norm
                                                                                 : ctl->rmax;
@@ -604,6 +697,7 @@ __device__ void ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long
     return;
   }
   ctl_finish_update(ctl, part, G);
+  if (ctl->rec) ctl_record(ctl, true);
   if (threadIdx.x != 0) return;
   double rcnvg = (ctl->icnvgopt == 2 || ctl->icnvgopt == 3 || ctl->icnvgopt == 4) ? ctl->l2norm
                                                                                 : ctl->rmax;
@@ -1177,6 +1271,12 @@ void kr_cg_pupdate64(int n, const double *z, double *p, const Ctl *ctl, cudaStre
 void kr_cg_update64(int n, double *x, double *d, const double *p, const double *q, double *part,
                     int G, const Ctl *ctl, cudaStream_t st) {
   k_cg_update64<<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
+}
+void kr_rec_models(bool bcgs, int nm, const int *modstart, const double *p, const double *q,
+                   const double *d, const double *dscale, double *part, int G, const Ctl *ctl,
+                   cudaStream_t st) {
+  if (bcgs) k_rec_models<true><<<G, kRedBlock, 0, st>>>(nm, modstart, p, q, d, dscale, part, ctl);
+  else k_rec_models<false><<<G, kRedBlock, 0, st>>>(nm, modstart, p, q, d, dscale, part, ctl);
 }
 void kr_cg_pupdate32(int n, const float *z, float *p, const Ctl *ctl, cudaStream_t st) {
   k_cg_pupdate32<<<egrid(n), 256, 0, st>>>(n, z, p, ctl);

@@ -11,6 +11,9 @@ void kr_ctl_cg_rho(Ctl *ctl, const double *part, int G, cudaStream_t st);
 void kr_ctl_alpha(Ctl *ctl, const double *part, int G, cudaStream_t st);
 void kr_cg_pupdate64(int n, const double *z, double *p, const Ctl *ctl, cudaStream_t st);
 void kr_cg_update64(int n, double *x, double *d, const double *p, const double *q, double *part, int G, const Ctl *ctl, cudaStream_t st);
+// Per-model maxima of the inner records (CONVNMOD > 1): PCG p = P, q unused;
+// BiCGSTAB p = PHAT, q = QHAT; d the updated residual.
+void kr_rec_models(bool bcgs, int nm, const int *modstart, const double *p, const double *q, const double *d, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st);
 void kr_ctl_cg_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond, cudaStream_t st);
 void kr_ctl_bcgs_rho(Ctl *ctl, const double *part, int G, cudaStream_t st);
 void kr_bcgs_p64(int n, const double *d, double *p, const double *v, const Ctl *ctl, cudaStream_t st);

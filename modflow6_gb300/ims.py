@@ -126,6 +126,39 @@ class ImsLinear:
             raise _lib.GbimsError(rc, lib.gbims_last_error(self._h).decode())
         return ApplyResult(icnvg.value, in_iter.value, rc, _summary(sm))
 
+    def set_inner_records(self, nconv: int, convmodstart=None, index_base: int = 0):
+        """Keep up to `nconv` per-inner-iteration records per apply
+        (imslinear_ap's NCONV; 0 switches them off).  `convmodstart`: the
+        first row of each model and neq (CONVMODSTART), default one model."""
+        lib = _lib.load()
+        ms = np.ascontiguousarray([index_base, self.neq + index_base] if convmodstart is None
+                                  else convmodstart, dtype=np.int32)
+        self._rec_nmod = int(ms.size - 1) if nconv > 0 else 0
+        self._rec_cap = int(nconv)
+        rc = lib.gbims_set_inner_records(self._h, int(nconv), self._rec_nmod or 1, _lib.iptr(ms))
+        if rc < 0:
+            raise _lib.GbimsError(rc, lib.gbims_last_error(self._h).decode())
+
+    def inner_records(self) -> dict:
+        """The last apply's records: itinner, alpha, omega (CACCEL), and per
+        model (shape [nrec, convnmod]) dvmax, locdv, rmax, locr."""
+        lib = _lib.load()
+        cap, nm = getattr(self, "_rec_cap", 0), max(getattr(self, "_rec_nmod", 0), 1)
+        it = np.zeros(max(cap, 1), np.int32)
+        al, om = np.zeros(max(cap, 1)), np.zeros(max(cap, 1))
+        ldv, lr = np.zeros(max(cap, 1) * nm, np.int32), np.zeros(max(cap, 1) * nm, np.int32)
+        dv, rm = np.zeros(max(cap, 1) * nm), np.zeros(max(cap, 1) * nm)
+        nrec = C.c_int(0)
+        rc = lib.gbims_get_inner_records(self._h, cap, C.byref(nrec), _lib.iptr(it), _lib.dptr(al),
+                                         _lib.dptr(om), _lib.iptr(ldv), _lib.dptr(dv),
+                                         _lib.iptr(lr), _lib.dptr(rm))
+        if rc < 0:
+            raise _lib.GbimsError(rc, lib.gbims_last_error(self._h).decode())
+        k = nrec.value
+        return dict(itinner=it[:k], alpha=al[:k], omega=om[:k], locdv=ldv[:k * nm].reshape(k, nm),
+                    dvmax=dv[:k * nm].reshape(k, nm), locr=lr[:k * nm].reshape(k, nm),
+                    rmax=rm[:k * nm].reshape(k, nm))
+
     def get_factor(self):
         """The preconditioner of the last factor or apply as (iapc, japc, apc),
         0-based: row i's L entries at [iapc[i], japc[i]), its U entries at

@@ -1047,7 +1047,7 @@ static void or_cg(int *icnvg, int itmax, int *innerit, int neq, int nja, int icn
                   double epfact, const int *ia0, const int *ja0, const double *a0,
                   const int *iapc, const int *japc, const double *apc, double *x,
                   double *b, double *d, double *p, double *q, double *z,
-                  or_cnvg_record *rec, int nrec) {
+                  or_cnvg_record *rec, int nrec, const or_models *mods) {
   double rho0 = 0.0, rho = 0.0;
   *innerit = 0;
   for (int iiter = 1; iiter <= itmax; ++iiter) {
@@ -1066,12 +1066,27 @@ static void or_cg(int *icnvg, int itmax, int *innerit, int neq, int nja, int icn
     double alpha = rho / denominator;
     double deltax = 0.0, rmax = 0.0, l2norm = 0.0;
     int xloc = -1, rloc = -1;
+    /* per-model maxima (ImsLinearBase.f90:141-182): reset every iteration */
+    const int nm = mods ? mods->nmod : 0;
+    double mdv[64], mrm[64];
+    for (int im = 0; im < nm; ++im) {
+      mods->loc[2 * im] = -1;
+      mods->loc[2 * im + 1] = -1;
+      mdv[im] = 0.0;
+      mrm[im] = 0.0;
+    }
+    int im = 0;
     for (int n = 0; n < neq; ++n) {
+      while (nm > 0 && n == mods->modstart[im + 1]) ++im;
       double tv = alpha * p[n];
       x[n] = x[n] + tv;
       if (fabs(tv) > fabs(deltax)) {
         deltax = tv;
         xloc = n;
+      }
+      if (nm > 0 && fabs(tv) > fabs(mdv[im])) {
+        mdv[im] = tv;
+        mods->loc[2 * im] = n;
       }
       tv = d[n];
       tv = tv - alpha * q[n];
@@ -1079,6 +1094,10 @@ static void or_cg(int *icnvg, int itmax, int *innerit, int neq, int nja, int icn
       if (fabs(tv) > fabs(rmax)) {
         rmax = tv;
         rloc = n;
+      }
+      if (nm > 0 && fabs(tv) > fabs(mrm[im])) {
+        mrm[im] = tv;
+        mods->loc[2 * im + 1] = n;
       }
       l2norm = l2norm + tv * tv;
     }
@@ -1088,6 +1107,11 @@ static void or_cg(int *icnvg, int itmax, int *innerit, int neq, int nja, int icn
       r->dvmax = deltax; r->rmax = rmax; r->locdv = xloc; r->locr = rloc;
       r->l2norm = l2norm; r->alpha = alpha; r->beta = (iiter == 1) ? 0.0 : rho / rho0;
       r->rho = rho; r->omega = 0.0;
+      for (int k = 0; k < nm; ++k) {
+        const int o = (iiter - 1) * nm + k;
+        mods->dvmax[o] = mdv[k]; mods->locdv[o] = mods->loc[2 * k];
+        mods->rmax[o] = mrm[k]; mods->locr[o] = mods->loc[2 * k + 1];
+      }
     }
     double rcnvg = (icnvgopt == 2 || icnvgopt == 3 || icnvgopt == 4) ? l2norm : rmax;
     or_testcnvg(icnvgopt, icnvg, *innerit, deltax, rcnvg, l2norm0, epfact, dvclose, rclose);
@@ -1110,7 +1134,7 @@ static void or_bcgs(int *icnvg, int itmax, int *innerit, int neq, int nja, int i
                     const int *ja0, const double *a0, const int *iapc, const int *japc,
                     const double *apc, double *x, double *b, double *d, double *p,
                     double *q, double *t, double *v, double *dhat, double *phat,
-                    double *qhat, or_cnvg_record *rec, int nrec) {
+                    double *qhat, or_cnvg_record *rec, int nrec, const or_models *mods) {
   *innerit = 0;
   double alpha = 0.0, alpha0 = 0.0, beta = 0.0, rho = 0.0, rho0 = 0.0;
   double omega = 0.0, omega0 = 0.0;
@@ -1138,13 +1162,27 @@ static void or_bcgs(int *icnvg, int itmax, int *innerit, int neq, int nja, int i
     omega = numerator / denominator;
     double deltax = 0.0, rmax = 0.0, l2norm = 0.0;
     int xloc = -1, rloc = -1;
+    /* per-model maxima (ImsLinearBase.f90:431-480): the values are reset
+     * every iteration, the locations are not */
+    const int nm = mods ? mods->nmod : 0;
+    double mdv[64], mrm[64];
+    for (int im = 0; im < nm; ++im) {
+      mdv[im] = 0.0;
+      mrm[im] = 0.0;
+    }
+    int im = 0;
     for (int n = 0; n < neq; ++n) {
+      while (nm > 0 && n == mods->modstart[im + 1]) ++im;
       double tv = alpha * phat[n] + omega * qhat[n];
       x[n] = x[n] + tv;
       if (iscl != 0) tv = tv * dscale[n];
       if (fabs(tv) > fabs(deltax)) {
         deltax = tv;
         xloc = n;
+      }
+      if (nm > 0 && fabs(tv) > fabs(mdv[im])) {
+        mdv[im] = tv;
+        mods->loc[2 * im] = n;
       }
       tv = q[n] - omega * t[n];
       d[n] = tv;
@@ -1153,6 +1191,10 @@ static void or_bcgs(int *icnvg, int itmax, int *innerit, int neq, int nja, int i
         rmax = tv;
         rloc = n;
       }
+      if (nm > 0 && fabs(tv) > fabs(mrm[im])) {
+        mrm[im] = tv;
+        mods->loc[2 * im + 1] = n;
+      }
       l2norm = l2norm + tv * tv;
     }
     l2norm = sqrt(l2norm);
@@ -1160,6 +1202,11 @@ static void or_bcgs(int *icnvg, int itmax, int *innerit, int neq, int nja, int i
       or_cnvg_record *r = &rec[iiter - 1];
       r->dvmax = deltax; r->rmax = rmax; r->locdv = xloc; r->locr = rloc;
       r->l2norm = l2norm; r->alpha = alpha; r->beta = beta; r->rho = rho; r->omega = omega;
+      for (int k = 0; k < nm; ++k) {
+        const int o = (iiter - 1) * nm + k;
+        mods->dvmax[o] = mdv[k]; mods->locdv[o] = mods->loc[2 * k];
+        mods->rmax[o] = mrm[k]; mods->locr[o] = mods->loc[2 * k + 1];
+      }
     }
     double rcnvg = (icnvgopt == 2 || icnvgopt == 3 || icnvgopt == 4) ? l2norm : rmax;
     or_testcnvg(icnvgopt, icnvg, *innerit, deltax, rcnvg, l2norm0, epfact, dvclose, rclose);
@@ -1200,7 +1247,10 @@ struct or_ims {
   double *dscale, *dscale2;
   double l2norm0, epfact;
   int npivot_retries;
+  const or_models *mods; /* per-model records, or NULL */
 };
+
+void or_ims_set_models(or_ims *h, const or_models *m) { h->mods = (m && m->nmod > 0 && m->nmod <= 64) ? m : NULL; }
 
 or_ims *or_ims_create(const or_ims_settings *s, int neq, int nja, const int *ia,
                       const int *ja) {
@@ -1324,13 +1374,13 @@ int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int 
   if (s->ilinmeth == 1) {
     or_cg(icnvg, itmax, &innerit, neq, nja, s->icnvgopt, s->north, s->dvclose,
           s->rclose, h->l2norm0, h->epfact, ia0, ja0, a0, h->iapc, h->japc,
-          h->apc, x, rhs, h->d, h->p, h->q, h->z, rec, nrec);
+          h->apc, x, rhs, h->d, h->p, h->q, h->z, rec, nrec, h->mods);
   } else {
     /* DSCALE keeps the unpermuted numbering, as in the reference */
     or_bcgs(icnvg, itmax, &innerit, neq, nja, s->icnvgopt, s->north, s->iscl,
             h->dscale, s->dvclose, s->rclose, h->l2norm0, h->epfact, ia0, ja0,
             a0, h->iapc, h->japc, h->apc, x, rhs, h->d, h->p, h->q, h->t, h->v,
-            h->dhat, h->phat, h->qhat, rec, nrec);
+            h->dhat, h->phat, h->qhat, rec, nrec, h->mods);
   }
   /* BACK PERMUTE (:730-737); AMAT itself was not permuted in place */
   if (s->iord != 0) {

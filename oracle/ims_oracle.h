@@ -25,6 +25,20 @@ typedef struct {
 
 typedef struct or_ims or_ims;
 
+/* Per-model rows of the convergence records (CONVNMOD, CONVMODSTART and the
+ * ConvergenceSummary arrays convdvmax, convlocdv, convrmax, convlocr; layout
+ * [nrec][nmod], model fastest).  modstart: first row of each model, 0-based,
+ * nmod + 1 entries ending at neq.  loc holds the per-model locations that the
+ * reference keeps in summary%locdv/locr between iterations (2*nmod, -1 at
+ * the start). */
+typedef struct {
+  int nmod;
+  const int *modstart;
+  double *dvmax, *rmax;
+  int *locdv, *locr;
+  int *loc;
+} or_models;
+
 int or_is_close(double a, double b);
 void or_amux(int n, const double *x, double *y, const double *a, const int *ja, const int *ia);
 double or_ddot(int n, const double *x, const double *y);
@@ -54,6 +68,8 @@ void or_ims_destroy(or_ims *h);
 int or_ims_apply(or_ims *h, double *amat, double *rhs, double *x, int kstp, int kiter,
                  int *icnvg, int *in_iter, or_cnvg_record *rec, int nrec);
 int or_ims_ipc(const or_ims *h);
+/* Per-model records for the next applies (NULL: none). */
+void or_ims_set_models(or_ims *h, const or_models *m);
 int or_ims_njapc(const or_ims *h);
 int or_ims_ilut_ierr(const or_ims *h);
 int or_ilut(int n, const double *a, const int *ja, const int *ia, int lfil, double droptol,

@@ -40,6 +40,11 @@ class CnvgRecord(C.Structure):
                 ("omega", C.c_double), ("locdv", C.c_int), ("locr", C.c_int)]
 
 
+class Models(C.Structure):
+    _fields_ = [("nmod", C.c_int), ("modstart", _ip), ("dvmax", _dp), ("rmax", _dp),
+                ("locdv", _ip), ("locr", _ip), ("loc", _ip)]
+
+
 class GwfModel(C.Structure):
     _fields_ = [("nlay", C.c_int), ("nrow", C.c_int), ("ncol", C.c_int), ("nodes", C.c_int),
                 ("nja", C.c_int), ("njas", C.c_int),
@@ -97,6 +102,7 @@ def load():
         lib.or_pcu_ilut.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, _dp, _ip, _ip, _dp,
                                     _ip, _ip, C.c_int, _dp, _ip, _ip]
         lib.or_amux.argtypes = [C.c_int, _dp, _dp, _dp, _ip, _ip]
+        lib.or_ims_set_models.argtypes = [C.c_void_p, C.c_void_p]
         lib.or_ilu0a.argtypes = [C.c_int, C.c_int, _dp, _ip, _ip, _dp, _dp]
         lib.or_amux_fma.argtypes = [C.c_int, _dp, _dp, _dp, _ip, _ip]
         lib.or_ilu0a_fma.argtypes = [C.c_int, _dp, _ip, _ip, _dp, _dp]
@@ -167,6 +173,24 @@ class Ims:
             raise RuntimeError(f"oracle apply failed: {rc}")
         recs = [{f: getattr(rec[i], f) for f, _ in CnvgRecord._fields_} for i in range(min(nrec, in_iter.value))]
         return icnvg.value, in_iter.value, recs
+
+    def set_models(self, modstart, nrec):
+        """Per-model records (CONVMODSTART, 0-based first rows ending at neq)
+        for the next applies with nrec records; read them with model_records."""
+        ms = np.ascontiguousarray(modstart, np.int32)
+        nm = ms.size - 1
+        self._mods = dict(ms=ms, dvmax=np.zeros(nrec * nm), rmax=np.zeros(nrec * nm),
+                          locdv=np.zeros(nrec * nm, np.int32), locr=np.zeros(nrec * nm, np.int32),
+                          loc=np.full(2 * nm, -1, np.int32), nm=nm)
+        m = self._mods
+        self._mstruct = Models(nm, ip(ms), dp(m["dvmax"]), dp(m["rmax"]), ip(m["locdv"]),
+                               ip(m["locr"]), ip(m["loc"]))
+        self.lib.or_ims_set_models(self.h, C.byref(self._mstruct))
+
+    def model_records(self, nrec):
+        m = self._mods
+        nm = m["nm"]
+        return {k: m[k][:nrec * nm].reshape(nrec, nm) for k in ("dvmax", "locdv", "rmax", "locr")}
 
     def apc(self) -> np.ndarray:
         n = self.lib.or_ims_njapc(self.h)
