@@ -32,6 +32,38 @@ def test_formulate_bitexact(gblib, name, scale):
     np.testing.assert_array_equal(rhs, ro)
 
 
+@pytest.mark.parametrize("inewton", [0, 1])
+@pytest.mark.parametrize("icellavg,ivarcv,idewatcv", [(1, 0, 0), (2, 0, 0), (3, 0, 0), (0, 1, 0),
+                                                      (0, 1, 1), (2, 1, 1)])
+def test_formulate_npf_options(gblib, inewton, icellavg, ivarcv, idewatcv):
+    """ALTERNATIVE_CELL_AVERAGING LOGARITHMIC / AMT-LMK / AMT-HMK
+    (GwfConductanceUtils.f90:226-305) and VARIABLECV [DEWATERED] (:149-222)
+    on the convertible c3 grid, with and without NEWTON, against the oracle.
+    AMT-HMK and VARIABLECV use no logarithm and must agree bit for bit; the
+    log-mean forms call the device's FP64 log, whose last bit may differ from
+    the host libm's, so they are held to 4 ulps (relative 1e-15) with most
+    entries still bit-exact."""
+    m = make_config("c3", seed=2, scale=0.04)
+    m.inewton, m.icellavg, m.ivarcv, m.idewatcv = inewton, icellavg, ivarcv, idewatcv
+    g = oracle.Gwf(m, oracle.settings())
+    sol = GwfSolution(m, ImsLinearSettings(), Nonlinear())
+    rng = np.random.default_rng(3)
+    # heads across the layer bottoms, so that cells are partly saturated and
+    # some are dewatered
+    h = m.strt + rng.uniform(-60.0, 3.0, m.nodes)
+    hold = m.strt + rng.uniform(-3.0, 3.0, m.nodes)
+    sol.heads = h
+    amat, rhs = sol.formulate(delt=2.5, hold=hold)
+    ao, ro = g.assemble(h, hold=hold, delt=2.5, transient=True)
+    if icellavg in (1, 2):
+        np.testing.assert_allclose(amat, ao, rtol=1e-15, atol=0)
+        np.testing.assert_allclose(rhs, ro, rtol=1e-15, atol=1e-300)
+        assert np.mean(amat == ao) > 0.9
+    else:
+        np.testing.assert_array_equal(amat, ao)
+        np.testing.assert_array_equal(rhs, ro)
+
+
 def test_timestep_c1_matches_oracle(gblib):
     m = make_config("c1", seed=0)
     tol = dict(dvclose=1e-8, rclose=1e-6, iter1=1000)
