@@ -81,6 +81,44 @@ def sln_ls_fixups(ia, ja, active, amat, rhs, x, isymmetric=True):
     return amat, rhs
 
 
+class LsFixups:
+    """The sln_ls loose ends (NumericalSolution.f90:2434-2478) for one matrix
+    structure and IBOUND, applied in place to host arrays each outer
+    iteration: the positions they touch are found once, so an application
+    costs a pass over the diagonal and the few CHD-related entries.  Results
+    equal `sln_ls_fixups` bit for bit (the CHD columns are moved to the
+    right-hand side row by row in JA order, as the reference loops)."""
+
+    def __init__(self, ia, ja, active, isymmetric=True):
+        ia = np.asarray(ia, np.int64)
+        ja = np.asarray(ja, np.int64)
+        n = ia.size - 1
+        self.diag = ia[:-1]
+        self.act = np.asarray(active) > 0
+        rows = np.repeat(np.arange(n), np.diff(ia))
+        off = rows != ja
+        self.inactive = np.flatnonzero(~self.act)
+        self.kill = np.flatnonzero(~self.act[rows] & off)
+        if isymmetric:
+            e = np.flatnonzero(off & self.act[rows] & (np.asarray(active)[ja] < 0))
+        else:
+            e = np.zeros(0, np.int64)
+        self.eidx, self.erow, self.ecol = e, rows[e], ja[e]
+
+    def apply(self, amat, rhs, x):
+        d = amat[self.diag]
+        small = np.flatnonzero(self.act & (np.abs(d) < 1e-15))
+        amat[self.diag[small]] = -1.0
+        rhs[small] = rhs[small] + (-1.0) * x[small]
+        amat[self.kill] = 0.0
+        amat[self.diag[self.inactive]] = 1.0
+        rhs[self.inactive] = x[self.inactive]
+        if self.eidx.size:
+            np.subtract.at(rhs, self.erow, amat[self.eidx] * x[self.ecol])
+            amat[self.eidx] = 0.0
+        return amat, rhs
+
+
 def _f(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
