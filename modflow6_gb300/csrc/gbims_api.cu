@@ -373,6 +373,7 @@ static int setup_structured(gbims_handle *h, const std::vector<int> &shapes,
   // (chunk 8, ring 4, prefetch 2, two CTAs per SM); gbims_autotune picks
   // per system
   h->D.cfg = 7;
+  if (const char *nv = std::getenv("GBIMS_SWEEP_NATIVE")) h->D.ext_allowed = (nv[0] == '0');
   h->structured = true;
   return GBIMS_OK;
 }
@@ -829,7 +830,15 @@ static int factor_core(gbims_handle *h) {
     if (icount > 10) break;
   }
   if (h->mixed) kr_f64_to_f32(h->nja, h->d_apc, h->d_apc32, st);
-  if (h->structured) launch_dia7_extract(h->D, n, h->d_iapc, h->d_japc, h->d_apc, h->mixed, st);
+  if (h->structured) {
+    const int was = h->D.ext;
+    if (launch_dia7_extract(h->D, n, h->d_iapc, h->d_japc, h->d_apc, h->mixed, st) < 0)
+      return fail(h, GBIMS_ERR_CUDA, "wavefront tile extraction failed");
+    // the captured inner loop holds the sweep kernels of the arithmetic
+    if (h->D.ext != was) drop_graph(h);
+    // the range check, and the seven in-place df64 conversions
+    h->launches += ((!h->mixed && h->D.ext_allowed) ? 1 : 0) + (h->D.ext ? 7 : 0);
+  }
   h->launches += (h->mixed ? 1 : 0) + (h->structured ? 1 : 0);
   GB_CUDA(h, cudaGetLastError());
   h->factored = true;

@@ -180,6 +180,10 @@ struct Dia7 {
   const Ctl *mctl = nullptr;  // batched ensembles: members that are done are skipped
   int ntickets = 0;
   int cfg = 0;  // sweep configuration (chunk, ring, prefetch): an index of dia7_cfg
+  // FP64 handles: 1 while the tiles hold df64 pairs (the factor lies in the
+  // float exponent range), 0 for native FP64 tiles; ext_allowed 0 keeps the
+  // native sweeps (GBIMS_SWEEP_NATIVE)
+  int ext = 0, ext_allowed = 1;
   // forward tiles: lower coefficients (unit diagonal) z (layer above),
   // y (row behind), x (column left); backward tiles: dinv*U for z, y, x and
   // dinv; zero where the neighbour or the cell does not exist
@@ -261,8 +265,10 @@ bool dia7_matches(int nlay, int nrow, int ncol, int n, const std::vector<int> &i
 // natural order (false if it is not one).
 bool dia7_detect(int n, const std::vector<int> &ia, const std::vector<int> &ja, int *nlay,
                  int *nrow, int *ncol);
-void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_japc,
-                         const double *d_apc, bool mixed, cudaStream_t st);
+// Factor -> skewed tiles; FP64 handles choose df64 or native tiles here (D.ext).
+// Returns 0, or -1 on a CUDA error.
+int launch_dia7_extract(Dia7 &D, int n, const int *d_iapc, const int *d_japc,
+                        const double *d_apc, bool mixed, cudaStream_t st);
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
                          cudaStream_t st);
 void launch_dia7_vfill(const Dia7 &D, const int *d_ia, const double *d_amat, cudaStream_t st);

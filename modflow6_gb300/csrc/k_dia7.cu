@@ -41,12 +41,21 @@
 // take a ticket in launch order and depend only on smaller tickets, so the
 // chain of waits always ends.
 //
-// Forward sweep: y = r - Lz*y(k-1) - Ly*y(i-1) - Lx*y(j-1), in the reference's
-// order (ascending column), so it rounds exactly like ilu0a with FMA.
-// Backward sweep: z = dinv*y - Uz'*z(k+1) - Uy'*z(i+1) - Ux'*z(j+1) with the
-// upper factors pre-scaled by the inverse pivot (U' = dinv*U), equal in exact
-// arithmetic to the reference's (y - sum U z)*dinv with one FMA instead of two
-// dependent operations on the critical path.
+// Forward sweep: y = r - Lz*y(k-1) - Lx*y(j-1) - Ly*y(i-1).  Backward sweep:
+// z = dinv*y - Uz'*z(k+1) - Ux'*z(j+1) - Uy'*z(i+1) with the upper factors
+// pre-scaled by the inverse pivot (U' = dinv*U).  Both are equal in exact
+// arithmetic to ilu0a's sums; the order puts the lane's own previous result
+// first, so that a step's chain through its own line is two FMAs and the
+// chain through the neighbour line (the shuffle) is one.
+//
+// Arithmetic.  The mixed form sweeps in FP32.  The FP64 form sweeps in df64
+// (pairs of floats, k_df64.cuh) when every factor tile lies in the float
+// exponent range, because GB300 issues a warp's FP64 FMA only every 64 cycles
+// or so and a step carries two of them; otherwise, or when GBIMS_SWEEP_NATIVE
+// is set, it sweeps in native FP64.  The df64 backward sweep leaves the
+// conversion of its result to FP64 (one FP64 add per cell) to the copy warp,
+// through a staging tile in the ring buffer, so the chain never waits on the
+// FP64 pipe.
 #include <algorithm>
 #include <cstdlib>
 
@@ -105,14 +114,64 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
 }
 
 
+// The arithmetic of a sweep: T is the element type of the tiles, the result
+// words and the chain; V the type of the natural-order vectors r and z.
+template <typename T>
+struct Elem;
+template <>
+struct Elem<double> {
+  using V = double;
+  static __device__ __forceinline__ double zero() { return 0.0; }
+  static __device__ __forceinline__ double fms(double a, double b, double c) { return fma(-a, b, c); }
+  static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+  static __device__ __forceinline__ double shfl_up(double v, int d) {
+    return __shfl_up_sync(0xffffffffu, v, d);
+  }
+  static __device__ __forceinline__ double from_vec(double v) { return v; }
+  static __device__ __forceinline__ double to_vec(double v) { return v; }
+  static __device__ __forceinline__ double from_factor(double v) { return v; }
+};
+template <>
+struct Elem<float> {
+  using V = float;
+  static __device__ __forceinline__ float zero() { return 0.0f; }
+  static __device__ __forceinline__ float fms(float a, float b, float c) { return fmaf(-a, b, c); }
+  static __device__ __forceinline__ float mul(float a, float b) { return a * b; }
+  static __device__ __forceinline__ float shfl_up(float v, int d) {
+    return __shfl_up_sync(0xffffffffu, v, d);
+  }
+  static __device__ __forceinline__ float from_vec(float v) { return v; }
+  static __device__ __forceinline__ float to_vec(float v) { return v; }
+  static __device__ __forceinline__ float from_factor(double v) { return (float)v; }
+};
+template <>
+struct Elem<DF> {
+  using V = double;
+  static __device__ __forceinline__ DF zero() { return df_zero(); }
+  static __device__ __forceinline__ DF fms(DF a, DF b, DF c) { return df_fms(a, b, c); }
+  static __device__ __forceinline__ DF mul(DF a, DF b) { return df_mul(a, b); }
+  static __device__ __forceinline__ DF shfl_up(DF v, int d) { return df_shfl_up(v, d); }
+  static __device__ __forceinline__ DF from_vec(double v) { return df_from_double(v); }
+  static __device__ __forceinline__ double to_vec(DF v) { return df_to_double(v); }
+  static __device__ __forceinline__ DF from_factor(double v) { return df_from_double_fp64(v); }
+};
+__device__ __forceinline__ bool dinv_zero(double d) { return d == 0.0; }
+__device__ __forceinline__ bool dinv_zero(float d) { return d == 0.0f; }
+__device__ __forceinline__ bool dinv_zero(DF d) { return d.hi == 0.0f; }
+
+template <typename T>
+constexpr bool kStagedOut = false;  // the backward result goes out through the copy warp
+template <>
+constexpr bool kStagedOut<DF> = true;
+
 template <typename T>
 struct SweepArgs {
   const Dia7Geo *geo;  // members, in ticket order
   int nm;
   const Ctl *mctl;     // per-member control blocks (batched ensembles) or null
   const T *A, *B, *X, *D;  // skewed factors (forward: Lz Ly Lx -, backward: Uz' Uy' Ux' dinv)
-  const T *rnat;           // forward: right-hand side, natural order
-  T *znat;                 // backward: result, natural order
+  const typename Elem<T>::V *rnat;  // forward: right-hand side, natural order
+  typename Elem<T>::V *znat;        // backward: result, natural order
   LLWord<T> *ysk;          // forward result, skewed (written forward, read backward)
   LLWord<T> *zsk;          // backward result, skewed (written and read backward)
   unsigned long long *ticket;  // this direction's ticket counter (zeroed once, never reset)
@@ -133,6 +192,7 @@ struct alignas(16) Stage<T, C, -1> {
   T a[C * 32], b[C * 32], x[C * 32], d[C * 32];
   LLWord<T> y[C * 32];  // own forward result, steps descending
   T yn[C];
+  T zo[kStagedOut<T> ? C * 32 : 1];  // df64: the chunk's results for the copy warp
 };
 
 // Warp roles of a sweep CTA.
@@ -161,6 +221,8 @@ template <typename T, int S, int C, int NS, int DIR, int PF>
 __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   constexpr int W = 32;
   using St = Stage<T, C, DIR>;
+  using E = Elem<T>;
+  using V = typename E::V;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   St *stg = reinterpret_cast<St *>(smem_raw);
   unsigned long long *full = reinterpret_cast<unsigned long long *>(smem_raw + NS * sizeof(St));
@@ -252,12 +314,13 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     // walks line b*W + l; step g is column g - S*l), in the same ring
     const int ri = b * W + lane;
     const bool rline = (DIR > 0) && ri < nrow;
-    const T *rrow = rline ? p.rnat + geo.row0 + ((long long)k * nrow + ri) * geo.ncol : nullptr;
+    const V *rrow = rline ? p.rnat + geo.row0 + ((long long)k * nrow + ri) * geo.ncol : nullptr;
     auto rload = [&](int c, T (&dst)[C]) {
 #pragma unroll
       for (int t = 0; t < C; ++t) {
         const int jj = c * C + t - S * lane;
-        dst[t] = (rline && (unsigned)jj < (unsigned)geo.ncol) ? __ldg(rrow + jj) : T(0);
+        dst[t] = (rline && (unsigned)jj < (unsigned)geo.ncol) ? E::from_vec(__ldg(rrow + jj))
+                                                              : E::zero();
       }
     };
     T rr[PF][C];
@@ -301,9 +364,15 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         for (int t = 0; t < C; ++t) {
           const int e = t * W + lane;
           T t0;
-          if constexpr (DIR > 0) t0 = rr[j][t];
-          else t0 = st.d[e] * ll_val(st.y[C * W - 1 - e]);
-          if (has_lay) t0 = fma(-st.a[e], zn[t], t0);
+          if constexpr (DIR > 0) {
+            t0 = rr[j][t];
+          } else {
+            // the forward words of padding slots (dinv zero) may not have
+            // been copied into this buffer: take zero, not 0 * stale bits
+            const T dv = st.d[e];
+            t0 = dinv_zero(dv) ? E::zero() : E::mul(dv, ll_val(st.y[C * W - 1 - e]));
+          }
+          if (has_lay) t0 = E::fms(st.a[e], zn[t], t0);
           st.a[e] = t0;
         }
         if constexpr (DIR > 0) {
@@ -347,7 +416,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         }
         if (has_blk) {
           const bool need = needs(c);
-          T v[1] = {T(0)};
+          T v[1] = {E::zero()};
           unsigned want = 0;
           if (need) {
             if (ll_ready<T>(yr[j], ep)) ll_take(yr[j], v[0]);
@@ -359,10 +428,10 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
             fail();
             return;
           }
-          if (lane < C) stg[s].yn[lane] = need ? v[0] : T(0);
+          if (lane < C) stg[s].yn[lane] = need ? v[0] : E::zero();
           if (c + PF < nch && needs(c + PF)) ll_issue(ysrc + (long long)yrow_of(c + PF) * W, yr[j]);
         } else if (lane < C) {
-          stg[s].yn[lane] = T(0);  // an edge block of the layer: no neighbour line
+          stg[s].yn[lane] = E::zero();  // an edge block of the layer: no neighbour line
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&prep[s]);
@@ -371,10 +440,31 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     return;
   }
 
+  // the cells of the compute warp's lane `lane` at chunk c: line i, and for
+  // step t the column g0 + t - S*lane of the sweep's direction
+  const int i = (DIR > 0) ? (b * W + lane) : (b * W + (W - 1 - lane));
+  const bool line_ok = i >= 0 && i < nrow;
+  const int ncol = geo.ncol;
+  V *zrow = (DIR < 0 && line_ok) ? p.znat + geo.row0 + ((long long)k * nrow + i) * ncol : nullptr;
+
   if (role == kRoleCopy) {
     // ---------------- copy warp ----------------
     // The block's own tiles have no producer in this launch: they stream
-    // into the ring as fast as buffers free up.
+    // into the ring as fast as buffers free up.  In the df64 backward sweep
+    // this warp also writes the results of each finished chunk to z in
+    // natural order (converted to FP64) before it refills the buffer.
+    auto flush = [&](int c) {
+      if constexpr (DIR < 0 && kStagedOut<T>) {
+        const St &st = stg[c % NS];
+        const int jc = c * C - S * lane;
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+          const int jj = jc + t;
+          if (line_ok && (unsigned)jj < (unsigned)ncol)
+            zrow[ncol - 1 - jj] = E::to_vec(st.zo[t * W + lane]);
+        }
+      }
+    };
     int issued = 0;
     bool ok = true;
     const unsigned tileb = C * W * sizeof(T);
@@ -384,6 +474,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         const bool got = mbar_wait(&empty[s], ((c / NS) - 1) & 1, v_abort);
         ok = __all_sync(0xffffffffu, got);
         if (!ok) break;
+        if constexpr (DIR < 0 && kStagedOut<T>) flush(c - NS);
       }
       if (lane == 0) {
         St &st = stg[s];
@@ -411,6 +502,14 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       issued = c + 1;
     }
     if (!ok) fail();
+    if constexpr (DIR < 0 && kStagedOut<T>) {
+      // the last chunks' results, once the compute warp has finished them
+      for (int c = max(0, nch - NS); ok && c < nch; ++c) {
+        const bool got = mbar_wait(&empty[c % NS], (c / NS) & 1, v_abort);
+        ok = __all_sync(0xffffffffu, got);
+        if (ok) flush(c);
+      }
+    }
     if (lane == 0) {
       // every copy issued has landed before this warp, and so the CTA, ends
       // (the other warps may have left early on an abort)
@@ -424,14 +523,11 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   }
 
   // ---------------- compute warp ----------------
-  // Per step one shuffle and the two FMAs of the row and column neighbours;
-  // each result goes straight out as a word of this epoch.
-  const int i = (DIR > 0) ? (b * W + lane) : (b * W + (W - 1 - lane));
-  const bool line_ok = i >= 0 && i < nrow;
-  const int ncol = geo.ncol;
+  // Per step one shuffle and the two FMAs of the column and row neighbours,
+  // on operands moved from the ring buffer into registers at the start of
+  // the chunk; each result goes straight out as a word of this epoch.
   LLWord<T> *outt = out + tile(k, b) + lane;
-  T *zrow = (DIR < 0 && line_ok) ? p.znat + geo.row0 + ((long long)k * nrow + i) * ncol : nullptr;
-  T h1 = T(0), h2 = T(0);
+  T h1 = E::zero(), h2 = E::zero();
   for (int c = 0; c < nch; ++c) {
     const int s = c % NS;
     const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort) &&
@@ -440,24 +536,36 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       if (lane == 0) *v_abort = 1;
       return;
     }
-    const St &st = stg[s];
+    St &st = stg[s];
     const int g0 = c * C;
     const int jc = g0 - S * lane;
+    T ra[C], rb[C], rx[C], ryn[C];
 #pragma unroll
     for (int t = 0; t < C; ++t) {
-      T yv = __shfl_up_sync(0xffffffffu, (S == 1) ? h1 : h2, 1);
-      if (lane == 0) yv = st.yn[t];
-      const int jj = jc + t;
-      const bool v = line_ok && (unsigned)jj < (unsigned)ncol;
-      T tv = st.a[t * W + lane];  // pre-computed r - Lz*zn (backward: dinv*y - Uz'*zn)
+      ra[t] = st.a[t * W + lane];  // pre-computed r - Lz*zn (backward: dinv*y - Uz'*zn)
+      rb[t] = st.b[t * W + lane];
+      rx[t] = st.x[t * W + lane];
+      ryn[t] = st.yn[t];
+    }
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+      T yv = E::shfl_up((S == 1) ? h1 : h2, 1);
+      if (lane == 0) yv = ryn[t];
       // the coefficients of absent neighbours are zero (first line of the
-      // grid, first column, padding slots) and their values finite, so both
-      // products are taken unconditionally: no divergent lanes on the chain
-      tv = fma(-st.b[t * W + lane], yv, tv);
-      tv = fma(-st.x[t * W + lane], h1, tv);
-      if (!v) tv = T(0);
+      // grid, first column, padding slots) and every value is finite, so
+      // both products are taken unconditionally and padding slots come out
+      // zero: no divergent lanes and no select on the chain
+      T tv = E::fms(rx[t], h1, ra[t]);
+      tv = E::fms(rb[t], yv, tv);
       ll_put(outt + (long long)(g0 + t) * W, tv, ep);
-      if (DIR < 0 && v) zrow[ncol - 1 - jj] = tv;  // the result in natural order
+      if constexpr (DIR < 0) {
+        if constexpr (kStagedOut<T>) {
+          stg[s].zo[t * W + lane] = tv;
+        } else {
+          const int jj = jc + t;
+          if (line_ok && (unsigned)jj < (unsigned)ncol) zrow[ncol - 1 - jj] = tv;  // natural order
+        }
+      }
       h2 = h1;
       h1 = tv;
     }
@@ -513,10 +621,41 @@ __global__ void k_dia7_extract(const Dia7Geo *__restrict__ geos, int nm, long lo
       }
       vd = d;
     }
-    A[q] = (T)va;
-    B[q] = (T)vb;
-    X[q] = (T)vx;
-    if (D) D[q] = (T)vd;
+    A[q] = Elem<T>::from_factor(va);
+    B[q] = Elem<T>::from_factor(vb);
+    X[q] = Elem<T>::from_factor(vx);
+    if (D) D[q] = Elem<T>::from_factor(vd);
+  }
+}
+
+// Sets *flag when a tile value is not finite or, being nonzero, lies outside
+// [2^-100, 2^100]: such factors keep the native FP64 sweeps.
+__global__ void k_dia7_range(long long nslot, const double *__restrict__ a0,
+                             const double *__restrict__ a1, const double *__restrict__ a2,
+                             const double *__restrict__ a3, const double *__restrict__ a4,
+                             const double *__restrict__ a5, const double *__restrict__ a6,
+                             int *flag) {
+  const double *arr[7] = {a0, a1, a2, a3, a4, a5, a6};
+  int bad = 0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nslot;
+       q += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int t = 0; t < 7; ++t) {
+      const unsigned long long u = (unsigned long long)__double_as_longlong(arr[t][q]);
+      const int e = (int)((u >> 52) & 0x7ff);  // biased exponent; 0 for zero and denormals
+      const bool zero = (u << 1) == 0ULL;
+      if (!zero && (e < 1023 - 100 || e > 1023 + 100)) bad = 1;
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+// FP64 tile -> df64 tile in place (8 bytes each, element by element).
+__global__ void k_dia7_to_df(long long nslot, double *a) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nslot;
+       q += (long long)gridDim.x * blockDim.x) {
+    const double v = a[q];
+    reinterpret_cast<DF *>(a)[q] = df_from_double_fp64(v);
   }
 }
 
@@ -536,6 +675,8 @@ template <typename T>
 constexpr int kSOf = 1;
 template <>
 constexpr int kSOf<float> = GB_DIA32_S;
+template <>
+constexpr int kSOf<DF> = 1;
 static_assert(GB_DIA32_S == 1 || GB_DIA32_S == 2, "lane skew 1 or 2");
 // OCC 2: the CTA asks for enough shared memory that at most two share an
 // SM, so that each compute warp has a sub-partition's FP64 pipe to itself.
@@ -666,16 +807,34 @@ static void extract_t(const Dia7 &D, const int *d_iapc, const int *d_japc, const
                                           d_apc, arr[3], arr[4], arr[5], arr[6]);
 }
 
-void launch_dia7_extract(const Dia7 &D, int n, const int *d_iapc, const int *d_japc,
-                         const double *d_apc, bool mixed, cudaStream_t st) {
+int launch_dia7_extract(Dia7 &D, int n, const int *d_iapc, const int *d_japc,
+                        const double *d_apc, bool mixed, cudaStream_t st) {
   (void)n;
   if (!mixed) {
     double *arr[7] = {D.d_lz, D.d_ly, D.d_lx, D.d_uz, D.d_uy, D.d_ux, D.d_dinv};
     extract_t<double>(D, d_iapc, d_japc, d_apc, arr, st);
+    D.ext = 0;
+    if (D.ext_allowed) {
+      // df64 sweeps when every tile value lies in the float exponent range
+      int *flag = D.d_err + 2;
+      int bad = 1;
+      const int grid = (int)std::min<long long>((D.slots + 255) / 256, 8LL * kNumSM);
+      if (cudaMemsetAsync(flag, 0, sizeof(int), st) != cudaSuccess) return -1;
+      k_dia7_range<<<grid, 256, 0, st>>>(D.slots, arr[0], arr[1], arr[2], arr[3], arr[4], arr[5],
+                                        arr[6], flag);
+      if (cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return -1;
+      if (!bad) {
+        for (double *a : arr) k_dia7_to_df<<<grid, 256, 0, st>>>(D.slots, a);
+        D.ext = 1;
+      }
+    }
   } else {
     float *arr[7] = {D.f_lz, D.f_ly, D.f_lx, D.f_uz, D.f_uy, D.f_ux, D.f_dinv};
     extract_t<float>(D, d_iapc, d_japc, d_apc, arr, st);
   }
+  return 0;
 }
 
 // The two sweeps of one configuration (opting in to more than 48 KB of
@@ -705,8 +864,8 @@ static void sweep_pair(SweepArgs<T> a, const T *const *arr, const Dia7 &D, int o
 // in the skewed layout as epoch-tagged words.  No memory is reset between
 // applications: each sweep launch writes its words with a new epoch.
 template <typename T>
-static void apply_t(const Dia7 &D, const T *const *arr, const T *r, T *z, const Ctl *ctl,
-                    cudaStream_t st) {
+static void apply_t(const Dia7 &D, const T *const *arr, const typename Elem<T>::V *r,
+                    typename Elem<T>::V *z, const Ctl *ctl, cudaStream_t st) {
   SweepArgs<T> a;
   a.geo = D.d_geo;
   a.nm = D.nm;
@@ -732,6 +891,14 @@ static void apply_t(const Dia7 &D, const T *const *arr, const T *r, T *z, const 
 
 void launch_dia7_apply64(const Dia7 &D, const double *r, double *z, const Ctl *ctl,
                          cudaStream_t st) {
+  if (D.ext) {
+    const DF *arr[7] = {reinterpret_cast<const DF *>(D.d_lz), reinterpret_cast<const DF *>(D.d_ly),
+                        reinterpret_cast<const DF *>(D.d_lx), reinterpret_cast<const DF *>(D.d_uz),
+                        reinterpret_cast<const DF *>(D.d_uy), reinterpret_cast<const DF *>(D.d_ux),
+                        reinterpret_cast<const DF *>(D.d_dinv)};
+    apply_t<DF>(D, arr, r, z, ctl, st);
+    return;
+  }
   const double *arr[7] = {D.d_lz, D.d_ly, D.d_lx, D.d_uz, D.d_uy, D.d_ux, D.d_dinv};
   apply_t<double>(D, arr, r, z, ctl, st);
 }

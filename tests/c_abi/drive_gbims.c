@@ -20,6 +20,12 @@
 #define NX 61
 #define NY 47
 
+/* conductance of the connection n-m, the same from either side */
+static double cond(int n, int m) {
+  const int lo = n < m ? n : m, hi = n < m ? m : n;
+  return 1.0 + 0.5 * ((lo * 7 + hi * 13) % 5);
+}
+
 static int fail(const char *what, int rc) {
   printf("drive_gbims FAILED: %s (status %d: %s)\n", what, rc, gbims_status_string(rc));
   return 1;
@@ -48,7 +54,7 @@ int main(void) {
     for (int k = 0; k < 4; ++k) {
       if (nb[k] < 0) continue;
       const int jn = nb[k] % NX;
-      const double c = 1.0 + 0.5 * ((n * 7 + k * 13) % 5);
+      const double c = cond(n, nb[k]);
       diag -= c;
       if (jn == 0 || jn == NX - 1) continue; /* constant head moved to the rhs below */
       ja[nja] = nb[k] + 1;
@@ -59,8 +65,7 @@ int main(void) {
     for (int k = 0; k < 4; ++k) {
       if (nb[k] < 0) continue;
       const int jn = nb[k] % NX;
-      const double c = 1.0 + 0.5 * ((n * 7 + k * 13) % 5);
-      if (jn == 0) rhs[n] -= c * 10.0;
+      if (jn == 0) rhs[n] -= cond(n, nb[k]) * 10.0;
     }
   }
   ia[neq] = nja + 1;

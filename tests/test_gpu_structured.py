@@ -1,10 +1,14 @@
 """Structured 7-point wavefront sweeps (DIS grids) against the oracle.
 
-The forward sweep keeps the reference's summation order; the backward sweep
-uses inverse-pivot-scaled upper factors, equal in exact arithmetic, so the
-preconditioner output is compared at 1e-12 relative to its scale, and solves
-at closure (heads within 0.1 x INNER_DVCLOSE of the oracle's IMS solve).
+The sweeps sum each cell's terms in another order than ilu0a (the lane's own
+line first), the backward sweep uses inverse-pivot-scaled upper factors, and
+the FP64 form computes in df64 (pairs of floats, about 48 significant bits)
+when the factor lies in the float exponent range: all equal to ilu0a in exact
+arithmetic, so the preconditioner output is compared at 1e-12 relative to its
+scale, and solves at closure (heads within 0.1 x INNER_DVCLOSE of the
+oracle's IMS solve).
 """
+import os
 import numpy as np
 import pytest
 
@@ -192,3 +196,70 @@ def test_reduced_pattern_keeps_the_level_sweeps(gblib):
     ims = ImsLinear(ImsLinearSettings(structure=GENERAL)).imslinear_allocate(m.nodes, ia, ja)
     res = ims.imslinear_apply(amat.copy(), rhs.copy(), x0.copy())
     assert res.summary["structured"] == 0
+
+
+def _precondition(gblib, shape, amat, con, v, native):
+    """The wavefront preconditioner applied to v, with df64 or native FP64
+    sweeps (GBIMS_SWEEP_NATIVE is read when the handle is created)."""
+    old = os.environ.get("GBIMS_SWEEP_NATIVE")
+    os.environ["GBIMS_SWEEP_NATIVE"] = "1" if native else "0"
+    try:
+        ims = ImsLinear(ImsLinearSettings(structure=shape)).imslinear_allocate(
+            con["nodes"], con["ia"], con["ja"])
+    finally:
+        if old is None:
+            del os.environ["GBIMS_SWEEP_NATIVE"]
+        else:
+            os.environ["GBIMS_SWEEP_NATIVE"] = old
+    assert gblib.gbims_factor(ims._h, _lib.dptr(amat), None) == 0
+    z = np.zeros_like(v)
+    assert gblib.gbims_precondition(ims._h, _lib.dptr(v), _lib.dptr(z)) == 0
+    return z
+
+
+@pytest.mark.parametrize("shape", [(1, 33, 5), (3, 40, 41), (10, 70, 64)], ids=lambda s: "x".join(map(str, s)))
+def test_df64_and_native_fp64_sweeps_agree(gblib, shape):
+    """The df64 sweeps and the native FP64 sweeps give the same
+    preconditioner to 1e-12 of its scale, and both meet ilu0a there."""
+    m, con, amat, rhs, x0 = dis_system(*shape)
+    v = np.random.default_rng(11).standard_normal(m.nodes)
+    zd = _precondition(gblib, shape, amat, con, v, native=False)
+    zn = _precondition(gblib, shape, amat, con, v, native=True)
+    o = oracle.Ims(oracle.settings(), con["ia"], con["ja"])
+    o.apply(amat.copy(), rhs.copy(), x0.copy())
+    zo = oracle.ilu0a(o.apc(), o.iapc(), o.japc(), v, fma=True)
+    scale = np.max(np.abs(zo))
+    assert np.max(np.abs(zd - zn)) <= 1e-12 * scale
+    assert np.max(np.abs(zd - zo)) <= 1e-12 * scale
+    assert np.max(np.abs(zn - zo)) <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("factor", [1e-40, 1e40])
+def test_out_of_float_range_factor_keeps_native_sweeps(gblib, factor):
+    """A system scaled so that its factor leaves the float exponent range
+    (inverse pivots near 1e40 or 1e-40) is swept in native FP64 and still
+    matches ilu0a; the residual scale that comes with it is tiny or huge."""
+    shape = (3, 40, 41)
+    m, con, amat, rhs, x0 = dis_system(*shape)
+    a = amat * factor
+    v = np.random.default_rng(12).standard_normal(m.nodes) * factor
+    z = _precondition(gblib, shape, a, con, v, native=False)
+    o = oracle.Ims(oracle.settings(), con["ia"], con["ja"])
+    o.apply(a.copy(), rhs.copy() * factor, x0.copy())
+    zo = oracle.ilu0a(o.apc(), o.iapc(), o.japc(), v, fma=True)
+    assert np.max(np.abs(z - zo)) <= 1e-12 * np.max(np.abs(zo))
+
+
+def test_df64_right_hand_side_extremes(gblib):
+    """df64 sweeps on right-hand sides that span many decades (1e-20 to 1e20
+    in one vector) stay within 1e-12 of ilu0a, relative to the result's
+    scale."""
+    shape = (2, 33, 40)
+    m, con, amat, rhs, x0 = dis_system(*shape)
+    rng = np.random.default_rng(13)
+    v = rng.standard_normal(m.nodes) * 10.0 ** rng.uniform(-20, 20, m.nodes)
+    z = _precondition(gblib, shape, amat, con, v, native=False)
+    o = oracle.Ims(oracle.settings(), con["ia"], con["ja"])
+    o.apply(amat.copy(), rhs.copy(), x0.copy())
+    zo = oracle.ilu0a(o.apc(), o.iapc(), o.japc(), v, fma=True)
+    assert np.max(np.abs(z - zo)) <= 1e-12 * np.max(np.abs(zo))
