@@ -24,6 +24,7 @@ extern "C" {
 
 #define GBIMS_OK 0
 #define GBIMS_WARN_PIVOT 1
+#define GBIMS_WARN_FALLBACK 2 /* gbsln_timestep_warm dropped its guess */
 #define GBIMS_ERR_ARG (-1)
 #define GBIMS_ERR_CUDA (-2)
 #define GBIMS_ERR_UNSUPPORTED (-3)
@@ -372,6 +373,16 @@ int gbsln_timestep(gbsln_handle *h, int kper, int kstp, double delt, gbsln_stats
  * unchanged, so a guess only changes how many iterations it takes. */
 int gbsln_timestep_guess(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
                          gbsln_stats *st);
+/* The warm start with its fallback (no counterpart in the reference, whose
+ * steps always start from the previous heads): the step starts from d_guess
+ * as gbsln_timestep_guess does, but when it has spent inner_cap inner
+ * iterations without closing, the guess is dropped and the step is solved
+ * again from the previous heads; then the status is GBIMS_WARN_FALLBACK and
+ * *st counts the iterations and device time of both attempts.  Give
+ * inner_cap the inner iterations the plain solver took on the previous step:
+ * a guess then never costs more than one step's worth of iterations. */
+int gbsln_timestep_warm(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
+                        int inner_cap, gbsln_stats *st);
 /* sln_buildsystem at the current heads (hold: previous-step heads, needed for
  * a transient step): the assembled amat (nja, CSR order of the DIS grid) and
  * rhs before the sln_ls fix-ups, copied to the host.  The reference writes
@@ -432,6 +443,24 @@ int gbmpnn_get_params(gbmpnn_handle *h, float *params);
 int gbmpnn_set_params(gbmpnn_handle *h, const float *params);
 const char *gbmpnn_last_error(const gbmpnn_handle *h);
 int gbmpnn_destroy(gbmpnn_handle *h);
+
+/* The scalings between heads and the network's units. */
+typedef struct gbmpnn_scaling {
+  double head_ref, head_scale; /* feature 1: (previous head - head_ref) / head_scale */
+  double dh_soft, dh_scale;    /* a head change dh in network units: asinh(dh / dh_soft) / dh_scale */
+  double unit_max;             /* bound on |output| in network units (0: none) */
+} gbmpnn_scaling;
+
+/* The guess for the next time step of a solution, on the device and on the
+ * solution's own stream (no host synchronisation): the features are built
+ * from d_static (nodes x 16 FP32: the static columns; columns 1 and 6 are
+ * replaced by the last step's heads and head change, the change taken as 0
+ * when first_step), the network runs, and d_guess (nodes, FP64) = heads +
+ * predicted change on active cells.  Pass d_guess to gbsln_timestep_warm or
+ * gbsln_timestep_guess.  device_ms (may be NULL) gets the device time of the
+ * guess; asking for it synchronises. */
+int gbsln_warm_guess(gbsln_handle *sln, gbmpnn_handle *net, const float *d_static,
+                     const gbmpnn_scaling *sc, int first_step, double *d_guess, float *device_ms);
 
 #ifdef __cplusplus
 }

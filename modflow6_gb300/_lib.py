@@ -15,6 +15,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libgbims.so"
 
 GBIMS_OK = 0
 GBIMS_WARN_PIVOT = 1
+GBIMS_WARN_FALLBACK = 2
 GBIMS_ERR_ARG = -1
 GBIMS_ERR_CUDA = -2
 GBIMS_ERR_UNSUPPORTED = -3
@@ -89,6 +90,11 @@ class GbslnStats(C.Structure):
     ]
 
 
+class GbmpnnScaling(C.Structure):
+    _fields_ = [("head_ref", C.c_double), ("head_scale", C.c_double), ("dh_soft", C.c_double),
+                ("dh_scale", C.c_double), ("unit_max", C.c_double)]
+
+
 class GbimsTuning(C.Structure):
     _fields_ = [
         ("sweep_config", C.c_int), ("sweep_chunk", C.c_int), ("sweep_ring", C.c_int),
@@ -159,6 +165,10 @@ _SIGS = {
     "gbmpnn_create": (C.c_int, [C.c_int, C.c_int, _ip, _ip, C.c_ulonglong, C.POINTER(C.c_void_p)]),
     "gbmpnn_set_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gbmpnn_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gbsln_warm_guess": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(GbmpnnScaling),
+                                   C.c_int, C.c_void_p, C.POINTER(C.c_float)]),
+    "gbsln_timestep_warm": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_void_p, C.c_int,
+                                      C.POINTER(GbslnStats)]),
     "gbmpnn_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
                                    C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "gbmpnn_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,

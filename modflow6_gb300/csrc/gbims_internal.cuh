@@ -287,6 +287,16 @@ int launch_scale(int iscl, int n, const int *ia, const int *ja, const int *cptr,
                  cudaStream_t st);
 void launch_unscale_x(int n, double *x, const double *dscale2, cudaStream_t st);
 
+// Device state of a time-step handle that the warm start reads: the heads of
+// the last step (x), those of the step before (xold), IBOUND and the stream.
+struct SlnView {
+  int n = 0;
+  const double *x = nullptr, *xold = nullptr;
+  const int *ibound = nullptr;
+  cudaStream_t st = nullptr;
+};
+int sln_view(gbsln_handle *h, SlnView *v);
+
 // IMS handle internals shared with the device-resident solution.
 void ims_buffers(gbims_handle *h, double **amat, double **rhs, double **x);
 cudaStream_t ims_stream(gbims_handle *h);

@@ -126,6 +126,35 @@ extern "C" int gbmpnn_set_graph(gbmpnn_handle *h, const double *d_amat) {
   return GBIMS_OK;
 }
 
+extern "C" int gbsln_warm_guess(gbsln_handle *sln, gbmpnn_handle *h, const float *d_static,
+                                const gbmpnn_scaling *sc, int first_step, double *d_guess,
+                                float *device_ms) {
+  if (!sln || !h || !d_static || !sc || !d_guess) return GBIMS_ERR_ARG;
+  SlnView v;
+  if (sln_view(sln, &v) != GBIMS_OK || v.n != h->n) return GBIMS_ERR_ARG;
+  if (!(sc->head_scale != 0.0) || !(sc->dh_soft > 0.0) || !(sc->dh_scale > 0.0))
+    return GBIMS_ERR_ARG;
+  const GuessScaling g{sc->head_ref, sc->head_scale, sc->dh_soft, sc->dh_scale, sc->unit_max};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (device_ms) {
+    MP_CUDA(h, cudaEventCreate(&e0));
+    MP_CUDA(h, cudaEventCreate(&e1));
+    MP_CUDA(h, cudaEventRecord(e0, v.st));
+  }
+  // on the time step's own stream: the step that reads the guess follows in
+  // stream order, with no host synchronisation in between
+  mpnn_guess(h->D, d_static, v.x, v.xold, first_step, v.ibound, g, d_guess, v.st);
+  MP_CUDA(h, cudaGetLastError());
+  if (device_ms) {
+    MP_CUDA(h, cudaEventRecord(e1, v.st));
+    MP_CUDA(h, cudaEventSynchronize(e1));
+    MP_CUDA(h, cudaEventElapsedTime(device_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  return GBIMS_OK;
+}
+
 extern "C" int gbmpnn_forward(gbmpnn_handle *h, const float *d_x, float *d_y) {
   if (!h || !d_x || !d_y) return GBIMS_ERR_ARG;
   mpnn_forward(h->D, d_x, nullptr, nullptr, 0.f, h->st);

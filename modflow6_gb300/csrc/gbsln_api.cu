@@ -442,7 +442,10 @@ static int reduce_host(gbsln_handle *h, bool max_not_sum, double *out) {
 }
 
 static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
-                         gbsln_stats *st);
+                         gbsln_stats *st, int inner_cap = 0);
+// timestep_core's status when a guessed step has used its inner-iteration
+// budget without closing (internal; gbsln_timestep_warm falls back on it)
+constexpr int kCapReached = 1000;
 
 extern "C" int gbsln_timestep(gbsln_handle *h, int kper, int kstp, double delt, gbsln_stats *st) {
   return timestep_core(h, kper, kstp, delt, nullptr, st);
@@ -454,8 +457,34 @@ extern "C" int gbsln_timestep_guess(gbsln_handle *h, int kper, int kstp, double 
   return timestep_core(h, kper, kstp, delt, d_guess, st);
 }
 
+extern "C" int gbsln_timestep_warm(gbsln_handle *h, int kper, int kstp, double delt,
+                                   const double *d_guess, int inner_cap, gbsln_stats *st) {
+  if (!h || !d_guess || inner_cap < 1) return GBIMS_ERR_ARG;
+  gbsln_stats a;
+  memset(&a, 0, sizeof(a));
+  int rc = timestep_core(h, kper, kstp, delt, d_guess, &a, inner_cap);
+  if (rc != kCapReached) {
+    if (st) *st = a;
+    return rc;
+  }
+  // fall back: the step again from the previous heads (xold still holds
+  // them: the guess only ever replaced the first iterate)
+  SLN_CUDA(h, cudaMemcpyAsync(h->x, h->xold, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
+  gbsln_stats b;
+  memset(&b, 0, sizeof(b));
+  rc = timestep_core(h, kper, kstp, delt, nullptr, &b);
+  b.inner_total += a.inner_total;
+  b.fill_ms += a.fill_ms;
+  b.solve_ms += a.solve_ms;
+  b.total_ms += a.total_ms;
+  b.pivot_retries += a.pivot_retries;
+  b.backtracks += a.backtracks;
+  if (st) *st = b;
+  return rc < 0 ? rc : GBIMS_WARN_FALLBACK;
+}
+
 static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
-                         gbsln_stats *st) {
+                         gbsln_stats *st, int inner_cap) {
   if (!h || !h->ims) return GBIMS_ERR_ARG;
   const int n = h->n;
   const bool transient = (delt > 0.0) && h->has_sto;
@@ -500,6 +529,16 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
     return rc;
   };
   for (int kiter = 1; kiter <= h->nl.mxiter; ++kiter) {
+    if (d_guess && inner_cap > 0 && kiter > 1 && s.inner_total >= inner_cap) {
+      // the guessed step has used its budget without closing
+      SLN_CUDA(h, cudaEventRecord(h->e1, h->st));
+      SLN_CUDA(h, cudaEventSynchronize(h->e1));
+      float tot = 0.f;
+      cudaEventElapsedTime(&tot, h->e0, h->e1);
+      s.total_ms = tot;
+      if (st) *st = s;
+      return kCapReached;
+    }
     if (h->nl.numtrack > 0) {
       // sln_backtracking (NumericalSolution.f90:2680-2760): from the second
       // outer iteration on, while the residual norm exceeds BTOL times the
@@ -764,6 +803,18 @@ extern "C" int gbsln_set_heads(gbsln_handle *h, const double *x) {
 }
 
 extern "C" gbims_handle *gbsln_ims(gbsln_handle *h) { return h ? h->ims : nullptr; }
+
+namespace gb {
+int sln_view(gbsln_handle *h, SlnView *v) {
+  if (!h || !v || !h->ims) return GBIMS_ERR_ARG;
+  v->n = h->n;
+  v->x = h->x;
+  v->xold = h->xold;
+  v->ibound = h->ibound;
+  v->st = h->st;
+  return GBIMS_OK;
+}
+}  // namespace gb
 
 extern "C" int gbsln_destroy(gbsln_handle *h) {
   if (!h) return GBIMS_OK;

@@ -225,20 +225,39 @@ __global__ void __launch_bounds__(256) k_ilu_sweep_sf(int n, const int *__restri
       j0 = japc[row];
       j1 = iapc[row + 1];
     }
-    for (int j = j0; j < j1; ++j) {
-      const LLWord<T> *w = out + japc[j];
-      T v;
-      if (!ll_get(w, ep, v)) {
-        const unsigned long long t0 = gtimer();
-        while (!ll_get(w, ep, v)) {
-          if ((vdone && *vdone) || gtimer() - t0 > kWaitNs) {
-            atomicExch(err, 1);
-            if (ctl) ctl->done = 1;
-            return;
+    // the words of up to kDeps dependencies are loaded together, then the
+    // missing ones polled (with a growing pause, so that spinning threads do
+    // not crowd the L2 the producers write through); the FMAs then run in
+    // JAPC order
+    constexpr int kDeps = 8;
+    for (int jb = j0; jb < j1; jb += kDeps) {
+      LLRaw w[kDeps];
+      const int nd = min(kDeps, j1 - jb);
+#pragma unroll
+      for (int q2 = 0; q2 < kDeps; ++q2)
+        if (q2 < nd) ll_issue(out + japc[jb + q2], w[q2]);
+#pragma unroll
+      for (int q2 = 0; q2 < kDeps; ++q2) {
+        if (q2 >= nd) break;
+        T v;
+        if (ll_ready<T>(w[q2], ep)) {
+          ll_take(w[q2], v);
+        } else {
+          const LLWord<T> *pw = out + japc[jb + q2];
+          const unsigned long long t0 = gtimer();
+          unsigned pause = 32;
+          while (!ll_get(pw, ep, v)) {
+            if ((vdone && *vdone) || gtimer() - t0 > kWaitNs) {
+              atomicExch(err, 1);
+              if (ctl) ctl->done = 1;
+              return;
+            }
+            __nanosleep(pause);
+            if (pause < 512) pause <<= 1;
           }
         }
+        tv = fms<T>(apc[jb + q2], v, tv);
       }
-      tv = fms<T>(apc[j], v, tv);
     }
     if (DIR < 0) {
       tv = tv * apc[row];

@@ -333,6 +333,11 @@ __global__ void __launch_bounds__(256) k_cg_pupdate32(int n, const float *__rest
 
 // x += alpha*p ; d -= alpha*q ; max|alpha p|, max|d|, sum d^2 (FP64 path).
 // partial slots: [0]=l2, [1]=dx val, [2]=dx idx, [3]=r val, [4]=r idx, [5]=nonfinite
+// The sum of squares is taken only when the closure test reads it (L2 =
+// true: RCLOSE options L2NORM_RCLOSE and RELATIVE_RCLOSE, ICNVGOPT 2-4); with
+// the infinity-norm tests the reference computes it but never reads it
+// inside the loop, and on GB300 it is a quarter of the kernel's FP64 work.
+template <bool L2>
 __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__restrict__ x,
                                                             double *__restrict__ d,
                                                             const double *__restrict__ p,
@@ -352,7 +357,7 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__rest
     double di = fma(-alpha, qi, dI);
     d[i] = di;
     if (absgt(di, m[1].val)) { m[1].val = di; m[1].idx = i; }
-    v[0] = fma(di, di, v[0]);
+    if (L2) v[0] = fma(di, di, v[0]);
     nf |= nonfinite(di) | nonfinite(tv);
   };
   // two rows per trip, loads first (same order of rows as one per trip)
@@ -647,7 +652,8 @@ __global__ void k_ctl_omega(Ctl *ctl, const double *part, int G) {
 }
 
 // x += alpha*phat + omega*qhat ; d = q - omega*t (ImsLinearBase.f90:428-480).
-template <typename T>
+// L2 as in k_cg_update64.
+template <typename T, bool L2>
 __global__ void __launch_bounds__(kRedBlock) k_bcgs_update(int n, double *__restrict__ x,
                                                             T *__restrict__ d,
                                                             const T *__restrict__ phat,
@@ -674,7 +680,7 @@ __global__ void __launch_bounds__(kRedBlock) k_bcgs_update(int n, double *__rest
     double rv = to_d(di);
     if (dscale) rv = rv / dscale[i];
     if (absgt(rv, m[1].val)) { m[1].val = rv; m[1].idx = i; }
-    v[0] = fma(rv, rv, v[0]);
+    if (L2) v[0] = fma(rv, rv, v[0]);
     nf |= nonfinite(rv) | nonfinite(tv);
   }
   v[1] = (double)nf;
@@ -920,6 +926,11 @@ __device__ void ctl_set_l2norm0(Ctl *ctl, const double *part, int G) {
 }
 __global__ void k_ctl_set_l2norm0(Ctl *ctl, const double *part, int G) {
   ctl_set_l2norm0(ctl, part, G);
+}
+// The L2 norm of the final residual, for a loop that did not take it.
+__global__ void k_ctl_set_l2norm(Ctl *ctl, const double *part, int G) {
+  double s = ctl_reduce_sum(part, G);
+  if (threadIdx.x == 0 && ctl->l2norm0 != 0.0) ctl->l2norm = sqrt(s);
 }
 
 // ---------------------------------------------------------------------------
@@ -1259,6 +1270,9 @@ void kr_sumsq64(int n, const double *a, double *part, int G, cudaStream_t st) {
 void kr_ctl_set_l2norm0(Ctl *ctl, const double *part, int G, cudaStream_t st) {
   k_ctl_set_l2norm0<<<1, kRedBlock, 0, st>>>(ctl, part, G);
 }
+void kr_ctl_set_l2norm(Ctl *ctl, const double *part, int G, cudaStream_t st) {
+  k_ctl_set_l2norm<<<1, kRedBlock, 0, st>>>(ctl, part, G);
+}
 void kr_ctl_cg_rho(Ctl *ctl, const double *part, int G, cudaStream_t st) {
   k_ctl_cg_rho<<<1, kRedBlock, 0, st>>>(ctl, part, G);
 }
@@ -1269,8 +1283,9 @@ void kr_cg_pupdate64(int n, const double *z, double *p, const Ctl *ctl, cudaStre
   k_cg_pupdate64<<<egrid(n), 256, 0, st>>>(n, z, p, ctl);
 }
 void kr_cg_update64(int n, double *x, double *d, const double *p, const double *q, double *part,
-                    int G, const Ctl *ctl, cudaStream_t st) {
-  k_cg_update64<<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
+                    int G, const Ctl *ctl, cudaStream_t st, bool l2) {
+  if (l2) k_cg_update64<true><<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
+  else k_cg_update64<false><<<G, kRedBlock, 0, st>>>(n, x, d, p, q, part, ctl);
 }
 void kr_rec_models(bool bcgs, int nm, const int *modstart, const double *p, const double *q,
                    const double *d, const double *dscale, double *part, int G, const Ctl *ctl,
@@ -1309,13 +1324,14 @@ void kr_ctl_omega(Ctl *ctl, const double *part, int G, cudaStream_t st) {
 }
 void kr_bcgs_update64(int n, double *x, double *d, const double *phat, const double *qhat,
                       const double *q, const double *t, const double *dscale, double *part, int G,
-                      const Ctl *ctl, cudaStream_t st) {
-  k_bcgs_update<double><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
+                      const Ctl *ctl, cudaStream_t st, bool l2) {
+  if (l2) k_bcgs_update<double, true><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
+  else k_bcgs_update<double, false><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
 }
 void kr_bcgs_update32(int n, double *x, float *d, const float *phat, const float *qhat,
                       const float *q, const float *t, const double *dscale, double *part, int G,
                       const Ctl *ctl, cudaStream_t st) {
-  k_bcgs_update<float><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
+  k_bcgs_update<float, true><<<G, kRedBlock, 0, st>>>(n, x, d, phat, qhat, q, t, dscale, part, ctl);
 }
 void kr_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond,
                       cudaStream_t st) {

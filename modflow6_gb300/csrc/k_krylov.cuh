@@ -7,10 +7,13 @@ void kr_dot64(int n, const double *a, const double *b, double *part, int G, cons
 void kr_dot_tq_tt64(int n, const double *t, const double *q, double *part, int G, const Ctl *ctl, cudaStream_t st);
 void kr_sumsq64(int n, const double *a, double *part, int G, cudaStream_t st);
 void kr_ctl_set_l2norm0(Ctl *ctl, const double *part, int G, cudaStream_t st);
+// Ctl::l2norm of the residual from sum-of-squares partials (after a loop that skipped it).
+void kr_ctl_set_l2norm(Ctl *ctl, const double *part, int G, cudaStream_t st);
 void kr_ctl_cg_rho(Ctl *ctl, const double *part, int G, cudaStream_t st);
 void kr_ctl_alpha(Ctl *ctl, const double *part, int G, cudaStream_t st);
 void kr_cg_pupdate64(int n, const double *z, double *p, const Ctl *ctl, cudaStream_t st);
-void kr_cg_update64(int n, double *x, double *d, const double *p, const double *q, double *part, int G, const Ctl *ctl, cudaStream_t st);
+// l2: take the sum of squares of the new residual (the RCLOSE L2 options)
+void kr_cg_update64(int n, double *x, double *d, const double *p, const double *q, double *part, int G, const Ctl *ctl, cudaStream_t st, bool l2);
 // Per-model maxima of the inner records (CONVNMOD > 1): PCG p = P, q unused;
 // BiCGSTAB p = PHAT, q = QHAT; d the updated residual.
 void kr_rec_models(bool bcgs, int nm, const int *modstart, const double *p, const double *q, const double *d, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st);
@@ -19,7 +22,7 @@ void kr_ctl_bcgs_rho(Ctl *ctl, const double *part, int G, cudaStream_t st);
 void kr_bcgs_p64(int n, const double *d, double *p, const double *v, const Ctl *ctl, cudaStream_t st);
 void kr_bcgs_q64(int n, const double *d, const double *v, double *q, const Ctl *ctl, cudaStream_t st);
 void kr_ctl_omega(Ctl *ctl, const double *part, int G, cudaStream_t st);
-void kr_bcgs_update64(int n, double *x, double *d, const double *phat, const double *qhat, const double *q, const double *t, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st);
+void kr_bcgs_update64(int n, double *x, double *d, const double *phat, const double *qhat, const double *q, const double *t, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st, bool l2);
 void kr_ctl_bcgs_cnvg(Ctl *ctl, const double *part, int G, unsigned long long cond, int use_cond, cudaStream_t st);
 void kr_ctl_mixed_inner(Ctl *ctl, const double *part, int G, int bcgs, double refine_factor, cudaStream_t st);
 void kr_true_resid_stats(int n, const double *r, float *d32, float *dhat32, double *dhat64, const double *dscale, double *part, int G, const Ctl *ctl, cudaStream_t st);

@@ -390,14 +390,71 @@ void mpnn_refresh_bf16(MpnnDev &D, cudaStream_t st) {
                                                           D.wbf[l - 1]);
 }
 
+// The network's input for a warm-start guess, written as BF16: the static
+// columns of `stat` (n x kIn: standardised ln K, well rate, CHD mask, layer
+// position, bias), column 1 the previous heads (x - head_ref) / head_scale,
+// column 6 the previous step's head change in network units
+// asinh(dh / dh_soft) / dh_scale (zero on the first step and on inactive
+// cells).
+__global__ void k_guess_features(int n, const float *__restrict__ stat, const double *__restrict__ x,
+                                 const double *__restrict__ xold, int first,
+                                 const int *__restrict__ ibound, GuessScaling sc,
+                                 __nv_bfloat16 *__restrict__ xbf) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < (long long)n * kIn;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(q / kIn), f = (int)(q % kIn);
+    float v;
+    if (f == 1) {
+      v = (float)((x[i] - sc.head_ref) / sc.head_scale);
+    } else if (f == 6) {
+      const double dh = (first || ibound[i] <= 0) ? 0.0 : x[i] - xold[i];
+      v = (float)(asinh(dh / sc.dh_soft) / sc.dh_scale);
+    } else {
+      v = stat[q];
+    }
+    xbf[q] = __float2bfloat16(v);
+  }
+}
+
+// guess = x + sinh(clamp(y) * dh_scale) * dh_soft on active cells, x elsewhere
+__global__ void k_guess_out(int n, const float *__restrict__ y, const double *__restrict__ x,
+                            const int *__restrict__ ibound, GuessScaling sc,
+                            double *__restrict__ guess) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double u = (double)y[i];
+    if (sc.unit_max > 0.0) u = fmin(fmax(u, -sc.unit_max), sc.unit_max);
+    const double dh = sinh(u * sc.dh_scale) * sc.dh_soft;
+    guess[i] = (ibound[i] > 0) ? x[i] + dh : x[i];
+  }
+}
+
+static void forward_from_xbf(MpnnDev &D, const float *target, const float *mask, float inv_count,
+                             cudaStream_t st);
+
+void mpnn_guess(MpnnDev &D, const float *d_static, const double *x, const double *xold,
+                int first, const int *ibound, const GuessScaling &sc, double *guess,
+                cudaStream_t st) {
+  const int n = D.n;
+  k_guess_features<<<ngrid((long long)n * kIn, 256), 256, 0, st>>>(n, d_static, x, xold, first,
+                                                                    ibound, sc, D.xbf);
+  forward_from_xbf(D, nullptr, nullptr, 0.f, st);
+  k_guess_out<<<ngrid(n, 256), 256, 0, st>>>(n, D.y, x, ibound, sc, guess);
+}
+
 // Forward pass from features (N x kIn FP32); y (N) written.  With a target,
 // the loss and dy are produced too.
 void mpnn_forward(MpnnDev &D, const float *d_x, const float *target, const float *mask,
                   float inv_count, cudaStream_t st) {
+  const int n = D.n;
+  k_f32_to_bf16<<<ngrid((long long)n * kIn, 256), 256, 0, st>>>((long long)n * kIn, d_x, D.xbf);
+  forward_from_xbf(D, target, mask, inv_count, st);
+}
+
+static void forward_from_xbf(MpnnDev &D, const float *target, const float *mask, float inv_count,
+                             cudaStream_t st) {
   using P = MpnnLayout;
   const int n = D.n;
   const int gb = (n + 63) / 64;
-  k_f32_to_bf16<<<ngrid((long long)n * kIn, 256), 256, 0, st>>>((long long)n * kIn, d_x, D.xbf);
   k_gemm_rows<kIn, 0, kH, 1><<<gb, 128, 0, st>>>(n, D.xbf, nullptr, D.bt0, D.p + P::b0, nullptr,
                                                   D.H[0], D.Hbf[0], D.mask[0]);
   const int ga = (int)(((long long)n * 32 + 255) / 256);

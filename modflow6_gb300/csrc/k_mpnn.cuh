@@ -38,5 +38,14 @@ void mpnn_forward(MpnnDev &D, const float *d_x, const float *target, const float
                   float inv_count, cudaStream_t st);
 void mpnn_backward(MpnnDev &D, cudaStream_t st);
 void mpnn_adam(MpnnDev &D, float lr, cudaStream_t st);
+// The warm start's guess on the device: features from the last two steps'
+// heads (x, xold; xold ignored when first), the forward pass, and
+// guess = x + the predicted change on active cells.
+struct GuessScaling {
+  double head_ref, head_scale, dh_soft, dh_scale, unit_max;
+};
+void mpnn_guess(MpnnDev &D, const float *d_static, const double *x, const double *xold,
+                int first, const int *ibound, const GuessScaling &sc, double *guess,
+                cudaStream_t st);
 
 }  // namespace gb

@@ -8,8 +8,9 @@ cell's K, the previous heads, the previous step's head change, the well
 rates and the boundary mask.  The
 prediction is only an initial guess: PCG + ILU0 still runs to the same
 INNER_DVCLOSE / INNER_RCLOSE closure, so the plain solver stays the judge.
-A guess that costs more inner iterations than the previous heads is
-discarded (the fallback rule `evaluate` reports).
+The guessed step may spend at most the inner iterations the plain solver took
+on the previous step; past that the guess is dropped and the step is solved
+from the previous heads (gbsln_timestep_warm).
 
 `Graph.features` builds the 16 input features of the cells, `generate` the
 training samples (heads from the plain solver), `WarmStartNet` wraps the C
@@ -248,21 +249,57 @@ def train(net: WarmStartNet, data, dh_scale: float, epochs: int = 4,
     return hist
 
 
+def scaling(net: WarmStartNet) -> _lib.GbmpnnScaling:
+    """The head <-> network-unit scalings of gbsln_warm_guess."""
+    return _lib.GbmpnnScaling(HEAD_REF, HEAD_SCALE, DH_SOFT, float(net.dh_scale), float(net.unit_max))
+
+
+def warm_guess(sol: GwfSolution, net: WarmStartNet, g: Graph, guess, first: bool) -> float:
+    """The network's guess for `sol`'s next step into the device tensor
+    `guess`, built and evaluated on the device on the solution's stream
+    (gbsln_warm_guess); returns its device time in ms."""
+    lib = _lib.load()
+    ms = C.c_float(0.0)
+    sc = scaling(net)
+    rc = lib.gbsln_warm_guess(sol._h, net._h, C.c_void_p(g.static.data_ptr()), C.byref(sc),
+                              1 if first else 0, C.c_void_p(guess.data_ptr()), C.byref(ms))
+    if rc < 0:
+        raise _lib.GbimsError(rc, net._err())
+    return float(ms.value)
+
+
+def timestep_warm(sol: GwfSolution, kper: int, kstp: int, delt: float, guess, inner_cap: int):
+    """gbsln_timestep_warm: the step from the guess, dropped in favour of the
+    previous heads once it has spent inner_cap inner iterations without
+    closing.  Returns (stats, fell_back)."""
+    lib = _lib.load()
+    st = _lib.GbslnStats()
+    rc = lib.gbsln_timestep_warm(sol._h, kper, kstp, delt, C.c_void_p(guess.data_ptr()),
+                                 int(inner_cap), C.byref(st))
+    if rc < 0:
+        raise _lib.GbimsError(rc, lib.gbsln_last_error(sol._h).decode())
+    return {f: getattr(st, f) for f, _ in st._fields_}, rc == _lib.GBIMS_WARN_FALLBACK
+
+
 def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0,
              delt: float = C5_DELT) -> dict:
-    """Held-out models: every step solved from the previous heads and, in a
-    second solution of the same model, from the network's guess, both to the
-    same closure.  Reported: inner iterations of both; the iterations with the
-    fallback rule (per step, the guess is discarded when it cost more
-    iterations than the previous heads); the RMS and maximum error of the
-    guess and of the previous heads against the converged heads; device time."""
+    """Held-out models, solved twice to the same closure: every step from the
+    previous heads (the plain solver), and from the network's guess with the
+    fallback rule (gbsln_timestep_warm: the guessed step may spend at most
+    the inner iterations the plain solver took on the previous step; past
+    that the guess is dropped and the step solved from the previous heads,
+    those iterations counted too).  The guess is built, evaluated and used on
+    the device with no host round trip in between.  Reported: inner
+    iterations and device time of both paths (the warm path's time includes
+    inference and any fallbacks), the steps that fell back, and the RMS and
+    maximum error of the guess and of the previous heads against the
+    converged heads."""
     import torch
 
-    it_prev, it_warm = [], []
+    it_prev, it_warm, fell = [], [], 0
     rms_g, rms_p, max_g, max_p = [], [], [], []
     ms_prev, ms_warm, ms_net = 0.0, 0.0, 0.0
     converged = True
-    dsc = net.dh_scale
     for s in seeds:
         m = c5_model(s, scale)
         g = Graph(m)
@@ -270,21 +307,17 @@ def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0
         amat, _ = base.formulate(delt, hold=m.strt)
         net.set_graph(torch.from_numpy(amat).cuda())
         nact = float(g.active64.sum().item())
-        dh_last = torch.zeros(m.nodes, dtype=torch.float64, device="cuda")
+        guess = torch.empty(m.nodes, dtype=torch.float64, device="cuda")
+        cap_unbounded = 10 ** 9
+        last_plain = None
         for kstp in range(1, steps + 1):
             st_b = base.timestep(1, kstp, delt)
             h_prev = torch.from_numpy(warm.heads).cuda()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            y = net.predict(g.features(h_prev, dh_last, dsc))
-            if net.unit_max > 0.0:
-                y = y.clamp(-net.unit_max, net.unit_max)
-            dh = from_unit(y.double() * dsc)
-            guess = (h_prev + dh * g.active64).contiguous()
-            e1.record()
-            e1.synchronize()
-            ms_net += e0.elapsed_time(e1)
-            st_w = warm.timestep(1, kstp, delt, guess=guess.data_ptr())
+            ms_net += warm_guess(warm, net, g, guess, first=(kstp == 1))
+            cap = cap_unbounded if last_plain is None else max(1, last_plain)
+            st_w, fb = timestep_warm(warm, 1, kstp, delt, guess, cap)
+            fell += int(fb)
+            last_plain = st_b["inner_total"]
             h_true = torch.from_numpy(warm.heads).cuda()
             eg = (guess - h_true) * g.active64
             ep = (h_prev - h_true) * g.active64
@@ -292,7 +325,6 @@ def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0
             rms_p.append(float(torch.sqrt((ep * ep).sum() / nact).item()))
             max_g.append(float(eg.abs().max().item()))
             max_p.append(float(ep.abs().max().item()))
-            dh_last = (h_true - h_prev) * g.active64
             it_prev.append(st_b["inner_total"])
             it_warm.append(st_w["inner_total"])
             ms_prev += st_b["total_ms"]
@@ -303,10 +335,11 @@ def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0
     ip, iw = np.array(it_prev), np.array(it_warm)
     return {"models": len(seeds), "steps": int(ip.size), "all_converged": converged,
             "inner_prev_heads": int(ip.sum()), "inner_warm": int(iw.sum()),
-            "inner_with_fallback": int(np.minimum(ip, iw).sum()),
+            "fallbacks": fell,
             "steps_guess_better": int((iw < ip).sum()), "steps_guess_worse": int((iw > ip).sum()),
             "iteration_ratio": float(iw.sum() / max(1, ip.sum())),
             "solve_ms_prev_heads": ms_prev, "solve_ms_warm": ms_warm, "inference_ms": ms_net,
+            "inference_ms_per_guess": ms_net / max(1, ip.size),
             "time_ratio": (ms_warm + ms_net) / max(1e-9, ms_prev),
             "rms_err_guess": float(np.mean(rms_g)), "rms_err_prev_heads": float(np.mean(rms_p)),
             "max_err_guess": float(np.max(max_g)), "max_err_prev_heads": float(np.max(max_p))}
