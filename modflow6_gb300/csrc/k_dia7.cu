@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   unsigned long long *full = reinterpret_cast<unsigned long long *>(smem_raw + NS * sizeof(St));
   unsigned long long *empty = full + NS;
   unsigned long long *prep = full + 2 * NS;
+  unsigned long long *zfree = full + 3 * NS;  // df64 backward: the copy warp has read zo
   __shared__ int s_id, s_abort, s_rot, s_m;
   __shared__ unsigned s_ep;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -261,6 +262,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
       mbar_init(&prep[s], 2);  // pre-compute warp + edge warp
+      mbar_init(&zfree[s], 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -474,7 +476,6 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         const bool got = mbar_wait(&empty[s], ((c / NS) - 1) & 1, v_abort);
         ok = __all_sync(0xffffffffu, got);
         if (!ok) break;
-        if constexpr (DIR < 0 && kStagedOut<T>) flush(c - NS);
       }
       if (lane == 0) {
         St &st = stg[s];
@@ -500,6 +501,16 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         bulk_g2s(st.x, p.X + tb, tileb, &full[s]);
       }
       issued = c + 1;
+      if constexpr (DIR < 0 && kStagedOut<T>) {
+        // the results of the chunk that last used this buffer, written out
+        // while the new tiles are in flight (zo is no copy target); the
+        // compute warp waits on zfree before it writes zo again
+        if (c >= NS) {
+          flush(c - NS);
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&zfree[s]);
+        }
+      }
     }
     if (!ok) fail();
     if constexpr (DIR < 0 && kStagedOut<T>) {
@@ -535,6 +546,15 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     if (!__all_sync(0xffffffffu, got)) {
       if (lane == 0) *v_abort = 1;
       return;
+    }
+    if constexpr (DIR < 0 && kStagedOut<T>) {
+      if (c >= NS) {
+        const bool zf = mbar_wait(&zfree[s], ((c / NS) - 1) & 1, v_abort);
+        if (!__all_sync(0xffffffffu, zf)) {
+          if (lane == 0) *v_abort = 1;
+          return;
+        }
+      }
     }
     St &st = stg[s];
     const int g0 = c * C;
@@ -691,7 +711,7 @@ constexpr int kNumSweepCfgs = sizeof(kSweepCfgs) / sizeof(kSweepCfgs[0]);
 
 template <typename T, int C, int NS, int DIR>
 constexpr size_t stage_bytes() {
-  return NS * sizeof(Stage<T, C, DIR>) + 3 * NS * sizeof(unsigned long long);
+  return NS * sizeof(Stage<T, C, DIR>) + 4 * NS * sizeof(unsigned long long);
 }
 static_assert(stage_bytes<double, 16, 2, -1>() <= 72 * 1024 && stage_bytes<double, 4, 8, -1>() <= 72 * 1024 &&
                   stage_bytes<double, 8, 4, -1>() <= 72 * 1024,
