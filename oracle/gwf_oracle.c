@@ -371,6 +371,202 @@ void or_npf_nur(const or_gwf_model *m, const int *ibound, double *x, const doubl
 }
 
 /* ------------------------------------------------------------------------ */
+/* DISV connectivity                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* DisvGeom.f90:416-427, distance */
+static double disv_distance(double x1, double y1, double x2, double y2) {
+  double d = (x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2);
+  return sqrt(d);
+}
+
+/* DisvGeom.f90:432-445, distance_normal */
+static double disv_distance_normal(double x0, double y0, double x1, double y1, double x2,
+                                   double y2) {
+  double d = fabs((x2 - x1) * (y1 - y0) - (x1 - x0) * (y2 - y1));
+  return d / disv_distance(x1, y1, x2, y2);
+}
+
+/* DisvGeom.f90:302-332, shared_edge: the first consecutive pair of cell 1's
+ * (closed) vertex list found reversed in cell 2's list. */
+static void disv_shared_edge(const int *l1, int nv1, const int *l2, int nv2, int *iv1, int *iv2) {
+  *iv1 = -1;
+  *iv2 = -1;
+  for (int a = 0; a < nv1 - 1; ++a) {
+    for (int b = nv2 - 1; b >= 1; --b) {
+      if (l1[a] == l2[b] && l1[a + 1] == l2[b - 1]) {
+        *iv1 = l1[a];
+        *iv2 = l1[a + 1];
+        return;
+      }
+    }
+  }
+}
+
+/* DisvGeom.f90:339-386, get_area (shoelace over the closed vertex list) */
+static double disv_area(int j, const int *iavert, const int *javert, const double *vx,
+                        const double *vy) {
+  double area = 0.0;
+  const int i0 = iavert[j], i1 = iavert[j + 1];
+  const int nvert = i1 - i0;
+  const double x1 = vx[javert[i0]], y1 = vy[javert[i0]];
+  int icount = 1;
+  for (int iv = i0; iv < i1; ++iv) {
+    double x = vx[javert[iv]];
+    double y = (icount < nvert) ? vy[javert[iv + 1]] : vy[javert[i0]];
+    area = area + (x - x1) * (y - y1);
+    icount++;
+  }
+  icount = 1;
+  for (int iv = i0; iv < i1; ++iv) {
+    double y = vy[javert[iv]];
+    double x = (icount < nvert) ? vx[javert[iv + 1]] : vx[javert[i0]];
+    area = area - (x - x1) * (y - y1);
+    icount++;
+  }
+  return fabs(area) * 0.5;
+}
+
+static int cmp_int(const void *a, const void *b) {
+  int x = *(const int *)a, y = *(const int *)b;
+  return (x > y) - (x < y);
+}
+
+/* Connections.f90:702-796 disvconnections with vertexconnect (:1272-1361) on
+ * a full grid (no IDOMAIN): node n = j + k*ncpl (GeomUtil.f90 get_node), the
+ * cell's vertex list closed as Disv.f90:548-585 define_cellverts closes it
+ * (0-based vertex numbers; iavert ncpl+1).  Each row: the diagonal, the cell
+ * above and below, then every cell of the same layer that shares an edge,
+ * collected over the vertices as vertexconnect does; the off-diagonals sorted
+ * ascending (Sparse.f90:217-239).  Then fillisym/filljas and cprops
+ * (DisvGeom.f90:136-202) for every n < m.  cap bounds nja; returns nja, or
+ * -1 if cap is too small. */
+int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, const int *iavert,
+                    const int *javert, const double *xc, const double *yc, const double *top,
+                    const double *bot, int cap, int *ia, int *ja, int *isym, int *jas, int *ihc,
+                    double *cl1, double *cl2, double *hwva, double *area) {
+  const int nodes = nlay * ncpl;
+  int nvert = 0;
+  for (int q = 0; q < iavert[ncpl]; ++q)
+    if (javert[q] + 1 > nvert) nvert = javert[q] + 1;
+  /* cells of each vertex (vertcellspm), in cell order */
+  int *vcnt = (int *)calloc(nvert + 1, sizeof(int));
+  for (int j = 0; j < ncpl; ++j)
+    for (int q = iavert[j]; q < iavert[j + 1]; ++q) vcnt[javert[q] + 1]++;
+  for (int v = 0; v < nvert; ++v) vcnt[v + 1] += vcnt[v];
+  int *vcell = (int *)malloc(sizeof(int) * (vcnt[nvert] + 1));
+  int *vfill = (int *)malloc(sizeof(int) * (nvert + 1));
+  memcpy(vfill, vcnt, sizeof(int) * (nvert + 1));
+  for (int j = 0; j < ncpl; ++j)
+    for (int q = iavert[j]; q < iavert[j + 1]; ++q) vcell[vfill[javert[q]]++] = j;
+  /* rows as growing lists without duplicates */
+  int rowcap = 64;
+  int *rows = (int *)malloc(sizeof(int) * (size_t)nodes * rowcap);
+  int *rn = (int *)calloc(nodes, sizeof(int));
+  int overflow = 0;
+#define DISV_ADD(r, c)                                              \
+  do {                                                              \
+    int dup_ = 0;                                                   \
+    for (int t_ = 0; t_ < rn[r]; ++t_)                              \
+      if (rows[(size_t)(r) * rowcap + t_] == (c)) dup_ = 1;         \
+    if (!dup_) {                                                    \
+      if (rn[r] < rowcap) rows[(size_t)(r) * rowcap + rn[r]++] = (c); \
+      else overflow = 1;                                            \
+    }                                                               \
+  } while (0)
+  for (int k = 0; k < nlay; ++k)
+    for (int j = 0; j < ncpl; ++j) {
+      int nr = j + k * ncpl;
+      DISV_ADD(nr, nr);
+      if (k > 0) DISV_ADD(nr, j + (k - 1) * ncpl);
+      if (k < nlay - 1) DISV_ADD(nr, j + (k + 1) * ncpl);
+    }
+  for (int v = 0; v < nvert; ++v)
+    for (int c1 = vcnt[v]; c1 < vcnt[v + 1]; ++c1) {
+      int j1 = vcell[c1];
+      for (int k = 0; k < nlay; ++k) {
+        int nr = j1 + k * ncpl;
+        for (int c2 = vcnt[v]; c2 < vcnt[v + 1]; ++c2) {
+          int j2 = vcell[c2];
+          if (j1 == j2) continue;
+          int mr = j2 + k * ncpl;
+          int a, b;
+          disv_shared_edge(javert + iavert[j1], iavert[j1 + 1] - iavert[j1], javert + iavert[j2],
+                           iavert[j2 + 1] - iavert[j2], &a, &b);
+          if (a >= 0 && b >= 0) DISV_ADD(nr, mr);
+        }
+      }
+    }
+#undef DISV_ADD
+  int nja = 0;
+  for (int n = 0; n < nodes; ++n) nja += rn[n];
+  if (overflow || nja > cap) {
+    free(vcnt); free(vcell); free(vfill); free(rows); free(rn);
+    return -1;
+  }
+  ia[0] = 0;
+  for (int n = 0; n < nodes; ++n) {
+    int *r = rows + (size_t)n * rowcap;
+    qsort(r + 1, rn[n] - 1, sizeof(int), cmp_int); /* diagonal stays in front */
+    for (int t = 0; t < rn[n]; ++t) ja[ia[n] + t] = r[t];
+    ia[n + 1] = ia[n] + rn[n];
+  }
+  /* fillisym / filljas (Connections.f90:1205-1268) */
+  for (int n = 0; n < nodes; ++n)
+    for (int ii = ia[n]; ii < ia[n + 1]; ++ii) {
+      int m = ja[ii];
+      isym[ii] = (m == n) ? ii : -1;
+      if (m != n)
+        for (int jj = ia[m]; jj < ia[m + 1]; ++jj)
+          if (ja[jj] == n) {
+            isym[ii] = jj;
+            break;
+          }
+    }
+  int ipos = 0;
+  for (int n = 0; n < nodes; ++n) {
+    jas[ia[n]] = -1;
+    for (int ii = ia[n] + 1; ii < ia[n + 1]; ++ii)
+      if (ja[ii] > n) jas[ii] = ipos++;
+  }
+  for (int n = 0; n < nodes; ++n)
+    for (int ii = ia[n]; ii < ia[n + 1]; ++ii)
+      if (ja[ii] < n) jas[ii] = jas[isym[ii]];
+  for (int j = 0; j < ncpl; ++j) area[j] = disv_area(j, iavert, javert, vx, vy);
+  /* cprops for n < m (DisvGeom.f90:136-202) */
+  for (int n = 0; n < nodes; ++n) {
+    const int jn = n % ncpl;
+    for (int ii = ia[n] + 1; ii < ia[n + 1]; ++ii) {
+      const int m = ja[ii];
+      if (m < n) continue;
+      const int jm = m % ncpl, s = jas[ii];
+      if (jn == jm) {
+        ihc[s] = 0;
+        hwva[s] = area[jn];
+        cl1[s] = 0.5 * (top[n] - bot[n]);
+        cl2[s] = 0.5 * (top[m] - bot[m]);
+      } else {
+        ihc[s] = 1;
+        int a, b;
+        disv_shared_edge(javert + iavert[jn], iavert[jn + 1] - iavert[jn], javert + iavert[jm],
+                         iavert[jm + 1] - iavert[jm], &a, &b);
+        if (a < 0 || b < 0) {
+          hwva[s] = 0.0;
+          cl1[s] = 1.0;
+          cl2[s] = 1.0;
+        } else {
+          hwva[s] = disv_distance(vx[a], vy[a], vx[b], vy[b]);
+          cl1[s] = disv_distance_normal(xc[jn], yc[jn], vx[a], vy[a], vx[b], vy[b]);
+          cl2[s] = disv_distance_normal(xc[jm], yc[jm], vx[a], vy[a], vx[b], vy[b]);
+        }
+      }
+    }
+  }
+  free(vcnt); free(vcell); free(vfill); free(rows); free(rn);
+  return nja;
+}
+
+/* ------------------------------------------------------------------------ */
 /* STO and boundary packages                                                 */
 /* ------------------------------------------------------------------------ */
 

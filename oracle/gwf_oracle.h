@@ -64,6 +64,10 @@ void or_dis_sizes(int nlay, int nrow, int ncol, int *nodes, int *nja, int *njas)
 void or_dis_connect(int nlay, int nrow, int ncol, const double *delr, const double *delc,
                     const double *top, const double *bot, int *ia, int *ja, int *isym,
                     int *jas, int *ihc, double *cl1, double *cl2, double *hwva);
+int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, const int *iavert,
+                    const int *javert, const double *xc, const double *yc, const double *top,
+                    const double *bot, int cap, int *ia, int *ja, int *isym, int *jas, int *ihc,
+                    double *cl1, double *cl2, double *hwva, double *area);
 double or_squadratic_sat(double top, double bot, double x, double eps);
 double or_squadratic_sat_derv(double top, double bot, double x, double eps);
 void or_npf_condsat(const or_gwf_model *m, double *condsat);

@@ -120,6 +120,8 @@ def load():
         lib.or_squadratic_sat_derv.restype = C.c_double
         lib.or_squadratic_sat_derv.argtypes = [C.c_double] * 4
         lib.or_dis_sizes.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip]
+        lib.or_disv_connect.argtypes = [C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp, _dp, _dp,
+                                        C.c_int, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
         lib.or_dis_connect.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, _ip, _ip,
                                        _ip, _ip, _dp, _dp, _dp]
         lib.or_npf_condsat.argtypes = [C.POINTER(GwfModel), _dp]
@@ -321,13 +323,51 @@ def dis_connect(nlay, nrow, ncol, delr, delc, top, bot) -> dict:
     return out
 
 
+def disv_connect(nlay, iavert, javert, vx, vy, xc, yc, top, bot) -> dict:
+    """or_disv_connect: the connectivity of a full DISV grid (closed vertex
+    lists iavert/javert, 0-based), with the cell areas."""
+    lib = load()
+    iavert = np.ascontiguousarray(iavert, np.int32)
+    javert = np.ascontiguousarray(javert, np.int32)
+    ncpl = iavert.size - 1
+    n = nlay * ncpl
+    cap = n * (3 + int(np.diff(iavert).max()))
+    out = dict(ia=np.zeros(n + 1, np.int32), ja=np.zeros(cap, np.int32), isym=np.zeros(cap, np.int32),
+               jas=np.zeros(cap, np.int32), ihc=np.zeros(cap, np.int32), cl1=np.zeros(cap),
+               cl2=np.zeros(cap), hwva=np.zeros(cap), area=np.zeros(ncpl))
+    f = lambda a: np.ascontiguousarray(a, np.float64)
+    keep = [f(vx), f(vy), f(xc), f(yc), f(top), f(bot)]
+    nja = lib.or_disv_connect(nlay, ncpl, dp(keep[0]), dp(keep[1]), ip(iavert), ip(javert),
+                              dp(keep[2]), dp(keep[3]), dp(keep[4]), dp(keep[5]), cap,
+                              ip(out["ia"]), ip(out["ja"]), ip(out["isym"]), ip(out["jas"]),
+                              ip(out["ihc"]), dp(out["cl1"]), dp(out["cl2"]), dp(out["hwva"]),
+                              dp(out["area"]))
+    if nja < 0:
+        raise RuntimeError("or_disv_connect: capacity exceeded")
+    njas = (nja - n) // 2
+    for k in ("ja", "isym", "jas"):
+        out[k] = out[k][:nja].copy()
+    for k in ("ihc", "cl1", "cl2", "hwva"):
+        out[k] = out[k][:njas].copy()
+    out.update(nodes=n, nja=nja, njas=njas)
+    return out
+
+
 class Gwf:
-    """Oracle GWF model + NumericalSolution for one DIS model (a GwfDisModel)."""
+    """Oracle GWF model + NumericalSolution for one DIS model (a GwfDisModel)
+    or one DISV model (a DisvModel: connectivity from or_disv_connect)."""
 
     def __init__(self, m, ims_settings: Settings, satomega=1.0e-6):
         self.lib = load()
         self.m = m
-        con = dis_connect(m.nlay, m.nrow, m.ncol, m.delr, m.delc, m.cell_top, m.cell_bot)
+        if getattr(m, "disv", False):
+            iav, jav = m.vertex_lists
+            con = disv_connect(m.nlay, iav, jav, m.vertices[:, 0], m.vertices[:, 1], m.xc, m.yc,
+                               m.cell_top, m.cell_bot)
+            area = np.tile(con["area"], m.nlay)
+        else:
+            con = dis_connect(m.nlay, m.nrow, m.ncol, m.delr, m.delc, m.cell_top, m.cell_bot)
+            area = m.area
         self.con = con
         keep = {}
 
@@ -348,7 +388,7 @@ class Gwf:
             m.nlay, m.nrow, m.ncol, n, con["nja"], con["njas"],
             i(con["ia"]), i(con["ja"]), i(con["isym"]), i(con["jas"]), i(con["ihc"]),
             d(con["cl1"]), d(con["cl2"]), d(con["hwva"]),
-            d(m.cell_top), d(m.cell_bot), d(m.area), d(m.k11), d(m.k33), i(m.icelltype),
+            d(m.cell_top), d(m.cell_bot), d(area), d(m.k11), d(m.k33), i(m.icelltype),
             int(m.inewton), int(getattr(m, "ivarcv", 0)), int(getattr(m, "idewatcv", 0)),
             int(getattr(m, "icellavg", 0)), satomega, int(getattr(m, "inewtonur", 0)),
             d(ss), d(sy), i(m.icelltype),
