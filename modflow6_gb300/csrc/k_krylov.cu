@@ -360,17 +360,27 @@ __global__ void __launch_bounds__(kRedBlock) k_cg_update64(int n, double *__rest
     if (L2) v[0] = fma(di, di, v[0]);
     nf |= nonfinite(di) | nonfinite(tv);
   };
-  // two rows per trip, loads first (same order of rows as one per trip)
+  // four rows per trip, their 16 loads issued before any row is used (the
+  // same order of rows per thread as one row per trip, so the same sums and
+  // maxima): the loads of a trip cover the latency of the FP64 work of the
+  // trip before
+  constexpr int R = 4;
   const int stride = gridDim.x * blockDim.x;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + stride < n; i += 2 * stride) {
-    const int j = i + stride;
-    const double p0 = p[i], x0 = x[i], q0 = q[i], d0 = d[i];
-    const double p1 = p[j], x1 = x[j], q1 = q[j], d1 = d[j];
-    row(i, p0, x0, q0, d0);
-    row(j, p1, x1, q1, d1);
+  for (; i + (R - 1) * stride < n; i += R * stride) {
+    double pr[R], xr[R], qr[R], dr[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int j = i + r * stride;
+      pr[r] = __ldcs(p + j);
+      xr[r] = __ldcs(x + j);
+      qr[r] = __ldcs(q + j);
+      dr[r] = __ldcs(d + j);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) row(i + r * stride, pr[r], xr[r], qr[r], dr[r]);
   }
-  if (i < n) row(i, p[i], x[i], q[i], d[i]);
+  for (; i < n; i += stride) row(i, p[i], x[i], q[i], d[i]);
   v[1] = (double)nf;
   block_sum<2>(v);
   block_maxloc<2>(m);
