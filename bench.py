@@ -622,7 +622,7 @@ def warmstart_form(a) -> dict:
     from modflow6_gb300.warmstart import WarmStartNet, evaluate, generate, train
 
     full = a.scale == 1.0
-    ntrain, nheld, steps = (24, 4, 20) if full else (4, 2, 8)
+    ntrain, nheld, steps = (48, 16, 20) if full else (4, 2, 8)
     sc = 1.0 if full else 0.1
     t0 = _t.perf_counter()
     data, dh_scale = generate(range(1000, 1000 + ntrain), steps=steps, scale=sc)

@@ -58,47 +58,39 @@ __device__ __forceinline__ DF df_shfl_up(DF v, int d) {
   return DF{__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d)};
 }
 
-// double -> df64 by bit manipulation: hi keeps the top 24 significant bits
-// (truncated), lo the next 29 rounded to float.  Zero, denormal doubles and
-// magnitudes below 2^-126 give zero; magnitudes from 2^128 give +-inf; NaN
-// stays NaN.
+// double -> df64 by bit manipulation, without branches or conversion
+// instructions: hi keeps the top 24 significant bits (truncated); lo the next
+// 23 of the remaining 29, built as the difference of two floats that share
+// hi's scale (2^(E-23) * 1.m - 2^(E-23), exact by Sterbenz), so the error is
+// below 2^-47 relative.  Magnitudes below 2^-126 give zero (lo is zero below
+// 2^-103); from 2^128 +-inf; NaN stays NaN.
 __device__ __forceinline__ DF df_from_double(double x) {
   const unsigned long long u = (unsigned long long)__double_as_longlong(x);
   const unsigned h = (unsigned)(u >> 32), l = (unsigned)u;
   const unsigned sign = h & 0x80000000u;
   const int e = (int)((h >> 20) & 0x7ffu);
   const int ef = e - 1023 + 127;
-  if (e == 0x7ff)  // inf keeps its sign; any NaN becomes a quiet NaN
-    return DF{__uint_as_float(sign | (((h & 0xfffffu) | l) ? 0x7fc00000u : 0x7f800000u)), 0.0f};
-  if (ef <= 0) return DF{__uint_as_float(sign), 0.0f};
-  if (ef >= 255) return DF{__uint_as_float(sign | 0x7f800000u), 0.0f};
   const unsigned mh = ((h & 0xfffffu) << 3) | (l >> 29);
-  const float hi = __uint_as_float(sign | ((unsigned)ef << 23) | mh);
-  // lo = (l & (2^29 - 1)) * 2^(e - 1075), scaled in two steps so that the
-  // intermediate stays a normal float
-  const unsigned rem = l & 0x1fffffffu;
-  float lo = 0.0f;
-  const int s1 = e - 1075 + 64 + 127;  // biased exponent of 2^(e - 1075 + 64)
-  if (rem != 0u && s1 > 0) {
-    lo = __fmul_rn(__uint2float_rn(rem), __uint_as_float((unsigned)s1 << 23));
-    lo = __fmul_rn(lo, 5.421010862427522e-20f);  // 2^-64
-    lo = __uint_as_float(__float_as_uint(lo) | sign);
-  }
-  return DF{hi, lo};
+  unsigned hb = sign | ((unsigned)ef << 23) | mh;
+  const unsigned base = (unsigned)(ef - 23) << 23;
+  float lo = __fsub_rn(__uint_as_float(base | ((l & 0x1fffffffu) >> 6)), __uint_as_float(base));
+  lo = (ef > 23 && ef < 255) ? lo : 0.0f;
+  const bool nan = (e == 0x7ff) && (((h & 0xfffffu) | l) != 0u);
+  hb = (ef <= 0) ? sign : hb;
+  hb = (ef >= 255) ? (sign | (nan ? 0x7fc00000u : 0x7f800000u)) : hb;
+  return DF{__uint_as_float(hb), __uint_as_float(__float_as_uint(lo) | sign)};
 }
 
 // float -> double bits, exact for normal floats and zero (denormal floats
-// give zero), with integer instructions only
+// give zero), with integer instructions and selects only
 __device__ __forceinline__ double df_widen(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
   const unsigned e = (u >> 23) & 0xffu;
-  if (e == 0u) return __longlong_as_double((long long)sign);
-  if (e == 0xffu)
-    return __longlong_as_double((long long)(sign | 0x7ff0000000000000ULL |
-                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
-  const unsigned long long bits =
-      sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+  const unsigned long long man = (unsigned long long)(u & 0x7fffffu) << 29;
+  unsigned long long bits = sign | ((unsigned long long)(e + 896u) << 52) | man;
+  bits = (e == 0u) ? sign : bits;
+  bits = (e == 0xffu) ? (sign | 0x7ff0000000000000ULL | man) : bits;
   return __longlong_as_double((long long)bits);
 }
 

@@ -52,10 +52,9 @@
 // (pairs of floats, k_df64.cuh) when every factor tile lies in the float
 // exponent range, because GB300 issues a warp's FP64 FMA only every 64 cycles
 // or so and a step carries two of them; otherwise, or when GBIMS_SWEEP_NATIVE
-// is set, it sweeps in native FP64.  The df64 backward sweep leaves the
-// conversion of its result to FP64 (one FP64 add per cell) to the copy warp,
-// through a staging tile in the ring buffer, so the chain never waits on the
-// FP64 pipe.
+// is set, it sweeps in native FP64.  The df64 backward sweep converts its
+// result to FP64 (one FP64 add per cell) in the compute warp, off the chain,
+// on the FP64 pipe that the df64 chain leaves idle.
 #include <algorithm>
 #include <cstdlib>
 
@@ -160,11 +159,6 @@ __device__ __forceinline__ bool dinv_zero(float d) { return d == 0.0f; }
 __device__ __forceinline__ bool dinv_zero(DF d) { return d.hi == 0.0f; }
 
 template <typename T>
-constexpr bool kStagedOut = false;  // the backward result goes out through the copy warp
-template <>
-constexpr bool kStagedOut<DF> = true;
-
-template <typename T>
 struct SweepArgs {
   const Dia7Geo *geo;  // members, in ticket order
   int nm;
@@ -192,7 +186,6 @@ struct alignas(16) Stage<T, C, -1> {
   T a[C * 32], b[C * 32], x[C * 32], d[C * 32];
   LLWord<T> y[C * 32];  // own forward result, steps descending
   T yn[C];
-  T zo[kStagedOut<T> ? C * 32 : 1];  // df64: the chunk's results for the copy warp
 };
 
 // Warp roles of a sweep CTA.
@@ -228,7 +221,6 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   unsigned long long *full = reinterpret_cast<unsigned long long *>(smem_raw + NS * sizeof(St));
   unsigned long long *empty = full + NS;
   unsigned long long *prep = full + 2 * NS;
-  unsigned long long *zfree = full + 3 * NS;  // df64 backward: the copy warp has read zo
   __shared__ int s_id, s_abort, s_rot, s_m;
   __shared__ unsigned s_ep;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -262,7 +254,6 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
       mbar_init(&prep[s], 2);  // pre-compute warp + edge warp
-      mbar_init(&zfree[s], 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -452,21 +443,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   if (role == kRoleCopy) {
     // ---------------- copy warp ----------------
     // The block's own tiles have no producer in this launch: they stream
-    // into the ring as fast as buffers free up.  In the df64 backward sweep
-    // this warp also writes the results of each finished chunk to z in
-    // natural order (converted to FP64) before it refills the buffer.
-    auto flush = [&](int c) {
-      if constexpr (DIR < 0 && kStagedOut<T>) {
-        const St &st = stg[c % NS];
-        const int jc = c * C - S * lane;
-#pragma unroll
-        for (int t = 0; t < C; ++t) {
-          const int jj = jc + t;
-          if (line_ok && (unsigned)jj < (unsigned)ncol)
-            zrow[ncol - 1 - jj] = E::to_vec(st.zo[t * W + lane]);
-        }
-      }
-    };
+    // into the ring as fast as buffers free up.
     int issued = 0;
     bool ok = true;
     const unsigned tileb = C * W * sizeof(T);
@@ -501,26 +478,8 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         bulk_g2s(st.x, p.X + tb, tileb, &full[s]);
       }
       issued = c + 1;
-      if constexpr (DIR < 0 && kStagedOut<T>) {
-        // the results of the chunk that last used this buffer, written out
-        // while the new tiles are in flight (zo is no copy target); the
-        // compute warp waits on zfree before it writes zo again
-        if (c >= NS) {
-          flush(c - NS);
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&zfree[s]);
-        }
-      }
     }
     if (!ok) fail();
-    if constexpr (DIR < 0 && kStagedOut<T>) {
-      // the last chunks' results, once the compute warp has finished them
-      for (int c = max(0, nch - NS); ok && c < nch; ++c) {
-        const bool got = mbar_wait(&empty[c % NS], (c / NS) & 1, v_abort);
-        ok = __all_sync(0xffffffffu, got);
-        if (ok) flush(c);
-      }
-    }
     if (lane == 0) {
       // every copy issued has landed before this warp, and so the CTA, ends
       // (the other warps may have left early on an abort)
@@ -547,15 +506,6 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       if (lane == 0) *v_abort = 1;
       return;
     }
-    if constexpr (DIR < 0 && kStagedOut<T>) {
-      if (c >= NS) {
-        const bool zf = mbar_wait(&zfree[s], ((c / NS) - 1) & 1, v_abort);
-        if (!__all_sync(0xffffffffu, zf)) {
-          if (lane == 0) *v_abort = 1;
-          return;
-        }
-      }
-    }
     St &st = stg[s];
     const int g0 = c * C;
     const int jc = g0 - S * lane;
@@ -579,12 +529,10 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       tv = E::fms(rb[t], yv, tv);
       ll_put(outt + (long long)(g0 + t) * W, tv, ep);
       if constexpr (DIR < 0) {
-        if constexpr (kStagedOut<T>) {
-          stg[s].zo[t * W + lane] = tv;
-        } else {
-          const int jj = jc + t;
-          if (line_ok && (unsigned)jj < (unsigned)ncol) zrow[ncol - 1 - jj] = tv;  // natural order
-        }
+        // the result in natural order (df64: widened and added in FP64, off
+        // the chain, on this sub-partition's otherwise idle FP64 pipe)
+        const int jj = jc + t;
+        if (line_ok && (unsigned)jj < (unsigned)ncol) zrow[ncol - 1 - jj] = E::to_vec(tv);
       }
       h2 = h1;
       h1 = tv;
@@ -711,7 +659,7 @@ constexpr int kNumSweepCfgs = sizeof(kSweepCfgs) / sizeof(kSweepCfgs[0]);
 
 template <typename T, int C, int NS, int DIR>
 constexpr size_t stage_bytes() {
-  return NS * sizeof(Stage<T, C, DIR>) + 4 * NS * sizeof(unsigned long long);
+  return NS * sizeof(Stage<T, C, DIR>) + 3 * NS * sizeof(unsigned long long);
 }
 static_assert(stage_bytes<double, 16, 2, -1>() <= 72 * 1024 && stage_bytes<double, 4, 8, -1>() <= 72 * 1024 &&
                   stage_bytes<double, 8, 4, -1>() <= 72 * 1024,

@@ -133,17 +133,22 @@ __global__ void __launch_bounds__(kRedBlock) k_dot(int n, const TA *__restrict__
                                                     const Ctl *__restrict__ ctl) {
   if (ctl->done) return;
   double v[1] = {0.0};
-  // two rows per trip, loads first: the same summation order as one row per
-  // trip, with twice the loads in flight
+  // four rows per trip, loads first: the same summation order as one row
+  // per trip, with four times the loads in flight
+  constexpr int R = 4;
   const int stride = gridDim.x * blockDim.x;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + stride < n; i += 2 * stride) {
-    const double a0 = to_d(a[i]), b0 = to_d(b[i]);
-    const double a1 = to_d(a[i + stride]), b1 = to_d(b[i + stride]);
-    v[0] = fma(a0, b0, v[0]);
-    v[0] = fma(a1, b1, v[0]);
+  for (; i + (R - 1) * stride < n; i += R * stride) {
+    double ar[R], br[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      ar[r] = to_d(a[i + r * stride]);
+      br[r] = to_d(b[i + r * stride]);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[0] = fma(ar[r], br[r], v[0]);
   }
-  if (i < n) v[0] = fma(to_d(a[i]), to_d(b[i]), v[0]);
+  for (; i < n; i += stride) v[0] = fma(to_d(a[i]), to_d(b[i]), v[0]);
   block_sum<1>(v);
   if (threadIdx.x == 0) part[blockIdx.x] = v[0];
 }
