@@ -357,6 +357,9 @@ typedef struct gbsln_stats {
   double dxmax;       /* last outer max head change */
   double fill_ms, solve_ms, total_ms; /* device time of the step */
   int backtracks;     /* backtracking reductions taken in the step */
+  double guess_alpha; /* the step's first iterate was xold + guess_alpha*(guess - xold):
+                         1 for gbsln_timestep_guess, the line-search factor for
+                         gbsln_timestep_warm, 0 for a step from the previous heads */
 } gbsln_stats;
 
 int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,
@@ -374,8 +377,12 @@ int gbsln_timestep(gbsln_handle *h, int kper, int kstp, double delt, gbsln_stats
 int gbsln_timestep_guess(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
                          gbsln_stats *st);
 /* The warm start with its fallback (no counterpart in the reference, whose
- * steps always start from the previous heads): the step starts from d_guess
- * as gbsln_timestep_guess does, but when it has spent inner_cap inner
+ * steps always start from the previous heads).  The first iterate of the
+ * active cells is xold + alpha*(d_guess - xold), alpha = d.r / d.(A d) with
+ * d = d_guess - xold and A, r the step's first system and residual at the
+ * previous heads, kept in [0, 2]: for the symmetric GWF matrix the point of
+ * that line closest to the solution in the energy norm, never farther from
+ * it than the previous heads.  When the step has spent inner_cap inner
  * iterations without closing, the guess is dropped and the step is solved
  * again from the previous heads; then the status is GBIMS_WARN_FALLBACK and
  * *st counts the iterations and device time of both attempts.  Give
@@ -425,7 +432,8 @@ int gbsln_destroy(gbsln_handle *h);
  * change; trained and evaluated on the GPU (BF16 tensor-core GEMMs, FP32
  * accumulation, FP32 Adam).  Device arrays: features nodes x 16 (row-major
  * FP32), targets, masks and outputs nodes (FP32).  The loss is
- * inv_count * sum(((y - target) * mask)^2). */
+ * inv_count * sum(((y - target) * mask)^2), or the energy loss that
+ * gbmpnn_set_loss selects. */
 typedef struct gbmpnn_handle gbmpnn_handle;
 long long gbmpnn_param_count(void);
 int gbmpnn_create(int nodes, int nja, const int *ia, const int *ja, unsigned long long seed,
@@ -450,6 +458,17 @@ typedef struct gbmpnn_scaling {
   double dh_soft, dh_scale;    /* a head change dh in network units: asinh(dh / dh_soft) / dh_scale */
   double unit_max;             /* bound on |output| in network units (0: none) */
 } gbmpnn_scaling;
+
+/* The training loss.  mode 0: the masked squared error in network units
+ * (the default).  mode 1: the relative energy error of the predicted head
+ * change, e'We / t'Wt with W = -A over the active (mask) cells, A the matrix
+ * of the last gbmpnn_set_graph (copied there), e = dh(y) - dh(target),
+ * t = dh(target), dh(u) = dh_soft * sinh(u * dh_scale) -- the error that a
+ * conjugate-gradient solve started from the guess has to remove, relative
+ * to the one it has from the previous heads -- plus mse_weight times the
+ * squared error of mode 0.  A sample whose t'Wt is not positive adds
+ * nothing. */
+int gbmpnn_set_loss(gbmpnn_handle *h, int mode, const gbmpnn_scaling *sc, float mse_weight);
 
 /* The guess for the next time step of a solution, on the device and on the
  * solution's own stream (no host synchronisation): the features are built

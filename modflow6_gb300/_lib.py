@@ -87,6 +87,7 @@ class GbslnStats(C.Structure):
         ("outer", C.c_int), ("inner_total", C.c_int), ("converged", C.c_int),
         ("pivot_retries", C.c_int), ("dxmax", C.c_double), ("fill_ms", C.c_double),
         ("solve_ms", C.c_double), ("total_ms", C.c_double), ("backtracks", C.c_int),
+        ("guess_alpha", C.c_double),
     ]
 
 
@@ -164,6 +165,7 @@ _SIGS = {
     "gbmpnn_param_count": (C.c_longlong, []),
     "gbmpnn_create": (C.c_int, [C.c_int, C.c_int, _ip, _ip, C.c_ulonglong, C.POINTER(C.c_void_p)]),
     "gbmpnn_set_graph": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gbmpnn_set_loss": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(GbmpnnScaling), C.c_float]),
     "gbmpnn_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "gbsln_warm_guess": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(GbmpnnScaling),
                                    C.c_int, C.c_void_p, C.POINTER(C.c_float)]),

@@ -92,6 +92,13 @@ extern "C" int gbmpnn_create(int nodes, int nja, const int *ia, const int *ja,
   MP_CUDA(h, alloc(&D.dHp, n * H));
   MP_CUDA(h, alloc(&D.dX, n * 2 * H));
   MP_CUDA(h, alloc(&D.dZ, n * H));
+  D.nja = nja;
+  MP_CUDA(h, alloc(&D.amat, (size_t)nja));
+  MP_CUDA(h, cudaMemset(D.amat, 0, sizeof(double) * nja));
+  MP_CUDA(h, alloc(&D.ee, n));
+  MP_CUDA(h, alloc(&D.tt, n));
+  MP_CUDA(h, alloc(&D.we, n));
+  MP_CUDA(h, alloc(&D.epart, (size_t)2 * kMpnnRedBlocks));
   // initial weights: uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)), zero biases
   // except the output, from a seeded host generator
   std::vector<float> p((size_t)h->np, 0.f);
@@ -123,6 +130,20 @@ extern "C" int gbmpnn_set_graph(gbmpnn_handle *h, const double *d_amat) {
   mpnn_set_graph(h->D, d_amat, h->st);
   MP_CUDA(h, cudaStreamSynchronize(h->st));
   MP_CUDA(h, cudaGetLastError());
+  return GBIMS_OK;
+}
+
+extern "C" int gbmpnn_set_loss(gbmpnn_handle *h, int mode, const gbmpnn_scaling *sc,
+                               float mse_weight) {
+  if (!h || (mode != 0 && mode != 1) || !(mse_weight >= 0.f)) return GBIMS_ERR_ARG;
+  if (mode == 1 && (!sc || !(sc->dh_soft > 0.0) || !(sc->dh_scale > 0.0))) return GBIMS_ERR_ARG;
+  MP_CUDA(h, cudaStreamSynchronize(h->st));
+  h->D.energy = mode;
+  h->D.mse_w = (mode == 1) ? mse_weight : 1.f;
+  if (mode == 1) {
+    h->D.dh_soft = sc->dh_soft;
+    h->D.dh_scale = sc->dh_scale;
+  }
   return GBIMS_OK;
 }
 
@@ -221,7 +242,8 @@ extern "C" int gbmpnn_destroy(gbmpnn_handle *h) {
   if (h->st) cudaStreamSynchronize(h->st);
   MpnnDev &D = h->D;
   std::vector<void *> ptrs = {h->d_ia, h->d_ja, D.w, D.deg, D.p, D.g, D.m, D.v, D.bt0, D.wbf0,
-                              D.xbf, D.A, D.y, D.dy, D.loss, D.dH, D.dHp, D.dX, D.dZ};
+                              D.xbf, D.A, D.y, D.dy, D.loss, D.dH, D.dHp, D.dX, D.dZ,
+                              D.amat, D.ee, D.tt, D.we, D.epart};
   for (int l = 0; l < kMpnnLayers; ++l) {
     ptrs.push_back(D.bt[l]);
     ptrs.push_back(D.wbf[l]);

@@ -243,6 +243,7 @@ struct gbsln_handle {
          *dxold = nullptr, *part = nullptr, *bnd_val = nullptr, *chd_head = nullptr;
   int *ibound = nullptr, *bnd_ptr = nullptr, *chd_node = nullptr, *flag = nullptr;
   int *bnd_kind = nullptr;  // per boundary entry: 0 WEL, 1 RCH
+  double *galpha = nullptr; // the last warm step's line-search factor
   double *bpart = nullptr;  // budget partials (kGwfBudgetSlots per block)
   int nchd = 0, G = 1;
   bool has_sto = false;
@@ -272,6 +273,78 @@ __global__ void k_apply_guess(int n, const int *__restrict__ ibound, const doubl
                               double *__restrict__ x) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     if (ibound[i] > 0) x[i] = guess[i];
+}
+
+// Energy line search of a guess (no counterpart in the reference): with
+// d = guess - xold on active cells (zero elsewhere) and r = rhs - A*xold, the
+// partials of d.r and d.(A d) per block (part[2b], part[2b+1]).  For the
+// symmetric (negative definite) GWF matrix, x0 = xold + alpha*d with
+// alpha = d.r / d.(A d) is the point of the line through xold and the guess
+// closest to the solution in the energy norm, so it is never farther from
+// the solution in that norm than the previous heads are.
+__global__ void k_guess_dots(int n, const int *__restrict__ ia, const int *__restrict__ ja,
+                             const double *__restrict__ amat, const double *__restrict__ rhs,
+                             const int *__restrict__ ibound, const double *__restrict__ guess,
+                             const double *__restrict__ xold, double *part) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (ibound[i] < 1) continue;
+    double ax = 0.0, ad = 0.0;
+    for (int k = ia[i]; k < ia[i + 1]; ++k) {
+      const int j = ja[k];
+      const double xj = xold[j];
+      const double dj = (ibound[j] > 0) ? guess[j] - xj : 0.0;
+      ax = fma(amat[k], xj, ax);
+      ad = fma(amat[k], dj, ad);
+    }
+    const double di = guess[i] - xold[i];
+    s1 = fma(di, rhs[i] - ax, s1);
+    s2 = fma(di, ad, s2);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  __shared__ double sh[2][32];
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = s1;
+    sh[1][threadIdx.x >> 5] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += sh[0][w];
+      b += sh[1][w];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+
+// x = xold + alpha*(guess - xold) on active cells, alpha from the G pairs of
+// partials summed in block order by every block (the same alpha everywhere),
+// kept in [0, 2]; block 0 also writes alpha to *alpha_out.
+__global__ void k_guess_blend(int n, int G, const double *__restrict__ part,
+                              const int *__restrict__ ibound, const double *__restrict__ guess,
+                              const double *__restrict__ xold, double *__restrict__ x,
+                              double *alpha_out) {
+  __shared__ double alpha;
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < G; ++q) {
+      a += part[2 * q];
+      b += part[2 * q + 1];
+    }
+    double al = (b != 0.0) ? a / b : 0.0;
+    al = (al == al) ? fmin(fmax(al, 0.0), 2.0) : 0.0;
+    alpha = al;
+    if (blockIdx.x == 0) *alpha_out = al;
+  }
+  __syncthreads();
+  const double al = alpha;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (ibound[i] > 0) x[i] = fma(al, guess[i] - xold[i], xold[i]);
 }
 
 __global__ void k_set_chd(int nchd, const int *__restrict__ node, const double *__restrict__ head,
@@ -380,6 +453,7 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
   h->G = std::max(1, std::min(2 * kNumSM * 2, (n + 255) / 256));
   chk(up<double>(&h->part, nullptr, (size_t)h->G * 2));
   chk(up<int>(&h->flag, nullptr, 4));
+  chk(up<double>(&h->galpha, nullptr, 1));
   chk(up(&h->strt, strt, (size_t)n));
   if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GBIMS_ERR_CUDA; }
   for (double **p : wv) cudaMemset(*p, 0, sizeof(double) * n);
@@ -442,7 +516,7 @@ static int reduce_host(gbsln_handle *h, bool max_not_sum, double *out) {
 }
 
 static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
-                         gbsln_stats *st, int inner_cap = 0);
+                         gbsln_stats *st, int inner_cap = 0, bool project = false);
 // timestep_core's status when a guessed step has used its inner-iteration
 // budget without closing (internal; gbsln_timestep_warm falls back on it)
 constexpr int kCapReached = 1000;
@@ -462,7 +536,7 @@ extern "C" int gbsln_timestep_warm(gbsln_handle *h, int kper, int kstp, double d
   if (!h || !d_guess || inner_cap < 1) return GBIMS_ERR_ARG;
   gbsln_stats a;
   memset(&a, 0, sizeof(a));
-  int rc = timestep_core(h, kper, kstp, delt, d_guess, &a, inner_cap);
+  int rc = timestep_core(h, kper, kstp, delt, d_guess, &a, inner_cap, true);
   if (rc != kCapReached) {
     if (st) *st = a;
     return rc;
@@ -473,6 +547,7 @@ extern "C" int gbsln_timestep_warm(gbsln_handle *h, int kper, int kstp, double d
   gbsln_stats b;
   memset(&b, 0, sizeof(b));
   rc = timestep_core(h, kper, kstp, delt, nullptr, &b);
+  b.guess_alpha = a.guess_alpha;
   b.inner_total += a.inner_total;
   b.fill_ms += a.fill_ms;
   b.solve_ms += a.solve_ms;
@@ -484,7 +559,7 @@ extern "C" int gbsln_timestep_warm(gbsln_handle *h, int kper, int kstp, double d
 }
 
 static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const double *d_guess,
-                         gbsln_stats *st, int inner_cap) {
+                         gbsln_stats *st, int inner_cap, bool project) {
   if (!h || !h->ims) return GBIMS_ERR_ARG;
   const int n = h->n;
   const bool transient = (delt > 0.0) && h->has_sto;
@@ -497,7 +572,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
   SLN_CUDA(h, cudaMemcpyAsync(h->xold, h->x, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->st));
   // warm start: the guess replaces the previous heads as the first iterate
   // (xold, the storage reference, keeps the previous heads)
-  if (d_guess)
+  if (d_guess && !project)
     k_apply_guess<<<std::min(4 * kNumSM, (n + 255) / 256), 256, 0, h->st>>>(n, h->ibound, d_guess, h->x);
   if (h->nchd > 0)
     k_set_chd<<<(h->nchd + 255) / 256, 256, 0, h->st>>>(h->nchd, h->chd_node, h->chd_head, h->x, h->xold);
@@ -528,6 +603,20 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
     *l2 = sqrt(ss);
     return rc;
   };
+  if (d_guess && project) {
+    // the first iterate on the line through the previous heads and the
+    // guess, at its energy-norm optimum for the step's first system (built
+    // at the previous heads, as the plain step's first outer iteration is)
+    SLN_CUDA(h, cudaMemsetAsync(h->amat, 0, sizeof(double) * h->nja, h->st));
+    SLN_CUDA(h, cudaMemsetAsync(h->rhs, 0, sizeof(double) * n, h->st));
+    gwf_npf_cf(n, h->g, h->ibound, h->x, h->d.sat, h->st);
+    gwf_fill(n, h->g, f, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, h->amat, h->rhs, h->st);
+    k_guess_dots<<<h->G, 256, 0, h->st>>>(n, h->d.ia, h->d.ja, h->amat, h->rhs, h->ibound, d_guess,
+                                            h->xold, h->part);
+    k_guess_blend<<<std::min(4 * kNumSM, (n + 255) / 256), 256, 0, h->st>>>(
+        n, h->G, h->part, h->ibound, d_guess, h->xold, h->x, h->galpha);
+    SLN_CUDA(h, cudaGetLastError());
+  }
   for (int kiter = 1; kiter <= h->nl.mxiter; ++kiter) {
     if (d_guess && inner_cap > 0 && kiter > 1 && s.inner_total >= inner_cap) {
       // the guessed step has used its budget without closing
@@ -536,6 +625,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
       float tot = 0.f;
       cudaEventElapsedTime(&tot, h->e0, h->e1);
       s.total_ms = tot;
+      if (project) SLN_CUDA(h, cudaMemcpy(&s.guess_alpha, h->galpha, sizeof(double), cudaMemcpyDeviceToHost));
       if (st) *st = s;
       return kCapReached;
     }
@@ -690,6 +780,9 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
   s.total_ms = tot;
   s.converged = converged ? 1 : 0;
   s.dxmax = hncg;
+  s.guess_alpha = (d_guess && !project) ? 1.0 : 0.0;
+  if (d_guess && project)
+    SLN_CUDA(h, cudaMemcpy(&s.guess_alpha, h->galpha, sizeof(double), cudaMemcpyDeviceToHost));
   if (st) *st = s;
   return GBIMS_OK;
 }
@@ -823,7 +916,7 @@ extern "C" int gbsln_destroy(gbsln_handle *h) {
   void *p[] = {h->strt, h->ss, h->sy, h->area, h->vol, h->xold, h->xtemp, h->wsave, h->hchold, h->deold,
                h->dxold, h->part, h->bnd_val, h->chd_head, h->ibound, h->bnd_ptr, h->chd_node,
                h->bnd_kind, h->bpart,
-               h->flag};
+               h->flag, h->galpha};
   for (void *q : p)
     if (q) cudaFree(q);
   if (h->e0) cudaEventDestroy(h->e0);

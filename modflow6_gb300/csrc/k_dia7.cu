@@ -308,15 +308,16 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     const int ri = b * W + lane;
     const bool rline = (DIR > 0) && ri < nrow;
     const V *rrow = rline ? p.rnat + geo.row0 + ((long long)k * nrow + ri) * geo.ncol : nullptr;
-    auto rload = [&](int c, T (&dst)[C]) {
+    // (kept as loaded and converted when used: a conversion right after the
+    // load would wait for it, and the prefetch would hide nothing)
+    auto rload = [&](int c, V (&dst)[C]) {
 #pragma unroll
       for (int t = 0; t < C; ++t) {
         const int jj = c * C + t - S * lane;
-        dst[t] = (rline && (unsigned)jj < (unsigned)geo.ncol) ? E::from_vec(__ldg(rrow + jj))
-                                                              : E::zero();
+        dst[t] = (rline && (unsigned)jj < (unsigned)geo.ncol) ? __ldg(rrow + jj) : V(0);
       }
     };
-    T rr[PF][C];
+    V rr[PF][C];
     if constexpr (DIR > 0) {
 #pragma unroll
       for (int j = 0; j < PF; ++j)
@@ -358,7 +359,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
           const int e = t * W + lane;
           T t0;
           if constexpr (DIR > 0) {
-            t0 = rr[j][t];
+            t0 = E::from_vec(rr[j][t]);
           } else {
             // the forward words of padding slots (dinv zero) may not have
             // been copied into this buffer: take zero, not 0 * stale bits

@@ -380,6 +380,87 @@ static int ngrid(long long work, int block) {
 void mpnn_set_graph(MpnnDev &D, const double *d_amat, cudaStream_t st) {
   k_edge_deg<<<ngrid(D.n, 256), 256, 0, st>>>(D.n, D.ia, d_amat, D.deg);
   k_edge_w<<<ngrid(D.n, 256), 256, 0, st>>>(D.n, D.ia, D.ja, d_amat, D.deg, D.w);
+  if (D.amat) cudaMemcpyAsync(D.amat, d_amat, sizeof(double) * D.nja, cudaMemcpyDeviceToDevice, st);
+}
+
+// ---- energy loss (mode 1) ----
+// e = mask*(dh(y) - dh(t)), tt = mask*dh(t) in head units, dh(u) = soft*sinh(u*scale).
+__global__ void k_energy_err(int n, const float *__restrict__ y, const float *__restrict__ t,
+                             const float *__restrict__ mask, double soft, double scale,
+                             double *__restrict__ ee, double *__restrict__ tt) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double m = mask[i] > 0.f ? 1.0 : 0.0;
+    const double dt = soft * sinh((double)t[i] * scale);
+    const double dy = soft * sinh((double)y[i] * scale);
+    ee[i] = m * (dy - dt);
+    tt[i] = m * dt;
+  }
+}
+
+// we = -A e over the active rows, and per-block partials of e'(-A e) and
+// t'(-A t) (epart[2b], epart[2b+1]).
+__global__ void k_energy_dots(int n, const int *__restrict__ ia, const int *__restrict__ ja,
+                              const double *__restrict__ amat, const float *__restrict__ mask,
+                              const double *__restrict__ ee, const double *__restrict__ tt,
+                              double *__restrict__ we, double *__restrict__ epart) {
+  double s1 = 0.0, s2 = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double ae = 0.0, at = 0.0;
+    if (mask[i] > 0.f) {
+      for (int k = ia[i]; k < ia[i + 1]; ++k) {
+        const int j = ja[k];
+        ae = fma(-amat[k], ee[j], ae);
+        at = fma(-amat[k], tt[j], at);
+      }
+    }
+    we[i] = ae;
+    s1 = fma(ee[i], ae, s1);
+    s2 = fma(tt[i], at, s2);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  __shared__ double sh[2][32];
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = s1;
+    sh[1][threadIdx.x >> 5] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += sh[0][w];
+      b += sh[1][w];
+    }
+    epart[2 * blockIdx.x] = a;
+    epart[2 * blockIdx.x + 1] = b;
+  }
+}
+
+// dy += 2 (W e)_i / t'Wt * dh'(y_i) on active cells and loss += e'We / t'Wt,
+// the partials summed in block order by every block.
+__global__ void k_energy_grad(int n, int G, const double *__restrict__ epart,
+                              const double *__restrict__ we, const float *__restrict__ y,
+                              const float *__restrict__ mask, double soft, double scale,
+                              float *__restrict__ dy, float *__restrict__ loss) {
+  __shared__ double s_inv;
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < G; ++q) {
+      a += epart[2 * q];
+      b += epart[2 * q + 1];
+    }
+    s_inv = (b > 0.0) ? 1.0 / b : 0.0;
+    if (blockIdx.x == 0) atomicAdd(loss, (float)(a * s_inv));
+  }
+  __syncthreads();
+  const double inv = s_inv;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!(mask[i] > 0.f)) continue;
+    const double d = soft * scale * cosh((double)y[i] * scale);
+    dy[i] += (float)(2.0 * we[i] * inv * d);
+  }
 }
 
 void mpnn_refresh_bf16(MpnnDev &D, cudaStream_t st) {
@@ -465,8 +546,16 @@ static void forward_from_xbf(MpnnDev &D, const float *target, const float *mask,
                                                     D.mask[l]);
   }
   if (target) cudaMemsetAsync(D.loss, 0, sizeof(float), st);
+  const bool energy = target && D.energy;
   k_readout<<<ga, 256, 0, st>>>(n, D.H[kL], D.p + P::wout, D.p + P::bout, D.y, target, mask,
-                                inv_count, D.dy, D.loss);
+                                energy ? inv_count * D.mse_w : inv_count, D.dy, D.loss);
+  if (energy) {
+    const int G = std::min(kMpnnRedBlocks, (n + 255) / 256);
+    k_energy_err<<<ngrid(n, 256), 256, 0, st>>>(n, D.y, target, mask, D.dh_soft, D.dh_scale, D.ee, D.tt);
+    k_energy_dots<<<G, 256, 0, st>>>(n, D.ia, D.ja, D.amat, mask, D.ee, D.tt, D.we, D.epart);
+    k_energy_grad<<<ngrid(n, 256), 256, 0, st>>>(n, G, D.epart, D.we, D.y, mask, D.dh_soft,
+                                                 D.dh_scale, D.dy, D.loss);
+  }
 }
 
 // Backward pass after mpnn_forward with a target: gradients into D.g.

@@ -29,7 +29,15 @@ struct MpnnDev {
   float *dH = nullptr, *dHp = nullptr, *dX = nullptr;
   __nv_bfloat16 *dZ = nullptr;
   int steps = 0;                              // Adam steps taken
+  // energy loss (mode 1): the matrix of the last set_graph, the errors and
+  // true changes in head units, W*e, and per-block partials of e'We, t'Wt
+  int nja = 0;
+  int energy = 0;
+  float mse_w = 1.f;
+  double dh_soft = 1.0, dh_scale = 1.0;
+  double *amat = nullptr, *ee = nullptr, *tt = nullptr, *we = nullptr, *epart = nullptr;
 };
+constexpr int kMpnnRedBlocks = 1024;  // grid of the energy-loss reductions
 
 long long mpnn_param_count();
 void mpnn_set_graph(MpnnDev &D, const double *d_amat, cudaStream_t st);

@@ -8,9 +8,13 @@ cell's K, the previous heads, the previous step's head change, the well
 rates and the boundary mask.  The
 prediction is only an initial guess: PCG + ILU0 still runs to the same
 INNER_DVCLOSE / INNER_RCLOSE closure, so the plain solver stays the judge.
-The guessed step may spend at most the inner iterations the plain solver took
-on the previous step; past that the guess is dropped and the step is solved
-from the previous heads (gbsln_timestep_warm).
+The first iterate is the point of the line from the previous heads through
+the guess that is closest to the solution in the energy norm of the step's
+first system (one SpMV and two dot products on the device), so a noisy guess
+is shrunk toward the previous heads instead of taken whole.  The guessed step
+may spend at most the inner iterations the plain solver took on the previous
+step; past that the guess is dropped and the step is solved from the
+previous heads (gbsln_timestep_warm).
 
 `Graph.features` builds the 16 input features of the cells, `generate` the
 training samples (heads from the plain solver), `WarmStartNet` wraps the C
@@ -171,6 +175,15 @@ class WarmStartNet:
     def set_graph(self, d_amat):
         self._chk(self._lib.gbmpnn_set_graph(self._h, C.c_void_p(d_amat.data_ptr())))
 
+    def set_loss(self, mode: str, mse_weight: float = 0.0):
+        """gbmpnn_set_loss: "mse" (squared error in network units) or
+        "energy" (relative energy error of the predicted head change under
+        the matrix of the last set_graph, plus mse_weight times the squared
+        error); the unit scalings are the network's current ones."""
+        m = {"mse": 0, "energy": 1}[mode]
+        sc = scaling(self)
+        self._chk(self._lib.gbmpnn_set_loss(self._h, m, C.byref(sc), float(mse_weight)))
+
     def predict(self, x):
         import torch
         y = torch.empty(self.nodes, dtype=torch.float32, device=x.device)
@@ -223,9 +236,13 @@ class WarmStartNet:
 
 
 def train(net: WarmStartNet, data, dh_scale: float, epochs: int = 4,
-          lr: float = 1e-3) -> list[float]:
+          lr: float = 1e-3, loss: str = "energy", mse_weight: float = 0.05) -> list[float]:
     """Adam over every sample of every model, `epochs` times, the learning
-    rate halved each epoch; mean loss per epoch."""
+    rate halved each epoch; mean loss per epoch.  The default loss is the
+    relative energy error of the predicted change (gbmpnn_set_loss), the
+    error a conjugate-gradient solve from the guess has to remove: a
+    pointwise squared error lets through high-frequency noise that is cheap
+    in that norm's eyes to the network and expensive to the solver."""
     net.dh_scale = dh_scale
     # predictions are bounded by the largest head change seen in training,
     # with a 25 % margin in metres (not in the asinh units, where the same
@@ -237,6 +254,7 @@ def train(net: WarmStartNet, data, dh_scale: float, epochs: int = 4,
             tmax = max(tmax, float(s.target.abs().max().item()))
     dh_max = float(np.sinh(tmax * dh_scale)) * DH_SOFT
     net.unit_max = float(np.arcsinh(1.25 * dh_max / DH_SOFT)) / dh_scale
+    net.set_loss(loss, mse_weight)
     hist = []
     for ep in range(epochs):
         tot, cnt = 0.0, 0
@@ -291,13 +309,16 @@ def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0
     those iterations counted too).  The guess is built, evaluated and used on
     the device with no host round trip in between.  Reported: inner
     iterations and device time of both paths (the warm path's time includes
-    inference and any fallbacks), the steps that fell back, and the RMS and
-    maximum error of the guess and of the previous heads against the
-    converged heads."""
+    inference and any fallbacks), the steps that fell back, the line-search
+    factors, the RMS and maximum error of the guess, of the first iterate
+    and of the previous heads against the converged heads, and the energy
+    errors e'(-A)e of the guess and of the first iterate relative to that of
+    the previous heads (A the step's matrix)."""
     import torch
 
     it_prev, it_warm, fell = [], [], 0
-    rms_g, rms_p, max_g, max_p = [], [], [], []
+    rms_g, rms_p, rms_0, max_g, max_p, alphas = [], [], [], [], [], []
+    en_g, en_0 = [], []   # energy errors relative to the previous heads'
     ms_prev, ms_warm, ms_net = 0.0, 0.0, 0.0
     converged = True
     for s in seeds:
@@ -305,7 +326,16 @@ def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0
         g = Graph(m)
         base, warm = new_solution(m), new_solution(m)
         amat, _ = base.formulate(delt, hold=m.strt)
-        net.set_graph(torch.from_numpy(amat).cuda())
+        d_amat = torch.from_numpy(amat).cuda()
+        net.set_graph(d_amat)
+        rows = torch.from_numpy(np.repeat(np.arange(m.nodes), np.diff(g.ia))).cuda()
+        cols = torch.from_numpy(np.asarray(g.ja, np.int64)).cuda()
+
+        def energy(e):
+            # e'(-A)e over the active cells (e is zero elsewhere)
+            we = torch.zeros_like(e).index_add_(0, rows, -d_amat * e[cols]) * g.active64
+            return float((e * we).sum().item())
+
         nact = float(g.active64.sum().item())
         guess = torch.empty(m.nodes, dtype=torch.float64, device="cuda")
         cap_unbounded = 10 ** 9
@@ -321,8 +351,15 @@ def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0
             h_true = torch.from_numpy(warm.heads).cuda()
             eg = (guess - h_true) * g.active64
             ep = (h_prev - h_true) * g.active64
+            e0 = ep + st_w["guess_alpha"] * (eg - ep)   # the first iterate's error
+            alphas.append(st_w["guess_alpha"])
             rms_g.append(float(torch.sqrt((eg * eg).sum() / nact).item()))
             rms_p.append(float(torch.sqrt((ep * ep).sum() / nact).item()))
+            rms_0.append(float(torch.sqrt((e0 * e0).sum() / nact).item()))
+            ep_en = energy(ep)
+            if ep_en > 0.0:
+                en_g.append(energy(eg) / ep_en)
+                en_0.append(energy(e0) / ep_en)
             max_g.append(float(eg.abs().max().item()))
             max_p.append(float(ep.abs().max().item()))
             it_prev.append(st_b["inner_total"])
@@ -342,4 +379,9 @@ def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0
             "inference_ms_per_guess": ms_net / max(1, ip.size),
             "time_ratio": (ms_warm + ms_net) / max(1e-9, ms_prev),
             "rms_err_guess": float(np.mean(rms_g)), "rms_err_prev_heads": float(np.mean(rms_p)),
+            "rms_err_first_iterate": float(np.mean(rms_0)), "alpha_mean": float(np.mean(alphas)),
+            "energy_err_guess_rel": float(np.mean(en_g)) if en_g else None,
+            "energy_err_first_iterate_rel": float(np.mean(en_0)) if en_0 else None,
+            "alpha_min": float(np.min(alphas)), "alpha_max": float(np.max(alphas)),
+            "inner_per_step_prev_heads": ip.tolist(), "inner_per_step_warm": iw.tolist(),
             "max_err_guess": float(np.max(max_g)), "max_err_prev_heads": float(np.max(max_p))}

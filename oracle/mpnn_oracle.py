@@ -11,7 +11,10 @@ of the oracle itself.
 Network (hidden 64, 8 layers, 16 input features):
   H0 = relu(X W0 + b0);  A_l = S H_{l-1};  Z_l = [H_{l-1}, A_l] W_l + b_l;
   H_l = H_{l-1} + relu(Z_l);  y = H_8 wout + bout;
-  loss = sum(((y - t) * mask)^2) * inv_count.
+  loss = sum(((y - t) * mask)^2) * inv_count, or with `energy` (the loss of
+  gbmpnn_set_loss mode 1, k_mpnn.cu k_energy_*): with dh(u) = soft*sinh(u*scale),
+  e = mask*(dh(y) - dh(t)), t' = mask*dh(t) and W = -A over the active rows,
+  loss = e'We / t''Wt' + mse_weight * sum(((y - t) * mask)^2) * inv_count.
 S_ij = c_ij / sqrt(d_i d_j) with c_ij = max(-a_ij, 0) over the off-diagonal
 CSR entries and d_i = sum_j c_ij.
 """
@@ -81,8 +84,25 @@ def unpack(p, dtype):
     return W
 
 
-def loss_and_grad(p, ia, ja, w, X, target, mask, inv_count, bf16_ops=True):
-    """(loss, flat gradient, y) of the network; see the module docstring."""
+def _energy_terms(ia, ja, amat, y, target, mask, soft, scale):
+    """(e'We / t'Wt, dLoss/dy) of the energy loss, in float64."""
+    y = np.asarray(y, np.float64)
+    m = (np.asarray(mask) > 0).astype(np.float64)
+    n = m.size
+    rows = np.repeat(np.arange(n), np.diff(ia))
+    dh_t = soft * np.sinh(np.asarray(target, np.float64) * scale)
+    e = m * (soft * np.sinh(y * scale) - dh_t)
+    t = m * dh_t
+    we = -np.bincount(rows, weights=amat * e[ja], minlength=n) * m
+    wt = -np.bincount(rows, weights=amat * t[ja], minlength=n) * m
+    den = float(t @ wt)
+    inv = 1.0 / den if den > 0.0 else 0.0
+    return float(e @ we) * inv, m * 2.0 * we * inv * soft * scale * np.cosh(y * scale)
+
+
+def loss_and_grad(p, ia, ja, w, X, target, mask, inv_count, bf16_ops=True, energy=None):
+    """(loss, flat gradient, y) of the network; see the module docstring.
+    `energy`: None, or dict(amat=, soft=, scale=, mse_weight=)."""
     dt = np.float32 if bf16_ops else np.float64
     r = bf16 if bf16_ops else (lambda a: np.asarray(a, dtype=dt))
     P = unpack(np.asarray(p, dtype=np.float64), dt)
@@ -102,8 +122,14 @@ def loss_and_grad(p, ia, ja, w, X, target, mask, inv_count, bf16_ops=True):
         Hq.append(r(H[l]))
     y = H[LAYERS] @ P["wout"] + P["bout"][0]
     e = (y - target.astype(dt)) * mask.astype(dt)
-    loss = float(np.sum(e * e) * inv_count)
-    dy = 2 * e * dt(inv_count)
+    mw = 1.0 if energy is None else float(energy["mse_weight"])
+    loss = float(np.sum(e * e) * inv_count * mw)
+    dy = 2 * e * dt(inv_count * mw)
+    if energy is not None:
+        le, dye = _energy_terms(ia, ja, energy["amat"], y, target, mask, energy["soft"],
+                                energy["scale"])
+        loss += le
+        dy = (dy + dye).astype(dt)
     G = {"wout": H[LAYERS].T @ dy, "bout": np.array([dy.sum()])}
     dH = np.outer(dy, P["wout"]).astype(dt)
     for l in range(LAYERS, 0, -1):
