@@ -453,6 +453,7 @@ def gb_arm(a):
         h = ws_res["heldout"]
         forms.update(warmstart_time_ratio=h.get("time_ratio"),
                      warmstart_iteration_ratio=h.get("iteration_ratio"),
+                     warmstart_extrap_only_iteration_ratio=h.get("iteration_ratio_extrap"),
                      warmstart_train_models=ws_res["train_models"],
                      warmstart_heldout_models=h.get("models"))
     line = {
@@ -616,8 +617,9 @@ def warmstart_form(a) -> dict:
     """The learned warm start on the transient 256x256x3 workload (C5): the
     network is trained on the GPU (its own BF16 tensor-core kernels) on heads
     the plain solver produces for seeded training models, then every time step
-    of held-out models is solved from the previous heads and from the
-    network's guess, to the same closure."""
+    of held-out models is solved from the previous heads, from the energy
+    projection onto the last step's change alone, and from the projection onto
+    the last change and the network's guess, all to the same closure."""
     import time as _t
     from modflow6_gb300.warmstart import WarmStartNet, evaluate, generate, train
 

@@ -195,7 +195,8 @@ int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times *t);
 /* Autotuner (no counterpart in the reference, which has no tunable kernels):
  * on the handle's own factored system it times every wavefront tiling of
  * the structured sweeps (chunk of steps per ring buffer, ring depth,
- * neighbour-word prefetch depth, CTAs per SM), the form of the level-
+ * neighbour-word prefetch depth, CTAs per SM, thread-block clusters whose
+ * row blocks hand over through distributed shared memory), the form of the level-
  * scheduled sweeps of other patterns, and the thread-block count of the
  * dot/update reductions, and keeps the fastest for the following applies.
  * The tiling does not change any cell's arithmetic; the reduction grid only
@@ -214,6 +215,8 @@ typedef struct gbims_tuning {
   double candidate_ms[16];          /* one ILU0 application per tiling */
   double precond_ms;                /* of the chosen tiling */
   double vector_ms;                 /* dot + update at the chosen grid */
+  int sweep_cluster;                /* CTAs per thread-block cluster of the chosen tiling
+                                       (1: none); candidate_ms is -1 for tilings not timed */
 } gbims_tuning;
 int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out);
 /* Applies a tuning found earlier (sweep_config < 0, reduction_blocks <= 0 or
@@ -357,9 +360,12 @@ typedef struct gbsln_stats {
   double dxmax;       /* last outer max head change */
   double fill_ms, solve_ms, total_ms; /* device time of the step */
   int backtracks;     /* backtracking reductions taken in the step */
-  double guess_alpha; /* the step's first iterate was xold + guess_alpha*(guess - xold):
-                         1 for gbsln_timestep_guess, the line-search factor for
-                         gbsln_timestep_warm, 0 for a step from the previous heads */
+  /* the step's first iterate on its active cells was
+   * xold + prev_alpha*(last step's change) + guess_alpha*(guess - xold):
+   * guess_alpha 1 for gbsln_timestep_guess, both projection factors for
+   * gbsln_timestep_warm, both 0 for a step from the previous heads */
+  double guess_alpha;
+  double prev_alpha;
 } gbsln_stats;
 
 int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,
@@ -378,13 +384,18 @@ int gbsln_timestep_guess(gbsln_handle *h, int kper, int kstp, double delt, const
                          gbsln_stats *st);
 /* The warm start with its fallback (no counterpart in the reference, whose
  * steps always start from the previous heads).  The first iterate of the
- * active cells is xold + alpha*(d_guess - xold), alpha = d.r / d.(A d) with
- * d = d_guess - xold and A, r the step's first system and residual at the
- * previous heads, kept in [0, 2]: for the symmetric GWF matrix the point of
- * that line closest to the solution in the energy norm, never farther from
- * it than the previous heads.  When the step has spent inner_cap inner
- * iterations without closing, the guess is dropped and the step is solved
- * again from the previous heads; then the status is GBIMS_WARN_FALLBACK and
+ * active cells is xold + a1*d1 + a2*d2 with d1 the head change of the last
+ * step (when the last step closed; none after create, restart or
+ * set_heads), d2 = d_guess - xold (none when d_guess is NULL), and
+ * (a1, a2) = (D'AD)^-1 D'r for A, r the step's first system and its
+ * residual at the previous heads: for the symmetric GWF matrix the point of
+ * that plane closest to the solution in the energy norm, never farther from
+ * it than the previous heads (a single direction when the two are nearly
+ * parallel; the previous heads when a factor is not finite or beyond +-4).
+ * A step with neither direction starts from the previous heads.  When the
+ * step has spent inner_cap inner iterations without closing, the projected
+ * start is dropped and the step is solved again from the previous heads;
+ * then the status is GBIMS_WARN_FALLBACK and
  * *st counts the iterations and device time of both attempts.  Give
  * inner_cap the inner iterations the plain solver took on the previous step:
  * a guess then never costs more than one step's worth of iterations. */

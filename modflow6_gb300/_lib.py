@@ -87,7 +87,7 @@ class GbslnStats(C.Structure):
         ("outer", C.c_int), ("inner_total", C.c_int), ("converged", C.c_int),
         ("pivot_retries", C.c_int), ("dxmax", C.c_double), ("fill_ms", C.c_double),
         ("solve_ms", C.c_double), ("total_ms", C.c_double), ("backtracks", C.c_int),
-        ("guess_alpha", C.c_double),
+        ("guess_alpha", C.c_double), ("prev_alpha", C.c_double),
     ]
 
 
@@ -102,6 +102,7 @@ class GbimsTuning(C.Structure):
         ("sweep_prefetch", C.c_int), ("sweep_occupancy", C.c_int), ("reduction_blocks", C.c_int),
         ("level_mode", C.c_int), ("level_ms", C.c_double * 2), ("ncandidates", C.c_int),
         ("candidate_ms", C.c_double * 16), ("precond_ms", C.c_double), ("vector_ms", C.c_double),
+        ("sweep_cluster", C.c_int),
     ]
 
 

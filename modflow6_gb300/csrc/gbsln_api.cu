@@ -243,7 +243,10 @@ struct gbsln_handle {
          *dxold = nullptr, *part = nullptr, *bnd_val = nullptr, *chd_head = nullptr;
   int *ibound = nullptr, *bnd_ptr = nullptr, *chd_node = nullptr, *flag = nullptr;
   int *bnd_kind = nullptr;  // per boundary entry: 0 WEL, 1 RCH
-  double *galpha = nullptr; // the last warm step's line-search factor
+  double *galpha = nullptr; // the last warm step's projection factors (2)
+  double *dprev = nullptr;  // the last step's head change (valid when have_prev)
+  double *gpart = nullptr;  // projection partials (5 per block)
+  bool have_prev = false;
   double *bpart = nullptr;  // budget partials (kGwfBudgetSlots per block)
   int nchd = 0, G = 1;
   bool has_sto = false;
@@ -275,76 +278,111 @@ __global__ void k_apply_guess(int n, const int *__restrict__ ibound, const doubl
     if (ibound[i] > 0) x[i] = guess[i];
 }
 
-// Energy line search of a guess (no counterpart in the reference): with
-// d = guess - xold on active cells (zero elsewhere) and r = rhs - A*xold, the
-// partials of d.r and d.(A d) per block (part[2b], part[2b+1]).  For the
-// symmetric (negative definite) GWF matrix, x0 = xold + alpha*d with
-// alpha = d.r / d.(A d) is the point of the line through xold and the guess
-// closest to the solution in the energy norm, so it is never farther from
-// the solution in that norm than the previous heads are.
+// Energy projection of the first iterate (no counterpart in the
+// reference).  With d1 = the previous step's head change (zero when there
+// is none), d2 = guess - xold (zero without a guess), both zero off the
+// active cells, and r = rhs - A*xold, the per-block partials (part[5b..])
+// of d1.r, d2.r, d1.(A d1), d1.(A d2), d2.(A d2).  For the symmetric
+// (negative definite) GWF matrix, x0 = xold + a1*d1 + a2*d2 with
+// (a1, a2) = (D'AD)^-1 D'r is the point of the plane through xold spanned
+// by d1 and d2 closest to the solution in the energy norm: never farther
+// from it than the previous heads, nor than the better of the two
+// directions alone.
 __global__ void k_guess_dots(int n, const int *__restrict__ ia, const int *__restrict__ ja,
                              const double *__restrict__ amat, const double *__restrict__ rhs,
-                             const int *__restrict__ ibound, const double *__restrict__ guess,
-                             const double *__restrict__ xold, double *part) {
-  double s1 = 0.0, s2 = 0.0;
+                             const int *__restrict__ ibound, const double *__restrict__ dprev,
+                             const double *__restrict__ guess, const double *__restrict__ xold,
+                             double *part) {
+  double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     if (ibound[i] < 1) continue;
-    double ax = 0.0, ad = 0.0;
+    double ax = 0.0, a1 = 0.0, a2 = 0.0;
     for (int k = ia[i]; k < ia[i + 1]; ++k) {
       const int j = ja[k];
       const double xj = xold[j];
-      const double dj = (ibound[j] > 0) ? guess[j] - xj : 0.0;
+      const bool act = ibound[j] > 0;
+      const double d1 = (act && dprev) ? dprev[j] : 0.0;
+      const double d2 = (act && guess) ? guess[j] - xj : 0.0;
       ax = fma(amat[k], xj, ax);
-      ad = fma(amat[k], dj, ad);
+      a1 = fma(amat[k], d1, a1);
+      a2 = fma(amat[k], d2, a2);
     }
-    const double di = guess[i] - xold[i];
-    s1 = fma(di, rhs[i] - ax, s1);
-    s2 = fma(di, ad, s2);
+    const double r = rhs[i] - ax;
+    const double d1 = dprev ? dprev[i] : 0.0;
+    const double d2 = guess ? guess[i] - xold[i] : 0.0;
+    s[0] = fma(d1, r, s[0]);
+    s[1] = fma(d2, r, s[1]);
+    s[2] = fma(d1, a1, s[2]);
+    s[3] = fma(d1, a2, s[3]);
+    s[4] = fma(d2, a2, s[4]);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-  }
-  __shared__ double sh[2][32];
-  if ((threadIdx.x & 31) == 0) {
-    sh[0][threadIdx.x >> 5] = s1;
-    sh[1][threadIdx.x >> 5] = s2;
+  __shared__ double sh[5][32];
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    double v = s[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = v;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      a += sh[0][w];
-      b += sh[1][w];
-    }
-    part[2 * blockIdx.x] = a;
-    part[2 * blockIdx.x + 1] = b;
+  if (threadIdx.x < 5) {
+    double a = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += sh[threadIdx.x][w];
+    part[5 * blockIdx.x + threadIdx.x] = a;
   }
 }
 
-// x = xold + alpha*(guess - xold) on active cells, alpha from the G pairs of
-// partials summed in block order by every block (the same alpha everywhere),
-// kept in [0, 2]; block 0 also writes alpha to *alpha_out.
+// The 2x2 projection from the G blocks' partials, summed in block order by
+// every block (the same factors everywhere): the plane when its Gram matrix
+// is well conditioned, else the better single direction; factors that are
+// not finite, or beyond +-4, give the previous heads.  Then
+// x = xold + a1*d1 + a2*d2 on active cells; block 0 writes (a1, a2).
 __global__ void k_guess_blend(int n, int G, const double *__restrict__ part,
-                              const int *__restrict__ ibound, const double *__restrict__ guess,
-                              const double *__restrict__ xold, double *__restrict__ x,
-                              double *alpha_out) {
-  __shared__ double alpha;
+                              const int *__restrict__ ibound, const double *__restrict__ dprev,
+                              const double *__restrict__ guess, const double *__restrict__ xold,
+                              double *__restrict__ x, double *alpha_out) {
+  __shared__ double s_a1, s_a2;
   if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0;
-    for (int q = 0; q < G; ++q) {
-      a += part[2 * q];
-      b += part[2 * q + 1];
+    double t[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int q = 0; q < G; ++q)
+      for (int c = 0; c < 5; ++c) t[c] += part[5 * q + c];
+    const double b1 = t[0], b2 = t[1], m11 = t[2], m12 = t[3], m22 = t[4];
+    double a1 = 0.0, a2 = 0.0;
+    const double det = m11 * m22 - m12 * m12;
+    if (m11 != 0.0 && m22 != 0.0 && det > 1e-10 * m11 * m22) {
+      a1 = (m22 * b1 - m12 * b2) / det;
+      a2 = (m11 * b2 - m12 * b1) / det;
+    } else {
+      // one direction: the one that removes more energy (b^2/|m|)
+      const double g1 = (m11 != 0.0) ? b1 * b1 / fabs(m11) : 0.0;
+      const double g2 = (m22 != 0.0) ? b2 * b2 / fabs(m22) : 0.0;
+      if (g1 >= g2 && m11 != 0.0) a1 = b1 / m11;
+      else if (m22 != 0.0) a2 = b2 / m22;
     }
-    double al = (b != 0.0) ? a / b : 0.0;
-    al = (al == al) ? fmin(fmax(al, 0.0), 2.0) : 0.0;
-    alpha = al;
-    if (blockIdx.x == 0) *alpha_out = al;
+    if (!(fabs(a1) <= 4.0) || !(fabs(a2) <= 4.0)) a1 = a2 = 0.0;
+    s_a1 = a1;
+    s_a2 = a2;
+    if (blockIdx.x == 0) {
+      alpha_out[0] = a1;
+      alpha_out[1] = a2;
+    }
   }
   __syncthreads();
-  const double al = alpha;
+  const double a1 = s_a1, a2 = s_a2;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (ibound[i] < 1) continue;
+    double v = xold[i];
+    if (dprev) v = fma(a1, dprev[i], v);
+    if (guess) v = fma(a2, guess[i] - xold[i], v);
+    x[i] = v;
+  }
+}
+
+// The head change of the step just taken (x - xold) on active cells, zero
+// elsewhere: the first direction of the next warm step's projection.
+__global__ void k_prev_change(int n, const int *__restrict__ ibound, const double *__restrict__ x,
+                              const double *__restrict__ xold, double *__restrict__ d) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    if (ibound[i] > 0) x[i] = fma(al, guess[i] - xold[i], xold[i]);
+    d[i] = (ibound[i] > 0) ? x[i] - xold[i] : 0.0;
 }
 
 __global__ void k_set_chd(int nchd, const int *__restrict__ node, const double *__restrict__ head,
@@ -453,7 +491,9 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
   h->G = std::max(1, std::min(2 * kNumSM * 2, (n + 255) / 256));
   chk(up<double>(&h->part, nullptr, (size_t)h->G * 2));
   chk(up<int>(&h->flag, nullptr, 4));
-  chk(up<double>(&h->galpha, nullptr, 1));
+  chk(up<double>(&h->galpha, nullptr, 2));
+  chk(up<double>(&h->dprev, nullptr, (size_t)n));
+  chk(up<double>(&h->gpart, nullptr, (size_t)h->G * 5));
   chk(up(&h->strt, strt, (size_t)n));
   if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GBIMS_ERR_CUDA; }
   for (double **p : wv) cudaMemset(*p, 0, sizeof(double) * n);
@@ -533,7 +573,7 @@ extern "C" int gbsln_timestep_guess(gbsln_handle *h, int kper, int kstp, double 
 
 extern "C" int gbsln_timestep_warm(gbsln_handle *h, int kper, int kstp, double delt,
                                    const double *d_guess, int inner_cap, gbsln_stats *st) {
-  if (!h || !d_guess || inner_cap < 1) return GBIMS_ERR_ARG;
+  if (!h || inner_cap < 1) return GBIMS_ERR_ARG;
   gbsln_stats a;
   memset(&a, 0, sizeof(a));
   int rc = timestep_core(h, kper, kstp, delt, d_guess, &a, inner_cap, true);
@@ -542,12 +582,13 @@ extern "C" int gbsln_timestep_warm(gbsln_handle *h, int kper, int kstp, double d
     return rc;
   }
   // fall back: the step again from the previous heads (xold still holds
-  // them: the guess only ever replaced the first iterate)
+  // them: the projection only ever replaced the first iterate)
   SLN_CUDA(h, cudaMemcpyAsync(h->x, h->xold, sizeof(double) * h->n, cudaMemcpyDeviceToDevice, h->st));
   gbsln_stats b;
   memset(&b, 0, sizeof(b));
   rc = timestep_core(h, kper, kstp, delt, nullptr, &b);
   b.guess_alpha = a.guess_alpha;
+  b.prev_alpha = a.prev_alpha;
   b.inner_total += a.inner_total;
   b.fill_ms += a.fill_ms;
   b.solve_ms += a.solve_ms;
@@ -603,20 +644,31 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
     *l2 = sqrt(ss);
     return rc;
   };
-  if (d_guess && project) {
-    // the first iterate on the line through the previous heads and the
-    // guess, at its energy-norm optimum for the step's first system (built
-    // at the previous heads, as the plain step's first outer iteration is)
+  const double *dprev = h->have_prev ? h->dprev : nullptr;
+  const bool projected = project && (d_guess || dprev);
+  if (projected) {
+    // the first iterate in the plane through the previous heads spanned by
+    // the last step's change and the guess's, at its energy-norm optimum
+    // for the step's first system (built at the previous heads, as the
+    // plain step's first outer iteration is)
     SLN_CUDA(h, cudaMemsetAsync(h->amat, 0, sizeof(double) * h->nja, h->st));
     SLN_CUDA(h, cudaMemsetAsync(h->rhs, 0, sizeof(double) * n, h->st));
     gwf_npf_cf(n, h->g, h->ibound, h->x, h->d.sat, h->st);
     gwf_fill(n, h->g, f, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, h->amat, h->rhs, h->st);
-    k_guess_dots<<<h->G, 256, 0, h->st>>>(n, h->d.ia, h->d.ja, h->amat, h->rhs, h->ibound, d_guess,
-                                            h->xold, h->part);
+    k_guess_dots<<<h->G, 256, 0, h->st>>>(n, h->d.ia, h->d.ja, h->amat, h->rhs, h->ibound, dprev,
+                                            d_guess, h->xold, h->gpart);
     k_guess_blend<<<std::min(4 * kNumSM, (n + 255) / 256), 256, 0, h->st>>>(
-        n, h->G, h->part, h->ibound, d_guess, h->xold, h->x, h->galpha);
+        n, h->G, h->gpart, h->ibound, dprev, d_guess, h->xold, h->x, h->galpha);
     SLN_CUDA(h, cudaGetLastError());
   }
+  auto read_alphas = [&]() -> int {
+    double al[2] = {0.0, 0.0};
+    if (projected) SLN_CUDA(h, cudaMemcpy(al, h->galpha, sizeof(al), cudaMemcpyDeviceToHost));
+    else if (d_guess) al[1] = 1.0;
+    s.prev_alpha = al[0];
+    s.guess_alpha = al[1];
+    return GBIMS_OK;
+  };
   for (int kiter = 1; kiter <= h->nl.mxiter; ++kiter) {
     if (d_guess && inner_cap > 0 && kiter > 1 && s.inner_total >= inner_cap) {
       // the guessed step has used its budget without closing
@@ -625,7 +677,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
       float tot = 0.f;
       cudaEventElapsedTime(&tot, h->e0, h->e1);
       s.total_ms = tot;
-      if (project) SLN_CUDA(h, cudaMemcpy(&s.guess_alpha, h->galpha, sizeof(double), cudaMemcpyDeviceToHost));
+      if (int rc = read_alphas()) return rc;
       if (st) *st = s;
       return kCapReached;
     }
@@ -780,9 +832,13 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
   s.total_ms = tot;
   s.converged = converged ? 1 : 0;
   s.dxmax = hncg;
-  s.guess_alpha = (d_guess && !project) ? 1.0 : 0.0;
-  if (d_guess && project)
-    SLN_CUDA(h, cudaMemcpy(&s.guess_alpha, h->galpha, sizeof(double), cudaMemcpyDeviceToHost));
+  if (int rc = read_alphas()) return rc;
+  // the step's head change, the first direction of the next warm step
+  if (converged)
+    k_prev_change<<<std::min(4 * kNumSM, (n + 255) / 256), 256, 0, h->st>>>(n, h->ibound, h->x,
+                                                                           h->xold, h->dprev);
+  h->have_prev = converged;
+  SLN_CUDA(h, cudaGetLastError());
   if (st) *st = s;
   return GBIMS_OK;
 }
@@ -878,6 +934,7 @@ extern "C" int gbsln_restart(gbsln_handle *h) {
   SLN_CUDA(h, cudaStreamSynchronize(h->st));
   h->bigch = h->bigchold = h->relaxold = h->l2norm0_ptc = h->ptcdel = 0.0;
   h->res_prev = h->res_new = 0.0;
+  h->have_prev = false;
   return GBIMS_OK;
 }
 
@@ -892,6 +949,7 @@ extern "C" int gbsln_set_heads(gbsln_handle *h, const double *x) {
   if (!h || !x) return GBIMS_ERR_ARG;
   SLN_CUDA(h, cudaStreamSynchronize(h->st));
   SLN_CUDA(h, cudaMemcpy(h->x, x, sizeof(double) * h->n, cudaMemcpyHostToDevice));
+  h->have_prev = false;
   return GBIMS_OK;
 }
 
@@ -916,7 +974,7 @@ extern "C" int gbsln_destroy(gbsln_handle *h) {
   void *p[] = {h->strt, h->ss, h->sy, h->area, h->vol, h->xold, h->xtemp, h->wsave, h->hchold, h->deold,
                h->dxold, h->part, h->bnd_val, h->chd_head, h->ibound, h->bnd_ptr, h->chd_node,
                h->bnd_kind, h->bpart,
-               h->flag, h->galpha};
+               h->flag, h->galpha, h->dprev, h->gpart};
   for (void *q : p)
     if (q) cudaFree(q);
   if (h->e0) cudaEventDestroy(h->e0);

@@ -14,9 +14,11 @@
 // few ulps of hi, which is all the next product needs.  Explicit _rn
 // intrinsics keep the compiler from contracting the error terms.
 //
-// Conversions to and from FP64 use integer instructions where they sit on a
-// hot path (no FP64 instruction per element): a double is split by bit
-// manipulation, a float is widened by rebuilding its exponent field.  Values
+// A double is split into a pair by bit manipulation (no FP64 instruction);
+// a pair goes back to FP64 as its two floats widened by rebuilding their
+// exponent fields and added once in FP64 (measured faster, in the sweeps,
+// than an all-integer conversion, which costs the chain's warp more issue
+// slots than the one FP64 add does).  Values
 // whose magnitude lies outside [2^-100, 2^100] do not keep their accuracy
 // (the float exponent range); the factor tiles are checked against that
 // range before the df64 sweeps are used.
@@ -97,36 +99,6 @@ __device__ __forceinline__ double df_widen(float f) {
 // df64 -> double: the two widened halves added once in FP64
 __device__ __forceinline__ double df_to_double(DF v) {
   return __dadd_rn(df_widen(v.hi), df_widen(v.lo));
-}
-
-// df64 -> double in integer instructions, within one unit in the last place
-// of the correctly rounded sum: hi's significand as a 53-bit integer plus
-// or minus lo's, aligned to it (lo's bits below double precision are cut),
-// renormalised by at most one place.  Pairs whose lo is not at least four
-// times smaller than hi, and zero, denormal or non-finite hi, take the FP64
-// add (rare in a sweep, whose pairs come from TwoSum).
-__device__ __forceinline__ double df_to_double_int(DF v) {
-  const unsigned uh = __float_as_uint(v.hi), ul = __float_as_uint(v.lo);
-  const int eh = (int)((uh >> 23) & 0xffu), el = (int)((ul >> 23) & 0xffu);
-  const int d = eh - el;
-  if (eh == 0 || eh == 0xff || (el != 0 && d < 2)) return df_to_double(v);
-  unsigned long long s = (unsigned long long)((uh & 0x7fffffu) | 0x800000u) << 29;
-  if (el != 0) {
-    const unsigned ml = (ul & 0x7fffffu) | 0x800000u;
-    const unsigned long long lm = (d <= 29) ? ((unsigned long long)ml << (29 - d))
-                                            : ((d < 61) ? (unsigned long long)(ml >> (d - 29)) : 0ULL);
-    s = ((uh ^ ul) >> 31) ? s - lm : s + lm;
-  }
-  unsigned long long e = (unsigned long long)(eh + 896);
-  if (s >> 53) {
-    s >>= 1;
-    e += 1;
-  } else if (!(s >> 52)) {
-    s <<= 1;
-    e -= 1;
-  }
-  return __longlong_as_double(
-      (long long)(((unsigned long long)(uh & 0x80000000u) << 32) | (e << 52) | (s & 0xfffffffffffffULL)));
 }
 
 // double -> df64 with FP64 instructions (exact split of the leading 48 bits;

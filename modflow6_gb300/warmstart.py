@@ -8,18 +8,22 @@ cell's K, the previous heads, the previous step's head change, the well
 rates and the boundary mask.  The
 prediction is only an initial guess: PCG + ILU0 still runs to the same
 INNER_DVCLOSE / INNER_RCLOSE closure, so the plain solver stays the judge.
-The first iterate is the point of the line from the previous heads through
-the guess that is closest to the solution in the energy norm of the step's
-first system (one SpMV and two dot products on the device), so a noisy guess
-is shrunk toward the previous heads instead of taken whole.  The guessed step
-may spend at most the inner iterations the plain solver took on the previous
-step; past that the guess is dropped and the step is solved from the
-previous heads (gbsln_timestep_warm).
+The first iterate is the point of the plane through the previous heads,
+spanned by the last step's head change and the network's predicted change,
+that is closest to the solution in the energy norm of the step's first
+system (one SpMV and five dot products on the device).  A transient step's
+change is close to a multiple of the last one once the first steps have
+passed, and the projection takes that multiple; the network's direction adds
+what the last change lacks (the first steps, new stresses), and a noisy
+prediction is shrunk instead of taken whole.  The warm step may spend at
+most the inner iterations the plain solver took on the previous step; past
+that it is solved again from the previous heads (gbsln_timestep_warm).
 
 `Graph.features` builds the 16 input features of the cells, `generate` the
 training samples (heads from the plain solver), `WarmStartNet` wraps the C
 ABI, `train` runs Adam on the GPU and `evaluate` compares inner iterations
-with and without the network on held-out models.
+from the previous heads, from the last change alone and with the network on
+held-out models.
 """
 from __future__ import annotations
 
@@ -236,13 +240,15 @@ class WarmStartNet:
 
 
 def train(net: WarmStartNet, data, dh_scale: float, epochs: int = 4,
-          lr: float = 1e-3, loss: str = "energy", mse_weight: float = 0.05) -> list[float]:
+          lr: float = 1e-3, loss: str = "mse", mse_weight: float = 0.05) -> list[float]:
     """Adam over every sample of every model, `epochs` times, the learning
-    rate halved each epoch; mean loss per epoch.  The default loss is the
-    relative energy error of the predicted change (gbmpnn_set_loss), the
-    error a conjugate-gradient solve from the guess has to remove: a
-    pointwise squared error lets through high-frequency noise that is cheap
-    in that norm's eyes to the network and expensive to the solver."""
+    rate halved each epoch; mean loss per epoch.  loss "mse" (the default)
+    is the squared error in network units; "energy" the relative energy
+    error of the predicted change (gbmpnn_set_loss), the error a
+    conjugate-gradient solve started from the guess has to remove.  The warm
+    step projects the guess in that norm anyway (gbsln_timestep_warm), so
+    only the direction of the prediction matters there, and the squared
+    error has proven the better teacher of directions."""
     net.dh_scale = dh_scale
     # predictions are bounded by the largest head change seen in training,
     # with a 25 % margin in metres (not in the asinh units, where the same
@@ -287,13 +293,15 @@ def warm_guess(sol: GwfSolution, net: WarmStartNet, g: Graph, guess, first: bool
 
 
 def timestep_warm(sol: GwfSolution, kper: int, kstp: int, delt: float, guess, inner_cap: int):
-    """gbsln_timestep_warm: the step from the guess, dropped in favour of the
-    previous heads once it has spent inner_cap inner iterations without
-    closing.  Returns (stats, fell_back)."""
+    """gbsln_timestep_warm: the step from the energy projection of the
+    previous heads onto the plane of the last step's change and the guess's
+    (guess None: the last change alone), dropped in favour of the previous
+    heads once it has spent inner_cap inner iterations without closing.
+    Returns (stats, fell_back)."""
     lib = _lib.load()
     st = _lib.GbslnStats()
-    rc = lib.gbsln_timestep_warm(sol._h, kper, kstp, delt, C.c_void_p(guess.data_ptr()),
-                                 int(inner_cap), C.byref(st))
+    gp = C.c_void_p(guess.data_ptr()) if guess is not None else None
+    rc = lib.gbsln_timestep_warm(sol._h, kper, kstp, delt, gp, int(inner_cap), C.byref(st))
     if rc < 0:
         raise _lib.GbimsError(rc, lib.gbsln_last_error(sol._h).decode())
     return {f: getattr(st, f) for f, _ in st._fields_}, rc == _lib.GBIMS_WARN_FALLBACK
@@ -301,30 +309,32 @@ def timestep_warm(sol: GwfSolution, kper: int, kstp: int, delt: float, guess, in
 
 def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0,
              delt: float = C5_DELT) -> dict:
-    """Held-out models, solved twice to the same closure: every step from the
-    previous heads (the plain solver), and from the network's guess with the
-    fallback rule (gbsln_timestep_warm: the guessed step may spend at most
-    the inner iterations the plain solver took on the previous step; past
-    that the guess is dropped and the step solved from the previous heads,
-    those iterations counted too).  The guess is built, evaluated and used on
-    the device with no host round trip in between.  Reported: inner
-    iterations and device time of both paths (the warm path's time includes
-    inference and any fallbacks), the steps that fell back, the line-search
-    factors, the RMS and maximum error of the guess, of the first iterate
-    and of the previous heads against the converged heads, and the energy
-    errors e'(-A)e of the guess and of the first iterate relative to that of
-    the previous heads (A the step's matrix)."""
+    """Held-out models, each solved three times to the same closure: every
+    step from the previous heads (the plain solver, as MODFLOW 6 does); from
+    the energy projection onto the last step's change alone ("extrap", no
+    network); and from the projection onto the last change and the
+    network's predicted change ("warm").  Both projected paths keep the
+    fallback rule (gbsln_timestep_warm: at most the inner iterations the
+    plain solver took on the previous step, then the step again from the
+    previous heads, those iterations counted too).  The guess is built,
+    evaluated and used on the device with no host round trip in between.
+    Reported: inner iterations and device time of the three paths (the warm
+    path's time includes inference), fallbacks, the projection factors, the
+    energy errors e'(-A)e of each path's first iterate relative to that of
+    the previous heads (A the step's matrix), and the RMS and maximum error
+    of the raw network guess and of the previous heads against the converged
+    heads."""
     import torch
 
-    it_prev, it_warm, fell = [], [], 0
-    rms_g, rms_p, rms_0, max_g, max_p, alphas = [], [], [], [], [], []
-    en_g, en_0 = [], []   # energy errors relative to the previous heads'
-    ms_prev, ms_warm, ms_net = 0.0, 0.0, 0.0
+    it_prev, it_ext, it_warm, fell = [], [], [], 0
+    rms_g, rms_p, max_g, max_p = [], [], [], []
+    en_ext, en_warm, a_prev, a_net = [], [], [], []
+    ms_prev, ms_ext, ms_warm, ms_net = 0.0, 0.0, 0.0, 0.0
     converged = True
     for s in seeds:
         m = c5_model(s, scale)
         g = Graph(m)
-        base, warm = new_solution(m), new_solution(m)
+        base, ext, warm = new_solution(m), new_solution(m), new_solution(m)
         amat, _ = base.formulate(delt, hold=m.strt)
         d_amat = torch.from_numpy(amat).cuda()
         net.set_graph(d_amat)
@@ -338,50 +348,67 @@ def evaluate(net: WarmStartNet, seeds, steps: int = C5_STEPS, scale: float = 1.0
 
         nact = float(g.active64.sum().item())
         guess = torch.empty(m.nodes, dtype=torch.float64, device="cuda")
-        cap_unbounded = 10 ** 9
         last_plain = None
+        prev_w = prev_e = None   # the last step's change on each projected path
         for kstp in range(1, steps + 1):
             st_b = base.timestep(1, kstp, delt)
-            h_prev = torch.from_numpy(warm.heads).cuda()
-            ms_net += warm_guess(warm, net, g, guess, first=(kstp == 1))
-            cap = cap_unbounded if last_plain is None else max(1, last_plain)
-            st_w, fb = timestep_warm(warm, 1, kstp, delt, guess, cap)
-            fell += int(fb)
+            cap = 10 ** 9 if last_plain is None else max(1, last_plain)
             last_plain = st_b["inner_total"]
-            h_true = torch.from_numpy(warm.heads).cuda()
-            eg = (guess - h_true) * g.active64
-            ep = (h_prev - h_true) * g.active64
-            e0 = ep + st_w["guess_alpha"] * (eg - ep)   # the first iterate's error
-            alphas.append(st_w["guess_alpha"])
+            # extrapolation only
+            he0 = torch.from_numpy(ext.heads).cuda()
+            st_e, fb_e = timestep_warm(ext, 1, kstp, delt, None, cap)
+            he1 = torch.from_numpy(ext.heads).cuda()
+            # network + extrapolation
+            hw0 = torch.from_numpy(warm.heads).cuda()
+            ms_net += warm_guess(warm, net, g, guess, first=(kstp == 1))
+            st_w, fb_w = timestep_warm(warm, 1, kstp, delt, guess, cap)
+            hw1 = torch.from_numpy(warm.heads).cuda()
+            fell += int(fb_e) + int(fb_w)
+            # first-iterate errors against each path's own converged heads
+            act = g.active64
+            ep_w = (hw0 - hw1) * act
+            eg = (guess - hw1) * act
+            d1w = prev_w if prev_w is not None else torch.zeros_like(ep_w)
+            e0_w = ep_w + st_w["prev_alpha"] * d1w + st_w["guess_alpha"] * (eg - ep_w)
+            ep_e = (he0 - he1) * act
+            d1e = prev_e if prev_e is not None else torch.zeros_like(ep_e)
+            e0_e = ep_e + st_e["prev_alpha"] * d1e
+            Ew, Ee = energy(ep_w), energy(ep_e)
+            if Ew > 0.0 and Ee > 0.0:
+                en_warm.append(energy(e0_w) / Ew)
+                en_ext.append(energy(e0_e) / Ee)
+            prev_w, prev_e = (hw1 - hw0) * act, (he1 - he0) * act
+            a_prev.append(st_w["prev_alpha"])
+            a_net.append(st_w["guess_alpha"])
             rms_g.append(float(torch.sqrt((eg * eg).sum() / nact).item()))
-            rms_p.append(float(torch.sqrt((ep * ep).sum() / nact).item()))
-            rms_0.append(float(torch.sqrt((e0 * e0).sum() / nact).item()))
-            ep_en = energy(ep)
-            if ep_en > 0.0:
-                en_g.append(energy(eg) / ep_en)
-                en_0.append(energy(e0) / ep_en)
+            rms_p.append(float(torch.sqrt((ep_w * ep_w).sum() / nact).item()))
             max_g.append(float(eg.abs().max().item()))
-            max_p.append(float(ep.abs().max().item()))
+            max_p.append(float(ep_w.abs().max().item()))
             it_prev.append(st_b["inner_total"])
+            it_ext.append(st_e["inner_total"])
             it_warm.append(st_w["inner_total"])
             ms_prev += st_b["total_ms"]
+            ms_ext += st_e["total_ms"]
             ms_warm += st_w["total_ms"]
-            converged = converged and st_b["converged"] == 1 and st_w["converged"] == 1
-        base.close()
-        warm.close()
-    ip, iw = np.array(it_prev), np.array(it_warm)
+            converged = converged and all(x["converged"] == 1 for x in (st_b, st_e, st_w))
+        for sol in (base, ext, warm):
+            sol.close()
+    ip, ie, iw = np.array(it_prev), np.array(it_ext), np.array(it_warm)
     return {"models": len(seeds), "steps": int(ip.size), "all_converged": converged,
-            "inner_prev_heads": int(ip.sum()), "inner_warm": int(iw.sum()),
-            "fallbacks": fell,
-            "steps_guess_better": int((iw < ip).sum()), "steps_guess_worse": int((iw > ip).sum()),
+            "inner_prev_heads": int(ip.sum()), "inner_extrap": int(ie.sum()),
+            "inner_warm": int(iw.sum()), "fallbacks": fell,
+            "steps_warm_better": int((iw < ip).sum()), "steps_warm_worse": int((iw > ip).sum()),
             "iteration_ratio": float(iw.sum() / max(1, ip.sum())),
-            "solve_ms_prev_heads": ms_prev, "solve_ms_warm": ms_warm, "inference_ms": ms_net,
-            "inference_ms_per_guess": ms_net / max(1, ip.size),
+            "iteration_ratio_extrap": float(ie.sum() / max(1, ip.sum())),
+            "solve_ms_prev_heads": ms_prev, "solve_ms_extrap": ms_ext, "solve_ms_warm": ms_warm,
+            "inference_ms": ms_net, "inference_ms_per_guess": ms_net / max(1, ip.size),
             "time_ratio": (ms_warm + ms_net) / max(1e-9, ms_prev),
+            "time_ratio_extrap": ms_ext / max(1e-9, ms_prev),
+            "energy_err_warm_rel": float(np.mean(en_warm)) if en_warm else None,
+            "energy_err_extrap_rel": float(np.mean(en_ext)) if en_ext else None,
+            "energy_err_warm_first_step_rel": en_warm[0] if en_warm else None,
+            "alpha_prev_mean": float(np.mean(a_prev)), "alpha_net_mean": float(np.mean(a_net)),
             "rms_err_guess": float(np.mean(rms_g)), "rms_err_prev_heads": float(np.mean(rms_p)),
-            "rms_err_first_iterate": float(np.mean(rms_0)), "alpha_mean": float(np.mean(alphas)),
-            "energy_err_guess_rel": float(np.mean(en_g)) if en_g else None,
-            "energy_err_first_iterate_rel": float(np.mean(en_0)) if en_0 else None,
-            "alpha_min": float(np.min(alphas)), "alpha_max": float(np.max(alphas)),
-            "inner_per_step_prev_heads": ip.tolist(), "inner_per_step_warm": iw.tolist(),
-            "max_err_guess": float(np.max(max_g)), "max_err_prev_heads": float(np.max(max_p))}
+            "max_err_guess": float(np.max(max_g)), "max_err_prev_heads": float(np.max(max_p)),
+            "inner_per_step_prev_heads": ip.tolist(), "inner_per_step_extrap": ie.tolist(),
+            "inner_per_step_warm": iw.tolist()}

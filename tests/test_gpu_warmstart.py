@@ -83,15 +83,18 @@ def test_training_lowers_loss_and_improves_the_initial_guess(gblib):
     assert hist[-1] < 0.5 * hist[0], hist
     res = evaluate(net, [900, 901], steps=10, scale=0.25)
     print(res)
-    # every step reaches the same closure from either start; the first
-    # iterate (previous heads + the line-searched network change) is clearly
-    # closer to the converged heads than the previous heads in the energy
-    # norm of the step's matrix, the error a CG solve has to remove; and the
-    # warm path, with any fallbacks and their wasted iterations counted,
-    # takes strictly fewer inner iterations
+    # every step of the three paths reaches the same closure
     assert res["all_converged"], res
-    assert res["energy_err_first_iterate_rel"] < 0.8, res
+    # the warm path takes strictly fewer inner iterations than MODFLOW 6's
+    # start from the previous heads, its fallbacks and their wasted
+    # iterations counted
     assert res["inner_warm"] < res["inner_prev_heads"], res
+    # what the network adds to the last step's change: on the first step
+    # there is no last change, and the network's direction alone removes a
+    # clear part of the energy error of the previous heads; over all steps
+    # the plane is no worse than the last change alone
+    assert res["energy_err_warm_first_step_rel"] < 0.97, res
+    assert res["energy_err_warm_rel"] <= res["energy_err_extrap_rel"] + 1e-3, res
     net.close()
 
 
