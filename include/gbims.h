@@ -195,8 +195,7 @@ int gbims_time_kernels(gbims_handle *h, int reps, gbims_kernel_times *t);
 /* Autotuner (no counterpart in the reference, which has no tunable kernels):
  * on the handle's own factored system it times every wavefront tiling of
  * the structured sweeps (chunk of steps per ring buffer, ring depth,
- * neighbour-word prefetch depth, CTAs per SM, thread-block clusters whose
- * row blocks hand over through distributed shared memory), the form of the level-
+ * neighbour-word prefetch depth, CTAs per SM), the form of the level-
  * scheduled sweeps of other patterns, and the thread-block count of the
  * dot/update reductions, and keeps the fastest for the following applies.
  * The tiling does not change any cell's arithmetic; the reduction grid only
@@ -215,8 +214,6 @@ typedef struct gbims_tuning {
   double candidate_ms[16];          /* one ILU0 application per tiling */
   double precond_ms;                /* of the chosen tiling */
   double vector_ms;                 /* dot + update at the chosen grid */
-  int sweep_cluster;                /* CTAs per thread-block cluster of the chosen tiling
-                                       (1: none); candidate_ms is -1 for tilings not timed */
 } gbims_tuning;
 int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out);
 /* Applies a tuning found earlier (sweep_config < 0, reduction_blocks <= 0 or

@@ -1154,14 +1154,11 @@ extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
     int best = 0;
     double bt = 1e300;
     for (int i = 0; i < nc; ++i) {
-      out->candidate_ms[i] = -1.0;
-      if (!dia7_cfg_ok(h->D, i)) continue;  // a cluster tiling the blocks do not allow
       h->D.cfg = i;
       const double ms = time_it([&] {
         if (!h->mixed) precond64(h, h->v_p, h->v_z);
         else precond32(h, h->f_p, h->f_z);
       });
-      if (cudaGetLastError() != cudaSuccess) continue;  // a cluster launch the GPU refused
       out->candidate_ms[i] = ms;
       if (ms < bt) {
         bt = ms;
@@ -1177,10 +1174,7 @@ extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
     h->D.cfg = best;
     out->ncandidates = nc;
     out->sweep_config = best;
-    int clu = 0;
-    dia7_cfg(best, &out->sweep_chunk, &out->sweep_ring, &out->sweep_prefetch, &out->sweep_occupancy,
-             &clu);
-    out->sweep_cluster = clu ? dia7_cluster_size(h->D) : 1;
+    dia7_cfg(best, &out->sweep_chunk, &out->sweep_ring, &out->sweep_prefetch, &out->sweep_occupancy);
     out->precond_ms = bt;
   }
   out->level_mode = -1;
@@ -1246,9 +1240,8 @@ extern "C" int gbims_set_tuning(gbims_handle *h, int sweep_config, int reduction
     h->LW.mode = level_mode;
   }
   if (sweep_config >= 0) {
-    if (!h->structured || !dia7_cfg_ok(h->D, sweep_config))
-      return fail(h, GBIMS_ERR_ARG,
-                  "sweep configuration out of range or not available (or not a structured handle)");
+    if (!h->structured || sweep_config >= dia7_num_cfgs())
+      return fail(h, GBIMS_ERR_ARG, "sweep configuration out of range (or not a structured handle)");
     h->D.cfg = sweep_config;
   }
   if (reduction_blocks > 0) {

@@ -208,12 +208,9 @@ struct Dia7 {
 constexpr int kVecPad = 256;
 void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, long long *slots);
 // The wavefront sweep configurations: chunk C, ring depth NS, prefetch PF,
-// occupancy cap OCC (0: as many CTAs per SM as fit, 2: at most two), CLU
-// (1: thread-block clusters of dia7_cluster_size CTAs).
+// occupancy cap OCC (0: as many CTAs per SM as fit, 2: at most two).
 int dia7_num_cfgs();
-void dia7_cfg(int i, int *C, int *NS, int *PF, int *OCC, int *CLU);
-int dia7_cluster_size(const Dia7 &D);
-bool dia7_cfg_ok(const Dia7 &D, int i);
+void dia7_cfg(int i, int *C, int *NS, int *PF, int *OCC);
 // Members (nlay, nrow, ncol) and their first rows -> D.geo, D.slots,
 // D.ntickets (host side; the caller uploads D.geo to D.d_geo).
 void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long long> &row0,

@@ -95,9 +95,9 @@ __device__ __forceinline__ bool mbar_test(unsigned long long *b, unsigned parity
 __device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity,
                                           volatile int *abort_flag) {
   if (mbar_test(b, parity)) return true;
-  unsigned long long t0 = gtimer();
+  unsigned long long t0 = wclock();
   while (!mbar_test(b, parity)) {
-    if (*abort_flag || gtimer() - t0 > kWaitNs) return false;
+    if (*abort_flag || wclock() - t0 > kWaitCycles) return false;
   }
   return true;
 }
@@ -112,75 +112,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
       : "memory");
 }
 
-// ---- thread-block cluster helpers (distributed shared memory) ----
-__device__ __forceinline__ unsigned cluster_rank() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ unsigned cluster_size() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
-  return r;
-}
-// every thread of every CTA of the cluster; release/acquire at cluster scope
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release;\n barrier.cluster.wait.acquire;" ::: "memory");
-}
-// the shared::cluster address of this CTA's shared variable at `p` in CTA `rank`
-__device__ __forceinline__ unsigned cluster_map(const void *p, unsigned rank) {
-  unsigned r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ unsigned long long ld_cluster_u64(unsigned addr) {
-  unsigned long long v;
-  asm volatile("ld.shared::cluster.u64 %0, [%1];" : "=l"(v) : "r"(addr) : "memory");
-  return v;
-}
-// remote arrive (release at cluster scope) on an mbarrier of another CTA
-__device__ __forceinline__ void mbar_arrive_remote(unsigned addr) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(addr) : "memory");
-}
-// bounded wait with acquire at cluster scope (data written by other CTAs)
-__device__ __forceinline__ bool mbar_test_cluster(unsigned long long *b, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(b)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ bool mbar_wait_cluster(unsigned long long *b, unsigned parity,
-                                                  volatile int *abort_flag) {
-  if (mbar_test_cluster(b, parity)) return true;
-  unsigned long long t0 = gtimer();
-  while (!mbar_test_cluster(b, parity)) {
-    if (*abort_flag || gtimer() - t0 > kWaitNs) return false;
-  }
-  return true;
-}
-// asynchronous store into another CTA's shared memory whose bytes complete
-// the transaction count of an mbarrier there
-__device__ __forceinline__ void st_async(unsigned addr, double v, unsigned bar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(addr),
-               "l"(__double_as_longlong(v)), "r"(bar)
-               : "memory");
-}
-__device__ __forceinline__ void st_async(unsigned addr, float v, unsigned bar) {
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(addr),
-               "r"(__float_as_uint(v)), "r"(bar)
-               : "memory");
-}
-__device__ __forceinline__ void st_async(unsigned addr, DF v, unsigned bar) {
-  const unsigned long long bits =
-      ((unsigned long long)__float_as_uint(v.lo) << 32) | __float_as_uint(v.hi);
-  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(addr),
-               "l"(bits), "r"(bar)
-               : "memory");
-}
 
 // The arithmetic of a sweep: T is the element type of the tiles, the result
 // words and the chain; V the type of the natural-order vectors r and z.
@@ -272,31 +203,16 @@ __device__ __forceinline__ bool ll_poll(const LLWord<T> *q, long long stride, un
       if ((want >> t) & 1u)
         if (ll_get(q + t * stride, ep, v[t])) want &= ~(1u << t);
     if (!__any_sync(0xffffffffu, want != 0)) return true;
-    if (t0 == 0) t0 = gtimer();
-    if (__any_sync(0xffffffffu, *abort_flag != 0 || gtimer() - t0 > kWaitNs)) return false;
+    if (t0 == 0) t0 = wclock();
+    if (__any_sync(0xffffffffu, *abort_flag != 0 || wclock() - t0 > kWaitCycles)) return false;
   }
 }
 
-// Thread-block cluster hand-off (CLU): the grid is launched in clusters of
-// `cs` CTAs (cs divides the blocks per layer), the consecutive blocks of one
-// layer in wavefront order.  The previous CTA of the cluster sends its last
-// line to the next one step by step with st.async into a ring of R chunks in
-// the receiver's shared memory; each slot has an mbarrier whose transaction
-// count the stores complete ("yfull", armed by the receiver) and one in the
-// sender for the slot's release ("yfree", arrived remotely by the receiver).
-// The first CTA of a cluster takes its neighbour line from global memory as
-// before.  A cluster takes cs tickets at once, so the tickets (and with them
-// the epochs) of a launch are those of the same grid without clusters, and
-// the cluster's CTAs agree on its ticket and on whether to sweep at all;
-// no CTA leaves before the whole cluster has finished (a final cluster
-// barrier), so nothing writes into the shared memory of a CTA that is gone.
-
 // DIR = +1 forward, -1 backward.  A CTA is one block: 32 lines of one layer.
 // PF: chunks of neighbour words whose loads are in flight ahead of use.
-template <typename T, int S, int C, int NS, int DIR, int PF, bool CLU>
+template <typename T, int S, int C, int NS, int DIR, int PF>
 __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   constexpr int W = 32;
-  constexpr int R = 128 / C;  // cluster ring depth, chunks
   using St = Stage<T, C, DIR>;
   using E = Elem<T>;
   using V = typename E::V;
@@ -305,24 +221,24 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   unsigned long long *full = reinterpret_cast<unsigned long long *>(smem_raw + NS * sizeof(St));
   unsigned long long *empty = full + NS;
   unsigned long long *prep = full + 2 * NS;
-  unsigned long long *yfull = full + 3 * NS;  // CLU: R slots, receiver side
-  unsigned long long *yfree = yfull + R;      // CLU: R slots, sender side
-  T *ynr = reinterpret_cast<T *>(yfree + R);  // CLU: R x C values
-  __shared__ int s_id, s_abort, s_rot, s_m, s_skip;
+  __shared__ int s_id, s_abort, s_rot, s_m;
   __shared__ unsigned s_ep;
-  __shared__ unsigned long long s_tk;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const unsigned crank = CLU ? cluster_rank() : 0u;
-  const unsigned csize = CLU ? cluster_size() : 1u;
   if (threadIdx.x == 0) {
     // Every CTA of a launch takes its ticket, also one that returns at once,
     // so that launch e (from 0) owns tickets [e*grid, (e+1)*grid): the local
     // ticket orders the CTAs, the launch number is the epoch of its words.
-    // A cluster's first CTA takes the tickets of the whole cluster.
-    if (!CLU || crank == 0) {
-      const unsigned long long tk = atomicAdd(p.ticket, (unsigned long long)csize);
-      s_tk = tk | ((p.ctl && p.ctl->done) ? (1ULL << 63) : 0ULL);
+    const unsigned long long tk = atomicAdd(p.ticket, 1ULL);
+    s_id = (int)(tk % gridDim.x);
+    s_ep = (unsigned)(tk / gridDim.x) + 1u;
+    // the member this ticket belongs to (members own contiguous tickets)
+    int lo = 0, hi = p.nm - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (p.geo[mid].ticket0 <= s_id) lo = mid;
+      else hi = mid - 1;
     }
+    s_m = lo;
     s_abort = 0;
     // Place the roles on the SM sub-partitions (each has its own FP64
     // pipe; warp w of the CTA is taken to sit on sub-partition
@@ -337,53 +253,25 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     for (int s = 0; s < NS; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
-      // pre-compute warp + edge warp; a cluster's later CTAs get their
-      // neighbour line from the cluster, without the edge warp
-      mbar_init(&prep[s], (CLU && crank > 0) ? 1 : 2);
-    }
-    if constexpr (CLU) {
-      for (int s = 0; s < R; ++s) {
-        mbar_init(&yfull[s], 1);
-        mbar_init(&yfree[s], 1);
-      }
+      mbar_init(&prep[s], 2);  // pre-compute warp + edge warp
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if constexpr (CLU) cluster_sync();  // barriers of every CTA ready, rank 0's ticket written
-  if (threadIdx.x == 0) {
-    const unsigned long long t = CLU ? ld_cluster_u64(cluster_map(&s_tk, 0)) : s_tk;
-    const unsigned long long tk = t & ~(1ULL << 63);
-    s_id = (int)(tk % gridDim.x);
-    s_ep = (unsigned)(tk / gridDim.x) + 1u;
-    // the member this ticket belongs to (members own contiguous tickets)
-    int lo = 0, hi = p.nm - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (p.geo[mid].ticket0 <= s_id) lo = mid;
-      else hi = mid - 1;
-    }
-    s_m = lo;
-    // a member of a batch that has reached its closure is not swept; its
-    // CTAs only depend on one another, so none of them waits for it
-    s_skip = ((t >> 63) != 0ULL || (p.mctl && p.mctl[lo].done)) ? 1 : 0;
-  }
-  __syncthreads();
+  if (p.ctl && p.ctl->done) return;
+  // a member of a batch that has reached its closure is not swept; its CTAs
+  // only depend on one another, so none of them waits for it
+  if (p.mctl && p.mctl[s_m].done) return;
   const int role = (warp - s_rot) & 3;
   const int id = s_id;
   const unsigned ep = s_ep;
   const Dia7Geo geo = p.geo[s_m];
-  // position of the block in the sweep order of its layer: clusters own cs
-  // consecutive positions
-  const int lid = CLU ? (id - geo.ticket0) / (int)csize : id - geo.ticket0;
+  const int lid = id - geo.ticket0;
   const int nlay = geo.nlay, nrow = geo.nrow, nb = geo.nb, G = geo.G;
   const int k = (DIR > 0) ? lid % nlay : nlay - 1 - (lid % nlay);
-  const int pos = CLU ? (lid / nlay) * (int)csize + (int)crank : lid / nlay;
-  const int b = (DIR > 0) ? pos : nb - 1 - pos;
+  const int b = (DIR > 0) ? lid / nlay : nb - 1 - lid / nlay;
   const int nch = G / C;
   const bool has_blk = (DIR > 0) ? (b > 0) : (b < nb - 1);
-  const bool dsm_in = CLU && crank > 0;             // neighbour line from the cluster
-  const bool dsm_out = CLU && crank + 1 < csize;    // last line to the cluster
   const bool has_lay = (DIR > 0) ? (k > 0) : (k < nlay - 1);
   const long long slot0 = geo.slot0;
   auto tile = [&](int kk, int bb) -> long long { return slot0 + ((long long)kk * nb + bb) * G * W; };
@@ -397,8 +285,6 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     }
   };
 
-  // the work of the warp's role (its returns end the role, not the kernel)
-  auto body = [&]() {
   if (role == kRolePre) {
     // ---------------- pre-compute warp ----------------
     // The terms of a step that do not depend on the wavefront: forward
@@ -500,9 +386,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     // ---------------- edge warp ----------------
     // The neighbour block's last line: lane t < C polls the word of step t
     // of the chunk (the neighbour's lane 31 reaches column g at its step
-    // g + S*31) and leaves it in the stage's `yn`.  Not used by a cluster's
-    // later CTAs, which receive the line from the CTA before them.
-    if (dsm_in) return;
+    // g + S*31) and leaves it in the stage's `yn`.
     const LLWord<T> *ysrc = has_blk ? out + tile(k, b - DIR) + (W - 1) : nullptr;
     // lane t < C: the word of step t of a chunk; loads PF chunks ahead
     auto yrow_of = [&](int c) { return c * C + S * (W - 1) + lane; };
@@ -601,9 +485,9 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       // every copy issued has landed before this warp, and so the CTA, ends
       // (the other warps may have left early on an abort)
       for (int c = max(0, issued - NS); c < issued; ++c) {
-        unsigned long long t0 = gtimer();
+        unsigned long long t0 = wclock();
         while (!mbar_test(&full[c % NS], (c / NS) & 1))
-          if (gtimer() - t0 > kWaitNs) break;
+          if (wclock() - t0 > kWaitCycles) break;
       }
     }
     return;
@@ -615,31 +499,12 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   // the chunk; each result goes straight out as a word of this epoch.
   LLWord<T> *outt = out + tile(k, b) + lane;
   T h1 = E::zero(), h2 = E::zero();
-  // cluster hand-off: consumer steps g' receive the sender's step g' + S*31
-  // (the sender's steps end at G-1), chunk cc gets ycount(cc) of its values
-  const int gvalid = G - S * (W - 1);
-  const int nchw = (gvalid + C - 1) / C;
-  auto ycount = [&](int cc) { return min(C, max(0, gvalid - cc * C)); };
-  unsigned r_ynr = 0, r_yfull = 0, r_yfree = 0;
-  if constexpr (CLU) {
-    if (dsm_out) {
-      r_ynr = cluster_map(ynr, crank + 1);
-      r_yfull = cluster_map(yfull, crank + 1);
-    }
-    if (dsm_in) {
-      r_yfree = cluster_map(yfree, crank - 1);
-      if (lane == 0)
-        for (int q = 0; q < R && q < nch; ++q) mbar_expect_tx(&yfull[q], ycount(q) * (unsigned)sizeof(T));
-    }
-  }
   for (int c = 0; c < nch; ++c) {
     const int s = c % NS;
-    bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort) &&
-               mbar_wait(&prep[s], (c / NS) & 1, v_abort);
-    if constexpr (CLU)
-      if (dsm_in) got = got && mbar_wait_cluster(&yfull[c % R], (c / R) & 1, v_abort);
+    const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort) &&
+                     mbar_wait(&prep[s], (c / NS) & 1, v_abort);
     if (!__all_sync(0xffffffffu, got)) {
-      fail();
+      if (lane == 0) *v_abort = 1;
       return;
     }
     St &st = stg[s];
@@ -651,12 +516,8 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       ra[t] = st.a[t * W + lane];  // pre-computed r - Lz*zn (backward: dinv*y - Uz'*zn)
       rb[t] = st.b[t * W + lane];
       rx[t] = st.x[t * W + lane];
-      if constexpr (CLU)
-        ryn[t] = dsm_in ? ((g0 + t < gvalid) ? ynr[(c % R) * C + t] : E::zero()) : st.yn[t];
-      else
-        ryn[t] = st.yn[t];
+      ryn[t] = st.yn[t];
     }
-    bool bad = false;
 #pragma unroll
     for (int t = 0; t < C; ++t) {
       T yv = E::shfl_up((S == 1) ? h1 : h2, 1);
@@ -668,20 +529,6 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       T tv = E::fms(rx[t], h1, ra[t]);
       tv = E::fms(rb[t], yv, tv);
       ll_put(outt + (long long)(g0 + t) * W, tv, ep);
-      if constexpr (CLU) {
-        // the last line to the next CTA of the cluster, step by step
-        if (dsm_out && lane == W - 1) {
-          const int gp = g0 + t - S * (W - 1);
-          if (gp >= 0) {
-            const int cc = gp / C, tt = gp - cc * C;
-            if (tt == 0 && cc >= R && !mbar_wait_cluster(&yfree[cc % R], ((cc / R) - 1) & 1, v_abort))
-              bad = true;
-            if (!bad)
-              st_async(r_ynr + (unsigned)(((cc % R) * C + tt) * sizeof(T)), tv,
-                       r_yfull + (unsigned)((cc % R) * sizeof(unsigned long long)));
-          }
-        }
-      }
       if constexpr (DIR < 0) {
         // the result in natural order (df64: widened and added in FP64, off
         // the chain, on this sub-partition's otherwise idle FP64 pipe)
@@ -691,28 +538,10 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       h2 = h1;
       h1 = tv;
     }
-    if (__any_sync(0xffffffffu, bad)) {
-      fail();
-      return;
-    }
-    // the input buffer goes back to the copy and edge warps; in a cluster,
-    // the ring slot is armed for its next chunk and released to the sender
+    // the input buffer goes back to the copy and edge warps
     __syncwarp();
-    if (lane == 0) {
-      mbar_arrive(&empty[s]);
-      if constexpr (CLU) {
-        if (dsm_in) {
-          if (c + R < nch) mbar_expect_tx(&yfull[c % R], ycount(c + R) * (unsigned)sizeof(T));
-          if (c + R < nchw) mbar_arrive_remote(r_yfree + (unsigned)((c % R) * sizeof(unsigned long long)));
-        }
-      }
-    }
+    if (lane == 0) mbar_arrive(&empty[s]);
   }
-  };  // body
-
-  if (!s_skip) body();
-  // no CTA of a cluster leaves while another may still write to it
-  if constexpr (CLU) cluster_sync();
 }
 
 // APC/JAPC -> skewed tiles.  Forward tiles hold Lz, Ly, Lx of the cell that
@@ -820,27 +649,21 @@ constexpr int kSOf<DF> = 1;
 static_assert(GB_DIA32_S == 1 || GB_DIA32_S == 2, "lane skew 1 or 2");
 // OCC 2: the CTA asks for enough shared memory that at most two share an
 // SM, so that each compute warp has a sub-partition's FP64 pipe to itself.
-// CLU 1: launched in thread-block clusters (row blocks hand over through
-// distributed shared memory) where the blocks per layer allow it.
 struct SweepCfg {
-  int C, NS, PF, OCC, CLU;
+  int C, NS, PF, OCC;
 };
-constexpr SweepCfg kSweepCfgs[] = {
-    {8, 4, 1, 0, 0},  {8, 4, 2, 0, 0},  {4, 8, 1, 0, 0},  {4, 8, 2, 0, 0},
-    {16, 2, 1, 0, 0}, {16, 2, 2, 0, 0}, {8, 4, 1, 2, 0},  {8, 4, 2, 2, 0},
-    {4, 8, 1, 2, 0},  {4, 8, 2, 2, 0},  {16, 2, 1, 2, 0}, {16, 2, 2, 2, 0},
-    {8, 4, 1, 0, 1},  {8, 4, 2, 0, 1},  {16, 2, 1, 0, 1}, {4, 8, 2, 0, 1}};
+constexpr SweepCfg kSweepCfgs[] = {{8, 4, 1, 0},  {8, 4, 2, 0},  {4, 8, 1, 0},  {4, 8, 2, 0},
+                                   {16, 2, 1, 0}, {16, 2, 2, 0}, {8, 4, 1, 2},  {8, 4, 2, 2},
+                                   {4, 8, 1, 2},  {4, 8, 2, 2},  {16, 2, 1, 2}, {16, 2, 2, 2}};
 constexpr size_t kOcc2Smem = 80 * 1024;
 constexpr int kNumSweepCfgs = sizeof(kSweepCfgs) / sizeof(kSweepCfgs[0]);
 
-template <typename T, int C, int NS, int DIR, bool CLU>
+template <typename T, int C, int NS, int DIR>
 constexpr size_t stage_bytes() {
-  return NS * sizeof(Stage<T, C, DIR>) + 3 * NS * sizeof(unsigned long long) +
-         (CLU ? (2 * (128 / C) * sizeof(unsigned long long) + (128 / C) * C * sizeof(T)) : 0);
+  return NS * sizeof(Stage<T, C, DIR>) + 3 * NS * sizeof(unsigned long long);
 }
-static_assert(stage_bytes<double, 16, 2, -1, true>() <= 72 * 1024 &&
-                  stage_bytes<double, 4, 8, -1, true>() <= 72 * 1024 &&
-                  stage_bytes<double, 8, 4, -1, true>() <= 72 * 1024,
+static_assert(stage_bytes<double, 16, 2, -1>() <= 72 * 1024 && stage_bytes<double, 4, 8, -1>() <= 72 * 1024 &&
+                  stage_bytes<double, 8, 4, -1>() <= 72 * 1024,
               "three sweep CTAs per SM");
 
 }  // namespace
@@ -905,25 +728,11 @@ void dia7_geometry(int nlay, int nrow, int ncol, bool fp32, int *nb, int *G, lon
 }
 
 int dia7_num_cfgs() { return kNumSweepCfgs; }
-void dia7_cfg(int i, int *C, int *NS, int *PF, int *OCC, int *CLU) {
+void dia7_cfg(int i, int *C, int *NS, int *PF, int *OCC) {
   *C = kSweepCfgs[i].C;
   *NS = kSweepCfgs[i].NS;
   *PF = kSweepCfgs[i].PF;
   *OCC = kSweepCfgs[i].OCC;
-  if (CLU) *CLU = kSweepCfgs[i].CLU;
-}
-
-// CTAs per cluster for the cluster tilings: the largest of 8, 4, 2 that
-// divides the blocks per layer of a single model; 1 (no cluster tiling)
-// for batches and for block counts none of them divides.
-int dia7_cluster_size(const Dia7 &D) {
-  if (D.nm != 1) return 1;
-  for (int c = 8; c >= 2; c >>= 1)
-    if (D.nb % c == 0) return c;
-  return 1;
-}
-bool dia7_cfg_ok(const Dia7 &D, int i) {
-  return i >= 0 && i < kNumSweepCfgs && (!kSweepCfgs[i].CLU || dia7_cluster_size(D) > 1);
 }
 
 void dia7_layout(Dia7 &D, const std::vector<int> &shapes, const std::vector<long long> &row0,
@@ -997,50 +806,26 @@ int launch_dia7_extract(Dia7 &D, int n, const int *d_iapc, const int *d_japc,
   return 0;
 }
 
-// One sweep launch, in clusters of cs CTAs when CLU.
-template <typename T, int C, int NS, int DIR, int PF, bool CLU>
-static void sweep_launch(const SweepArgs<T> &a, int grid, size_t smem, int cs, cudaStream_t st) {
-  auto kern = k_dia7_sweep<T, kSOf<T>, C, NS, DIR, PF, CLU>;
-  if constexpr (!CLU) {
-    kern<<<grid, 128, smem, st>>>(a);
-  } else {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(128);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = cs;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kern, a);
-  }
-}
-
 // The two sweeps of one configuration (opting in to more than 48 KB of
 // dynamic shared memory once per kernel).
-template <typename T, int C, int NS, int PF, bool CLU>
+template <typename T, int C, int NS, int PF>
 static void sweep_pair(SweepArgs<T> a, const T *const *arr, const Dia7 &D, int occ,
                        cudaStream_t st) {
-  constexpr size_t bf = stage_bytes<T, C, NS, 1, CLU>(), bb = stage_bytes<T, C, NS, -1, CLU>();
+  constexpr size_t bf = stage_bytes<T, C, NS, 1>(), bb = stage_bytes<T, C, NS, -1>();
   static bool opted = false;
   if (!opted) {  // allow up to the two-per-SM request
-    cudaFuncSetAttribute(k_dia7_sweep<T, kSOf<T>, C, NS, 1, PF, CLU>,
+    cudaFuncSetAttribute(k_dia7_sweep<T, kSOf<T>, C, NS, 1, PF>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(bf, kOcc2Smem));
-    cudaFuncSetAttribute(k_dia7_sweep<T, kSOf<T>, C, NS, -1, PF, CLU>,
+    cudaFuncSetAttribute(k_dia7_sweep<T, kSOf<T>, C, NS, -1, PF>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(bb, kOcc2Smem));
     opted = true;
   }
   const size_t smf = (occ == 2) ? std::max(bf, kOcc2Smem) : bf;
   const size_t smb = (occ == 2) ? std::max(bb, kOcc2Smem) : bb;
-  const int cs = CLU ? dia7_cluster_size(D) : 1;
-  sweep_launch<T, C, NS, 1, PF, CLU>(a, D.ntickets, smf, cs, st);
+  k_dia7_sweep<T, kSOf<T>, C, NS, 1, PF><<<D.ntickets, 128, smf, st>>>(a);
   a.A = arr[3]; a.B = arr[4]; a.X = arr[5]; a.D = arr[6];
   a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags + 32);
-  sweep_launch<T, C, NS, -1, PF, CLU>(a, D.ntickets, smb, cs, st);
+  k_dia7_sweep<T, kSOf<T>, C, NS, -1, PF><<<D.ntickets, 128, smb, st>>>(a);
 }
 
 // One ILU0 application: the forward sweep reads r in natural order, the
@@ -1062,25 +847,14 @@ static void apply_t(const Dia7 &D, const T *const *arr, const typename Elem<T>::
   a.ctl = const_cast<Ctl *>(ctl);
   a.A = arr[0]; a.B = arr[1]; a.X = arr[2]; a.D = nullptr;
   a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags);
-  // a cluster tiling that the model's blocks do not allow runs unclustered
-  const int cfg = dia7_cfg_ok(D, D.cfg) ? D.cfg : 0;
-  const int occ = kSweepCfgs[cfg].OCC;
-  if (kSweepCfgs[cfg].CLU) {
-    switch (cfg) {
-      case 13: sweep_pair<T, 8, 4, 2, true>(a, arr, D, occ, st); break;
-      case 14: sweep_pair<T, 16, 2, 1, true>(a, arr, D, occ, st); break;
-      case 15: sweep_pair<T, 4, 8, 2, true>(a, arr, D, occ, st); break;
-      default: sweep_pair<T, 8, 4, 1, true>(a, arr, D, occ, st); break;
-    }
-    return;
-  }
-  switch (cfg % 6) {
-    case 1: sweep_pair<T, 8, 4, 2, false>(a, arr, D, occ, st); break;
-    case 2: sweep_pair<T, 4, 8, 1, false>(a, arr, D, occ, st); break;
-    case 3: sweep_pair<T, 4, 8, 2, false>(a, arr, D, occ, st); break;
-    case 4: sweep_pair<T, 16, 2, 1, false>(a, arr, D, occ, st); break;
-    case 5: sweep_pair<T, 16, 2, 2, false>(a, arr, D, occ, st); break;
-    default: sweep_pair<T, 8, 4, 1, false>(a, arr, D, occ, st); break;
+  const int occ = kSweepCfgs[D.cfg].OCC;
+  switch (D.cfg % 6) {
+    case 1: sweep_pair<T, 8, 4, 2>(a, arr, D, occ, st); break;
+    case 2: sweep_pair<T, 4, 8, 1>(a, arr, D, occ, st); break;
+    case 3: sweep_pair<T, 4, 8, 2>(a, arr, D, occ, st); break;
+    case 4: sweep_pair<T, 16, 2, 1>(a, arr, D, occ, st); break;
+    case 5: sweep_pair<T, 16, 2, 2>(a, arr, D, occ, st); break;
+    default: sweep_pair<T, 8, 4, 1>(a, arr, D, occ, st); break;
   }
 }
 

@@ -244,10 +244,10 @@ __global__ void __launch_bounds__(256) k_ilu_sweep_sf(int n, const int *__restri
           ll_take(w[q2], v);
         } else {
           const LLWord<T> *pw = out + japc[jb + q2];
-          const unsigned long long t0 = gtimer();
+          const unsigned long long t0 = wclock();
           unsigned pause = 32;
           while (!ll_get(pw, ep, v)) {
-            if ((vdone && *vdone) || gtimer() - t0 > kWaitNs) {
+            if ((vdone && *vdone) || wclock() - t0 > kWaitCycles) {
               atomicExch(err, 1);
               if (ctl) ctl->done = 1;
               return;

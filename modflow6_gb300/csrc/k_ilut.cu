@@ -8,7 +8,7 @@
 // ahead of time: every thread claims the next row from a counter and, before
 // it eliminates row jrow, waits for jrow's completion word.  Rows are claimed
 // in increasing order, so the lowest unfinished claimed row never waits on an
-// unclaimed one and every wait ends; each wait is still bounded (kWaitNs) and
+// unclaimed one and every wait ends; each wait is still bounded (kWaitCycles) and
 // gives up when the attempt is void (a pivot failed, an error was raised).
 //
 // The working row follows the reference's bookkeeping where it decides the
@@ -57,12 +57,12 @@ __device__ __forceinline__ void raise_error(IlutStatus *s, int code, int row) {
 // attempt became void or the wait ran out (then an error is raised).
 __device__ bool wait_row(const IlutDev &I, int r) {
   if (ld_acquire_u32(I.rdone + r) == I.epoch) return true;
-  const unsigned long long t0 = gtimer();
+  const unsigned long long t0 = wclock();
   for (;;) {
     __nanosleep(64);
     if (ld_acquire_u32(I.rdone + r) == I.epoch) return true;
     if (attempt_void(I.stat)) return false;
-    if (gtimer() - t0 > kWaitNs) {
+    if (wclock() - t0 > kWaitCycles) {
       raise_error(I.stat, kIlutErrWait, r);
       return false;
     }

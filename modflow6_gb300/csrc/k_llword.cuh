@@ -8,13 +8,14 @@
 
 namespace gb {
 
-constexpr unsigned long long kWaitNs = 2000000000ULL;  // 2 s per wait
+// Every spin-wait is bounded by the SM's cycle counter: 4e9 cycles, about
+// 2 s at the GB300's 2.07 GHz maximum (longer at lower clocks, never
+// unbounded).  The cycle counter is read in a few cycles; the global timer,
+// read on every turn of a wait loop, delayed each wait's exit by far more
+// than the hand-off it waited for.
+constexpr unsigned long long kWaitCycles = 4000000000ULL;
 
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
+__device__ __forceinline__ unsigned long long wclock() { return (unsigned long long)clock64(); }
 
 // One result element with its sweep epoch.  The epoch travels in the same
 // naturally aligned 8-byte access as the data it guards (FP64: both halves

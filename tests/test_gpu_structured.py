@@ -103,11 +103,11 @@ def test_structured_solve_c2_small(gblib, ilinmeth, precision):
 
 
 @pytest.mark.parametrize("precision", [_lib.GBIMS_FP64, _lib.GBIMS_MIXED])
-@pytest.mark.parametrize("shape", [(2, 65, 3), (3, 40, 41), (4, 97, 150)], ids=lambda s: "x".join(map(str, s)) if isinstance(s, tuple) else str(s))
+@pytest.mark.parametrize("shape", [(2, 65, 3), (3, 40, 41), (4, 97, 150), (2, 256, 40)], ids=lambda s: "x".join(map(str, s)) if isinstance(s, tuple) else str(s))
 def test_every_sweep_tiling_gives_the_same_result(gblib, shape, precision):
-    """The wavefront tilings (chunk, ring depth, prefetch depth) the
-    autotuner chooses among compute every cell in the same order: the
-    preconditioner output is bit for bit the same under each."""
+    """The wavefront tilings (chunk, ring depth, prefetch depth, CTAs per
+    SM) the autotuner chooses among compute every cell in the same order:
+    the preconditioner output is bit for bit the same under each."""
     import ctypes as C
     m, con, amat, rhs, x0 = dis_system(*shape)
     ims = ImsLinear(ImsLinearSettings(structure=shape, precision=precision)).imslinear_allocate(
