@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-warmstart", action="store_true")
-    ap.add_argument("--no-c3", action="store_true")
+    ap.add_argument("--no-c3", action="store_true", help="skip the C1 and C3 forms")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the library's default sweep tiling and reduction grid")
     ap.add_argument("--kernels", action="store_true",
@@ -409,6 +409,7 @@ def gb_arm(a):
         ims.imslinear_da()
     ens = None if a.no_ensemble else ensemble_form(a, lib, barrier, maxr)
     c3 = None if a.no_c3 else c3_form(a, barrier)
+    c1 = None if a.no_c3 else c1_form(a, barrier)
     ws_res = None if a.no_warmstart else warmstart_form(a)
     last = st64[-1]
     cpu = None
@@ -426,7 +427,7 @@ def gb_arm(a):
     # the details (tuning candidates, per-form breakdowns) go to stderr as one
     # line; stdout carries the contract line, with the forms' summary last
     detail = {"tuning_fp64": tune64, "mixed": mixed, "ensemble": ens, "warm_start": ws_res,
-              "c3": c3,
+              "c3": c3, "c1": c1,
               "roofline_spmv": {"kernel": "k_dia7_spmv<double>", "achieved": spmv_gbs,
                                 "frac": spmv_gbs / peak, "launch_ms": kt.spmv_ms,
                                 "traffic": traffic.get("spmv_fp64_bytes_per_launch")},
@@ -444,6 +445,10 @@ def gb_arm(a):
         if ens.get("mixed"):
             forms.update(ensemble_mixed_s=ens["mixed"]["value"],
                          ensemble_mixed_vs_fp64=ens["mixed"]["vs_fp64"])
+    if c1:
+        forms.update(c1_fp64_s=c1["fp64"]["value"], c1_inner=c1["fp64"]["inner"])
+        if "oracle" in c1:
+            forms.update(c1_oracle_s=c1["oracle"]["value"])
     if c3:
         forms.update(c3_fp64_s=c3["fp64"]["value"], c3_outer=c3["fp64"]["outer"])
         if "mixed" in c3:
@@ -559,6 +564,62 @@ def ensemble_form(a, lib, barrier, maxr) -> dict:
                          "refinement, same closure")
         mixed["vs_fp64"] = mixed["value"] / out["value"]
         out["mixed"] = mixed
+    return out
+
+
+def c1_form(a, barrier) -> dict:
+    """The 100x100x1 steady confined case (C1, the reference's CPU-runnable
+    case): one steady step to closure (INNER_DVCLOSE 1e-8, INNER_RCLOSE 1e-6,
+    PCG + ILU0) on the device, FP64 and mixed, CUDA events over 20 solves from
+    the initial heads; beside it the oracle's full solve of the same step on
+    one core (wall clock, median of 5)."""
+    import torch
+    from modflow6_gb300 import _lib
+    from modflow6_gb300.dis import make_config
+    from modflow6_gb300.ims import ImsLinearSettings
+    from modflow6_gb300.solution import GwfSolution, Nonlinear
+    from modflow6_gb300.workloads import C1_IMS, C1_OUTER
+
+    m = make_config("c1", seed=a.seed)
+    nl = Nonlinear(dvclose=C1_OUTER["dvclose"], mxiter=C1_OUTER["mxiter"])
+    out = {"workload": f"DIS {m.nlay}x{m.nrow}x{m.ncol} confined steady state", "cells": m.nodes}
+    heads = {}
+    reps = 20
+    for name, prec in (("fp64", _lib.GBIMS_FP64), ("mixed", _lib.GBIMS_MIXED)):
+        if name == "mixed" and a.no_mixed:
+            continue
+        sol = GwfSolution(m, ImsLinearSettings(precision=prec, structure=(m.nlay, m.nrow, m.ncol),
+                                               **C1_IMS), nl)
+        sol.timestep(1, 1, 1.0)  # warm-up: builds the graphs
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tot, sts = 0.0, []
+        for _ in range(reps):
+            sol.restart()
+            e0.record()
+            sts.append(sol.timestep(1, 1, 1.0))
+            e1.record()
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        heads[name] = sol.heads
+        sol.close()
+        out[name] = {"value": tot / reps / 1e3, "unit": "s", "outer": int(sts[-1]["outer"]),
+                     "inner": int(sts[-1]["inner_total"]),
+                     "converged": int(all(st["converged"] == 1 for st in sts))}
+    if "mixed" in heads:
+        out["mixed_max_head_diff_m"] = float(np.max(np.abs(heads["mixed"] - heads["fp64"])))
+    if not a.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+        ts = []
+        for _ in range(5):
+            g = oracle.Gwf(m, oracle.settings(**C1_IMS))
+            t0 = time.perf_counter()
+            so = g.timestep(kper=1, kstp=1, delt=1.0, transient=False, **C1_OUTER)
+            ts.append(time.perf_counter() - t0)
+        out["oracle"] = {"value": float(np.median(ts)), "unit": "s", "cores": 1,
+                         "outer": int(so["outer"]), "inner": int(so["inner_total"]),
+                         "max_head_diff_vs_gpu_fp64_m": float(np.max(np.abs(g.x - heads["fp64"])))}
     return out
 
 

@@ -184,14 +184,20 @@ __global__ void k_ilu_bwd_level(const int *__restrict__ rows, int nrows,
   d[n] = tv * apc[n];
 }
 
-// Sync-free sweeps: one launch per sweep instead of one per level.  Every
-// thread walks the level-ordered row list with a grid stride; a row reads the
-// rows it depends on as result words tagged with the launch's epoch and
-// waits (bounded) for those not written yet.  Rows depend only on rows of
-// lower levels, which come earlier in the list, and the grid is sized so
-// that all of its CTAs are resident: the lowest unfinished row of the list
-// can always proceed, so every wait ends.  Each row sums its entries in
-// JAPC order with FMA, as the per-level kernels do (bit-identical results).
+// Sync-free sweeps: one launch per sweep instead of one per level.  The
+// warps walk the level-ordered row list with a grid stride, 32 consecutive
+// rows per warp; a row reads the rows it depends on as result words tagged
+// with the launch's epoch.  The polling is warp-synchronous: in each round
+// every unfinished lane loads all its dependencies' words (up to kDeps in
+// flight at once), and a lane whose words are all of this epoch finishes its
+// row; the warp repeats the round until all its lanes are done.  A lane may
+// depend on a lane of its own warp (a warp can straddle two levels): that
+// row is written in one round and seen in the next.  Rows depend only on
+// rows of lower levels, which come earlier in the list, and the grid is
+// sized so that all of its CTAs are resident: the lowest unfinished row of
+// the list can always proceed, so every wait ends (and is bounded besides).
+// Each row sums its entries in JAPC order with FMA, as the per-level kernels
+// do (bit-identical results).
 template <typename T, int DIR>
 __global__ void __launch_bounds__(256) k_ilu_sweep_sf(int n, const int *__restrict__ rows,
                                                       const int *__restrict__ iapc,
@@ -211,59 +217,68 @@ __global__ void __launch_bounds__(256) k_ilu_sweep_sf(int n, const int *__restri
   __syncthreads();
   if (ctl && ctl->done) return;
   const unsigned ep = s_ep;
+  const int lane = threadIdx.x & 31;
   volatile int *vdone = ctl ? &ctl->done : nullptr;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int row = rows[q];
-    T tv;
-    int j0, j1;
-    if (DIR > 0) {
-      tv = r[row];
-      j0 = iapc[row];
-      j1 = japc[row];
-    } else {
-      tv = ll_val(yin[row]);
-      j0 = japc[row];
-      j1 = iapc[row + 1];
-    }
-    // the words of up to kDeps dependencies are loaded together, then the
-    // missing ones polled (with a growing pause, so that spinning threads do
-    // not crowd the L2 the producers write through); the FMAs then run in
-    // JAPC order
-    constexpr int kDeps = 8;
-    for (int jb = j0; jb < j1; jb += kDeps) {
-      LLRaw w[kDeps];
-      const int nd = min(kDeps, j1 - jb);
-#pragma unroll
-      for (int q2 = 0; q2 < kDeps; ++q2)
-        if (q2 < nd) ll_issue(out + japc[jb + q2], w[q2]);
-#pragma unroll
-      for (int q2 = 0; q2 < kDeps; ++q2) {
-        if (q2 >= nd) break;
-        T v;
-        if (ll_ready<T>(w[q2], ep)) {
-          ll_take(w[q2], v);
-        } else {
-          const LLWord<T> *pw = out + japc[jb + q2];
-          const unsigned long long t0 = wclock();
-          unsigned pause = 32;
-          while (!ll_get(pw, ep, v)) {
-            if ((vdone && *vdone) || wclock() - t0 > kWaitCycles) {
-              atomicExch(err, 1);
-              if (ctl) ctl->done = 1;
-              return;
-            }
-            __nanosleep(pause);
-            if (pause < 512) pause <<= 1;
-          }
-        }
-        tv = fms<T>(apc[jb + q2], v, tv);
+  constexpr int kDeps = 8;
+  const int stride = gridDim.x * blockDim.x;
+  for (int q0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); q0 < n; q0 += stride) {
+    const int q = q0 + lane;
+    bool done = q >= n;
+    int row = 0, j0 = 0, j1 = 0;
+    T tv0 = T(0);
+    if (!done) {
+      row = rows[q];
+      if (DIR > 0) {
+        tv0 = r[row];
+        j0 = iapc[row];
+        j1 = japc[row];
+      } else {
+        tv0 = ll_val(yin[row]);
+        j0 = japc[row];
+        j1 = iapc[row + 1];
       }
     }
-    if (DIR < 0) {
-      tv = tv * apc[row];
-      d[row] = tv;
+    const unsigned long long t0 = wclock();
+    while (true) {
+      if (!done) {
+        T tv = tv0;
+        bool ok = true;
+        for (int jb = j0; ok && jb < j1; jb += kDeps) {
+          LLRaw w[kDeps];
+          const int nd = min(kDeps, j1 - jb);
+#pragma unroll
+          for (int q2 = 0; q2 < kDeps; ++q2)
+            if (q2 < nd) ll_issue(out + japc[jb + q2], w[q2]);
+#pragma unroll
+          for (int q2 = 0; q2 < kDeps; ++q2) {
+            if (q2 >= nd || !ok) break;
+            if (!ll_ready<T>(w[q2], ep)) {
+              ok = false;
+            } else {
+              T v;
+              ll_take(w[q2], v);
+              tv = fms<T>(apc[jb + q2], v, tv);
+            }
+          }
+        }
+        if (ok) {
+          if (DIR < 0) {
+            tv = tv * apc[row];
+            d[row] = tv;
+          }
+          ll_put(out + row, tv, ep);
+          done = true;
+        }
+      }
+      if (!__any_sync(0xffffffffu, !done)) break;
+      if (__any_sync(0xffffffffu, (vdone && *vdone) || wclock() - t0 > kWaitCycles)) {
+        if (lane == 0) {
+          atomicExch(err, 1);
+          if (ctl) ctl->done = 1;
+        }
+        return;
+      }
     }
-    ll_put(out + row, tv, ep);
   }
 }
 
