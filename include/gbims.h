@@ -216,6 +216,16 @@ typedef struct gbims_tuning {
   double vector_ms;                 /* dot + update at the chosen grid */
 } gbims_tuning;
 int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out);
+/* A DIS grid reduced by IDOMAIN (no counterpart call in the reference; it
+ * holds the same map as DisType%nodeuser, Dis.f90): nodeuser[n] is the user
+ * cell (k*nrow*ncol + i*ncol + j, plus index_base) of node n, strictly
+ * increasing, and the pattern must be the full grid's (settings nlay, nrow,
+ * ncol) with the inactive cells removed.  The ILU0 factor is still that of
+ * the reduced matrix; its triangular sweeps then run as wavefront sweeps on
+ * the full grid, the inactive cells decoupled with zero factors, r spread
+ * onto it and z gathered back.  Call after gbims_create and before the
+ * first factorisation; single models, ILU0/MILU0, no reordering. */
+int gbims_set_dis_nodes(gbims_handle *h, const int *nodeuser);
 /* Applies a tuning found earlier (sweep_config < 0, reduction_blocks <= 0 or
  * level_mode < 0 leave that part unchanged). */
 int gbims_set_tuning(gbims_handle *h, int sweep_config, int reduction_blocks, int level_mode);

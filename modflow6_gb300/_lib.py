@@ -157,6 +157,7 @@ _SIGS = {
     "gbsln_restart": (C.c_int, [C.c_void_p]),
     "gbsln_budget": (C.c_int, [C.c_void_p, _dp, C.POINTER(GbslnBudgetTable)]),
     "gbims_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(GbimsTuning)]),
+    "gbims_set_dis_nodes": (C.c_int, [C.c_void_p, _ip]),
     "gbims_set_tuning": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "gbsln_get_heads": (C.c_int, [C.c_void_p, _dp]),
     "gbsln_set_heads": (C.c_int, [C.c_void_p, _dp]),

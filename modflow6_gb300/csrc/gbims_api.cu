@@ -139,13 +139,22 @@ static int level_words_error(gbims_handle *h) {
 }
 
 static void precond64(gbims_handle *h, const double *r, double *z) {
-  if (h->structured) launch_dia7_apply64(h->D, r, z, h->d_ctl, h->st);
+  if (h->structured && h->D.mapped) {
+    // an IDOMAIN-reduced grid: the sweeps on the full grid
+    launch_dia7_spread(h->D, h->n, r, h->D.d_rfull, h->st);
+    launch_dia7_apply64(h->D, h->D.d_rfull, h->D.d_zfull, h->d_ctl, h->st);
+    launch_dia7_collect(h->D, h->n, h->D.d_zfull, z, h->st);
+  } else if (h->structured) launch_dia7_apply64(h->D, r, z, h->d_ctl, h->st);
   else launch_ilu_apply_levels(h->n, h->d_iapc, h->d_japc, h->d_apc, h->F, h->B, h->LW, r, z, h->d_ctl, h->st);
 }
 
 // The mixed form's preconditioner: FP32 factors, vectors and sweeps.
 static void precond32(gbims_handle *h, const float *r, float *z) {
-  if (h->structured) launch_dia7_apply32(h->D, r, z, h->d_ctl, h->st);
+  if (h->structured && h->D.mapped) {
+    launch_dia7_spread32(h->D, h->n, r, h->D.f_rfull, h->st);
+    launch_dia7_apply32(h->D, h->D.f_rfull, h->D.f_zfull, h->d_ctl, h->st);
+    launch_dia7_collect32(h->D, h->n, h->D.f_zfull, z, h->st);
+  } else if (h->structured) launch_dia7_apply32(h->D, r, z, h->d_ctl, h->st);
   else launch_ilu_apply_levels32(h->n, h->d_iapc, h->d_japc, h->d_apc32, h->F, h->B, h->LW, r, z, h->d_ctl, h->st);
 }
 
@@ -1231,6 +1240,48 @@ extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
   return GBIMS_OK;
 }
 
+extern "C" int gbims_set_dis_nodes(gbims_handle *h, const int *nodeuser) {
+  if (!h || !nodeuser) return GBIMS_ERR_ARG;
+  if (h->structured) return fail(h, GBIMS_ERR_ARG, "the handle already has the wavefront sweeps");
+  if (h->factored) return fail(h, GBIMS_ERR_ARG, "set the DIS node map before the first factorisation");
+  if (h->nm > 0 || h->reorder || h->ipc >= 3)
+    return fail(h, GBIMS_ERR_UNSUPPORTED,
+                "a node map needs a single model, no reordering and ILU0/MILU0");
+  const int dl = h->s.nlay, dr = h->s.nrow, dc = h->s.ncol;
+  if (dl <= 0 || dr <= 0 || dc <= 0)
+    return fail(h, GBIMS_ERR_ARG, "a node map needs the grid shape (settings nlay, nrow, ncol)");
+  const int n = h->n;
+  const int base = h->s.index_base;
+  std::vector<int> nu(n);
+  for (int r = 0; r < n; ++r) nu[r] = nodeuser[r] - base;
+  if (!dia7_matches_reduced(dl, dr, dc, n, h->ia, h->ja, nu.data()))
+    return fail(h, GBIMS_ERR_ARG, "the pattern is not the DIS grid reduced by the node map");
+  std::vector<int> shape = {dl, dr, dc};
+  if (int rc = setup_structured(h, shape, std::vector<long long>{0})) return rc;
+  const long long nuser = (long long)dl * dr * dc;
+  std::vector<int> ur((size_t)nuser, -1);
+  for (int r = 0; r < n; ++r) ur[(size_t)nu[r]] = r;
+  Dia7 &D = h->D;
+  D.nuser = nuser;
+  GB_CUDA(h, dalloc(&D.d_nodeuser, (size_t)n));
+  GB_CUDA(h, dalloc(&D.d_userred, (size_t)nuser));
+  GB_CUDA(h, cudaMemcpy(D.d_nodeuser, nu.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+  GB_CUDA(h, cudaMemcpy(D.d_userred, ur.data(), sizeof(int) * nuser, cudaMemcpyHostToDevice));
+  // full-grid vectors, with the sweeps' slack after the last cell
+  if (!h->mixed) {
+    GB_CUDA(h, dalloc(&D.d_rfull, (size_t)nuser + kVecPad));
+    GB_CUDA(h, dalloc(&D.d_zfull, (size_t)nuser + kVecPad));
+    GB_CUDA(h, cudaMemset(D.d_rfull, 0, sizeof(double) * ((size_t)nuser + kVecPad)));
+  } else {
+    GB_CUDA(h, dalloc(&D.f_rfull, (size_t)nuser + kVecPad));
+    GB_CUDA(h, dalloc(&D.f_zfull, (size_t)nuser + kVecPad));
+    GB_CUDA(h, cudaMemset(D.f_rfull, 0, sizeof(float) * ((size_t)nuser + kVecPad)));
+  }
+  D.mapped = true;
+  drop_graph(h);
+  return GBIMS_OK;
+}
+
 extern "C" int gbims_set_tuning(gbims_handle *h, int sweep_config, int reduction_blocks,
                                 int level_mode) {
   if (!h) return GBIMS_ERR_ARG;
@@ -1406,7 +1457,8 @@ extern "C" int gbims_destroy(gbims_handle *h) {
                   h->I.lval, h->I.ucol, h->I.uval, h->I.nl, h->I.nu, h->I.dinv, h->I.rdone,
                   h->I.stat, h->d_lorder, h->d_iorder, h->d_asrc, h->d_ia_u, h->d_ja_u,
                   h->u_amat, h->u_rhs, h->u_x, h->d_modstart, h->d_rec, h->d_rec_part,
-                  h->d_rec_loc};
+                  h->d_rec_loc, h->D.d_nodeuser, h->D.d_userred, h->D.d_rfull, h->D.d_zfull,
+                  h->D.f_rfull, h->D.f_zfull};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);

@@ -201,6 +201,15 @@ struct Dia7 {
   int *d_flags = nullptr;  // the sweeps' ticket counters (forward, backward), one 128-byte line each
   int nflags = 0;
   int *d_err = nullptr;    // wait-limit error flag
+  // a DIS grid reduced by IDOMAIN (gbims_set_dis_nodes): the sweeps run on
+  // the full grid, inactive cells decoupled with zero factors; r is spread
+  // onto it and z gathered back (nodeuser: reduced -> user cell, userred:
+  // user cell -> reduced node or -1)
+  bool mapped = false;
+  long long nuser = 0;
+  int *d_nodeuser = nullptr, *d_userred = nullptr;
+  double *d_rfull = nullptr, *d_zfull = nullptr;
+  float *f_rfull = nullptr, *f_zfull = nullptr;
 };
 
 // Elements of slack after every n-vector, so that a kernel may read or
@@ -263,6 +272,12 @@ bool dia7_matches(int nlay, int nrow, int ncol, int n, const std::vector<int> &i
                   const std::vector<int> &ja);
 // The DIS shape of a 0-based CSR pattern that is a full 7-point grid in
 // natural order (false if it is not one).
+bool dia7_matches_reduced(int nlay, int nrow, int ncol, int n, const std::vector<int> &ia,
+                          const std::vector<int> &ja, const int *nodeuser);
+void launch_dia7_spread(const Dia7 &D, int n, const double *r, double *rfull, cudaStream_t st);
+void launch_dia7_spread32(const Dia7 &D, int n, const float *r, float *rfull, cudaStream_t st);
+void launch_dia7_collect(const Dia7 &D, int n, const double *zfull, double *z, cudaStream_t st);
+void launch_dia7_collect32(const Dia7 &D, int n, const float *zfull, float *z, cudaStream_t st);
 bool dia7_detect(int n, const std::vector<int> &ia, const std::vector<int> &ja, int *nlay,
                  int *nrow, int *ncol);
 // Factor -> skewed tiles; FP64 handles choose df64 or native tiles here (D.ext).

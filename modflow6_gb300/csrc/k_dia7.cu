@@ -547,10 +547,15 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
 // APC/JAPC -> skewed tiles.  Forward tiles hold Lz, Ly, Lx of the cell that
 // lane l visits at step g; backward tiles hold dinv*Uz, dinv*Uy, dinv*Ux and
 // dinv.  Slots outside the grid are zero.
+// With an IDOMAIN-reduced grid (userred/nodeuser not null) the factor rows
+// are those of the reduced nodes: a slot's cell reads the row of its reduced
+// node (an inactive cell keeps zeros, dinv included) and recognises its
+// neighbours by their user cells.
 template <typename T>
 __global__ void k_dia7_extract(const Dia7Geo *__restrict__ geos, int nm, long long nslot, int W,
                                int S, int dir, const int *__restrict__ iapc,
                                const int *__restrict__ japc, const double *__restrict__ apc,
+                               const int *__restrict__ userred, const int *__restrict__ nodeuser,
                                T *A, T *B, T *X, T *D) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nslot;
        q += (long long)gridDim.x * blockDim.x) {
@@ -571,12 +576,13 @@ __global__ void k_dia7_extract(const Dia7Geo *__restrict__ geos, int nm, long lo
     const int jj = gg - S * l;
     const int i = (dir > 0) ? b * W + l : b * W + (W - 1 - l);
     double va = 0, vb = 0, vx = 0, vd = 0;
-    if (i < g.nrow && jj >= 0 && jj < g.ncol) {
-      const int j = (dir > 0) ? jj : g.ncol - 1 - jj;
-      const long long n = g.row0 + k * nrc + (long long)i * g.ncol + j;
-      const double d = apc[n];
-      for (int pp = iapc[n]; pp < iapc[n + 1]; ++pp) {
-        const long long c = japc[pp];
+    const int j = (dir > 0) ? jj : g.ncol - 1 - jj;
+    const long long n = g.row0 + k * nrc + (long long)i * g.ncol + j;
+    const long long rn = (i < g.nrow && jj >= 0 && jj < g.ncol) ? (userred ? userred[n] : n) : -1;
+    if (rn >= 0) {
+      const double d = apc[rn];
+      for (int pp = iapc[rn]; pp < iapc[rn + 1]; ++pp) {
+        const long long c = nodeuser ? nodeuser[japc[pp]] : japc[pp];
         const double a = apc[pp];
         if (dir > 0) {
           if (k > 0 && c == n - nrc) va = a;
@@ -692,6 +698,79 @@ bool dia7_matches(int nlay, int nrow, int ncol, int n, const std::vector<int> &i
   return true;
 }
 
+// The pattern of a DIS grid whose inactive cells were removed (IDOMAIN):
+// row r is user cell nodeuser[r] (strictly increasing), with the active
+// ones of its six neighbours, in the full grid's JA order, renumbered.
+bool dia7_matches_reduced(int nlay, int nrow, int ncol, int n, const std::vector<int> &ia,
+                          const std::vector<int> &ja, const int *nodeuser) {
+  const long long nrc = (long long)nrow * ncol, nu = nrc * nlay;
+  if (n <= 0 || (long long)n > nu || (int)ia.size() != n + 1) return false;
+  std::vector<int> red((size_t)nu, -1);
+  for (int r = 0; r < n; ++r) {
+    const long long u = nodeuser[r];
+    if (u < 0 || u >= nu || (r > 0 && u <= nodeuser[r - 1])) return false;
+    red[(size_t)u] = r;
+  }
+  for (int r = 0; r < n; ++r) {
+    const long long u = nodeuser[r];
+    const int k = (int)(u / nrc);
+    const long long rem = u - k * nrc;
+    const int i = (int)(rem / ncol), j = (int)(rem - (long long)i * ncol);
+    long long nb[7];
+    int w = 0;
+    nb[w++] = u;
+    if (k > 0) nb[w++] = u - nrc;
+    if (i > 0) nb[w++] = u - ncol;
+    if (j > 0) nb[w++] = u - 1;
+    if (j < ncol - 1) nb[w++] = u + 1;
+    if (i < nrow - 1) nb[w++] = u + ncol;
+    if (k < nlay - 1) nb[w++] = u + nrc;
+    int q = ia[r];
+    for (int t = 0; t < w; ++t) {
+      const int rr = red[(size_t)nb[t]];
+      if (rr < 0) continue;
+      if (q >= ia[r + 1] || ja[q] != rr) return false;
+      ++q;
+    }
+    if (q != ia[r + 1]) return false;
+  }
+  return true;
+}
+
+namespace {
+template <typename V>
+__global__ void k_dia7_spread(long long nuser, const int *__restrict__ userred,
+                              const V *__restrict__ r, V *__restrict__ rfull) {
+  for (long long u = blockIdx.x * (long long)blockDim.x + threadIdx.x; u < nuser;
+       u += (long long)gridDim.x * blockDim.x) {
+    const int rr = userred[u];
+    rfull[u] = (rr >= 0) ? r[rr] : V(0);
+  }
+}
+template <typename V>
+__global__ void k_dia7_collect(int n, const int *__restrict__ nodeuser, const V *__restrict__ zfull,
+                               V *__restrict__ z) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    z[q] = zfull[nodeuser[q]];
+}
+int vgrid(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 8LL * kNumSM)); }
+}  // namespace
+
+void launch_dia7_spread(const Dia7 &D, int n, const double *r, double *rfull, cudaStream_t st) {
+  (void)n;
+  k_dia7_spread<double><<<vgrid(D.nuser), 256, 0, st>>>(D.nuser, D.d_userred, r, rfull);
+}
+void launch_dia7_spread32(const Dia7 &D, int n, const float *r, float *rfull, cudaStream_t st) {
+  (void)n;
+  k_dia7_spread<float><<<vgrid(D.nuser), 256, 0, st>>>(D.nuser, D.d_userred, r, rfull);
+}
+void launch_dia7_collect(const Dia7 &D, int n, const double *zfull, double *z, cudaStream_t st) {
+  k_dia7_collect<double><<<vgrid(n), 256, 0, st>>>(n, D.d_nodeuser, zfull, z);
+}
+void launch_dia7_collect32(const Dia7 &D, int n, const float *zfull, float *z, cudaStream_t st) {
+  k_dia7_collect<float><<<vgrid(n), 256, 0, st>>>(n, D.d_nodeuser, zfull, z);
+}
+
 bool dia7_detect(int n, const std::vector<int> &ia, const std::vector<int> &ja, int *nlay,
                  int *nrow, int *ncol) {
   if (n < 2 || (int)ia.size() != n + 1) return false;
@@ -771,9 +850,11 @@ static void extract_t(const Dia7 &D, const int *d_iapc, const int *d_japc, const
   const long long nslot = D.slots;
   int grid = (int)std::min<long long>((nslot + 255) / 256, 8LL * kNumSM);
   k_dia7_extract<T><<<grid, 256, 0, st>>>(D.d_geo, D.nm, nslot, kW, kSOf<T>, 1, d_iapc, d_japc,
-                                          d_apc, arr[0], arr[1], arr[2], nullptr);
+                                          d_apc, D.d_userred, D.d_nodeuser, arr[0], arr[1], arr[2],
+                                          nullptr);
   k_dia7_extract<T><<<grid, 256, 0, st>>>(D.d_geo, D.nm, nslot, kW, kSOf<T>, -1, d_iapc, d_japc,
-                                          d_apc, arr[3], arr[4], arr[5], arr[6]);
+                                          d_apc, D.d_userred, D.d_nodeuser, arr[3], arr[4], arr[5],
+                                          arr[6]);
 }
 
 int launch_dia7_extract(Dia7 &D, int n, const int *d_iapc, const int *d_japc,

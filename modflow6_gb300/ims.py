@@ -126,6 +126,20 @@ class ImsLinear:
             raise _lib.GbimsError(rc, lib.gbims_last_error(self._h).decode())
         return ApplyResult(icnvg.value, in_iter.value, rc, _summary(sm))
 
+    def set_dis_nodes(self, nodeuser: np.ndarray):
+        """gbims_set_dis_nodes: the handle's pattern is the DIS grid of the
+        settings' shape with IDOMAIN cells removed, `nodeuser` the user cell
+        of each node (DisType%nodeuser): the ILU0 sweeps then run as
+        wavefront sweeps on the full grid.  Before the first apply."""
+        lib = _lib.load()
+        nu = np.ascontiguousarray(nodeuser, dtype=np.int32)
+        if nu.size != self.neq:
+            raise _lib.GbimsError(_lib.GBIMS_ERR_ARG, "nodeuser needs one entry per node")
+        rc = lib.gbims_set_dis_nodes(self._h, _lib.iptr(nu))
+        if rc < 0:
+            raise _lib.GbimsError(rc, lib.gbims_last_error(self._h).decode())
+        return self
+
     def set_inner_records(self, nconv: int, convmodstart=None, index_base: int = 0):
         """Keep up to `nconv` per-inner-iteration records per apply
         (imslinear_ap's NCONV; 0 switches them off).  `convmodstart`: the

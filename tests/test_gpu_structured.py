@@ -263,3 +263,80 @@ def test_df64_right_hand_side_extremes(gblib):
     o.apply(amat.copy(), rhs.copy(), x0.copy())
     zo = oracle.ilu0a(o.apc(), o.iapc(), o.japc(), v, fma=True)
     assert np.max(np.abs(z - zo)) <= 1e-12 * np.max(np.abs(zo))
+
+
+def reduced_system(nlay, nrow, ncol, frac, seed=3):
+    """The DIS system of dis_system with a seeded fraction of its cells
+    removed as IDOMAIN does (rows and columns dropped, the kept cells
+    renumbered in user order; the CHD cell 0 is kept): (nodeuser, ia, ja,
+    amat, rhs, x0)."""
+    m, con, amat, rhs, x0 = dis_system(nlay, nrow, ncol)
+    ia, ja = con["ia"], con["ja"]
+    keep = np.random.default_rng(seed).uniform(size=m.nodes) >= frac
+    keep[0] = True
+    new = np.cumsum(keep) - 1
+    rows, vals = [], []
+    for r in np.flatnonzero(keep):
+        sel = [q for q in range(ia[r], ia[r + 1]) if keep[ja[q]]]
+        rows.append([new[ja[q]] for q in sel])
+        vals.append([amat[q] for q in sel])
+    ia2 = np.concatenate([[0], np.cumsum([len(c) for c in rows])]).astype(np.int32)
+    ja2 = np.concatenate(rows).astype(np.int32)
+    a2 = np.concatenate(vals)
+    nodeuser = np.flatnonzero(keep).astype(np.int32)
+    return nodeuser, ia2, ja2, a2, rhs[keep].copy(), x0[keep].copy()
+
+
+@pytest.mark.parametrize("precision", [_lib.GBIMS_FP64, _lib.GBIMS_MIXED])
+@pytest.mark.parametrize("shape,frac", [((2, 40, 37), 0.1), ((3, 70, 64), 0.3), ((1, 33, 9), 0.5)],
+                         ids=["2x40x37", "3x70x64", "1x33x9"])
+def test_idomain_grid_sweeps_on_the_full_grid(gblib, shape, frac, precision):
+    """An IDOMAIN-reduced DIS grid with its node map runs the wavefront
+    sweeps on the full grid (inactive cells decoupled): the preconditioner
+    matches the oracle's ilu0a of the reduced matrix (FP64: 1e-12 of its
+    scale; FP32: 1e-5), and the same handle solves to the oracle's closure."""
+    nodeuser, ia, ja, amat, rhs, x0 = reduced_system(*shape, frac)
+    n = ia.size - 1
+    ims = ImsLinear(ImsLinearSettings(structure=shape, precision=precision)).imslinear_allocate(
+        n, ia, ja)
+    ims.set_dis_nodes(nodeuser)
+    assert gblib.gbims_factor(ims._h, _lib.dptr(amat), None) == 0
+    v = np.random.default_rng(5).standard_normal(n)
+    z = np.zeros_like(v)
+    assert gblib.gbims_precondition(ims._h, _lib.dptr(v), _lib.dptr(z)) == 0
+    o = oracle.Ims(oracle.settings(), ia, ja)
+    o.apply(amat.copy(), rhs.copy(), x0.copy())
+    zo = oracle.ilu0a(o.apc(), o.iapc(), o.japc(), v, fma=True)
+    scale = np.max(np.abs(zo))
+    tol = 1e-12 if precision == _lib.GBIMS_FP64 else 1e-5
+    assert np.max(np.abs(z - zo)) <= tol * scale, np.max(np.abs(z - zo)) / scale
+    tol_s = dict(dvclose=1e-9, rclose=1e-7, iter1=2000)
+    ob = oracle.Ims(oracle.settings(**tol_s), ia, ja)
+    xo = x0.copy()
+    ob.apply(amat.copy(), rhs.copy(), xo)
+    ims2 = ImsLinear(ImsLinearSettings(structure=shape, precision=precision, **tol_s)).imslinear_allocate(
+        n, ia, ja)
+    ims2.set_dis_nodes(nodeuser)
+    x2 = x0.copy()
+    r2 = ims2.imslinear_apply(amat.copy(), rhs.copy(), x2)
+    assert r2.summary["structured"] == 1 and r2.icnvg == 1
+    bar = 1e-6 if precision == _lib.GBIMS_FP64 else 1e-4
+    assert np.max(np.abs(x2 - xo)) <= bar * max(1.0, np.max(np.abs(xo))), np.max(np.abs(x2 - xo))
+
+
+def test_idomain_node_map_is_checked(gblib):
+    """A node map that does not describe the pattern, or that comes after the
+    first factorisation, is refused; the handle keeps its level sweeps."""
+    nodeuser, ia, ja, amat, rhs, x0 = reduced_system(2, 20, 11, 0.2)
+    n = ia.size - 1
+    ims = ImsLinear(ImsLinearSettings(structure=(2, 20, 11))).imslinear_allocate(n, ia, ja)
+    bad = nodeuser.copy()
+    bad[3] += 1 if bad[4] > bad[3] + 1 else 0
+    bad[-1] = 2 * 20 * 11 + 5  # outside the grid
+    with pytest.raises(_lib.GbimsError):
+        ims.set_dis_nodes(bad)
+    assert gblib.gbims_factor(ims._h, _lib.dptr(amat), None) == 0
+    with pytest.raises(_lib.GbimsError):
+        ims.set_dis_nodes(nodeuser)
+    res = ims.imslinear_apply(amat.copy(), rhs.copy(), x0.copy())
+    assert res.summary["structured"] == 0
