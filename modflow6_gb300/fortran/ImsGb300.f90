@@ -97,6 +97,14 @@ module ImsGb300Module
       integer(c_int), intent(out) :: itinner(*), locdv(*), locr(*)
       real(c_double), intent(out) :: alpha(*), omega(*), dvmax(*), rmax(*)
     end function gbims_get_inner_records
+    ! a DIS grid reduced by IDOMAIN: the user cell of each node (DisType%nodeuser,
+    ! 1-based with index_base = 1); the settings carry the grid's shape
+    integer(c_int) function gbims_set_dis_nodes(h, nodeuser) &
+      bind(C, name='gbims_set_dis_nodes')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), intent(in) :: nodeuser(*)
+    end function gbims_set_dis_nodes
     ! ims_base_calc_order (ImsLinearBase.f90:556-610): LORDER/IORDER of RCM
     ! (iord 1) or MD (iord 2), 1-based with index_base = 1; host only (the
     ! handle computes its own ordering at gbims_create)
@@ -145,11 +153,14 @@ contains
 
   !> @brief imslinear_allocate: the settings IMS already holds and the
   !! solution's 1-based IA/JA (diagonal first in each row).  The DIS shape is
-  !! found from the pattern (nlay = nrow = ncol = 0); NCONV > 1 asks for the
+  !! found from the pattern (nlay = nrow = ncol = 0) unless the solution's one
+  !! model is a DIS grid that passes its shape (DIS_SHAPE = nlay, nrow, ncol)
+  !! and, with IDOMAIN cells removed, its NODEUSER map; NCONV > 1 asks for the
   !! per-inner-iteration records of CONVNMOD models starting at CONVMODSTART.
   subroutine gb_allocate(this, dvclose, rclose, icnvgopt, iter1, ilinmeth, &
                          iscl, iord, north, relax, level, droptol, neq, nja, &
-                         ia, ja, nconv, convnmod, convmodstart)
+                         ia, ja, nconv, convnmod, convmodstart, dis_shape, &
+                         nodeuser)
     class(ImsGb300Type), intent(inout) :: this
     real(DP), intent(in) :: dvclose, rclose, relax, droptol
     integer(I4B), intent(in) :: icnvgopt, iter1, ilinmeth, iscl, iord, north
@@ -157,6 +168,8 @@ contains
     integer(I4B), dimension(neq + 1), intent(in) :: ia
     integer(I4B), dimension(nja), intent(in) :: ja
     integer(I4B), dimension(convnmod + 1), intent(in) :: convmodstart
+    integer(I4B), dimension(3), intent(in), optional :: dis_shape
+    integer(I4B), dimension(:), intent(in), optional :: nodeuser
     type(gbims_settings_t) :: s
     integer(c_int) :: ierr
     s%dvclose = dvclose
@@ -175,10 +188,24 @@ contains
     s%nlay = 0
     s%nrow = 0
     s%ncol = 0
+    if (present(dis_shape)) then
+      s%nlay = dis_shape(1)
+      s%nrow = dis_shape(2)
+      s%ncol = dis_shape(3)
+    end if
     ierr = gbims_create(s, neq, nja, ia, ja, this%h)
     if (ierr < 0) then
       call store_error('GB300 IMS allocation failed: '// &
                        trim(gb_message(this%h)), terminate=.TRUE.)
+    end if
+    if (present(dis_shape) .and. present(nodeuser)) then
+      if (neq < dis_shape(1) * dis_shape(2) * dis_shape(3)) then
+        ierr = gbims_set_dis_nodes(this%h, nodeuser)
+        if (ierr < 0) then
+          call store_error('GB300 IMS node map: '//trim(gb_message(this%h)), &
+                           terminate=.TRUE.)
+        end if
+      end if
     end if
     this%neq = neq
     this%ilinmeth = ilinmeth
