@@ -24,11 +24,14 @@
 // warps per CTA, so that no wait stalls the dependent chain:
 //  * copy: streams the block's own factor tiles (and, backward, its forward
 //    result) into a ring of NS shared-memory buffers with bulk copies
-//    (cp.async.bulk), one "full" mbarrier per buffer;
+//    (cp.async.bulk), one "full" mbarrier per buffer; it also writes each
+//    chunk's own right-hand side (forward r read in natural order and split
+//    into df64 pairs, backward dinv*y) into the buffer ("rdy" mbarrier): in
+//    the layers with a layer neighbour the pre-compute warp was the slowest
+//    warp with that work, and this warp idles between its copies;
 //  * pre-compute: loads the layer neighbour's words (PF chunks ahead) and
-//    folds the right-hand side and the layer term (forward r - Lz*zn, with
-//    r read in natural order; backward dinv*y - Uz'*zn) into one tile,
-//    released through a "prep" mbarrier;
+//    folds the layer term into the right-hand side (forward r - Lz*zn,
+//    backward dinv*y - Uz'*zn), released through a "prep" mbarrier;
 //  * edge: loads the neighbour block's last line (PF chunks ahead) for the
 //    first lane;
 //  * compute: per step one shuffle and the two FMAs of the row and column
@@ -176,15 +179,19 @@ struct SweepArgs {
 // One ring buffer of a sweep CTA: C steps of the block's tiles (32 lanes).
 template <typename T, int C, int DIR>
 struct Stage;
+// rv: the step's own right-hand side (forward r, backward dinv*y), written
+// by the edge warp; the pre-compute warp folds the layer term into it.
 template <typename T, int C>
 struct alignas(16) Stage<T, C, 1> {
   T a[C * 32], b[C * 32], x[C * 32];
+  T rv[C * 32];
   T yn[C];  // the neighbour block's last line, one value per step
 };
 template <typename T, int C>
 struct alignas(16) Stage<T, C, -1> {
   T a[C * 32], b[C * 32], x[C * 32], d[C * 32];
   LLWord<T> y[C * 32];  // own forward result, steps descending
+  T rv[C * 32];
   T yn[C];
 };
 
@@ -221,6 +228,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
   unsigned long long *full = reinterpret_cast<unsigned long long *>(smem_raw + NS * sizeof(St));
   unsigned long long *empty = full + NS;
   unsigned long long *prep = full + 2 * NS;
+  unsigned long long *rdy = full + 3 * NS;  // rv written (edge warp)
   __shared__ int s_id, s_abort, s_rot, s_m;
   __shared__ unsigned s_ep;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -254,6 +262,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
       mbar_init(&prep[s], 2);  // pre-compute warp + edge warp
+      mbar_init(&rdy[s], 1);   // edge warp
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -303,33 +312,14 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
 #pragma unroll
           for (int t = 0; t < C; ++t) ll_issue(zsrc + (long long)(j * C + t) * W, zr[j][t]);
     }
-    // forward: the right-hand side straight from natural order (lane l
-    // walks line b*W + l; step g is column g - S*l), in the same ring
-    const int ri = b * W + lane;
-    const bool rline = (DIR > 0) && ri < nrow;
-    const V *rrow = rline ? p.rnat + geo.row0 + ((long long)k * nrow + ri) * geo.ncol : nullptr;
-    // (kept as loaded and converted when used: a conversion right after the
-    // load would wait for it, and the prefetch would hide nothing)
-    auto rload = [&](int c, V (&dst)[C]) {
-#pragma unroll
-      for (int t = 0; t < C; ++t) {
-        const int jj = c * C + t - S * lane;
-        dst[t] = (rline && (unsigned)jj < (unsigned)geo.ncol) ? __ldg(rrow + jj) : V(0);
-      }
-    };
-    V rr[PF][C];
-    if constexpr (DIR > 0) {
-#pragma unroll
-      for (int j = 0; j < PF; ++j)
-        if (j < nch) rload(j, rr[j]);
-    }
     for (int c0 = 0; c0 < nch; c0 += PF) {
 #pragma unroll
       for (int j = 0; j < PF; ++j) {
         const int c = c0 + j;
         if (c >= nch) break;
         const int s = c % NS;
-        const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort);
+        const bool got = mbar_wait(&full[s], (c / NS) & 1, v_abort) &&
+                         mbar_wait(&rdy[s], (c / NS) & 1, v_abort);
         if (!__all_sync(0xffffffffu, got)) {
           if (lane == 0) *v_abort = 1;
           return;
@@ -357,20 +347,9 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
 #pragma unroll
         for (int t = 0; t < C; ++t) {
           const int e = t * W + lane;
-          T t0;
-          if constexpr (DIR > 0) {
-            t0 = E::from_vec(rr[j][t]);
-          } else {
-            // the forward words of padding slots (dinv zero) may not have
-            // been copied into this buffer: take zero, not 0 * stale bits
-            const T dv = st.d[e];
-            t0 = dinv_zero(dv) ? E::zero() : E::mul(dv, ll_val(st.y[C * W - 1 - e]));
-          }
+          T t0 = st.rv[e];
           if (has_lay) t0 = E::fms(st.a[e], zn[t], t0);
           st.a[e] = t0;
-        }
-        if constexpr (DIR > 0) {
-          if (c + PF < nch) rload(c + PF, rr[j]);
         }
         // the buffer is refilled by the async proxy after the compute warp
         // has released it: order these generic writes before that
@@ -448,7 +427,58 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     int issued = 0;
     bool ok = true;
     const unsigned tileb = C * W * sizeof(T);
-    for (int c = 0; c < nch; ++c) {
+    // It also writes each chunk's own right-hand side for the pre-compute
+    // warp: forward r
+    // from natural order (lane l walks line b*W + l; step g is column
+    // g - S*l), kept as loaded until it is used (a conversion right after
+    // the load would wait for it and the prefetch would hide nothing);
+    // backward dinv*y from the stage's tiles
+    const int ri = b * W + lane;
+    const bool rline = (DIR > 0) && ri < nrow;
+    const V *rrow = rline ? p.rnat + geo.row0 + ((long long)k * nrow + ri) * geo.ncol : nullptr;
+    auto rload = [&](int c, V (&dst)[C]) {
+#pragma unroll
+      for (int t = 0; t < C; ++t) {
+        const int jj = c * C + t - S * lane;
+        dst[t] = (rline && (unsigned)jj < (unsigned)geo.ncol) ? __ldg(rrow + jj) : V(0);
+      }
+    };
+    V rr[PF][C];
+    if constexpr (DIR > 0) {
+#pragma unroll
+      for (int j = 0; j < PF; ++j)
+        if (j < nch) rload(j, rr[j]);
+    }
+    // chunk q's rv: forward right after its tiles are issued (r has no
+    // producer in the launch), backward once its tiles have landed (one
+    // chunk behind the copies, so that no wait delays an issue)
+    auto make_rv = [&](int q, int j) -> bool {
+      St &st = stg[q % NS];
+      if constexpr (DIR > 0) {
+#pragma unroll
+        for (int t = 0; t < C; ++t) st.rv[t * W + lane] = E::from_vec(rr[j][t]);
+        if (q + PF < nch) rload(q + PF, rr[j]);
+      } else {
+        (void)j;
+        if (!__all_sync(0xffffffffu, mbar_wait(&full[q % NS], (q / NS) & 1, v_abort))) return false;
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+          const int e = t * W + lane;
+          // the forward words of padding slots (dinv zero) may not have
+          // been copied into this buffer: take zero, not 0 * stale bits
+          const T dv = st.d[e];
+          st.rv[e] = dinv_zero(dv) ? E::zero() : E::mul(dv, ll_val(st.y[C * W - 1 - e]));
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&rdy[q % NS]);
+      return true;
+    };
+    for (int c0 = 0; ok && c0 < nch; c0 += PF) {
+#pragma unroll
+    for (int j = 0; j < PF; ++j) {
+      const int c = c0 + j;
+      if (c >= nch) break;
       const int s = c % NS;
       if (c >= NS) {
         const bool got = mbar_wait(&empty[s], ((c / NS) - 1) & 1, v_abort);
@@ -479,6 +509,17 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         bulk_g2s(st.x, p.X + tb, tileb, &full[s]);
       }
       issued = c + 1;
+      __syncwarp();
+      if constexpr (DIR > 0) {
+        ok = make_rv(c, j);
+      } else {
+        if (c >= 1) ok = make_rv(c - 1, 0);
+      }
+      if (!ok) break;
+    }
+    }
+    if constexpr (DIR < 0) {
+      if (ok && nch > 0) ok = make_rv(nch - 1, 0);
     }
     if (!ok) fail();
     if (lane == 0) {
@@ -666,7 +707,7 @@ constexpr int kNumSweepCfgs = sizeof(kSweepCfgs) / sizeof(kSweepCfgs[0]);
 
 template <typename T, int C, int NS, int DIR>
 constexpr size_t stage_bytes() {
-  return NS * sizeof(Stage<T, C, DIR>) + 3 * NS * sizeof(unsigned long long);
+  return NS * sizeof(Stage<T, C, DIR>) + 4 * NS * sizeof(unsigned long long);
 }
 static_assert(stage_bytes<double, 16, 2, -1>() <= 72 * 1024 && stage_bytes<double, 4, 8, -1>() <= 72 * 1024 &&
                   stage_bytes<double, 8, 4, -1>() <= 72 * 1024,
