@@ -490,7 +490,8 @@ def autotune(lib, h, reps=5):
         out.update(level_mode=("sync-free" if t.level_mode == 1 else "per-level launches"),
                    level_ms=[round(t.level_ms[0], 4), round(t.level_ms[1], 4)])
     if t.sweep_config >= 0:
-        out.update(sweep_chunk=t.sweep_chunk, sweep_ring=t.sweep_ring,
+        out.update(sweep_config=t.sweep_config, sweep_config_backward=t.sweep_config_backward,
+                   sweep_chunk=t.sweep_chunk, sweep_ring=t.sweep_ring,
                    sweep_prefetch=t.sweep_prefetch, sweep_occupancy=t.sweep_occupancy,
                    precond_ms=t.precond_ms,
                    candidates_ms=[round(t.candidate_ms[i], 4) for i in range(t.ncandidates)])

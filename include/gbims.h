@@ -212,8 +212,10 @@ typedef struct gbims_tuning {
   double level_ms[2];               /* one ILU0 application in each level mode */
   int ncandidates;                  /* tilings timed */
   double candidate_ms[16];          /* one ILU0 application per tiling */
-  double precond_ms;                /* of the chosen tiling */
+  double precond_ms;                /* of the chosen tilings */
   double vector_ms;                 /* dot + update at the chosen grid */
+  int sweep_config_backward;        /* the backward sweep's tiling (sweep_config: the
+                                       forward sweep's); candidate_ms sums both sweeps */
 } gbims_tuning;
 int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out);
 /* A DIS grid reduced by IDOMAIN (no counterpart call in the reference; it
@@ -227,7 +229,8 @@ int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out);
  * first factorisation; single models, ILU0/MILU0, no reordering. */
 int gbims_set_dis_nodes(gbims_handle *h, const int *nodeuser);
 /* Applies a tuning found earlier (sweep_config < 0, reduction_blocks <= 0 or
- * level_mode < 0 leave that part unchanged). */
+ * level_mode < 0 leave that part unchanged); sweep_config sets the tiling of
+ * both sweeps. */
 int gbims_set_tuning(gbims_handle *h, int sweep_config, int reduction_blocks, int level_mode);
 
 int gbims_factor(gbims_handle *h, const double *amat, int *pivot_retries);

@@ -102,6 +102,7 @@ class GbimsTuning(C.Structure):
         ("sweep_prefetch", C.c_int), ("sweep_occupancy", C.c_int), ("reduction_blocks", C.c_int),
         ("level_mode", C.c_int), ("level_ms", C.c_double * 2), ("ncandidates", C.c_int),
         ("candidate_ms", C.c_double * 16), ("precond_ms", C.c_double), ("vector_ms", C.c_double),
+        ("sweep_config_backward", C.c_int),
     ]
 
 

@@ -1159,30 +1159,46 @@ extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
     return ms / reps;
   };
   if (h->structured) {
+    // each tiling timed on each sweep alone (the backward sweep reads the
+    // forward words of the last forward launch), the fastest kept for each
     const int nc = std::min(dia7_num_cfgs(), (int)(sizeof(out->candidate_ms) / sizeof(double)));
-    int best = 0;
-    double bt = 1e300;
+    int best = 0, best_b = 0;
+    double bt = 1e300, btf = 1e300, btb = 1e300;
+    auto pre = [&] {
+      if (!h->mixed) precond64(h, h->v_p, h->v_z);
+      else precond32(h, h->f_p, h->f_z);
+    };
+    h->D.cfg_b = -1;
     for (int i = 0; i < nc; ++i) {
       h->D.cfg = i;
-      const double ms = time_it([&] {
-        if (!h->mixed) precond64(h, h->v_p, h->v_z);
-        else precond32(h, h->f_p, h->f_z);
-      });
-      out->candidate_ms[i] = ms;
-      if (ms < bt) {
-        bt = ms;
+      h->D.only = 1;
+      const double tf = time_it(pre);
+      h->D.only = -1;
+      const double tb = time_it(pre);
+      h->D.only = 0;
+      out->candidate_ms[i] = tf + tb;
+      if (tf + tb < bt) bt = tf + tb;
+      if (tf < btf) {
+        btf = tf;
         best = i;
       }
+      if (tb < btb) {
+        btb = tb;
+        best_b = i;
+      }
     }
+    h->D.cfg = best;
+    h->D.cfg_b = best_b;
+    bt = time_it(pre);
     int err = 0;
     GB_CUDA(h, cudaMemcpy(&err, h->D.d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {
       cudaMemset(h->D.d_err, 0, sizeof(int));
       return fail(h, GBIMS_ERR_CUDA, "structured sweep wait limit reached while tuning");
     }
-    h->D.cfg = best;
     out->ncandidates = nc;
     out->sweep_config = best;
+    out->sweep_config_backward = best_b;
     dia7_cfg(best, &out->sweep_chunk, &out->sweep_ring, &out->sweep_prefetch, &out->sweep_occupancy);
     out->precond_ms = bt;
   }
@@ -1294,6 +1310,7 @@ extern "C" int gbims_set_tuning(gbims_handle *h, int sweep_config, int reduction
     if (!h->structured || sweep_config >= dia7_num_cfgs())
       return fail(h, GBIMS_ERR_ARG, "sweep configuration out of range (or not a structured handle)");
     h->D.cfg = sweep_config;
+    h->D.cfg_b = -1;
   }
   if (reduction_blocks > 0) {
     if (h->nm > 0 || reduction_blocks > h->G_alloc)

@@ -180,6 +180,8 @@ struct Dia7 {
   const Ctl *mctl = nullptr;  // batched ensembles: members that are done are skipped
   int ntickets = 0;
   int cfg = 0;  // sweep configuration (chunk, ring, prefetch): an index of dia7_cfg
+  int cfg_b = -1;  // the backward sweep's configuration (-1: cfg)
+  int only = 0;    // timing: 1 forward sweep only, -1 backward sweep only, 0 both
   // FP64 handles: 1 while the tiles hold df64 pairs (the factor lies in the
   // float exponent range), 0 for native FP64 tiles; ext_allowed 0 keeps the
   // native sweeps (GBIMS_SWEEP_NATIVE)

@@ -928,32 +928,40 @@ int launch_dia7_extract(Dia7 &D, int n, const int *d_iapc, const int *d_japc,
   return 0;
 }
 
-// The two sweeps of one configuration (opting in to more than 48 KB of
-// dynamic shared memory once per kernel).
-template <typename T, int C, int NS, int PF>
-static void sweep_pair(SweepArgs<T> a, const T *const *arr, const Dia7 &D, int occ,
-                       cudaStream_t st) {
-  constexpr size_t bf = stage_bytes<T, C, NS, 1>(), bb = stage_bytes<T, C, NS, -1>();
+// One sweep of one configuration (opting in to more than 48 KB of dynamic
+// shared memory once per kernel).
+template <typename T, int C, int NS, int PF, int DIR>
+static void sweep_one(const SweepArgs<T> &a, const Dia7 &D, int occ, cudaStream_t st) {
+  constexpr size_t bytes = stage_bytes<T, C, NS, DIR>();
   static bool opted = false;
   if (!opted) {  // allow up to the two-per-SM request
-    cudaFuncSetAttribute(k_dia7_sweep<T, kSOf<T>, C, NS, 1, PF>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(bf, kOcc2Smem));
-    cudaFuncSetAttribute(k_dia7_sweep<T, kSOf<T>, C, NS, -1, PF>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(bb, kOcc2Smem));
+    cudaFuncSetAttribute(k_dia7_sweep<T, kSOf<T>, C, NS, DIR, PF>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max(bytes, kOcc2Smem));
     opted = true;
   }
-  const size_t smf = (occ == 2) ? std::max(bf, kOcc2Smem) : bf;
-  const size_t smb = (occ == 2) ? std::max(bb, kOcc2Smem) : bb;
-  k_dia7_sweep<T, kSOf<T>, C, NS, 1, PF><<<D.ntickets, 128, smf, st>>>(a);
-  a.A = arr[3]; a.B = arr[4]; a.X = arr[5]; a.D = arr[6];
-  a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags + 32);
-  k_dia7_sweep<T, kSOf<T>, C, NS, -1, PF><<<D.ntickets, 128, smb, st>>>(a);
+  const size_t sm = (occ == 2) ? std::max(bytes, kOcc2Smem) : bytes;
+  k_dia7_sweep<T, kSOf<T>, C, NS, DIR, PF><<<D.ntickets, 128, sm, st>>>(a);
+}
+
+template <typename T, int DIR>
+static void sweep_cfg(const SweepArgs<T> &a, const Dia7 &D, int cfg, cudaStream_t st) {
+  const int occ = kSweepCfgs[cfg].OCC;
+  switch (cfg % 6) {
+    case 1: sweep_one<T, 8, 4, 2, DIR>(a, D, occ, st); break;
+    case 2: sweep_one<T, 4, 8, 1, DIR>(a, D, occ, st); break;
+    case 3: sweep_one<T, 4, 8, 2, DIR>(a, D, occ, st); break;
+    case 4: sweep_one<T, 16, 2, 1, DIR>(a, D, occ, st); break;
+    case 5: sweep_one<T, 16, 2, 2, DIR>(a, D, occ, st); break;
+    default: sweep_one<T, 8, 4, 1, DIR>(a, D, occ, st); break;
+  }
 }
 
 // One ILU0 application: the forward sweep reads r in natural order, the
 // backward sweep writes z in natural order; between them the results live
 // in the skewed layout as epoch-tagged words.  No memory is reset between
-// applications: each sweep launch writes its words with a new epoch.
+// applications: each sweep launch writes its words with a new epoch.  The
+// two sweeps may use different tilings (D.cfg, D.cfg_b); D.only restricts
+// an application to one of them (the autotuner's timing).
 template <typename T>
 static void apply_t(const Dia7 &D, const T *const *arr, const typename Elem<T>::V *r,
                     typename Elem<T>::V *z, const Ctl *ctl, cudaStream_t st) {
@@ -967,16 +975,15 @@ static void apply_t(const Dia7 &D, const T *const *arr, const typename Elem<T>::
   a.zsk = static_cast<LLWord<T> *>(D.ll_z);
   a.err = D.d_err;
   a.ctl = const_cast<Ctl *>(ctl);
-  a.A = arr[0]; a.B = arr[1]; a.X = arr[2]; a.D = nullptr;
-  a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags);
-  const int occ = kSweepCfgs[D.cfg].OCC;
-  switch (D.cfg % 6) {
-    case 1: sweep_pair<T, 8, 4, 2>(a, arr, D, occ, st); break;
-    case 2: sweep_pair<T, 4, 8, 1>(a, arr, D, occ, st); break;
-    case 3: sweep_pair<T, 4, 8, 2>(a, arr, D, occ, st); break;
-    case 4: sweep_pair<T, 16, 2, 1>(a, arr, D, occ, st); break;
-    case 5: sweep_pair<T, 16, 2, 2>(a, arr, D, occ, st); break;
-    default: sweep_pair<T, 8, 4, 1>(a, arr, D, occ, st); break;
+  if (D.only >= 0) {
+    a.A = arr[0]; a.B = arr[1]; a.X = arr[2]; a.D = nullptr;
+    a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags);
+    sweep_cfg<T, 1>(a, D, D.cfg, st);
+  }
+  if (D.only <= 0) {
+    a.A = arr[3]; a.B = arr[4]; a.X = arr[5]; a.D = arr[6];
+    a.ticket = reinterpret_cast<unsigned long long *>(D.d_flags + 32);
+    sweep_cfg<T, -1>(a, D, D.cfg_b >= 0 ? D.cfg_b : D.cfg, st);
   }
 }
 
