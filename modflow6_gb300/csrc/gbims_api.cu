@@ -1206,22 +1206,33 @@ extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
   if (!h->structured) {
     // level-scheduled sweeps: one launch per level, or one sync-free launch
     // per sweep
+    // per sweep (the sync-free form also with 1, 2 or 4 threads per row of
+    // the widest level; level_ms[1] is its best)
     double bt = 1e300;
-    int best = 1;
-    for (int mode = 0; mode < 2; ++mode) {
-      h->LW.mode = mode;
-      const double ms = time_it([&] {
-        if (!h->mixed) precond64(h, h->v_p, h->v_z);
-        else precond32(h, h->f_p, h->f_z);
-      });
-      out->level_ms[mode] = ms;
+    int best = 1, best_mult = 1;
+    auto pre = [&] {
+      if (!h->mixed) precond64(h, h->v_p, h->v_z);
+      else precond32(h, h->f_p, h->f_z);
+    };
+    h->LW.mode = 0;
+    out->level_ms[0] = time_it(pre);
+    bt = out->level_ms[0];
+    best = 0;
+    out->level_ms[1] = 1e300;
+    for (int mult : {1, 2, 4}) {
+      h->LW.mode = 1;
+      h->LW.sf_mult = mult;
+      const double ms = time_it(pre);
+      out->level_ms[1] = std::min(out->level_ms[1], ms);
       if (ms < bt) {
         bt = ms;
-        best = mode;
+        best = 1;
+        best_mult = mult;
       }
     }
     if (int rc = level_words_error(h)) return rc;
     h->LW.mode = best;
+    h->LW.sf_mult = best_mult;
     out->level_mode = best;
     out->precond_ms = bt;
   }

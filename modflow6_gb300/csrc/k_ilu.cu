@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(256) k_ilu_sweep_sf(int n, const int *__restri
                                                       const LLWord<T> *__restrict__ yin,
                                                       LLWord<T> *out, T *d,
                                                       unsigned long long *ticket, int *err,
-                                                      Ctl *ctl) {
+                                                      Ctl *ctl, int active) {
   __shared__ unsigned s_ep;
   if (threadIdx.x == 0) {
     // every CTA takes a ticket, so launch e owns tickets [e*grid, (e+1)*grid)
@@ -216,11 +216,15 @@ __global__ void __launch_bounds__(256) k_ilu_sweep_sf(int n, const int *__restri
   }
   __syncthreads();
   if (ctl && ctl->done) return;
+  // the launch always has the same (resident) grid, so that its tickets and
+  // epochs line up with every other launch; CTAs past `active` only take
+  // their ticket
+  if ((int)blockIdx.x >= active) return;
   const unsigned ep = s_ep;
   const int lane = threadIdx.x & 31;
   volatile int *vdone = ctl ? &ctl->done : nullptr;
   constexpr int kDeps = 8;
-  const int stride = gridDim.x * blockDim.x;
+  const int stride = active * blockDim.x;
   for (int q0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); q0 < n; q0 += stride) {
     const int q = q0 + lane;
     bool done = q >= n;
@@ -286,16 +290,22 @@ __global__ void __launch_bounds__(256) k_ilu_sweep_sf(int n, const int *__restri
 // level, so that a thread's next row is about one level ahead of the front
 // (more threads only add threads spinning far ahead of it), and never more
 // CTAs than are resident at once.
+// The launch grid is every CTA that can be resident (always the same, see
+// the kernel); `mult` threads per row of the widest level work, the rest
+// return after their ticket.
 template <typename T, int DIR>
-static int sf_grid(int n, int maxwidth) {
+static int sf_grid() {
   static int per_sm = -1;
   if (per_sm < 0) {
     per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_sweep_sf<T, DIR>, 256, 0);
     per_sm = std::max(1, per_sm);
   }
-  const int want = (std::max(1, std::min(n, maxwidth)) + 255) / 256;
-  return std::max(1, std::min(want, per_sm * kNumSM));
+  return per_sm * kNumSM;
+}
+static int sf_active(int grid, int n, int maxwidth, int mult) {
+  const long long want = ((long long)std::max(1, std::min(n, maxwidth)) * std::max(1, mult) + 255) / 256;
+  return (int)std::max<long long>(1, std::min<long long>(want, grid));
 }
 
 template <typename T>
@@ -304,12 +314,13 @@ static void apply_sf(int n, const int *d_iapc, const int *d_japc, const T *d_apc
                      cudaStream_t st) {
   LLWord<T> *yf = static_cast<LLWord<T> *>(Wd.fwd);
   LLWord<T> *zb = static_cast<LLWord<T> *>(Wd.bwd);
-  k_ilu_sweep_sf<T, 1><<<sf_grid<T, 1>(n, F.maxwidth), 256, 0, st>>>(n, F.d_rows, d_iapc, d_japc, d_apc, r,
-                                                          nullptr, yf, nullptr, Wd.ticket,
-                                                          Wd.err, ctl);
-  k_ilu_sweep_sf<T, -1><<<sf_grid<T, -1>(n, B.maxwidth), 256, 0, st>>>(n, B.d_rows, d_iapc, d_japc, d_apc,
-                                                            nullptr, yf, zb, d, Wd.ticket + 16,
-                                                            Wd.err, ctl);
+  const int gf = sf_grid<T, 1>(), gb = sf_grid<T, -1>();
+  k_ilu_sweep_sf<T, 1><<<gf, 256, 0, st>>>(n, F.d_rows, d_iapc, d_japc, d_apc, r, nullptr, yf,
+                                           nullptr, Wd.ticket, Wd.err, ctl,
+                                           sf_active(gf, n, F.maxwidth, Wd.sf_mult));
+  k_ilu_sweep_sf<T, -1><<<gb, 256, 0, st>>>(n, B.d_rows, d_iapc, d_japc, d_apc, nullptr, yf, zb,
+                                            d, Wd.ticket + 16, Wd.err, ctl,
+                                            sf_active(gb, n, B.maxwidth, Wd.sf_mult));
 }
 
 template <typename T>
