@@ -274,9 +274,10 @@ const char *gbims_status_string(int status);
  * Limit: neq <= 155,648 rows (608 reduction blocks of 256 rows, held in a
  * static device array); larger systems get GBIMS_ERR_ARG.  Runs on `stream`
  * (a cudaStream_t, NULL = the legacy default stream); it copies its three
- * results to the host and synchronizes `stream` before it returns.  The
- * first call on a device looks up the static array and loads the library's
- * device code: make it before any stream capture.  The static array is shared
+ * results to the host and synchronizes `stream` before it returns, so it
+ * must not be called while `stream` is capturing.  The first call on a
+ * device looks up the static array and loads the library's device code:
+ * make it before any stream capture.  The static array is shared
  * by all callers on a device: calls that overlap in time (two host threads,
  * or work on two streams in flight) race on it. */
 int gbims_residual_noalloc(int neq, int nja, const int *d_ia, const int *d_ja,

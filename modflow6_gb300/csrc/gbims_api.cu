@@ -1206,8 +1206,9 @@ extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
   if (!h->structured) {
     // level-scheduled sweeps: one launch per level, or one sync-free launch
     // per sweep
-    // per sweep (the sync-free form also with 1, 2 or 4 threads per row of
-    // the widest level; level_ms[1] is its best)
+    // per sweep (the sync-free form also with 1 to 16 threads per row of
+    // the widest level, as far as the resident grid goes; level_ms[1] is its
+    // best)
     double bt = 1e300;
     int best = 1, best_mult = 1;
     auto pre = [&] {
@@ -1219,7 +1220,7 @@ extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
     bt = out->level_ms[0];
     best = 0;
     out->level_ms[1] = 1e300;
-    for (int mult : {1, 2, 4}) {
+    for (int mult : {1, 2, 4, 8, 16}) {
       h->LW.mode = 1;
       h->LW.sf_mult = mult;
       const double ms = time_it(pre);

@@ -196,7 +196,10 @@ struct alignas(16) Stage<T, C, -1> {
 };
 
 // Warp roles of a sweep CTA.
-enum { kRoleCompute = 0, kRolePre = 1, kRoleCopy = 2, kRoleEdge = 3 };
+// (numbered so that, with two CTAs on an SM, each compute warp shares its
+// sub-partition with the other CTA's edge warp, the lightest role, and each
+// pre-compute warp with the other CTA's copy warp; see the placement below)
+enum { kRoleCompute = 0, kRolePre = 1, kRoleEdge = 2, kRoleCopy = 3 };
 
 // Poll result words of the current epoch, bounded; warp-uniform result.
 // `want` marks the lanes' words still missing (bit t = word t).
@@ -248,12 +251,13 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
     }
     s_m = lo;
     s_abort = 0;
-    // Place the roles on the SM sub-partitions (each has its own FP64
-    // pipe; warp w of the CTA is taken to sit on sub-partition
-    // (slot of warp 0 + w) mod 4): the compute warp on sub-partition 2p and
-    // the pre-compute warp on 2p+1, p the parity of the CTA's 4-slot group,
-    // so that two co-resident CTAs keep their FP64 warps apart.  The roles
-    // are a rotation of the warps in any case.
+    // Place the roles on the SM sub-partitions (each has its own issue
+    // slots and FP64 pipe; warp w of the CTA is taken to sit on
+    // sub-partition (slot of warp 0 + w) mod 4): compute on 2p, pre-compute
+    // on 2p+1, edge on 2p+2 and copy on 2p+3 (mod 4), p the parity of the
+    // CTA's 4-slot group.  Two co-resident CTAs then pair each compute warp
+    // with the other's edge warp and each pre-compute warp with the other's
+    // copy warp.  The roles are a rotation of the warps in any case.
     unsigned hw;
     asm volatile("mov.u32 %0, %%warpid;" : "=r"(hw));
     const int w0 = (int)(hw & 3u), par = (int)((hw >> 2) & 1u);
