@@ -447,10 +447,13 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         dst[t] = (rline && (unsigned)jj < (unsigned)geo.ncol) ? __ldg(rrow + jj) : V(0);
       }
     };
-    V rr[PF][C];
+    // r is loaded PR chunks ahead of its chunk (at least four: under the
+    // load of a full grid its latency reaches several chunks)
+    constexpr int PR = (PF < 4) ? 4 : PF;
+    V rr[PR][C];
     if constexpr (DIR > 0) {
 #pragma unroll
-      for (int j = 0; j < PF; ++j)
+      for (int j = 0; j < PR; ++j)
         if (j < nch) rload(j, rr[j]);
     }
     // chunk q's rv: forward right after its tiles are issued (r has no
@@ -461,7 +464,7 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       if constexpr (DIR > 0) {
 #pragma unroll
         for (int t = 0; t < C; ++t) st.rv[t * W + lane] = E::from_vec(rr[j][t]);
-        if (q + PF < nch) rload(q + PF, rr[j]);
+        if (q + PR < nch) rload(q + PR, rr[j]);
       } else {
         (void)j;
         if (!__all_sync(0xffffffffu, mbar_wait(&full[q % NS], (q / NS) & 1, v_abort))) return false;
@@ -478,9 +481,9 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       if (lane == 0) mbar_arrive(&rdy[q % NS]);
       return true;
     };
-    for (int c0 = 0; ok && c0 < nch; c0 += PF) {
+    for (int c0 = 0; ok && c0 < nch; c0 += PR) {
 #pragma unroll
-    for (int j = 0; j < PF; ++j) {
+    for (int j = 0; j < PR; ++j) {
       const int c = c0 + j;
       if (c >= nch) break;
       const int s = c % NS;
