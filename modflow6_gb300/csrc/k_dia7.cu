@@ -457,8 +457,13 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
         if (j < nch) rload(j, rr[j]);
     }
     // chunk q's rv: forward right after its tiles are issued (r has no
-    // producer in the launch), backward once its tiles have landed (one
-    // chunk behind the copies, so that no wait delays an issue)
+    // producer in the launch), backward once its tiles have landed, LB
+    // chunks behind the copies (half the ring: the copies of LB chunks stay
+    // in flight, and a chunk's tiles have had LB chunks' time to land).
+    // LB <= NS - 1 keeps the waits acyclic: rv of chunk q is made after the
+    // copy of q + LB, which waits for the compute warp's chunk q + LB - NS,
+    // whose rv came LB chunks earlier still.
+    constexpr int LB = (NS / 2 > 1) ? NS / 2 : 1;
     auto make_rv = [&](int q, int j) -> bool {
       St &st = stg[q % NS];
       if constexpr (DIR > 0) {
@@ -520,13 +525,13 @@ __global__ void __launch_bounds__(128) k_dia7_sweep(SweepArgs<T> p) {
       if constexpr (DIR > 0) {
         ok = make_rv(c, j);
       } else {
-        if (c >= 1) ok = make_rv(c - 1, 0);
+        if (c >= LB) ok = make_rv(c - LB, 0);
       }
       if (!ok) break;
     }
     }
     if constexpr (DIR < 0) {
-      if (ok && nch > 0) ok = make_rv(nch - 1, 0);
+      for (int q = max(0, nch - LB); ok && q < nch; ++q) ok = make_rv(q, 0);
     }
     if (!ok) fail();
     if (lane == 0) {
