@@ -202,16 +202,24 @@ struct alignas(16) Stage<T, C, -1> {
 enum { kRoleCompute = 0, kRolePre = 1, kRoleEdge = 2, kRoleCopy = 3 };
 
 // Poll result words of the current epoch, bounded; warp-uniform result.
-// `want` marks the lanes' words still missing (bit t = word t).
+// `want` marks the lanes' words still missing (bit t = word t).  A round
+// issues the loads of all missing words before it looks at any of them, so
+// that their round trips overlap.
 template <typename T, int C>
 __device__ __forceinline__ bool ll_poll(const LLWord<T> *q, long long stride, unsigned want,
                                         unsigned ep, T (&v)[C], volatile int *abort_flag) {
   unsigned long long t0 = 0;
   while (true) {
+    LLRaw r[C];
 #pragma unroll
     for (int t = 0; t < C; ++t)
-      if ((want >> t) & 1u)
-        if (ll_get(q + t * stride, ep, v[t])) want &= ~(1u << t);
+      if ((want >> t) & 1u) ll_issue(q + t * stride, r[t]);
+#pragma unroll
+    for (int t = 0; t < C; ++t)
+      if (((want >> t) & 1u) && ll_ready<T>(r[t], ep)) {
+        ll_take(r[t], v[t]);
+        want &= ~(1u << t);
+      }
     if (!__any_sync(0xffffffffu, want != 0)) return true;
     if (t0 == 0) t0 = wclock();
     if (__any_sync(0xffffffffu, *abort_flag != 0 || wclock() - t0 > kWaitCycles)) return false;
