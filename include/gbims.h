@@ -382,6 +382,33 @@ typedef struct gbsln_stats {
 int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,
                  const gbims_settings *ims, const gbsln_nonlinear *nl,
                  const double *strt, gbsln_handle **out);
+
+/* A grid given by its connectivity: a DISV or DISU grid (or DIS written out
+ * this way), in the form Connections.f90 keeps it (con_finalize, :160-316),
+ * all 0-based.  ia/ja is the symmetric CSR pattern with each row's diagonal
+ * first and the off-diagonals ascending; ihc, cl1, cl2 and hwva hold one
+ * value per connection n < m, numbered in row order of the upper triangle
+ * (the reference's JAS numbering): ihc 0 vertical, 1 horizontal, 2
+ * horizontal between vertically staggered cells; cl1 the distance from n,
+ * cl2 from m, to the shared face; hwva the face area (ihc 0) or width. */
+typedef struct gbsln_grid {
+  int nodes, nja;
+  const int *ia, *ja;               /* nodes+1, nja */
+  const int *ihc;                   /* (nja - nodes)/2 */
+  const double *cl1, *cl2, *hwva;   /* (nja - nodes)/2 */
+  const double *top, *bot, *area;   /* nodes */
+} gbsln_grid;
+
+/* gbsln_create on a grid given by its connectivity.  The model's K,
+ * ICELLTYPE, storage and boundaries are read from `model` (its nlay, nrow,
+ * ncol, delr, delc, top and botm are not read).  The solve takes the
+ * general-pattern path (SELL-32 product, level-scheduled ILU0).  The checks
+ * of con_finalize are made (diagonal first, ascending rows, every
+ * connection with its counterpart, ihc in 0..2): GBIMS_ERR_ARG with the
+ * reason in gbsln_last_error. */
+int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *model,
+                      const gbnpf_options *npf, const gbims_settings *ims,
+                      const gbsln_nonlinear *nl, const double *strt, gbsln_handle **out);
 /* One time step (prepareSolve + outer loop).  The step is transient when the
  * model has ss/sy and delt > 0, steady state otherwise; delt is also the
  * step length used by the pseudo-transient continuation default

@@ -73,6 +73,13 @@ class GbslnModel(C.Structure):
     ]
 
 
+class GbslnGrid(C.Structure):
+    _fields_ = [
+        ("nodes", C.c_int), ("nja", C.c_int), ("ia", _ip), ("ja", _ip), ("ihc", _ip),
+        ("cl1", _dp), ("cl2", _dp), ("hwva", _dp), ("top", _dp), ("bot", _dp), ("area", _dp),
+    ]
+
+
 class GbslnNonlinear(C.Structure):
     _fields_ = [
         ("dvclose", C.c_double), ("mxiter", C.c_int), ("nonmeth", C.c_int),
@@ -150,6 +157,9 @@ _SIGS = {
     "gbnpf_destroy": (C.c_int, [C.c_void_p]),
     "gbsln_create": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbnpfOptions), C.POINTER(GbimsSettings),
                                C.POINTER(GbslnNonlinear), _dp, C.POINTER(C.c_void_p)]),
+    "gbsln_create_grid": (C.c_int, [C.POINTER(GbslnGrid), C.POINTER(GbslnModel), C.POINTER(GbnpfOptions),
+                                    C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,
+                                    C.POINTER(C.c_void_p)]),
     "gbsln_timestep": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.POINTER(GbslnStats)]),
     "gbsln_timestep_guess": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_void_p,
                                        C.POINTER(GbslnStats)]),

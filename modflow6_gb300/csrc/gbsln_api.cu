@@ -243,6 +243,7 @@ struct gbsln_handle {
          *dxold = nullptr, *part = nullptr, *bnd_val = nullptr, *chd_head = nullptr;
   int *ibound = nullptr, *bnd_ptr = nullptr, *chd_node = nullptr, *flag = nullptr;
   int *bnd_kind = nullptr;  // per boundary entry: 0 WEL, 1 RCH
+  int *ibotnode = nullptr;  // NEWTON UNDER_RELAXATION: the lowest cell below each cell
   double *galpha = nullptr; // the last warm step's projection factors (2)
   double *dprev = nullptr;  // the last step's head change (valid when have_prev)
   double *gpart = nullptr;  // projection partials (5 per block)
@@ -394,38 +395,41 @@ __global__ void k_set_chd(int nchd, const int *__restrict__ node, const double *
   }
 }
 
-extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
-                            const gbims_settings *ims, const gbsln_nonlinear *nl,
-                            const double *strt, gbsln_handle **out) {
-  if (!out) return GBIMS_ERR_ARG;
-  *out = nullptr;
-  if (!m || !npf || !ims || !nl || !strt || m->nlay <= 0 || m->nrow <= 0 || m->ncol <= 0 ||
-      !m->delr || !m->delc || !m->top || !m->botm || !m->k11 || !m->k33 || !m->icelltype)
-    return GBIMS_ERR_ARG;
-  gbsln_handle *h = new (std::nothrow) gbsln_handle();
-  if (!h) return GBIMS_ERR_NOMEM;
-  *out = h;
-  h->nlay = m->nlay; h->nrow = m->nrow; h->ncol = m->ncol;
-  const long long nrc = (long long)m->nrow * m->ncol;
-  const long long nn = nrc * m->nlay;
-  if (nn > 400000000LL) { h->err = "grid too large"; return GBIMS_ERR_UNSUPPORTED; }
-  const int n = (int)nn;
-  h->n = n;
-  h->nl = *nl;
-  h->ims_s = *ims;
-  h->ims_s.index_base = 0;
-  h->ims_s.nlay = m->nlay; h->ims_s.nrow = m->nrow; h->ims_s.ncol = m->ncol;
-  // cell geometry (Dis.f90: top of layer 1 is TOP, of layer k>1 the bottom above)
-  std::vector<double> top(n), bot(m->botm, m->botm + n), area(n), vol(n);
-  for (long long p = 0; p < nn; ++p) {
-    top[p] = (p < nrc) ? m->top[p] : m->botm[p - nrc];
-    long long rem = p % nrc;
-    int i = (int)(rem / m->ncol), j = (int)(rem % m->ncol);
-    area[p] = m->delc[i] * m->delr[j];
-    vol[p] = area[p] * (top[p] - bot[p]);
+namespace {
+
+// The lowest cell reached from each cell by following, from cell to cell,
+// the vertical connection to a higher-numbered cell with the lowest bottom
+// (gwf-npf.f90:1904-1939, the cell NEWTON UNDER_RELAXATION relaxes toward).
+std::vector<int> bottom_nodes(int n, const Conn &c, const std::vector<double> &bot) {
+  std::vector<int> ib(n);
+  for (int p = 0; p < n; ++p) {
+    double minbot = bot[p];
+    int nn = p;
+    for (;;) {
+      int next = -1;
+      for (int q = c.ia[nn] + 1; q < c.ia[nn + 1]; ++q) {
+        const int m = c.ja[q];
+        if (c.ihc[c.jas[q]] == 0 && m > nn && bot[m] < minbot) {
+          next = m;
+          minbot = bot[m];
+        }
+      }
+      if (next < 0) break;
+      nn = next;
+    }
+    ib[p] = nn;
   }
-  Conn c;
-  build_connections(m->nlay, m->nrow, m->ncol, m->delr, m->delc, top, bot, c);
+  return ib;
+}
+
+// Everything of gbsln_create after the grid: boundaries, device arrays,
+// the IMS handle and the saturated conductances.
+int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, const double *strt,
+              const Conn &c, const std::vector<double> &top, const std::vector<double> &bot,
+              const std::vector<double> &area) {
+  const int n = h->n;
+  std::vector<double> vol(n);
+  for (int p = 0; p < n; ++p) vol[p] = area[p] * (top[p] - bot[p]);
   h->nja = (int)c.ja.size();
   std::vector<int> ibound(n, 1);
   for (int i = 0; i < m->nchd; ++i) {
@@ -455,6 +459,7 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
     }
   }
   bptr[n] = (int)bval.size();
+  h->inewtonur = npf->inewton && npf->inewtonur;
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
   chk(up(&h->d.ia, c.ia.data(), c.ia.size()));
@@ -472,6 +477,10 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
   chk(up(&h->d.icelltype, m->icelltype, (size_t)n));
   chk(up<double>(&h->d.condsat, nullptr, c.cl1.size()));
   chk(up<double>(&h->d.sat, nullptr, (size_t)n));
+  if (h->inewtonur) {
+    std::vector<int> ib = bottom_nodes(n, c, bot);
+    chk(up(&h->ibotnode, ib.data(), ib.size()));
+  }
   h->has_sto = (m->ss != nullptr && m->sy != nullptr);
   if (h->has_sto) {
     chk(up(&h->ss, m->ss, (size_t)n));
@@ -516,12 +525,127 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
   h->g.idewatcv = npf->idewatcv;
   h->g.icellavg = npf->icellavg;
   h->g.satomega = npf->satomega > 0 ? npf->satomega : 1.0e-6;
-  h->inewtonur = npf->inewton && npf->inewtonur;
   SLN_CUDA(h, cudaMemcpyAsync(h->x, strt, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
   gwf_condsat(n, h->g, h->d.condsat, h->st);
   SLN_CUDA(h, cudaStreamSynchronize(h->st));
   SLN_CUDA(h, cudaGetLastError());
   return GBIMS_OK;
+}
+
+bool model_props_ok(const gbsln_model *m) {
+  return m->k11 && m->k33 && m->icelltype && m->nchd >= 0 && m->nwel >= 0 && m->nrch >= 0 &&
+         (m->nchd == 0 || (m->chd_node && m->chd_head)) &&
+         (m->nwel == 0 || (m->wel_node && m->wel_q)) &&
+         (m->nrch == 0 || (m->rch_node && m->rch_rate));
+}
+
+}  // namespace
+
+extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
+                            const gbims_settings *ims, const gbsln_nonlinear *nl,
+                            const double *strt, gbsln_handle **out) {
+  if (!out) return GBIMS_ERR_ARG;
+  *out = nullptr;
+  if (!m || !npf || !ims || !nl || !strt || m->nlay <= 0 || m->nrow <= 0 || m->ncol <= 0 ||
+      !m->delr || !m->delc || !m->top || !m->botm || !model_props_ok(m))
+    return GBIMS_ERR_ARG;
+  gbsln_handle *h = new (std::nothrow) gbsln_handle();
+  if (!h) return GBIMS_ERR_NOMEM;
+  *out = h;
+  h->nlay = m->nlay; h->nrow = m->nrow; h->ncol = m->ncol;
+  const long long nrc = (long long)m->nrow * m->ncol;
+  const long long nn = nrc * m->nlay;
+  if (nn > 400000000LL) { h->err = "grid too large"; return GBIMS_ERR_UNSUPPORTED; }
+  const int n = (int)nn;
+  h->n = n;
+  h->nl = *nl;
+  h->ims_s = *ims;
+  h->ims_s.index_base = 0;
+  h->ims_s.nlay = m->nlay; h->ims_s.nrow = m->nrow; h->ims_s.ncol = m->ncol;
+  // cell geometry (Dis.f90: top of layer 1 is TOP, of layer k>1 the bottom above)
+  std::vector<double> top(n), bot(m->botm, m->botm + n), area(n);
+  for (long long p = 0; p < nn; ++p) {
+    top[p] = (p < nrc) ? m->top[p] : m->botm[p - nrc];
+    long long rem = p % nrc;
+    int i = (int)(rem / m->ncol), j = (int)(rem % m->ncol);
+    area[p] = m->delc[i] * m->delr[j];
+  }
+  Conn c;
+  build_connections(m->nlay, m->nrow, m->ncol, m->delr, m->delc, top, bot, c);
+  return sln_setup(h, m, npf, strt, c, top, bot, area);
+}
+
+extern "C" int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *m,
+                                 const gbnpf_options *npf, const gbims_settings *ims,
+                                 const gbsln_nonlinear *nl, const double *strt,
+                                 gbsln_handle **out) {
+  if (!out) return GBIMS_ERR_ARG;
+  *out = nullptr;
+  if (!grid || !m || !npf || !ims || !nl || !strt || grid->nodes <= 0 ||
+      grid->nja < grid->nodes || !grid->ia || !grid->ja || !grid->ihc || !grid->cl1 ||
+      !grid->cl2 || !grid->hwva || !grid->top || !grid->bot || !grid->area ||
+      !model_props_ok(m))
+    return GBIMS_ERR_ARG;
+  gbsln_handle *h = new (std::nothrow) gbsln_handle();
+  if (!h) return GBIMS_ERR_NOMEM;
+  *out = h;
+  const int n = grid->nodes, nja = grid->nja;
+  h->n = n;
+  h->nl = *nl;
+  h->ims_s = *ims;
+  h->ims_s.index_base = 0;
+  h->ims_s.nlay = 0; h->ims_s.nrow = 0; h->ims_s.ncol = 0;  // the general-pattern path
+  if (grid->ia[0] != 0 || grid->ia[n] != nja) { h->err = "IA does not span JA"; return GBIMS_ERR_ARG; }
+  Conn c;
+  c.ia.assign(grid->ia, grid->ia + n + 1);
+  c.ja.assign(grid->ja, grid->ja + nja);
+  // con_finalize's checks (Connections.f90:203-247): the diagonal first,
+  // the off-diagonals ascending, every connection with its counterpart
+  for (int p = 0; p < n; ++p) {
+    if (c.ia[p + 1] <= c.ia[p] || c.ja[c.ia[p]] != p) {
+      h->err = "JA: the first entry of row " + std::to_string(p) + " is not its diagonal";
+      return GBIMS_ERR_ARG;
+    }
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
+      const int m2 = c.ja[q];
+      if (m2 < 0 || m2 >= n || m2 == p || (q + 1 < c.ia[p + 1] && m2 >= c.ja[q + 1])) {
+        h->err = "JA: row " + std::to_string(p) + " is not sorted or names a bad node";
+        return GBIMS_ERR_ARG;
+      }
+    }
+  }
+  // fillisym / filljas (Connections.f90:1205-1268), 0-based
+  c.isym.assign(nja, -1);
+  c.jas.assign(nja, -1);
+  for (int p = 0; p < n; ++p)
+    for (int q = c.ia[p]; q < c.ia[p + 1]; ++q) {
+      const int m2 = c.ja[q];
+      if (m2 == p) { c.isym[q] = q; continue; }
+      for (int r = c.ia[m2]; r < c.ia[m2 + 1]; ++r)
+        if (c.ja[r] == p) { c.isym[q] = r; break; }
+      if (c.isym[q] < 0) {
+        h->err = "JA: connection " + std::to_string(p) + "-" + std::to_string(m2) +
+                 " has no symmetric counterpart";
+        return GBIMS_ERR_ARG;
+      }
+    }
+  int ipos = 0;
+  for (int p = 0; p < n; ++p)
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q)
+      if (c.ja[q] > p) c.jas[q] = ipos++;
+  for (int p = 0; p < n; ++p)
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q)
+      if (c.ja[q] < p) c.jas[q] = c.jas[c.isym[q]];
+  c.njas = ipos;
+  c.ihc.assign(grid->ihc, grid->ihc + ipos);
+  for (int s2 = 0; s2 < ipos; ++s2)
+    if (c.ihc[s2] < 0 || c.ihc[s2] > 2) { h->err = "IHC must be 0, 1, or 2"; return GBIMS_ERR_ARG; }
+  c.cl1.assign(grid->cl1, grid->cl1 + ipos);
+  c.cl2.assign(grid->cl2, grid->cl2 + ipos);
+  c.hwva.assign(grid->hwva, grid->hwva + ipos);
+  std::vector<double> top(grid->top, grid->top + n), bot(grid->bot, grid->bot + n),
+      area(grid->area, grid->area + n);
+  return sln_setup(h, m, npf, strt, c, top, bot, area);
 }
 
 static int read_dxmax(gbsln_handle *h, double *hncg, int *loc) {
@@ -797,8 +921,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
       }
       if (h->inewtonur) {  // gwf_nur (gwf.f90:717): NEWTON UNDER_RELAXATION only
         SLN_CUDA(h, cudaMemsetAsync(h->flag, 0, sizeof(int), h->st));
-        gwf_npf_nur(n, (int)((long long)h->nrow * h->ncol), h->nlay, h->g, h->ibound, h->x,
-                    h->xtemp, h->dxold, h->flag, h->st);
+        gwf_npf_nur(n, h->ibotnode, h->g, h->ibound, h->x, h->xtemp, h->dxold, h->flag, h->st);
         int flag = 0;
         SLN_CUDA(h, cudaMemcpyAsync(&flag, h->flag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
         SLN_CUDA(h, cudaStreamSynchronize(h->st));
@@ -973,7 +1096,7 @@ extern "C" int gbsln_destroy(gbsln_handle *h) {
   h->d.release();
   void *p[] = {h->strt, h->ss, h->sy, h->area, h->vol, h->xold, h->xtemp, h->wsave, h->hchold, h->deold,
                h->dxold, h->part, h->bnd_val, h->chd_head, h->ibound, h->bnd_ptr, h->chd_node,
-               h->bnd_kind, h->bpart,
+               h->bnd_kind, h->bpart, h->ibotnode,
                h->flag, h->galpha, h->dprev, h->gpart};
   for (void *q : p)
     if (q) cudaFree(q);

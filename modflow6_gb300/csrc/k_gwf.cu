@@ -51,19 +51,36 @@ __device__ double d_condmean(double k1, double k2, double thick1, double thick2,
   }
 }
 
-// GwfConductanceUtils.f90:43-145, hcond (ihc 1)
-__device__ double d_hcond(int ibdn, int ibdm, int ictn, int ictm, int iupstream, int icellavg,
-                          double condsat, double hn, double hm, double satn, double satm,
-                          double hkn, double hkm, double topn, double topm, double botn,
-                          double botm, double cln, double clm, double fawidth) {
+// GwfConductanceUtils.f90:375-393, staggered_thkfrac: the wetted part of a
+// cell that lies within the vertical overlap (sill) of the two cells
+__device__ double d_staggered_thk(double top, double bot, double sat, double topc,
+                                  double botc) {
+  const double sill_top = fmin(top, topc);
+  const double sill_bot = fmax(bot, botc);
+  const double tp = DADD(bot, DMUL(sat, DSUB(top, bot)));
+  return fmax(DSUB(fmin(tp, sill_top), sill_bot), 0.0);
+}
+
+// GwfConductanceUtils.f90:43-145, hcond and convertible_standard; ihc 2 is a
+// horizontal connection between vertically staggered cells
+__device__ double d_hcond(int ibdn, int ibdm, int ictn, int ictm, int iupstream, int ihc,
+                          int icellavg, double condsat, double hn, double hm, double satn,
+                          double satm, double hkn, double hkm, double topn, double topm,
+                          double botn, double botm, double cln, double clm, double fawidth) {
   if (ibdn == 0 || ibdm == 0) return 0.0;
   if (ictn == 0 && ictm == 0) return condsat;
   if (iupstream == 1) {
     double sat_up = (hn > hm) ? satn : satm;
     return DMUL(sat_up, condsat);
   }
-  double thksatn = DMUL(satn, DSUB(topn, botn));
-  double thksatm = DMUL(satm, DSUB(topm, botm));
+  double thksatn, thksatm;
+  if (ihc == 2) {
+    thksatn = d_staggered_thk(topn, botn, satn, topm, botm);
+    thksatm = d_staggered_thk(topm, botm, satm, topn, botn);
+  } else {
+    thksatn = DMUL(satn, DSUB(topn, botn));
+    thksatm = DMUL(satm, DSUB(topm, botm));
+  }
   return d_condmean(hkn, hkm, thksatn, thksatm, cln, clm, fawidth, icellavg);
 }
 
@@ -136,7 +153,7 @@ __global__ void k_condsat(int nodes, NpfDev g, double *condsat) {
         csat = d_vcond(1, 1, 1, 1, 1, 1, 1.0, g.bot[n], g.bot[m], g.k33[n], g.k33[m], 1.0, 1.0,
                        g.top[n], g.top[m], g.bot[n], g.bot[m], g.hwva[jj]);
       } else {
-        csat = d_hcond(1, 1, 1, 1, 0, g.icellavg, 1.0, g.top[n], g.top[m], 1.0, 1.0, g.k11[n],
+        csat = d_hcond(1, 1, 1, 1, 0, g.ihc[jj], g.icellavg, 1.0, g.top[n], g.top[m], 1.0, 1.0, g.k11[n],
                        g.k11[m], g.top[n], g.top[m], g.bot[n], g.bot[m], g.cl1[jj], g.cl2[jj],
                        g.hwva[jj]);
       }
@@ -173,7 +190,8 @@ __device__ __forceinline__ double conn_cond(const NpfDev &g, const int *ibound, 
                    condsat[jj], h[n], h[m], g.k33[n], g.k33[m], sat[n], sat[m], g.top[n],
                    g.top[m], g.bot[n], g.bot[m], g.hwva[jj]);
   }
-  return d_hcond(ibound[n], ibound[m], g.icelltype[n], g.icelltype[m], g.inewton, g.icellavg,
+  return d_hcond(ibound[n], ibound[m], g.icelltype[n], g.icelltype[m], g.inewton, g.ihc[jj],
+                 g.icellavg,
                  condsat[jj], h[n], h[m], sat[n], sat[m], g.k11[n], g.k11[m], g.top[n],
                  g.top[m], g.bot[n], g.bot[m], g.cl1[jj], g.cl2[jj], g.hwva[jj]);
 }
@@ -252,9 +270,16 @@ __global__ void k_gwf_fill(int nodes, NpfDev g, FillDev f, const int *__restrict
         int iups = (h[m] < h[n]) ? n : m;
         int idn = (iups == n) ? m : n;
         if (g.icelltype[iups] == 0) continue;
+        // the upstream cell's top and bottom; for a staggered connection the
+        // overlap of the two cells
+        double topup = g.top[iups], botup = g.bot[iups];
+        if (g.ihc[jj] == 2) {
+          topup = fmin(g.top[n], g.top[m]);
+          botup = fmax(g.bot[n], g.bot[m]);
+        }
         double cond = condsat[jj];
         double consterm = DMUL(-cond, DSUB(h[iups], h[idn]));
-        double derv = d_sqsat_derv(g.top[iups], g.bot[iups], h[iups], g.satomega);
+        double derv = d_sqsat_derv(topup, botup, h[iups], g.satomega);
         if (p == n) {  // p is the lower-numbered end: the "n" updates
           if (iups == n) {
             double term = DMUL(consterm, derv);
@@ -613,12 +638,13 @@ __global__ void k_calcdx(int nodes, const int *__restrict__ active, const double
 }
 
 // npf_nur (gwf-npf.f90:705-741); flag[0] set when any cell was relaxed.
-__global__ void k_npf_nur(int nodes, int nrc, int nlay, NpfDev g, const int *__restrict__ ibound,
-                          double *x, const double *__restrict__ xtemp, double *dx, int *flag) {
+// ibotnode: the lowest cell below each cell (gwf-npf.f90:1904-1939).
+__global__ void k_npf_nur(int nodes, const int *__restrict__ ibotnode, NpfDev g,
+                          const int *__restrict__ ibound, double *x,
+                          const double *__restrict__ xtemp, double *dx, int *flag) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nodes; n += gridDim.x * blockDim.x) {
     if (ibound[n] < 1 || g.icelltype[n] <= 0) continue;
-    int ibot = (nlay - 1) * nrc + (n % nrc);
-    double botm = g.bot[ibot];
+    double botm = g.bot[ibotnode[n]];
     if (x[n] < botm) {
       flag[0] = 1;
       x[n] = DADD(DMUL(xtemp[n], DSUB(1.0, 0.9)), DMUL(botm, 0.9));
@@ -678,9 +704,9 @@ void gwf_calcdx(int nodes, const int *active, const double *x, const double *xte
                 cudaStream_t st) {
   k_calcdx<<<g_grid(nodes), 256, 0, st>>>(nodes, active, x, xtemp, dx);
 }
-void gwf_npf_nur(int nodes, int nrc, int nlay, const NpfDev &g, const int *ibound, double *x,
+void gwf_npf_nur(int nodes, const int *ibotnode, const NpfDev &g, const int *ibound, double *x,
                  const double *xtemp, double *dx, int *flag, cudaStream_t st) {
-  k_npf_nur<<<g_grid(nodes), 256, 0, st>>>(nodes, nrc, nlay, g, ibound, x, xtemp, dx, flag);
+  k_npf_nur<<<g_grid(nodes), 256, 0, st>>>(nodes, ibotnode, g, ibound, x, xtemp, dx, flag);
 }
 
 // apply_backtracking (NumericalSolution.f90:2823-2838), the same two

@@ -50,7 +50,7 @@ void gwf_relax_scale(int nodes, double relax, const int *active, double *x, cons
                      double *dxold, cudaStream_t st);
 void gwf_calcdx(int nodes, const int *active, const double *x, const double *xtemp, double *dx,
                 cudaStream_t st);
-void gwf_npf_nur(int nodes, int nrc, int nlay, const NpfDev &g, const int *ibound, double *x,
+void gwf_npf_nur(int nodes, const int *ibotnode, const NpfDev &g, const int *ibound, double *x,
                  const double *xtemp, double *dx, int *flag, cudaStream_t st);
 // apply_backtracking: x = xtemp + breduc * (x - xtemp) on active cells
 void gwf_backtrack(int nodes, double breduc, const int *active, double *x, const double *xtemp,

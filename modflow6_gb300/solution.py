@@ -1,4 +1,6 @@
-"""Device-resident NumericalSolution for one GWF DIS model (gbsln_* C ABI).
+"""Device-resident NumericalSolution for one GWF model (gbsln_* C ABI) on a
+DIS grid, or on a DISV or DISU grid through its connectivity
+(gbsln_create_grid).
 
 `GwfSolution` mirrors the per-time-step use of NumericalSolutionType
 (src/Solution/NumericalSolution.f90: sln_ca :1287, solve :1482-1837) for a
@@ -132,8 +134,21 @@ class GwfSolution:
                  satomega: float = 1.0e-6):
         lib = _lib.load()
         self.m = m
-        keep = dict(delr=_f(m.delr), delc=_f(m.delc), top=_f(m.top), botm=_f(m.botm),
-                    k11=_f(m.k11), k33=_f(m.k33), ict=_i(m.icelltype),
+        general = bool(getattr(m, "disv", False) or getattr(m, "disu", False))
+        if general:
+            con = m.connections()
+            keep = dict(delr=_f([0.0]), delc=_f([0.0]), top=_f([0.0]), botm=_f([0.0]),
+                        g_ia=_i(con["ia"]), g_ja=_i(con["ja"]), g_ihc=_i(con["ihc"]),
+                        g_cl1=_f(con["cl1"]), g_cl2=_f(con["cl2"]), g_hwva=_f(con["hwva"]),
+                        g_top=_f(m.cell_top), g_bot=_f(m.cell_bot), g_area=_f(m.area))
+            grid = _lib.GbslnGrid(int(m.nodes), int(con["nja"]), _lib.iptr(keep["g_ia"]),
+                                  _lib.iptr(keep["g_ja"]), _lib.iptr(keep["g_ihc"]),
+                                  _lib.dptr(keep["g_cl1"]), _lib.dptr(keep["g_cl2"]),
+                                  _lib.dptr(keep["g_hwva"]), _lib.dptr(keep["g_top"]),
+                                  _lib.dptr(keep["g_bot"]), _lib.dptr(keep["g_area"]))
+        else:
+            keep = dict(delr=_f(m.delr), delc=_f(m.delc), top=_f(m.top), botm=_f(m.botm))
+        keep.update(k11=_f(m.k11), k33=_f(m.k33), ict=_i(m.icelltype),
                     chd_node=_i(m.chd_node), chd_head=_f(m.chd_head), wel_node=_i(m.wel_node),
                     wel_q=_f(m.wel_q), rch_node=_i(m.rch_node), rch_rate=_f(m.rch_rate),
                     strt=_f(m.strt))
@@ -155,8 +170,12 @@ class GwfSolution:
                                   nl.amomentum, nl.iallowptc, nl.numtrack, nl.btol, nl.breduc,
                                   nl.res_lim)
         self._h = C.c_void_p()
-        rc = lib.gbsln_create(C.byref(cm), C.byref(npf), C.byref(cs), C.byref(cnl),
-                              _lib.dptr(keep["strt"]), C.byref(self._h))
+        if general:
+            rc = lib.gbsln_create_grid(C.byref(grid), C.byref(cm), C.byref(npf), C.byref(cs),
+                                       C.byref(cnl), _lib.dptr(keep["strt"]), C.byref(self._h))
+        else:
+            rc = lib.gbsln_create(C.byref(cm), C.byref(npf), C.byref(cs), C.byref(cnl),
+                                  _lib.dptr(keep["strt"]), C.byref(self._h))
         if rc < 0:
             msg = lib.gbsln_last_error(self._h).decode() if self._h else ""
             lib.gbsln_destroy(self._h)

@@ -151,10 +151,20 @@ static double condmean(double k1, double k2, double thick1, double thick2, doubl
   }
 }
 
-/* GwfConductanceUtils.f90:43-145, hcond (ihc 1 only; no staggered). */
-static double hcond(int ibdn, int ibdm, int ictn, int ictm, int iupstream, int icellavg,
-                    double condsat, double hn, double hm, double satn, double satm,
-                    double hkn, double hkm, double topn, double topm, double botn,
+/* GwfConductanceUtils.f90:375-393, staggered_thkfrac. */
+static double staggered_thkfrac(double top, double bot, double sat, double topc, double botc) {
+  double sill_top = (top < topc) ? top : topc;
+  double sill_bot = (bot > botc) ? bot : botc;
+  double tp = bot + sat * (top - bot);
+  double t = ((tp < sill_top) ? tp : sill_top) - sill_bot;
+  return (t > 0.0) ? t : 0.0;
+}
+
+/* GwfConductanceUtils.f90:43-145, hcond with convertible_standard (ihc 2:
+ * vertically staggered cells). */
+static double hcond(int ibdn, int ibdm, int ictn, int ictm, int iupstream, int ihc,
+                    int icellavg, double condsat, double hn, double hm, double satn,
+                    double satm, double hkn, double hkm, double topn, double topm, double botn,
                     double botm, double cln, double clm, double fawidth) {
   if (ibdn == 0 || ibdm == 0) return 0.0;
   if (ictn == 0 && ictm == 0) return condsat;
@@ -162,8 +172,14 @@ static double hcond(int ibdn, int ibdm, int ictn, int ictm, int iupstream, int i
     double sat_up = (hn > hm) ? satn : satm;
     return sat_up * condsat;
   }
-  double thksatn = satn * (topn - botn);
-  double thksatm = satm * (topm - botm);
+  double thksatn, thksatm;
+  if (ihc == 2) {
+    thksatn = staggered_thkfrac(topn, botn, satn, topm, botm);
+    thksatm = staggered_thkfrac(topm, botm, satm, topn, botn);
+  } else {
+    thksatn = satn * (topn - botn);
+    thksatm = satm * (topm - botm);
+  }
   return condmean(hkn, hkm, thksatn, thksatm, cln, clm, fawidth, icellavg);
 }
 
@@ -229,6 +245,143 @@ double or_squadratic_sat_derv(double top, double bot, double x, double eps) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* DISU connectivity                                                         */
+/* ------------------------------------------------------------------------ */
+
+static int cmp_int(const void *a, const void *b);
+
+/* disuconnections (Connections.f90:801-928) then con_finalize (:160-316),
+ * 0-based.  A full grid copies IA/JA; a reduced one builds each kept row as
+ * the sparse matrix does (the diagonal, then every kept neighbour once, the
+ * neighbours sorted, Sparse.f90:217-239) and compresses the per-entry arrays
+ * in input order. */
+int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int *ihcinp,
+                    const double *cl12inp, const double *hwvainp, const int *nodereduced,
+                    int cap, int *nodes_out, int *ia, int *ja, int *isym, int *jas, int *ihc,
+                    double *cl1, double *cl2, double *hwva) {
+  int nodes = nodesuser;
+  if (nodereduced) {
+    nodes = 0;
+    for (int u = 0; u < nodesuser; ++u)
+      if (nodereduced[u] >= 0) nodes++;
+  }
+  *nodes_out = nodes;
+  if (nodes == 0) return -8;
+  int nja = 0;
+  double *cl12t = NULL, *hwvat = NULL;
+  int *ihcti = NULL;
+  if (!nodereduced) {
+    nja = iainp[nodesuser];
+    if (nja > cap) return -1;
+    ihcti = (int *)malloc(sizeof(int) * (nja + 1));
+    cl12t = (double *)malloc(sizeof(double) * (nja + 1));
+    hwvat = (double *)malloc(sizeof(double) * (nja + 1));
+    for (int n = 0; n <= nodes; ++n) ia[n] = iainp[n];
+    for (int q = 0; q < nja; ++q) {
+      int v = jainp[q];
+      ja[q] = (v < 0 ? -v : v) - 1; /* negative JA made positive */
+      ihcti[q] = ihcinp[q];
+      cl12t[q] = cl12inp[q];
+      hwvat[q] = hwvainp[q];
+    }
+  } else {
+    /* rows of the sparse matrix, in reduced order */
+    int total = 0;
+    ia[0] = 0;
+    for (int u = 0; u < nodesuser; ++u) {
+      int nr = nodereduced[u];
+      if (nr < 0) continue;
+      int start = total;
+      if (total >= cap) return -1;
+      ja[total++] = nr;
+      for (int q = iainp[u] + 1; q < iainp[u + 1]; ++q) {
+        int mu = (jainp[q] < 0 ? -jainp[q] : jainp[q]) - 1;
+        int mr = nodereduced[mu];
+        if (mr < 0) continue;
+        int dup = 0;
+        for (int t = start; t < total; ++t)
+          if (ja[t] == mr) dup = 1;
+        if (dup) continue;
+        if (total >= cap) return -1;
+        ja[total++] = mr;
+      }
+      qsort(ja + start + 1, total - start - 1, sizeof(int), cmp_int);
+      ia[nr + 1] = total;
+    }
+    nja = total;
+    ihcti = (int *)malloc(sizeof(int) * (nja + 1));
+    cl12t = (double *)malloc(sizeof(double) * (nja + 1));
+    hwvat = (double *)malloc(sizeof(double) * (nja + 1));
+    int iposr = 0;
+    for (int u = 0; u < nodesuser; ++u) {
+      int nr = nodereduced[u];
+      for (int q = iainp[u]; q < iainp[u + 1]; ++q) {
+        int mu = (jainp[q] < 0 ? -jainp[q] : jainp[q]) - 1;
+        int mr = nodereduced[mu];
+        if (nr < 0 || mr < 0) continue;
+        if (iposr >= nja) { /* a duplicated entry: the arrays would overrun */
+          free(ihcti); free(cl12t); free(hwvat);
+          return -3;
+        }
+        ihcti[iposr] = ihcinp[q];
+        cl12t[iposr] = cl12inp[q];
+        hwvat[iposr] = hwvainp[q];
+        iposr++;
+      }
+    }
+  }
+  int rc = nja;
+  /* con_finalize: the diagonal first, the rest ascending */
+  for (int n = 0; n < nodes && rc >= 0; ++n) {
+    if (ja[ia[n]] != n) rc = -2;
+    for (int q = ia[n] + 1; q < ia[n + 1] - 1 && rc >= 0; ++q)
+      if (ja[q] > ja[q + 1]) rc = -3;
+  }
+  /* fillisym */
+  for (int n = 0; n < nodes && rc >= 0; ++n)
+    for (int q = ia[n]; q < ia[n + 1]; ++q) {
+      int m = ja[q];
+      if (m == n) { isym[q] = q; continue; }
+      isym[q] = -1;
+      for (int r = ia[m]; r < ia[m + 1]; ++r)
+        if (ja[r] == n) { isym[q] = r; break; }
+      if (isym[q] < 0) rc = -4;
+    }
+  if (rc >= 0) {
+    /* filljas */
+    int ipos = 0;
+    for (int n = 0; n < nodes; ++n) {
+      jas[ia[n]] = -1;
+      for (int q = ia[n] + 1; q < ia[n + 1]; ++q)
+        if (ja[q] > n) jas[q] = ipos++;
+    }
+    for (int n = 0; n < nodes; ++n)
+      for (int q = ia[n]; q < ia[n + 1]; ++q)
+        if (ja[q] < n) jas[q] = jas[isym[q]];
+    /* ihc, cl12 and hwva into the symmetric arrays */
+    for (int n = 0; n < nodes && rc >= 0; ++n)
+      for (int q = ia[n] + 1; q < ia[n + 1]; ++q) {
+        if (ihcti[q] != ihcti[isym[q]]) { rc = -5; break; }
+        ihc[jas[q]] = ihcti[q];
+      }
+    for (int n = 0; n < nodes && rc >= 0; ++n)
+      for (int q = ia[n] + 1; q < ia[n + 1]; ++q) {
+        int m = ja[q];
+        if (m > n) cl1[jas[q]] = cl12t[q];
+        else if (n > m) cl2[jas[q]] = cl12t[q];
+      }
+    for (int n = 0; n < nodes && rc >= 0; ++n)
+      for (int q = ia[n] + 1; q < ia[n + 1]; ++q) {
+        if (hwvat[q] != hwvat[isym[q]]) { rc = -6; break; }
+        if (ihcti[q] < 0 || ihcti[q] > 2) { rc = -7; break; }
+        hwva[jas[q]] = hwvat[q];
+      }
+  }
+  free(ihcti); free(cl12t); free(hwvat);
+  return rc;
+}
+
+/* ------------------------------------------------------------------------ */
 /* NPF                                                                       */
 /* ------------------------------------------------------------------------ */
 
@@ -248,7 +401,7 @@ void or_npf_condsat(const or_gwf_model *m, double *condsat) {
                      m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->hwva[jj]);
       } else {
         double hyn = m->k11[n], hym = m->k11[mm];
-        csat = hcond(1, 1, 1, 1, 0, m->icellavg, 1.0, m->top[n], m->top[mm], 1.0, 1.0,
+        csat = hcond(1, 1, 1, 1, 0, ihc, m->icellavg, 1.0, m->top[n], m->top[mm], 1.0, 1.0,
                      hyn, hym, m->top[n], m->top[mm], m->bot[n], m->bot[mm],
                      m->cl1[jj], m->cl2[jj], m->hwva[jj]);
       }
@@ -293,7 +446,7 @@ void or_npf_fc(const or_gwf_model *m, const int *ibound, const double *condsat,
                      m->bot[mm], m->hwva[jj]);
       } else {
         cond = hcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm],
-                     m->inewton, m->icellavg, condsat[jj], hnew[n], hnew[mm], sat[n],
+                     m->inewton, ihc, m->icellavg, condsat[jj], hnew[n], hnew[mm], sat[n],
                      sat[mm], m->k11[n], m->k11[mm], m->top[n], m->top[mm], m->bot[n],
                      m->bot[mm], m->cl1[jj], m->cl2[jj], m->hwva[jj]);
       }
@@ -325,6 +478,10 @@ void or_npf_fn(const or_gwf_model *m, const int *ibound, const double *condsat,
       if (m->icelltype[iups] == 0) continue;
       double topup = m->top[iups];
       double botup = m->bot[iups];
+      if (m->ihc[jj] == 2) { /* the overlap of the two cells */
+        topup = (m->top[n] < m->top[mm]) ? m->top[n] : m->top[mm];
+        botup = (m->bot[n] > m->bot[mm]) ? m->bot[n] : m->bot[mm];
+      }
       double cond = condsat[jj];
       double consterm = -cond * (hnew[iups] - hnew[idn]);
       double derv = or_squadratic_sat_derv(topup, botup, hnew[iups], m->satomega);
@@ -349,11 +506,25 @@ void or_npf_fn(const or_gwf_model *m, const int *ibound, const double *condsat,
 /* gwf-npf.f90:705-741, npf_nur. */
 void or_npf_nur(const or_gwf_model *m, const int *ibound, double *x, const double *xtemp,
                 double *dx, int *inewtonur, double *dxmax, int *locmax) {
-  int nrc = m->nrow * m->ncol;
   for (int n = 0; n < m->nodes; ++n) {
     if (ibound[n] < 1) continue;
     if (m->icelltype[n] > 0) {
-      int ibot = (m->nlay - 1) * nrc + (n % nrc); /* ibotnode: bottom cell in column */
+      /* ibotnode (gwf-npf.f90:1904-1939): follow the vertical connection to
+       * a higher-numbered cell with the lowest bottom while there is one */
+      double minbot = m->bot[n];
+      int ibot = n;
+      for (;;) {
+        int nextn = -1;
+        for (int ii = m->ia[ibot] + 1; ii < m->ia[ibot + 1]; ++ii) {
+          int mm = m->ja[ii];
+          if (m->ihc[m->jas[ii]] == 0 && mm > ibot && m->bot[mm] < minbot) {
+            nextn = mm;
+            minbot = m->bot[mm];
+          }
+        }
+        if (nextn < 0) break;
+        ibot = nextn;
+      }
       double botm = m->bot[ibot];
       if (x[n] < botm) {
         *inewtonur = 1;
@@ -706,7 +877,7 @@ void or_gwf_budget(const or_gwf_model *m, const int *ibound, const double *conds
                      sat[mm], m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->hwva[jj]);
       } else {
         cond = hcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm], m->inewton,
-                     m->icellavg, condsat[jj], hnew[n], hnew[mm], sat[n], sat[mm], m->k11[n],
+                     m->ihc[jj], m->icellavg, condsat[jj], hnew[n], hnew[mm], sat[n], sat[mm], m->k11[n],
                      m->k11[mm], m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->cl1[jj],
                      m->cl2[jj], m->hwva[jj]);
       }

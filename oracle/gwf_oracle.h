@@ -68,6 +68,18 @@ int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, cons
                     const int *javert, const double *xc, const double *yc, const double *top,
                     const double *bot, int cap, int *ia, int *ja, int *isym, int *jas, int *ihc,
                     double *cl1, double *cl2, double *hwva, double *area);
+/* DISU: disuconnections + con_finalize (Connections.f90:801-928, 160-316).
+ * iainp (nodesuser+1, 0-based offsets from IAC), jainp (1-based, a negative
+ * number read as its magnitude), ihcinp/cl12inp/hwvainp per entry;
+ * nodereduced (nodesuser, 0-based reduced number or -1) or NULL for a full
+ * grid.  Returns nja, or -1 (cap too small), -2 (diagonal not first), -3 (a
+ * row not ascending), -4 (no symmetric counterpart), -5 (IHC not
+ * symmetric), -6 (HWVA not symmetric), -7 (IHC outside 0..2), -8 (no
+ * active cell). */
+int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int *ihcinp,
+                    const double *cl12inp, const double *hwvainp, const int *nodereduced,
+                    int cap, int *nodes, int *ia, int *ja, int *isym, int *jas, int *ihc,
+                    double *cl1, double *cl2, double *hwva);
 double or_squadratic_sat(double top, double bot, double x, double eps);
 double or_squadratic_sat_derv(double top, double bot, double x, double eps);
 void or_npf_condsat(const or_gwf_model *m, double *condsat);

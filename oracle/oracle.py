@@ -124,6 +124,8 @@ def load():
                                         C.c_int, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
         lib.or_dis_connect.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, _ip, _ip,
                                        _ip, _ip, _dp, _dp, _dp]
+        lib.or_disu_connect.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _ip, C.c_int, _ip, _ip,
+                                        _ip, _ip, _ip, _ip, _dp, _dp, _dp]
         lib.or_npf_condsat.argtypes = [C.POINTER(GwfModel), _dp]
         lib.or_gwf_fc.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, C.c_double, C.c_int, _dp, _dp, _dp, _dp]
         lib.or_sln_ls_fixups.argtypes = [C.c_int, _ip, _ip, _ip, C.c_int, _dp, _dp, _dp, _dp]
@@ -353,14 +355,63 @@ def disv_connect(nlay, iavert, javert, vx, vy, xc, yc, top, bot) -> dict:
     return out
 
 
+DISU_ERRORS = {-1: "capacity exceeded", -2: "diagonal not first", -3: "row not ascending",
+               -4: "no symmetric counterpart", -5: "IHC not symmetric",
+               -6: "HWVA not symmetric", -7: "IHC outside 0..2", -8: "no active cell"}
+
+
+def disu_connect(iac, ja, ihc, cl12, hwva, idomain=None) -> dict:
+    """or_disu_connect: the connectivity of a DISU grid from its input arrays
+    (JA 1-based), reduced to the cells with IDOMAIN > 0.  Raises ValueError
+    with the failing check."""
+    lib = load()
+    iac = np.asarray(iac, np.int64)
+    nu = iac.size
+    iainp = np.zeros(nu + 1, np.int32)
+    iainp[1:] = np.cumsum(iac)
+    f = lambda a: np.ascontiguousarray(a, np.float64)
+    jainp = np.ascontiguousarray(ja, np.int32)
+    ihcinp = np.ascontiguousarray(ihc, np.int32)
+    cl12inp, hwvainp = f(cl12), f(hwva)
+    red = None
+    if idomain is not None:
+        keep = np.asarray(idomain) > 0
+        red = np.full(nu, -1, np.int32)
+        red[keep] = np.arange(int(keep.sum()), dtype=np.int32)
+    cap = int(iainp[-1])
+    n = C.c_int()
+    out = dict(ia=np.zeros(nu + 1, np.int32), ja=np.zeros(cap, np.int32), isym=np.zeros(cap, np.int32),
+               jas=np.zeros(cap, np.int32), ihc=np.zeros(cap, np.int32), cl1=np.zeros(cap),
+               cl2=np.zeros(cap), hwva=np.zeros(cap))
+    nja = lib.or_disu_connect(nu, ip(iainp), ip(jainp), ip(ihcinp), dp(cl12inp), dp(hwvainp),
+                              ip(red) if red is not None else None, cap, C.byref(n),
+                              ip(out["ia"]), ip(out["ja"]), ip(out["isym"]), ip(out["jas"]),
+                              ip(out["ihc"]), dp(out["cl1"]), dp(out["cl2"]), dp(out["hwva"]))
+    if nja < 0:
+        raise ValueError("or_disu_connect: " + DISU_ERRORS.get(nja, str(nja)))
+    nodes = n.value
+    njas = (nja - nodes) // 2
+    out["ia"] = out["ia"][:nodes + 1].copy()
+    for k in ("ja", "isym", "jas"):
+        out[k] = out[k][:nja].copy()
+    for k in ("ihc", "cl1", "cl2", "hwva"):
+        out[k] = out[k][:njas].copy()
+    out.update(nodes=nodes, nja=nja, njas=njas)
+    return out
+
+
 class Gwf:
-    """Oracle GWF model + NumericalSolution for one DIS model (a GwfDisModel)
-    or one DISV model (a DisvModel: connectivity from or_disv_connect)."""
+    """Oracle GWF model + NumericalSolution for one DIS model (a GwfDisModel),
+    one DISV model (a DisvModel: connectivity from or_disv_connect) or one
+    DISU model (a DisuModel: connectivity from or_disu_connect)."""
 
     def __init__(self, m, ims_settings: Settings, satomega=1.0e-6):
         self.lib = load()
         self.m = m
-        if getattr(m, "disv", False):
+        if getattr(m, "disu", False):
+            con = disu_connect(m.iac, m.ja, m.ihc_u, m.cl12, m.hwva_u, m.idomain)
+            area = m.area
+        elif getattr(m, "disv", False):
             iav, jav = m.vertex_lists
             con = disv_connect(m.nlay, iav, jav, m.vertices[:, 0], m.vertices[:, 1], m.xc, m.yc,
                                m.cell_top, m.cell_bot)
