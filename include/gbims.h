@@ -402,7 +402,8 @@ typedef struct gbsln_grid {
 /* gbsln_create on a grid given by its connectivity.  The model's K,
  * ICELLTYPE, storage and boundaries are read from `model` (its nlay, nrow,
  * ncol, delr, delc, top and botm are not read).  The solve takes the
- * general-pattern path (SELL-32 product, level-scheduled ILU0).  The checks
+ * general-pattern path (SELL-32 product, level-scheduled ILU0) unless the
+ * pattern is that of a full DIS grid, which is found from IA/JA.  The checks
  * of con_finalize are made (diagonal first, ascending rows, every
  * connection with its counterpart, ihc in 0..2): GBIMS_ERR_ARG with the
  * reason in gbsln_last_error. */

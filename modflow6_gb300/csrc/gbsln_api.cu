@@ -594,7 +594,9 @@ extern "C" int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *m,
   h->nl = *nl;
   h->ims_s = *ims;
   h->ims_s.index_base = 0;
-  h->ims_s.nlay = 0; h->ims_s.nrow = 0; h->ims_s.ncol = 0;  // the general-pattern path
+  // no shape given: a DIS pattern is found from IA/JA, any other takes the
+  // general-pattern path
+  h->ims_s.nlay = 0; h->ims_s.nrow = 0; h->ims_s.ncol = 0;
   if (grid->ia[0] != 0 || grid->ia[n] != nja) { h->err = "IA does not span JA"; return GBIMS_ERR_ARG; }
   Conn c;
   c.ia.assign(grid->ia, grid->ia + n + 1);

@@ -222,8 +222,11 @@ def test_gpu_timestep_on_general_grid_matches_oracle(gblib, grid):
     elif grid == "disu":
         m = make_disu_model(2, 12, 16, seed=8, idomain_holes=5)
     else:
+        # wells at 0.3x, so that Newton converges with two cells below their
+        # bottoms but above the model bottom (the ibotnode cell's)
         m = make_disu_model(3, 12, 16, seed=8, stagger=2.0, newton=True)
         m.inewtonur = 1
+        m.wel_q = 0.3 * m.wel_q
     tol = dict(dvclose=1e-9, rclose=1e-7, iter1=2000, ilinmeth=2 if m.inewton else 1)
     g = oracle.Gwf(m, oracle.settings(**tol))
     so = g.timestep(kper=1, kstp=1, delt=1.0, dvclose=1e-7, mxiter=50)
