@@ -383,6 +383,26 @@ int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,
                  const gbims_settings *ims, const gbsln_nonlinear *nl,
                  const double *strt, gbsln_handle **out);
 
+/* XT3D, the NPF formulation with the full hydraulic conductivity tensor on
+ * the neighbours-of-neighbours stencil (NPF option XT3D without RHS;
+ * Xt3dInterface.f90, Xt3dAlgorithm.f90), for a DIS model.  k22: K22 per
+ * cell, or NULL for K22 = K11; angle1..3: ANGLE1..3 per cell in degrees, or
+ * NULL (ANGLE1 then 0; ANGLE2 and ANGLE3 both or neither; without them the
+ * horizontal connections have no z component, as in the reference).  The
+ * matrix then has the wider pattern (each row: the cell, its neighbours and
+ * their neighbours) and the solve takes the level-scheduled path. */
+typedef struct gbsln_xt3d {
+  const double *k22;
+  const double *angle1, *angle2, *angle3;
+} gbsln_xt3d;
+
+/* gbsln_create with XT3D.  ALTERNATIVE_CELL_AVERAGING (icellavg > 0) is
+ * refused as the reference refuses it (GBIMS_ERR_ARG); gbsln_budget returns
+ * GBIMS_ERR_UNSUPPORTED (xt3d_flowja is not built). */
+int gbsln_create_xt3d(const gbsln_model *model, const gbsln_xt3d *xt3d,
+                      const gbnpf_options *npf, const gbims_settings *ims,
+                      const gbsln_nonlinear *nl, const double *strt, gbsln_handle **out);
+
 /* A grid given by its connectivity: a DISV or DISU grid (or DIS written out
  * this way), in the form Connections.f90 keeps it (con_finalize, :160-316),
  * all 0-based.  ia/ja is the symmetric CSR pattern with each row's diagonal

@@ -80,6 +80,10 @@ class GbslnGrid(C.Structure):
     ]
 
 
+class GbslnXt3d(C.Structure):
+    _fields_ = [("k22", _dp), ("angle1", _dp), ("angle2", _dp), ("angle3", _dp)]
+
+
 class GbslnNonlinear(C.Structure):
     _fields_ = [
         ("dvclose", C.c_double), ("mxiter", C.c_int), ("nonmeth", C.c_int),
@@ -157,6 +161,9 @@ _SIGS = {
     "gbnpf_destroy": (C.c_int, [C.c_void_p]),
     "gbsln_create": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbnpfOptions), C.POINTER(GbimsSettings),
                                C.POINTER(GbslnNonlinear), _dp, C.POINTER(C.c_void_p)]),
+    "gbsln_create_xt3d": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbslnXt3d), C.POINTER(GbnpfOptions),
+                                    C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,
+                                    C.POINTER(C.c_void_p)]),
     "gbsln_create_grid": (C.c_int, [C.POINTER(GbslnGrid), C.POINTER(GbslnModel), C.POINTER(GbnpfOptions),
                                     C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,
                                     C.POINTER(C.c_void_p)]),

@@ -16,7 +16,10 @@ CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIB = PKG / "libgbims.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# host code without contraction of a*b+c, so that host-side setup arithmetic
+# rounds as the oracle's C does on both x86-64 and aarch64
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:
@@ -57,7 +60,7 @@ def build(verbose: bool = False) -> Path:
     OBJ.mkdir(exist_ok=True)
     srcs = sources()
     stamp = OBJ / "flags.txt"
-    flags = " ".join(extra_flags())
+    flags = " ".join(FLAGS + extra_flags())
     stale = not stamp.exists() or stamp.read_text() != flags
     with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose, stale), srcs))

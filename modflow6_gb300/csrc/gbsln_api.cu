@@ -244,6 +244,11 @@ struct gbsln_handle {
   int *ibound = nullptr, *bnd_ptr = nullptr, *chd_node = nullptr, *flag = nullptr;
   int *bnd_kind = nullptr;  // per boundary entry: 0 WEL, 1 RCH
   int *ibotnode = nullptr;  // NEWTON UNDER_RELAXATION: the lowest cell below each cell
+  // the matrix pattern: the model's connections, or with XT3D the wider one
+  const int *s_ia = nullptr, *s_ja = nullptr;
+  Xt3dDev xt{};             // XT3D on the device (xt.on 0: off)
+  int njas = 0;
+  void *xt_mem[16] = {};    // XT3D device arrays, freed by gbsln_destroy
   double *galpha = nullptr; // the last warm step's projection factors (2)
   double *dprev = nullptr;  // the last step's head change (valid when have_prev)
   double *gpart = nullptr;  // projection partials (5 per block)
@@ -424,13 +429,181 @@ std::vector<int> bottom_nodes(int n, const Conn &c, const std::vector<double> &b
 
 // Everything of gbsln_create after the grid: boundaries, device arrays,
 // the IMS handle and the saturated conductances.
+// XT3D setup on a full DIS grid (Xt3dInterface.f90: xt3d_ac :124-189 for
+// the wider pattern, xt3d_mc :191-271 for the positions of the extended
+// neighbours, xt3d_iallpc :1109-1179, xt3d_fillrmatck :1577-1613 and the
+// tensor of xt3d_load :1230-1237; the DIS connection geometry of Dis.f90:
+// 1039-1160).  Fills the solution pattern sia/sja and the host arrays of
+// the device view.
+struct Xt3dHost {
+  std::vector<int> sia, sja, idxglo, iallpc, pair_n, pair_il0, pair_il10;
+  std::vector<unsigned char> sflag;
+  std::vector<double> ck, geo;
+  int lamatsaved = 0, nozee = 0;
+};
+
+int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const Conn &c,
+              const std::vector<int> &ibound, Xt3dHost &o, std::string &err) {
+  const int n = (int)c.ia.size() - 1;
+  if ((xt->angle2 == nullptr) != (xt->angle3 == nullptr)) {
+    err = "XT3D: ANGLE2 and ANGLE3 must be given both or neither";
+    return GBIMS_ERR_ARG;
+  }
+  for (int p = 0; p < n; ++p)
+    if (c.ia[p + 1] - c.ia[p] - 1 > kXtNb) {
+      err = "XT3D: more neighbours per cell than supported";
+      return GBIMS_ERR_UNSUPPORTED;
+    }
+  o.nozee = (xt->angle2 == nullptr) ? 1 : 0;
+  // the tensor per cell, angles from degrees (DPIO180 = atan(1)/45)
+  const double dpio180 = std::atan(1.0) / 45.0;
+  o.ck.assign((size_t)9 * n, 0.0);
+  for (int p = 0; p < n; ++p) {
+    const double ang1 = xt->angle1 ? xt->angle1[p] * dpio180 : 0.0;
+    const double ang2 = (!o.nozee) ? xt->angle2[p] * dpio180 : 0.0;
+    const double ang3 = (!o.nozee) ? xt->angle3[p] * dpio180 : 0.0;
+    const double s1 = std::sin(ang1), c1 = std::cos(ang1), s2 = std::sin(ang2), c2 = std::cos(ang2),
+                 s3 = std::sin(ang3), c3 = std::cos(ang3);
+    double r[3][3];
+    r[0][0] = c1 * c2;
+    r[0][1] = c1 * s2 * s3 - s1 * c3;
+    r[0][2] = -c1 * s2 * c3 - s1 * s3;
+    r[1][0] = s1 * c2;
+    r[1][1] = s1 * s2 * s3 + c1 * c3;
+    r[1][2] = -s1 * s2 * c3 + c1 * s3;
+    r[2][0] = s2;
+    r[2][1] = -c2 * s3;
+    r[2][2] = c2 * c3;
+    const double kd[3] = {m->k11[p], xt->k22 ? xt->k22[p] : m->k11[p], m->k33[p]};
+    double t[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double acc = 0.0;
+        for (int k = 0; k < 3; ++k) acc = acc + r[i][k] * (k == j ? kd[k] : 0.0);
+        t[i][j] = acc;
+      }
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double acc = 0.0;
+        for (int k = 0; k < 3; ++k) acc = acc + t[i][k] * r[j][k];
+        o.ck[(size_t)9 * p + 3 * i + j] = acc;
+      }
+  }
+  // horizontal geometry of each connection n < m, from n to m: right
+  // neighbour (j+1): displacement (ds, 0), normal (1, 0); front neighbour
+  // (i+1): (0, -ds), (0, -1); ds = cl1 + cl2
+  o.geo.assign((size_t)4 * c.njas, 0.0);
+  for (int p = 0; p < n; ++p)
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
+      const int mm = c.ja[q], sidx = c.jas[q];
+      if (mm < p || c.ihc[sidx] == 0) continue;
+      const double ds = c.cl1[sidx] + c.cl2[sidx];
+      double *gg = &o.geo[(size_t)4 * sidx];
+      if (mm == p + 1) {
+        gg[0] = ds;
+        gg[2] = 1.0;
+      } else {
+        gg[1] = -ds;
+        gg[3] = -1.0;
+      }
+    }
+  // the solution pattern: each row the connections and the neighbours of
+  // the neighbours, diagonal first, the rest ascending; flags 1 (a model
+  // connection) and 2 (an extended neighbour, xt3d_ac)
+  o.sia.assign(n + 1, 0);
+  o.sja.clear();
+  o.sflag.clear();
+  o.idxglo.assign(c.ja.size(), -1);
+  std::vector<int> row;
+  std::vector<unsigned char> fl;
+  for (int p = 0; p < n; ++p) {
+    row.clear();
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
+      row.push_back(c.ja[q]);
+      const int j = c.ja[q];
+      for (int k = c.ia[j] + 1; k < c.ia[j + 1]; ++k) row.push_back(c.ja[k]);
+    }
+    std::sort(row.begin(), row.end());
+    row.erase(std::unique(row.begin(), row.end()), row.end());
+    row.erase(std::remove(row.begin(), row.end(), p), row.end());
+    row.insert(row.begin(), p);
+    if ((int)row.size() > kXtRow) {
+      err = "XT3D: a matrix row is longer than supported";
+      return GBIMS_ERR_UNSUPPORTED;
+    }
+    o.sia[p] = (int)o.sja.size();
+    for (int col : row) {
+      unsigned char f = 0;
+      for (int q = c.ia[p]; q < c.ia[p + 1]; ++q)
+        if (c.ja[q] == col) {
+          f |= 1;
+          o.idxglo[q] = (int)o.sja.size();
+        }
+      for (int q = c.ia[p] + 1; q < c.ia[p + 1] && !(f & 2); ++q) {
+        const int j = c.ja[q];
+        for (int k = c.ia[j] + 1; k < c.ia[j + 1]; ++k)
+          if (c.ja[k] == col) {
+            f |= 2;
+            break;
+          }
+      }
+      o.sja.push_back(col);
+      o.sflag.push_back(f);
+    }
+  }
+  o.sia[n] = (int)o.sja.size();
+  // xt3d_iallpc: every cell the terms of whose connections never change
+  o.iallpc.assign(n, 1);
+  for (int p = 0; p < n; ++p) {
+    if (m->icelltype[p] != 0) {
+      o.iallpc[p] = 0;
+      continue;
+    }
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
+      const int mm = ibound[c.ja[q]] != 0 ? c.ja[q] : -1;
+      if (mm < p) continue;
+      if (m->icelltype[mm] != 0) {
+        o.iallpc[p] = 0;
+        o.iallpc[mm] = 0;
+        continue;
+      }
+      for (int k = c.ia[mm] + 1; k < c.ia[mm + 1]; ++k) {
+        const int qq = ibound[c.ja[k]] != 0 ? c.ja[k] : -1;
+        if (qq >= 0 && m->icelltype[qq] != 0) {
+          o.iallpc[p] = 0;
+          o.iallpc[mm] = 0;
+          o.iallpc[qq] = 0;
+        }
+      }
+    }
+  }
+  o.lamatsaved = 0;
+  for (int p = 0; p < n; ++p)
+    if (o.iallpc[p] == 1) o.lamatsaved = 1;
+  // each connection n < m: n, m's slot in n's row, n's slot in m's row
+  o.pair_n.assign(c.njas, 0);
+  o.pair_il0.assign(c.njas, 0);
+  o.pair_il10.assign(c.njas, 0);
+  for (int p = 0; p < n; ++p)
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
+      const int mm = c.ja[q];
+      if (mm < p) continue;
+      const int sidx = c.jas[q];
+      o.pair_n[sidx] = p;
+      o.pair_il0[sidx] = q - c.ia[p] - 1;
+      o.pair_il10[sidx] = c.isym[q] - c.ia[mm] - 1;
+    }
+  return GBIMS_OK;
+}
+
 int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, const double *strt,
               const Conn &c, const std::vector<double> &top, const std::vector<double> &bot,
-              const std::vector<double> &area) {
+              const std::vector<double> &area, const gbsln_xt3d *xt = nullptr) {
   const int n = h->n;
   std::vector<double> vol(n);
   for (int p = 0; p < n; ++p) vol[p] = area[p] * (top[p] - bot[p]);
   h->nja = (int)c.ja.size();
+  h->njas = c.njas;
   std::vector<int> ibound(n, 1);
   for (int i = 0; i < m->nchd; ++i) {
     int node = m->chd_node[i];
@@ -460,6 +633,17 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
   }
   bptr[n] = (int)bval.size();
   h->inewtonur = npf->inewton && npf->inewtonur;
+  Xt3dHost xh;
+  if (xt) {
+    if (npf->icellavg != 0) {
+      h->err = "ALTERNATIVE_CELL_AVERAGING cannot be used with XT3D";
+      return GBIMS_ERR_ARG;
+    }
+    int rc = xt3d_host(m, xt, c, ibound, xh, h->err);
+    if (rc < 0) return rc;
+    h->nja = (int)xh.sja.size();
+    h->ims_s.nlay = -1;  // the wider pattern: the level-scheduled sweeps
+  }
   cudaError_t e = cudaSuccess;
   auto chk = [&](cudaError_t x) { if (x != cudaSuccess && e == cudaSuccess) e = x; };
   chk(up(&h->d.ia, c.ia.data(), c.ia.size()));
@@ -504,12 +688,58 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
   chk(up<double>(&h->dprev, nullptr, (size_t)n));
   chk(up<double>(&h->gpart, nullptr, (size_t)h->G * 5));
   chk(up(&h->strt, strt, (size_t)n));
+  if (xt) {
+    Xt3dDev &x = h->xt;
+    int *d_sia = nullptr, *d_sja = nullptr, *d_idx = nullptr, *d_pc = nullptr, *d_pn = nullptr,
+        *d_p0 = nullptr, *d_p1 = nullptr;
+    unsigned char *d_fl = nullptr;
+    double *d_ck = nullptr, *d_geo = nullptr, *d_coef = nullptr, *d_pcval = nullptr,
+           *d_ones = nullptr;
+    chk(up(&d_sia, xh.sia.data(), xh.sia.size()));
+    chk(up(&d_sja, xh.sja.data(), xh.sja.size()));
+    chk(up(&d_idx, xh.idxglo.data(), xh.idxglo.size()));
+    chk(up(&d_fl, xh.sflag.data(), xh.sflag.size()));
+    chk(up(&d_pc, xh.iallpc.data(), xh.iallpc.size()));
+    chk(up(&d_ck, xh.ck.data(), xh.ck.size()));
+    chk(up(&d_geo, xh.geo.data(), xh.geo.size()));
+    chk(up(&d_pn, xh.pair_n.data(), xh.pair_n.size()));
+    chk(up(&d_p0, xh.pair_il0.data(), xh.pair_il0.size()));
+    chk(up(&d_p1, xh.pair_il10.data(), xh.pair_il10.size()));
+    chk(up<double>(&d_coef, nullptr, (size_t)c.njas * kXtStride));
+    chk(up<double>(&d_pcval, nullptr, xh.sja.size()));
+    std::vector<double> ones(n, 1.0);
+    chk(up(&d_ones, ones.data(), ones.size()));
+    void *mem[] = {d_sia, d_sja, d_idx, d_fl, d_pc, d_ck, d_geo, d_pn, d_p0, d_p1, d_coef, d_pcval,
+                   d_ones};
+    for (int i = 0; i < 13; ++i) h->xt_mem[i] = mem[i];
+    x.on = 1;
+    x.lamatsaved = xh.lamatsaved;
+    x.nozee = xh.nozee;
+    x.sia = d_sia;
+    x.sja = d_sja;
+    x.idxglo = d_idx;
+    x.sflag = d_fl;
+    x.iallpc = d_pc;
+    x.ck = d_ck;
+    x.geo = d_geo;
+    x.pair_n = d_pn;
+    x.pair_il0 = d_p0;
+    x.pair_il10 = d_p1;
+    x.coef = d_coef;
+    x.pcval = d_pcval;
+    h->s_ia = d_sia;
+    h->s_ja = d_sja;
+  } else {
+    h->s_ia = h->d.ia;
+    h->s_ja = h->d.ja;
+  }
   if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GBIMS_ERR_CUDA; }
   for (double **p : wv) cudaMemset(*p, 0, sizeof(double) * n);
   cudaMemset(h->d.sat, 0, sizeof(double) * n);
   h->hpart.resize((size_t)h->G * 2);
   // IMS handle (imslinear_allocate) on the same connectivity
-  int rc = gbims_create(&h->ims_s, n, h->nja, c.ia.data(), c.ja.data(), &h->ims);
+  int rc = xt ? gbims_create(&h->ims_s, n, h->nja, xh.sia.data(), xh.sja.data(), &h->ims)
+              : gbims_create(&h->ims_s, n, h->nja, c.ia.data(), c.ja.data(), &h->ims);
   if (rc < 0) {
     h->err = std::string("IMS: ") + (h->ims ? gbims_last_error(h->ims) : "create failed");
     return rc;
@@ -527,6 +757,13 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
   h->g.satomega = npf->satomega > 0 ? npf->satomega : 1.0e-6;
   SLN_CUDA(h, cudaMemcpyAsync(h->x, strt, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
   gwf_condsat(n, h->g, h->d.condsat, h->st);
+  if (xt && h->xt.lamatsaved) {
+    // the permanently confined coefficients, once, with every saturation 1
+    // (npf_ar's initial sat, xt3d_ar :366-367)
+    const double *ones = (const double *)h->xt_mem[12];
+    xt3d_pairs(h->njas, h->g, h->xt, h->ibound, ones, h->x, 1, h->st);
+    xt3d_pcrows(n, h->g, h->xt, h->ibound, (double *)h->xt_mem[11], h->st);
+  }
   SLN_CUDA(h, cudaStreamSynchronize(h->st));
   SLN_CUDA(h, cudaGetLastError());
   return GBIMS_OK;
@@ -541,9 +778,9 @@ bool model_props_ok(const gbsln_model *m) {
 
 }  // namespace
 
-extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
-                            const gbims_settings *ims, const gbsln_nonlinear *nl,
-                            const double *strt, gbsln_handle **out) {
+static int create_dis(const gbsln_model *m, const gbsln_xt3d *xt, const gbnpf_options *npf,
+                      const gbims_settings *ims, const gbsln_nonlinear *nl, const double *strt,
+                      gbsln_handle **out) {
   if (!out) return GBIMS_ERR_ARG;
   *out = nullptr;
   if (!m || !npf || !ims || !nl || !strt || m->nlay <= 0 || m->nrow <= 0 || m->ncol <= 0 ||
@@ -572,7 +809,24 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
   }
   Conn c;
   build_connections(m->nlay, m->nrow, m->ncol, m->delr, m->delc, top, bot, c);
-  return sln_setup(h, m, npf, strt, c, top, bot, area);
+  return sln_setup(h, m, npf, strt, c, top, bot, area, xt);
+}
+
+extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
+                            const gbims_settings *ims, const gbsln_nonlinear *nl,
+                            const double *strt, gbsln_handle **out) {
+  return create_dis(m, nullptr, npf, ims, nl, strt, out);
+}
+
+extern "C" int gbsln_create_xt3d(const gbsln_model *m, const gbsln_xt3d *xt,
+                                 const gbnpf_options *npf, const gbims_settings *ims,
+                                 const gbsln_nonlinear *nl, const double *strt,
+                                 gbsln_handle **out) {
+  if (!xt) {
+    if (out) *out = nullptr;
+    return GBIMS_ERR_ARG;
+  }
+  return create_dis(m, xt, npf, ims, nl, strt, out);
 }
 
 extern "C" int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *m,
@@ -751,6 +1005,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
   f.area = h->area;
   f.bnd_ptr = h->bnd_ptr;
   f.bnd_val = h->bnd_val;
+  f.xt = h->xt;
   const int isymmetric = (h->ims_s.ilinmeth == 1) ? 1 : 0;
   const bool steady_newton = !transient && h->g.inewton;
   bool converged = false;
@@ -763,8 +1018,9 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
     SLN_CUDA(h, cudaMemsetAsync(h->amat, 0, sizeof(double) * h->nja, h->st));
     SLN_CUDA(h, cudaMemsetAsync(h->rhs, 0, sizeof(double) * n, h->st));
     gwf_npf_cf(n, h->g, h->ibound, h->x, h->d.sat, h->st);
+    if (f0.xt.on) xt3d_pairs(h->njas, h->g, f0.xt, h->ibound, h->d.sat, h->x, 0, h->st);
     gwf_fill(n, h->g, f0, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, h->amat, h->rhs, h->st);
-    gwf_l2_resid(n, h->d.ia, h->d.ja, h->amat, h->x, h->rhs, h->ibound, h->part, h->G, h->st);
+    gwf_l2_resid(n, h->s_ia, h->s_ja, h->amat, h->x, h->rhs, h->ibound, h->part, h->G, h->st);
     double ss = 0.0;
     int rc = reduce_host(h, false, &ss);
     *l2 = sqrt(ss);
@@ -780,8 +1036,9 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
     SLN_CUDA(h, cudaMemsetAsync(h->amat, 0, sizeof(double) * h->nja, h->st));
     SLN_CUDA(h, cudaMemsetAsync(h->rhs, 0, sizeof(double) * n, h->st));
     gwf_npf_cf(n, h->g, h->ibound, h->x, h->d.sat, h->st);
+    if (f.xt.on) xt3d_pairs(h->njas, h->g, f.xt, h->ibound, h->d.sat, h->x, 0, h->st);
     gwf_fill(n, h->g, f, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, h->amat, h->rhs, h->st);
-    k_guess_dots<<<h->G, 256, 0, h->st>>>(n, h->d.ia, h->d.ja, h->amat, h->rhs, h->ibound, dprev,
+    k_guess_dots<<<h->G, 256, 0, h->st>>>(n, h->s_ia, h->s_ja, h->amat, h->rhs, h->ibound, dprev,
                                             d_guess, h->xold, h->gpart);
     k_guess_blend<<<std::min(4 * kNumSM, (n + 255) / 256), 256, 0, h->st>>>(
         n, h->G, h->gpart, h->ibound, dprev, d_guess, h->xold, h->x, h->galpha);
@@ -842,24 +1099,25 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
     SLN_CUDA(h, cudaMemsetAsync(h->amat, 0, sizeof(double) * h->nja, h->st));
     SLN_CUDA(h, cudaMemsetAsync(h->rhs, 0, sizeof(double) * n, h->st));
     gwf_npf_cf(n, h->g, h->ibound, h->x, h->d.sat, h->st);
+    if (f.xt.on) xt3d_pairs(h->njas, h->g, f.xt, h->ibound, h->d.sat, h->x, 0, h->st);
     gwf_fill(n, h->g, f, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, h->amat, h->rhs, h->st);
     cudaEventRecord(f1, h->st);
     // sln_calc_ptc -> gwf_ptc (steady-state Newton models)
     int iptc = 0;
     double ptcf = 0.0;
     if (steady_newton) {
-      gwf_ptc_resid(n, h->d.ia, h->d.ja, h->amat, h->x, h->rhs, h->ibound, h->vol, h->part, h->G, h->st);
+      gwf_ptc_resid(n, h->s_ia, h->s_ja, h->amat, h->x, h->rhs, h->ibound, h->vol, h->part, h->G, h->st);
       int rc = reduce_host(h, true, &ptcf);
       if (rc < 0) return rc;
       if (ptcf == 0.0) ptcf = 1.0 / (delt * 10.0);
       iptc = 1;
     }
     // sln_ls: loose ends, then pseudo-transient continuation
-    gwf_fixups(n, h->d.ia, h->d.ja, h->ibound, isymmetric, h->amat, h->rhs, h->x, h->xtemp, h->st);
+    gwf_fixups(n, h->s_ia, h->s_ja, h->ibound, isymmetric, h->amat, h->rhs, h->x, h->xtemp, h->st);
     int iallowptc = h->nl.iallowptc;
     if (iallowptc < 0) iallowptc = (kper > 1) ? 1 : 0;
     if (iptc * iallowptc != 0) {
-      gwf_l2_resid(n, h->d.ia, h->d.ja, h->amat, h->x, h->rhs, h->ibound, h->part, h->G, h->st);
+      gwf_l2_resid(n, h->s_ia, h->s_ja, h->amat, h->x, h->rhs, h->ibound, h->part, h->G, h->st);
       double ss2 = 0.0;
       int rc = reduce_host(h, false, &ss2);
       if (rc < 0) return rc;
@@ -875,7 +1133,7 @@ static int timestep_core(gbsln_handle *h, int kper, int kstp, double delt, const
         if (kiter == 1) h->ptcdel = 1.0 / ptcf;
         else h->ptcdel = (l2norm > 0.0) ? h->ptcdel * (h->l2norm0_ptc / l2norm) : 0.0;
         double ptcval = (h->ptcdel > 0.0) ? 1.0 / h->ptcdel : 1.0;
-        gwf_ptc_apply(n, h->d.ia, h->ibound, ptcval, h->amat, h->rhs, h->x, h->st);
+        gwf_ptc_apply(n, h->s_ia, h->ibound, ptcval, h->amat, h->rhs, h->x, h->st);
         h->l2norm0_ptc = l2norm;
       }
     }
@@ -984,9 +1242,11 @@ extern "C" int gbsln_formulate(gbsln_handle *h, double delt, const double *hold,
   f.area = h->area;
   f.bnd_ptr = h->bnd_ptr;
   f.bnd_val = h->bnd_val;
+  f.xt = h->xt;
   SLN_CUDA(h, cudaMemsetAsync(h->amat, 0, sizeof(double) * h->nja, h->st));
   SLN_CUDA(h, cudaMemsetAsync(h->rhs, 0, sizeof(double) * n, h->st));
   gwf_npf_cf(n, h->g, h->ibound, h->x, h->d.sat, h->st);
+  if (f.xt.on) xt3d_pairs(h->njas, h->g, f.xt, h->ibound, h->d.sat, h->x, 0, h->st);
   gwf_fill(n, h->g, f, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, h->amat, h->rhs, h->st);
   SLN_CUDA(h, cudaGetLastError());
   SLN_CUDA(h, cudaMemcpyAsync(amat, h->amat, sizeof(double) * h->nja, cudaMemcpyDeviceToHost, h->st));
@@ -997,6 +1257,10 @@ extern "C" int gbsln_formulate(gbsln_handle *h, double delt, const double *hold,
 
 extern "C" int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table *out) {
   if (!h || !out) return GBIMS_ERR_ARG;
+  if (h->xt.on) {
+    h->err = "the budget of an XT3D model (xt3d_flowja) is not built";
+    return GBIMS_ERR_UNSUPPORTED;
+  }
   const int n = h->n;
   const bool transient = (h->last_delt > 0.0) && h->has_sto;
   if (!h->bpart) SLN_CUDA(h, cudaMalloc((void **)&h->bpart, sizeof(double) * kGwfBudgetSlots * h->G));
@@ -1010,6 +1274,7 @@ extern "C" int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table 
   f.area = h->area;
   f.bnd_ptr = h->bnd_ptr;
   f.bnd_val = h->bnd_val;
+  f.xt = h->xt;
   gwf_budget(n, h->g, f, h->bnd_kind, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, dflow,
              h->bpart, h->G, h->st);
   std::vector<double> part((size_t)kGwfBudgetSlots * h->G);
@@ -1101,6 +1366,8 @@ extern "C" int gbsln_destroy(gbsln_handle *h) {
                h->bnd_kind, h->bpart, h->ibotnode,
                h->flag, h->galpha, h->dprev, h->gpart};
   for (void *q : p)
+    if (q) cudaFree(q);
+  for (void *q : h->xt_mem)
     if (q) cudaFree(q);
   if (h->e0) cudaEventDestroy(h->e0);
   if (h->e1) cudaEventDestroy(h->e1);

@@ -14,6 +14,7 @@
 // and rhs are bit-for-bit those of the Fortran compiled without contraction.
 #include "gbims_internal.cuh"
 #include "k_gwf.cuh"
+#include "k_xt3d.cuh"
 #include <cfloat>
 
 namespace gb {
@@ -197,21 +198,136 @@ __device__ __forceinline__ double conn_cond(const NpfDev &g, const int *ibound, 
 }
 
 // One row of gwf_fc in gather form: NPF fc, STO fc, BND fc, NPF fn, STO fn.
+// XT3D fc of row p (xt3d_fc, Xt3dInterface.f90:371-497) in gather form:
+// the row's positions start from the permanently confined part (amatpc and
+// amatpcx, already summed) or zero, then take the terms of the connections
+// (n, p), n < p, by n (p is cell 1: its primary terms, xt3d_amat_nbrs over
+// p's neighbours, xt3d_amat_nbrnbrs over n's), then of (p, m), m > p, by m
+// (p is cell 0), which is the order in which the reference adds them.
+__device__ inline void xt_row_fc(const NpfDev &g, const Xt3dDev &x, const int *ibound, int p,
+                                 int s0, int len, double *val) {
+  for (int k = 0; k < len; ++k) val[k] = x.lamatsaved ? x.pcval[s0 + k] : 0.0;
+  const int r0 = g.ia[p], r1 = g.ia[p + 1], np = r1 - r0 - 1;
+  if (ibound[p] == 0) return;
+  for (int ii = r0 + 1; ii < r1; ++ii) {
+    const int n = g.ja[ii];
+    if (n > p) break;
+    if (ibound[n] == 0 || (x.lamatsaved && x.iallpc[n] == 1)) continue;
+    const double *cf = x.coef + (size_t)g.jas[ii] * kXtStride;
+    const int q10 = x.idxglo[ii] - s0;
+    val[0] = DADD(val[0], -cf[0]);
+    val[q10] = DADD(val[q10], cf[0]);
+    const double *c1j = cf + 1 + kXtNb;
+    for (int iil = 0; iil < np; ++iil) {
+      if (ibound[g.ja[r0 + 1 + iil]] == 0) continue;
+      const int q = x.idxglo[r0 + 1 + iil] - s0;
+      val[0] = DADD(val[0], -c1j[iil]);
+      val[q] = DADD(val[q], c1j[iil]);
+    }
+    const double *ci0 = cf + 1;
+    const int n0 = g.ia[n], nn = g.ia[n + 1] - n0 - 1;
+    for (int iil = 0; iil < nn; ++iil) {
+      const int jjj = g.ja[n0 + 1 + iil];
+      if (ibound[jjj] == 0) continue;
+      val[q10] = DADD(val[q10], ci0[iil]);
+      const int q = xt_pos(x, s0, len, jjj);
+      val[q] = DADD(val[q], -ci0[iil]);
+    }
+  }
+  if (x.lamatsaved && x.iallpc[p] == 1) return;
+  for (int ii = r0 + 1; ii < r1; ++ii) {
+    const int m = g.ja[ii];
+    if (m < p || ibound[m] == 0) continue;
+    const double *cf = x.coef + (size_t)g.jas[ii] * kXtStride;
+    const int q01 = x.idxglo[ii] - s0;
+    val[0] = DADD(val[0], -cf[0]);
+    val[q01] = DADD(val[q01], cf[0]);
+    const double *ci0 = cf + 1;
+    for (int iil = 0; iil < np; ++iil) {
+      if (ibound[g.ja[r0 + 1 + iil]] == 0) continue;
+      const int q = x.idxglo[r0 + 1 + iil] - s0;
+      val[0] = DADD(val[0], -ci0[iil]);
+      val[q] = DADD(val[q], ci0[iil]);
+    }
+    const double *c1j = cf + 1 + kXtNb;
+    const int m0 = g.ia[m], nm = g.ia[m + 1] - m0 - 1;
+    for (int iil = 0; iil < nm; ++iil) {
+      const int jjj = g.ja[m0 + 1 + iil];
+      if (ibound[jjj] == 0) continue;
+      val[q01] = DADD(val[q01], c1j[iil]);
+      const int q = xt_pos(x, s0, len, jjj);
+      val[q] = DADD(val[q], -c1j[iil]);
+    }
+  }
+}
+
+// XT3D fn of row p (xt3d_fn, Xt3dInterface.f90:693-795) in the same order;
+// the saturation derivative takes its default smoothing 1e-6
+__device__ inline void xt_row_fn(const NpfDev &g, const Xt3dDev &x, const int *ibound,
+                                 const double *h, int p, int s0, double *val, double &r) {
+  const int r0 = g.ia[p], r1 = g.ia[p + 1];
+  if (ibound[p] == 0) return;
+  for (int ii = r0 + 1; ii < r1; ++ii) {
+    const int q = g.ja[ii];
+    const bool lower = q < p;
+    const int n = lower ? q : p, m = lower ? p : q;
+    if (ibound[q] == 0) continue;
+    if (x.lamatsaved && x.iallpc[n] == 1) continue;
+    const int jjs = g.jas[ii];
+    const int iups = (h[m] < h[n]) ? n : m;
+    if (g.icelltype[iups] == 0) continue;
+    double topup = g.top[iups], botup = g.bot[iups];
+    if (g.ihc[jjs] == 2) {
+      topup = fmin(g.top[n], g.top[m]);
+      botup = fmax(g.bot[n], g.bot[m]);
+    }
+    const double derv = d_sqsat_derv(topup, botup, h[iups], 1.0e-6);
+    const double term = DMUL(x.coef[(size_t)jjs * kXtStride + 1 + 2 * kXtNb], derv);
+    const int qp = x.idxglo[ii] - s0;
+    if (!lower) {  // p is cell 0
+      if (iups == n) {
+        val[0] = DADD(val[0], term);
+        r = DADD(r, DMUL(term, h[n]));
+      } else {
+        val[qp] = DADD(val[qp], term);
+        r = DADD(r, DMUL(term, h[m]));
+      }
+    } else {  // p is cell 1
+      if (iups == n) {
+        val[qp] = DADD(val[qp], -term);
+        r = DSUB(r, DMUL(term, h[n]));
+      } else {
+        val[0] = DADD(val[0], -term);
+        r = DSUB(r, DMUL(term, h[m]));
+      }
+    }
+  }
+}
+
+template <bool XT>
 __global__ void k_gwf_fill(int nodes, NpfDev g, FillDev f, const int *__restrict__ ibound,
                            const double *__restrict__ h, const double *__restrict__ hold,
                            const double *__restrict__ sat, const double *__restrict__ condsat,
                            double *amat, double *rhs) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < nodes; p += gridDim.x * blockDim.x) {
-    const int i0 = g.ia[p], i1 = g.ia[p + 1];
-    double diag = amat[i0];
+    const int i0 = XT ? f.xt.sia[p] : g.ia[p], i1 = g.ia[p + 1];
+    double val[XT ? kXtRow : 1];
+    const int xlen = XT ? f.xt.sia[p + 1] - i0 : 0;
+    double diag;
     double r = rhs[p];
-    // NPF fc: row p in JA order
-    for (int ii = i0 + 1; ii < i1; ++ii) {
-      int q = g.ja[ii];
-      int n = min(p, q), m = max(p, q);
-      double cond = conn_cond(g, ibound, h, sat, condsat, n, m, g.jas[ii]);
-      amat[ii] = DADD(amat[ii], cond);
-      diag = DADD(diag, -cond);
+    if constexpr (XT) {
+      xt_row_fc(g, f.xt, ibound, p, i0, xlen, val);
+      diag = val[0];
+    } else {
+      diag = amat[i0];
+      // NPF fc: row p in JA order
+      for (int ii = i0 + 1; ii < i1; ++ii) {
+        int q = g.ja[ii];
+        int n = min(p, q), m = max(p, q);
+        double cond = conn_cond(g, ibound, h, sat, condsat, n, m, g.jas[ii]);
+        amat[ii] = DADD(amat[ii], cond);
+        diag = DADD(diag, -cond);
+      }
     }
     // STO fc (gwf-sto.f90:226-345)
     if (f.transient && ibound[p] >= 1) {
@@ -260,8 +376,15 @@ __global__ void k_gwf_fill(int nodes, NpfDev g, FillDev f, const int *__restrict
       r = DADD(r, (ibound[p] <= 0) ? 0.0 : -v);
       diag = DADD(diag, 0.0);
     }
+    if constexpr (XT) {
+      if (g.inewton && f.fn) {
+        val[0] = diag;
+        xt_row_fn(g, f.xt, ibound, h, p, i0, val, r);
+        diag = val[0];
+      }
+    }
     // NPF fn (gwf-npf.f90:578-698), gather form
-    if (g.inewton && f.fn) {
+    if (!XT && g.inewton && f.fn) {
       for (int ii = i0 + 1; ii < i1; ++ii) {
         int q = g.ja[ii];
         int n = min(p, q), m = max(p, q);
@@ -323,6 +446,8 @@ __global__ void k_gwf_fill(int nodes, NpfDev g, FillDev f, const int *__restrict
       }
     }
     amat[i0] = diag;
+    if constexpr (XT)
+      for (int k = 1; k < xlen; ++k) amat[i0 + k] = val[k];
     rhs[p] = r;
   }
 }
@@ -666,7 +791,12 @@ void gwf_npf_cf(int nodes, const NpfDev &g, const int *ibound, const double *h, 
 void gwf_fill(int nodes, const NpfDev &g, const FillDev &f, const int *ibound, const double *h,
               const double *hold, const double *sat, const double *condsat, double *amat,
               double *rhs, cudaStream_t st) {
-  k_gwf_fill<<<g_grid(nodes), 256, 0, st>>>(nodes, g, f, ibound, h, hold, sat, condsat, amat, rhs);
+  if (f.xt.on)
+    k_gwf_fill<true><<<g_grid(nodes), 128, 0, st>>>(nodes, g, f, ibound, h, hold, sat, condsat,
+                                                    amat, rhs);
+  else
+    k_gwf_fill<false><<<g_grid(nodes), 256, 0, st>>>(nodes, g, f, ibound, h, hold, sat, condsat,
+                                                     amat, rhs);
 }
 void gwf_ptc_resid(int nodes, const int *ia, const int *ja, const double *amat, const double *x,
                    const double *rhs, const int *ibound, const double *vol, double *part, int G,

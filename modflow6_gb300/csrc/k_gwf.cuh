@@ -15,6 +15,28 @@ struct NpfDev {
   double satomega;
 };
 
+// XT3D (Xt3dInterface.f90, Xt3dAlgorithm.f90), the NPF formulation with the
+// full conductivity tensor on the neighbours-of-neighbours stencil, matrix
+// form, on DIS grids.  With XT3D on, amat is indexed by the solution pattern
+// sia/sja (each row: the connections and the neighbours of the neighbours,
+// diagonal first, ascending); idxglo maps a model position into it.
+constexpr int kXtNb = 8;                    // neighbours per cell at most
+constexpr int kXtRow = 48;                  // solution-row length at most
+constexpr int kXtStride = 2 + 2 * kXtNb;    // chat01, chati0[kXtNb], chat1j[kXtNb], qsat
+struct Xt3dDev {
+  int on = 0;
+  int lamatsaved = 0;    // some cells have all their connections permanently confined
+  int nozee = 0;         // no ANGLE2: horizontal connections have no z component
+  const int *sia = nullptr, *sja = nullptr, *idxglo = nullptr;
+  const unsigned char *sflag = nullptr;  // per solution position: 1 connection, 2 extended
+  const int *iallpc = nullptr;           // per cell (xt3d_iallpc)
+  const double *ck = nullptr;            // per cell, 9 (row-major tensor)
+  const double *geo = nullptr;           // per connection n < m: dx, dy, nx, ny from n to m
+  const int *pair_n = nullptr, *pair_il0 = nullptr, *pair_il10 = nullptr;  // per connection
+  double *coef = nullptr;                // per connection, kXtStride
+  const double *pcval = nullptr;         // per solution position (lamatsaved)
+};
+
 // Storage and boundary inputs of one fill.  bnd_ptr/bnd_val list, per node,
 // the WEL q then the RCH rate*area values in package and list order.
 struct FillDev {
@@ -24,7 +46,19 @@ struct FillDev {
   const double *ss, *sy, *area;
   const int *bnd_ptr;
   const double *bnd_val;
+  Xt3dDev xt{};
 };
+
+// XT3D coefficients of every connection n < m (xt3d_fc's loop body,
+// Xt3dInterface.f90:416-465): mode 0 for the fill (the permanently confined
+// cells skipped when lamatsaved), mode 1 for those cells alone with
+// saturated areas (xt3d_fcpc, :499-571)
+void xt3d_pairs(int njas, const NpfDev &g, const Xt3dDev &x, const int *ibound, const double *sat,
+                const double *h, int mode, cudaStream_t st);
+// The permanently confined part of every solution position (amatpc, then
+// amatpcx, added to a zero matrix as xt3d_fc does first)
+void xt3d_pcrows(int nodes, const NpfDev &g, const Xt3dDev &x, const int *ibound, double *pcval,
+                 cudaStream_t st);
 
 void gwf_condsat(int nodes, const NpfDev &g, double *condsat, cudaStream_t st);
 void gwf_npf_cf(int nodes, const NpfDev &g, const int *ibound, const double *h, double *sat,

@@ -118,6 +118,11 @@ class GwfDisModel:
     idewatcv: int = 0       # NPF VARIABLECV DEWATERED
     icellavg: int = 0       # ALTERNATIVE_CELL_AVERAGING: 0 harmonic, 1 LOGARITHMIC, 2 AMT-LMK, 3 AMT-HMK
     name: str = ""
+    ixt3d: int = 0          # NPF XT3D (matrix form)
+    k22: np.ndarray | None = None      # NPF K22 (default K11)
+    angle1: np.ndarray | None = None   # NPF ANGLE1..3 in degrees; XT3D without ANGLE2
+    angle2: np.ndarray | None = None   # has no z component in its horizontal terms
+    angle3: np.ndarray | None = None
 
     @property
     def nodes(self) -> int:

@@ -170,7 +170,25 @@ class GwfSolution:
                                   nl.amomentum, nl.iallowptc, nl.numtrack, nl.btol, nl.breduc,
                                   nl.res_lim)
         self._h = C.c_void_p()
-        if general:
+        xt3d = bool(int(getattr(m, "ixt3d", 0)))
+        if xt3d and general:
+            raise _lib.GbimsError(_lib.GBIMS_ERR_UNSUPPORTED, "XT3D is built for DIS grids")
+        if xt3d:
+            from .xt3d import xt3d_pattern
+            con = m.connections()
+            self._nja = int(xt3d_pattern(con["ia"], con["ja"])[1].size)
+
+            def opt(name):
+                v = getattr(m, name, None)
+                if v is None:
+                    return None
+                keep["xt_" + name] = _f(v)
+                return _lib.dptr(keep["xt_" + name])
+
+            cx = _lib.GbslnXt3d(opt("k22"), opt("angle1"), opt("angle2"), opt("angle3"))
+            rc = lib.gbsln_create_xt3d(C.byref(cm), C.byref(cx), C.byref(npf), C.byref(cs),
+                                       C.byref(cnl), _lib.dptr(keep["strt"]), C.byref(self._h))
+        elif general:
             rc = lib.gbsln_create_grid(C.byref(grid), C.byref(cm), C.byref(npf), C.byref(cs),
                                        C.byref(cnl), _lib.dptr(keep["strt"]), C.byref(self._h))
         else:

@@ -244,6 +244,11 @@ double or_squadratic_sat_derv(double top, double bot, double x, double eps) {
   return y / b;
 }
 
+/* The solution's pattern: the model's, or with XT3D the wider one. */
+#define SIA(m) ((m)->ixt3d ? (m)->sia : (m)->ia)
+#define SJA(m) ((m)->ixt3d ? (m)->sja : (m)->ja)
+#define SNJA(m) ((m)->ixt3d ? (m)->nja_sln : (m)->nja)
+
 /* ------------------------------------------------------------------------ */
 /* DISU connectivity                                                         */
 /* ------------------------------------------------------------------------ */
@@ -747,7 +752,7 @@ void or_sto_fc(const or_gwf_model *m, const int *ibound, double delt, const doub
                const double *hnew, double *amat, double *rhs) {
   double tled = 1.0 / delt;
   for (int n = 0; n < m->nodes; ++n) {
-    int idiag = m->ia[n];
+    int idiag = SIA(m)[n];
     if (ibound[n] < 1) continue;
     double tp = m->top[n], bt = m->bot[n];
     int iconvert = m->iconvert[n];
@@ -803,7 +808,7 @@ void or_sto_fn(const or_gwf_model *m, const int *ibound, double delt, const doub
                double *amat, double *rhs) {
   double tled = 1.0 / delt;
   for (int n = 0; n < m->nodes; ++n) {
-    int idiag = m->ia[n];
+    int idiag = SIA(m)[n];
     if (ibound[n] <= 0) continue;
     double tp = m->top[n], bt = m->bot[n];
     double tthk = tp - bt;
@@ -838,14 +843,14 @@ void or_bnd_fc(const or_gwf_model *m, const int *ibound, double *amat, double *r
     int node = m->wel_node[i];
     double r = (ibound[node] <= 0) ? 0.0 : -m->wel_q[i];
     rhs[node] = rhs[node] + r;
-    amat[m->ia[node]] = amat[m->ia[node]] + 0.0;
+    amat[SIA(m)[node]] = amat[SIA(m)[node]] + 0.0;
   }
   for (int i = 0; i < m->nrch; ++i) {
     int node = m->rch_node[i];
     double r = -m->rch_rate[i] * m->area[node];
     if (ibound[node] <= 0) r = 0.0;
     rhs[node] = rhs[node] + r;
-    amat[m->ia[node]] = amat[m->ia[node]] + 0.0;
+    amat[SIA(m)[node]] = amat[SIA(m)[node]] + 0.0;
   }
 }
 
@@ -975,13 +980,22 @@ static void gwf_fc_flag(const or_gwf_model *m, const int *ibound, const double *
                         double *sat, double delt, int transient, const double *hold,
                         const double *hnew, double *amat, double *rhs, int inwtflag) {
   or_npf_cf(m, ibound, hnew, sat);
-  or_npf_fc(m, ibound, condsat, sat, hnew, amat, rhs);
+  double *qsat = NULL;
+  if (m->ixt3d) {
+    /* npf_fc with XT3D (gwf-npf.f90:492-493) */
+    qsat = (double *)calloc(m->nja, sizeof(double));
+    or_xt3d_fc(m, ibound, sat, hnew, amat, qsat);
+  } else {
+    or_npf_fc(m, ibound, condsat, sat, hnew, amat, rhs);
+  }
   if (transient) or_sto_fc(m, ibound, delt, hold, hnew, amat, rhs);
   or_bnd_fc(m, ibound, amat, rhs);
   if (inwtflag && m->inewton) {
-    or_npf_fn(m, ibound, condsat, hnew, amat, rhs);
+    if (m->ixt3d) or_xt3d_fn(m, ibound, hnew, qsat, amat, rhs);
+    else or_npf_fn(m, ibound, condsat, hnew, amat, rhs);
     if (transient) or_sto_fn(m, ibound, delt, hnew, amat, rhs);
   }
+  free(qsat);
 }
 
 void or_gwf_fc(const or_gwf_model *m, const int *ibound, const double *condsat,
@@ -1147,7 +1161,7 @@ static double sln_l2norm(int neq, const int *ia, const int *ja, const double *am
 int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
                     const double *condsat, int *ibound, int kper, int kstp, double delt,
                     int transient, double *x, double *xold, or_timestep_stats *st) {
-  int neq = m->nodes, nja = m->nja;
+  int neq = m->nodes, nja = SNJA(m);
   double *amat = (double *)calloc(nja, sizeof(double));
   double *rhs = (double *)calloc(neq, sizeof(double));
   double *sat = (double *)calloc(neq, sizeof(double));
@@ -1175,7 +1189,7 @@ int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
       memset(amat, 0, sizeof(double) * nja);
       memset(rhs, 0, sizeof(double) * neq);
       gwf_fc_flag(m, ibound, condsat, sat, delt, transient, xold, x, amat, rhs, 0);
-      double l2 = sln_l2norm(neq, m->ia, m->ja, amat, x, rhs, ibound, work);
+      double l2 = sln_l2norm(neq, SIA(m), SJA(m), amat, x, rhs, ibound, work);
       if (kiter == 1) {
         nl->res_prev = l2;
       } else {
@@ -1198,7 +1212,7 @@ int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
             memset(amat, 0, sizeof(double) * nja);
             memset(rhs, 0, sizeof(double) * neq);
             gwf_fc_flag(m, ibound, condsat, sat, delt, transient, xold, x, amat, rhs, 0);
-            nl->res_new = sln_l2norm(neq, m->ia, m->ja, amat, x, rhs, ibound, work);
+            nl->res_new = sln_l2norm(neq, SIA(m), SJA(m), amat, x, rhs, ibound, work);
             if (nb == nl->numtrack) break;
             if (nl->res_new < nl->res_prev * nl->btol) break;
             if (nl->res_new < nl->res_lim) break;
@@ -1215,7 +1229,7 @@ int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
     double ptcf = 0.0;
     int iptct = (steady && m->inewton > 0) ? 1 : 0;
     if (iptct > 0) {
-      or_amux(neq, x, work, amat, m->ja, m->ia);
+      or_amux(neq, x, work, amat, SJA(m), SIA(m));
       for (int n = 0; n < neq; ++n) {
         work[n] = work[n] - rhs[n];
         if (ibound[n] < 1) work[n] = 0.0;
@@ -1230,12 +1244,12 @@ int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
       iptc = 1;
     }
     /* sln_ls */
-    or_sln_ls_fixups(neq, m->ia, m->ja, ibound, isymmetric, amat, rhs, x, xtemp);
+    or_sln_ls_fixups(neq, SIA(m), SJA(m), ibound, isymmetric, amat, rhs, x, xtemp);
     int iallowptc = nl->iallowptc;
     if (iallowptc < 0) iallowptc = (kper > 1) ? 1 : 0;
     iptct = iptc * iallowptc;
     if (iptct != 0) {
-      double l2norm = sln_l2norm(neq, m->ia, m->ja, amat, x, rhs, ibound, work);
+      double l2norm = sln_l2norm(neq, SIA(m), SJA(m), amat, x, rhs, ibound, work);
       if (kiter == 1) {
         if (kper > 1 || kstp > 1) {
           if (l2norm <= l2norm0_ptc) iptc = 0;
@@ -1254,7 +1268,7 @@ int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
         double ptcval = (ptcdel > 0.0) ? 1.0 / ptcdel : 1.0;
         for (int ieq = 0; ieq < neq; ++ieq) {
           if (ibound[ieq] > 0) {
-            amat[m->ia[ieq]] = amat[m->ia[ieq]] + (-ptcval);
+            amat[SIA(m)[ieq]] = amat[SIA(m)[ieq]] + (-ptcval);
             rhs[ieq] = rhs[ieq] - ptcval * x[ieq];
           }
         }

@@ -38,6 +38,14 @@ typedef struct {
   int nchd;
   const int *chd_node;
   const double *chd_head;
+  /* XT3D (NPF option XT3D, matrix form), DIS grids only; 0 off.  ck: the
+   * conductivity tensor per cell (9, row-major, or_xt3d_ck); nozee when
+   * ANGLE2 is not given.  With XT3D amat is indexed by the solution pattern
+   * sia/sja (nja_sln entries: the connections and the neighbours of
+   * neighbours), idxglo maps each model position into it. */
+  int ixt3d, nozee, nja_sln;
+  const double *ck;
+  const int *sia, *sja, *idxglo;
 } or_gwf_model;
 
 /* NONLINEAR block state (NumericalSolution.f90 members). */
@@ -80,6 +88,15 @@ int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int
                     const double *cl12inp, const double *hwvainp, const int *nodereduced,
                     int cap, int *nodes, int *ia, int *ja, int *isym, int *jas, int *ihc,
                     double *cl1, double *cl2, double *hwva);
+void or_xt3d_ck(int nodes, const double *k11, const double *k22, const double *k33,
+                const double *angle1, const double *angle2, const double *angle3, int nozee,
+                double *ck);
+int or_xt3d_pattern(int nodes, const int *ia, const int *ja, int cap, int *sia, int *sja,
+                    int *idxglo);
+int or_xt3d_fc(const or_gwf_model *m, const int *ibound, const double *sat,
+               const double *hnew, double *amat, double *qsat);
+void or_xt3d_fn(const or_gwf_model *m, const int *ibound, const double *hnew,
+                const double *qsat, double *amat, double *rhs);
 double or_squadratic_sat(double top, double bot, double x, double eps);
 double or_squadratic_sat_derv(double top, double bot, double x, double eps);
 void or_npf_condsat(const or_gwf_model *m, double *condsat);

@@ -7,6 +7,7 @@ reference legs, never by the product package.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import subprocess
 from pathlib import Path
 
@@ -56,7 +57,9 @@ class GwfModel(C.Structure):
                 ("inewtonur", C.c_int), ("ss", _dp), ("sy", _dp), ("iconvert", _ip),
                 ("nwel", C.c_int), ("wel_node", _ip), ("wel_q", _dp),
                 ("nrch", C.c_int), ("rch_node", _ip), ("rch_rate", _dp),
-                ("nchd", C.c_int), ("chd_node", _ip), ("chd_head", _dp)]
+                ("nchd", C.c_int), ("chd_node", _ip), ("chd_head", _dp),
+                ("ixt3d", C.c_int), ("nozee", C.c_int), ("nja_sln", C.c_int), ("ck", _dp),
+                ("sia", _ip), ("sja", _ip), ("idxglo", _ip)]
 
 
 class Nonlinear(C.Structure):
@@ -124,6 +127,10 @@ def load():
                                         C.c_int, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
         lib.or_dis_connect.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, _ip, _ip,
                                        _ip, _ip, _dp, _dp, _dp]
+        lib.or_xt3d_ck.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp]
+        lib.or_xt3d_pattern.argtypes = [C.c_int, _ip, _ip, C.c_int, _ip, _ip, _ip]
+        lib.or_xt3d_fc.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, _dp, _dp]
+        lib.or_xt3d_fn.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, _dp, _dp]
         lib.or_disu_connect.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _ip, C.c_int, _ip, _ip,
                                         _ip, _ip, _ip, _ip, _dp, _dp, _dp]
         lib.or_npf_condsat.argtypes = [C.POINTER(GwfModel), _dp]
@@ -446,6 +453,31 @@ class Gwf:
             int(m.wel_node.size), i(m.wel_node), d(m.wel_q),
             int(m.rch_node.size), i(m.rch_node), d(m.rch_rate),
             int(m.chd_node.size), i(m.chd_node), d(m.chd_head))
+        self.mcon = con
+        if int(getattr(m, "ixt3d", 0)):
+            # XT3D on a DIS grid: the tensor per cell and the wider pattern
+            if getattr(m, "disv", False) or getattr(m, "disu", False):
+                raise NotImplementedError("the oracle restates XT3D on DIS grids")
+            nozee = m.angle2 is None
+            dpio180 = math.atan(1.0) / 45.0
+            rad = lambda a: (np.zeros(n) if a is None else np.asarray(a, float) * dpio180)
+            k22 = m.k11 if m.k22 is None else m.k22
+            ck = np.zeros(9 * n)
+            self.lib.or_xt3d_ck(n, d(m.k11), d(k22), d(m.k33), d(rad(m.angle1)), d(rad(m.angle2)),
+                                d(rad(m.angle3)), int(nozee), dp(ck))
+            cap = int(np.diff(con["ia"])[con["ja"]].sum()) + n
+            sia = np.zeros(n + 1, np.int32)
+            sja = np.zeros(cap, np.int32)
+            idxglo = np.zeros(con["nja"], np.int32)
+            nja_sln = self.lib.or_xt3d_pattern(n, i(con["ia"]), i(con["ja"]), cap, ip(sia), ip(sja),
+                                               ip(idxglo))
+            if nja_sln < 0:
+                raise RuntimeError("or_xt3d_pattern: capacity exceeded")
+            sja = sja[:nja_sln].copy()
+            self.model.ixt3d, self.model.nozee, self.model.nja_sln = 1, int(nozee), nja_sln
+            self.model.ck, self.model.sia, self.model.sja, self.model.idxglo = d(ck), i(sia), i(sja), i(idxglo)
+            con = dict(con, ia=sia, ja=sja, nja=nja_sln, idxglo=idxglo, ck=ck)
+        self.con = con
         self._keep = keep
         self.condsat = np.zeros(con["njas"])
         self.lib.or_npf_condsat(C.byref(self.model), dp(self.condsat))
@@ -485,6 +517,8 @@ class Gwf:
         (entries STO-SS, STO-SY, CHD, WEL, RCH; totals and percent difference
         summed in entry order, Budget.f90:250-266).  sat defaults to npf_cf at
         hnew."""
+        if self.model.ixt3d:
+            raise NotImplementedError("the oracle budget does not restate xt3d_flowja")
         hnew = np.ascontiguousarray(hnew, np.float64)
         hold = np.ascontiguousarray(hnew if hold is None else hold, np.float64)
         sat = self.sat(hnew) if sat is None else np.ascontiguousarray(sat, np.float64)
