@@ -231,7 +231,7 @@ __device__ inline void xt_row_fc(const NpfDev &g, const Xt3dDev &x, const int *i
       if (ibound[jjj] == 0) continue;
       val[q10] = DADD(val[q10], ci0[iil]);
       const int q = xt_pos(x, s0, len, jjj);
-      val[q] = DADD(val[q], -ci0[iil]);
+      if (q >= 0) val[q] = DADD(val[q], -ci0[iil]);
     }
   }
   if (x.lamatsaved && x.iallpc[p] == 1) return;
@@ -256,7 +256,7 @@ __device__ inline void xt_row_fc(const NpfDev &g, const Xt3dDev &x, const int *i
       if (ibound[jjj] == 0) continue;
       val[q01] = DADD(val[q01], c1j[iil]);
       const int q = xt_pos(x, s0, len, jjj);
-      val[q] = DADD(val[q], -c1j[iil]);
+      if (q >= 0) val[q] = DADD(val[q], -c1j[iil]);
     }
   }
 }

@@ -152,6 +152,7 @@ __global__ void k_xt3d_pcrows(int nodes, NpfDev g, Xt3dDev x, const int *__restr
       for (int iil = 0; iil < nn; ++iil) {
         A[q10] = XADD(A[q10], ci0[iil]);
         const int q = xt_pos(x, s0, len, g.ja[n0 + 1 + iil]);
+        if (q < 0) continue;
         if (x.sflag[s0 + q] & 2) B[q] = XSUB(B[q], ci0[iil]);
         else A[q] = XSUB(A[q], ci0[iil]);
       }
@@ -176,6 +177,7 @@ __global__ void k_xt3d_pcrows(int nodes, NpfDev g, Xt3dDev x, const int *__restr
         for (int iil = 0; iil < nm; ++iil) {
           A[q01] = XADD(A[q01], c1j[iil]);
           const int q = xt_pos(x, s0, len, g.ja[m0 + 1 + iil]);
+          if (q < 0) continue;
           if (x.sflag[s0 + q] & 2) B[q] = XSUB(B[q], c1j[iil]);
           else A[q] = XSUB(A[q], c1j[iil]);
         }
