@@ -489,22 +489,28 @@ int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const Conn &c,
         o.ck[(size_t)9 * p + 3 * i + j] = acc;
       }
   }
-  // horizontal geometry of each connection n < m, from n to m: right
-  // neighbour (j+1): displacement (ds, 0), normal (1, 0); front neighbour
-  // (i+1): (0, -ds), (0, -1); ds = cl1 + cl2
-  o.geo.assign((size_t)4 * c.njas, 0.0);
+  // horizontal geometry of each connection n < m, from n to m and from m
+  // to n: the displacement (x2 - x1, y2 - y1) and the face normal.  Right
+  // neighbour (j+1): (ds, 0), (1, 0); back from it (left): (-ds, 0),
+  // (-1, 0); front neighbour (i+1): (0, -ds), (0, -1); back from it:
+  // (0, ds), (0, 1); ds = cl1 + cl2
+  o.geo.assign((size_t)8 * c.njas, 0.0);
   for (int p = 0; p < n; ++p)
     for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
       const int mm = c.ja[q], sidx = c.jas[q];
       if (mm < p || c.ihc[sidx] == 0) continue;
       const double ds = c.cl1[sidx] + c.cl2[sidx];
-      double *gg = &o.geo[(size_t)4 * sidx];
+      double *gg = &o.geo[(size_t)8 * sidx];
       if (mm == p + 1) {
         gg[0] = ds;
         gg[2] = 1.0;
+        gg[4] = -ds;
+        gg[6] = -1.0;
       } else {
         gg[1] = -ds;
         gg[3] = -1.0;
+        gg[5] = ds;
+        gg[7] = 1.0;
       }
     }
   // the solution pattern: each row the connections and the neighbours of

@@ -31,7 +31,8 @@ struct Xt3dDev {
   const unsigned char *sflag = nullptr;  // per solution position: 1 connection, 2 extended
   const int *iallpc = nullptr;           // per cell (xt3d_iallpc)
   const double *ck = nullptr;            // per cell, 9 (row-major tensor)
-  const double *geo = nullptr;           // per connection n < m: dx, dy, nx, ny from n to m
+  const double *geo = nullptr;           // per connection n < m: dx, dy, nx, ny from n to m,
+                                         // then from m to n (8)
   const int *pair_n = nullptr, *pair_il0 = nullptr, *pair_il10 = nullptr;  // per connection
   double *coef = nullptr;                // per connection, kXtStride
   const double *pcval = nullptr;         // per solution position (lamatsaved)

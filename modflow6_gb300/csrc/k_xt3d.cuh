@@ -29,10 +29,6 @@ struct XtCell {
   double dl[kXtNb], dln[kXtNb];
 };
 
-// the reverse direction of a connection: nonzero components negated, zeros
-// kept +0 (the DIS geometry is built from +0 and +-ds, Dis.f90:1146-1158)
-__device__ __forceinline__ double xt_rev(double v) { return v == 0.0 ? 0.0 : -v; }
-
 // xt3d_load (Xt3dInterface.f90:1211-1275) with the DIS connection_normal
 // (Dis.f90:1039-1087) and connection_vector (:1094-1160, line_unit_vector
 // DisvGeom.f90:473-496); the horizontal geometry comes from x.geo
@@ -62,12 +58,11 @@ __device__ inline void xt_load(const NpfDev &g, const Xt3dDev &x, const int *ibo
       const double z2 = XADD(g.bot[jj], XMUL(0.5, XSUB(g.top[jj], g.bot[jj])));
       dltot = fabs(XSUB(z2, z1));
     } else {
-      const double *gg = x.geo + 4 * (size_t)jjs;
-      const bool fwd = jj > n;
-      const double dx = fwd ? gg[0] : xt_rev(gg[0]);
-      const double dy = fwd ? gg[1] : xt_rev(gg[1]);
-      c.vn[il][0] = fwd ? gg[2] : xt_rev(gg[2]);
-      c.vn[il][1] = fwd ? gg[3] : xt_rev(gg[3]);
+      // x.geo: per connection n < m, from n to m then from m to n
+      const double *gg = x.geo + 8 * (size_t)jjs + ((jj > n) ? 0 : 4);
+      const double dx = gg[0], dy = gg[1];
+      c.vn[il][0] = gg[2];
+      c.vn[il][1] = gg[3];
       c.vn[il][2] = 0.0;
       double z1 = 0.0, z2 = 0.0;
       if (!x.nozee) {
