@@ -430,6 +430,26 @@ typedef struct gbsln_grid {
 int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *model,
                       const gbnpf_options *npf, const gbims_settings *ims,
                       const gbsln_nonlinear *nl, const double *strt, gbsln_handle **out);
+
+/* The connection geometry XT3D needs on a grid given by its connectivity
+ * (connection_normal and connection_vector of Disv.f90:979-1080 and
+ * Disu.f90:1062-1164): xc, yc the cell centres (nodes; CELL2D); anglex per
+ * connection n < m in JAS order, the angle in radians between the x axis
+ * and the normal of the shared face, pointing from n to m (DISV: from the
+ * shared edge, DisvGeom.f90:394-412; DISU: ANGLDEGX); centre_vertical 1
+ * when vertical connections also run between the cell centres (DISU), 0 when
+ * they are vertical lines (DISV). */
+typedef struct gbsln_xt3d_geometry {
+  const double *xc, *yc;
+  const double *anglex;
+  int centre_vertical;
+} gbsln_xt3d_geometry;
+
+/* gbsln_create_grid with XT3D (gbsln_xt3d) on a DISV or DISU grid. */
+int gbsln_create_grid_xt3d(const gbsln_grid *grid, const gbsln_model *model,
+                           const gbsln_xt3d *xt3d, const gbsln_xt3d_geometry *geometry,
+                           const gbnpf_options *npf, const gbims_settings *ims,
+                           const gbsln_nonlinear *nl, const double *strt, gbsln_handle **out);
 /* One time step (prepareSolve + outer loop).  The step is transient when the
  * model has ss/sy and delt > 0, steady state otherwise; delt is also the
  * step length used by the pseudo-transient continuation default

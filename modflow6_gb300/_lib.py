@@ -84,6 +84,10 @@ class GbslnXt3d(C.Structure):
     _fields_ = [("k22", _dp), ("angle1", _dp), ("angle2", _dp), ("angle3", _dp)]
 
 
+class GbslnXt3dGeometry(C.Structure):
+    _fields_ = [("xc", _dp), ("yc", _dp), ("anglex", _dp), ("centre_vertical", C.c_int)]
+
+
 class GbslnNonlinear(C.Structure):
     _fields_ = [
         ("dvclose", C.c_double), ("mxiter", C.c_int), ("nonmeth", C.c_int),
@@ -164,6 +168,10 @@ _SIGS = {
     "gbsln_create_xt3d": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbslnXt3d), C.POINTER(GbnpfOptions),
                                     C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,
                                     C.POINTER(C.c_void_p)]),
+    "gbsln_create_grid_xt3d": (C.c_int, [C.POINTER(GbslnGrid), C.POINTER(GbslnModel), C.POINTER(GbslnXt3d),
+                                         C.POINTER(GbslnXt3dGeometry), C.POINTER(GbnpfOptions),
+                                         C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,
+                                         C.POINTER(C.c_void_p)]),
     "gbsln_create_grid": (C.c_int, [C.POINTER(GbslnGrid), C.POINTER(GbslnModel), C.POINTER(GbnpfOptions),
                                     C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,
                                     C.POINTER(C.c_void_p)]),

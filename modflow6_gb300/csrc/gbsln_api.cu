@@ -439,11 +439,11 @@ struct Xt3dHost {
   std::vector<int> sia, sja, idxglo, iallpc, pair_n, pair_il0, pair_il10;
   std::vector<unsigned char> sflag;
   std::vector<double> ck, geo;
-  int lamatsaved = 0, nozee = 0;
+  int lamatsaved = 0, nozee = 0, vcentre = 0;
 };
 
-int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const Conn &c,
-              const std::vector<int> &ibound, Xt3dHost &o, std::string &err) {
+int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const gbsln_xt3d_geometry *geom,
+              const Conn &c, const std::vector<int> &ibound, Xt3dHost &o, std::string &err) {
   const int n = (int)c.ia.size() - 1;
   if ((xt->angle2 == nullptr) != (xt->angle3 == nullptr)) {
     err = "XT3D: ANGLE2 and ANGLE3 must be given both or neither";
@@ -495,7 +495,32 @@ int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const Conn &c,
   // (-1, 0); front neighbour (i+1): (0, -ds), (0, -1); back from it:
   // (0, ds), (0, 1); ds = cl1 + cl2
   o.geo.assign((size_t)8 * c.njas, 0.0);
-  for (int p = 0; p < n; ++p)
+  if (geom) {
+    // a grid given by its cell centres and face-normal angles (DISV
+    // connection_normal/vector, Disv.f90:979-1080; DISU, Disu.f90:1062-1164):
+    // the displacement between the centres (for DISU vertical connections
+    // too) and the normal cos/sin(anglex) times +1 or -1
+    for (int p = 0; p < n; ++p)
+      for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
+        const int mm = c.ja[q], sidx = c.jas[q];
+        if (mm < p) continue;
+        if (c.ihc[sidx] == 0 && !geom->centre_vertical) continue;
+        double *gg = &o.geo[(size_t)8 * sidx];
+        gg[0] = geom->xc[mm] - geom->xc[p];
+        gg[1] = geom->yc[mm] - geom->yc[p];
+        gg[4] = geom->xc[p] - geom->xc[mm];
+        gg[5] = geom->yc[p] - geom->yc[mm];
+        if (c.ihc[sidx] != 0) {
+          const double angle = geom->anglex[sidx];
+          gg[2] = std::cos(angle) * 1.0;
+          gg[3] = std::sin(angle) * 1.0;
+          gg[6] = std::cos(angle) * -1.0;
+          gg[7] = std::sin(angle) * -1.0;
+        }
+      }
+    o.vcentre = geom->centre_vertical ? 1 : 0;
+  }
+  for (int p = 0; p < n && !geom; ++p)
     for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
       const int mm = c.ja[q], sidx = c.jas[q];
       if (mm < p || c.ihc[sidx] == 0) continue;
@@ -604,7 +629,8 @@ int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const Conn &c,
 
 int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, const double *strt,
               const Conn &c, const std::vector<double> &top, const std::vector<double> &bot,
-              const std::vector<double> &area, const gbsln_xt3d *xt = nullptr) {
+              const std::vector<double> &area, const gbsln_xt3d *xt = nullptr,
+              const gbsln_xt3d_geometry *geom = nullptr) {
   const int n = h->n;
   std::vector<double> vol(n);
   for (int p = 0; p < n; ++p) vol[p] = area[p] * (top[p] - bot[p]);
@@ -645,7 +671,7 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
       h->err = "ALTERNATIVE_CELL_AVERAGING cannot be used with XT3D";
       return GBIMS_ERR_ARG;
     }
-    int rc = xt3d_host(m, xt, c, ibound, xh, h->err);
+    int rc = xt3d_host(m, xt, geom, c, ibound, xh, h->err);
     if (rc < 0) return rc;
     h->nja = (int)xh.sja.size();
     h->ims_s.nlay = -1;  // the wider pattern: the level-scheduled sweeps
@@ -721,6 +747,7 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
     x.on = 1;
     x.lamatsaved = xh.lamatsaved;
     x.nozee = xh.nozee;
+    x.vcentre = xh.vcentre;
     x.sia = d_sia;
     x.sja = d_sja;
     x.idxglo = d_idx;
@@ -835,10 +862,10 @@ extern "C" int gbsln_create_xt3d(const gbsln_model *m, const gbsln_xt3d *xt,
   return create_dis(m, xt, npf, ims, nl, strt, out);
 }
 
-extern "C" int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *m,
-                                 const gbnpf_options *npf, const gbims_settings *ims,
-                                 const gbsln_nonlinear *nl, const double *strt,
-                                 gbsln_handle **out) {
+static int create_grid(const gbsln_grid *grid, const gbsln_model *m, const gbsln_xt3d *xt,
+                       const gbsln_xt3d_geometry *geom, const gbnpf_options *npf,
+                       const gbims_settings *ims, const gbsln_nonlinear *nl, const double *strt,
+                       gbsln_handle **out) {
   if (!out) return GBIMS_ERR_ARG;
   *out = nullptr;
   if (!grid || !m || !npf || !ims || !nl || !strt || grid->nodes <= 0 ||
@@ -907,7 +934,26 @@ extern "C" int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *m,
   c.hwva.assign(grid->hwva, grid->hwva + ipos);
   std::vector<double> top(grid->top, grid->top + n), bot(grid->bot, grid->bot + n),
       area(grid->area, grid->area + n);
-  return sln_setup(h, m, npf, strt, c, top, bot, area);
+  return sln_setup(h, m, npf, strt, c, top, bot, area, xt, geom);
+}
+
+extern "C" int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *m,
+                                 const gbnpf_options *npf, const gbims_settings *ims,
+                                 const gbsln_nonlinear *nl, const double *strt,
+                                 gbsln_handle **out) {
+  return create_grid(grid, m, nullptr, nullptr, npf, ims, nl, strt, out);
+}
+
+extern "C" int gbsln_create_grid_xt3d(const gbsln_grid *grid, const gbsln_model *m,
+                                      const gbsln_xt3d *xt, const gbsln_xt3d_geometry *geom,
+                                      const gbnpf_options *npf, const gbims_settings *ims,
+                                      const gbsln_nonlinear *nl, const double *strt,
+                                      gbsln_handle **out) {
+  if (!xt || !geom || !geom->xc || !geom->yc || !geom->anglex) {
+    if (out) *out = nullptr;
+    return GBIMS_ERR_ARG;
+  }
+  return create_grid(grid, m, xt, geom, npf, ims, nl, strt, out);
 }
 
 static int read_dxmax(gbsln_handle *h, double *hncg, int *loc) {

@@ -27,6 +27,7 @@ struct Xt3dDev {
   int on = 0;
   int lamatsaved = 0;    // some cells have all their connections permanently confined
   int nozee = 0;         // no ANGLE2: horizontal connections have no z component
+  int vcentre = 0;       // vertical connections run between the cell centres (DISU)
   const int *sia = nullptr, *sja = nullptr, *idxglo = nullptr;
   const unsigned char *sflag = nullptr;  // per solution position: 1 connection, 2 extended
   const int *iallpc = nullptr;           // per cell (xt3d_iallpc)

@@ -29,9 +29,10 @@ struct XtCell {
   double dl[kXtNb], dln[kXtNb];
 };
 
-// xt3d_load (Xt3dInterface.f90:1211-1275) with the DIS connection_normal
-// (Dis.f90:1039-1087) and connection_vector (:1094-1160, line_unit_vector
-// DisvGeom.f90:473-496); the horizontal geometry comes from x.geo
+// xt3d_load (Xt3dInterface.f90:1211-1275) with the grid's connection_normal
+// and connection_vector (Dis.f90:1039-1160, Disv.f90:979-1080,
+// Disu.f90:1062-1164; line_unit_vector DisvGeom.f90:473-496); the
+// displacements and normals come from x.geo
 __device__ inline void xt_load(const NpfDev &g, const Xt3dDev &x, const int *ibound,
                                const double *sat, int n, XtCell &c) {
   c.nnbr = g.ia[n + 1] - g.ia[n] - 1;
@@ -51,12 +52,23 @@ __device__ inline void xt_load(const NpfDev &g, const Xt3dDev &x, const int *ibo
       c.vn[il][0] = 0.0;
       c.vn[il][1] = 0.0;
       c.vn[il][2] = z;
-      c.vc[il][0] = 0.0;
-      c.vc[il][1] = 0.0;
-      c.vc[il][2] = z;
       const double z1 = XADD(g.bot[n], XMUL(0.5, XSUB(g.top[n], g.bot[n])));
       const double z2 = XADD(g.bot[jj], XMUL(0.5, XSUB(g.top[jj], g.bot[jj])));
-      dltot = fabs(XSUB(z2, z1));
+      if (x.vcentre) {
+        // DISU: between the cell centres (line_unit_vector)
+        const double *gg = x.geo + 8 * (size_t)jjs + ((jj > n) ? 0 : 4);
+        const double dx = gg[0], dy = gg[1], dz = XSUB(z2, z1);
+        const double vmag = __dsqrt_rn(XADD(XADD(XMUL(dx, dx), XMUL(dy, dy)), XMUL(dz, dz)));
+        c.vc[il][0] = XDIV(dx, vmag);
+        c.vc[il][1] = XDIV(dy, vmag);
+        c.vc[il][2] = XDIV(dz, vmag);
+        dltot = vmag;
+      } else {
+        c.vc[il][0] = 0.0;
+        c.vc[il][1] = 0.0;
+        c.vc[il][2] = z;
+        dltot = fabs(XSUB(z2, z1));
+      }
     } else {
       // x.geo: per connection n < m, from n to m then from m to n
       const double *gg = x.geo + 8 * (size_t)jjs + ((jj > n) ? 0 : 4);

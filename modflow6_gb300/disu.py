@@ -29,6 +29,7 @@ a grid with the attributes the NPF fill and the oracle read.
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -94,7 +95,7 @@ def disu_check(top, bot, area, iac, ja, ihc, idomain=None, voffsettol: float = 0
     return ja
 
 
-def _finalize(n, ia, ja, ihct, cl12t, hwvat) -> dict:
+def _finalize(n, ia, ja, ihct, cl12t, hwvat, angt=None) -> dict:
     """con_finalize (Connections.f90:160-316) on 0-based ia/ja (nja) and the
     per-entry arrays in the same order."""
     nja = ja.size
@@ -147,14 +148,19 @@ def _finalize(n, ia, ja, ihct, cl12t, hwvat) -> dict:
     cl1[jas[upper]] = cl12t[upper]
     cl2[jas[lower]] = cl12t[lower]
     hwva[jas[off]] = hwvat[off]
+    # anglex: the upper triangle's ANGLDEGX in radians (:300-312)
+    anglex = np.zeros(njas)
+    if angt is not None:
+        anglex[jas[upper]] = angt[upper] * (math.atan(1.0) / 45.0)
     return dict(nodes=n, nja=nja, njas=njas, ia=ia.astype(np.int32), ja=ja.astype(np.int32),
                 isym=isym.astype(np.int32), jas=jas.astype(np.int32), ihc=ihc.astype(np.int32),
-                cl1=cl1, cl2=cl2, hwva=hwva)
+                cl1=cl1, cl2=cl2, hwva=hwva, anglex=anglex)
 
 
-def disu_connections(iac, ja, ihc, cl12, hwva, idomain=None) -> dict:
+def disu_connections(iac, ja, ihc, cl12, hwva, idomain=None, angldegx=None) -> dict:
     """The connectivity of a DISU grid from its input arrays (JA 1-based; a
-    negative diagonal entry allowed), reduced to the cells with IDOMAIN 1.
+    negative diagonal entry allowed), reduced to the cells with IDOMAIN 1,
+    with anglex (radians, per connection n < m) from ANGLDEGX when given.
     The result also holds `nodeuser` (reduced -> user, 0-based) and
     `nodereduced` (user -> reduced, -1 for a removed cell)."""
     ia_u = iac_to_ia(iac)
@@ -162,6 +168,7 @@ def disu_connections(iac, ja, ihc, cl12, hwva, idomain=None) -> dict:
     ihc_u = np.asarray(ihc, np.int64)
     cl12_u = np.asarray(cl12, float)
     hwva_u = np.asarray(hwva, float)
+    ang_u = None if angldegx is None else np.asarray(angldegx, float)
     nu = ia_u.size - 1
     idomain = np.ones(nu, np.int64) if idomain is None else np.asarray(idomain, np.int64)
     keep = idomain > 0
@@ -173,7 +180,7 @@ def disu_connections(iac, ja, ihc, cl12, hwva, idomain=None) -> dict:
     nodereduced[keep] = np.arange(n)
     nodeuser = np.flatnonzero(keep)
     if n == nu:
-        out = _finalize(n, ia_u, ja_u, ihc_u, cl12_u, hwva_u)
+        out = _finalize(n, ia_u, ja_u, ihc_u, cl12_u, hwva_u, ang_u)
     else:
         row_u = np.repeat(np.arange(nu), np.diff(ia_u))
         sel = keep[row_u] & keep[ja_u]
@@ -188,7 +195,8 @@ def disu_connections(iac, ja, ihc, cl12, hwva, idomain=None) -> dict:
             raise DisuError(["JA: a row names the same cell twice"])
         ia = np.zeros(n + 1, np.int64)
         np.cumsum(np.bincount(r2, minlength=n), out=ia[1:])
-        out = _finalize(n, ia, c2, ihc_u[sel], cl12_u[sel], hwva_u[sel])
+        out = _finalize(n, ia, c2, ihc_u[sel], cl12_u[sel], hwva_u[sel],
+                        None if ang_u is None else ang_u[sel])
     out.update(nodeuser=nodeuser.astype(np.int32), nodereduced=nodereduced.astype(np.int32))
     return out
 
@@ -271,26 +279,32 @@ def refined_grid(nlay: int, nrow: int, ncol: int, size: float, box: tuple, thick
             top[q + k * ncpl] = thick * (nlay - k) - shift[k, j] * (k > 0)
             bot[q + k * ncpl] = thick * (nlay - k - 1) - shift[k + 1, j] * (k + 1 < nlay)
 
+    # ANGLDEGX of a face by its direction (rows grow southward): east 0,
+    # north 90, west 180, south 270 degrees
+    face_angle = {(0, 1): 0.0, (-1, 0): 90.0, (0, -1): 180.0, (1, 0): 270.0}
+
     def horiz(q):
-        """(neighbour, width) over the four faces of layer cell q"""
+        """(neighbour, width, face angle) over the four faces of layer cell q"""
         i, j, a, b = cells[q]
         out = []
         if fine[i, j]:
             # within the parent, then across the parent's faces
             for da, db in ((-1, 0), (1, 0), (0, -1), (0, 1)):
+                ang = face_angle[(da, db)]
                 na, nb = a + da, b + db
                 if 0 <= na <= 1 and 0 <= nb <= 1:
-                    out.append((idx[(i, j, na, nb)], 0.5 * size))
+                    out.append((idx[(i, j, na, nb)], 0.5 * size, ang))
                     continue
                 ii, jj = i + (na > 1) - (na < 0), j + (nb > 1) - (nb < 0)
                 if not (0 <= ii < nrow and 0 <= jj < ncol):
                     continue
                 if fine[ii, jj]:
-                    out.append((idx[(ii, jj, na % 2, nb % 2)], 0.5 * size))
+                    out.append((idx[(ii, jj, na % 2, nb % 2)], 0.5 * size, ang))
                 else:
-                    out.append((idx[(ii, jj, 0, 0)], 0.5 * size))
+                    out.append((idx[(ii, jj, 0, 0)], 0.5 * size, ang))
         else:
             for di, dj in ((-1, 0), (1, 0), (0, -1), (0, 1)):
+                ang = face_angle[(di, dj)]
                 ii, jj = i + di, j + dj
                 if not (0 <= ii < nrow and 0 <= jj < ncol):
                     continue
@@ -298,39 +312,40 @@ def refined_grid(nlay: int, nrow: int, ncol: int, size: float, box: tuple, thick
                     # the two children along the shared face
                     if di:
                         a2 = 1 if di < 0 else 0
-                        out += [(idx[(ii, jj, a2, b2)], 0.5 * size) for b2 in (0, 1)]
+                        out += [(idx[(ii, jj, a2, b2)], 0.5 * size, ang) for b2 in (0, 1)]
                     else:
                         b2 = 1 if dj < 0 else 0
-                        out += [(idx[(ii, jj, a2, b2)], 0.5 * size) for a2 in (0, 1)]
+                        out += [(idx[(ii, jj, a2, b2)], 0.5 * size, ang) for a2 in (0, 1)]
                 else:
-                    out.append((idx[(ii, jj, 0, 0)], size))
+                    out.append((idx[(ii, jj, 0, 0)], size, ang))
         return out
 
-    iac, ja, ihc, cl12, hwva = [], [], [], [], []
+    iac, ja, ihc, cl12, hwva, angx = [], [], [], [], [], []
     for k in range(nlay):
         for q in range(ncpl):
             p = q + k * ncpl
-            ent = [(p, 1, 0.0, 0.0)]
+            ent = [(p, 1, 0.0, 0.0, 0.0)]
             area_q = (2 * half[q]) ** 2
             if k > 0:
-                ent.append((p - ncpl, 0, 0.5 * (top[p] - bot[p]), area_q))
+                ent.append((p - ncpl, 0, 0.5 * (top[p] - bot[p]), area_q, 0.0))
             if k < nlay - 1:
-                ent.append((p + ncpl, 0, 0.5 * (top[p] - bot[p]), area_q))
-            for q2, w in horiz(q):
+                ent.append((p + ncpl, 0, 0.5 * (top[p] - bot[p]), area_q, 0.0))
+            for q2, w, ang in horiz(q):
                 p2 = q2 + k * ncpl
                 stag = top[p] != top[p2] or bot[p] != bot[p2]
-                ent.append((p2, 2 if stag else 1, half[q], w))
+                ent.append((p2, 2 if stag else 1, half[q], w, ang))
             ent = [ent[0]] + sorted(ent[1:])
             iac.append(len(ent))
-            for m, h, c, w in ent:
+            for m, h, c, w, ang in ent:
                 ja.append(m + 1)
                 ihc.append(h)
                 cl12.append(c)
                 hwva.append(w)
+                angx.append(ang)
     area = np.tile((2 * half) ** 2, nlay)
     return dict(iac=np.array(iac), ja=np.array(ja), ihc=np.array(ihc), cl12=np.array(cl12),
-                hwva=np.array(hwva), top=top, bot=bot, area=area, xc=np.tile(xc, nlay),
-                yc=np.tile(yc, nlay), ncpl=ncpl)
+                hwva=np.array(hwva), angldegx=np.array(angx), top=top, bot=bot, area=area,
+                xc=np.tile(xc, nlay), yc=np.tile(yc, nlay), ncpl=ncpl)
 
 
 @dataclass
@@ -371,12 +386,28 @@ class DisuModel:
     icellavg: int = 0
     name: str = ""
     disu: bool = True
+    angldegx: np.ndarray | None = None  # per entry, degrees (ANGLDEGX)
+    xc_u: np.ndarray | None = None      # per user cell: the cell centre (CELL2D)
+    yc_u: np.ndarray | None = None
+    ixt3d: int = 0                      # NPF XT3D (matrix form): needs angldegx and the centres
+    k22: np.ndarray | None = None
+    angle1: np.ndarray | None = None    # degrees
+    angle2: np.ndarray | None = None
+    angle3: np.ndarray | None = None
 
     def __post_init__(self):
         self.ja = disu_check(self.top_u, self.bot_u, self.area_u, self.iac, self.ja, self.ihc_u,
                              self.idomain, self.voffsettol)
         self._con = disu_connections(self.iac, self.ja, self.ihc_u, self.cl12, self.hwva_u,
-                                     self.idomain)
+                                     self.idomain, self.angldegx)
+
+    @property
+    def xc(self) -> np.ndarray:
+        return np.asarray(self.xc_u, float)[self.nodeuser]
+
+    @property
+    def yc(self) -> np.ndarray:
+        return np.asarray(self.yc_u, float)[self.nodeuser]
 
     @property
     def nlay(self) -> int:
@@ -455,7 +486,8 @@ def make_disu_model(nlay: int = 2, nrow: int = 12, ncol: int = 16, seed: int = 0
                                  np.full(east.size * nlay, 7.0 * nlay)])
     m = DisuModel(g["top"], g["bot"], g["area"], g["iac"], g["ja"], g["ihc"], g["cl12"], g["hwva"],
                   k, 0.1 * k, ict, strt, idomain=idomain if idomain_holes else None,
-                  inewton=1 if newton else 0, name="disu-refined")
+                  inewton=1 if newton else 0, name="disu-refined", angldegx=g["angldegx"],
+                  xc_u=g["xc"], yc_u=g["yc"])
     if transient:
         m.ss, m.sy = np.full(n, 1e-5), np.full(n, 0.15)
     m.chd_node = red[chd_u].astype(np.int32)

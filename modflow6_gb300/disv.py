@@ -24,6 +24,7 @@ with the attributes the NPF fill and the oracle read.
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -167,9 +168,17 @@ def disv_connections(nlay: int, iavert, javert, vx, vy, xc, yc, top, bot) -> dic
 
     cl1[sh] = dnorm(xc[jn[hz]], yc[jn[hz]])
     cl2[sh] = dnorm(xc[jm[hz]], yc[jm[hz]])
+    # anglex (DisvGeom.f90:193-199, 394-412): the angle of the shared edge's
+    # normal, atan2(dx, -dy) of the edge in the lower-numbered cell's vertex
+    # order, in [0, 2 pi); evaluated with the C library's atan2 one value at
+    # a time, as the Fortran does
+    anglex = np.zeros(njas)
+    two_pi = 2.0 * (4.0 * math.atan(1.0))
+    ax = [math.atan2(float(a), float(-b)) for a, b in zip(x2 - x1, y2 - y1)]
+    anglex[sh] = [v if v >= 0.0 else two_pi + v for v in ax]
     return dict(nodes=n, nja=nja, njas=njas, ia=ia.astype(np.int32), ja=ja.astype(np.int32),
                 isym=isym.astype(np.int32), jas=jas.astype(np.int32), ihc=ihc.astype(np.int32),
-                cl1=cl1, cl2=cl2, hwva=hwva, area=area)
+                cl1=cl1, cl2=cl2, hwva=hwva, area=area, anglex=anglex)
 
 
 @dataclass
@@ -204,6 +213,11 @@ class DisvModel:
     icellavg: int = 0
     name: str = ""
     disv: bool = True
+    ixt3d: int = 0                     # NPF XT3D (matrix form)
+    k22: np.ndarray | None = None
+    angle1: np.ndarray | None = None   # degrees
+    angle2: np.ndarray | None = None
+    angle3: np.ndarray | None = None
 
     @property
     def ncpl(self) -> int:

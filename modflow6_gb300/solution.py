@@ -171,8 +171,6 @@ class GwfSolution:
                                   nl.res_lim)
         self._h = C.c_void_p()
         xt3d = bool(int(getattr(m, "ixt3d", 0)))
-        if xt3d and general:
-            raise _lib.GbimsError(_lib.GBIMS_ERR_UNSUPPORTED, "XT3D is built for DIS grids")
         if xt3d:
             from .xt3d import xt3d_pattern
             con = m.connections()
@@ -186,6 +184,20 @@ class GwfSolution:
                 return _lib.dptr(keep["xt_" + name])
 
             cx = _lib.GbslnXt3d(opt("k22"), opt("angle1"), opt("angle2"), opt("angle3"))
+        if xt3d and general:
+            # the connection geometry: cell centres and face-normal angles
+            disu = bool(getattr(m, "disu", False))
+            if disu:
+                xcn, ycn = m.xc, m.yc
+            else:
+                xcn, ycn = np.tile(m.xc, m.nlay), np.tile(m.yc, m.nlay)
+            keep.update(x_xc=_f(xcn), x_yc=_f(ycn), x_ax=_f(con["anglex"]))
+            cg = _lib.GbslnXt3dGeometry(_lib.dptr(keep["x_xc"]), _lib.dptr(keep["x_yc"]),
+                                        _lib.dptr(keep["x_ax"]), int(disu))
+            rc = lib.gbsln_create_grid_xt3d(C.byref(grid), C.byref(cm), C.byref(cx), C.byref(cg),
+                                            C.byref(npf), C.byref(cs), C.byref(cnl),
+                                            _lib.dptr(keep["strt"]), C.byref(self._h))
+        elif xt3d:
             rc = lib.gbsln_create_xt3d(C.byref(cm), C.byref(cx), C.byref(npf), C.byref(cs),
                                        C.byref(cnl), _lib.dptr(keep["strt"]), C.byref(self._h))
         elif general:

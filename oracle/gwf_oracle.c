@@ -254,6 +254,7 @@ double or_squadratic_sat_derv(double top, double bot, double x, double eps) {
 /* ------------------------------------------------------------------------ */
 
 static int cmp_int(const void *a, const void *b);
+static void disv_shared_edge(const int *l1, int nv1, const int *l2, int nv2, int *iv1, int *iv2);
 
 /* disuconnections (Connections.f90:801-928) then con_finalize (:160-316),
  * 0-based.  A full grid copies IA/JA; a reduced one builds each kept row as
@@ -261,9 +262,9 @@ static int cmp_int(const void *a, const void *b);
  * neighbours sorted, Sparse.f90:217-239) and compresses the per-entry arrays
  * in input order. */
 int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int *ihcinp,
-                    const double *cl12inp, const double *hwvainp, const int *nodereduced,
-                    int cap, int *nodes_out, int *ia, int *ja, int *isym, int *jas, int *ihc,
-                    double *cl1, double *cl2, double *hwva) {
+                    const double *cl12inp, const double *hwvainp, const double *angldegxinp,
+                    const int *nodereduced, int cap, int *nodes_out, int *ia, int *ja, int *isym,
+                    int *jas, int *ihc, double *cl1, double *cl2, double *hwva, double *anglex) {
   int nodes = nodesuser;
   if (nodereduced) {
     nodes = 0;
@@ -273,7 +274,7 @@ int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int
   *nodes_out = nodes;
   if (nodes == 0) return -8;
   int nja = 0;
-  double *cl12t = NULL, *hwvat = NULL;
+  double *cl12t = NULL, *hwvat = NULL, *angt = NULL;
   int *ihcti = NULL;
   if (!nodereduced) {
     nja = iainp[nodesuser];
@@ -281,6 +282,7 @@ int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int
     ihcti = (int *)malloc(sizeof(int) * (nja + 1));
     cl12t = (double *)malloc(sizeof(double) * (nja + 1));
     hwvat = (double *)malloc(sizeof(double) * (nja + 1));
+    angt = (double *)malloc(sizeof(double) * (nja + 1));
     for (int n = 0; n <= nodes; ++n) ia[n] = iainp[n];
     for (int q = 0; q < nja; ++q) {
       int v = jainp[q];
@@ -288,6 +290,7 @@ int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int
       ihcti[q] = ihcinp[q];
       cl12t[q] = cl12inp[q];
       hwvat[q] = hwvainp[q];
+      angt[q] = angldegxinp ? angldegxinp[q] : 0.0;
     }
   } else {
     /* rows of the sparse matrix, in reduced order */
@@ -317,6 +320,7 @@ int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int
     ihcti = (int *)malloc(sizeof(int) * (nja + 1));
     cl12t = (double *)malloc(sizeof(double) * (nja + 1));
     hwvat = (double *)malloc(sizeof(double) * (nja + 1));
+    angt = (double *)malloc(sizeof(double) * (nja + 1));
     int iposr = 0;
     for (int u = 0; u < nodesuser; ++u) {
       int nr = nodereduced[u];
@@ -325,12 +329,13 @@ int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int
         int mr = nodereduced[mu];
         if (nr < 0 || mr < 0) continue;
         if (iposr >= nja) { /* a duplicated entry: the arrays would overrun */
-          free(ihcti); free(cl12t); free(hwvat);
+          free(ihcti); free(cl12t); free(hwvat); free(angt);
           return -3;
         }
         ihcti[iposr] = ihcinp[q];
         cl12t[iposr] = cl12inp[q];
         hwvat[iposr] = hwvainp[q];
+        angt[iposr] = angldegxinp ? angldegxinp[q] : 0.0;
         iposr++;
       }
     }
@@ -381,9 +386,42 @@ int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int
         if (ihcti[q] < 0 || ihcti[q] > 2) { rc = -7; break; }
         hwva[jas[q]] = hwvat[q];
       }
+    /* anglex: the upper triangle's ANGLDEGX in radians (:300-307) */
+    if (rc >= 0 && anglex) {
+      const double dpio180 = atan(1.0) / 45.0;
+      for (int n = 0; n < nodes; ++n)
+        for (int q = ia[n] + 1; q < ia[n + 1]; ++q)
+          if (ja[q] > n) anglex[jas[q]] = angt[q] * dpio180;
+    }
   }
-  free(ihcti); free(cl12t); free(hwvat);
+  free(ihcti); free(cl12t); free(hwvat); free(angt);
   return rc;
+}
+
+void or_disv_anglex(int nlay, int ncpl, const double *vx, const double *vy, const int *iavert,
+                    const int *javert, const int *ia, const int *ja, const int *jas,
+                    const int *ihc, double *anglex) {
+  const double dpi = 4.0 * atan(1.0);
+  const int nodes = nlay * ncpl;
+  for (int n = 0; n < nodes; ++n) {
+    const int jn = n % ncpl;
+    for (int ii = ia[n] + 1; ii < ia[n + 1]; ++ii) {
+      const int m = ja[ii];
+      if (m < n) continue;
+      const int s = jas[ii];
+      anglex[s] = 0.0;
+      if (ihc[s] == 0) continue;
+      const int jm = m % ncpl;
+      int a, b;
+      disv_shared_edge(javert + iavert[jn], iavert[jn + 1] - iavert[jn], javert + iavert[jm],
+                       iavert[jm + 1] - iavert[jm], &a, &b);
+      if (a < 0 || b < 0) continue;
+      double dx = vx[b] - vx[a], dy = vy[b] - vy[a];
+      double ax = atan2(dx, -dy);
+      if (ax < 0.0) ax = 2.0 * dpi + ax;
+      anglex[s] = ax;
+    }
+  }
 }
 
 /* ------------------------------------------------------------------------ */

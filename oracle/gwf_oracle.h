@@ -46,6 +46,11 @@ typedef struct {
   int ixt3d, nozee, nja_sln;
   const double *ck;
   const int *sia, *sja, *idxglo;
+  /* the grid's connection geometry for XT3D: 0 DIS (from the cell's row
+   * and column), 1 DISV, 2 DISU (cell centres xc/yc per node, anglex per
+   * connection n < m in radians) */
+  int xt_grid;
+  const double *xc, *yc, *anglex;
 } or_gwf_model;
 
 /* NONLINEAR block state (NumericalSolution.f90 members). */
@@ -85,9 +90,15 @@ int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, cons
  * symmetric), -6 (HWVA not symmetric), -7 (IHC outside 0..2), -8 (no
  * active cell). */
 int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int *ihcinp,
-                    const double *cl12inp, const double *hwvainp, const int *nodereduced,
-                    int cap, int *nodes, int *ia, int *ja, int *isym, int *jas, int *ihc,
-                    double *cl1, double *cl2, double *hwva);
+                    const double *cl12inp, const double *hwvainp, const double *angldegxinp,
+                    const int *nodereduced, int cap, int *nodes, int *ia, int *ja, int *isym,
+                    int *jas, int *ihc, double *cl1, double *cl2, double *hwva, double *anglex);
+/* DisvGeom.f90:193-199 and :394-412 (cprops' anglex): the angle of the
+ * shared edge's normal for each horizontal connection n < m of a full DISV
+ * grid, 0 for vertical ones */
+void or_disv_anglex(int nlay, int ncpl, const double *vx, const double *vy, const int *iavert,
+                    const int *javert, const int *ia, const int *ja, const int *jas,
+                    const int *ihc, double *anglex);
 void or_xt3d_ck(int nodes, const double *k11, const double *k22, const double *k33,
                 const double *angle1, const double *angle2, const double *angle3, int nozee,
                 double *ck);

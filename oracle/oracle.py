@@ -59,7 +59,8 @@ class GwfModel(C.Structure):
                 ("nrch", C.c_int), ("rch_node", _ip), ("rch_rate", _dp),
                 ("nchd", C.c_int), ("chd_node", _ip), ("chd_head", _dp),
                 ("ixt3d", C.c_int), ("nozee", C.c_int), ("nja_sln", C.c_int), ("ck", _dp),
-                ("sia", _ip), ("sja", _ip), ("idxglo", _ip)]
+                ("sia", _ip), ("sja", _ip), ("idxglo", _ip),
+                ("xt_grid", C.c_int), ("xc", _dp), ("yc", _dp), ("anglex", _dp)]
 
 
 class Nonlinear(C.Structure):
@@ -131,8 +132,10 @@ def load():
         lib.or_xt3d_pattern.argtypes = [C.c_int, _ip, _ip, C.c_int, _ip, _ip, _ip]
         lib.or_xt3d_fc.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, _dp, _dp]
         lib.or_xt3d_fn.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, _dp, _dp]
-        lib.or_disu_connect.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _ip, C.c_int, _ip, _ip,
-                                        _ip, _ip, _ip, _ip, _dp, _dp, _dp]
+        lib.or_disu_connect.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _ip, C.c_int, _ip,
+                                        _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
+        lib.or_disv_anglex.argtypes = [C.c_int, C.c_int, _dp, _dp, _ip, _ip, _ip, _ip, _ip, _ip,
+                                       _dp]
         lib.or_npf_condsat.argtypes = [C.POINTER(GwfModel), _dp]
         lib.or_gwf_fc.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, C.c_double, C.c_int, _dp, _dp, _dp, _dp]
         lib.or_sln_ls_fixups.argtypes = [C.c_int, _ip, _ip, _ip, C.c_int, _dp, _dp, _dp, _dp]
@@ -367,10 +370,11 @@ DISU_ERRORS = {-1: "capacity exceeded", -2: "diagonal not first", -3: "row not a
                -6: "HWVA not symmetric", -7: "IHC outside 0..2", -8: "no active cell"}
 
 
-def disu_connect(iac, ja, ihc, cl12, hwva, idomain=None) -> dict:
+def disu_connect(iac, ja, ihc, cl12, hwva, idomain=None, angldegx=None) -> dict:
     """or_disu_connect: the connectivity of a DISU grid from its input arrays
-    (JA 1-based), reduced to the cells with IDOMAIN > 0.  Raises ValueError
-    with the failing check."""
+    (JA 1-based), reduced to the cells with IDOMAIN > 0, with anglex
+    (radians, per connection n < m) when ANGLDEGX is given.  Raises
+    ValueError with the failing check."""
     lib = load()
     iac = np.asarray(iac, np.int64)
     nu = iac.size
@@ -389,11 +393,14 @@ def disu_connect(iac, ja, ihc, cl12, hwva, idomain=None) -> dict:
     n = C.c_int()
     out = dict(ia=np.zeros(nu + 1, np.int32), ja=np.zeros(cap, np.int32), isym=np.zeros(cap, np.int32),
                jas=np.zeros(cap, np.int32), ihc=np.zeros(cap, np.int32), cl1=np.zeros(cap),
-               cl2=np.zeros(cap), hwva=np.zeros(cap))
+               cl2=np.zeros(cap), hwva=np.zeros(cap), anglex=np.zeros(cap))
+    ang = f(angldegx) if angldegx is not None else None
     nja = lib.or_disu_connect(nu, ip(iainp), ip(jainp), ip(ihcinp), dp(cl12inp), dp(hwvainp),
+                              dp(ang) if ang is not None else None,
                               ip(red) if red is not None else None, cap, C.byref(n),
                               ip(out["ia"]), ip(out["ja"]), ip(out["isym"]), ip(out["jas"]),
-                              ip(out["ihc"]), dp(out["cl1"]), dp(out["cl2"]), dp(out["hwva"]))
+                              ip(out["ihc"]), dp(out["cl1"]), dp(out["cl2"]), dp(out["hwva"]),
+                              dp(out["anglex"]))
     if nja < 0:
         raise ValueError("or_disu_connect: " + DISU_ERRORS.get(nja, str(nja)))
     nodes = n.value
@@ -401,7 +408,7 @@ def disu_connect(iac, ja, ihc, cl12, hwva, idomain=None) -> dict:
     out["ia"] = out["ia"][:nodes + 1].copy()
     for k in ("ja", "isym", "jas"):
         out[k] = out[k][:nja].copy()
-    for k in ("ihc", "cl1", "cl2", "hwva"):
+    for k in ("ihc", "cl1", "cl2", "hwva", "anglex"):
         out[k] = out[k][:njas].copy()
     out.update(nodes=nodes, nja=nja, njas=njas)
     return out
@@ -416,7 +423,8 @@ class Gwf:
         self.lib = load()
         self.m = m
         if getattr(m, "disu", False):
-            con = disu_connect(m.iac, m.ja, m.ihc_u, m.cl12, m.hwva_u, m.idomain)
+            con = disu_connect(m.iac, m.ja, m.ihc_u, m.cl12, m.hwva_u, m.idomain,
+                               getattr(m, "angldegx", None))
             area = m.area
         elif getattr(m, "disv", False):
             iav, jav = m.vertex_lists
@@ -456,8 +464,6 @@ class Gwf:
         self.mcon = con
         if int(getattr(m, "ixt3d", 0)):
             # XT3D on a DIS grid: the tensor per cell and the wider pattern
-            if getattr(m, "disv", False) or getattr(m, "disu", False):
-                raise NotImplementedError("the oracle restates XT3D on DIS grids")
             nozee = m.angle2 is None
             dpio180 = math.atan(1.0) / 45.0
             rad = lambda a: (np.zeros(n) if a is None else np.asarray(a, float) * dpio180)
@@ -476,6 +482,22 @@ class Gwf:
             sja = sja[:nja_sln].copy()
             self.model.ixt3d, self.model.nozee, self.model.nja_sln = 1, int(nozee), nja_sln
             self.model.ck, self.model.sia, self.model.sja, self.model.idxglo = d(ck), i(sia), i(sja), i(idxglo)
+            if getattr(m, "disv", False) or getattr(m, "disu", False):
+                # DISV: the shared edges' normal angles (cprops); DISU: ANGLDEGX
+                if getattr(m, "disv", False):
+                    iav, jav = m.vertex_lists
+                    ax = np.zeros(con["njas"])
+                    self.lib.or_disv_anglex(m.nlay, len(m.icvert), d(m.vertices[:, 0]),
+                                            d(m.vertices[:, 1]), i(iav), i(jav), i(con["ia"]),
+                                            i(con["ja"]), i(con["jas"]), i(con["ihc"]), dp(ax))
+                    xcn, ycn = np.tile(m.xc, m.nlay), np.tile(m.yc, m.nlay)
+                    self.model.xt_grid = 1
+                else:
+                    ax = con["anglex"]
+                    xcn, ycn = m.xc, m.yc
+                    self.model.xt_grid = 2
+                self.model.xc, self.model.yc, self.model.anglex = d(xcn), d(ycn), d(ax)
+                con = dict(con, anglex=ax)
             con = dict(con, ia=sia, ja=sja, nja=nja_sln, idxglo=idxglo, ck=ck)
         self.con = con
         self._keep = keep

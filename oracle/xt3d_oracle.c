@@ -1,7 +1,8 @@
 /*
  * xt3d_oracle.c -- CPU restatement of XT3D, the NPF formulation with the
  * full conductivity tensor and the extended stencil (Xt3dInterface.f90,
- * Xt3dAlgorithm.f90), matrix form (XT3D without RHS), on DIS grids.
+ * Xt3dAlgorithm.f90), matrix form (XT3D without RHS), on DIS, DISV and
+ * DISU grids.
  * TEST INFRASTRUCTURE ONLY (the oracle); the product never includes this.
  *
  * Loops, branches and the order of every sum follow the Fortran.  Arrays are
@@ -194,6 +195,59 @@ static void dis_vector(const or_gwf_model *m, int n, int nm, int nozee, double s
   }
 }
 
+/* line_unit_vector (DisvGeom.f90:473-496) */
+static void unit_vector(double x0, double y0, double z0, double x1, double y1, double z1,
+                        double *v, double *vmag) {
+  double dx = x1 - x0, dy = y1 - y0, dz = z1 - z0;
+  *vmag = sqrt(dx * dx + dy * dy + dz * dz);
+  v[0] = dx / *vmag;
+  v[1] = dy / *vmag;
+  v[2] = dz / *vmag;
+}
+
+/* connection_normal: DIS (Dis.f90:1039-1087); DISV and DISU from anglex
+ * (Disv.f90:979-1018, Disu.f90:1062-1102) */
+static void conn_normal(const or_gwf_model *m, int n, int nm, int ihc, int ipos, double *v) {
+  if (m->xt_grid == 0) {
+    dis_normal(m, n, nm, ihc, v);
+    return;
+  }
+  if (ihc == 0) {
+    v[0] = 0.0;
+    v[1] = 0.0;
+    v[2] = (nm < n) ? 1.0 : -1.0;
+  } else {
+    double angle = m->anglex[m->jas[ipos]];
+    double dmult = (nm < n) ? -1.0 : 1.0;
+    v[0] = cos(angle) * dmult;
+    v[1] = sin(angle) * dmult;
+    v[2] = 0.0;
+  }
+}
+
+/* connection_vector: DIS (Dis.f90:1094-1160), DISV (Disv.f90:1024-1080:
+ * vertical as DIS, horizontal between the cell centres) and DISU
+ * (Disu.f90:1108-1164: between the cell centres, vertical ones included) */
+static void conn_vector(const or_gwf_model *m, int n, int nm, int nozee, double satn,
+                        double satm, int ihc, double *v, double *conlen) {
+  if (m->xt_grid == 0 || (m->xt_grid == 1 && ihc == 0)) {
+    dis_vector(m, n, nm, nozee, satn, satm, ihc, v, conlen);
+    return;
+  }
+  double zn, zm;
+  if (ihc == 0) {
+    zn = m->bot[n] + 0.5 * (m->top[n] - m->bot[n]);
+    zm = m->bot[nm] + 0.5 * (m->top[nm] - m->bot[nm]);
+  } else if (nozee) {
+    zn = 0.0;
+    zm = 0.0;
+  } else {
+    zn = m->bot[n] + 0.5 * satn * (m->top[n] - m->bot[n]);
+    zm = m->bot[nm] + 0.5 * satm * (m->top[nm] - m->bot[nm]);
+  }
+  unit_vector(m->xc[n], m->yc[n], zn, m->xc[nm], m->yc[nm], zm, v, conlen);
+}
+
 /* xt3d_load (Xt3dInterface.f90:1211-1275) */
 static void xt3d_load(const xt3d_t *x, int n, int nnbr, int *inbr, double vc[][3],
                       double vn[][3], double *dl, double *dln, int *allhc) {
@@ -208,8 +262,8 @@ static void xt3d_load(const xt3d_t *x, int n, int nnbr, int *inbr, double vc[][3
       double satn = x->sat[n], satjj = x->sat[jj];
       int ihc = m->ihc[jjs];
       double dltot;
-      dis_normal(m, n, jj, ihc, vn[il]);
-      dis_vector(m, n, jj, m->nozee, satn, satjj, ihc, vc[il], &dltot);
+      conn_normal(m, n, jj, ihc, ii, vn[il]);
+      conn_vector(m, n, jj, m->nozee, satn, satjj, ihc, vc[il], &dltot);
       double cl1njj, cl2njj;
       if (jj > n) {
         cl1njj = m->cl1[jjs];

@@ -215,3 +215,129 @@ def test_gpu_xt3d_newton_timestep_matches_oracle(gblib):
     assert so["converged"] == 1 and sg["converged"] == 1
     assert abs(sg["outer"] - so["outer"]) <= 1
     assert np.abs(sol.heads - g.x).max() < 1e-6
+
+
+# ---- DISV and DISU grids ---------------------------------------------------
+
+def _general_linear(m, xt3d=True, icelltype=0, angle=30.0):
+    """XT3D on a DISV or DISU model: K = R diag(5, 1, 0.5) R^T rotated by
+    ANGLE1 in the plane, CHD on the cells of the grid's outer ring with
+    h = 100 + 0.03 x - 0.02 y, which is then the exact solution (no flux
+    through the top and bottom: the tensor has no vertical coupling)."""
+    n = m.nodes
+    con = m.connections()
+    m.k11, m.k33 = np.full(n, 5.0), np.full(n, 0.5)
+    m.k22 = np.full(n, 1.0)
+    m.angle1 = np.full(n, angle)
+    m.angle2 = m.angle3 = None
+    m.icelltype = np.full(n, icelltype, np.int32)
+    m.ixt3d = 1 if xt3d else 0
+    if getattr(m, "disu", False):
+        x, y = m.xc, m.yc
+        full = 4
+    else:
+        x, y = np.tile(m.xc, m.nlay), np.tile(m.yc, m.nlay)
+        full = 6
+    h = 100.0 + 0.03 * x - 0.02 * y
+    rown = np.repeat(np.arange(n), np.diff(con["ia"]))
+    off = con["ja"] != rown
+    hz = off & (con["ihc"][np.maximum(con["jas"], 0)] != 0)
+    hdeg = np.bincount(rown[hz], minlength=n)
+    bnd = hdeg < full
+    m.chd_node = np.flatnonzero(bnd).astype(np.int32)
+    m.chd_head = h[bnd]
+    m.wel_node = np.zeros(0, np.int32)
+    m.wel_q = np.zeros(0)
+    m.rch_node = np.zeros(0, np.int32)
+    m.rch_rate = np.zeros(0)
+    m.strt = np.where(bnd, h, 100.0)
+    return m, h
+
+
+def _disv():
+    from modflow6_gb300.disv import make_disv_model
+    return make_disv_model(3, 14, 10, seed=3)
+
+
+def _disu():
+    from modflow6_gb300.disu import make_disu_model
+    return make_disu_model(2, 12, 15, seed=3)
+
+
+GENERAL = [("disv", _disv), ("disu", _disu)]
+
+
+def test_anglex_matches_oracle():
+    from modflow6_gb300.disu import refined_grid
+    m = _disv()
+    con = m.connections()
+    iav, jav = m.vertex_lists
+    ax = np.zeros(con["njas"])
+    lib = oracle.load()
+    keep = [np.ascontiguousarray(a, np.float64) for a in (m.vertices[:, 0], m.vertices[:, 1])]
+    ints = [np.ascontiguousarray(a, np.int32) for a in (iav, jav, con["ia"], con["ja"], con["jas"],
+                                                        con["ihc"])]
+    lib.or_disv_anglex(m.nlay, len(m.icvert), oracle.dp(keep[0]), oracle.dp(keep[1]),
+                       *[oracle.ip(a) for a in ints], oracle.dp(ax))
+    np.testing.assert_array_equal(con["anglex"], ax)
+    assert (ax[con["ihc"] != 0] > 0).any()
+    g = refined_grid(2, 8, 10, 50.0, (2, 5, 3, 6), seed=1)
+    from modflow6_gb300.disu import disu_connections
+    c = disu_connections(g["iac"], g["ja"], g["ihc"], g["cl12"], g["hwva"], angldegx=g["angldegx"])
+    o = oracle.disu_connect(g["iac"], g["ja"], g["ihc"], g["cl12"], g["hwva"], angldegx=g["angldegx"])
+    np.testing.assert_array_equal(c["anglex"], o["anglex"])
+    # each connection n < m points from n to m: east 0, south 3 pi / 2
+    assert set(np.round(np.degrees(c["anglex"][c["ihc"] != 0]))) <= {0.0, 270.0}
+
+
+@pytest.mark.parametrize("name,make", GENERAL, ids=[g[0] for g in GENERAL])
+def test_oracle_general_grid_reproduces_uniform_anisotropic_flow(name, make):
+    tol = dict(dvclose=1e-12, rclose=1e-10, iter1=4000, ilinmeth=2)
+    m, h = _general_linear(make())
+    g = oracle.Gwf(m, oracle.settings(**tol))
+    st = g.timestep(kper=1, kstp=1, delt=1.0, dvclose=1e-11, mxiter=20)
+    assert st["converged"] == 1
+    assert np.abs(g.x - h).max() < 1e-9
+    ms, _ = _general_linear(make(), xt3d=False)
+    gs = oracle.Gwf(ms, oracle.settings(**tol))
+    gs.timestep(kper=1, kstp=1, delt=1.0, dvclose=1e-11, mxiter=20)
+    assert np.abs(gs.x - h).max() > 0.05
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("icelltype,newton,transient", [(0, 0, 0), (1, 0, 1), (1, 1, 1)],
+                         ids=["confined", "convertible", "newton"])
+@pytest.mark.parametrize("name,make", GENERAL, ids=[g[0] for g in GENERAL])
+def test_gpu_general_grid_xt3d_fill_bitexact(gblib, name, make, icelltype, newton, transient):
+    """The device fill with XT3D on DISV and DISU grids (cell-centre vectors,
+    face normals from the edges or ANGLDEGX, DISU's centre-to-centre vertical
+    vectors) against the oracle's, bit for bit."""
+    m, h = _general_linear(make(), icelltype=icelltype, angle=35.0)
+    m.inewton = newton
+    if transient:
+        m.ss, m.sy = np.full(m.nodes, 1e-5), np.full(m.nodes, 0.15)
+    g, sol = _gpu_pair(m)
+    rng = np.random.default_rng(4)
+    cb = m.cell_bot
+    hh = np.maximum(h, cb + 1.0) + rng.uniform(-12.0, 2.0, m.nodes)
+    hold = h + rng.uniform(-1.0, 1.0, m.nodes)
+    sol.heads = hh
+    delt = 2.5 if transient else 0.0
+    amat, rhs = sol.formulate(delt=delt, hold=hold if transient else None)
+    ao, ro = g.assemble(hh, hold=hold, delt=delt, transient=bool(transient))
+    assert amat.size == ao.size == g.con["nja"]
+    np.testing.assert_array_equal(amat, ao)
+    np.testing.assert_array_equal(rhs, ro)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,make", GENERAL, ids=[g[0] for g in GENERAL])
+def test_gpu_general_grid_xt3d_timestep(gblib, name, make):
+    from modflow6_gb300.ims import ImsLinearSettings
+    from modflow6_gb300.solution import GwfSolution, Nonlinear
+    tol = dict(dvclose=1e-12, rclose=1e-10, iter1=4000, ilinmeth=2)
+    m, h = _general_linear(make())
+    sol = GwfSolution(m, ImsLinearSettings(**tol), Nonlinear(dvclose=1e-11, mxiter=20))
+    sg = sol.timestep(1, 1, 1.0)
+    assert sg["converged"] == 1
+    assert np.abs(sol.heads - h).max() < 1e-9
