@@ -394,11 +394,13 @@ int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,
 typedef struct gbsln_xt3d {
   const double *k22;
   const double *angle1, *angle2, *angle3;
+  int rhs;  /* 1: XT3D RHS, the neighbours' terms on the right-hand side at
+               the current heads and the model's own pattern (:478-490) */
 } gbsln_xt3d;
 
 /* gbsln_create with XT3D.  ALTERNATIVE_CELL_AVERAGING (icellavg > 0) is
- * refused as the reference refuses it (GBIMS_ERR_ARG); gbsln_budget returns
- * GBIMS_ERR_UNSUPPORTED (xt3d_flowja is not built). */
+ * refused as the reference refuses it (GBIMS_ERR_ARG); gbsln_budget takes
+ * the flows from xt3d_flowja (Xt3dInterface.f90:797-875). */
 int gbsln_create_xt3d(const gbsln_model *model, const gbsln_xt3d *xt3d,
                       const gbnpf_options *npf, const gbims_settings *ims,
                       const gbsln_nonlinear *nl, const double *strt, gbsln_handle **out);

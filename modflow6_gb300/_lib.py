@@ -81,7 +81,7 @@ class GbslnGrid(C.Structure):
 
 
 class GbslnXt3d(C.Structure):
-    _fields_ = [("k22", _dp), ("angle1", _dp), ("angle2", _dp), ("angle3", _dp)]
+    _fields_ = [("k22", _dp), ("angle1", _dp), ("angle2", _dp), ("angle3", _dp), ("rhs", C.c_int)]
 
 
 class GbslnXt3dGeometry(C.Structure):

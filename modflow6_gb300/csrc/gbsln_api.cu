@@ -181,7 +181,12 @@ extern "C" int gbnpf_create(const gbnpf_options *opt, int nodes, int nja, int nj
   h->g.idewatcv = opt->idewatcv;
   h->g.icellavg = opt->icellavg;
   h->g.satomega = opt->satomega > 0 ? opt->satomega : 1.0e-6;
-  cudaMemset(h->d.sat, 0, sizeof(double) * nodes);
+  {
+    // npf_ar's initial saturation: 1 in every cell; npf_cf updates the
+    // convertible ones (gwf-npf.f90:1853-1884)
+    std::vector<double> one((size_t)nodes, 1.0);
+    cudaMemcpy(h->d.sat, one.data(), sizeof(double) * nodes, cudaMemcpyHostToDevice);
+  }
   gwf_condsat(nodes, h->g, h->d.condsat, h->st);
   e = cudaStreamSynchronize(h->st);
   if (e == cudaSuccess) e = cudaGetLastError();
@@ -248,6 +253,7 @@ struct gbsln_handle {
   const int *s_ia = nullptr, *s_ja = nullptr;
   Xt3dDev xt{};             // XT3D on the device (xt.on 0: off)
   int njas = 0;
+  int nja_m = 0;            // the model's connections (FLOW-JA-FACE entries)
   void *xt_mem[16] = {};    // XT3D device arrays, freed by gbsln_destroy
   double *galpha = nullptr; // the last warm step's projection factors (2)
   double *dprev = nullptr;  // the last step's head change (valid when have_prev)
@@ -439,7 +445,7 @@ struct Xt3dHost {
   std::vector<int> sia, sja, idxglo, iallpc, pair_n, pair_il0, pair_il10;
   std::vector<unsigned char> sflag;
   std::vector<double> ck, geo;
-  int lamatsaved = 0, nozee = 0, vcentre = 0;
+  int lamatsaved = 0, nozee = 0, vcentre = 0, rhsform = 0;
 };
 
 int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const gbsln_xt3d_geometry *geom,
@@ -538,16 +544,24 @@ int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const gbsln_xt3d_geome
         gg[7] = 1.0;
       }
     }
+  // XT3D RHS: the model's own pattern (xt3d_ac adds nothing, :139)
+  o.rhsform = xt->rhs ? 1 : 0;
+  if (o.rhsform) {
+    o.sia = c.ia;
+    o.sja = c.ja;
+    o.sflag.assign(c.ja.size(), 1);
+    o.idxglo.resize(c.ja.size());
+    for (size_t q = 0; q < c.ja.size(); ++q) o.idxglo[q] = (int)q;
+  }
   // the solution pattern: each row the connections and the neighbours of
   // the neighbours, diagonal first, the rest ascending; flags 1 (a model
   // connection) and 2 (an extended neighbour, xt3d_ac)
-  o.sia.assign(n + 1, 0);
+  if (!o.rhsform) o.sia.assign(n + 1, 0);
   o.sja.clear();
   o.sflag.clear();
   o.idxglo.assign(c.ja.size(), -1);
   std::vector<int> row;
-  std::vector<unsigned char> fl;
-  for (int p = 0; p < n; ++p) {
+  for (int p = 0; p < n && !o.rhsform; ++p) {
     row.clear();
     for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
       row.push_back(c.ja[q]);
@@ -582,7 +596,7 @@ int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const gbsln_xt3d_geome
       o.sflag.push_back(f);
     }
   }
-  o.sia[n] = (int)o.sja.size();
+  if (!o.rhsform) o.sia[n] = (int)o.sja.size();
   // xt3d_iallpc: every cell the terms of whose connections never change
   o.iallpc.assign(n, 1);
   for (int p = 0; p < n; ++p) {
@@ -609,7 +623,7 @@ int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const gbsln_xt3d_geome
     }
   }
   o.lamatsaved = 0;
-  for (int p = 0; p < n; ++p)
+  for (int p = 0; p < n && !o.rhsform; ++p)
     if (o.iallpc[p] == 1) o.lamatsaved = 1;
   // each connection n < m: n, m's slot in n's row, n's slot in m's row
   o.pair_n.assign(c.njas, 0);
@@ -635,6 +649,7 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
   std::vector<double> vol(n);
   for (int p = 0; p < n; ++p) vol[p] = area[p] * (top[p] - bot[p]);
   h->nja = (int)c.ja.size();
+  h->nja_m = h->nja;
   h->njas = c.njas;
   std::vector<int> ibound(n, 1);
   for (int i = 0; i < m->nchd; ++i) {
@@ -748,6 +763,7 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
     x.lamatsaved = xh.lamatsaved;
     x.nozee = xh.nozee;
     x.vcentre = xh.vcentre;
+    x.rhsform = xh.rhsform;
     x.sia = d_sia;
     x.sja = d_sja;
     x.idxglo = d_idx;
@@ -768,7 +784,12 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
   }
   if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GBIMS_ERR_CUDA; }
   for (double **p : wv) cudaMemset(*p, 0, sizeof(double) * n);
-  cudaMemset(h->d.sat, 0, sizeof(double) * n);
+  {
+    // npf_ar's initial saturation: 1 in every cell; npf_cf updates the
+    // convertible ones (gwf-npf.f90:1853-1884)
+    std::vector<double> one((size_t)n, 1.0);
+    cudaMemcpy(h->d.sat, one.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+  }
   h->hpart.resize((size_t)h->G * 2);
   // IMS handle (imslinear_allocate) on the same connectivity
   int rc = xt ? gbims_create(&h->ims_s, n, h->nja, xh.sia.data(), xh.sja.data(), &h->ims)
@@ -1309,15 +1330,11 @@ extern "C" int gbsln_formulate(gbsln_handle *h, double delt, const double *hold,
 
 extern "C" int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table *out) {
   if (!h || !out) return GBIMS_ERR_ARG;
-  if (h->xt.on) {
-    h->err = "the budget of an XT3D model (xt3d_flowja) is not built";
-    return GBIMS_ERR_UNSUPPORTED;
-  }
   const int n = h->n;
   const bool transient = (h->last_delt > 0.0) && h->has_sto;
   if (!h->bpart) SLN_CUDA(h, cudaMalloc((void **)&h->bpart, sizeof(double) * kGwfBudgetSlots * h->G));
   double *dflow = nullptr;
-  if (flowja) SLN_CUDA(h, cudaMallocAsync((void **)&dflow, sizeof(double) * h->nja, h->st));
+  if (flowja) SLN_CUDA(h, cudaMallocAsync((void **)&dflow, sizeof(double) * h->nja_m, h->st));
   FillDev f{};
   f.transient = transient ? 1 : 0;
   f.tled = transient ? 1.0 / h->last_delt : 0.0;
@@ -1327,6 +1344,7 @@ extern "C" int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table 
   f.bnd_ptr = h->bnd_ptr;
   f.bnd_val = h->bnd_val;
   f.xt = h->xt;
+  if (f.xt.on) xt3d_pairs(h->njas, h->g, f.xt, h->ibound, h->d.sat, h->x, 2, h->st);
   gwf_budget(n, h->g, f, h->bnd_kind, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, dflow,
              h->bpart, h->G, h->st);
   std::vector<double> part((size_t)kGwfBudgetSlots * h->G);
@@ -1334,7 +1352,7 @@ extern "C" int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table 
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(part.data(), h->bpart, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->st);
   if (e == cudaSuccess && flowja)
-    e = cudaMemcpyAsync(flowja, dflow, sizeof(double) * h->nja, cudaMemcpyDeviceToHost, h->st);
+    e = cudaMemcpyAsync(flowja, dflow, sizeof(double) * h->nja_m, cudaMemcpyDeviceToHost, h->st);
   if (dflow) cudaFreeAsync(dflow, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   if (e != cudaSuccess) {

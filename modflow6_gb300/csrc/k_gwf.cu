@@ -204,11 +204,46 @@ __device__ __forceinline__ double conn_cond(const NpfDev &g, const int *ibound, 
 // (n, p), n < p, by n (p is cell 1: its primary terms, xt3d_amat_nbrs over
 // p's neighbours, xt3d_amat_nbrnbrs over n's), then of (p, m), m > p, by m
 // (p is cell 0), which is the order in which the reference adds them.
-__device__ inline void xt_row_fc(const NpfDev &g, const Xt3dDev &x, const int *ibound, int p,
-                                 int s0, int len, double *val) {
+__device__ inline void xt_row_fc(const NpfDev &g, const Xt3dDev &x, const int *ibound,
+                                 const double *h, int p, int s0, int len, double *val,
+                                 double &r) {
   for (int k = 0; k < len; ++k) val[k] = x.lamatsaved ? x.pcval[s0 + k] : 0.0;
   const int r0 = g.ia[p], r1 = g.ia[p + 1], np = r1 - r0 - 1;
   if (ibound[p] == 0) return;
+  if (x.rhsform) {
+    // XT3D RHS: the primary terms in the matrix, the neighbours' terms into
+    // the right-hand side at the current heads (xt3d_rhs, :1522-1546)
+    for (int ii = r0 + 1; ii < r1; ++ii) {
+      const int q = g.ja[ii];
+      if (ibound[q] == 0) continue;
+      const bool lower = q < p;
+      if (!lower && (x.lamatsaved && x.iallpc[p] == 1)) continue;
+      if (lower && (x.lamatsaved && x.iallpc[q] == 1)) continue;
+      const double *cf = x.coef + (size_t)g.jas[ii] * kXtStride;
+      const int qp = x.idxglo[ii] - s0;
+      val[0] = DADD(val[0], -cf[0]);
+      val[qp] = DADD(val[qp], cf[0]);
+      const int n = lower ? q : p, m = lower ? p : q;
+      const double *ci0 = cf + 1, *c1j = cf + 1 + kXtNb;
+      const int n0 = g.ia[n], nn = g.ia[n + 1] - n0 - 1;
+      const int m0 = g.ia[m], nm = g.ia[m + 1] - m0 - 1;
+      // cell 0's neighbours: -term to n, +term to m
+      for (int iil = 0; iil < nn; ++iil) {
+        const int jjj = g.ja[n0 + 1 + iil];
+        if (ibound[jjj] == 0) continue;
+        const double term = DMUL(ci0[iil], DSUB(h[jjj], h[n]));
+        r = lower ? DADD(r, term) : DSUB(r, term);
+      }
+      // cell 1's neighbours: -term to m, +term to n
+      for (int iil = 0; iil < nm; ++iil) {
+        const int jjj = g.ja[m0 + 1 + iil];
+        if (ibound[jjj] == 0) continue;
+        const double term = DMUL(c1j[iil], DSUB(h[jjj], h[m]));
+        r = lower ? DSUB(r, term) : DADD(r, term);
+      }
+    }
+    return;
+  }
   for (int ii = r0 + 1; ii < r1; ++ii) {
     const int n = g.ja[ii];
     if (n > p) break;
@@ -275,7 +310,7 @@ __device__ inline void xt_row_fn(const NpfDev &g, const Xt3dDev &x, const int *i
     if (x.lamatsaved && x.iallpc[n] == 1) continue;
     const int jjs = g.jas[ii];
     const int iups = (h[m] < h[n]) ? n : m;
-    if (g.icelltype[iups] == 0) continue;
+    if (g.icelltype[iups] == 0 && !x.rhsform) continue;
     double topup = g.top[iups], botup = g.bot[iups];
     if (g.ihc[jjs] == 2) {
       topup = fmin(g.top[n], g.top[m]);
@@ -316,7 +351,7 @@ __global__ void k_gwf_fill(int nodes, NpfDev g, FillDev f, const int *__restrict
     double diag;
     double r = rhs[p];
     if constexpr (XT) {
-      xt_row_fc(g, f.xt, ibound, p, i0, xlen, val);
+      xt_row_fc(g, f.xt, ibound, h, p, i0, xlen, val, r);
       diag = val[0];
     } else {
       diag = amat[i0];
@@ -531,9 +566,21 @@ __global__ void __launch_bounds__(256) k_gwf_budget(int nodes, NpfDev g, FillDev
     for (int ii = i0 + 1; ii < i1; ++ii) {
       const int q = g.ja[ii];
       const int n = min(p, q), m = max(p, q);
-      const double cond = conn_cond(g, ibound, h, sat, condsat, n, m, g.jas[ii]);
-      const double qnm = DMUL(cond, DSUB(h[m], h[n]));
-      const double fj = (p == n) ? qnm : -qnm;
+      double fj;
+      if (f.xt.on) {
+        // xt3d_flowja (Xt3dInterface.f90:797-875): the connection's flow,
+        // added to zero with its sign for each end
+        if (ibound[n] == 0 || ibound[m] == 0) {
+          fj = 0.0;
+        } else {
+          const double qx = f.xt.coef[(size_t)g.jas[ii] * kXtStride];
+          fj = (p == n) ? DADD(0.0, qx) : DSUB(0.0, qx);
+        }
+      } else {
+        const double cond = conn_cond(g, ibound, h, sat, condsat, n, m, g.jas[ii]);
+        const double qnm = DMUL(cond, DSUB(h[m], h[n]));
+        fj = (p == n) ? qnm : -qnm;
+      }
       if (flowja) flowja[ii] = fj;
       diag = DADD(diag, fj);
       if (chd) {

@@ -28,6 +28,7 @@ struct Xt3dDev {
   int lamatsaved = 0;    // some cells have all their connections permanently confined
   int nozee = 0;         // no ANGLE2: horizontal connections have no z component
   int vcentre = 0;       // vertical connections run between the cell centres (DISU)
+  int rhsform = 0;       // XT3D RHS: the neighbours' terms go to the right-hand side
   const int *sia = nullptr, *sja = nullptr, *idxglo = nullptr;
   const unsigned char *sflag = nullptr;  // per solution position: 1 connection, 2 extended
   const int *iallpc = nullptr;           // per cell (xt3d_iallpc)
@@ -54,7 +55,8 @@ struct FillDev {
 // XT3D coefficients of every connection n < m (xt3d_fc's loop body,
 // Xt3dInterface.f90:416-465): mode 0 for the fill (the permanently confined
 // cells skipped when lamatsaved), mode 1 for those cells alone with
-// saturated areas (xt3d_fcpc, :499-571)
+// saturated areas (xt3d_fcpc, :499-571), mode 2 the flow of every connection
+// into coef[0] (xt3d_flowja, :797-875)
 void xt3d_pairs(int njas, const NpfDev &g, const Xt3dDev &x, const int *ibound, const double *sat,
                 const double *h, int mode, cudaStream_t st);
 // The permanently confined part of every solution position (amatpc, then

@@ -67,14 +67,19 @@ __global__ void k_xt3d_pairs(int njas, NpfDev g, Xt3dDev x, const int *__restric
     const int ii01 = g.ia[n] + 1 + il0;
     const int m = g.ja[ii01];
     const bool pc = x.lamatsaved && x.iallpc[n] == 1;
-    const bool use = ibound[n] != 0 && ibound[m] != 0 && (mode == 1 ? pc : !pc);
+    const bool use = ibound[n] != 0 && ibound[m] != 0 && (mode == 2 || (mode == 1 ? pc : !pc));
     if (!use) continue;  // never read
     XtCell c0, c1;
     xt_load(g, x, ibound, sat, n, c0);
     xt_load(g, x, ibound, sat, m, c1);
     const int jjs01 = g.jas[ii01];
-    double ar01, ar10;
-    if (mode == 1) {
+    double ar01 = 0.0, ar10 = 0.0;
+    if (mode == 2) {
+      // xt3d_flowja's areas: under Newton the saturated area scaled by the
+      // upstream saturation
+      if (g.inewton != 0) xt_areas(g, sat, h, n, m, jjs01, true, ar01, ar10);
+      xt_areas(g, sat, h, n, m, jjs01, false, ar01, ar10);
+    } else if (mode == 1) {
       xt_areas(g, sat, h, n, m, jjs01, true, ar01, ar10);
     } else if (g.inewton != 0) {
       ar01 = 1.0;
@@ -86,6 +91,18 @@ __global__ void k_xt3d_pairs(int njas, NpfDev g, Xt3dDev x, const int *__restric
     xt_qconds(c0, il0, x.ck + 9 * (size_t)n, c1, il10, x.ck + 9 * (size_t)m, ar01, ar10, 1e-10,
               chat01, chati0, chat1j);
     double qsat = 0.0;
+    if (mode == 2) {
+      double qnm = XMUL(chat01, XSUB(h[m], h[n]));
+      double qn = 0.0;
+      for (int iil = 0; iil < c0.nnbr; ++iil)
+        if (c0.nb[iil] >= 0) qn = XADD(qn, XMUL(chati0[iil], XSUB(h[c0.nb[iil]], h[n])));
+      qnm = XADD(qnm, qn);
+      qn = 0.0;
+      for (int iil = 0; iil < c1.nnbr; ++iil)
+        if (c1.nb[iil] >= 0) qn = XADD(qn, XMUL(chat1j[iil], XSUB(h[c1.nb[iil]], h[m])));
+      x.coef[(size_t)s * kXtStride] = XSUB(qnm, qn);
+      continue;
+    }
     if (mode == 0 && g.inewton != 0) {
       // xt3d_qnbrs (:1548-1575) on both sides, then the saturated and the
       // actual areas

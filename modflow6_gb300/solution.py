@@ -183,7 +183,11 @@ class GwfSolution:
                 keep["xt_" + name] = _f(v)
                 return _lib.dptr(keep["xt_" + name])
 
-            cx = _lib.GbslnXt3d(opt("k22"), opt("angle1"), opt("angle2"), opt("angle3"))
+            rhsform = int(getattr(m, "ixt3d", 0)) == 2
+            if rhsform:
+                self._nja = int(con["nja"])
+            cx = _lib.GbslnXt3d(opt("k22"), opt("angle1"), opt("angle2"), opt("angle3"),
+                                int(rhsform))
         if xt3d and general:
             # the connection geometry: cell centres and face-normal angles
             disu = bool(getattr(m, "disu", False))
@@ -253,9 +257,12 @@ class GwfSolution:
         lib = _lib.load()
         t = _lib.GbslnBudgetTable()
         m = self.m
-        njas = (m.nlay * (m.nrow * (m.ncol - 1) + m.ncol * (m.nrow - 1))
-                + (m.nlay - 1) * m.nrow * m.ncol)
-        fj = np.zeros(m.nodes + 2 * njas) if flowja else None
+        if getattr(m, "disv", False) or getattr(m, "disu", False):
+            nja = int(m.connections()["nja"])
+        else:
+            nja = m.nodes + 2 * (m.nlay * (m.nrow * (m.ncol - 1) + m.ncol * (m.nrow - 1))
+                                 + (m.nlay - 1) * m.nrow * m.ncol)
+        fj = np.zeros(nja) if flowja else None
         rc = lib.gbsln_budget(self._h, _lib.dptr(fj) if fj is not None else None, C.byref(t))
         if rc < 0:
             raise _lib.GbimsError(rc, lib.gbsln_last_error(self._h).decode())

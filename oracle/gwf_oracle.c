@@ -907,8 +907,9 @@ void or_gwf_budget(const or_gwf_model *m, const int *ibound, const double *conds
                    const double *hnew, double *flowja, double *terms) {
   for (int k = 0; k < 10; ++k) terms[k] = 0.0;
   for (int k = 0; k < m->nja; ++k) flowja[k] = 0.0;
-  /* npf_cq */
-  for (int n = 0; n < m->nodes; ++n) {
+  /* npf_cq (with XT3D: xt3d_flowja, gwf-npf.f90:756-757) */
+  if (m->ixt3d) or_xt3d_flowja(m, ibound, sat, hnew, flowja);
+  for (int n = 0; n < m->nodes && !m->ixt3d; ++n) {
     for (int ii = m->ia[n] + 1; ii < m->ia[n + 1]; ++ii) {
       int mm = m->ja[ii];
       if (mm < n) continue;
@@ -1022,7 +1023,7 @@ static void gwf_fc_flag(const or_gwf_model *m, const int *ibound, const double *
   if (m->ixt3d) {
     /* npf_fc with XT3D (gwf-npf.f90:492-493) */
     qsat = (double *)calloc(m->nja, sizeof(double));
-    or_xt3d_fc(m, ibound, sat, hnew, amat, qsat);
+    or_xt3d_fc(m, ibound, sat, hnew, amat, rhs, qsat);
   } else {
     or_npf_fc(m, ibound, condsat, sat, hnew, amat, rhs);
   }
@@ -1205,6 +1206,9 @@ int or_gwf_timestep(const or_gwf_model *m, or_ims *ims, or_nonlinear *nl,
   double *sat = (double *)calloc(neq, sizeof(double));
   double *xtemp = (double *)calloc(neq, sizeof(double));
   double *work = (double *)calloc(neq, sizeof(double));
+  /* npf_ar's initial saturation (gwf-npf.f90:1853-1884): 1 in every cell;
+   * npf_cf updates the convertible ones */
+  for (int n = 0; n < neq; ++n) sat[n] = 1.0;
   /* gwf_ad: xold = x ; chd_ad: x = xold = chd head */
   for (int n = 0; n < neq; ++n) xold[n] = x[n];
   for (int i = 0; i < m->nchd; ++i) {

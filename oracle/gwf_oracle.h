@@ -38,7 +38,7 @@ typedef struct {
   int nchd;
   const int *chd_node;
   const double *chd_head;
-  /* XT3D (NPF option XT3D, matrix form), DIS grids only; 0 off.  ck: the
+  /* XT3D (NPF option XT3D): 0 off, 1 the matrix form, 2 XT3D RHS.  ck: the
    * conductivity tensor per cell (9, row-major, or_xt3d_ck); nozee when
    * ANGLE2 is not given.  With XT3D amat is indexed by the solution pattern
    * sia/sja (nja_sln entries: the connections and the neighbours of
@@ -105,7 +105,9 @@ void or_xt3d_ck(int nodes, const double *k11, const double *k22, const double *k
 int or_xt3d_pattern(int nodes, const int *ia, const int *ja, int cap, int *sia, int *sja,
                     int *idxglo);
 int or_xt3d_fc(const or_gwf_model *m, const int *ibound, const double *sat,
-               const double *hnew, double *amat, double *qsat);
+               const double *hnew, double *amat, double *rhs, double *qsat);
+void or_xt3d_flowja(const or_gwf_model *m, const int *ibound, const double *sat,
+                    const double *hnew, double *flowja);
 void or_xt3d_fn(const or_gwf_model *m, const int *ibound, const double *hnew,
                 const double *qsat, double *amat, double *rhs);
 double or_squadratic_sat(double top, double bot, double x, double eps);

@@ -130,7 +130,8 @@ def load():
                                        _ip, _ip, _dp, _dp, _dp]
         lib.or_xt3d_ck.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp]
         lib.or_xt3d_pattern.argtypes = [C.c_int, _ip, _ip, C.c_int, _ip, _ip, _ip]
-        lib.or_xt3d_fc.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, _dp, _dp]
+        lib.or_xt3d_fc.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, _dp, _dp, _dp]
+        lib.or_xt3d_flowja.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, _dp]
         lib.or_xt3d_fn.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, _dp, _dp]
         lib.or_disu_connect.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _ip, C.c_int, _ip,
                                         _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
@@ -471,16 +472,24 @@ class Gwf:
             ck = np.zeros(9 * n)
             self.lib.or_xt3d_ck(n, d(m.k11), d(k22), d(m.k33), d(rad(m.angle1)), d(rad(m.angle2)),
                                 d(rad(m.angle3)), int(nozee), dp(ck))
-            cap = int(np.diff(con["ia"])[con["ja"]].sum()) + n
-            sia = np.zeros(n + 1, np.int32)
-            sja = np.zeros(cap, np.int32)
-            idxglo = np.zeros(con["nja"], np.int32)
-            nja_sln = self.lib.or_xt3d_pattern(n, i(con["ia"]), i(con["ja"]), cap, ip(sia), ip(sja),
-                                               ip(idxglo))
-            if nja_sln < 0:
-                raise RuntimeError("or_xt3d_pattern: capacity exceeded")
-            sja = sja[:nja_sln].copy()
-            self.model.ixt3d, self.model.nozee, self.model.nja_sln = 1, int(nozee), nja_sln
+            ixt3d = int(m.ixt3d)
+            if ixt3d == 2:
+                # XT3D RHS: the model's own pattern
+                sia = np.ascontiguousarray(con["ia"], np.int32)
+                sja = np.ascontiguousarray(con["ja"], np.int32)
+                idxglo = np.arange(con["nja"], dtype=np.int32)
+                nja_sln = int(con["nja"])
+            else:
+                cap = int(np.diff(con["ia"])[con["ja"]].sum()) + n
+                sia = np.zeros(n + 1, np.int32)
+                sja = np.zeros(cap, np.int32)
+                idxglo = np.zeros(con["nja"], np.int32)
+                nja_sln = self.lib.or_xt3d_pattern(n, i(con["ia"]), i(con["ja"]), cap, ip(sia),
+                                                   ip(sja), ip(idxglo))
+                if nja_sln < 0:
+                    raise RuntimeError("or_xt3d_pattern: capacity exceeded")
+                sja = sja[:nja_sln].copy()
+            self.model.ixt3d, self.model.nozee, self.model.nja_sln = ixt3d, int(nozee), nja_sln
             self.model.ck, self.model.sia, self.model.sja, self.model.idxglo = d(ck), i(sia), i(sja), i(idxglo)
             if getattr(m, "disv", False) or getattr(m, "disu", False):
                 # DISV: the shared edges' normal angles (cprops); DISU: ANGLDEGX
@@ -514,7 +523,7 @@ class Gwf:
         n, nja = self.m.nodes, self.con["nja"]
         amat = np.zeros(nja)
         rhs = np.zeros(n)
-        sat = np.zeros(n)
+        sat = np.ones(n)  # npf_ar's initial saturation; npf_cf updates convertible cells
         hnew = np.ascontiguousarray(hnew, np.float64)
         hold = np.ascontiguousarray(hnew if hold is None else hold, np.float64)
         self.lib.or_gwf_fc(C.byref(self.model), ip(self.ibound), dp(self.condsat), dp(sat), delt,
@@ -529,7 +538,7 @@ class Gwf:
 
     def sat(self, hnew):
         """npf_cf: cell saturation at the given heads."""
-        s = np.zeros(self.m.nodes)
+        s = np.ones(self.m.nodes)
         h = np.ascontiguousarray(hnew, np.float64)
         self.lib.or_npf_cf(C.byref(self.model), ip(self.ibound), dp(h), dp(s))
         return s
@@ -539,12 +548,10 @@ class Gwf:
         (entries STO-SS, STO-SY, CHD, WEL, RCH; totals and percent difference
         summed in entry order, Budget.f90:250-266).  sat defaults to npf_cf at
         hnew."""
-        if self.model.ixt3d:
-            raise NotImplementedError("the oracle budget does not restate xt3d_flowja")
         hnew = np.ascontiguousarray(hnew, np.float64)
         hold = np.ascontiguousarray(hnew if hold is None else hold, np.float64)
         sat = self.sat(hnew) if sat is None else np.ascontiguousarray(sat, np.float64)
-        flowja = np.zeros(self.con["nja"])
+        flowja = np.zeros(self.mcon["nja"])
         terms = np.zeros(10)
         self.lib.or_gwf_budget(C.byref(self.model), ip(self.ibound), dp(self.condsat), dp(sat), delt,
                                int(transient), dp(hold), dp(hnew), dp(flowja), dp(terms))
@@ -556,7 +563,7 @@ class Gwf:
         avg = (tin + tout) / 2.0
         pd = 100.0 * (tin - tout) / avg if avg != 0.0 else 0.0
         act = self.ibound > 0
-        diag = flowja[self.con["ia"][:-1]]
+        diag = flowja[self.mcon["ia"][:-1]]
         imb = np.abs(np.where(act, diag, 0.0))
         return flowja, dict(rate_in=rin, rate_out=rout, total_in=tin, total_out=tout,
                             percent_discrepancy=pd, max_cell_imbalance=float(imb.max()),

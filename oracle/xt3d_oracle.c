@@ -617,6 +617,7 @@ static int xt3d_setup(xt3d_t *x, const or_gwf_model *m, const int *ibound, const
   x->lamatsaved = 0;
   for (int n = 0; n < nodes; ++n)
     if (x->iallpc[n] == 1) x->lamatsaved = 1;
+  if (m->ixt3d == 2) x->lamatsaved = 0; /* the RHS form saves nothing */
   return 0;
 }
 
@@ -694,7 +695,7 @@ static void pair_coefs(const xt3d_t *x, int n, int il0, int mode, const double *
  * allocation.  amat is in the solution pattern; qsat (model nja) gets the
  * saturated flows under Newton. */
 int or_xt3d_fc(const or_gwf_model *m, const int *ibound, const double *sat,
-               const double *hnew, double *amat, double *qsat) {
+               const double *hnew, double *amat, double *rhs, double *qsat) {
   xt3d_t x;
   double *one = (double *)malloc(sizeof(double) * m->nodes);
   for (int n = 0; n < m->nodes; ++n) one[n] = 1.0;
@@ -784,6 +785,23 @@ int or_xt3d_fc(const or_gwf_model *m, const int *ibound, const double *sat,
       amat[G[ii01]] = amat[G[ii01]] + chat01;
       amat[G[ii11]] = amat[G[ii11]] + (-chat01);
       amat[G[ii10]] = amat[G[ii10]] + chat01;
+      if (m->ixt3d == 2) {
+        /* the RHS form: xt3d_rhs (:1522-1546) for both cells */
+        for (int side = 0; side < 2; ++side) {
+          int a = side ? mm : n, b = side ? n : mm;
+          int nnb = side ? nnbr1 : nnbr0;
+          const int *inb = side ? inbr1 : inbr0;
+          const double *ch = side ? chat1j : chati0;
+          for (int iil = 0; iil < nnb; ++iil) {
+            if (inb[iil] < 0) continue;
+            int jjj = m->ja[m->ia[a] + 1 + iil];
+            double term = ch[iil] * (hnew[jjj] - hnew[a]);
+            rhs[a] = rhs[a] - term;
+            rhs[b] = rhs[b] + term;
+          }
+        }
+        continue;
+      }
       /* xt3d_amat_nbrs and xt3d_amat_nbrnbrs (:1382-1435), active slots */
       for (int side = 0; side < 4; ++side) {
         int a = (side < 2) ? n : mm, b = (side < 2) ? mm : n;
@@ -836,7 +854,7 @@ void or_xt3d_fn(const or_gwf_model *m, const int *ibound, const double *hnew,
       int ii11 = m->ia[mm];
       int ii10 = pos_in(m->ia, m->ja, mm, n);
       int iups = (hnew[mm] < hnew[n]) ? n : mm;
-      if (m->icelltype[iups] == 0) continue;
+      if (m->icelltype[iups] == 0 && m->ixt3d == 1) continue;
       double topup = m->top[iups], botup = m->bot[iups];
       if (m->ihc[jjs01] == 2) {
         topup = (m->top[n] < m->top[mm]) ? m->top[n] : m->top[mm];
@@ -855,6 +873,60 @@ void or_xt3d_fn(const or_gwf_model *m, const int *ibound, const double *hnew,
         amat[G[ii11]] = amat[G[ii11]] + (-term);
         rhs[mm] = rhs[mm] - term * hnew[mm];
       }
+    }
+  }
+  xt3d_free(&x);
+}
+
+/* xt3d_flowja (Xt3dInterface.f90:797-875): the flow through every
+ * connection of two active cells, from the coefficients with the current
+ * saturation (and, under Newton, the saturated area scaled by the upstream
+ * saturation); flowja must hold zeros on the connections. */
+void or_xt3d_flowja(const or_gwf_model *m, const int *ibound, const double *sat,
+                    const double *hnew, double *flowja) {
+  xt3d_t x;
+  if (xt3d_setup(&x, m, ibound, sat) != 0) return;
+  double chat01, chati0[NBRMX], chat1j[NBRMX];
+  int inbr0[NBRMX], inbr1[NBRMX];
+  for (int n = 0; n < m->nodes; ++n) {
+    if (ibound[n] == 0) continue;
+    int nnbr0 = m->ia[n + 1] - m->ia[n] - 1;
+    double vc0[NBRMX][3], vn0[NBRMX][3], dl0[NBRMX], dl0n[NBRMX];
+    int allhc0;
+    xt3d_load(&x, n, nnbr0, inbr0, vc0, vn0, dl0, dl0n, &allhc0);
+    for (int il0 = 0; il0 < nnbr0; ++il0) {
+      int mm = inbr0[il0];
+      if (mm < 0 || mm < n) continue;
+      int nnbr1 = m->ia[mm + 1] - m->ia[mm] - 1;
+      double vc1[NBRMX][3], vn1[NBRMX][3], dl1[NBRMX], dl1n[NBRMX];
+      int allhc1;
+      xt3d_load(&x, mm, nnbr1, inbr1, vc1, vn1, dl1, dl1n, &allhc1);
+      int ii01 = m->ia[n] + 1 + il0;
+      int jjs01 = m->jas[ii01];
+      int il10 = pos_in(m->ia, m->ja, mm, n) - m->ia[mm] - 1;
+      double ar01 = 0.0, ar10 = 0.0;
+      if (m->inewton != 0) xt3d_areas(&x, n, mm, jjs01, 1, &ar01, &ar10, hnew);
+      xt3d_areas(&x, n, mm, jjs01, 0, &ar01, &ar10, hnew);
+      qconds(x.nbrmax, nnbr0, inbr0, il0, vc0, vn0, dl0, dl0n, m->ck + 9 * (size_t)n, nnbr1,
+             inbr1, il10, vc1, vn1, dl1, dl1n, m->ck + 9 * (size_t)mm, ar01, ar10, 1e-10, allhc0,
+             allhc1, &chat01, chati0, chat1j);
+      double qnm = chat01 * (hnew[mm] - hnew[n]);
+      double qnbrs = 0.0;
+      for (int iil = 0; iil < nnbr0; ++iil)
+        if (inbr0[iil] >= 0) {
+          int jjj = m->ja[m->ia[n] + 1 + iil];
+          qnbrs = qnbrs + chati0[iil] * (hnew[jjj] - hnew[n]);
+        }
+      qnm = qnm + qnbrs;
+      qnbrs = 0.0;
+      for (int iil = 0; iil < nnbr1; ++iil)
+        if (inbr1[iil] >= 0) {
+          int jjj = m->ja[m->ia[mm] + 1 + iil];
+          qnbrs = qnbrs + chat1j[iil] * (hnew[jjj] - hnew[mm]);
+        }
+      qnm = qnm - qnbrs;
+      flowja[ii01] = flowja[ii01] + qnm;
+      flowja[m->isym[ii01]] = flowja[m->isym[ii01]] - qnm;
     }
   }
   xt3d_free(&x);

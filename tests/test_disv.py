@@ -80,7 +80,7 @@ def test_gpu_fill_on_disv_bitexact(gblib, newton):
     rng = np.random.default_rng(6)
     h = np.ascontiguousarray(m.strt + rng.uniform(-15.0, 3.0, m.nodes))
     ib = np.ascontiguousarray(m.ibound, np.int32)
-    sat = np.zeros(m.nodes)
+    sat = np.ones(m.nodes)  # npf_ar initial saturation
     ao, ro = np.zeros(con["nja"]), np.zeros(m.nodes)
     lib.or_npf_cf(C.byref(g.model), oracle.ip(ib), oracle.dp(h), oracle.dp(sat))
     lib.or_npf_fc(C.byref(g.model), oracle.ip(ib), oracle.dp(g.condsat), oracle.dp(sat),

@@ -280,7 +280,7 @@ def test_gbnpf_fill_newton_bitexact(gblib):
     rng = np.random.default_rng(4)
     h = np.ascontiguousarray(m.strt + rng.uniform(-8.0, 3.0, m.nodes))
     ib = np.ascontiguousarray(m.ibound, np.int32)
-    sat = np.zeros(m.nodes)
+    sat = np.ones(m.nodes)  # npf_ar initial saturation
     ao, ro = np.zeros(con["nja"]), np.zeros(m.nodes)
     lib.or_npf_cf(C.byref(g.model), oracle.ip(ib), oracle.dp(h), oracle.dp(sat))
     lib.or_npf_fc(C.byref(g.model), oracle.ip(ib), oracle.dp(g.condsat), oracle.dp(sat), oracle.dp(h),

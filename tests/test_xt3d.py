@@ -341,3 +341,104 @@ def test_gpu_general_grid_xt3d_timestep(gblib, name, make):
     sg = sol.timestep(1, 1, 1.0)
     assert sg["converged"] == 1
     assert np.abs(sol.heads - h).max() < 1e-9
+
+
+# ---- XT3D RHS and the flows -------------------------------------------------
+
+def test_oracle_xt3d_flows_are_darcy_fluxes():
+    """xt3d_flowja at the analytical heads of the 2-D case: the flow through
+    every face between two cells of the same row is the Darcy flux of the
+    uniform flow, (K grad h)_x times the face area, and through the faces
+    between rows (where K grad h has no y component) it is zero."""
+    m, h = aniso_model(*CASES[0])
+    g = oracle.Gwf(m, oracle.settings())
+    fj, _ = g.budget(h)
+    K = ktensor(5.0, 1.0, 0.5, *CASES[0][3])
+    b = -0.03 * K[1, 0] / K[1, 1]
+    qx = K[0, 0] * 0.03 + K[0, 1] * b
+    con = g.mcon
+    rown = np.repeat(np.arange(m.nodes), np.diff(con["ia"]))
+    ncol = m.ncol
+    east = con["ja"] == rown + 1
+    south = con["ja"] == rown + ncol
+    area = m.delc[(rown % (m.nrow * ncol)) // ncol] * 10.0
+    np.testing.assert_allclose(fj[east], qx * area[east], rtol=1e-10)
+    assert np.abs(fj[south]).max() <= 1e-10 * abs(qx) * area.max()
+
+
+@pytest.mark.parametrize("case", CASES, ids=["2d", "3d"])
+def test_oracle_rhs_form_reaches_the_same_heads(case):
+    """XT3D RHS (the neighbours' terms lagged on the right-hand side)
+    converges over the outer iterations to the matrix form's heads."""
+    tol = dict(dvclose=1e-12, rclose=1e-10, iter1=4000, ilinmeth=2)
+    m, h = aniso_model(*case)
+    m.ixt3d = 2
+    g = oracle.Gwf(m, oracle.settings(**tol))
+    assert g.con["nja"] == g.mcon["nja"]
+    st = g.timestep(kper=1, kstp=1, delt=1.0, dvclose=1e-10, mxiter=400)
+    assert st["converged"] == 1 and st["outer"] > 2
+    assert np.abs(g.x - h).max() < 1e-8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("icelltype,newton,transient", [(0, 0, 0), (1, 1, 1)],
+                         ids=["confined", "newton"])
+def test_gpu_xt3d_rhs_fill_bitexact(gblib, icelltype, newton, transient):
+    m, h = aniso_model(*CASES[1], icelltype=icelltype)
+    m.ixt3d = 2
+    m.inewton = newton
+    if transient:
+        m.ss, m.sy = np.full(m.nodes, 1e-5), np.full(m.nodes, 0.15)
+    g, sol = _gpu_pair(m)
+    rng = np.random.default_rng(5)
+    hh = h + rng.uniform(-14.0, 2.0, m.nodes)
+    hold = h + rng.uniform(-1.0, 1.0, m.nodes)
+    sol.heads = hh
+    delt = 2.5 if transient else 0.0
+    amat, rhs = sol.formulate(delt=delt, hold=hold if transient else None)
+    ao, ro = g.assemble(hh, hold=hold, delt=delt, transient=bool(transient))
+    assert amat.size == ao.size == g.mcon["nja"]
+    np.testing.assert_array_equal(amat, ao)
+    np.testing.assert_array_equal(rhs, ro)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("grid", ["dis-3d", "disv", "disu-newton"])
+def test_gpu_xt3d_budget_flows_bitexact(gblib, grid):
+    """FLOW-JA-FACE of an XT3D model (xt3d_flowja) on the device against the
+    oracle's, bit for bit, and the model budget to rounding."""
+    if grid == "dis-3d":
+        m, h = aniso_model(*CASES[1], icelltype=1)
+        m.ss, m.sy = np.full(m.nodes, 1e-5), np.full(m.nodes, 0.15)
+    elif grid == "disv":
+        m, h = _general_linear(_disv(), icelltype=1)
+    else:
+        m, h = _general_linear(_disu(), icelltype=1)
+        m.inewton = 1
+    g, sol = _gpu_pair(m)
+    rng = np.random.default_rng(6)
+    hh = np.maximum(h, m.cell_bot + 1.0) + rng.uniform(-6.0, 1.0, m.nodes)
+    hold = h.copy()
+    transient = m.ss is not None
+    delt = 2.0 if transient else 0.0
+    sol.heads = hh
+    sol.formulate(delt=delt, hold=hold if transient else None)
+    fj, bg = sol.budget(flowja=True)
+    fo, bo = g.budget(hh, hold=hold, delt=delt, transient=transient)
+    np.testing.assert_array_equal(fj, fo)
+    scale = max(1.0, float(np.abs(bo["rate_in"]).max()))
+    np.testing.assert_allclose(bg["rate_in"], bo["rate_in"], rtol=1e-12, atol=1e-12 * scale)
+    np.testing.assert_allclose(bg["rate_out"], bo["rate_out"], rtol=1e-12, atol=1e-12 * scale)
+
+
+@pytest.mark.gpu
+def test_gpu_xt3d_rhs_timestep(gblib):
+    from modflow6_gb300.ims import ImsLinearSettings
+    from modflow6_gb300.solution import GwfSolution, Nonlinear
+    tol = dict(dvclose=1e-12, rclose=1e-10, iter1=4000, ilinmeth=2)
+    m, h = aniso_model(*CASES[1])
+    m.ixt3d = 2
+    sol = GwfSolution(m, ImsLinearSettings(**tol), Nonlinear(dvclose=1e-10, mxiter=400))
+    sg = sol.timestep(1, 1, 1.0)
+    assert sg["converged"] == 1
+    assert np.abs(sol.heads - h).max() < 1e-8
