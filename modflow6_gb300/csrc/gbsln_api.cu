@@ -556,10 +556,12 @@ int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const gbsln_xt3d_geome
   // the solution pattern: each row the connections and the neighbours of
   // the neighbours, diagonal first, the rest ascending; flags 1 (a model
   // connection) and 2 (an extended neighbour, xt3d_ac)
-  if (!o.rhsform) o.sia.assign(n + 1, 0);
-  o.sja.clear();
-  o.sflag.clear();
-  o.idxglo.assign(c.ja.size(), -1);
+  if (!o.rhsform) {
+    o.sia.assign(n + 1, 0);
+    o.sja.clear();
+    o.sflag.clear();
+    o.idxglo.assign(c.ja.size(), -1);
+  }
   std::vector<int> row;
   for (int p = 0; p < n && !o.rhsform; ++p) {
     row.clear();
