@@ -383,27 +383,33 @@ int gbsln_create(const gbsln_model *model, const gbnpf_options *npf,
                  const gbims_settings *ims, const gbsln_nonlinear *nl,
                  const double *strt, gbsln_handle **out);
 
-/* XT3D, the NPF formulation with the full hydraulic conductivity tensor on
- * the neighbours-of-neighbours stencil (NPF option XT3D without RHS;
- * Xt3dInterface.f90, Xt3dAlgorithm.f90), for a DIS model.  k22: K22 per
- * cell, or NULL for K22 = K11; angle1..3: ANGLE1..3 per cell in degrees, or
- * NULL (ANGLE1 then 0; ANGLE2 and ANGLE3 both or neither; without them the
- * horizontal connections have no z component, as in the reference).  The
- * matrix then has the wider pattern (each row: the cell, its neighbours and
- * their neighbours) and the solve takes the level-scheduled path. */
-typedef struct gbsln_xt3d {
+/* The hydraulic conductivity tensor of NPF (K22, ANGLE1..3) and its
+ * formulation.  k22: K22 per cell, or NULL (K22 = K11); angle1..3: ANGLE1..3
+ * per cell in degrees, or NULL (ANGLE2 needs ANGLE1; ANGLE2 and ANGLE3 both
+ * or neither).  xt3d 0: the standard two-point conductances with the
+ * effective K of each connection's direction (hy_eff, gwf-npf.f90:2280-2357;
+ * hyeff, HGeoUtil.f90:29-108; iavgkeff 0 harmonic, 1 arithmetic
+ * weighting); 1: XT3D, the full tensor on the neighbours-of-neighbours
+ * stencil (Xt3dInterface.f90, Xt3dAlgorithm.f90; without ANGLE2 the
+ * horizontal connections have no z component, as in the reference), whose
+ * matrix has the wider pattern (each row: the cell, its neighbours and
+ * theirs) and is solved on the level-scheduled path; 2: XT3D RHS, the
+ * neighbours' terms on the right-hand side at the current heads and the
+ * model's own pattern (:478-490). */
+typedef struct gbsln_ktensor {
   const double *k22;
   const double *angle1, *angle2, *angle3;
-  int rhs;  /* 1: XT3D RHS, the neighbours' terms on the right-hand side at
-               the current heads and the model's own pattern (:478-490) */
-} gbsln_xt3d;
+  int xt3d;
+  int iavgkeff;
+} gbsln_ktensor;
 
-/* gbsln_create with XT3D.  ALTERNATIVE_CELL_AVERAGING (icellavg > 0) is
- * refused as the reference refuses it (GBIMS_ERR_ARG); gbsln_budget takes
- * the flows from xt3d_flowja (Xt3dInterface.f90:797-875). */
-int gbsln_create_xt3d(const gbsln_model *model, const gbsln_xt3d *xt3d,
-                      const gbnpf_options *npf, const gbims_settings *ims,
-                      const gbsln_nonlinear *nl, const double *strt, gbsln_handle **out);
+/* gbsln_create with the conductivity tensor on a DIS model.  With XT3D,
+ * ALTERNATIVE_CELL_AVERAGING (icellavg > 0) is refused as the reference
+ * refuses it (GBIMS_ERR_ARG), and gbsln_budget takes the flows from
+ * xt3d_flowja (Xt3dInterface.f90:797-875). */
+int gbsln_create_tensor(const gbsln_model *model, const gbsln_ktensor *kt,
+                        const gbnpf_options *npf, const gbims_settings *ims,
+                        const gbsln_nonlinear *nl, const double *strt, gbsln_handle **out);
 
 /* A grid given by its connectivity: a DISV or DISU grid (or DIS written out
  * this way), in the form Connections.f90 keeps it (con_finalize, :160-316),
@@ -433,7 +439,7 @@ int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *model,
                       const gbnpf_options *npf, const gbims_settings *ims,
                       const gbsln_nonlinear *nl, const double *strt, gbsln_handle **out);
 
-/* The connection geometry XT3D needs on a grid given by its connectivity
+/* The connection geometry the tensor needs on a grid given by its connectivity
  * (connection_normal and connection_vector of Disv.f90:979-1080 and
  * Disu.f90:1062-1164): xc, yc the cell centres (nodes; CELL2D); anglex per
  * connection n < m in JAS order, the angle in radians between the x axis
@@ -441,17 +447,19 @@ int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *model,
  * shared edge, DisvGeom.f90:394-412; DISU: ANGLDEGX); centre_vertical 1
  * when vertical connections also run between the cell centres (DISU), 0 when
  * they are vertical lines (DISV). */
-typedef struct gbsln_xt3d_geometry {
+typedef struct gbsln_geometry {
   const double *xc, *yc;
   const double *anglex;
   int centre_vertical;
-} gbsln_xt3d_geometry;
+} gbsln_geometry;
 
-/* gbsln_create_grid with XT3D (gbsln_xt3d) on a DISV or DISU grid. */
-int gbsln_create_grid_xt3d(const gbsln_grid *grid, const gbsln_model *model,
-                           const gbsln_xt3d *xt3d, const gbsln_xt3d_geometry *geometry,
-                           const gbnpf_options *npf, const gbims_settings *ims,
-                           const gbsln_nonlinear *nl, const double *strt, gbsln_handle **out);
+/* gbsln_create_grid with the conductivity tensor (gbsln_ktensor) on a DISV
+ * or DISU grid. */
+int gbsln_create_grid_tensor(const gbsln_grid *grid, const gbsln_model *model,
+                             const gbsln_ktensor *kt, const gbsln_geometry *geometry,
+                             const gbnpf_options *npf, const gbims_settings *ims,
+                             const gbsln_nonlinear *nl, const double *strt,
+                             gbsln_handle **out);
 /* One time step (prepareSolve + outer loop).  The step is transient when the
  * model has ss/sy and delt > 0, steady state otherwise; delt is also the
  * step length used by the pseudo-transient continuation default

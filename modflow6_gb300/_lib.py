@@ -80,11 +80,12 @@ class GbslnGrid(C.Structure):
     ]
 
 
-class GbslnXt3d(C.Structure):
-    _fields_ = [("k22", _dp), ("angle1", _dp), ("angle2", _dp), ("angle3", _dp), ("rhs", C.c_int)]
+class GbslnKTensor(C.Structure):
+    _fields_ = [("k22", _dp), ("angle1", _dp), ("angle2", _dp), ("angle3", _dp), ("xt3d", C.c_int),
+                ("iavgkeff", C.c_int)]
 
 
-class GbslnXt3dGeometry(C.Structure):
+class GbslnGeometry(C.Structure):
     _fields_ = [("xc", _dp), ("yc", _dp), ("anglex", _dp), ("centre_vertical", C.c_int)]
 
 
@@ -165,11 +166,11 @@ _SIGS = {
     "gbnpf_destroy": (C.c_int, [C.c_void_p]),
     "gbsln_create": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbnpfOptions), C.POINTER(GbimsSettings),
                                C.POINTER(GbslnNonlinear), _dp, C.POINTER(C.c_void_p)]),
-    "gbsln_create_xt3d": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbslnXt3d), C.POINTER(GbnpfOptions),
+    "gbsln_create_tensor": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbslnKTensor), C.POINTER(GbnpfOptions),
                                     C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,
                                     C.POINTER(C.c_void_p)]),
-    "gbsln_create_grid_xt3d": (C.c_int, [C.POINTER(GbslnGrid), C.POINTER(GbslnModel), C.POINTER(GbslnXt3d),
-                                         C.POINTER(GbslnXt3dGeometry), C.POINTER(GbnpfOptions),
+    "gbsln_create_grid_tensor": (C.c_int, [C.POINTER(GbslnGrid), C.POINTER(GbslnModel), C.POINTER(GbslnKTensor),
+                                         C.POINTER(GbslnGeometry), C.POINTER(GbnpfOptions),
                                          C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,
                                          C.POINTER(C.c_void_p)]),
     "gbsln_create_grid": (C.c_int, [C.POINTER(GbslnGrid), C.POINTER(GbslnModel), C.POINTER(GbnpfOptions),

@@ -448,7 +448,7 @@ struct Xt3dHost {
   int lamatsaved = 0, nozee = 0, vcentre = 0, rhsform = 0;
 };
 
-int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const gbsln_xt3d_geometry *geom,
+int xt3d_host(const gbsln_model *m, const gbsln_ktensor *xt, const gbsln_geometry *geom,
               const Conn &c, const std::vector<int> &ibound, Xt3dHost &o, std::string &err) {
   const int n = (int)c.ia.size() - 1;
   if ((xt->angle2 == nullptr) != (xt->angle3 == nullptr)) {
@@ -545,7 +545,7 @@ int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const gbsln_xt3d_geome
       }
     }
   // XT3D RHS: the model's own pattern (xt3d_ac adds nothing, :139)
-  o.rhsform = xt->rhs ? 1 : 0;
+  o.rhsform = (xt->xt3d == 2) ? 1 : 0;
   if (o.rhsform) {
     o.sia = c.ia;
     o.sja = c.ja;
@@ -643,10 +643,103 @@ int xt3d_host(const gbsln_model *m, const gbsln_xt3d *xt, const gbsln_xt3d_geome
   return GBIMS_OK;
 }
 
+// hy_eff (gwf-npf.f90:2280-2357) with hyeff (HGeoUtil.f90:29-108) for every
+// connection n < m, from n toward m and from m toward n.  The connection
+// normal is DIS's (from the cells' rows and columns, Dis.f90:1039-1087) or,
+// with a geometry, cos/sin of anglex flipped for the reverse direction
+// (Disv.f90:979-1018, Disu.f90:1062-1102).
+std::vector<double> npf_hy_host(const gbsln_model *m, const gbsln_ktensor *kt,
+                                const gbsln_geometry *geom, const Conn &c, int nrow, int ncol) {
+  const int n = (int)c.ia.size() - 1;
+  const double dpio180 = std::atan(1.0) / 45.0;
+  auto rad = [&](const double *a, int p) { return a ? a[p] * dpio180 : 0.0; };
+  auto normal = [&](int a, int b, int ihc, int sidx, double v[3]) {
+    v[0] = 0.0;
+    v[1] = 0.0;
+    v[2] = 0.0;
+    if (ihc == 0) {
+      v[2] = (b < a) ? 1.0 : -1.0;
+    } else if (geom) {
+      const double angle = geom->anglex[sidx];
+      const double dmult = (b < a) ? -1.0 : 1.0;
+      v[0] = std::cos(angle) * dmult;
+      v[1] = std::sin(angle) * dmult;
+    } else {
+      const int nrc = nrow * ncol;
+      const int ra = a % nrc, rb = b % nrc;
+      const int i1 = ra / ncol, j1 = ra % ncol, i2 = rb / ncol, j2 = rb % ncol;
+      if (i2 < i1) v[1] = 1.0;
+      else if (j2 < j1) v[0] = -1.0;
+      else if (j2 > j1) v[0] = 1.0;
+      else v[1] = -1.0;
+    }
+  };
+  auto hyeff = [&](double k11, double k22, double k33, double ang1, double ang2, double ang3,
+                   const double *vg) {
+    const double s1 = std::sin(ang1), c1 = std::cos(ang1), s2 = std::sin(ang2),
+                 c2 = std::cos(ang2), s3 = std::sin(ang3), c3 = std::cos(ang3);
+    double r[3][3];
+    r[0][0] = c1 * c2;
+    r[0][1] = c1 * s2 * s3 - s1 * c3;
+    r[0][2] = -c1 * s2 * c3 - s1 * s3;
+    r[1][0] = s1 * c2;
+    r[1][1] = s1 * s2 * s3 + c1 * c3;
+    r[1][2] = -s1 * s2 * c3 + c1 * s3;
+    r[2][0] = s2;
+    r[2][1] = -c2 * s3;
+    r[2][2] = c2 * c3;
+    const double ve1 = r[0][0] * vg[0] + r[1][0] * vg[1] + r[2][0] * vg[2];
+    const double ve2 = r[0][1] * vg[0] + r[1][1] * vg[1] + r[2][1] * vg[2];
+    const double ve3 = r[0][2] * vg[0] + r[1][2] * vg[1] + r[2][2] * vg[2];
+    double k = 0.0;
+    if (kt->iavgkeff == 0) {
+      double dnum = 1.0, d1 = ve1 * ve1, d2 = ve2 * ve2, d3 = ve3 * ve3;
+      if (ve1 != 0.0) { dnum = dnum * k11; d2 = d2 * k11; d3 = d3 * k11; }
+      if (ve2 != 0.0) { dnum = dnum * k22; d1 = d1 * k22; d3 = d3 * k22; }
+      if (ve3 != 0.0) { dnum = dnum * k33; d1 = d1 * k33; d2 = d2 * k33; }
+      const double denom = d1 + d2 + d3;
+      if (denom > 0.0) k = dnum / denom;
+    } else if (kt->iavgkeff == 1) {
+      k = ve1 * ve1 * k11 + ve2 * ve2 * k22 + ve3 * ve3 * k33;
+    }
+    return k;
+  };
+  auto hy_eff = [&](int a, int b, int ihc, int sidx) {
+    const double hy11 = m->k11[a], hy22 = kt->k22 ? kt->k22[a] : m->k11[a], hy33 = m->k33[a];
+    double v[3];
+    if (ihc == 0) {
+      if (!kt->angle2) return hy33;
+      normal(a, b, ihc, sidx, v);
+      return hyeff(hy11, hy22, hy33, rad(kt->angle1, a), rad(kt->angle2, a), rad(kt->angle3, a), v);
+    }
+    if (!kt->k22) return hy11;
+    normal(a, b, ihc, sidx, v);
+    double ang1 = 0.0, ang2 = 0.0, ang3 = 0.0;
+    if (kt->angle1) {
+      ang1 = rad(kt->angle1, a);
+      if (kt->angle2) {
+        ang2 = rad(kt->angle2, a);
+        if (kt->angle3) ang3 = rad(kt->angle3, a);
+      }
+    }
+    return hyeff(hy11, hy22, hy33, ang1, ang2, ang3, v);
+  };
+  std::vector<double> hy((size_t)2 * c.njas, 0.0);
+  for (int p = 0; p < n; ++p)
+    for (int q = c.ia[p] + 1; q < c.ia[p + 1]; ++q) {
+      const int mm = c.ja[q];
+      if (mm < p) continue;
+      const int sidx = c.jas[q];
+      hy[2 * (size_t)sidx] = hy_eff(p, mm, c.ihc[sidx], sidx);
+      hy[2 * (size_t)sidx + 1] = hy_eff(mm, p, c.ihc[sidx], sidx);
+    }
+  return hy;
+}
+
 int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, const double *strt,
               const Conn &c, const std::vector<double> &top, const std::vector<double> &bot,
-              const std::vector<double> &area, const gbsln_xt3d *xt = nullptr,
-              const gbsln_xt3d_geometry *geom = nullptr) {
+              const std::vector<double> &area, const gbsln_ktensor *xt = nullptr,
+              const gbsln_geometry *geom = nullptr) {
   const int n = h->n;
   std::vector<double> vol(n);
   for (int p = 0; p < n; ++p) vol[p] = area[p] * (top[p] - bot[p]);
@@ -683,6 +776,19 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
   bptr[n] = (int)bval.size();
   h->inewtonur = npf->inewton && npf->inewtonur;
   Xt3dHost xh;
+  std::vector<double> hyv;
+  if (xt && xt->xt3d == 0) {
+    if (xt->angle2 && !xt->angle1) {
+      h->err = "ANGLE2 SPECIFIED BUT NOT ANGLE1";
+      return GBIMS_ERR_ARG;
+    }
+    if ((xt->angle2 == nullptr) != (xt->angle3 == nullptr)) {
+      h->err = "ANGLE2 and ANGLE3 must be given both or neither";
+      return GBIMS_ERR_ARG;
+    }
+    if (xt->k22 || xt->angle2) hyv = npf_hy_host(m, xt, geom, c, h->nrow, h->ncol);
+    xt = nullptr;  // the standard formulation
+  }
   if (xt) {
     if (npf->icellavg != 0) {
       h->err = "ALTERNATIVE_CELL_AVERAGING cannot be used with XT3D";
@@ -713,6 +819,11 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
   if (h->inewtonur) {
     std::vector<int> ib = bottom_nodes(n, c, bot);
     chk(up(&h->ibotnode, ib.data(), ib.size()));
+  }
+  double *d_hy = nullptr;
+  if (!hyv.empty()) {
+    chk(up(&d_hy, hyv.data(), hyv.size()));
+    h->xt_mem[14] = d_hy;
   }
   h->has_sto = (m->ss != nullptr && m->sy != nullptr);
   if (h->has_sto) {
@@ -811,6 +922,7 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
   h->g.idewatcv = npf->idewatcv;
   h->g.icellavg = npf->icellavg;
   h->g.satomega = npf->satomega > 0 ? npf->satomega : 1.0e-6;
+  h->g.hy = d_hy;
   SLN_CUDA(h, cudaMemcpyAsync(h->x, strt, sizeof(double) * n, cudaMemcpyHostToDevice, h->st));
   gwf_condsat(n, h->g, h->d.condsat, h->st);
   if (xt && h->xt.lamatsaved) {
@@ -834,7 +946,7 @@ bool model_props_ok(const gbsln_model *m) {
 
 }  // namespace
 
-static int create_dis(const gbsln_model *m, const gbsln_xt3d *xt, const gbnpf_options *npf,
+static int create_dis(const gbsln_model *m, const gbsln_ktensor *xt, const gbnpf_options *npf,
                       const gbims_settings *ims, const gbsln_nonlinear *nl, const double *strt,
                       gbsln_handle **out) {
   if (!out) return GBIMS_ERR_ARG;
@@ -874,7 +986,7 @@ extern "C" int gbsln_create(const gbsln_model *m, const gbnpf_options *npf,
   return create_dis(m, nullptr, npf, ims, nl, strt, out);
 }
 
-extern "C" int gbsln_create_xt3d(const gbsln_model *m, const gbsln_xt3d *xt,
+extern "C" int gbsln_create_tensor(const gbsln_model *m, const gbsln_ktensor *xt,
                                  const gbnpf_options *npf, const gbims_settings *ims,
                                  const gbsln_nonlinear *nl, const double *strt,
                                  gbsln_handle **out) {
@@ -885,8 +997,8 @@ extern "C" int gbsln_create_xt3d(const gbsln_model *m, const gbsln_xt3d *xt,
   return create_dis(m, xt, npf, ims, nl, strt, out);
 }
 
-static int create_grid(const gbsln_grid *grid, const gbsln_model *m, const gbsln_xt3d *xt,
-                       const gbsln_xt3d_geometry *geom, const gbnpf_options *npf,
+static int create_grid(const gbsln_grid *grid, const gbsln_model *m, const gbsln_ktensor *xt,
+                       const gbsln_geometry *geom, const gbnpf_options *npf,
                        const gbims_settings *ims, const gbsln_nonlinear *nl, const double *strt,
                        gbsln_handle **out) {
   if (!out) return GBIMS_ERR_ARG;
@@ -967,12 +1079,12 @@ extern "C" int gbsln_create_grid(const gbsln_grid *grid, const gbsln_model *m,
   return create_grid(grid, m, nullptr, nullptr, npf, ims, nl, strt, out);
 }
 
-extern "C" int gbsln_create_grid_xt3d(const gbsln_grid *grid, const gbsln_model *m,
-                                      const gbsln_xt3d *xt, const gbsln_xt3d_geometry *geom,
+extern "C" int gbsln_create_grid_tensor(const gbsln_grid *grid, const gbsln_model *m,
+                                      const gbsln_ktensor *xt, const gbsln_geometry *geom,
                                       const gbnpf_options *npf, const gbims_settings *ims,
                                       const gbsln_nonlinear *nl, const double *strt,
                                       gbsln_handle **out) {
-  if (!xt || !geom || !geom->xc || !geom->yc || !geom->anglex) {
+  if (!xt || !geom || !geom->anglex || (xt->xt3d != 0 && (!geom->xc || !geom->yc))) {
     if (out) *out = nullptr;
     return GBIMS_ERR_ARG;
   }

@@ -141,6 +141,15 @@ __device__ double d_sqsat_derv(double top, double bot, double x, double eps) {
   return DDIV(y, b);
 }
 
+// the effective K of connection jj (n < m) at its lower- (hy_n) and higher-
+// numbered (hy_m) cell: hy_eff (gwf-npf.f90:2280-2357)
+__device__ __forceinline__ double hy_n(const NpfDev &g, int jj, int n, bool vert) {
+  return g.hy ? g.hy[2 * jj] : (vert ? g.k33[n] : g.k11[n]);
+}
+__device__ __forceinline__ double hy_m(const NpfDev &g, int jj, int m, bool vert) {
+  return g.hy ? g.hy[2 * jj + 1] : (vert ? g.k33[m] : g.k11[m]);
+}
+
 // calc_condsat (gwf-npf.f90:1950-2044) for every upper connection, with the
 // default initial saturation of one.
 __global__ void k_condsat(int nodes, NpfDev g, double *condsat) {
@@ -151,12 +160,13 @@ __global__ void k_condsat(int nodes, NpfDev g, double *condsat) {
       int jj = g.jas[ii];
       double csat;
       if (g.ihc[jj] == 0) {
-        csat = d_vcond(1, 1, 1, 1, 1, 1, 1.0, g.bot[n], g.bot[m], g.k33[n], g.k33[m], 1.0, 1.0,
-                       g.top[n], g.top[m], g.bot[n], g.bot[m], g.hwva[jj]);
-      } else {
-        csat = d_hcond(1, 1, 1, 1, 0, g.ihc[jj], g.icellavg, 1.0, g.top[n], g.top[m], 1.0, 1.0, g.k11[n],
-                       g.k11[m], g.top[n], g.top[m], g.bot[n], g.bot[m], g.cl1[jj], g.cl2[jj],
+        csat = d_vcond(1, 1, 1, 1, 1, 1, 1.0, g.bot[n], g.bot[m], hy_n(g, jj, n, true),
+                       hy_m(g, jj, m, true), 1.0, 1.0, g.top[n], g.top[m], g.bot[n], g.bot[m],
                        g.hwva[jj]);
+      } else {
+        csat = d_hcond(1, 1, 1, 1, 0, g.ihc[jj], g.icellavg, 1.0, g.top[n], g.top[m], 1.0, 1.0,
+                       hy_n(g, jj, n, false), hy_m(g, jj, m, false), g.top[n], g.top[m],
+                       g.bot[n], g.bot[m], g.cl1[jj], g.cl2[jj], g.hwva[jj]);
       }
       condsat[jj] = csat;
     }
@@ -188,13 +198,13 @@ __device__ __forceinline__ double conn_cond(const NpfDev &g, const int *ibound, 
                                             int jj) {
   if (g.ihc[jj] == 0) {
     return d_vcond(ibound[n], ibound[m], g.icelltype[n], g.icelltype[m], g.ivarcv, g.idewatcv,
-                   condsat[jj], h[n], h[m], g.k33[n], g.k33[m], sat[n], sat[m], g.top[n],
-                   g.top[m], g.bot[n], g.bot[m], g.hwva[jj]);
+                   condsat[jj], h[n], h[m], hy_n(g, jj, n, true), hy_m(g, jj, m, true), sat[n],
+                   sat[m], g.top[n], g.top[m], g.bot[n], g.bot[m], g.hwva[jj]);
   }
   return d_hcond(ibound[n], ibound[m], g.icelltype[n], g.icelltype[m], g.inewton, g.ihc[jj],
-                 g.icellavg,
-                 condsat[jj], h[n], h[m], sat[n], sat[m], g.k11[n], g.k11[m], g.top[n],
-                 g.top[m], g.bot[n], g.bot[m], g.cl1[jj], g.cl2[jj], g.hwva[jj]);
+                 g.icellavg, condsat[jj], h[n], h[m], sat[n], sat[m], hy_n(g, jj, n, false),
+                 hy_m(g, jj, m, false), g.top[n], g.top[m], g.bot[n], g.bot[m], g.cl1[jj],
+                 g.cl2[jj], g.hwva[jj]);
 }
 
 // One row of gwf_fc in gather form: NPF fc, STO fc, BND fc, NPF fn, STO fn.

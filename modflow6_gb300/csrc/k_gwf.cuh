@@ -13,6 +13,9 @@ struct NpfDev {
   const int *icelltype;
   int inewton, ivarcv, idewatcv, icellavg;
   double satomega;
+  // hy_eff per connection n < m (2 each: from n toward m, from m toward n)
+  // when K22 or the angles are given; nullptr: K11 horizontal, K33 vertical
+  const double *hy = nullptr;
 };
 
 // XT3D (Xt3dInterface.f90, Xt3dAlgorithm.f90), the NPF formulation with the

@@ -118,7 +118,8 @@ class GwfDisModel:
     idewatcv: int = 0       # NPF VARIABLECV DEWATERED
     icellavg: int = 0       # ALTERNATIVE_CELL_AVERAGING: 0 harmonic, 1 LOGARITHMIC, 2 AMT-LMK, 3 AMT-HMK
     name: str = ""
-    ixt3d: int = 0          # NPF XT3D (matrix form)
+    ixt3d: int = 0          # NPF XT3D: 0 off, 1 XT3D, 2 XT3D RHS
+    iavgkeff: int = 0       # effective K of K22/ANGLE1..3 without XT3D: 0 harmonic, 1 arithmetic
     k22: np.ndarray | None = None      # NPF K22 (default K11)
     angle1: np.ndarray | None = None   # NPF ANGLE1..3 in degrees; XT3D without ANGLE2
     angle2: np.ndarray | None = None   # has no z component in its horizontal terms

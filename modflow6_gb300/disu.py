@@ -389,7 +389,8 @@ class DisuModel:
     angldegx: np.ndarray | None = None  # per entry, degrees (ANGLDEGX)
     xc_u: np.ndarray | None = None      # per user cell: the cell centre (CELL2D)
     yc_u: np.ndarray | None = None
-    ixt3d: int = 0                      # NPF XT3D (matrix form): needs angldegx and the centres
+    ixt3d: int = 0          # NPF XT3D: 0 off, 1 XT3D, 2 XT3D RHS
+    iavgkeff: int = 0       # effective K of K22/ANGLE1..3 without XT3D: 0 harmonic, 1 arithmetic
     k22: np.ndarray | None = None
     angle1: np.ndarray | None = None    # degrees
     angle2: np.ndarray | None = None

@@ -213,7 +213,8 @@ class DisvModel:
     icellavg: int = 0
     name: str = ""
     disv: bool = True
-    ixt3d: int = 0                     # NPF XT3D (matrix form)
+    ixt3d: int = 0          # NPF XT3D: 0 off, 1 XT3D, 2 XT3D RHS
+    iavgkeff: int = 0       # effective K of K22/ANGLE1..3 without XT3D: 0 harmonic, 1 arithmetic
     k22: np.ndarray | None = None
     angle1: np.ndarray | None = None   # degrees
     angle2: np.ndarray | None = None

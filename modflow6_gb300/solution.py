@@ -170,25 +170,26 @@ class GwfSolution:
                                   nl.amomentum, nl.iallowptc, nl.numtrack, nl.btol, nl.breduc,
                                   nl.res_lim)
         self._h = C.c_void_p()
-        xt3d = bool(int(getattr(m, "ixt3d", 0)))
-        if xt3d:
-            from .xt3d import xt3d_pattern
+        ixt3d = int(getattr(m, "ixt3d", 0))
+        # the conductivity tensor: XT3D, or K22/ANGLE2 in the standard form
+        tensor = ixt3d != 0 or getattr(m, "k22", None) is not None or \
+            getattr(m, "angle2", None) is not None
+        if tensor:
             con = m.connections()
-            self._nja = int(xt3d_pattern(con["ia"], con["ja"])[1].size)
+            if ixt3d == 1:
+                from .xt3d import xt3d_pattern
+                self._nja = int(xt3d_pattern(con["ia"], con["ja"])[1].size)
 
             def opt(name):
                 v = getattr(m, name, None)
                 if v is None:
                     return None
-                keep["xt_" + name] = _f(v)
-                return _lib.dptr(keep["xt_" + name])
+                keep["kt_" + name] = _f(v)
+                return _lib.dptr(keep["kt_" + name])
 
-            rhsform = int(getattr(m, "ixt3d", 0)) == 2
-            if rhsform:
-                self._nja = int(con["nja"])
-            cx = _lib.GbslnXt3d(opt("k22"), opt("angle1"), opt("angle2"), opt("angle3"),
-                                int(rhsform))
-        if xt3d and general:
+            cx = _lib.GbslnKTensor(opt("k22"), opt("angle1"), opt("angle2"), opt("angle3"), ixt3d,
+                                   int(getattr(m, "iavgkeff", 0)))
+        if tensor and general:
             # the connection geometry: cell centres and face-normal angles
             disu = bool(getattr(m, "disu", False))
             if disu:
@@ -196,14 +197,14 @@ class GwfSolution:
             else:
                 xcn, ycn = np.tile(m.xc, m.nlay), np.tile(m.yc, m.nlay)
             keep.update(x_xc=_f(xcn), x_yc=_f(ycn), x_ax=_f(con["anglex"]))
-            cg = _lib.GbslnXt3dGeometry(_lib.dptr(keep["x_xc"]), _lib.dptr(keep["x_yc"]),
-                                        _lib.dptr(keep["x_ax"]), int(disu))
-            rc = lib.gbsln_create_grid_xt3d(C.byref(grid), C.byref(cm), C.byref(cx), C.byref(cg),
-                                            C.byref(npf), C.byref(cs), C.byref(cnl),
-                                            _lib.dptr(keep["strt"]), C.byref(self._h))
-        elif xt3d:
-            rc = lib.gbsln_create_xt3d(C.byref(cm), C.byref(cx), C.byref(npf), C.byref(cs),
-                                       C.byref(cnl), _lib.dptr(keep["strt"]), C.byref(self._h))
+            cg = _lib.GbslnGeometry(_lib.dptr(keep["x_xc"]), _lib.dptr(keep["x_yc"]),
+                                    _lib.dptr(keep["x_ax"]), int(disu))
+            rc = lib.gbsln_create_grid_tensor(C.byref(grid), C.byref(cm), C.byref(cx), C.byref(cg),
+                                              C.byref(npf), C.byref(cs), C.byref(cnl),
+                                              _lib.dptr(keep["strt"]), C.byref(self._h))
+        elif tensor:
+            rc = lib.gbsln_create_tensor(C.byref(cm), C.byref(cx), C.byref(npf), C.byref(cs),
+                                         C.byref(cnl), _lib.dptr(keep["strt"]), C.byref(self._h))
         elif general:
             rc = lib.gbsln_create_grid(C.byref(grid), C.byref(cm), C.byref(npf), C.byref(cs),
                                        C.byref(cnl), _lib.dptr(keep["strt"]), C.byref(self._h))

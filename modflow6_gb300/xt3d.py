@@ -1,7 +1,7 @@
 """XT3D: the NPF formulation with the full hydraulic conductivity tensor
 (src/Model/ModelUtilities/Xt3dInterface.f90, Xt3dAlgorithm.f90).
 
-The device computes the XT3D terms (gbsln_create_xt3d); this module gives
+The device computes the XT3D terms (gbsln_create_tensor); this module gives
 the matrix pattern they need: with XT3D each row holds the cell, its
 neighbours and the neighbours of its neighbours (xt3d_ac,
 Xt3dInterface.f90:124-189), the diagonal first and the rest ascending as

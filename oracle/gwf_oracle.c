@@ -244,6 +244,12 @@ double or_squadratic_sat_derv(double top, double bot, double x, double eps) {
   return y / b;
 }
 
+/* hy_eff (gwf-npf.f90:2280-2357) of connection jas from its lower- (HYN)
+ * and higher-numbered (HYM) cell: the per-connection values when K22 or the
+ * angles are given, else K11 (horizontal) or K33 (vertical). */
+#define HYN(m, jj, n, vert) ((m)->hy ? (m)->hy[2 * (jj)] : ((vert) ? (m)->k33[n] : (m)->k11[n]))
+#define HYM(m, jj, mm, vert) ((m)->hy ? (m)->hy[2 * (jj) + 1] : ((vert) ? (m)->k33[mm] : (m)->k11[mm]))
+
 /* The solution's pattern: the model's, or with XT3D the wider one. */
 #define SIA(m) ((m)->ixt3d ? (m)->sia : (m)->ia)
 #define SJA(m) ((m)->ixt3d ? (m)->sja : (m)->ja)
@@ -439,11 +445,11 @@ void or_npf_condsat(const or_gwf_model *m, double *condsat) {
       int ihc = m->ihc[jj];
       double csat;
       if (ihc == 0) {
-        double hyn = m->k33[n], hym = m->k33[mm];
+        double hyn = HYN(m, jj, n, 1), hym = HYM(m, jj, mm, 1);
         csat = vcond(1, 1, 1, 1, 1, 1, 1.0, m->bot[n], m->bot[mm], hyn, hym, 1.0, 1.0,
                      m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->hwva[jj]);
       } else {
-        double hyn = m->k11[n], hym = m->k11[mm];
+        double hyn = HYN(m, jj, n, 0), hym = HYM(m, jj, mm, 0);
         csat = hcond(1, 1, 1, 1, 0, ihc, m->icellavg, 1.0, m->top[n], m->top[mm], 1.0, 1.0,
                      hyn, hym, m->top[n], m->top[mm], m->bot[n], m->bot[mm],
                      m->cl1[jj], m->cl2[jj], m->hwva[jj]);
@@ -484,13 +490,13 @@ void or_npf_fc(const or_gwf_model *m, const int *ibound, const double *condsat,
       double cond;
       if (ihc == 0) {
         cond = vcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm],
-                     m->ivarcv, m->idewatcv, condsat[jj], hnew[n], hnew[mm], m->k33[n],
-                     m->k33[mm], sat[n], sat[mm], m->top[n], m->top[mm], m->bot[n],
+                     m->ivarcv, m->idewatcv, condsat[jj], hnew[n], hnew[mm], HYN(m, jj, n, 1),
+                     HYM(m, jj, mm, 1), sat[n], sat[mm], m->top[n], m->top[mm], m->bot[n],
                      m->bot[mm], m->hwva[jj]);
       } else {
         cond = hcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm],
                      m->inewton, ihc, m->icellavg, condsat[jj], hnew[n], hnew[mm], sat[n],
-                     sat[mm], m->k11[n], m->k11[mm], m->top[n], m->top[mm], m->bot[n],
+                     sat[mm], HYN(m, jj, n, 0), HYM(m, jj, mm, 0), m->top[n], m->top[mm], m->bot[n],
                      m->bot[mm], m->cl1[jj], m->cl2[jj], m->hwva[jj]);
       }
       int idiag = m->ia[n];
@@ -917,12 +923,12 @@ void or_gwf_budget(const or_gwf_model *m, const int *ibound, const double *conds
       double cond;
       if (m->ihc[jj] == 0) {
         cond = vcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm], m->ivarcv,
-                     m->idewatcv, condsat[jj], hnew[n], hnew[mm], m->k33[n], m->k33[mm], sat[n],
+                     m->idewatcv, condsat[jj], hnew[n], hnew[mm], HYN(m, jj, n, 1), HYM(m, jj, mm, 1), sat[n],
                      sat[mm], m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->hwva[jj]);
       } else {
         cond = hcond(ibound[n], ibound[mm], m->icelltype[n], m->icelltype[mm], m->inewton,
-                     m->ihc[jj], m->icellavg, condsat[jj], hnew[n], hnew[mm], sat[n], sat[mm], m->k11[n],
-                     m->k11[mm], m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->cl1[jj],
+                     m->ihc[jj], m->icellavg, condsat[jj], hnew[n], hnew[mm], sat[n], sat[mm], HYN(m, jj, n, 0),
+                     HYM(m, jj, mm, 0), m->top[n], m->top[mm], m->bot[n], m->bot[mm], m->cl1[jj],
                      m->cl2[jj], m->hwva[jj]);
       }
       double qnm = cond * (hnew[mm] - hnew[n]);

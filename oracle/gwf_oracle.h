@@ -51,6 +51,9 @@ typedef struct {
    * connection n < m in radians) */
   int xt_grid;
   const double *xc, *yc, *anglex;
+  /* hy_eff per connection n < m (2 each: from n toward m, from m toward
+   * n) when K22 or the angles are given (or_npf_hy), else NULL */
+  const double *hy;
 } or_gwf_model;
 
 /* NONLINEAR block state (NumericalSolution.f90 members). */
@@ -110,6 +113,11 @@ void or_xt3d_flowja(const or_gwf_model *m, const int *ibound, const double *sat,
                     const double *hnew, double *flowja);
 void or_xt3d_fn(const or_gwf_model *m, const int *ibound, const double *hnew,
                 const double *qsat, double *amat, double *rhs);
+/* hy_eff (gwf-npf.f90:2280-2357) with hyeff (HGeoUtil.f90:29-108) for
+ * every connection n < m: hy[2s] of cell n toward m, hy[2s+1] of m toward
+ * n; k22 NULL for none, angles in radians or NULL. */
+void or_npf_hy(const or_gwf_model *m, const double *k22, const double *angle1,
+               const double *angle2, const double *angle3, int iavgkeff, double *hy);
 double or_squadratic_sat(double top, double bot, double x, double eps);
 double or_squadratic_sat_derv(double top, double bot, double x, double eps);
 void or_npf_condsat(const or_gwf_model *m, double *condsat);

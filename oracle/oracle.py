@@ -60,7 +60,7 @@ class GwfModel(C.Structure):
                 ("nchd", C.c_int), ("chd_node", _ip), ("chd_head", _dp),
                 ("ixt3d", C.c_int), ("nozee", C.c_int), ("nja_sln", C.c_int), ("ck", _dp),
                 ("sia", _ip), ("sja", _ip), ("idxglo", _ip),
-                ("xt_grid", C.c_int), ("xc", _dp), ("yc", _dp), ("anglex", _dp)]
+                ("xt_grid", C.c_int), ("xc", _dp), ("yc", _dp), ("anglex", _dp), ("hy", _dp)]
 
 
 class Nonlinear(C.Structure):
@@ -135,6 +135,7 @@ def load():
         lib.or_xt3d_fn.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, _dp, _dp]
         lib.or_disu_connect.argtypes = [C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _ip, C.c_int, _ip,
                                         _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
+        lib.or_npf_hy.argtypes = [C.POINTER(GwfModel), _dp, _dp, _dp, _dp, C.c_int, _dp]
         lib.or_disv_anglex.argtypes = [C.c_int, C.c_int, _dp, _dp, _ip, _ip, _ip, _ip, _ip, _ip,
                                        _dp]
         lib.or_npf_condsat.argtypes = [C.POINTER(GwfModel), _dp]
@@ -463,15 +464,46 @@ class Gwf:
             int(m.rch_node.size), i(m.rch_node), d(m.rch_rate),
             int(m.chd_node.size), i(m.chd_node), d(m.chd_head))
         self.mcon = con
+        general = getattr(m, "disv", False) or getattr(m, "disu", False)
+        dpio180 = math.atan(1.0) / 45.0
+        rad = lambda a: (None if a is None else np.asarray(a, float) * dpio180)
+        if general and (int(getattr(m, "ixt3d", 0)) or getattr(m, "k22", None) is not None
+                        or getattr(m, "angle2", None) is not None):
+            # the connection geometry: DISV, the shared edges' normal angles
+            # (cprops); DISU, ANGLDEGX
+            if getattr(m, "disv", False):
+                iav, jav = m.vertex_lists
+                ax = np.zeros(con["njas"])
+                self.lib.or_disv_anglex(m.nlay, len(m.icvert), d(m.vertices[:, 0]),
+                                        d(m.vertices[:, 1]), i(iav), i(jav), i(con["ia"]),
+                                        i(con["ja"]), i(con["jas"]), i(con["ihc"]), dp(ax))
+                xcn, ycn = np.tile(m.xc, m.nlay), np.tile(m.yc, m.nlay)
+                self.model.xt_grid = 1
+            else:
+                ax = con["anglex"]
+                xcn, ycn = m.xc, m.yc
+                self.model.xt_grid = 2
+            self.model.xc, self.model.yc, self.model.anglex = d(xcn), d(ycn), d(ax)
+            con = dict(con, anglex=ax)
+        if not int(getattr(m, "ixt3d", 0)) and (getattr(m, "k22", None) is not None
+                                                or getattr(m, "angle2", None) is not None):
+            # hy_eff per connection (K22 and the angles, standard formulation)
+            hy = np.zeros(2 * con["njas"])
+            opt = lambda a: d(a) if a is not None else None
+            self.lib.or_npf_hy(C.byref(self.model), opt(getattr(m, "k22", None)),
+                               opt(rad(getattr(m, "angle1", None))), opt(rad(getattr(m, "angle2", None))),
+                               opt(rad(getattr(m, "angle3", None))), int(getattr(m, "iavgkeff", 0)),
+                               dp(hy))
+            self.model.hy = d(hy)
+            con = dict(con, hy=hy)
         if int(getattr(m, "ixt3d", 0)):
             # XT3D on a DIS grid: the tensor per cell and the wider pattern
             nozee = m.angle2 is None
-            dpio180 = math.atan(1.0) / 45.0
-            rad = lambda a: (np.zeros(n) if a is None else np.asarray(a, float) * dpio180)
+            radz = lambda a: (np.zeros(n) if a is None else np.asarray(a, float) * dpio180)
             k22 = m.k11 if m.k22 is None else m.k22
             ck = np.zeros(9 * n)
-            self.lib.or_xt3d_ck(n, d(m.k11), d(k22), d(m.k33), d(rad(m.angle1)), d(rad(m.angle2)),
-                                d(rad(m.angle3)), int(nozee), dp(ck))
+            self.lib.or_xt3d_ck(n, d(m.k11), d(k22), d(m.k33), d(radz(m.angle1)), d(radz(m.angle2)),
+                                d(radz(m.angle3)), int(nozee), dp(ck))
             ixt3d = int(m.ixt3d)
             if ixt3d == 2:
                 # XT3D RHS: the model's own pattern
@@ -491,22 +523,6 @@ class Gwf:
                 sja = sja[:nja_sln].copy()
             self.model.ixt3d, self.model.nozee, self.model.nja_sln = ixt3d, int(nozee), nja_sln
             self.model.ck, self.model.sia, self.model.sja, self.model.idxglo = d(ck), i(sia), i(sja), i(idxglo)
-            if getattr(m, "disv", False) or getattr(m, "disu", False):
-                # DISV: the shared edges' normal angles (cprops); DISU: ANGLDEGX
-                if getattr(m, "disv", False):
-                    iav, jav = m.vertex_lists
-                    ax = np.zeros(con["njas"])
-                    self.lib.or_disv_anglex(m.nlay, len(m.icvert), d(m.vertices[:, 0]),
-                                            d(m.vertices[:, 1]), i(iav), i(jav), i(con["ia"]),
-                                            i(con["ja"]), i(con["jas"]), i(con["ihc"]), dp(ax))
-                    xcn, ycn = np.tile(m.xc, m.nlay), np.tile(m.yc, m.nlay)
-                    self.model.xt_grid = 1
-                else:
-                    ax = con["anglex"]
-                    xcn, ycn = m.xc, m.yc
-                    self.model.xt_grid = 2
-                self.model.xc, self.model.yc, self.model.anglex = d(xcn), d(ycn), d(ax)
-                con = dict(con, anglex=ax)
             con = dict(con, ia=sia, ja=sja, nja=nja_sln, idxglo=idxglo, ck=ck)
         self.con = con
         self._keep = keep

@@ -931,3 +931,85 @@ void or_xt3d_flowja(const or_gwf_model *m, const int *ibound, const double *sat,
   }
   xt3d_free(&x);
 }
+
+/* hyeff (HGeoUtil.f90:29-108) */
+static double hyeff(double k11, double k22, double k33, double ang1, double ang2, double ang3,
+                    double vg1, double vg2, double vg3, int iavgmeth) {
+  double s1 = sin(ang1), c1 = cos(ang1), s2 = sin(ang2), c2 = cos(ang2), s3 = sin(ang3),
+         c3 = cos(ang3);
+  double r[3][3];
+  r[0][0] = c1 * c2;
+  r[0][1] = c1 * s2 * s3 - s1 * c3;
+  r[0][2] = -c1 * s2 * c3 - s1 * s3;
+  r[1][0] = s1 * c2;
+  r[1][1] = s1 * s2 * s3 + c1 * c3;
+  r[1][2] = -s1 * s2 * c3 + c1 * s3;
+  r[2][0] = s2;
+  r[2][1] = -c2 * s3;
+  r[2][2] = c2 * c3;
+  double ve1 = r[0][0] * vg1 + r[1][0] * vg2 + r[2][0] * vg3;
+  double ve2 = r[0][1] * vg1 + r[1][1] * vg2 + r[2][1] * vg3;
+  double ve3 = r[0][2] * vg1 + r[1][2] * vg2 + r[2][2] * vg3;
+  double k = 0.0;
+  if (iavgmeth == 0) {
+    double dnum = 1.0, d1 = ve1 * ve1, d2 = ve2 * ve2, d3 = ve3 * ve3;
+    if (ve1 != 0.0) {
+      dnum = dnum * k11;
+      d2 = d2 * k11;
+      d3 = d3 * k11;
+    }
+    if (ve2 != 0.0) {
+      dnum = dnum * k22;
+      d1 = d1 * k22;
+      d3 = d3 * k22;
+    }
+    if (ve3 != 0.0) {
+      dnum = dnum * k33;
+      d1 = d1 * k33;
+      d2 = d2 * k33;
+    }
+    double denom = d1 + d2 + d3;
+    if (denom > 0.0) k = dnum / denom;
+  } else if (iavgmeth == 1) {
+    k = ve1 * ve1 * k11 + ve2 * ve2 * k22 + ve3 * ve3 * k33;
+  }
+  return k;
+}
+
+/* hy_eff (gwf-npf.f90:2280-2357) of cell a toward cell b; ipos is the
+ * position of the connection in the lower-numbered cell's row */
+static double hy_eff(const or_gwf_model *m, const double *k22, const double *angle1,
+                     const double *angle2, const double *angle3, int iavgkeff, int a, int b,
+                     int ihc, int ipos) {
+  double hy11 = m->k11[a], hy22 = k22 ? k22[a] : m->k11[a], hy33 = m->k33[a];
+  double v[3];
+  if (ihc == 0) {
+    if (!angle2) return hy33;
+    conn_normal(m, a, b, ihc, ipos, v);
+    double ang1 = angle1[a], ang2 = angle2[a], ang3 = angle3 ? angle3[a] : 0.0;
+    return hyeff(hy11, hy22, hy33, ang1, ang2, ang3, v[0], v[1], v[2], iavgkeff);
+  }
+  if (!k22) return hy11;
+  conn_normal(m, a, b, ihc, ipos, v);
+  double ang1 = 0.0, ang2 = 0.0, ang3 = 0.0;
+  if (angle1) {
+    ang1 = angle1[a];
+    if (angle2) {
+      ang2 = angle2[a];
+      if (angle3) ang3 = angle3[a];
+    }
+  }
+  return hyeff(hy11, hy22, hy33, ang1, ang2, ang3, v[0], v[1], v[2], iavgkeff);
+}
+
+void or_npf_hy(const or_gwf_model *m, const double *k22, const double *angle1,
+               const double *angle2, const double *angle3, int iavgkeff, double *hy) {
+  for (int n = 0; n < m->nodes; ++n)
+    for (int ii = m->ia[n] + 1; ii < m->ia[n + 1]; ++ii) {
+      int mm = m->ja[ii];
+      if (mm < n) continue;
+      int s = m->jas[ii], ihc = m->ihc[s];
+      hy[2 * s] = hy_eff(m, k22, angle1, angle2, angle3, iavgkeff, n, mm, ihc, ii);
+      hy[2 * s + 1] = hy_eff(m, k22, angle1, angle2, angle3, iavgkeff, mm, n, ihc, ii);
+    }
+}

@@ -442,3 +442,62 @@ def test_gpu_xt3d_rhs_timestep(gblib):
     sg = sol.timestep(1, 1, 1.0)
     assert sg["converged"] == 1
     assert np.abs(sol.heads - h).max() < 1e-8
+
+
+# ---- K22 and the angles in the standard formulation (hy_eff) ---------------
+
+def test_oracle_k22_standard_conductances_by_hand():
+    """K22 without XT3D: a connection along x takes K11, one along y K22
+    (hy_eff with ANGLE1 0), in the harmonic mean of the transmissivities;
+    ANGLE1 90 with K11 and K22 swapped gives the same matrix to rounding."""
+    m, h = aniso_model(1, 4, 5, (0.0, 0.0, 0.0), False, xt3d=False)
+    m.k22 = np.full(m.nodes, 1.0)
+    m.angle1 = None
+    g = oracle.Gwf(m, oracle.settings())
+    a, _ = g.assemble(h)
+    con = g.con
+    p = 1 * m.ncol + 1
+    row = slice(con["ia"][p], con["ia"][p + 1])
+    cols = con["ja"][row]
+    east = con["ia"][p] + int(np.flatnonzero(cols == p + 1)[0])
+    south = con["ia"][p] + int(np.flatnonzero(cols == p + m.ncol)[0])
+    i, j = 1, 1
+    tx = 5.0 * 10.0
+    hm = lambda t1, t2, c1, c2, w: w * t1 * t2 / (t1 * c2 + t2 * c1)
+    assert a[east] == pytest.approx(hm(tx, tx, 0.5 * m.delr[j], 0.5 * m.delr[j + 1], m.delc[i]), rel=1e-14)
+    ty = 1.0 * 10.0
+    assert a[south] == pytest.approx(hm(ty, ty, 0.5 * m.delc[i], 0.5 * m.delc[i + 1], m.delr[j]), rel=1e-14)
+    m.k11, m.k22 = np.full(m.nodes, 1.0), np.full(m.nodes, 5.0)
+    m.angle1 = np.full(m.nodes, 90.0)
+    a90, _ = oracle.Gwf(m, oracle.settings()).assemble(h)
+    np.testing.assert_allclose(a90, a, rtol=1e-12, atol=1e-12 * np.abs(a).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("grid", ["dis", "dis-angle2", "disv", "disu"])
+@pytest.mark.parametrize("iavgkeff", [0, 1])
+def test_gpu_k22_angles_fill_bitexact(gblib, grid, iavgkeff):
+    """K22 and ANGLE1..3 in the standard formulation: the effective K of each
+    connection's direction (hy_eff, hyeff) made on the host, the saturated
+    conductances and the fill on the device, against the oracle bit for bit
+    (convertible cells, Newton, transient)."""
+    if grid.startswith("dis") and not grid.startswith("disv") and not grid.startswith("disu"):
+        m, h = aniso_model(*CASES[1], xt3d=False, icelltype=1)
+        if grid == "dis":
+            m.angle2 = m.angle3 = None
+    elif grid == "disv":
+        m, h = _general_linear(_disv(), xt3d=False, icelltype=1)
+    else:
+        m, h = _general_linear(_disu(), xt3d=False, icelltype=1)
+    m.iavgkeff = iavgkeff
+    m.inewton = 1
+    m.ss, m.sy = np.full(m.nodes, 1e-5), np.full(m.nodes, 0.15)
+    g, sol = _gpu_pair(m)
+    rng = np.random.default_rng(7)
+    hh = np.maximum(h, m.cell_bot + 1.0) + rng.uniform(-8.0, 2.0, m.nodes)
+    hold = h + rng.uniform(-1.0, 1.0, m.nodes)
+    sol.heads = hh
+    amat, rhs = sol.formulate(delt=2.5, hold=hold)
+    ao, ro = g.assemble(hh, hold=hold, delt=2.5, transient=True)
+    np.testing.assert_array_equal(amat, ao)
+    np.testing.assert_array_equal(rhs, ro)
