@@ -518,6 +518,12 @@ typedef struct gbsln_budget_table {
  * a converged time step.  flowja: host array of nja values (FLOW-JA-FACE,
  * CSR order; the diagonal holds the cell's net flow) or NULL. */
 int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table *out);
+/* The per-cell and per-entry rates behind the budget, as the packages save
+ * them to the budget file (sto_cq strgss/strgsy per cell; the CHD, WEL and
+ * RCH rates per list entry in list order; bnd_cq, gwf-chd.f90:264-346).  Any
+ * pointer may be NULL. */
+int gbsln_budget_cells(gbsln_handle *h, double *sto_ss, double *sto_sy, double *chd_rate,
+                       double *wel_rate, double *rch_rate);
 /* Restores the initial heads (IC STRT) on the device: the state at the start
  * of the simulation, for repeated runs of the same model. */
 int gbsln_restart(gbsln_handle *h);

@@ -169,6 +169,7 @@ _SIGS = {
     "gbsln_create_tensor": (C.c_int, [C.POINTER(GbslnModel), C.POINTER(GbslnKTensor), C.POINTER(GbnpfOptions),
                                     C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,
                                     C.POINTER(C.c_void_p)]),
+    "gbsln_budget_cells": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp, _dp]),
     "gbsln_create_grid_tensor": (C.c_int, [C.POINTER(GbslnGrid), C.POINTER(GbslnModel), C.POINTER(GbslnKTensor),
                                          C.POINTER(GbslnGeometry), C.POINTER(GbnpfOptions),
                                          C.POINTER(GbimsSettings), C.POINTER(GbslnNonlinear), _dp,

@@ -254,6 +254,9 @@ struct gbsln_handle {
   Xt3dDev xt{};             // XT3D on the device (xt.on 0: off)
   int njas = 0;
   int nja_m = 0;            // the model's connections (FLOW-JA-FACE entries)
+  // boundary entries in bnd_ptr order: their package list index and kind
+  std::vector<int> bnd_list, bnd_kind_h, chd_node_h;
+  int nwel = 0, nrch = 0;
   void *xt_mem[16] = {};    // XT3D device arrays, freed by gbsln_destroy
   double *galpha = nullptr; // the last warm step's projection factors (2)
   double *dprev = nullptr;  // the last step's head change (valid when have_prev)
@@ -753,26 +756,34 @@ int sln_setup(gbsln_handle *h, const gbsln_model *m, const gbnpf_options *npf, c
     ibound[node] = -1;
   }
   // boundary values per node: WEL q, then RCH rate*area (package order)
-  std::vector<std::vector<std::pair<double, int>>> per(n);
+  struct BndEntry { double v; int kind, list; };
+  std::vector<std::vector<BndEntry>> per(n);
   for (int i = 0; i < m->nwel; ++i) {
     int node = m->wel_node[i];
     if (node < 0 || node >= n) { h->err = "WEL node out of range"; return GBIMS_ERR_ARG; }
-    per[node].push_back({m->wel_q[i], 0});
+    per[node].push_back({m->wel_q[i], 0, i});
   }
   for (int i = 0; i < m->nrch; ++i) {
     int node = m->rch_node[i];
     if (node < 0 || node >= n) { h->err = "RCH node out of range"; return GBIMS_ERR_ARG; }
-    per[node].push_back({m->rch_rate[i] * area[node], 1});
+    per[node].push_back({m->rch_rate[i] * area[node], 1, i});
   }
   std::vector<int> bptr(n + 1, 0), bkind;
   std::vector<double> bval;
+  h->bnd_list.clear();
+  h->bnd_kind_h.clear();
   for (int p = 0; p < n; ++p) {
     bptr[p] = (int)bval.size();
     for (const auto &v : per[p]) {
-      bval.push_back(v.first);
-      bkind.push_back(v.second);
+      bval.push_back(v.v);
+      bkind.push_back(v.kind);
+      h->bnd_list.push_back(v.list);
+      h->bnd_kind_h.push_back(v.kind);
     }
   }
+  h->nwel = m->nwel;
+  h->nrch = m->nrch;
+  h->chd_node_h.assign(m->chd_node, m->chd_node + m->nchd);
   bptr[n] = (int)bval.size();
   h->inewtonur = npf->inewton && npf->inewtonur;
   Xt3dHost xh;
@@ -1459,8 +1470,8 @@ extern "C" int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table 
   f.bnd_val = h->bnd_val;
   f.xt = h->xt;
   if (f.xt.on) xt3d_pairs(h->njas, h->g, f.xt, h->ibound, h->d.sat, h->x, 2, h->st);
-  gwf_budget(n, h->g, f, h->bnd_kind, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat, dflow,
-             h->bpart, h->G, h->st);
+  gwf_budget(n, h->g, f, h->bnd_kind, nullptr, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat,
+             dflow, h->bpart, h->G, h->st);
   std::vector<double> part((size_t)kGwfBudgetSlots * h->G);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
@@ -1495,6 +1506,48 @@ extern "C" int gbsln_budget(gbsln_handle *h, double *flowja, gbsln_budget_table 
   out->percent_discrepancy = (avg != 0.0) ? 100.0 * (out->total_in - out->total_out) / avg : 0.0;
   out->max_cell_imbalance = best;
   out->max_cell = (int)row;
+  return GBIMS_OK;
+}
+
+extern "C" int gbsln_budget_cells(gbsln_handle *h, double *sto_ss, double *sto_sy,
+                                  double *chd_rate, double *wel_rate, double *rch_rate) {
+  if (!h) return GBIMS_ERR_ARG;
+  const int n = h->n;
+  const size_t nb = h->bnd_list.size();
+  const bool transient = (h->last_delt > 0.0) && h->has_sto;
+  if (!h->bpart) SLN_CUDA(h, cudaMalloc((void **)&h->bpart, sizeof(double) * kGwfBudgetSlots * h->G));
+  double *dcells = nullptr;
+  SLN_CUDA(h, cudaMallocAsync((void **)&dcells, sizeof(double) * (3 * (size_t)n + nb + 1), h->st));
+  FillDev f{};
+  f.transient = transient ? 1 : 0;
+  f.tled = transient ? 1.0 / h->last_delt : 0.0;
+  f.ss = h->ss;
+  f.sy = h->sy;
+  f.area = h->area;
+  f.bnd_ptr = h->bnd_ptr;
+  f.bnd_val = h->bnd_val;
+  f.xt = h->xt;
+  if (f.xt.on) xt3d_pairs(h->njas, h->g, f.xt, h->ibound, h->d.sat, h->x, 2, h->st);
+  gwf_budget(n, h->g, f, h->bnd_kind, dcells, h->ibound, h->x, h->xold, h->d.sat, h->d.condsat,
+             nullptr, h->bpart, h->G, h->st);
+  std::vector<double> c(3 * (size_t)n + nb);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c.data(), dcells, sizeof(double) * c.size(), cudaMemcpyDeviceToHost, h->st);
+  cudaFreeAsync(dcells, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) {
+    h->err = std::string("gbsln_budget_cells: ") + cudaGetErrorString(e);
+    return GBIMS_ERR_CUDA;
+  }
+  if (sto_ss) std::copy(c.begin(), c.begin() + n, sto_ss);
+  if (sto_sy) std::copy(c.begin() + n, c.begin() + 2 * (size_t)n, sto_sy);
+  if (chd_rate)
+    for (size_t i = 0; i < h->chd_node_h.size(); ++i) chd_rate[i] = c[2 * (size_t)n + h->chd_node_h[i]];
+  for (size_t e2 = 0; e2 < nb; ++e2) {
+    double *dst = (h->bnd_kind_h[e2] == 0) ? wel_rate : rch_rate;
+    if (dst) dst[h->bnd_list[e2]] = c[3 * (size_t)n + e2];
+  }
   return GBIMS_OK;
 }
 

@@ -518,7 +518,8 @@ __global__ void __launch_bounds__(256) k_gwf_budget(int nodes, NpfDev g, FillDev
                                                     const double *__restrict__ hold,
                                                     const double *__restrict__ sat,
                                                     const double *__restrict__ condsat,
-                                                    double *flowja, double *part) {
+                                                    double *flowja, double *part,
+                                                    double *cells) {
   double acc[kGwfBudgetSlots];
 #pragma unroll
   for (int t = 0; t < kGwfBudgetSlots; ++t) acc[t] = 0.0;
@@ -554,6 +555,7 @@ __global__ void __launch_bounds__(256) k_gwf_budget(int nodes, NpfDev g, FillDev
       const double rss = DSUB(DMUL(aterm, h[p]), rhsterm);
       diag = DADD(diag, rss);
       inout(0, rss);
+      if (cells) cells[p] = rss;
       double rsy = 0.0;
       if (iconvert != 0) {
         const double rho2 = DMUL(DMUL(f.sy[p], f.area[p]), f.tled);
@@ -562,6 +564,10 @@ __global__ void __launch_bounds__(256) k_gwf_budget(int nodes, NpfDev g, FillDev
       }
       diag = DADD(diag, rsy);
       inout(1, rsy);
+      if (cells) cells[nodes + p] = rsy;
+    } else if (cells) {
+      cells[p] = 0.0;
+      cells[nodes + p] = 0.0;
     }
     // WEL, RCH: rhs = -v, hcof = 0
     for (int e = f.bnd_ptr[p]; e < f.bnd_ptr[p + 1]; ++e) {
@@ -569,6 +575,7 @@ __global__ void __launch_bounds__(256) k_gwf_budget(int nodes, NpfDev g, FillDev
       if (ibound[p] > 0) rr = DSUB(DMUL(0.0, h[p]), -f.bnd_val[e]);
       diag = DADD(diag, rr);
       inout(3 + bnd_kind[e], rr);
+      if (cells) cells[3 * (size_t)nodes + e] = rr;
     }
     // NPF flows, diagonal sum, CHD
     const bool chd = ibound[p] < 0;
@@ -606,6 +613,7 @@ __global__ void __launch_bounds__(256) k_gwf_budget(int nodes, NpfDev g, FillDev
       acc[4] = DADD(acc[4], cin);
       acc[5] = DADD(acc[5], cout);
     }
+    if (cells) cells[2 * (size_t)nodes + p] = crate;
     if (flowja) flowja[i0] = diag;
     if (ibound[p] > 0 && fabs(diag) > acc[10]) {
       acc[10] = fabs(diag);
@@ -911,10 +919,11 @@ void gwf_backtrack(int nodes, double breduc, const int *active, double *x, const
   k_backtrack<<<g_grid(nodes), 256, 0, st>>>(nodes, breduc, active, x, xtemp);
 }
 
-void gwf_budget(int nodes, const NpfDev &g, const FillDev &f, const int *bnd_kind,
+void gwf_budget(int nodes, const NpfDev &g, const FillDev &f, const int *bnd_kind, double *cells,
                 const int *ibound, const double *h, const double *hold, const double *sat,
                 const double *condsat, double *flowja, double *part, int G, cudaStream_t st) {
-  k_gwf_budget<<<G, 256, 0, st>>>(nodes, g, f, bnd_kind, ibound, h, hold, sat, condsat, flowja, part);
+  k_gwf_budget<<<G, 256, 0, st>>>(nodes, g, f, bnd_kind, ibound, h, hold, sat, condsat, flowja, part,
+                                  cells);
 }
 
 }  // namespace gb

@@ -98,8 +98,10 @@ void gwf_backtrack(int nodes, double breduc, const int *active, double *x, const
                    cudaStream_t st);
 // Flows and model budget terms; part holds kGwfBudgetSlots doubles per block
 // (in/out of STO-SS, STO-SY, CHD, WEL, RCH; max |flowja diagonal|, its row).
+// cells (or nullptr): the per-cell rates STO-SS [0, n), STO-SY [n, 2n), CHD
+// [2n, 3n), then each boundary entry's rate in bnd_ptr order.
 constexpr int kGwfBudgetSlots = 12;
-void gwf_budget(int nodes, const NpfDev &g, const FillDev &f, const int *bnd_kind,
+void gwf_budget(int nodes, const NpfDev &g, const FillDev &f, const int *bnd_kind, double *cells,
                 const int *ibound, const double *h, const double *hold, const double *sat,
                 const double *condsat, double *flowja, double *part, int G, cudaStream_t st);
 

@@ -251,6 +251,32 @@ class GwfSolution:
 
     BUDGET_ENTRIES = ("STO-SS", "STO-SY", "CHD", "WEL", "RCH")
 
+    def budget_cells(self) -> dict:
+        """The rates the packages save to the budget file for the last time
+        step (gbsln_budget_cells): sto_ss and sto_sy per cell; chd, wel and
+        rch per list entry."""
+        lib = _lib.load()
+        m = self.m
+        out = dict(sto_ss=np.zeros(self.nodes), sto_sy=np.zeros(self.nodes),
+                   chd=np.zeros(len(m.chd_node)), wel=np.zeros(len(m.wel_node)),
+                   rch=np.zeros(len(m.rch_node)))
+        rc = lib.gbsln_budget_cells(self._h, *[_lib.dptr(out[k]) for k in
+                                               ("sto_ss", "sto_sy", "chd", "wel", "rch")])
+        if rc < 0:
+            raise _lib.GbimsError(rc, lib.gbsln_last_error(self._h).decode())
+        return out
+
+    def save_budget(self, path, name: str = "gwf", kstp: int = 1, kper: int = 1,
+                    delt: float = 1.0, pertim: float = 1.0, totim: float = 1.0,
+                    append: bool = False) -> None:
+        """Writes the last time step's flows as MODFLOW 6's budget file does
+        (OC SAVE BUDGET; mf6io.write_budget)."""
+        from .mf6io import gwf_budget_records, write_budget
+        fj, _ = self.budget(flowja=True)
+        recs = gwf_budget_records(self.m, name, fj, self.budget_cells(), kstp, kper, delt,
+                                  pertim, totim)
+        write_budget(path, recs, append=append)
+
     def budget(self, flowja: bool = False):
         """Model budget of the last time step (gbsln_budget): rates in/out per
         entry, totals, percent discrepancy and the largest cell imbalance;
