@@ -99,16 +99,34 @@ def _shared_edges(iavert, javert, nvert):
     return e[:, [0, 1, 3, 4]]
 
 
-def disv_connections(nlay: int, iavert, javert, vx, vy, xc, yc, top, bot) -> dict:
-    """CSR connectivity and symmetric-connection geometry of a full DISV grid
-    (top/bot per node, layer-major); also the cell areas (ncpl)."""
+def disv_nodereduced(idomain) -> np.ndarray:
+    """nodereduced in the reference's convention (Disv.f90 grid finalize):
+    the 1-based reduced number of a cell with IDOMAIN > 0, 0 for IDOMAIN 0
+    (removed), -1 for IDOMAIN < 0 (a vertical pass-through cell)."""
+    idomain = np.asarray(idomain, np.int64)
+    red = np.where(idomain > 0, 0, np.where(idomain < 0, -1, 0)).astype(np.int64)
+    act = idomain > 0
+    red[act] = np.arange(1, int(act.sum()) + 1)
+    return red
+
+
+def disv_connections(nlay: int, iavert, javert, vx, vy, xc, yc, top, bot, idomain=None) -> dict:
+    """CSR connectivity and symmetric-connection geometry of a DISV grid
+    (top/bot per user node, layer-major), reduced to the cells with IDOMAIN
+    > 0 as vertexconnect (Connections.f90:1272-1361) does: a vertical
+    connection passes through cells with IDOMAIN < 0 to the next cell above
+    or below that is not one, and exists if that cell is active; also the
+    cell areas (ncpl) and nodeuser (reduced -> user, 0-based)."""
     iavert = np.asarray(iavert, np.int64)
     javert = np.asarray(javert, np.int64)
     vx, vy = np.asarray(vx, float), np.asarray(vy, float)
     xc, yc = np.asarray(xc, float), np.asarray(yc, float)
     top, bot = np.asarray(top, float), np.asarray(bot, float)
     ncpl = iavert.size - 1
-    n = nlay * ncpl
+    nu = nlay * ncpl
+    red = disv_nodereduced(np.ones(nu) if idomain is None else idomain)
+    nodeuser = np.flatnonzero(red > 0)
+    n = nodeuser.size
     nvert = int(javert.max()) + 1
     edges = _shared_edges(iavert, javert, nvert)  # (j1, j2, a, b)
     # horizontal neighbours per cell, ascending
@@ -118,12 +136,17 @@ def disv_connections(nlay: int, iavert, javert, vx, vy, xc, yc, top, bot) -> dic
         nbr[j1].append(j2)
         eab[(j1, j2)] = (a, b)
     rows = []
-    for k in range(nlay):
-        for j in range(ncpl):
-            node = j + k * ncpl
-            off = [node + ncpl * d for d, ok in ((-1, k > 0), (1, k < nlay - 1)) if ok]
-            off += [j2 + k * ncpl for j2 in nbr[j]]
-            rows.append([node] + sorted(off))
+    for u in nodeuser:
+        k, j = divmod(int(u), ncpl)
+        off = []
+        for step in (-1, 1):
+            kk = k + step
+            while 0 <= kk < nlay and red[j + kk * ncpl] < 0:
+                kk += step
+            if 0 <= kk < nlay and red[j + kk * ncpl] > 0:
+                off.append(int(red[j + kk * ncpl]) - 1)
+        off += [int(red[j2 + k * ncpl]) - 1 for j2 in nbr[j] if red[j2 + k * ncpl] > 0]
+        rows.append([int(red[u]) - 1] + sorted(set(off)))
     ia = np.zeros(n + 1, np.int64)
     ia[1:] = np.cumsum([len(r) for r in rows])
     ja = np.concatenate([np.array(r, np.int64) for r in rows])
@@ -146,13 +169,14 @@ def disv_connections(nlay: int, iavert, javert, vx, vy, xc, yc, top, bot) -> dic
     pu = np.flatnonzero(upper)
     nn, mm = rown[pu], ja[pu]
     s = jas[pu]
-    jn, jm = nn % ncpl, mm % ncpl
+    un, um = nodeuser[nn], nodeuser[mm]
+    jn, jm = un % ncpl, um % ncpl
     vert = jn == jm
     sv = s[vert]
     ihc[sv] = 0
     hwva[sv] = area[jn[vert]]
-    cl1[sv] = 0.5 * (top[nn[vert]] - bot[nn[vert]])
-    cl2[sv] = 0.5 * (top[mm[vert]] - bot[mm[vert]])
+    cl1[sv] = 0.5 * (top[un[vert]] - bot[un[vert]])
+    cl2[sv] = 0.5 * (top[um[vert]] - bot[um[vert]])
     hz = ~vert
     sh = s[hz]
     ihc[sh] = 1
@@ -178,7 +202,8 @@ def disv_connections(nlay: int, iavert, javert, vx, vy, xc, yc, top, bot) -> dic
     anglex[sh] = [v if v >= 0.0 else two_pi + v for v in ax]
     return dict(nodes=n, nja=nja, njas=njas, ia=ia.astype(np.int32), ja=ja.astype(np.int32),
                 isym=isym.astype(np.int32), jas=jas.astype(np.int32), ihc=ihc.astype(np.int32),
-                cl1=cl1, cl2=cl2, hwva=hwva, area=area, anglex=anglex)
+                cl1=cl1, cl2=cl2, hwva=hwva, area=area, anglex=anglex,
+                nodeuser=nodeuser.astype(np.int32), nodereduced=red.astype(np.int32))
 
 
 @dataclass
@@ -213,6 +238,7 @@ class DisvModel:
     icellavg: int = 0
     name: str = ""
     disv: bool = True
+    idomain: np.ndarray | None = None  # per user cell; the cell arrays are per active cell
     ixt3d: int = 0          # NPF XT3D: 0 off, 1 XT3D, 2 XT3D RHS
     iavgkeff: int = 0       # effective K of K22/ANGLE1..3 without XT3D: 0 harmonic, 1 arithmetic
     k22: np.ndarray | None = None
@@ -233,32 +259,52 @@ class DisvModel:
         return self.ncpl
 
     @property
+    def nodeuser(self) -> np.ndarray:
+        nu = self.nlay * self.ncpl
+        if self.idomain is None:
+            return np.arange(nu)
+        return np.flatnonzero(np.asarray(self.idomain) > 0)
+
+    @property
     def nodes(self) -> int:
-        return self.nlay * self.ncpl
+        return int(self.nodeuser.size)
 
     @property
     def vertex_lists(self):
         return close_vertex_lists(self.icvert)
 
     @property
-    def cell_top(self) -> np.ndarray:
-        t = np.empty(self.nodes)
+    def user_top(self) -> np.ndarray:
+        t = np.empty(self.nlay * self.ncpl)
         t[:self.ncpl] = self.top
         t[self.ncpl:] = self.botm[:-self.ncpl]
         return t
 
     @property
+    def cell_top(self) -> np.ndarray:
+        return self.user_top[self.nodeuser]
+
+    @property
     def cell_bot(self) -> np.ndarray:
-        return self.botm
+        return np.asarray(self.botm)[self.nodeuser]
 
     def connections(self) -> dict:
         iav, jav = self.vertex_lists
         return disv_connections(self.nlay, iav, jav, self.vertices[:, 0], self.vertices[:, 1],
-                                self.xc, self.yc, self.cell_top, self.cell_bot)
+                                self.xc, self.yc, self.user_top, self.botm, self.idomain)
 
     @property
     def area(self) -> np.ndarray:
-        return np.tile(self.connections()["area"], self.nlay)
+        return np.tile(self.connections()["area"], self.nlay)[self.nodeuser]
+
+    @property
+    def xcn(self) -> np.ndarray:
+        """cell centres per active cell"""
+        return np.tile(self.xc, self.nlay)[self.nodeuser]
+
+    @property
+    def ycn(self) -> np.ndarray:
+        return np.tile(self.yc, self.nlay)[self.nodeuser]
 
     @property
     def ibound(self) -> np.ndarray:
@@ -308,7 +354,8 @@ def hex_mesh(nx: int, ny: int, size: float = 10.0, seed: int = 0, jitter: float 
 
 
 def make_disv_model(nlay: int = 3, nx: int = 30, ny: int = 20, seed: int = 0,
-                    transient: bool = False, newton: bool = False) -> DisvModel:
+                    transient: bool = False, newton: bool = False,
+                    idomain: np.ndarray | None = None) -> DisvModel:
     """A seeded DISV workload on the hexagon mesh: lognormal K per layer,
     CHD on the cells of the first and last columns of every layer, wells and
     recharge."""
@@ -340,4 +387,21 @@ def make_disv_model(nlay: int = 3, nx: int = 30, ny: int = 20, seed: int = 0,
     m.wel_q = rng.uniform(-300.0, -20.0, m.wel_node.size)
     m.rch_node = np.arange(ncpl, dtype=np.int32)
     m.rch_rate = np.full(ncpl, 2.0e-4)
+    if idomain is not None:
+        # keep the active cells: cell arrays and boundaries in the reduced
+        # numbering (boundaries on removed cells dropped)
+        idomain = np.asarray(idomain)
+        keep = idomain > 0
+        red = np.full(n, -1)
+        red[keep] = np.arange(int(keep.sum()))
+        m.idomain = idomain
+        for f in ("k11", "k33", "icelltype", "strt", "ss", "sy"):
+            v = getattr(m, f)
+            if v is not None:
+                setattr(m, f, np.asarray(v)[keep])
+        for nf, vf in (("chd_node", "chd_head"), ("wel_node", "wel_q"), ("rch_node", "rch_rate")):
+            nodes = getattr(m, nf)
+            ok = keep[nodes]
+            setattr(m, nf, red[nodes[ok]].astype(np.int32))
+            setattr(m, vf, np.asarray(getattr(m, vf))[ok])
     return m

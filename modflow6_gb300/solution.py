@@ -195,7 +195,7 @@ class GwfSolution:
             if disu:
                 xcn, ycn = m.xc, m.yc
             else:
-                xcn, ycn = np.tile(m.xc, m.nlay), np.tile(m.yc, m.nlay)
+                xcn, ycn = m.xcn, m.ycn
             keep.update(x_xc=_f(xcn), x_yc=_f(ycn), x_ax=_f(con["anglex"]))
             cg = _lib.GbslnGeometry(_lib.dptr(keep["x_xc"]), _lib.dptr(keep["x_yc"]),
                                     _lib.dptr(keep["x_ax"]), int(disu))

@@ -404,20 +404,19 @@ int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int
   return rc;
 }
 
-void or_disv_anglex(int nlay, int ncpl, const double *vx, const double *vy, const int *iavert,
-                    const int *javert, const int *ia, const int *ja, const int *jas,
-                    const int *ihc, double *anglex) {
+void or_disv_anglex(int nodes, int ncpl, const double *vx, const double *vy, const int *iavert,
+                    const int *javert, const int *nodeuser, const int *ia, const int *ja,
+                    const int *jas, const int *ihc, double *anglex) {
   const double dpi = 4.0 * atan(1.0);
-  const int nodes = nlay * ncpl;
   for (int n = 0; n < nodes; ++n) {
-    const int jn = n % ncpl;
+    const int jn = (nodeuser ? nodeuser[n] : n) % ncpl;
     for (int ii = ia[n] + 1; ii < ia[n + 1]; ++ii) {
       const int m = ja[ii];
       if (m < n) continue;
       const int s = jas[ii];
       anglex[s] = 0.0;
       if (ihc[s] == 0) continue;
-      const int jm = m % ncpl;
+      const int jm = (nodeuser ? nodeuser[m] : m) % ncpl;
       int a, b;
       disv_shared_edge(javert + iavert[jn], iavert[jn + 1] - iavert[jn], javert + iavert[jm],
                        iavert[jm + 1] - iavert[jm], &a, &b);
@@ -663,9 +662,23 @@ static int cmp_int(const void *a, const void *b) {
  * -1 if cap is too small. */
 int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, const int *iavert,
                     const int *javert, const double *xc, const double *yc, const double *top,
-                    const double *bot, int cap, int *ia, int *ja, int *isym, int *jas, int *ihc,
-                    double *cl1, double *cl2, double *hwva, double *area) {
-  const int nodes = nlay * ncpl;
+                    const double *bot, const int *nodereduced, int cap, int *ia, int *ja,
+                    int *isym, int *jas, int *ihc, double *cl1, double *cl2, double *hwva,
+                    double *area) {
+  /* nodereduced (the reference's convention, user node -> 1-based reduced
+   * number, 0 removed, -1 pass-through) or NULL for a full grid; top/bot per
+   * user node */
+  const int nodesuser = nlay * ncpl;
+  int nodes = nodesuser;
+  if (nodereduced) {
+    nodes = 0;
+    for (int u = 0; u < nodesuser; ++u)
+      if (nodereduced[u] > 0) nodes++;
+  }
+  int *nodeuser = (int *)malloc(sizeof(int) * (nodes + 1));
+  for (int u = 0, r = 0; u < nodesuser; ++u)
+    if (!nodereduced || nodereduced[u] > 0) nodeuser[r++] = u;
+#define RED(u) (nodereduced ? nodereduced[u] : (u) + 1) /* 1-based, 0 removed, -1 pass */
   int nvert = 0;
   for (int q = 0; q < iavert[ncpl]; ++q)
     if (javert[q] + 1 > nvert) nvert = javert[q] + 1;
@@ -694,22 +707,42 @@ int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, cons
       else overflow = 1;                                            \
     }                                                               \
   } while (0)
+  /* vertexconnect (Connections.f90:1272-1361): the diagonal and the
+   * vertical neighbours, passing through cells with nodereduced -1 */
   for (int k = 0; k < nlay; ++k)
     for (int j = 0; j < ncpl; ++j) {
-      int nr = j + k * ncpl;
+      int nr = RED(j + k * ncpl);
+      if (nr <= 0) continue;
+      nr -= 1;
       DISV_ADD(nr, nr);
-      if (k > 0) DISV_ADD(nr, j + (k - 1) * ncpl);
-      if (k < nlay - 1) DISV_ADD(nr, j + (k + 1) * ncpl);
+      if (k > 0) {
+        int mr = 0;
+        for (int kk = k - 1; kk >= 0; --kk) {
+          mr = RED(j + kk * ncpl);
+          if (mr >= 0) break;
+        }
+        if (mr > 0) DISV_ADD(nr, mr - 1);
+      }
+      if (k < nlay - 1) {
+        int mr = 0;
+        for (int kk = k + 1; kk < nlay; ++kk) {
+          mr = RED(j + kk * ncpl);
+          if (mr >= 0) break;
+        }
+        if (mr > 0) DISV_ADD(nr, mr - 1);
+      }
     }
   for (int v = 0; v < nvert; ++v)
     for (int c1 = vcnt[v]; c1 < vcnt[v + 1]; ++c1) {
       int j1 = vcell[c1];
       for (int k = 0; k < nlay; ++k) {
-        int nr = j1 + k * ncpl;
+        int nr = RED(j1 + k * ncpl) - 1;
+        if (nr < 0) continue;
         for (int c2 = vcnt[v]; c2 < vcnt[v + 1]; ++c2) {
           int j2 = vcell[c2];
           if (j1 == j2) continue;
-          int mr = j2 + k * ncpl;
+          int mr = RED(j2 + k * ncpl) - 1;
+          if (mr < 0) continue;
           int a, b;
           disv_shared_edge(javert + iavert[j1], iavert[j1 + 1] - iavert[j1], javert + iavert[j2],
                            iavert[j2 + 1] - iavert[j2], &a, &b);
@@ -721,7 +754,7 @@ int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, cons
   int nja = 0;
   for (int n = 0; n < nodes; ++n) nja += rn[n];
   if (overflow || nja > cap) {
-    free(vcnt); free(vcell); free(vfill); free(rows); free(rn);
+    free(vcnt); free(vcell); free(vfill); free(rows); free(rn); free(nodeuser);
     return -1;
   }
   ia[0] = 0;
@@ -755,16 +788,16 @@ int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, cons
   for (int j = 0; j < ncpl; ++j) area[j] = disv_area(j, iavert, javert, vx, vy);
   /* cprops for n < m (DisvGeom.f90:136-202) */
   for (int n = 0; n < nodes; ++n) {
-    const int jn = n % ncpl;
+    const int un = nodeuser[n], jn = un % ncpl;
     for (int ii = ia[n] + 1; ii < ia[n + 1]; ++ii) {
       const int m = ja[ii];
       if (m < n) continue;
-      const int jm = m % ncpl, s = jas[ii];
+      const int um = nodeuser[m], jm = um % ncpl, s = jas[ii];
       if (jn == jm) {
         ihc[s] = 0;
         hwva[s] = area[jn];
-        cl1[s] = 0.5 * (top[n] - bot[n]);
-        cl2[s] = 0.5 * (top[m] - bot[m]);
+        cl1[s] = 0.5 * (top[un] - bot[un]);
+        cl2[s] = 0.5 * (top[um] - bot[um]);
       } else {
         ihc[s] = 1;
         int a, b;
@@ -782,7 +815,8 @@ int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, cons
       }
     }
   }
-  free(vcnt); free(vcell); free(vfill); free(rows); free(rn);
+  free(vcnt); free(vcell); free(vfill); free(rows); free(rn); free(nodeuser);
+#undef RED
   return nja;
 }
 

@@ -82,8 +82,9 @@ void or_dis_connect(int nlay, int nrow, int ncol, const double *delr, const doub
                     int *jas, int *ihc, double *cl1, double *cl2, double *hwva);
 int or_disv_connect(int nlay, int ncpl, const double *vx, const double *vy, const int *iavert,
                     const int *javert, const double *xc, const double *yc, const double *top,
-                    const double *bot, int cap, int *ia, int *ja, int *isym, int *jas, int *ihc,
-                    double *cl1, double *cl2, double *hwva, double *area);
+                    const double *bot, const int *nodereduced, int cap, int *ia, int *ja,
+                    int *isym, int *jas, int *ihc, double *cl1, double *cl2, double *hwva,
+                    double *area);
 /* DISU: disuconnections + con_finalize (Connections.f90:801-928, 160-316).
  * iainp (nodesuser+1, 0-based offsets from IAC), jainp (1-based, a negative
  * number read as its magnitude), ihcinp/cl12inp/hwvainp per entry;
@@ -97,11 +98,11 @@ int or_disu_connect(int nodesuser, const int *iainp, const int *jainp, const int
                     const int *nodereduced, int cap, int *nodes, int *ia, int *ja, int *isym,
                     int *jas, int *ihc, double *cl1, double *cl2, double *hwva, double *anglex);
 /* DisvGeom.f90:193-199 and :394-412 (cprops' anglex): the angle of the
- * shared edge's normal for each horizontal connection n < m of a full DISV
- * grid, 0 for vertical ones */
-void or_disv_anglex(int nlay, int ncpl, const double *vx, const double *vy, const int *iavert,
-                    const int *javert, const int *ia, const int *ja, const int *jas,
-                    const int *ihc, double *anglex);
+ * shared edge's normal for each horizontal connection n < m of a DISV grid
+ * (nodeuser: reduced -> user cell, or NULL), 0 for vertical ones */
+void or_disv_anglex(int nodes, int ncpl, const double *vx, const double *vy, const int *iavert,
+                    const int *javert, const int *nodeuser, const int *ia, const int *ja,
+                    const int *jas, const int *ihc, double *anglex);
 void or_xt3d_ck(int nodes, const double *k11, const double *k22, const double *k33,
                 const double *angle1, const double *angle2, const double *angle3, int nozee,
                 double *ck);

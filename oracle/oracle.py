@@ -125,7 +125,7 @@ def load():
         lib.or_squadratic_sat_derv.argtypes = [C.c_double] * 4
         lib.or_dis_sizes.argtypes = [C.c_int, C.c_int, C.c_int, _ip, _ip, _ip]
         lib.or_disv_connect.argtypes = [C.c_int, C.c_int, _dp, _dp, _ip, _ip, _dp, _dp, _dp, _dp,
-                                        C.c_int, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
+                                        _ip, C.c_int, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
         lib.or_dis_connect.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, _ip, _ip,
                                        _ip, _ip, _dp, _dp, _dp]
         lib.or_xt3d_ck.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int, _dp]
@@ -137,7 +137,7 @@ def load():
                                         _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
         lib.or_npf_hy.argtypes = [C.POINTER(GwfModel), _dp, _dp, _dp, _dp, C.c_int, _dp]
         lib.or_disv_anglex.argtypes = [C.c_int, C.c_int, _dp, _dp, _ip, _ip, _ip, _ip, _ip, _ip,
-                                       _dp]
+                                       _ip, _dp]
         lib.or_npf_condsat.argtypes = [C.POINTER(GwfModel), _dp]
         lib.or_gwf_fc.argtypes = [C.POINTER(GwfModel), _ip, _dp, _dp, C.c_double, C.c_int, _dp, _dp, _dp, _dp]
         lib.or_sln_ls_fixups.argtypes = [C.c_int, _ip, _ip, _ip, C.c_int, _dp, _dp, _dp, _dp]
@@ -337,14 +337,23 @@ def dis_connect(nlay, nrow, ncol, delr, delc, top, bot) -> dict:
     return out
 
 
-def disv_connect(nlay, iavert, javert, vx, vy, xc, yc, top, bot) -> dict:
-    """or_disv_connect: the connectivity of a full DISV grid (closed vertex
-    lists iavert/javert, 0-based), with the cell areas."""
+def disv_connect(nlay, iavert, javert, vx, vy, xc, yc, top, bot, idomain=None) -> dict:
+    """or_disv_connect: the connectivity of a DISV grid (closed vertex lists
+    iavert/javert, 0-based; top/bot per user cell) reduced by IDOMAIN
+    (> 0 active, 0 removed, < 0 vertical pass-through), with the cell
+    areas."""
     lib = load()
     iavert = np.ascontiguousarray(iavert, np.int32)
     javert = np.ascontiguousarray(javert, np.int32)
     ncpl = iavert.size - 1
+    red = None
     n = nlay * ncpl
+    if idomain is not None:
+        idomain = np.asarray(idomain)
+        red = np.where(idomain < 0, -1, 0).astype(np.int32)
+        act = idomain > 0
+        red[act] = np.arange(1, int(act.sum()) + 1, dtype=np.int32)
+        n = int(act.sum())
     cap = n * (3 + int(np.diff(iavert).max()))
     out = dict(ia=np.zeros(n + 1, np.int32), ja=np.zeros(cap, np.int32), isym=np.zeros(cap, np.int32),
                jas=np.zeros(cap, np.int32), ihc=np.zeros(cap, np.int32), cl1=np.zeros(cap),
@@ -352,7 +361,8 @@ def disv_connect(nlay, iavert, javert, vx, vy, xc, yc, top, bot) -> dict:
     f = lambda a: np.ascontiguousarray(a, np.float64)
     keep = [f(vx), f(vy), f(xc), f(yc), f(top), f(bot)]
     nja = lib.or_disv_connect(nlay, ncpl, dp(keep[0]), dp(keep[1]), ip(iavert), ip(javert),
-                              dp(keep[2]), dp(keep[3]), dp(keep[4]), dp(keep[5]), cap,
+                              dp(keep[2]), dp(keep[3]), dp(keep[4]), dp(keep[5]),
+                              ip(red) if red is not None else None, cap,
                               ip(out["ia"]), ip(out["ja"]), ip(out["isym"]), ip(out["jas"]),
                               ip(out["ihc"]), dp(out["cl1"]), dp(out["cl2"]), dp(out["hwva"]),
                               dp(out["area"]))
@@ -431,8 +441,8 @@ class Gwf:
         elif getattr(m, "disv", False):
             iav, jav = m.vertex_lists
             con = disv_connect(m.nlay, iav, jav, m.vertices[:, 0], m.vertices[:, 1], m.xc, m.yc,
-                               m.cell_top, m.cell_bot)
-            area = np.tile(con["area"], m.nlay)
+                               m.user_top, m.botm, getattr(m, "idomain", None))
+            area = np.tile(con["area"], m.nlay)[m.nodeuser]
         else:
             con = dis_connect(m.nlay, m.nrow, m.ncol, m.delr, m.delc, m.cell_top, m.cell_bot)
             area = m.area
@@ -474,10 +484,11 @@ class Gwf:
             if getattr(m, "disv", False):
                 iav, jav = m.vertex_lists
                 ax = np.zeros(con["njas"])
-                self.lib.or_disv_anglex(m.nlay, len(m.icvert), d(m.vertices[:, 0]),
-                                        d(m.vertices[:, 1]), i(iav), i(jav), i(con["ia"]),
-                                        i(con["ja"]), i(con["jas"]), i(con["ihc"]), dp(ax))
-                xcn, ycn = np.tile(m.xc, m.nlay), np.tile(m.yc, m.nlay)
+                self.lib.or_disv_anglex(m.nodes, len(m.icvert), d(m.vertices[:, 0]),
+                                        d(m.vertices[:, 1]), i(iav), i(jav), i(m.nodeuser),
+                                        i(con["ia"]), i(con["ja"]), i(con["jas"]), i(con["ihc"]),
+                                        dp(ax))
+                xcn, ycn = m.xcn, m.ycn
                 self.model.xt_grid = 1
             else:
                 ax = con["anglex"]

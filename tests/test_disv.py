@@ -17,7 +17,7 @@ def test_connectivity_matches_oracle(nlay, nx, ny, seed):
     con = m.connections()
     iav, jav = m.vertex_lists
     o = oracle.disv_connect(nlay, iav, jav, m.vertices[:, 0], m.vertices[:, 1], m.xc, m.yc,
-                            m.cell_top, m.cell_bot)
+                            m.user_top, m.botm)
     for k in ("ia", "ja", "isym", "jas", "ihc"):
         np.testing.assert_array_equal(con[k], o[k], err_msg=k)
     for k in ("cl1", "cl2", "hwva", "area"):
@@ -25,6 +25,38 @@ def test_connectivity_matches_oracle(nlay, nx, ny, seed):
     # hexagons: every interior cell has six horizontal neighbours
     deg = np.diff(con["ia"]) - 1 - (2 if nlay > 2 else (1 if nlay == 2 else 0))
     assert deg.max() == 6
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_reduced_connectivity_matches_oracle(seed):
+    """IDOMAIN 0 (removed) and -1 (vertical pass-through) cells: the
+    library's connectivity equals the oracle's restatement of vertexconnect
+    (Connections.f90:1272-1361), and a vertical connection through a
+    pass-through cell joins the cells above and below it."""
+    rng = np.random.default_rng(seed)
+    nlay, nx, ny = 4, 10, 8
+    ncpl = nx * ny
+    idomain = np.ones(nlay * ncpl, int)
+    idomain[rng.choice(nlay * ncpl, 25, replace=False)] = 0
+    mid = rng.choice(ncpl, 12, replace=False) + ncpl  # layer 2 pass-through cells
+    idomain[mid] = -1
+    idomain[mid - ncpl] = 1
+    idomain[mid + ncpl] = 1
+    m = make_disv_model(nlay, nx, ny, seed=seed, idomain=idomain)
+    con = m.connections()
+    iav, jav = m.vertex_lists
+    o = oracle.disv_connect(nlay, iav, jav, m.vertices[:, 0], m.vertices[:, 1], m.xc, m.yc,
+                            m.user_top, m.botm, idomain)
+    assert con["nodes"] == o["nodes"] == int((idomain > 0).sum())
+    for k in ("ia", "ja", "isym", "jas", "ihc", "cl1", "cl2", "hwva"):
+        np.testing.assert_array_equal(con[k], o[k], err_msg=k)
+    red = con["nodereduced"]
+    a, b = red[mid[0] - ncpl] - 1, red[mid[0] + ncpl] - 1
+    assert b in con["ja"][con["ia"][a]:con["ia"][a + 1]]
+    # the oracle solves the reduced model
+    g = oracle.Gwf(m, oracle.settings(dvclose=1e-8, rclose=1e-6, iter1=2000, ilinmeth=1))
+    st = g.timestep(kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-8, mxiter=20)
+    assert st["converged"] == 1
 
 
 def test_rectangular_disv_equals_dis():
@@ -141,3 +173,27 @@ def test_gpu_solve_on_disv(gblib, ilinmeth):
     x_star = x0.copy()
     oracle.Ims(ts, g.con["ia"], g.con["ja"]).apply(amat.copy(), rhs.copy(), x_star)
     assert_closure_parity(x, xo, x_star, tol["dvclose"], ilinmeth == 1)
+
+
+@pytest.mark.gpu
+def test_gpu_timestep_on_reduced_disv(gblib):
+    """A DISV grid with removed and pass-through cells through the
+    device-resident time step (gbsln_create_grid), against the oracle's."""
+    from modflow6_gb300.ims import ImsLinearSettings
+    from modflow6_gb300.solution import GwfSolution, Nonlinear
+    rng = np.random.default_rng(3)
+    nlay, nx, ny = 3, 16, 12
+    ncpl = nx * ny
+    idomain = np.ones(nlay * ncpl, int)
+    interior = np.flatnonzero((np.arange(ncpl) % nx > 0) & (np.arange(ncpl) % nx < nx - 1))
+    idomain[rng.choice(interior, 8, replace=False)] = 0
+    idomain[ncpl + rng.choice(interior, 10, replace=False)] = -1
+    m = make_disv_model(nlay, nx, ny, seed=3, idomain=idomain)
+    tol = dict(dvclose=1e-9, rclose=1e-7, iter1=2000, ilinmeth=1)
+    g = oracle.Gwf(m, oracle.settings(**tol))
+    so = g.timestep(kper=1, kstp=1, delt=1.0, dvclose=1e-7, mxiter=50)
+    sol = GwfSolution(m, ImsLinearSettings(**tol), Nonlinear(dvclose=1e-7, mxiter=50))
+    sg = sol.timestep(1, 1, 1.0)
+    assert so["converged"] == 1 and sg["converged"] == 1
+    assert abs(sg["outer"] - so["outer"]) <= 1
+    assert np.max(np.abs(sol.heads - g.x)) <= 1e-8

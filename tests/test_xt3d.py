@@ -236,7 +236,7 @@ def _general_linear(m, xt3d=True, icelltype=0, angle=30.0):
         x, y = m.xc, m.yc
         full = 4
     else:
-        x, y = np.tile(m.xc, m.nlay), np.tile(m.yc, m.nlay)
+        x, y = m.xcn, m.ycn
         full = 6
     h = 100.0 + 0.03 * x - 0.02 * y
     rown = np.repeat(np.arange(n), np.diff(con["ia"]))
@@ -275,9 +275,9 @@ def test_anglex_matches_oracle():
     ax = np.zeros(con["njas"])
     lib = oracle.load()
     keep = [np.ascontiguousarray(a, np.float64) for a in (m.vertices[:, 0], m.vertices[:, 1])]
-    ints = [np.ascontiguousarray(a, np.int32) for a in (iav, jav, con["ia"], con["ja"], con["jas"],
-                                                        con["ihc"])]
-    lib.or_disv_anglex(m.nlay, len(m.icvert), oracle.dp(keep[0]), oracle.dp(keep[1]),
+    ints = [np.ascontiguousarray(a, np.int32) for a in (iav, jav, m.nodeuser, con["ia"], con["ja"],
+                                                        con["jas"], con["ihc"])]
+    lib.or_disv_anglex(m.nodes, len(m.icvert), oracle.dp(keep[0]), oracle.dp(keep[1]),
                        *[oracle.ip(a) for a in ints], oracle.dp(ax))
     np.testing.assert_array_equal(con["anglex"], ax)
     assert (ax[con["ihc"] != 0] > 0).any()
