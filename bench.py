@@ -51,6 +51,11 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-warmstart", action="store_true")
     ap.add_argument("--no-c3", action="store_true", help="skip the C1 and C3 forms")
+    ap.add_argument("--no-grids", action="store_true", help="skip the DISV, DISU and XT3D form")
+    ap.add_argument("--grids", action="store_true",
+                    help="only the DISV, DISU and XT3D steady steps (one JSON line)")
+    ap.add_argument("--grid-cases", default="disv,disu,xt3d",
+                    help="which of the general-grid workloads to run")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the library's default sweep tiling and reduction grid")
     ap.add_argument("--kernels", action="store_true",
@@ -410,6 +415,7 @@ def gb_arm(a):
     ens = None if a.no_ensemble else ensemble_form(a, lib, barrier, maxr)
     c3 = None if a.no_c3 else c3_form(a, barrier)
     c1 = None if a.no_c3 else c1_form(a, barrier)
+    grids = None if a.no_grids else grids_form(a, barrier)
     ws_res = None if a.no_warmstart else warmstart_form(a)
     last = st64[-1]
     cpu = None
@@ -427,7 +433,7 @@ def gb_arm(a):
     # the details (tuning candidates, per-form breakdowns) go to stderr as one
     # line; stdout carries the contract line, with the forms' summary last
     detail = {"tuning_fp64": tune64, "mixed": mixed, "ensemble": ens, "warm_start": ws_res,
-              "c3": c3, "c1": c1,
+              "c3": c3, "c1": c1, "grids": grids,
               "roofline_spmv": {"kernel": "k_dia7_spmv<double>", "achieved": spmv_gbs,
                                 "frac": spmv_gbs / peak, "launch_ms": kt.spmv_ms,
                                 "traffic": traffic.get("spmv_fp64_bytes_per_launch")},
@@ -454,6 +460,11 @@ def gb_arm(a):
         if "mixed" in c3:
             forms.update(c3_mixed_s=c3["mixed"]["value"], c3_mixed_vs_fp64=c3["mixed_vs_fp64"],
                          c3_mixed_max_head_diff_m=c3["mixed_max_head_diff_m"])
+    if grids:
+        for gname, gr in grids.items():
+            forms[f"{gname}_s"] = gr["value"]
+            if "oracle" in gr:
+                forms[f"{gname}_oracle_s"] = gr["oracle"]["value"]
     if ws_res:
         h = ws_res["heldout"]
         forms.update(warmstart_time_ratio=h.get("time_ratio"),
@@ -675,6 +686,73 @@ def c3_form(a, barrier) -> dict:
     return out
 
 
+GRID_IMS = dict(dvclose=1e-8, rclose=1e-6, iter1=4000)
+GRID_OUTER = dict(dvclose=1e-8, mxiter=20)
+
+
+def grids_form(a, barrier) -> dict:
+    """The general grids and the full-tensor formulation, one steady step to
+    closure each (INNER_DVCLOSE 1e-8, INNER_RCLOSE 1e-6, OUTER_DVCLOSE 1e-8):
+    a DISV hexagon grid and a DISU locally refined grid (SELL-32 product,
+    sync-free level-scheduled ILU0 sweeps, PCG), and a DIS grid with XT3D
+    (the wider pattern, BiCGSTAB).  FP64 on the device-resident solution:
+    the time step's own CUDA-event times (fill, solve, total), the median of
+    3 steps from the initial heads after a warm-up step and (unless
+    --no-tune) gbims_autotune on the factored system (level-sweep form and
+    threads per row, reduction grid).  Beside each, the
+    oracle's full solve of the same step on one core (wall clock) and the
+    largest head difference."""
+    from modflow6_gb300 import _lib
+    from modflow6_gb300.dis import make_config
+    from modflow6_gb300.disu import make_disu_model
+    from modflow6_gb300.disv import make_disv_model
+    from modflow6_gb300.ims import ImsLinearSettings
+    from modflow6_gb300.solution import GwfSolution, Nonlinear
+
+    lib = _lib.load()
+    s = a.scale
+    nv, nu = max(8, int(round(250 * s))), max(6, int(round(240 * s)))
+    cases = (("disv", f"DISV 4x{nv}x{nv} hexagons", lambda: make_disv_model(4, nv, nv, seed=a.seed), 1),
+             ("disu", f"DISU 3 layers, {nu}x{nu} cells with the middle ninth refined 2x2",
+              lambda: make_disu_model(3, nu, nu, seed=a.seed), 1),
+             ("xt3d", None, lambda: make_config("xt3d", seed=a.seed, scale=s), 2))
+    out = {}
+    want = set(a.grid_cases.split(","))
+    for name, desc, build, ilinmeth in cases:
+        if name not in want:
+            continue
+        m = build()
+        if desc is None:
+            desc = f"DIS {m.nlay}x{m.nrow}x{m.ncol} XT3D, K11:K22:K33 1:0.2:0.05, angles 30/15/5"
+        tol = dict(ilinmeth=ilinmeth, **GRID_IMS)
+        sol = GwfSolution(m, ImsLinearSettings(**tol), Nonlinear(**GRID_OUTER))
+        sol.timestep(1, 1, 1.0)  # warm-up: builds the graphs, factors the matrix
+        tuning = None if a.no_tune else autotune(lib, sol.ims_handle())
+        barrier()
+        sts = []
+        for _ in range(3):
+            sol.restart()
+            sts.append(sol.timestep(1, 1, 1.0))
+        heads = sol.heads
+        sol.close()
+        med = lambda f: float(np.median([st[f] for st in sts]))
+        r = {"workload": desc, "cells": int(len(m.k11)), "value": med("total_ms") / 1e3, "unit": "s",
+             "fill_ms": med("fill_ms"), "solve_ms": med("solve_ms"),
+             "outer": int(sts[-1]["outer"]), "inner": int(sts[-1]["inner_total"]),
+             "converged": int(all(st["converged"] == 1 for st in sts)), "tuning": tuning}
+        if not a.no_cpu:
+            sys.path.insert(0, str(ROOT / "oracle"))
+            import oracle
+            g = oracle.Gwf(m, oracle.settings(**tol))
+            t0 = time.perf_counter()
+            so = g.timestep(kper=1, kstp=1, delt=1.0, transient=False, **GRID_OUTER)
+            r["oracle"] = {"value": time.perf_counter() - t0, "unit": "s", "cores": 1,
+                           "outer": int(so["outer"]), "inner": int(so["inner_total"]),
+                           "max_head_diff_vs_gpu_m": float(np.max(np.abs(g.x - heads)))}
+        out[name] = r
+    return out
+
+
 def warmstart_form(a) -> dict:
     """The learned warm start on the transient 256x256x3 workload (C5): the
     network is trained on the GPU (its own BF16 tensor-core kernels) on heads
@@ -756,10 +834,22 @@ def kernels_arm(a):
     print(json.dumps(out), flush=True)
 
 
+def grids_arm(a):
+    """The general-grid steady steps alone (for launch lists and quick
+    measurements); prints the form's results as one JSON line."""
+    import torch
+    from modflow6_gb300 import build
+    build.build()
+    torch.cuda.set_device(0)
+    print(json.dumps(grids_form(a, torch.cuda.synchronize)), flush=True)
+
+
 def main():
     a = parse()
     if a.kernels:
         kernels_arm(a)
+    elif a.grids:
+        grids_arm(a)
     elif a.impl == "reference":
         reference_arm(a)
     else:

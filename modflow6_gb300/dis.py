@@ -177,6 +177,9 @@ def make_config(name: str, seed: int = 0, scale: float = 1.0) -> GwfDisModel:
     c3 : 500x500x5 convertible (Newton), Sy 0.15, Ss 1e-5, top 50, bottom
          sloping 0 to -40, 2000 wells U(-1000,0), recharge U(0,5e-4).
     c5 : 256x256x3 transient confined, 50 wells U(-800,0).
+    xt3d : 200x200x3 confined, full-tensor (NPF XT3D): lnK11~N(0,1) corr 10,
+         K22 0.2 K11, K33 0.05 K11, ANGLE1/2/3 30/15/5 degrees, CHD 28/22 m
+         on the west/east faces, 200 wells U(-200,-20) m3/d.
     `scale` < 1 shrinks nrow/ncol for CPU-sized parity cases of c2/c3/c5.
     """
     rng = np.random.default_rng(seed)
@@ -245,5 +248,25 @@ def make_config(name: str, seed: int = 0, scale: float = 1.0) -> GwfDisModel:
         nwel = 50
         m.wel_node = np.sort(rng.choice(np.flatnonzero(~chd), size=nwel, replace=False)).astype(np.int32)
         m.wel_q = rng.uniform(-800.0, 0.0, nwel)
+        return m
+    if name == "xt3d":
+        nlay = 3
+        nrow = ncol = max(6, int(round(200 * scale)))
+        nrc = nrow * ncol
+        n = nlay * nrc
+        delr = np.full(ncol, 10.0); delc = np.full(nrow, 10.0)
+        top = np.full(nrc, 30.0)
+        botm = np.repeat(np.array([20.0, 10.0, 0.0]), nrc)
+        k = np.concatenate([lognormal_field(rng, (nrow, ncol), 1.0, 10.0).ravel() for _ in range(nlay)])
+        m = GwfDisModel(nlay, nrow, ncol, delr, delc, top, botm, k, 0.05 * k,
+                        np.zeros(n, np.int32), np.full(n, 25.0), name="xt3d")
+        m.ixt3d = 1
+        m.k22 = 0.2 * k
+        m.angle1, m.angle2, m.angle3 = np.full(n, 30.0), np.full(n, 15.0), np.full(n, 5.0)
+        m.chd_node, m.chd_head = _faces_chd(nlay, nrow, ncol, 28.0, 22.0)
+        chd = np.zeros(n, bool); chd[m.chd_node] = True
+        nwel = max(1, int(round(200 * scale * scale)))
+        m.wel_node = np.sort(rng.choice(np.flatnonzero(~chd), size=nwel, replace=False)).astype(np.int32)
+        m.wel_q = rng.uniform(-200.0, -20.0, nwel)
         return m
     raise ValueError(f"unknown config {name!r}")
