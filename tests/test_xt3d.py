@@ -501,3 +501,21 @@ def test_gpu_k22_angles_fill_bitexact(gblib, grid, iavgkeff):
     ao, ro = g.assemble(hh, hold=hold, delt=2.5, transient=True)
     np.testing.assert_array_equal(amat, ao)
     np.testing.assert_array_equal(rhs, ro)
+
+
+def test_oracle_solves_the_xt3d_workload():
+    """The seeded full-tensor workload that the bench measures (a scaled
+    copy): the wider pattern, BiCGSTAB to closure in the oracle, heads
+    between the CHD heads where the wells do not pull them down, and the
+    model budget closing (percent discrepancy below 1e-6)."""
+    from modflow6_gb300.dis import make_config
+    m = make_config("xt3d", seed=0, scale=0.1)
+    assert m.ixt3d == 1 and m.nodes == 3 * 20 * 20
+    tol = dict(dvclose=1e-8, rclose=1e-6, iter1=4000, ilinmeth=2)
+    g = oracle.Gwf(m, oracle.settings(**tol))
+    assert g.con["nja"] > 7 * m.nodes  # neighbours of neighbours
+    so = g.timestep(kper=1, kstp=1, delt=1.0, transient=False, dvclose=1e-8, mxiter=20)
+    assert so["converged"] == 1
+    assert g.x.max() <= 28.0 + 1e-9
+    _, b = g.budget(g.x)
+    assert abs(b["percent_discrepancy"]) < 1e-6
