@@ -499,7 +499,10 @@ def autotune(lib, h, reps=5):
     out = {"reduction_blocks": t.reduction_blocks}
     if t.level_mode >= 0:
         out.update(level_mode=("sync-free" if t.level_mode == 1 else "per-level launches"),
-                   level_ms=[round(t.level_ms[0], 4), round(t.level_ms[1], 4)])
+                   level_ms=[round(t.level_ms[0], 4), round(t.level_ms[1], 4)],
+                   sync_free_ms_by_threads_per_row=dict(zip(
+                       ("1", "2", "4", "8", "16"),
+                       (round(t.candidate_ms[i], 4) for i in range(t.ncandidates)))))
     if t.sweep_config >= 0:
         out.update(sweep_config=t.sweep_config, sweep_config_backward=t.sweep_config_backward,
                    sweep_chunk=t.sweep_chunk, sweep_ring=t.sweep_ring,

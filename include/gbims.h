@@ -210,8 +210,10 @@ typedef struct gbims_tuning {
                                        sweeps): 0 one launch per level, 1 one sync-free
                                        launch per sweep; -1 not applicable */
   double level_ms[2];               /* one ILU0 application in each level mode */
-  int ncandidates;                  /* tilings timed */
-  double candidate_ms[16];          /* one ILU0 application per tiling */
+  int ncandidates;                  /* tilings timed (level-scheduled handles: the
+                                       sync-free form at 1, 2, 4, 8, 16 threads per
+                                       row of the widest level) */
+  double candidate_ms[16];          /* one ILU0 application per candidate */
   double precond_ms;                /* of the chosen tilings */
   double vector_ms;                 /* dot + update at the chosen grid */
   int sweep_config_backward;        /* the backward sweep's tiling (sweep_config: the

@@ -1205,10 +1205,9 @@ extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
   out->level_mode = -1;
   if (!h->structured) {
     // level-scheduled sweeps: one launch per level, or one sync-free launch
-    // per sweep
     // per sweep (the sync-free form also with 1 to 16 threads per row of
     // the widest level, as far as the resident grid goes; level_ms[1] is its
-    // best)
+    // best, candidate_ms[0..4] its time at each)
     double bt = 1e300;
     int best = 1, best_mult = 1;
     auto pre = [&] {
@@ -1224,6 +1223,7 @@ extern "C" int gbims_autotune(gbims_handle *h, int reps, gbims_tuning *out) {
       h->LW.mode = 1;
       h->LW.sf_mult = mult;
       const double ms = time_it(pre);
+      out->candidate_ms[out->ncandidates++] = ms;
       out->level_ms[1] = std::min(out->level_ms[1], ms);
       if (ms < bt) {
         bt = ms;

@@ -126,7 +126,7 @@ struct Levels {
 // FP32, zeroed once; ticket: two counters, 128 bytes apart, zeroed once).
 struct LevelWords {
   int mode = 1;
-  int sf_mult = 1;  // sync-free sweeps: threads per row of the widest level (tuned)
+  int sf_mult = 8;  // sync-free sweeps: threads per row of the widest level (tuned)
   void *fwd = nullptr, *bwd = nullptr;
   unsigned long long *ticket = nullptr;
   int *err = nullptr;
