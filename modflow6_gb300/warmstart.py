@@ -7,7 +7,7 @@ forward and backward kernels) predicts the head change of the step from the
 cell's K, the previous heads, the previous step's head change, the well
 rates and the boundary mask.  The
 prediction is only an initial guess: PCG + ILU0 still runs to the same
-INNER_DVCLOSE / INNER_RCLOSE closure, so the plain solver stays the judge.
+INNER_DVCLOSE / INNER_RCLOSE closure, so the plain solver decides the heads.
 The first iterate is the point of the plane through the previous heads,
 spanned by the last step's head change and the network's predicted change,
 that is closest to the solution in the energy norm of the step's first
